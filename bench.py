@@ -1,0 +1,342 @@
+"""Benchmark: Gcell-updates/s of the FDTD time step and its fraction of the HBM roofline.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config 512|64|hbm]
+
+Default workload: the 512^3 random-box scenario (64 seeded dielectric boxes, 65 materials in a
+uint8 index, 10-cell CPML, 4 delayed 50-ohm lumped sources, 16 Ez/Hx probes). A step is one Yee
+time step (E update with source injection, H update, CPML, probes) over all 134,217,728 cells.
+The fields (3.2 GB) are far larger than L2, so no flush is needed between steps.
+
+Our arm prints one JSON line with: value (device-timed Gcell-updates/s, inputs resident),
+e2e (same metric through the C ABI from host buffers: handle creation, material/waveform
+upload, the K steps and the probe read-back), roofline (algorithmic bytes per cell-update x
+cells / measured step time, against MEASURED_PEAKS.json), cpu_baseline (the CPU oracle on a
+bounded sample) and clocks. The reference arm runs the reference's own CUDA kernels (calc_e +
+calc_h built from fdtdrav.h, oracle/_ref) on the same workload and GPU.
+
+Multi-GPU: the path does not shard (one resident grid per GPU); with --gpus N each rank runs an
+independent replica of the workload (weak scaling, no collective), value = total over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", choices=["512", "64", "hbm"], default="512")
+    ap.add_argument("--schedule", type=int, default=0, help="0 auto, 1 two-pass, 2 fused")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def scenario_for(cfg: str):
+    from fdtd_gb300 import scenario as S
+    if cfg == "64":
+        return S.config_small(), "vacuum 64^3, 10-cell CPML, 1 z-edge source, 1 Ez probe"
+    if cfg == "hbm":
+        return S.config_hbm(), ("1024x1024x896 random boxes (64 boxes, 65 materials, uint8 index), "
+                                "10-cell CPML, 4 sources, 16 probes")
+    return S.config_512(), "512^3 random boxes (64 boxes, 65 materials, uint8 index), 10-cell CPML, 4 sources, 16 probes"
+
+
+def algorithmic_bytes_per_cell(sc) -> float:
+    """48 B (6 FP32 components read + written once) + 1 B material index + 8 B per CPML psi update
+    (4 B read + 4 B write), psi counted exactly from the update masks."""
+    nx, ny, nz = sc.nx, sc.ny, sc.nz
+    pxn, pxp, pyn, pyp, pzn, pzp = sc.pml
+    i = np.arange(nx); j = np.arange(ny); k = np.arange(nz)
+
+    def slab(q, n, pn, pp):
+        return (q < pn) | (q >= n - pp)
+
+    xs, ys, zs = slab(i, nx, pxn, pxp), slab(j, ny, pyn, pyp), slab(k, nz, pzn, pzp)
+
+    def count(mi, mj, mk, si, sj, sk):
+        # number of nodes in mask (mi x mj x mk) and in the slab product
+        return int((mi & si).sum()) * int((mj & sj).sum()) * int((mk & sk).sum())
+
+    T = np.ones_like
+    inner = lambda q, n: (q > 0) & (q < n - 1)
+    lo = lambda q, n: q < n - 1
+    # E components (masks of calc_e) and H components (masks of calc_h), each with its two psi axes
+    ex = (lo(i, nx), inner(j, ny), inner(k, nz))
+    ey = (inner(i, nx), lo(j, ny), inner(k, nz))
+    ez = (inner(i, nx), inner(j, ny), lo(k, nz))
+    hx = (T(i, bool), lo(j, ny), lo(k, nz))
+    hy = (lo(i, nx), T(j, bool), lo(k, nz))
+    hz = (lo(i, nx), lo(j, ny), T(k, bool))
+    allx, ally, allz = T(i, bool), T(j, bool), T(k, bool)
+    psi = 0
+    psi += count(*ex, allx, ys, allz) + count(*ex, allx, ally, zs)
+    psi += count(*ey, xs, ally, allz) + count(*ey, allx, ally, zs)
+    psi += count(*ez, xs, ally, allz) + count(*ez, allx, ys, allz)
+    psi += count(*hx, allx, ys, allz) + count(*hx, allx, ally, zs)
+    psi += count(*hy, xs, ally, allz) + count(*hy, allx, ally, zs)
+    psi += count(*hz, xs, ally, allz) + count(*hz, allx, ys, allz)
+    return 48.0 + 1.0 + 8.0 * psi / (nx * ny * nz)
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0])); mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_setup(n_gpus):
+    import torch
+    rank, world = 0, 1
+    if n_gpus > 1 or "RANK" in os.environ:
+        import torch.distributed as dist
+        rank = int(os.environ.get("RANK", "0"))
+        world = int(os.environ.get("WORLD_SIZE", "1"))
+        local = int(os.environ.get("LOCAL_RANK", "0"))
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline(sc_full, seconds_budget=20.0):
+    """The CPU oracle (FP32 restatement of the reference's calc_e/calc_h) on a bounded sample: a
+    256 x 256 x 128 sub-domain of the same generator, timed over a few steps on all host cores."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from fdtd_gb300 import scenario as S
+    sub = S.random_boxes(256, 256, 128, 8, seed=512, edge=(8, 64), name="cpu_sample")
+    cores = os.cpu_count() or 1
+    # setup cost is excluded by timing two runs of different length
+    t0 = time.perf_counter(); oracle.run(sub, steps=2, threads=cores); t1 = time.perf_counter()
+    t2 = time.perf_counter(); oracle.run(sub, steps=8, threads=cores); t3 = time.perf_counter()
+    per_step = max(((t3 - t2) - (t1 - t0)) / 6.0, 1e-9)
+    return {"value": sub.cells / per_step / 1e9, "unit": "Gcell-updates/s", "cores": cores, "kind": "port",
+            "sample": "CPU oracle (FP32, OpenMP) on a 256x256x128 sub-domain of the random-box generator, "
+                      "6 steps (difference of an 8-step and a 2-step run, setup excluded)"}
+
+
+def bench_ours(args, rank, world):
+    import torch
+    from fdtd_gb300 import solver
+    sc, desc = scenario_for(args.config)
+    B = algorithmic_bytes_per_cell(sc)
+    N = sc.cells
+    total_steps = args.warmup + args.steps
+    if len(sc.sources[0].waveform) < total_steps:
+        from fdtd_gb300 import scenario as S
+        for s in sc.sources:
+            s.waveform = np.resize(s.waveform, total_steps).astype(np.float32)
+    mat = sc.material_index()
+    stream = torch.cuda.Stream()
+    sim = solver.Simulation.from_scenario(sc, args.schedule, material_index=mat, probe_capacity=total_steps)
+    sim.set_stream(stream.cuda_stream)
+    sim.prepare()
+    sim.step(args.warmup)
+    sim.synchronize()
+    launches_per_step = 1 if args.schedule == 2 else 2
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(torch.cuda.current_device())
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    e0.record(stream)
+    sim.step(args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(ms, world)
+    probes = sim.read_probes(total_steps - 1, 1)
+    assert np.all(np.isfinite(probes))
+    sim.close()
+    del sim
+    value = world * N * args.steps / (ms * 1e-3) / 1e9
+    step_ms = ms / args.steps
+    peak, peak_kind = measured_peak()
+    achieved = B * N / (step_ms * 1e-3) / 1e9
+    out = {"metric": "Gcell-updates/s", "value": round(value, 3), "unit": "Gcell-updates/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_ms, 4),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded random-box scenario)",
+           "config": {"workload": desc, "cells": N, "grid": [sc.nx, sc.ny, sc.nz], "cpml": 10,
+                      "schedule": {0: "auto", 1: "two-pass", 2: "fused"}[args.schedule],
+                      "l2": "inputs larger than L2 (fields 24 B/cell x 134M cells)", "parallelism": f"replicas{world}"},
+           "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                        "frac": round(achieved / peak, 4), "traffic": None,
+                        "bytes_per_cell_update": round(B, 3), "peak_source": peak_kind,
+                        "kernel": "one full time step (all update launches of the step)"},
+           "gpu_launches": launches_per_step * args.steps, "clocks": clk}
+    if not args.no_e2e:
+        out["e2e"] = e2e_ours(args, sc, mat)
+        out["e2e"]["value"] = round(world * out["e2e"]["value"], 3)
+    return out
+
+
+def e2e_ours(args, sc, mat):
+    """Same metric through the C ABI from host buffers: handle creation, material table and index
+    upload, waveform upload, K steps, probe read-back, destroy."""
+    import torch
+    from fdtd_gb300 import solver
+    pinned = torch.from_numpy(mat).pin_memory()
+    host_mat = pinned.numpy()
+    steps = args.steps
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim = solver.Simulation.from_scenario(sc, args.schedule, material_index=host_mat, probe_capacity=steps)
+    sim.step(steps)
+    probes = sim.read_probes(0, steps)
+    sim.close()
+    t1 = time.perf_counter()
+    h2d = host_mat.nbytes + sum(s.waveform.nbytes for s in sc.sources)
+    d2h = probes.nbytes
+    return {"value": sc.cells * steps / (t1 - t0) / 1e9, "unit": "Gcell-updates/s",
+            "h2d_bytes_per_step": round(h2d / steps, 1), "d2h_bytes_per_step": round(d2h / steps, 1),
+            "seconds": round(t1 - t0, 3)}
+
+
+def bench_reference(args, rank, world):
+    """The reference's own kernels (calc_e + calc_h from fdtdrav.h, built into oracle/_ref) on the
+    same workload, single slab on this GPU."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle", "ref_harness"))
+    import refharness
+    sc, desc = scenario_for(args.config)
+    if not refharness.available():
+        return {"impl": "reference", "unavailable": "oracle/_ref (reference kernels) not built"}
+    need = sc.cells * 84 * 4
+    import torch
+    free, _ = torch.cuda.mem_get_info()
+    if need > free * 0.95:
+        return {"impl": "reference", "unavailable": f"the reference layout needs {need / 1e9:.0f} GB (84 arrays x 4 B x "
+                                                    f"{sc.cells} cells), more than this GPU holds"}
+    h = refharness.RefHarness()
+    h.setup(sc)
+    sig = np.resize(sc.signal_per_node(0), args.warmup + args.steps + 1).astype(np.float32)
+    h.run(args.warmup, 0, 0, sig)
+    barrier(world)
+    _, ms = h.run(args.steps, args.warmup, 0, sig)
+    h.close()
+    ms = max_over_ranks(ms, world)
+    value = world * sc.cells * args.steps / (ms * 1e-3) / 1e9
+    return {"impl": "reference", "metric": "Gcell-updates/s", "value": round(value, 3), "unit": "Gcell-updates/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded random-box scenario)",
+            "config": {"workload": desc, "cells": sc.cells, "grid": [sc.nx, sc.ny, sc.nz],
+                       "l2": "inputs larger than L2", "parallelism": f"replicas{world}",
+                       "note": "reference kernels inject one source per launch; timing does not depend on it"},
+            "cpu_baseline": {"value": round(value, 3), "unit": "Gcell-updates/s", "cores": 0, "kind": "reference",
+                             "sample": "the reference's own CUDA kernels (calc_e + calc_h per step, fdtdrav.h "
+                                       "built for sm_103a) timed with CUDA events on this GPU; the reference has "
+                                       "no CPU implementation of the path"},
+            "e2e": {"value": round(value, 3), "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "gpu_launches": 2 * args.steps}
+
+
+def main():
+    args = parse()
+    import torch
+    rank, world = dist_setup(args.gpus)
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        out = bench_reference(args, rank, 1)
+        print(json.dumps(out))
+        return
+    out = bench_ours(args, rank, world)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            sc, _ = scenario_for(args.config)
+            out["cpu_baseline"] = cpu_baseline(sc)
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,635 @@
+// C ABI of the solver: handle lifetime, validation, device memory, setup and the time loop.
+//
+// Replaces the host side of the reference's hot path: the allocation, setup-kernel order and time
+// loop of marchingLoop (fdtdrav.h:3425-4387) and the per-step driver solver (fdtdrav.h:3188-3422).
+// Differences by design: one resident grid on one GPU (no z-slabs, ghost planes or peer copies),
+// status codes instead of exit(), a compact layout (6 field arrays, a uint8 material index, CPML
+// memory on the faces only) instead of 84 per-cell arrays, and stream-ordered asynchronous steps.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/fdtd_api.h"
+#include "yee_kernels.h"
+
+using namespace fdtd;
+
+namespace {
+
+thread_local std::string t_err;
+
+int fail(int code, const std::string& msg) {
+    t_err = msg;
+    return code;
+}
+
+#define CUDA_TRY(expr)                                                                        \
+    do {                                                                                      \
+        cudaError_t _e = (expr);                                                              \
+        if (_e != cudaSuccess) {                                                              \
+            return fail(_e == cudaErrorMemoryAllocation ? FDTD_ERR_OOM : FDTD_ERR_CUDA,       \
+                        std::string(#expr) + ": " + cudaGetErrorString(_e));                  \
+        }                                                                                     \
+    } while (0)
+
+struct LumpedDef {
+    int box[6];
+    float resistance;
+    int source;  // waveform index or -1
+};
+
+}  // namespace
+
+struct fdtd_handle {
+    fdtd_grid grid{};
+    DeviceGrid g{};
+    cudaStream_t stream = nullptr;
+    int schedule = FDTD_SCHEDULE_AUTO;
+    int device = 0;
+
+    // device state
+    float* field[6] = {};
+    uint8_t* mat = nullptr;
+    MatProps* props = nullptr;
+    MatCoef* coef = nullptr;
+    float* prof[18] = {};
+    PsiSet psi{};
+    std::vector<void*> allocs;
+    long long psi_elems[6] = {};  // elements per psi array of each face
+
+    // host-side definitions
+    std::vector<fdtd_material> materials;
+    std::vector<LumpedDef> lumped;
+    std::vector<std::vector<float>> waves;  // per source, per-edge signal
+    std::vector<Probe> probes;
+
+    // prepared device tables
+    bool prepared = false;
+    bool dirty_lumped = true, dirty_probes = true, dirty_materials = true;
+    LumpedEdge* d_lumped = nullptr;
+    int* d_lumped_k = nullptr;
+    Probe* d_probes = nullptr;
+    int* d_probe_k = nullptr;
+    int* d_probe_ids = nullptr;
+    float** d_waves = nullptr;
+    long long* d_wave_len = nullptr;
+    std::vector<float*> d_wave_bufs;
+    int* d_lumped_box = nullptr;
+    float* d_lumped_r = nullptr;
+    int* d_lumped_owner = nullptr;
+    float* ring = nullptr;
+    long long ring_cap = 4096;
+    int* status = nullptr;
+
+    long long step = 0;
+    long long bytes = 0;
+
+    cudaError_t alloc(void** p, size_t n) {
+        cudaError_t e = cudaMalloc(p, n);
+        if (e == cudaSuccess) {
+            allocs.push_back(*p);
+            bytes += (long long)n;
+        }
+        return e;
+    }
+    void release(void* p) {
+        if (!p) return;
+        auto it = std::find(allocs.begin(), allocs.end(), p);
+        if (it != allocs.end()) allocs.erase(it);
+        cudaFree(p);
+    }
+};
+
+namespace {
+
+long long vol(const fdtd_handle* h) { return h->g.plane * (long long)h->g.nz; }
+
+StepParams make_params(fdtd_handle* h) {
+    StepParams p{};
+    p.g = h->g;
+    p.mat = h->mat;
+    p.props = h->props;
+    p.coef = h->coef;
+    const float* const* P = h->prof;
+    p.bex = P[0]; p.aex = P[1]; p.bmx = P[2]; p.amx = P[3]; p.kex = P[4]; p.kmx = P[5];
+    p.bey = P[6]; p.aey = P[7]; p.bmy = P[8]; p.amy = P[9]; p.key = P[10]; p.kmy = P[11];
+    p.bez = P[12]; p.aez = P[13]; p.bmz = P[14]; p.amz = P[15]; p.kez = P[16]; p.kmz = P[17];
+    p.lumped = h->d_lumped;
+    p.lumped_k = h->d_lumped_k;
+    p.probes = h->d_probes;
+    p.probe_k = h->d_probe_k;
+    p.probe_ids = h->d_probe_ids;
+    p.waves = h->d_waves;
+    p.wave_len = h->d_wave_len;
+    p.probe_ring = h->ring;
+    p.n_probes = (int)h->probes.size();
+    p.ring_cap = h->ring_cap;
+    p.status = h->status;
+    return p;
+}
+
+int validate_grid(const fdtd_grid* g) {
+    if (!g) return fail(FDTD_ERR_INVALID, "grid is NULL");
+    if (g->nx < 3 || g->ny < 3 || g->nz < 3) return fail(FDTD_ERR_INVALID, "grid needs at least 3 nodes per axis");
+    if ((long long)g->nx * g->ny * g->nz > (1LL << 40)) return fail(FDTD_ERR_INVALID, "grid too large");
+    const float v[7] = {g->dx, g->dy, g->dz, g->dt, g->eps0, g->mu0, g->pi};
+    for (float x : v)
+        if (!(x > 0.f) || !std::isfinite(x)) return fail(FDTD_ERR_INVALID, "cell sizes, dt and constants must be positive and finite");
+    const int n[3] = {g->nx, g->ny, g->nz};
+    for (int a = 0; a < 3; ++a) {
+        const int pn = g->pml[2 * a], pp = g->pml[2 * a + 1];
+        if (pn < 0 || pp < 0) return fail(FDTD_ERR_INVALID, "negative CPML thickness");
+        // the reference applies both faces' blocks where they overlap; require disjoint slabs
+        // with at least one node between them
+        if (pn + pp > n[a] - 1) return fail(FDTD_ERR_INVALID, "CPML slabs of opposite faces overlap on axis " + std::to_string(a));
+    }
+    return FDTD_OK;
+}
+
+int ensure_prepared(fdtd_handle* h);
+
+}  // namespace
+
+extern "C" {
+
+const char* fdtd_last_error(void) { return t_err.c_str(); }
+const char* fdtd_version(void) { return "fdtd_gb300 0.1 (sm_103a)"; }
+
+int fdtd_create(const fdtd_grid* grid, fdtd_handle** out) {
+    if (!out) return fail(FDTD_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    int rc = validate_grid(grid);
+    if (rc) return rc;
+    fdtd_handle* h = new fdtd_handle();
+    h->grid = *grid;
+    cudaGetDevice(&h->device);
+    DeviceGrid& g = h->g;
+    g.nx = grid->nx; g.ny = grid->ny; g.nz = grid->nz;
+    g.pitch = (grid->nx + 31) / 32 * 32;
+    g.plane = (long long)g.pitch * g.ny;
+    g.pxn = grid->pml[0]; g.pxp = grid->pml[1]; g.pyn = grid->pml[2]; g.pyp = grid->pml[3];
+    g.pzn = grid->pml[4]; g.pzp = grid->pml[5];
+    g.dx = grid->dx; g.dy = grid->dy; g.dz = grid->dz; g.dt = grid->dt; g.eps0 = grid->eps0; g.mu0 = grid->mu0;
+    auto cleanup = [&](int code) { fdtd_destroy(h); return code; };
+    const long long V = vol(h);
+    for (int c = 0; c < 6; ++c) {
+        cudaError_t e = h->alloc((void**)&h->field[c], (size_t)V * sizeof(float));
+        if (e != cudaSuccess) return cleanup(fail(FDTD_ERR_OOM, "field allocation failed: " + std::string(cudaGetErrorString(e))));
+    }
+    if (h->alloc((void**)&h->mat, (size_t)V) != cudaSuccess) return cleanup(fail(FDTD_ERR_OOM, "material index allocation failed"));
+    if (h->alloc((void**)&h->props, sizeof(MatProps) * kMaxMaterials) != cudaSuccess ||
+        h->alloc((void**)&h->coef, sizeof(MatCoef) * (kMaxMaterials + 1)) != cudaSuccess ||
+        h->alloc((void**)&h->status, sizeof(int)) != cudaSuccess)
+        return cleanup(fail(FDTD_ERR_OOM, "table allocation failed"));
+    const int ns[3] = {g.nx, g.ny, g.nz};
+    for (int a = 0; a < 3; ++a)
+        for (int q = 0; q < 6; ++q)
+            if (h->alloc((void**)&h->prof[6 * a + q], sizeof(float) * ns[a]) != cudaSuccess)
+                return cleanup(fail(FDTD_ERR_OOM, "profile allocation failed"));
+    // CPML memory: x faces (nz, ny, P), y faces (nz, P, pitch), z faces (P, ny, pitch)
+    const int P[6] = {g.pxn, g.pxp, g.pyn, g.pyp, g.pzn, g.pzp};
+    for (int f = 0; f < 6; ++f) {
+        long long n = 0;
+        if (f < 2) n = (long long)g.nz * g.ny * P[f];
+        else if (f < 4) n = (long long)g.nz * P[f] * g.pitch;
+        else n = (long long)P[f] * g.ny * g.pitch;
+        h->psi_elems[f] = n;
+        for (int s = 0; s < 2; ++s) {
+            float* pe = nullptr; float* ph = nullptr;
+            if (n > 0) {
+                if (h->alloc((void**)&pe, sizeof(float) * n) != cudaSuccess || h->alloc((void**)&ph, sizeof(float) * n) != cudaSuccess)
+                    return cleanup(fail(FDTD_ERR_OOM, "CPML memory allocation failed"));
+            }
+            h->psi.f[f].e[s] = pe;
+            h->psi.f[f].h[s] = ph;
+        }
+    }
+    // initial state of setZero: fields and psi 1.2e-38, material 0 everywhere
+    for (int c = 0; c < 6; ++c)
+        if (launch_fill(h->field[c], V, kTiny, nullptr) != cudaSuccess) return cleanup(fail(FDTD_ERR_CUDA, "fill failed"));
+    for (int f = 0; f < 6; ++f)
+        for (int s = 0; s < 2; ++s) {
+            launch_fill(h->psi.f[f].e[s], h->psi_elems[f], kTiny, nullptr);
+            launch_fill(h->psi.f[f].h[s], h->psi_elems[f], kTiny, nullptr);
+        }
+    if (cudaMemset(h->mat, 0, (size_t)V) != cudaSuccess || cudaMemset(h->status, 0, sizeof(int)) != cudaSuccess)
+        return cleanup(fail(FDTD_ERR_CUDA, "memset failed"));
+    h->materials.push_back(fdtd_material{1.0f, kTiny, 1.0f, kTiny});
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cleanup(fail(FDTD_ERR_CUDA, std::string("init: ") + cudaGetErrorString(e)));
+    *out = h;
+    return FDTD_OK;
+}
+
+int fdtd_destroy(fdtd_handle* h) {
+    if (!h) return FDTD_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    else cudaDeviceSynchronize();
+    for (void* p : h->allocs) cudaFree(p);
+    h->allocs.clear();
+    delete h;
+    return FDTD_OK;
+}
+
+int fdtd_set_stream(fdtd_handle* h, void* s) {
+    if (!h) return fail(FDTD_ERR_INVALID, "handle is NULL");
+    h->stream = (cudaStream_t)s;
+    return FDTD_OK;
+}
+
+int fdtd_set_schedule(fdtd_handle* h, int32_t schedule) {
+    if (!h) return fail(FDTD_ERR_INVALID, "handle is NULL");
+    if (schedule < FDTD_SCHEDULE_AUTO || schedule > FDTD_SCHEDULE_FUSED) return fail(FDTD_ERR_INVALID, "unknown schedule");
+    if (schedule == FDTD_SCHEDULE_FUSED) return fail(FDTD_ERR_INVALID, "fused schedule not available in this build");
+    h->schedule = schedule;
+    return FDTD_OK;
+}
+
+int fdtd_set_materials(fdtd_handle* h, const fdtd_material* table, int32_t n) {
+    if (!h || !table) return fail(FDTD_ERR_INVALID, "NULL argument");
+    if (n < 1 || n > kMaxMaterials) return fail(FDTD_ERR_INVALID, "material count must be 1..256");
+    for (int q = 0; q < n; ++q) {
+        const fdtd_material& m = table[q];
+        if (!(m.eps_r > 0.f) || !(m.mu_r > 0.f) || !std::isfinite(m.eps_r) || !std::isfinite(m.mu_r))
+            return fail(FDTD_ERR_INVALID, "material " + std::to_string(q) + ": eps_r and mu_r must be positive");
+        if (!(m.sigma_e >= 0.f) || !std::isfinite(m.sigma_e))
+            return fail(FDTD_ERR_INVALID, "material " + std::to_string(q) + ": sigma_e must be >= 0");
+        // the harmonic mean of two magnetic conductivities (fdtdrav.h:1187) is 0/0 for zeros
+        if (!(m.sigma_m > 0.f) || !std::isfinite(m.sigma_m))
+            return fail(FDTD_ERR_INVALID, "material " + std::to_string(q) + ": sigma_m must be > 0 (use 1.2e-38 for a lossless medium)");
+    }
+    if (h->prepared && n < (int)h->materials.size())
+        return fail(FDTD_ERR_STATE, "cannot shrink the material table after the index uses it");
+    h->materials.assign(table, table + n);
+    h->dirty_materials = true;
+    return FDTD_OK;
+}
+
+int fdtd_set_material_index(fdtd_handle* h, const uint8_t* cells) {
+    if (!h || !cells) return fail(FDTD_ERR_INVALID, "NULL argument");
+    const DeviceGrid& g = h->g;
+    const size_t n = (size_t)g.nx * g.ny * g.nz;
+    const uint8_t mx = *std::max_element(cells, cells + n);
+    if ((int)mx >= (int)h->materials.size())
+        return fail(FDTD_ERR_INVALID, "material index " + std::to_string(mx) + " outside the material table");
+    CUDA_TRY(cudaMemcpy2DAsync(h->mat, g.pitch, cells, g.nx, g.nx, (size_t)g.ny * g.nz, cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    h->dirty_lumped = true;
+    return FDTD_OK;
+}
+
+int fdtd_add_brick(fdtd_handle* h, const int32_t box[6], int32_t material) {
+    if (!h || !box) return fail(FDTD_ERR_INVALID, "NULL argument");
+    if (material < 0 || material >= (int)h->materials.size()) return fail(FDTD_ERR_INVALID, "material outside the table");
+    int b[6];
+    for (int q = 0; q < 6; ++q) b[q] = box[q];
+    CUDA_TRY(launch_paint(h->mat, h->g, b, (uint8_t)material, h->stream));
+    h->dirty_lumped = true;
+    return FDTD_OK;
+}
+
+static int check_lumped_box(fdtd_handle* h, int32_t axis, const int32_t box[6], float r) {
+    if (!box) return fail(FDTD_ERR_INVALID, "box is NULL");
+    if (axis != 2) return fail(FDTD_ERR_INVALID, "only z-directed lumped elements (axis 2) are supported");
+    const DeviceGrid& g = h->g;
+    const int is = box[0], js = box[1], ks = box[2], ie = box[3], je = box[4], ke = box[5];
+    // Ez is updated for 0 < i < nx-1, 0 < j < ny-1, k < nz-1 (fdtdrav.h:720)
+    if (is < 1 || ie > g.nx - 2 || is > ie || js < 1 || je > g.ny - 2 || js > je || ks < 0 || ke > g.nz - 1 || ks >= ke)
+        return fail(FDTD_ERR_INVALID, "lumped box outside the updated Ez edges or empty (k range is half-open)");
+    if (!(r > 0.f) || !std::isfinite(r)) return fail(FDTD_ERR_INVALID, "resistance must be positive");
+    for (const LumpedDef& L : h->lumped) {
+        const int* o = L.box;
+        if (is <= o[3] && o[0] <= ie && js <= o[4] && o[1] <= je && ks < o[5] && o[2] < ke)
+            return fail(FDTD_ERR_INVALID, "lumped elements may not share edges");
+    }
+    return FDTD_OK;
+}
+
+int fdtd_add_lumped_source(fdtd_handle* h, int32_t axis, const int32_t box[6], float resistance,
+                           const float* voltage, int64_t n_samples, int32_t* id_out) {
+    if (!h) return fail(FDTD_ERR_INVALID, "handle is NULL");
+    int rc = check_lumped_box(h, axis, box, resistance);
+    if (rc) return rc;
+    if (n_samples < 0 || (n_samples > 0 && !voltage)) return fail(FDTD_ERR_INVALID, "bad waveform");
+    LumpedDef L;
+    std::memcpy(L.box, box, sizeof(L.box));
+    L.resistance = resistance;
+    L.source = (int)h->waves.size();
+    // per-edge signal = V / (ke - ks) (setGauss fdtdrav.h:1494 with v_mag_factor fdtdrav.h:3613)
+    const float nseg = (float)(box[5] - box[2]);
+    std::vector<float> w((size_t)n_samples);
+    for (int64_t m = 0; m < n_samples; ++m) w[(size_t)m] = voltage[m] / nseg;
+    h->waves.push_back(std::move(w));
+    h->lumped.push_back(L);
+    h->dirty_lumped = true;
+    if (id_out) *id_out = L.source;
+    return FDTD_OK;
+}
+
+int fdtd_add_resistor(fdtd_handle* h, int32_t axis, const int32_t box[6], float resistance) {
+    if (!h) return fail(FDTD_ERR_INVALID, "handle is NULL");
+    int rc = check_lumped_box(h, axis, box, resistance);
+    if (rc) return rc;
+    LumpedDef L;
+    std::memcpy(L.box, box, sizeof(L.box));
+    L.resistance = resistance;
+    L.source = -1;
+    h->lumped.push_back(L);
+    h->dirty_lumped = true;
+    return FDTD_OK;
+}
+
+int fdtd_add_probe(fdtd_handle* h, int32_t comp, int32_t i, int32_t j, int32_t k, int32_t* id_out) {
+    if (!h) return fail(FDTD_ERR_INVALID, "handle is NULL");
+    if (comp < 0 || comp > 5) return fail(FDTD_ERR_INVALID, "component must be 0..5");
+    if (i < 0 || i >= h->g.nx || j < 0 || j >= h->g.ny || k < 0 || k >= h->g.nz) return fail(FDTD_ERR_INVALID, "probe outside the grid");
+    if (h->step > 0) return fail(FDTD_ERR_STATE, "probes must be added before the first step");
+    h->probes.push_back(Probe{comp, i, j, k});
+    h->dirty_probes = true;
+    if (id_out) *id_out = (int)h->probes.size() - 1;
+    return FDTD_OK;
+}
+
+int fdtd_set_probe_capacity(fdtd_handle* h, int64_t steps) {
+    if (!h) return fail(FDTD_ERR_INVALID, "handle is NULL");
+    if (steps < 1) return fail(FDTD_ERR_INVALID, "capacity must be >= 1");
+    if (h->step > 0) return fail(FDTD_ERR_STATE, "capacity must be set before the first step");
+    h->ring_cap = steps;
+    h->dirty_probes = true;
+    return FDTD_OK;
+}
+
+int fdtd_prepare(fdtd_handle* h) {
+    if (!h) return fail(FDTD_ERR_INVALID, "handle is NULL");
+    return ensure_prepared(h);
+}
+
+int fdtd_step(fdtd_handle* h, int64_t n) {
+    if (!h) return fail(FDTD_ERR_INVALID, "handle is NULL");
+    if (n < 0) return fail(FDTD_ERR_INVALID, "negative step count");
+    int rc = ensure_prepared(h);
+    if (rc) return rc;
+    StepParams p = make_params(h);
+    FieldPtrs f{h->field[0], h->field[1], h->field[2], h->field[3], h->field[4], h->field[5]};
+    for (int64_t s = 0; s < n; ++s) {
+        CUDA_TRY(launch_two_pass(p, f, h->psi, h->step, h->stream));
+        ++h->step;
+    }
+    return FDTD_OK;
+}
+
+int fdtd_synchronize(fdtd_handle* h) {
+    if (!h) return fail(FDTD_ERR_INVALID, "handle is NULL");
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    int st = 0;
+    CUDA_TRY(cudaMemcpy(&st, h->status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (st) return fail(FDTD_ERR_DEVICE, "device status word " + std::to_string(st));
+    return FDTD_OK;
+}
+
+int64_t fdtd_current_step(const fdtd_handle* h) { return h ? h->step : -1; }
+int32_t fdtd_probe_count(const fdtd_handle* h) { return h ? (int32_t)h->probes.size() : -1; }
+
+int fdtd_read_probes(fdtd_handle* h, int64_t first, int64_t n, float* out) {
+    if (!h || (!out && n > 0)) return fail(FDTD_ERR_INVALID, "NULL argument");
+    if (n == 0 || h->probes.empty()) return FDTD_OK;
+    if (first < 0 || first + n > h->step) return fail(FDTD_ERR_RANGE, "steps not computed yet");
+    if (first < h->step - h->ring_cap) return fail(FDTD_ERR_RANGE, "steps already overwritten in the probe ring buffer");
+    const int np = (int)h->probes.size();
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    int64_t done = 0;
+    while (done < n) {
+        const int64_t m = first + done;
+        const int64_t row = m % h->ring_cap;
+        const int64_t run = std::min<int64_t>(n - done, h->ring_cap - row);
+        CUDA_TRY(cudaMemcpy(out + done * np, h->ring + row * np, (size_t)run * np * sizeof(float), cudaMemcpyDeviceToHost));
+        done += run;
+    }
+    return FDTD_OK;
+}
+
+int fdtd_get_field(fdtd_handle* h, int32_t comp, float* out) {
+    if (!h || !out) return fail(FDTD_ERR_INVALID, "NULL argument");
+    if (comp < 0 || comp > 5) return fail(FDTD_ERR_INVALID, "component must be 0..5");
+    const DeviceGrid& g = h->g;
+    CUDA_TRY(cudaMemcpy2DAsync(out, (size_t)g.nx * 4, h->field[comp], (size_t)g.pitch * 4, (size_t)g.nx * 4,
+                               (size_t)g.ny * g.nz, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return FDTD_OK;
+}
+
+int fdtd_set_field(fdtd_handle* h, int32_t comp, const float* in) {
+    if (!h || !in) return fail(FDTD_ERR_INVALID, "NULL argument");
+    if (comp < 0 || comp > 5) return fail(FDTD_ERR_INVALID, "component must be 0..5");
+    const DeviceGrid& g = h->g;
+    CUDA_TRY(cudaMemcpy2DAsync(h->field[comp], (size_t)g.pitch * 4, in, (size_t)g.nx * 4, (size_t)g.nx * 4,
+                               (size_t)g.ny * g.nz, cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return FDTD_OK;
+}
+
+int fdtd_get_field_device(fdtd_handle* h, int32_t comp, float* out) {
+    if (!h || !out) return fail(FDTD_ERR_INVALID, "NULL argument");
+    if (comp < 0 || comp > 5) return fail(FDTD_ERR_INVALID, "component must be 0..5");
+    const DeviceGrid& g = h->g;
+    CUDA_TRY(cudaMemcpy2DAsync(out, (size_t)g.nx * 4, h->field[comp], (size_t)g.pitch * 4, (size_t)g.nx * 4,
+                               (size_t)g.ny * g.nz, cudaMemcpyDeviceToDevice, h->stream));
+    return FDTD_OK;
+}
+
+int fdtd_set_field_device(fdtd_handle* h, int32_t comp, const float* in) {
+    if (!h || !in) return fail(FDTD_ERR_INVALID, "NULL argument");
+    if (comp < 0 || comp > 5) return fail(FDTD_ERR_INVALID, "component must be 0..5");
+    const DeviceGrid& g = h->g;
+    CUDA_TRY(cudaMemcpy2DAsync(h->field[comp], (size_t)g.pitch * 4, in, (size_t)g.nx * 4, (size_t)g.nx * 4,
+                               (size_t)g.ny * g.nz, cudaMemcpyDeviceToDevice, h->stream));
+    return FDTD_OK;
+}
+
+int64_t fdtd_state_bytes(const fdtd_handle* h) {
+    if (!h) return -1;
+    long long n = 6 * vol(h);
+    for (int f = 0; f < 6; ++f) n += 4 * h->psi_elems[f];
+    return n * (int64_t)sizeof(float) + 64;
+}
+
+int fdtd_save_state(fdtd_handle* h, void* buf) {
+    if (!h || !buf) return fail(FDTD_ERR_INVALID, "NULL argument");
+    char* p = (char*)buf;
+    const size_t V = (size_t)vol(h) * sizeof(float);
+    for (int c = 0; c < 6; ++c, p += V) CUDA_TRY(cudaMemcpyAsync(p, h->field[c], V, cudaMemcpyDeviceToDevice, h->stream));
+    for (int f = 0; f < 6; ++f) {
+        const size_t n = (size_t)h->psi_elems[f] * sizeof(float);
+        float* arr[4] = {h->psi.f[f].e[0], h->psi.f[f].e[1], h->psi.f[f].h[0], h->psi.f[f].h[1]};
+        for (int q = 0; q < 4; ++q, p += n)
+            if (n) CUDA_TRY(cudaMemcpyAsync(p, arr[q], n, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    long long hdr[8] = {h->step, h->g.nx, h->g.ny, h->g.nz, 0, 0, 0, 0};
+    CUDA_TRY(cudaMemcpyAsync(p, hdr, sizeof(hdr), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return FDTD_OK;
+}
+
+int fdtd_load_state(fdtd_handle* h, const void* buf) {
+    if (!h || !buf) return fail(FDTD_ERR_INVALID, "NULL argument");
+    const char* p = (const char*)buf;
+    const size_t V = (size_t)vol(h) * sizeof(float);
+    for (int c = 0; c < 6; ++c, p += V) CUDA_TRY(cudaMemcpyAsync(h->field[c], p, V, cudaMemcpyDeviceToDevice, h->stream));
+    for (int f = 0; f < 6; ++f) {
+        const size_t n = (size_t)h->psi_elems[f] * sizeof(float);
+        float* arr[4] = {h->psi.f[f].e[0], h->psi.f[f].e[1], h->psi.f[f].h[0], h->psi.f[f].h[1]};
+        for (int q = 0; q < 4; ++q, p += n)
+            if (n) CUDA_TRY(cudaMemcpyAsync(arr[q], p, n, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    long long hdr[8];
+    CUDA_TRY(cudaMemcpyAsync(hdr, p, sizeof(hdr), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    if (hdr[1] != h->g.nx || hdr[2] != h->g.ny || hdr[3] != h->g.nz) return fail(FDTD_ERR_INVALID, "state belongs to another grid");
+    h->step = hdr[0];
+    return FDTD_OK;
+}
+
+int fdtd_get_cpml_profile(fdtd_handle* h, int32_t axis, int32_t kind, float* out) {
+    if (!h || !out) return fail(FDTD_ERR_INVALID, "NULL argument");
+    if (axis < 0 || axis > 2 || kind < 0 || kind > 5) return fail(FDTD_ERR_INVALID, "axis 0..2, kind 0..5");
+    int rc = ensure_prepared(h);
+    if (rc) return rc;
+    const int n = axis == 0 ? h->g.nx : axis == 1 ? h->g.ny : h->g.nz;
+    CUDA_TRY(cudaMemcpy(out, h->prof[6 * axis + kind], sizeof(float) * n, cudaMemcpyDeviceToHost));
+    return FDTD_OK;
+}
+
+int64_t fdtd_device_bytes(const fdtd_handle* h) { return h ? h->bytes : -1; }
+
+}  // extern "C"
+
+namespace {
+
+int build_lumped(fdtd_handle* h) {
+    // free the previous tables
+    h->release(h->d_lumped); h->release(h->d_lumped_k); h->release(h->d_waves); h->release(h->d_wave_len);
+    h->release(h->d_lumped_box); h->release(h->d_lumped_r); h->release(h->d_lumped_owner);
+    for (float* w : h->d_wave_bufs) h->release(w);
+    h->d_wave_bufs.clear();
+    h->d_lumped = nullptr; h->d_lumped_k = nullptr; h->d_waves = nullptr; h->d_wave_len = nullptr;
+    h->d_lumped_box = nullptr; h->d_lumped_r = nullptr; h->d_lumped_owner = nullptr;
+    const DeviceGrid& g = h->g;
+    // edges bucketed by plane k
+    std::vector<LumpedEdge> edges;
+    std::vector<int> owner;
+    for (size_t q = 0; q < h->lumped.size(); ++q) {
+        const LumpedDef& L = h->lumped[q];
+        for (int k = L.box[2]; k < L.box[5]; ++k)
+            for (int j = L.box[1]; j <= L.box[4]; ++j)
+                for (int i = L.box[0]; i <= L.box[3]; ++i) {
+                    edges.push_back(LumpedEdge{i, j, k, L.source, 0.f, 0.f, 0.f, 0.f});
+                    owner.push_back((int)q);
+                }
+    }
+    std::vector<int> order(edges.size());
+    for (size_t q = 0; q < order.size(); ++q) order[q] = (int)q;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return edges[a].k < edges[b].k; });
+    std::vector<LumpedEdge> se;
+    std::vector<int> so;
+    for (int q : order) { se.push_back(edges[q]); so.push_back(owner[q]); }
+    std::vector<int> koff(g.nz + 1, 0);
+    for (const LumpedEdge& e : se) koff[e.k + 1]++;
+    for (int k = 0; k < g.nz; ++k) koff[k + 1] += koff[k];
+    const size_t ne = se.size();
+    CUDA_TRY(h->alloc((void**)&h->d_lumped_k, sizeof(int) * (g.nz + 1)));
+    CUDA_TRY(cudaMemcpy(h->d_lumped_k, koff.data(), sizeof(int) * (g.nz + 1), cudaMemcpyHostToDevice));
+    CUDA_TRY(h->alloc((void**)&h->d_lumped, sizeof(LumpedEdge) * std::max<size_t>(ne, 1)));
+    if (ne) {
+        std::vector<int> boxes;
+        std::vector<float> rs;
+        for (const LumpedDef& L : h->lumped) { boxes.insert(boxes.end(), L.box, L.box + 6); rs.push_back(L.resistance); }
+        CUDA_TRY(h->alloc((void**)&h->d_lumped_box, sizeof(int) * boxes.size()));
+        CUDA_TRY(h->alloc((void**)&h->d_lumped_r, sizeof(float) * rs.size()));
+        CUDA_TRY(h->alloc((void**)&h->d_lumped_owner, sizeof(int) * ne));
+        CUDA_TRY(cudaMemcpy(h->d_lumped, se.data(), sizeof(LumpedEdge) * ne, cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemcpy(h->d_lumped_box, boxes.data(), sizeof(int) * boxes.size(), cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemcpy(h->d_lumped_r, rs.data(), sizeof(float) * rs.size(), cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemcpy(h->d_lumped_owner, so.data(), sizeof(int) * ne, cudaMemcpyHostToDevice));
+        CUDA_TRY(launch_lumped_coefs(g, h->mat, h->props, h->d_lumped, h->d_lumped_box, h->d_lumped_r,
+                                     h->d_lumped_owner, (int)ne, h->stream));
+    }
+    // waveforms
+    const size_t nw = h->waves.size();
+    std::vector<float*> ptrs(std::max<size_t>(nw, 1), nullptr);
+    std::vector<long long> lens(std::max<size_t>(nw, 1), 0);
+    for (size_t w = 0; w < nw; ++w) {
+        float* d = nullptr;
+        CUDA_TRY(h->alloc((void**)&d, sizeof(float) * std::max<size_t>(h->waves[w].size(), 1)));
+        if (!h->waves[w].empty())
+            CUDA_TRY(cudaMemcpy(d, h->waves[w].data(), sizeof(float) * h->waves[w].size(), cudaMemcpyHostToDevice));
+        h->d_wave_bufs.push_back(d);
+        ptrs[w] = d;
+        lens[w] = (long long)h->waves[w].size();
+    }
+    CUDA_TRY(h->alloc((void**)&h->d_waves, sizeof(float*) * ptrs.size()));
+    CUDA_TRY(h->alloc((void**)&h->d_wave_len, sizeof(long long) * lens.size()));
+    CUDA_TRY(cudaMemcpy(h->d_waves, ptrs.data(), sizeof(float*) * ptrs.size(), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(h->d_wave_len, lens.data(), sizeof(long long) * lens.size(), cudaMemcpyHostToDevice));
+    h->dirty_lumped = false;
+    return FDTD_OK;
+}
+
+int build_probes(fdtd_handle* h) {
+    h->release(h->d_probes); h->release(h->d_probe_k); h->release(h->d_probe_ids); h->release(h->ring);
+    h->d_probes = nullptr; h->d_probe_k = nullptr; h->d_probe_ids = nullptr; h->ring = nullptr;
+    const DeviceGrid& g = h->g;
+    const size_t np = h->probes.size();
+    std::vector<int> order(np);
+    for (size_t q = 0; q < np; ++q) order[q] = (int)q;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return h->probes[a].k < h->probes[b].k; });
+    std::vector<Probe> sp;
+    for (int q : order) sp.push_back(h->probes[q]);
+    std::vector<int> koff(g.nz + 1, 0);
+    for (const Probe& p : sp) koff[p.k + 1]++;
+    for (int k = 0; k < g.nz; ++k) koff[k + 1] += koff[k];
+    CUDA_TRY(h->alloc((void**)&h->d_probe_k, sizeof(int) * (g.nz + 1)));
+    CUDA_TRY(cudaMemcpy(h->d_probe_k, koff.data(), sizeof(int) * (g.nz + 1), cudaMemcpyHostToDevice));
+    CUDA_TRY(h->alloc((void**)&h->d_probes, sizeof(Probe) * std::max<size_t>(np, 1)));
+    CUDA_TRY(h->alloc((void**)&h->d_probe_ids, sizeof(int) * std::max<size_t>(np, 1)));
+    if (np) {
+        CUDA_TRY(cudaMemcpy(h->d_probes, sp.data(), sizeof(Probe) * np, cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemcpy(h->d_probe_ids, order.data(), sizeof(int) * np, cudaMemcpyHostToDevice));
+    }
+    CUDA_TRY(h->alloc((void**)&h->ring, sizeof(float) * (size_t)h->ring_cap * std::max<size_t>(np, 1)));
+    h->dirty_probes = false;
+    return FDTD_OK;
+}
+
+int ensure_prepared(fdtd_handle* h) {
+    if (!h->dirty_materials && !h->dirty_lumped && !h->dirty_probes && h->prepared) return FDTD_OK;
+    if (h->dirty_materials || !h->prepared) {
+        std::vector<MatProps> props(kMaxMaterials);
+        for (int q = 0; q < kMaxMaterials; ++q) {
+            const fdtd_material m = q < (int)h->materials.size() ? h->materials[q] : fdtd_material{1.0f, kTiny, 1.0f, kTiny};
+            props[q] = MatProps{m.eps_r, m.sigma_e, m.mu_r, m.sigma_m};
+        }
+        CUDA_TRY(cudaMemcpy(h->props, props.data(), sizeof(MatProps) * kMaxMaterials, cudaMemcpyHostToDevice));
+        CUDA_TRY(launch_material_tables(h->g, h->props, (int)h->materials.size(), h->coef, h->stream));
+        h->dirty_materials = false;
+        h->dirty_lumped = true;
+    }
+    if (!h->prepared) CUDA_TRY(launch_cpml_profiles(h->g, h->grid.pi, h->prof, h->stream));
+    if (h->dirty_lumped) {
+        int rc = build_lumped(h);
+        if (rc) return rc;
+    }
+    if (h->dirty_probes) {
+        int rc = build_probes(h);
+        if (rc) return rc;
+    }
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    h->prepared = true;
+    return FDTD_OK;
+}
+
+}  // namespace

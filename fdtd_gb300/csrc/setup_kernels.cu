@@ -1,0 +1,177 @@
+// Setup kernels: CPML profiles, per-material coefficient tables, lumped-edge coefficients,
+// material painting and fills. They run once per simulation (fdtd_prepare).
+//
+// The CPML profile and lumped-element expressions are evaluated on the device with the same
+// float/double mix and the same device powf/expf as the reference's setABCPML and defineSourceZ /
+// defineResistor, so the resulting tables equal the reference's bit for bit.
+#include "yee_common.cuh"
+#include "yee_kernels.h"
+
+namespace fdtd {
+
+// One axis of setABCPML (fdtdrav.h:1774-1891 for x_n, 1912-1941 for x_p, and the y / z mirrors).
+// prof = {b_e, a_e, b_m, a_m, kappa_e, kappa_m}, each n entries. Nodes outside both slabs keep
+// b = a = 1.2e-38 (setZero) and kappa = 1.
+__global__ void k_cpml_axis(float* be, float* ae, float* bm, float* am, float* ke, float* km, int n,
+                            int pn_i, int pp_i, float delta, float dt, float eps_0, float mu_0, float pi) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    // parameters of fdtdrav.h:1774-1812, as float locals
+    float npml = 3;
+    float sigma_factor = 1.5;
+    float kappa_max = 5;
+    float alpha_max = 0.05;
+    float alpha_min = 0.00;
+    float sigma_opt = (npml + 1) / (150 * pi * 1 * delta);
+    float sigma_max = sigma_factor * sigma_opt;
+    const float pn = (float)pn_i, pp = (float)pp_i;
+    float roe, rom;
+    bool in = false;
+    if (q < pn_i) {
+        roe = (pn - q - 0.75) / pn;
+        rom = (pn - q - 0.25) / pn;
+        in = true;
+    } else if (q >= n - pp_i) {
+        roe = (q - (n - pp - 1) - 0.75) / pp;
+        rom = (q - (n - pp - 1) - 0.25) / pp;
+        in = true;
+    }
+    if (!in) {
+        be[q] = kTiny; ae[q] = kTiny; bm[q] = kTiny; am[q] = kTiny; ke[q] = 1.0f; km[q] = 1.0f;
+        return;
+    }
+    float sigma_pe = sigma_max * powf(roe, npml);
+    float sigma_pm = sigma_max * powf(rom, npml);
+    sigma_pm = sigma_pm * (mu_0 / eps_0);
+    float kappa_e = 1 + (kappa_max - 1) * powf(roe, npml);
+    float kappa_m = 1 + (kappa_max - 1) * powf(rom, npml);
+    float alpha_e = alpha_min + (alpha_max - alpha_min) * (1 - roe);
+    float alpha_m = alpha_min + (alpha_max - alpha_min) * (1 - rom);
+    alpha_m = alpha_m * (mu_0 / eps_0);
+    float b_e = expf((-dt / eps_0) * ((sigma_pe / kappa_e) + alpha_e));
+    float a_e = (1 / delta) * (b_e - 1) * sigma_pe / (kappa_e * (sigma_pe + kappa_e * alpha_e));
+    float b_m = expf((-dt / mu_0) * ((sigma_pm / kappa_m) + alpha_m));
+    float a_m = (1 / delta) * (b_m - 1) * sigma_pm / (kappa_m * (sigma_pm + kappa_m * alpha_m));
+    be[q] = b_e; ae[q] = a_e; bm[q] = b_m; am[q] = a_m; ke[q] = kappa_e; km[q] = kappa_m;
+}
+
+cudaError_t launch_cpml_profiles(const DeviceGrid& g, float pi, float* const prof[18], cudaStream_t st) {
+    const int ns[3] = {g.nx, g.ny, g.nz};
+    const int pn[3] = {g.pxn, g.pyn, g.pzn};
+    const int pp[3] = {g.pxp, g.pyp, g.pzp};
+    const float d[3] = {g.dx, g.dy, g.dz};
+    for (int a = 0; a < 3; ++a) {
+        float* const* P = prof + 6 * a;
+        k_cpml_axis<<<(ns[a] + 127) / 128, 128, 0, st>>>(P[0], P[1], P[2], P[3], P[4], P[5], ns[a], pn[a], pp[a],
+                                                         d[a], g.dt, g.eps0, g.mu0, pi);
+    }
+    return cudaGetLastError();
+}
+
+// Coefficients of edges whose surrounding cells share material m (the averages of four / two equal
+// values computed with the reference's formulas), plus the default entry for H faces on the low
+// boundary of their axis (mu = 1, sigma_m = 1.2e-38).
+__global__ void k_material_tables(const MatProps* props, int n, MatCoef* coef, DeviceGrid g) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m > kMaxMaterials) return;
+    MatCoef c;
+    MatProps a;
+    if (m == kDefaultEntry) {
+        a.eps = 1.0f; a.sig = kTiny; a.mu = 1.0f; a.sigm = kTiny;
+    } else if (m < n) {
+        a = props[m];
+    } else {
+        a.eps = 1.0f; a.sig = kTiny; a.mu = 1.0f; a.sigm = kTiny;
+    }
+    const float eps = avg4(a.eps, a.eps, a.eps, a.eps);
+    const float sig = avg4(a.sig, a.sig, a.sig, a.sig);
+    const float mu = m == kDefaultEntry ? 1.0f : harm2(a.mu, a.mu);
+    const float sm = m == kDefaultEntry ? kTiny : harm2(a.sigm, a.sigm);
+    const float dp_e[3] = {g.dy, g.dz, g.dx}, dm_e[3] = {g.dz, g.dx, g.dy};
+    const float dp_h[3] = {g.dz, g.dx, g.dy}, dm_h[3] = {g.dy, g.dz, g.dx};
+    for (int q = 0; q < 3; ++q) {
+        Coef3 e = coef3(eps, sig, g.dt, g.eps0, dp_e[q], dm_e[q]);
+        c.e[q][0] = e.a; c.e[q][1] = e.bp; c.e[q][2] = e.bm;
+        Coef3 h = coef3(mu, sm, g.dt, g.mu0, dp_h[q], dm_h[q]);
+        c.h[q][0] = h.a; c.h[q][1] = h.bp; c.h[q][2] = h.bm;
+    }
+    coef[m] = c;
+}
+
+cudaError_t launch_material_tables(const DeviceGrid& g, const MatProps* props, int n, MatCoef* coef,
+                                   cudaStream_t st) {
+    k_material_tables<<<(kMaxMaterials + 1 + 127) / 128, 128, 0, st>>>(props, n, coef, g);
+    return cudaGetLastError();
+}
+
+// Lumped-edge coefficient overrides (defineSourceZ fdtdrav.h:1368-1426 for sources,
+// defineResistor fdtdrav.h:1429-1483 for resistors), from the edge-averaged eps_z / sigma_z.
+// boxes: per owner {is,js,ks,ie,je,ke}; owner[e] = index of the element an edge belongs to.
+__global__ void k_lumped_coefs(DeviceGrid g, const uint8_t* mat, const MatProps* props, LumpedEdge* edges,
+                               const int* boxes, const float* resist, const int* owner, int n_edges) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_edges) return;
+    LumpedEdge L = edges[e];
+    const int* b = boxes + 6 * owner[e];
+    float dt = g.dt, dx = g.dx, dy = g.dy, dz = g.dz, eps_0 = g.eps0;
+    float rs = resist[owner[e]];
+    float _is = (float)b[0], _js = (float)b[1], _ks = (float)b[2];
+    float _ie = (float)b[3], _je = (float)b[4], _ke = (float)b[5];
+    float r_comp = (1 + _ie - _is) * (1 + _je - _js) / (_ke - _ks);
+    r_comp = r_comp * rs;
+    float rfactor = (dt * dz) / (r_comp * dx * dy);
+    float rfactor_aux = (r_comp * dx * dy);
+    // eps_z / sigma_z of the edge: average of cells (i,j), (i-1,j), (i,j-1), (i-1,j-1) in plane k
+    const long long n = (long long)L.k * g.plane + (long long)L.j * g.pitch + L.i;
+    const MatProps a = props[mat[n]], bb = props[mat[n - 1]], c = props[mat[n - g.pitch]], d = props[mat[n - 1 - g.pitch]];
+    float eps_z = avg4(a.eps, bb.eps, c.eps, d.eps);
+    float sig_z = avg4(a.sig, bb.sig, c.sig, d.sig);
+    float den = __fadd_rn(__fmaf_rn(2.0f * eps_z, eps_0, __fmul_rn(dt, sig_z)), rfactor);
+    float num = __fsub_rn(__fmaf_rn(2.0f * eps_z, eps_0, -__fmul_rn(dt, sig_z)), rfactor);
+    L.ceze = __fdiv_rn(num, den);
+    L.cezhy = __fdiv_rn(__fdiv_rn(2.0f * dt, dx), den);
+    L.cezhx = __fdiv_rn(__fdiv_rn(-2.0f * dt, dy), den);
+    L.cezj = L.source >= 0 ? __fdiv_rn(__fdiv_rn(-2.0f * dt, rfactor_aux), den) : 0.0f;
+    edges[e] = L;
+}
+
+cudaError_t launch_lumped_coefs(const DeviceGrid& g, const uint8_t* mat, const MatProps* props,
+                                LumpedEdge* edges, const int* boxes, const float* resist, const int* owner,
+                                int n_edges, cudaStream_t st) {
+    if (n_edges == 0) return cudaSuccess;
+    k_lumped_coefs<<<(n_edges + 127) / 128, 128, 0, st>>>(g, mat, props, edges, boxes, resist, owner, n_edges);
+    return cudaGetLastError();
+}
+
+__global__ void k_fill(float* p, long long n, float v) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
+        p[q] = v;
+}
+
+cudaError_t launch_fill(float* p, long long n, float v, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    long long blocks = (n + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    k_fill<<<(int)blocks, 256, 0, st>>>(p, n, v);
+    return cudaGetLastError();
+}
+
+// setBrick (fdtdrav.h:1524-1571) on the material index: cells [is,ie) x [js,je) x [ks,ke).
+__global__ void k_paint(uint8_t* mat, DeviceGrid g, int is, int js, int ks, int ie, int je, int ke, uint8_t v) {
+    const int i = is + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = js + blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = ks + blockIdx.z;
+    if (i < ie && j < je && k < ke) mat[(long long)k * g.plane + (long long)j * g.pitch + i] = v;
+}
+
+cudaError_t launch_paint(uint8_t* mat, const DeviceGrid& g, const int box[6], uint8_t value, cudaStream_t st) {
+    const int is = box[0] < 0 ? 0 : box[0], js = box[1] < 0 ? 0 : box[1], ks = box[2] < 0 ? 0 : box[2];
+    const int ie = box[3] > g.nx ? g.nx : box[3], je = box[4] > g.ny ? g.ny : box[4], ke = box[5] > g.nz ? g.nz : box[5];
+    if (is >= ie || js >= je || ks >= ke) return cudaSuccess;
+    dim3 block(32, 8, 1);
+    dim3 grid((ie - is + 31) / 32, (je - js + 7) / 8, ke - ks);
+    k_paint<<<grid, block, 0, st>>>(mat, g, is, js, ks, ie, je, ke, value);
+    return cudaGetLastError();
+}
+
+}  // namespace fdtd

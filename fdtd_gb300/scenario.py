@@ -1,0 +1,265 @@
+"""Scenario description and seeded generators for the FDTD workloads.
+
+A scenario is everything the reference's host driver ``marchingLoop`` (fdtdrav.h:3425) derives
+before its time loop, expressed in index space:
+
+* grid: node counts ``nx, ny, nz`` (the reference's NXX, NYY, NZ, fdtdrav.h:3487-3491), cell sizes,
+  time step and the physical constants the reference passes around as floats (source.cu:30-46);
+* CPML thickness per face (x_n, x_p, y_n, y_p, z_n, z_p);
+* bricks: cell boxes ``[is,ie) x [js,je) x [ks,ke)`` painted with a material id, the last box
+  painted wins (setBrick, fdtdrav.h:1524-1571, applied in order at fdtdrav.h:4104-4128);
+* lumped z-directed sources ``i in [is,ie], j in [js,je], k in [ks,ke)`` with a resistance and a
+  voltage waveform (defineSourceZ fdtdrav.h:1368-1426, injection fdtdrav.h:726-733) and
+  resistors (defineResistor fdtdrav.h:1429-1483);
+* point probes (component, i, j, k), the point form of sampleField (fdtdrav.h:234-246).
+
+The generators reproduce the workload shapes used for parity and benchmarking: a vacuum cube
+with one Gaussian-derivative source (64^3), seeded random dielectric boxes with several delayed
+sources (512^3 and its scaled-down forms), and the HBM-sized 1024x1024x896 domain.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+
+# Components, in the order the C ABI numbers them.
+EX, EY, EZ, HX, HY, HZ = range(6)
+COMPONENT_NAMES = ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")
+
+# Constants exactly as the reference's main() builds them in float (source.cu:30-33).
+REF_EPS0 = np.float32(8.854187817e-12)
+REF_PI = np.float32(3.1415)
+REF_MU0 = np.float32(np.float64(np.float32(4.0) * REF_PI) * 1e-7)
+# Background cells hold eps_r = mu_r = 1 and conductivities 1.2e-38 (setZero, fdtdrav.h:939-962).
+REF_TINY = np.float32(1.2e-38)
+
+
+def ref_light_speed(eps0=REF_EPS0, mu0=REF_MU0) -> np.float32:
+    """c = 1 / sqrt(mu0 * eps0) in float (source.cu:33)."""
+    return np.float32(np.float32(1.0) / np.sqrt(np.float32(np.float32(mu0) * np.float32(eps0))))
+
+
+def courant_dt(dx, dy, dz, courant=1.0, eps0=REF_EPS0, mu0=REF_MU0) -> np.float32:
+    """Time step of source.cu:45-46: 1/(c*sqrt(1/dx^2+1/dy^2+1/dz^2)) times the Courant factor.
+
+    The reference evaluates the sum with double-precision pow and stores the result in a float.
+    """
+    c = float(ref_light_speed(eps0, mu0))
+    dx, dy, dz = float(np.float32(dx)), float(np.float32(dy)), float(np.float32(dz))
+    dt = np.float32(1.0 / (np.float32(c) * math.sqrt(1.0 / dx ** 2 + 1.0 / dy ** 2 + 1.0 / dz ** 2)))
+    return np.float32(np.float32(courant) * dt)
+
+
+def calc_index(coordinate: float, delta: float) -> int:
+    """Metre -> node index, ``(int)round(coordinate / delta)`` in float (calc_index, fdtdrav.h:198-206)."""
+    q = np.float32(np.float32(coordinate) / np.float32(delta))
+    # C round(): half away from zero
+    return int(math.floor(abs(float(q)) + 0.5)) * (1 if q >= 0 else -1)
+
+
+@dataclasses.dataclass
+class Material:
+    eps_r: float = 1.0
+    sigma_e: float = float(REF_TINY)
+    mu_r: float = 1.0
+    sigma_m: float = float(REF_TINY)
+
+
+@dataclasses.dataclass
+class Brick:
+    box: Tuple[int, int, int, int, int, int]  # is, js, ks, ie, je, ke (half-open cell box)
+    material: int                             # index into Scenario.materials
+
+
+@dataclasses.dataclass
+class LumpedSource:
+    box: Tuple[int, int, int, int, int, int]  # is, js, ks, ie, je, ke (i,j closed, k half-open)
+    resistance: float
+    waveform: np.ndarray                      # float32 voltage V(t) per time step
+
+
+@dataclasses.dataclass
+class Resistor:
+    box: Tuple[int, int, int, int, int, int]
+    resistance: float
+
+
+@dataclasses.dataclass
+class Probe:
+    component: int
+    i: int
+    j: int
+    k: int
+
+
+@dataclasses.dataclass
+class Scenario:
+    name: str
+    nx: int
+    ny: int
+    nz: int
+    dx: float
+    dy: float
+    dz: float
+    dt: float
+    pml: Tuple[int, int, int, int, int, int]  # x_n, x_p, y_n, y_p, z_n, z_p
+    steps: int
+    materials: List[Material]
+    bricks: List[Brick] = dataclasses.field(default_factory=list)
+    sources: List[LumpedSource] = dataclasses.field(default_factory=list)
+    resistors: List[Resistor] = dataclasses.field(default_factory=list)
+    probes: List[Probe] = dataclasses.field(default_factory=list)
+    eps0: float = float(REF_EPS0)
+    mu0: float = float(REF_MU0)
+    pi: float = float(REF_PI)
+    seed: Optional[int] = None
+
+    @property
+    def cells(self) -> int:
+        return self.nx * self.ny * self.nz
+
+    def material_index(self) -> np.ndarray:
+        """uint8 cell material index, shape (nz, ny, nx), bricks painted in order (last wins)."""
+        idx = np.zeros((self.nz, self.ny, self.nx), dtype=np.uint8)
+        for b in self.bricks:
+            is_, js, ks, ie, je, ke = b.box
+            is_, js, ks = max(is_, 0), max(js, 0), max(ks, 0)
+            ie, je, ke = min(ie, self.nx), min(je, self.ny), min(ke, self.nz)
+            if is_ < ie and js < je and ks < ke:
+                idx[ks:ke, js:je, is_:ie] = b.material
+        return idx
+
+    def material_table(self) -> np.ndarray:
+        """float32 table (n_materials, 4): eps_r, sigma_e, mu_r, sigma_m."""
+        return np.array([[m.eps_r, m.sigma_e, m.mu_r, m.sigma_m] for m in self.materials], dtype=np.float32)
+
+    def signal_per_node(self, s: int) -> np.ndarray:
+        """Per-edge source signal, V(t) / (ke - ks) in float (setGauss, fdtdrav.h:1494; fdtdrav.h:3613)."""
+        src = self.sources[s]
+        n = np.float32(src.box[5] - src.box[2])
+        return (np.asarray(src.waveform, dtype=np.float32) / n).astype(np.float32)
+
+
+# ----------------------------------------------------------------------------------------------
+# Waveforms
+# ----------------------------------------------------------------------------------------------
+
+def gaussian_derivative(steps: int, dt: float, fmax: float, dmin: float, delay_steps: float = 0.0,
+                        amp: float = 1.0) -> np.ndarray:
+    """s(t) = -sqrt(2e) * ((t - t0)/tau) * exp(-((t - t0)/tau)^2), unit peak.
+
+    tau = nc * delta / (2 c) with nc = c / (fmax * delta) (the reference's tau formula of
+    source.cu:176-177 with nc derived from fmax), t0 = 4.5 tau, plus an optional delay.
+    Evaluated in float64, stored as float32.
+    """
+    c = float(ref_light_speed())
+    nc = c / (fmax * dmin)
+    tau = nc * dmin / (2.0 * c)
+    t0 = 4.5 * tau + delay_steps * float(dt)
+    t = np.arange(steps, dtype=np.float64) * float(np.float32(dt))
+    u = (t - t0) / tau
+    return (amp * -math.sqrt(2.0 * math.e) * u * np.exp(-u * u)).astype(np.float32)
+
+
+def gaussian(steps: int, dt: float, tau: float, t0: float, amp: float = 1.0) -> np.ndarray:
+    """amp * exp(-((m dt - t0)^2) / tau^2) (setGauss, fdtdrav.h:1486-1501), float64 -> float32."""
+    t = np.arange(steps, dtype=np.float64) * float(np.float32(dt))
+    return (amp * np.exp(-((t - t0) ** 2) / tau ** 2)).astype(np.float32)
+
+
+# ----------------------------------------------------------------------------------------------
+# Workloads
+# ----------------------------------------------------------------------------------------------
+
+def vacuum_cube(n: int = 64, steps: int = 1000, pml: int = 10, delta: float = 1e-3,
+                courant: float = 0.99, fmax: float = 30e9, probe_offset: int = 20,
+                name: Optional[str] = None) -> Scenario:
+    """Vacuum cube with one 50-ohm z-edge source at the centre and an Ez probe ``probe_offset``
+    cells away along x (the 64^3 small / FP64-oracle workload)."""
+    dt = courant_dt(delta, delta, delta, courant)
+    c = n // 2
+    wf = gaussian_derivative(steps, dt, fmax, delta)
+    src = LumpedSource((c, c, c, c, c, c + 1), 50.0, wf)
+    probes = [Probe(EZ, c + probe_offset, c, c)]
+    return Scenario(name or f"vacuum{n}", n, n, n, delta, delta, delta, float(dt), (pml,) * 6, steps,
+                    [Material()], [], [src], [], probes)
+
+
+def random_boxes(nx: int, ny: int, nz: int, steps: int, seed: int = 2024, n_boxes: int = 64,
+                 edge: Tuple[int, int] = (16, 128), pml: int = 10, n_sources: int = 4,
+                 n_probes: int = 16, src_margin: int = 20, delta: float = 1e-3,
+                 courant: float = 0.99, fmax: float = 30e9, max_delay: int = 200,
+                 eps_range=(1.0, 12.0), sigma_range=(0.0, 0.05), name: Optional[str] = None) -> Scenario:
+    """Seeded random dielectric boxes with delayed lumped sources and Ez/Hx probes.
+
+    64 boxes with per-axis edge lengths uniform in ``edge`` cells, positions uniform and clipped to
+    the non-CPML interior, eps_r ~ U(eps_range), sigma ~ U(sigma_range) S/m, last box wins; one
+    material per box (65 materials with the background). ``n_sources`` 50-ohm z-edge sources at
+    least ``src_margin`` cells from the CPML, with delays ~ U[0, max_delay] steps. Half the probes
+    are Ez and half Hx, at random interior nodes.
+    """
+    rng = np.random.default_rng(seed)
+    dt = courant_dt(delta, delta, delta, courant)
+    lo = np.array([pml, pml, pml])
+    hi = np.array([nx - pml, ny - pml, nz - pml])
+    mats = [Material()]
+    bricks = []
+    for b in range(n_boxes):
+        size = rng.integers(edge[0], edge[1] + 1, size=3)
+        start = np.array([rng.integers(lo[a], max(lo[a] + 1, hi[a] - 1)) for a in range(3)])
+        end = np.minimum(start + size, hi)
+        eps = float(rng.uniform(*eps_range))
+        sig = float(rng.uniform(*sigma_range))
+        mats.append(Material(eps_r=eps, sigma_e=sig))
+        bricks.append(Brick((int(start[0]), int(start[1]), int(start[2]), int(end[0]), int(end[1]), int(end[2])),
+                            len(mats) - 1))
+    sources = []
+    m = pml + src_margin
+    used = set()
+    for s in range(n_sources):
+        while True:
+            i = int(rng.integers(m, nx - m)); j = int(rng.integers(m, ny - m)); k = int(rng.integers(m, nz - m - 1))
+            if (i, j, k) not in used:
+                used.add((i, j, k))
+                break
+        delay = float(rng.uniform(0, max_delay))
+        wf = gaussian_derivative(steps, dt, fmax, delta, delay_steps=delay)
+        sources.append(LumpedSource((i, j, k, i, j, k + 1), 50.0, wf))
+    probes = []
+    pm = pml + 2
+    for p in range(n_probes):
+        comp = EZ if p < n_probes // 2 else HX
+        probes.append(Probe(comp, int(rng.integers(pm, nx - pm)), int(rng.integers(pm, ny - pm)),
+                            int(rng.integers(pm, nz - pm))))
+    return Scenario(name or f"boxes{nx}x{ny}x{nz}", nx, ny, nz, delta, delta, delta, float(dt), (pml,) * 6,
+                    steps, mats, bricks, sources, [], probes, seed=seed)
+
+
+def config_small() -> Scenario:
+    """64^3 vacuum, 10-cell CPML, centre z-edge Gaussian-derivative source, Ez probe 20 cells away,
+    1000 steps."""
+    return vacuum_cube(64, 1000, name="vacuum64")
+
+
+def config_512() -> Scenario:
+    """512^3 with 64 seeded random dielectric boxes, 4 delayed sources, 16 probes, 2000 steps."""
+    return random_boxes(512, 512, 512, 2000, seed=512, name="boxes512")
+
+
+def config_hbm() -> Scenario:
+    """1024 x 1024 x 896 single domain, same box generator (seed family of the 512^3 case, box
+    edges scaled with the domain), 1000 steps."""
+    return random_boxes(1024, 1024, 896, 1000, seed=1024, edge=(32, 256), name="boxes1024x1024x896")
+
+
+def scaled_boxes(nx: int, ny: int, nz: int, steps: int, seed: int = 7, pml: int = 6,
+                 n_boxes: int = 12, n_sources: int = 1, n_probes: int = 8, name=None) -> Scenario:
+    """A small version of the random-box workload for parity runs the oracle finishes in seconds."""
+    e0 = max(2, min(nx, ny, nz) // 8)
+    e1 = max(e0 + 1, min(nx, ny, nz) // 2)
+    return random_boxes(nx, ny, nz, steps, seed=seed, n_boxes=n_boxes, edge=(e0, e1), pml=pml,
+                        n_sources=n_sources, n_probes=n_probes, src_margin=2, max_delay=20,
+                        name=name or f"small_boxes{nx}x{ny}x{nz}")

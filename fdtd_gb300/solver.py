@@ -1,0 +1,290 @@
+"""Python host API over the C ABI of libfdtd_gb300.so (include/fdtd_api.h).
+
+This mirrors the setup-and-run sequence of the reference's marchingLoop (fdtdrav.h:3425-4387):
+materials and bricks (setBrick), lumped sources and resistors (defineSourceZ / defineResistor),
+probes (sampleField), then the time loop (solver). All compute runs in the CUDA library; there is no
+CPU fallback: constructing a Simulation without the built library or without a GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Iterable, Optional, Sequence
+
+import numpy as np
+
+from . import scenario as S
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfdtd_gb300.so")
+
+FDTD_OK = 0
+SCHEDULE_AUTO, SCHEDULE_TWO_PASS, SCHEDULE_FUSED = 0, 1, 2
+
+_i32 = ctypes.c_int32
+_i64 = ctypes.c_int64
+_f = ctypes.c_float
+_pf = ctypes.POINTER(ctypes.c_float)
+_pi32 = ctypes.POINTER(ctypes.c_int32)
+_pu8 = ctypes.POINTER(ctypes.c_uint8)
+_vp = ctypes.c_void_p
+
+
+class Grid(ctypes.Structure):
+    _fields_ = [("nx", _i32), ("ny", _i32), ("nz", _i32),
+                ("dx", _f), ("dy", _f), ("dz", _f), ("dt", _f),
+                ("eps0", _f), ("mu0", _f), ("pi", _f), ("pml", _i32 * 6)]
+
+
+class Material(ctypes.Structure):
+    _fields_ = [("eps_r", _f), ("sigma_e", _f), ("mu_r", _f), ("sigma_m", _f)]
+
+
+class FDTDError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"fdtd error {code}: {msg}")
+        self.code = code
+
+
+# Every exported symbol of include/fdtd_api.h with its ctypes signature.
+SIGNATURES = {
+    "fdtd_last_error": (ctypes.c_char_p, []),
+    "fdtd_version": (ctypes.c_char_p, []),
+    "fdtd_create": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(_vp)]),
+    "fdtd_destroy": (ctypes.c_int, [_vp]),
+    "fdtd_set_stream": (ctypes.c_int, [_vp, _vp]),
+    "fdtd_set_schedule": (ctypes.c_int, [_vp, _i32]),
+    "fdtd_set_materials": (ctypes.c_int, [_vp, ctypes.POINTER(Material), _i32]),
+    "fdtd_set_material_index": (ctypes.c_int, [_vp, _pu8]),
+    "fdtd_add_brick": (ctypes.c_int, [_vp, _pi32, _i32]),
+    "fdtd_add_lumped_source": (ctypes.c_int, [_vp, _i32, _pi32, _f, _pf, _i64, _pi32]),
+    "fdtd_add_resistor": (ctypes.c_int, [_vp, _i32, _pi32, _f]),
+    "fdtd_add_probe": (ctypes.c_int, [_vp, _i32, _i32, _i32, _i32, _pi32]),
+    "fdtd_set_probe_capacity": (ctypes.c_int, [_vp, _i64]),
+    "fdtd_prepare": (ctypes.c_int, [_vp]),
+    "fdtd_step": (ctypes.c_int, [_vp, _i64]),
+    "fdtd_synchronize": (ctypes.c_int, [_vp]),
+    "fdtd_current_step": (_i64, [_vp]),
+    "fdtd_read_probes": (ctypes.c_int, [_vp, _i64, _i64, _pf]),
+    "fdtd_probe_count": (_i32, [_vp]),
+    "fdtd_get_field": (ctypes.c_int, [_vp, _i32, _pf]),
+    "fdtd_set_field": (ctypes.c_int, [_vp, _i32, _pf]),
+    "fdtd_get_field_device": (ctypes.c_int, [_vp, _i32, _vp]),
+    "fdtd_set_field_device": (ctypes.c_int, [_vp, _i32, _vp]),
+    "fdtd_state_bytes": (_i64, [_vp]),
+    "fdtd_save_state": (ctypes.c_int, [_vp, _vp]),
+    "fdtd_load_state": (ctypes.c_int, [_vp, _vp]),
+    "fdtd_get_cpml_profile": (ctypes.c_int, [_vp, _i32, _i32, _pf]),
+    "fdtd_device_bytes": (_i64, [_vp]),
+}
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Load libfdtd_gb300.so and declare its C ABI. Raises if the library was not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with `python -m fdtd_gb300.build` "
+                           "(the solver has no CPU fallback)")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(rc: int) -> None:
+    if rc != FDTD_OK:
+        raise FDTDError(rc, _lib.fdtd_last_error().decode())
+
+
+def _box(box: Sequence[int]):
+    return (_i32 * 6)(*[int(v) for v in box])
+
+
+class Simulation:
+    """One simulation handle on the current CUDA device."""
+
+    def __init__(self, nx: int, ny: int, nz: int, dx: float, dy: float, dz: float, dt: float,
+                 pml: Sequence[int] = (10,) * 6, eps0: float = float(S.REF_EPS0), mu0: float = float(S.REF_MU0),
+                 pi: float = float(S.REF_PI), schedule: int = SCHEDULE_AUTO):
+        lib = load_library()
+        g = Grid()
+        g.nx, g.ny, g.nz = nx, ny, nz
+        g.dx, g.dy, g.dz, g.dt = dx, dy, dz, dt
+        g.eps0, g.mu0, g.pi = eps0, mu0, pi
+        for q in range(6):
+            g.pml[q] = int(pml[q])
+        h = _vp()
+        _check(lib.fdtd_create(ctypes.byref(g), ctypes.byref(h)))
+        self._h = h
+        self.shape = (nz, ny, nx)
+        self.n_probes = 0
+        if schedule != SCHEDULE_AUTO:
+            _check(lib.fdtd_set_schedule(self._h, schedule))
+
+    # -- lifetime -------------------------------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _lib.fdtd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- setup ----------------------------------------------------------------------------------
+    def set_stream(self, stream_ptr: int) -> None:
+        _check(_lib.fdtd_set_stream(self._h, _vp(stream_ptr)))
+
+    def set_schedule(self, schedule: int) -> None:
+        _check(_lib.fdtd_set_schedule(self._h, schedule))
+
+    def set_materials(self, table: np.ndarray) -> None:
+        t = np.asarray(table, dtype=np.float32).reshape(-1, 4)
+        arr = (Material * len(t))(*[Material(*row) for row in t.tolist()])
+        _check(_lib.fdtd_set_materials(self._h, arr, len(t)))
+
+    def set_material_index(self, cells: np.ndarray) -> None:
+        c = np.ascontiguousarray(cells, dtype=np.uint8)
+        if c.shape != self.shape:
+            raise ValueError(f"material index must have shape {self.shape}")
+        _check(_lib.fdtd_set_material_index(self._h, c.ctypes.data_as(_pu8)))
+
+    def add_brick(self, box: Sequence[int], material: int) -> None:
+        _check(_lib.fdtd_add_brick(self._h, _box(box), material))
+
+    def add_source(self, box: Sequence[int], resistance: float, voltage: np.ndarray, axis: int = 2) -> int:
+        v = np.ascontiguousarray(voltage, dtype=np.float32)
+        out = _i32()
+        _check(_lib.fdtd_add_lumped_source(self._h, axis, _box(box), resistance, v.ctypes.data_as(_pf), v.size,
+                                           ctypes.byref(out)))
+        return out.value
+
+    def add_resistor(self, box: Sequence[int], resistance: float, axis: int = 2) -> None:
+        _check(_lib.fdtd_add_resistor(self._h, axis, _box(box), resistance))
+
+    def add_probe(self, component: int, i: int, j: int, k: int) -> int:
+        out = _i32()
+        _check(_lib.fdtd_add_probe(self._h, component, i, j, k, ctypes.byref(out)))
+        self.n_probes = out.value + 1
+        return out.value
+
+    def set_probe_capacity(self, steps: int) -> None:
+        _check(_lib.fdtd_set_probe_capacity(self._h, steps))
+
+    def prepare(self) -> None:
+        _check(_lib.fdtd_prepare(self._h))
+
+    # -- run ------------------------------------------------------------------------------------
+    def step(self, n: int = 1) -> None:
+        _check(_lib.fdtd_step(self._h, n))
+
+    def synchronize(self) -> None:
+        _check(_lib.fdtd_synchronize(self._h))
+
+    @property
+    def current_step(self) -> int:
+        return _lib.fdtd_current_step(self._h)
+
+    def read_probes(self, first: int = 0, n: Optional[int] = None) -> np.ndarray:
+        n = self.current_step - first if n is None else n
+        out = np.zeros((n, max(self.n_probes, 1)), dtype=np.float32)
+        _check(_lib.fdtd_read_probes(self._h, first, n, out.ctypes.data_as(_pf)))
+        return out[:, :self.n_probes]
+
+    def get_field(self, component: int) -> np.ndarray:
+        out = np.empty(self.shape, dtype=np.float32)
+        _check(_lib.fdtd_get_field(self._h, component, out.ctypes.data_as(_pf)))
+        return out
+
+    def set_field(self, component: int, values: np.ndarray) -> None:
+        v = np.ascontiguousarray(values, dtype=np.float32).reshape(self.shape)
+        _check(_lib.fdtd_set_field(self._h, component, v.ctypes.data_as(_pf)))
+
+    def fields(self) -> np.ndarray:
+        return np.stack([self.get_field(c) for c in range(6)])
+
+    def get_field_device(self, component: int, dev_ptr: int) -> None:
+        _check(_lib.fdtd_get_field_device(self._h, component, _vp(dev_ptr)))
+
+    def set_field_device(self, component: int, dev_ptr: int) -> None:
+        _check(_lib.fdtd_set_field_device(self._h, component, _vp(dev_ptr)))
+
+    def state_bytes(self) -> int:
+        return _lib.fdtd_state_bytes(self._h)
+
+    def save_state(self, dev_ptr: int) -> None:
+        _check(_lib.fdtd_save_state(self._h, _vp(dev_ptr)))
+
+    def load_state(self, dev_ptr: int) -> None:
+        _check(_lib.fdtd_load_state(self._h, _vp(dev_ptr)))
+
+    def cpml_profile(self, axis: int, kind: int) -> np.ndarray:
+        """1-D CPML profile: kind 0 b_e, 1 a_e, 2 b_m, 3 a_m, 4 kappa_e, 5 kappa_m."""
+        n = (self.shape[2], self.shape[1], self.shape[0])[axis]
+        out = np.empty(n, dtype=np.float32)
+        _check(_lib.fdtd_get_cpml_profile(self._h, axis, kind, out.ctypes.data_as(_pf)))
+        return out
+
+    def cpml_profiles(self) -> dict:
+        """All 18 profiles keyed like the oracle's override names (b_ex, a_ex, b_mx, a_mx, k_ex, k_mx, ...)."""
+        out = {}
+        for a, ax in enumerate("xyz"):
+            for kind, nm in enumerate(("b_e", "a_e", "b_m", "a_m", "k_e", "k_m")):
+                out[nm + ax] = self.cpml_profile(a, kind)
+        return out
+
+    def device_bytes(self) -> int:
+        return _lib.fdtd_device_bytes(self._h)
+
+    # -- scenarios ------------------------------------------------------------------------------
+    @classmethod
+    def from_scenario(cls, sc: "S.Scenario", schedule: int = SCHEDULE_AUTO, material_index: Optional[np.ndarray] = None,
+                      probe_capacity: Optional[int] = None) -> "Simulation":
+        """Build a simulation from a scenario in the reference's setup order (fdtdrav.h:4104-4310)."""
+        sim = cls(sc.nx, sc.ny, sc.nz, sc.dx, sc.dy, sc.dz, sc.dt, sc.pml, sc.eps0, sc.mu0, sc.pi, schedule)
+        sim.set_materials(sc.material_table())
+        if material_index is not None:
+            sim.set_material_index(material_index)
+        else:
+            for b in sc.bricks:
+                sim.add_brick(b.box, b.material)
+        for s in sc.sources:
+            sim.add_source(s.box, s.resistance, s.waveform)
+        for r in sc.resistors:
+            sim.add_resistor(r.box, r.resistance)
+        for p in sc.probes:
+            sim.add_probe(p.component, p.i, p.j, p.k)
+        if probe_capacity is not None:
+            sim.set_probe_capacity(probe_capacity)
+        return sim
+
+
+def run_scenario(sc: "S.Scenario", steps: Optional[int] = None, schedule: int = SCHEDULE_AUTO,
+                 fields: bool = True):
+    """Run a scenario on the GPU; returns (probes (steps, n_probes), fields (6, nz, ny, nx) or None)."""
+    steps = sc.steps if steps is None else steps
+    with Simulation.from_scenario(sc, schedule, probe_capacity=max(steps, 1)) as sim:
+        sim.step(steps)
+        sim.synchronize()
+        p = sim.read_probes(0, steps)
+        f = sim.fields() if fields else None
+    return p, f

@@ -1,0 +1,149 @@
+/* fdtd_api.h - C ABI of the GB300-native 3D FDTD solver (libfdtd_gb300.so).
+ *
+ * A single-domain, single-GPU replacement for the Yee time step of ravelec/FDTD and for the host
+ * setup that feeds it. The reference has no plugin layer: its "API" is the host functions and
+ * kernels of fdtdrav.h driven by marchingLoop (fdtdrav.h:3425-4387). Each entry point below names
+ * the reference code it replaces.
+ *
+ * Conventions
+ *  - Nodes are indexed (i, j, k), 0 <= i < nx, x fastest, exactly as the reference's
+ *    idx = i + j*NX + k*NX*NY (fdtdrav.h:278); nx, ny, nz are the reference's NXX, NYY, NZ.
+ *  - Host arrays are dense (nz, ny, nx) float32 / uint8, x fastest; the library pads rows itself.
+ *  - All state is FP32. Every call returns FDTD_OK (0) or an error code and never exits the
+ *    process; fdtd_last_error() returns the message of the calling thread's last failure.
+ *  - One handle may be used by one host thread at a time; handles share no state.
+ */
+#ifndef FDTD_API_H
+#define FDTD_API_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FDTD_OK 0
+#define FDTD_ERR_INVALID 1   /* bad argument or configuration (checked on the host)          */
+#define FDTD_ERR_CUDA 2      /* a CUDA runtime call failed                                   */
+#define FDTD_ERR_OOM 3       /* device allocation failed                                     */
+#define FDTD_ERR_STATE 4     /* call not allowed in the handle's current state               */
+#define FDTD_ERR_RANGE 5     /* requested data outside what the handle holds                 */
+#define FDTD_ERR_DEVICE 6    /* a kernel reported an error through its device status word     */
+
+/* Field components. */
+enum { FDTD_EX = 0, FDTD_EY = 1, FDTD_EZ = 2, FDTD_HX = 3, FDTD_HY = 4, FDTD_HZ = 5 };
+
+/* Update-kernel schedules (fdtd_set_schedule). */
+enum {
+    FDTD_SCHEDULE_AUTO = 0,   /* fused sweep when the grid allows it, otherwise two passes   */
+    FDTD_SCHEDULE_TWO_PASS = 1, /* E pass then H pass per step, in place (the reference's order) */
+    FDTD_SCHEDULE_FUSED = 2   /* one z-marching sweep per step over ping-pong field buffers   */
+};
+
+typedef struct fdtd_handle fdtd_handle;
+
+/* Grid and constants. Replaces the scalar parameters of marchingLoop (fdtdrav.h:3425-3430) after
+ * its sizing (fdtdrav.h:3485-3498): nx/ny/nz are node counts including air buffer and CPML. */
+typedef struct {
+    int32_t nx, ny, nz;
+    float dx, dy, dz, dt;
+    float eps0, mu0, pi;     /* the reference passes these as floats (source.cu:30-33)      */
+    int32_t pml[6];          /* CPML cells per face: x_n, x_p, y_n, y_p, z_n, z_p           */
+} fdtd_grid;
+
+/* One material: relative permittivity, electric conductivity (S/m), relative permeability,
+ * magnetic conductivity. Replaces the per-brick scalars of setBrick (fdtdrav.h:1524-1571).
+ * The background (material 0 by default) is eps_r = mu_r = 1, sigma = 1.2e-38 (setZero). */
+typedef struct {
+    float eps_r, sigma_e, mu_r, sigma_m;
+} fdtd_material;
+
+const char* fdtd_last_error(void);
+const char* fdtd_version(void);
+
+/* Allocate a simulation on the current CUDA device: fields set to 1.2e-38 (setZero,
+ * fdtdrav.h:919-1094), material 0 everywhere. Replaces the allocation and initialisation part of
+ * marchingLoop (fdtdrav.h:3874-4086). Validates the grid (CPML faces may not overlap). */
+int fdtd_create(const fdtd_grid* grid, fdtd_handle** out);
+/* Free everything the handle owns (the reference frees nothing, fdtdrav.h:4384). */
+int fdtd_destroy(fdtd_handle* h);
+
+/* Run all device work of this handle on a caller stream (a cudaStream_t); NULL = legacy stream. */
+int fdtd_set_stream(fdtd_handle* h, void* cuda_stream);
+int fdtd_set_schedule(fdtd_handle* h, int32_t schedule);
+
+/* Material table (at most 256 entries). Replaces the per-brick material scalars that setBrick
+ * paints into 12 per-cell arrays (fdtdrav.h:1524-1571). */
+int fdtd_set_materials(fdtd_handle* h, const fdtd_material* table, int32_t n);
+/* Per-cell material index, host array of nz*ny*nx bytes. Replaces the painted per-cell
+ * material arrays; edge averaging (setSigmaEpsSigmaMu, fdtdrav.h:1097-1220) is done on the fly. */
+int fdtd_set_material_index(fdtd_handle* h, const uint8_t* cells);
+/* Paint cells [is,ie) x [js,je) x [ks,ke) with a material, last call wins (setBrick,
+ * fdtdrav.h:1524-1571, called in order at fdtdrav.h:4104-4128). box = {is,js,ks,ie,je,ke}. */
+int fdtd_add_brick(fdtd_handle* h, const int32_t box[6], int32_t material);
+
+/* Lumped voltage source with internal resistance on the edges i in [is,ie], j in [js,je],
+ * k in [ks,ke) (axis 2 = z, the only orientation the reference implements correctly).
+ * voltage[m] is the source voltage at step m; each edge is driven with voltage[m]/(ke-ks)
+ * (fdtdrav.h:1494, 3613). Replaces defineSourceZ (fdtdrav.h:1368-1426), setGauss/setSine
+ * (fdtdrav.h:1486-1520) and the injection in calc_e (fdtdrav.h:726-733). Several sources may
+ * be added; their edges may not overlap. Steps past n_samples inject zero. */
+int fdtd_add_lumped_source(fdtd_handle* h, int32_t axis, const int32_t box[6], float resistance,
+                           const float* voltage, int64_t n_samples, int32_t* id_out);
+/* Lumped resistor on the same kind of edge box (defineResistor, fdtdrav.h:1429-1483). */
+int fdtd_add_resistor(fdtd_handle* h, int32_t axis, const int32_t box[6], float resistance);
+
+/* Point probe of one field component at node (i,j,k): records, every step, the value right after
+ * the component's main update and before its CPML correction, as sampleField does
+ * (fdtdrav.h:234-246, called at 347, 372, 391, 740). Returns the probe's column in
+ * fdtd_read_probes output. */
+int fdtd_add_probe(fdtd_handle* h, int32_t component, int32_t i, int32_t j, int32_t k, int32_t* id_out);
+/* Number of steps the device probe ring buffer keeps (default 4096). */
+int fdtd_set_probe_capacity(fdtd_handle* h, int64_t steps);
+
+/* Build the device tables (CPML profiles, per-material coefficients, lumped-edge coefficients):
+ * replaces setCoefficients, setABCPML, defineSourceZ and defineResistor (fdtdrav.h:1223-1308,
+ * 1747-2160, 1368-1483). Called implicitly by the first fdtd_step. */
+int fdtd_prepare(fdtd_handle* h);
+
+/* Advance n time steps: per step the E update (with source injection) then the H update, with
+ * the CPML corrections and probe sampling fused in. Replaces the time loop of marchingLoop
+ * (fdtdrav.h:4320-4355) and solver (fdtdrav.h:3188-3422). Stream-ordered, does not synchronise. */
+int fdtd_step(fdtd_handle* h, int64_t n);
+int fdtd_synchronize(fdtd_handle* h);
+int64_t fdtd_current_step(const fdtd_handle* h);
+
+/* Probe values of steps [first_step, first_step+n_steps) into out[n_steps][n_probes]
+ * (host memory). FDTD_ERR_RANGE if some of those steps left the ring buffer. */
+int fdtd_read_probes(fdtd_handle* h, int64_t first_step, int64_t n_steps, float* out);
+int32_t fdtd_probe_count(const fdtd_handle* h);
+
+/* Whole-field copies between the simulation and host memory (nz*ny*nx floats) or device memory
+ * (dense nz*ny*nx floats, caller-owned). */
+int fdtd_get_field(fdtd_handle* h, int32_t component, float* host_out);
+int fdtd_set_field(fdtd_handle* h, int32_t component, const float* host_in);
+int fdtd_get_field_device(fdtd_handle* h, int32_t component, float* dev_out);
+int fdtd_set_field_device(fdtd_handle* h, int32_t component, const float* dev_in);
+
+/* Checkpoint / resume of the full dynamic state (fields, CPML memory, step counter). The
+ * reference has none. fdtd_state_bytes gives the size of the device buffer fdtd_save_state
+ * writes (device memory, caller-owned). */
+int64_t fdtd_state_bytes(const fdtd_handle* h);
+int fdtd_save_state(fdtd_handle* h, void* dev_buf);
+int fdtd_load_state(fdtd_handle* h, const void* dev_buf);
+
+/* One 1-D CPML profile of an axis (0 = x, 1 = y, 2 = z) into host memory (n_axis floats):
+ * kind 0 = b_e, 1 = a_e, 2 = b_m, 3 = a_m, 4 = kappa_e, 5 = kappa_m. These are the d_cpml_b/a
+ * arrays and the kappa values that setABCPML computes (fdtdrav.h:1863-1906); nodes outside the
+ * CPML hold b = a = 1.2e-38 and kappa = 1. Builds the tables if needed. */
+int fdtd_get_cpml_profile(fdtd_handle* h, int32_t axis, int32_t kind, float* host_out);
+
+/* Bytes of device memory the handle holds. */
+int64_t fdtd_device_bytes(const fdtd_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FDTD_API_H */

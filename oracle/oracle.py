@@ -1,0 +1,163 @@
+"""ctypes wrapper of the CPU oracle (oracle/fdtd_oracle.cpp). TEST INFRASTRUCTURE ONLY.
+
+The oracle restates the reference's setup and calc_e / calc_h on the CPU (FP32 with the
+reference's rounding sequence, and FP64 as the error reference). Only tests, smoke() and the
+benchmark's CPU-baseline leg may use it, always as the checker or the timed CPU baseline.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from typing import Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD_DIR, "libfdtd_oracle.so")
+SRC = os.path.join(HERE, "fdtd_oracle.cpp")
+
+_i = ctypes.c_int
+_f = ctypes.c_float
+_pi = ctypes.POINTER(ctypes.c_int)
+_pf = ctypes.POINTER(ctypes.c_float)
+_pd = ctypes.POINTER(ctypes.c_double)
+_pu8 = ctypes.POINTER(ctypes.c_uint8)
+
+# Override slots: per axis b_e, a_e, b_m, a_m, kappa_e, kappa_m.
+OVERRIDE_NAMES = ["b_ex", "a_ex", "b_mx", "a_mx", "k_ex", "k_mx", "b_ey", "a_ey", "b_my", "a_my", "k_ey", "k_my",
+                  "b_ez", "a_ez", "b_mz", "a_mz", "k_ez", "k_mz"]
+# 1-D arrays the reference keeps (its kappa values are locals of setABCPML).
+PROFILE_NAMES = ["b_ex", "a_ex", "b_mx", "a_mx", "b_ey", "a_ey", "b_my", "a_my", "b_ez", "a_ez", "b_mz", "a_mz"]
+
+
+class _Scenario(ctypes.Structure):
+    _fields_ = [("nx", _i), ("ny", _i), ("nz", _i), ("pml", _i * 6),
+                ("dx", _f), ("dy", _f), ("dz", _f), ("dt", _f), ("eps0", _f), ("mu0", _f), ("pi", _f),
+                ("mat", _pu8), ("table", _pf), ("n_mat", _i),
+                ("nsrc", _i), ("src_box", _pi), ("src_r", _pf),
+                ("nres", _i), ("res_box", _pi), ("res_r", _pf),
+                ("nprobe", _i), ("probe", _pi),
+                ("profile_override", ctypes.POINTER(_pf))]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with g++ (no contraction: the FMA sequence is written out in the source)."""
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
+        subprocess.check_call(["g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-shared", "-fPIC",
+                               "-o", LIB, SRC])
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        L.or_error.restype = ctypes.c_char_p
+        L.or_run_f32.argtypes = [ctypes.POINTER(_Scenario), _i, _pf, _i, _pf, _pf, _pf, _i]
+        L.or_run_f64.argtypes = [ctypes.POINTER(_Scenario), _i, _pf, _i, _pf, _pd, _pd, _i]
+        L.or_onestep_f32.argtypes = [ctypes.POINTER(_Scenario), _i, _pf, _i, _pf, _pf]
+        L.or_coef_f32.argtypes = [ctypes.POINTER(_Scenario), ctypes.c_char_p, _pf]
+        _lib = L
+    return _lib
+
+
+class _Prepared:
+    def __init__(self, sc, profile_override: Optional[dict] = None, probes: Optional[Sequence] = None):
+        self.keep = []
+        s = _Scenario()
+        s.nx, s.ny, s.nz = sc.nx, sc.ny, sc.nz
+        for q in range(6):
+            s.pml[q] = sc.pml[q]
+        s.dx, s.dy, s.dz, s.dt = sc.dx, sc.dy, sc.dz, sc.dt
+        s.eps0, s.mu0, s.pi = sc.eps0, sc.mu0, sc.pi
+        mat = np.ascontiguousarray(sc.material_index())
+        tab = np.ascontiguousarray(sc.material_table())
+        sb = np.array([x.box for x in sc.sources], dtype=np.int32).reshape(-1, 6)
+        sr = np.array([x.resistance for x in sc.sources], dtype=np.float32)
+        rb = np.array([x.box for x in sc.resistors], dtype=np.int32).reshape(-1, 6)
+        rr = np.array([x.resistance for x in sc.resistors], dtype=np.float32)
+        probes = sc.probes if probes is None else probes
+        pr = np.array([[p.component, p.i, p.j, p.k] for p in probes], dtype=np.int32).reshape(-1, 4)
+        self.keep += [mat, tab, sb, sr, rb, rr, pr]
+        s.mat, s.table, s.n_mat = mat.ctypes.data_as(_pu8), tab.ctypes.data_as(_pf), tab.shape[0]
+        s.nsrc, s.src_box, s.src_r = len(sc.sources), sb.ctypes.data_as(_pi), sr.ctypes.data_as(_pf)
+        s.nres, s.res_box, s.res_r = len(sc.resistors), rb.ctypes.data_as(_pi), rr.ctypes.data_as(_pf)
+        s.nprobe, s.probe = len(probes), pr.ctypes.data_as(_pi)
+        if profile_override:
+            arr = (_pf * 18)()
+            for q, n in enumerate(OVERRIDE_NAMES):
+                if n in profile_override:
+                    a = np.ascontiguousarray(profile_override[n], dtype=np.float32)
+                    self.keep.append(a)
+                    arr[q] = a.ctypes.data_as(_pf)
+                else:
+                    arr[q] = None
+            self.keep.append(arr)
+            s.profile_override = ctypes.cast(arr, ctypes.POINTER(_pf))
+        else:
+            s.profile_override = None
+        steps = max(sc.steps, 1)
+        sig = np.zeros((max(len(sc.sources), 1), steps), dtype=np.float32)
+        for q in range(len(sc.sources)):
+            v = sc.signal_per_node(q)[:steps]
+            sig[q, :v.size] = v
+        self.sig = np.ascontiguousarray(sig)
+        self.n_sig = steps
+        self.s = s
+        self.n_probes = len(probes)
+
+
+def run(sc, steps: Optional[int] = None, precision: str = "f32", init_fields: Optional[np.ndarray] = None,
+        profile_override: Optional[dict] = None, threads: int = 0, probes: Optional[Sequence] = None):
+    """Run the oracle. Returns (probes (steps, n_probes), fields (6, nz, ny, nx))."""
+    steps = sc.steps if steps is None else steps
+    p = _Prepared(sc, profile_override, probes)
+    dt = np.float32 if precision == "f32" else np.float64
+    pout = np.zeros((steps, max(p.n_probes, 1)), dtype=dt)
+    fout = np.zeros((6, sc.nz, sc.ny, sc.nx), dtype=dt)
+    init = None
+    if init_fields is not None:
+        init = np.ascontiguousarray(init_fields, dtype=np.float32)
+    L = lib()
+    fn = L.or_run_f32 if precision == "f32" else L.or_run_f64
+    ptr = _pf if precision == "f32" else _pd
+    rc = fn(ctypes.byref(p.s), steps, p.sig.ctypes.data_as(_pf), p.n_sig,
+            None if init is None else init.ctypes.data_as(_pf),
+            pout.ctypes.data_as(ptr), fout.ctypes.data_as(ptr), threads)
+    if rc != 0:
+        raise RuntimeError("oracle: " + L.or_error().decode())
+    return pout[:, :p.n_probes], fout
+
+
+def onestep(sc, m: int, init_fields: np.ndarray, profile_override: Optional[dict] = None) -> np.ndarray:
+    """One calc_e then one calc_h from ``init_fields`` (6, nz, ny, nx); returns the 6 fields after."""
+    p = _Prepared(sc, profile_override)
+    init = np.ascontiguousarray(init_fields, dtype=np.float32)
+    out = np.zeros((6, sc.nz, sc.ny, sc.nx), dtype=np.float32)
+    L = lib()
+    rc = L.or_onestep_f32(ctypes.byref(p.s), m, p.sig.ctypes.data_as(_pf), p.n_sig, init.ctypes.data_as(_pf),
+                          out.ctypes.data_as(_pf))
+    if rc != 0:
+        raise RuntimeError("oracle: " + L.or_error().decode())
+    return out
+
+
+def coef(sc, name: str, profile_override: Optional[dict] = None) -> np.ndarray:
+    """A per-edge coefficient array (reference naming) after the oracle's setup."""
+    p = _Prepared(sc, profile_override)
+    n_line = {"x": sc.nx, "y": sc.ny, "z": sc.nz}
+    if name in PROFILE_NAMES:
+        out = np.zeros(n_line[name[-1]], dtype=np.float32)
+    else:
+        out = np.zeros((sc.nz, sc.ny, sc.nx), dtype=np.float32)
+    L = lib()
+    if L.or_coef_f32(ctypes.byref(p.s), name.encode(), out.ctypes.data_as(_pf)) != 0:
+        raise RuntimeError("oracle: " + L.or_error().decode())
+    return out

@@ -1,0 +1,490 @@
+// Host-side runner for the reference kernels (test infrastructure only; never part of the product).
+//
+// Loads the cubin built from the reference's fdtdrav.h (see ref_kernels.cu and oracle/build_ref.sh),
+// allocates the reference's 84 per-cell arrays plus its 1-D CPML arrays and ghost planes for a
+// single slab (NUMDEV = 1, gpu_offset = 0), and drives the reference's setup kernels in the order
+// of marchingLoop (fdtdrav.h:4047-4310) followed by calc_e then calc_h per step (solver,
+// fdtdrav.h:3222-3333). Launch shapes follow fdtdrav.h:3714-3720: block (16,16,4), NX and NY padded
+// to multiples of 16 (fdtdrav.h:3493-3494).
+//
+// Differences from marchingLoop, all on the host side:
+//  * the scenario comes in as index-space boxes instead of metres (the metre->index mapping,
+//    calc_index fdtdrav.h:198-206, is restated in fdtd_gb300/scenario.py);
+//  * sizes are computed in size_t (the reference computes byte counts in float, fdtdrav.h:3700);
+//  * several lumped sources may be defined (defineSourceZ once per box); calc_e injects only the
+//    one whose box is passed to it, so multi-source runs are done once per source and summed;
+//  * the per-node source signal is supplied by the caller instead of setGauss/setSine;
+//  * the reference's own sample boxes are placed outside the grid and a gather kernel of ours
+//    records probe values after every step.
+// Every error is returned as a status code with a message; nothing exits the process.
+
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <string>
+#include <vector>
+#include <map>
+#include <algorithm>
+
+namespace {
+
+std::string g_err;
+cudaLibrary_t g_lib = nullptr;
+
+struct Kern { const char* name; cudaKernel_t k; };
+enum { K_SETZERO, K_SETBRICK, K_SETSIGMA, K_SETCOEF, K_SETABCPML, K_SRCZ, K_RES, K_CALCE, K_CALCH, K_GATHER, K_COUNT };
+Kern g_k[K_COUNT] = {
+    {"_Z7setZero", nullptr}, {"_Z8setBrick", nullptr}, {"_Z18setSigmaEpsSigmaMu", nullptr},
+    {"_Z15setCoefficients", nullptr}, {"_Z9setABCPML", nullptr}, {"_Z13defineSourceZ", nullptr},
+    {"_Z14defineResistor", nullptr}, {"_Z6calc_e", nullptr}, {"_Z6calc_h", nullptr},
+    {"harness_gather", nullptr}};
+
+// Itanium-ABI names of the reference kernels: the parameter lists of fdtdrav.h reduce to runs of
+// int (i), float (f) and float* (Pf, then the substitution S_).
+std::string mangled(const char* prefix, const char* spec) {
+    // spec: sequence of <count><code>, code in {i, f, p}; the first p emits Pf, the rest S_.
+    std::string out(prefix);
+    bool seen_p = false;
+    const char* s = spec;
+    while (*s) {
+        int n = 0;
+        while (*s >= '0' && *s <= '9') n = n * 10 + (*s++ - '0');
+        char c = *s++;
+        for (int r = 0; r < n; ++r) {
+            if (c == 'i') out += "i";
+            else if (c == 'f') out += "f";
+            else { out += seen_p ? "S_" : "Pf"; seen_p = true; }
+        }
+    }
+    return out;
+}
+
+struct Dims { int NX, NXX, NY, NYY, NZ, NZ_N; int pml[6]; float dx, dy, dz, dt, eps0, pi, mu0; };
+Dims g_d;
+bool g_ready = false;
+
+// All reference arrays by name. Volume arrays hold NX*NY*NZ floats, 1-D CPML arrays hold
+// max(NX, NY, NZ) floats, ghost planes NX*NY floats.
+std::map<std::string, float*> g_arr;
+std::vector<std::string> g_order;
+size_t g_vol = 0, g_line = 0, g_plane = 0;
+float* g_gather_fields = nullptr;  // device array of 6 pointers (float**)
+float* g_probe_dev = nullptr;
+int* g_probe_comp_dev = nullptr;
+long long* g_probe_idx_dev = nullptr;
+float* g_signal_dev = nullptr;
+size_t g_signal_cap = 0;
+int g_probe_cap = 0;
+
+std::vector<std::vector<int>> g_src_box;
+
+const char* kVolumeNames[] = {
+    "Ex", "Jx", "Cexe", "Cexhz", "Cexhy", "Cexj", "eps_r_x", "sigma_e_x",
+    "Ey", "Jy", "Ceye", "Ceyhx", "Ceyhz", "Ceyj", "eps_r_y", "sigma_e_y",
+    "Ez", "Jz", "Ceze", "Cezhy", "Cezhx", "Cezj", "eps_r_z", "sigma_e_z",
+    "Hx", "Mx", "Chxh", "Chxey", "Chxez", "Chxm", "mu_r_x", "sigma_m_x",
+    "Hy", "My", "Chyh", "Chyez", "Chyex", "Chym", "mu_r_y", "sigma_m_y",
+    "Hz", "Mz", "Chzh", "Chzex", "Chzey", "Chzm", "mu_r_z", "sigma_m_z",
+    "mat_eps_x", "mat_eps_y", "mat_eps_z", "mat_sigma_e_x", "mat_sigma_e_y", "mat_sigma_e_z",
+    "mat_mu_x", "mat_mu_y", "mat_mu_z", "mat_sigma_m_x", "mat_sigma_m_y", "mat_sigma_m_z",
+    "Psi_eyx", "Psi_ezx", "Psi_hyx", "Psi_hzx", "cpsi_eyx", "cpsi_ezx", "cpsi_hyx", "cpsi_hzx",
+    "Psi_exy", "Psi_ezy", "Psi_hxy", "Psi_hzy", "cpsi_exy", "cpsi_ezy", "cpsi_hxy", "cpsi_hzy",
+    "Psi_exz", "Psi_eyz", "Psi_hxz", "Psi_hyz", "cpsi_exz", "cpsi_eyz", "cpsi_hxz", "cpsi_hyz"};
+const char* kLineNames[] = {"cpml_b_ex", "cpml_a_ex", "cpml_b_mx", "cpml_a_mx",
+                            "cpml_b_ey", "cpml_a_ey", "cpml_b_my", "cpml_a_my",
+                            "cpml_b_ez", "cpml_a_ez", "cpml_b_mz", "cpml_a_mz"};
+const char* kPlaneNames[] = {"gEx", "gEy", "gHx", "gHy"};
+const char* kSampleNames[] = {"sampE", "sampHx", "sampHy", "sampHz"};
+
+float* A(const char* n) { return g_arr.at(n); }
+
+bool ck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) {
+        g_err = std::string(what) + ": " + cudaGetErrorString(e);
+        return false;
+    }
+    return true;
+}
+
+dim3 grid3d() { return dim3(g_d.NX / 16, g_d.NY / 16, (g_d.NZ_N + 3) / 4); }
+dim3 block3d() { return dim3(16, 16, 4); }
+
+bool launch(int kid, dim3 g, dim3 b, std::vector<void*>& args) {
+    cudaError_t e = cudaLaunchKernel((const void*)g_k[kid].k, g, b, args.data(), 0, 0);
+    return ck(e, g_k[kid].name);
+}
+
+void free_all() {
+    for (auto& kv : g_arr) cudaFree(kv.second);
+    g_arr.clear();
+    g_order.clear();
+    if (g_gather_fields) cudaFree(g_gather_fields);
+    if (g_probe_dev) cudaFree(g_probe_dev);
+    if (g_probe_comp_dev) cudaFree(g_probe_comp_dev);
+    if (g_probe_idx_dev) cudaFree(g_probe_idx_dev);
+    if (g_signal_dev) cudaFree(g_signal_dev);
+    g_gather_fields = nullptr; g_probe_dev = nullptr; g_probe_comp_dev = nullptr;
+    g_probe_idx_dev = nullptr; g_signal_dev = nullptr; g_signal_cap = 0; g_probe_cap = 0;
+    g_ready = false;
+}
+
+}  // namespace
+
+extern "C" {
+
+typedef struct {
+    int nxx, nyy, nz;
+    int pml[6];  // x_n, x_p, y_n, y_p, z_n, z_p
+    float dx, dy, dz, dt, eps0, pi, mu0;
+    int nbricks; const int* brick_box; const float* brick_mat;  // box is,js,ks,ie,je,ke; eps_r, sigma_e, mu_r, sigma_m
+    int nsources; const int* src_box; const float* src_r;       // box is,js,ks,ie,je,ke
+    int nres; const int* res_box; const float* res_r;
+} rh_scenario;
+
+const char* rh_error(void) { return g_err.c_str(); }
+
+int rh_load(const char* cubin_path) {
+    if (g_lib) return 0;
+    if (!ck(cudaLibraryLoadFromFile(&g_lib, cubin_path, nullptr, nullptr, 0, nullptr, nullptr, 0),
+            "cudaLibraryLoadFromFile")) return -1;
+    const char* specs[K_COUNT] = {
+        "96p3i",                       // setZero
+        "5i12p6i12f",                  // setBrick
+        "5i24p",                       // setSigmaEpsSigmaMu
+        "7i36p7f",                     // setCoefficients
+        "7i36p13f",                    // setABCPML
+        "13i6p6f",                     // defineSourceZ
+        "14i5p6f",                     // defineResistor
+        "14i57p16i1p",                 // calc_e
+        "13i56p10i3p",                 // calc_h
+        nullptr};
+    for (int k = 0; k < K_COUNT; ++k) {
+        std::string nm = specs[k] ? mangled(g_k[k].name, specs[k]) : std::string(g_k[k].name);
+        if (!ck(cudaLibraryGetKernel(&g_k[k].k, g_lib, nm.c_str()), nm.c_str())) return -1;
+    }
+    return 0;
+}
+
+int rh_setup(const rh_scenario* s) {
+    if (!g_lib) { g_err = "rh_load not called"; return -1; }
+    free_all();
+    Dims d;
+    d.NXX = s->nxx; d.NYY = s->nyy; d.NZ = s->nz;
+    d.NX = (d.NXX % 16 == 0) ? d.NXX : (d.NXX / 16 + 1) * 16;
+    d.NY = (d.NYY % 16 == 0) ? d.NYY : (d.NYY / 16 + 1) * 16;
+    d.NZ_N = d.NZ;
+    for (int q = 0; q < 6; ++q) d.pml[q] = s->pml[q];
+    d.dx = s->dx; d.dy = s->dy; d.dz = s->dz; d.dt = s->dt; d.eps0 = s->eps0; d.pi = s->pi; d.mu0 = s->mu0;
+    g_d = d;
+    g_vol = (size_t)d.NX * d.NY * d.NZ;
+    g_line = (size_t)std::max(d.NX, std::max(d.NY, d.NZ));
+    g_plane = (size_t)d.NX * d.NY;
+    for (const char* n : kVolumeNames) {
+        float* p = nullptr;
+        if (!ck(cudaMalloc(&p, g_vol * sizeof(float)), "cudaMalloc volume")) { free_all(); return -1; }
+        g_arr[n] = p; g_order.push_back(n);
+    }
+    for (const char* n : kLineNames) {
+        float* p = nullptr;
+        if (!ck(cudaMalloc(&p, g_line * sizeof(float)), "cudaMalloc line")) { free_all(); return -1; }
+        g_arr[n] = p; g_order.push_back(n);
+    }
+    for (const char* n : kPlaneNames) {
+        float* p = nullptr;
+        if (!ck(cudaMalloc(&p, g_plane * sizeof(float)), "cudaMalloc plane")) { free_all(); return -1; }
+        cudaMemset(p, 0, g_plane * sizeof(float));
+        g_arr[n] = p; g_order.push_back(n);
+    }
+    for (const char* n : kSampleNames) {  // never written: the sample boxes lie outside the grid
+        float* p = nullptr;
+        if (!ck(cudaMalloc(&p, 64 * sizeof(float)), "cudaMalloc sample")) { free_all(); return -1; }
+        g_arr[n] = p; g_order.push_back(n);
+    }
+    {
+        float* ptrs[6] = {A("Ex"), A("Ey"), A("Ez"), A("Hx"), A("Hy"), A("Hz")};
+        if (!ck(cudaMalloc(&g_gather_fields, sizeof(ptrs)), "cudaMalloc gather")) { free_all(); return -1; }
+        cudaMemcpy(g_gather_fields, ptrs, sizeof(ptrs), cudaMemcpyHostToDevice);
+    }
+    int NX = d.NX, NXX = d.NXX, NY = d.NY, NYY = d.NYY, NZ = d.NZ, NZ_N = d.NZ_N, off = 0;
+
+    // setZero (fdtdrav.h:919), argument order of fdtdrav.h:4047-4067
+    {
+        std::vector<void*> a;
+        static float* P[96];
+        const char* order[] = {
+            "Ex", "Jx", "Cexe", "Cexhz", "Cexhy", "Cexj", "eps_r_x", "sigma_e_x",
+            "Ey", "Jy", "Ceye", "Ceyhx", "Ceyhz", "Ceyj", "eps_r_y", "sigma_e_y",
+            "Ez", "Jz", "Ceze", "Cezhy", "Cezhx", "Cezj", "eps_r_z", "sigma_e_z",
+            "Hx", "Mx", "Chxh", "Chxey", "Chxez", "Chxm", "mu_r_x", "sigma_m_x",
+            "Hy", "My", "Chyh", "Chyez", "Chyex", "Chym", "mu_r_y", "sigma_m_y",
+            "Hz", "Mz", "Chzh", "Chzex", "Chzey", "Chzm", "mu_r_z", "sigma_m_z",
+            "mat_eps_x", "mat_eps_y", "mat_eps_z", "mat_sigma_e_x", "mat_sigma_e_y", "mat_sigma_e_z",
+            "mat_mu_x", "mat_mu_y", "mat_mu_z", "mat_sigma_m_x", "mat_sigma_m_y", "mat_sigma_m_z",
+            "cpml_b_ex", "cpml_a_ex", "cpml_b_mx", "cpml_a_mx",
+            "cpml_b_ey", "cpml_a_ey", "cpml_b_my", "cpml_a_my",
+            "cpml_b_ez", "cpml_a_ez", "cpml_b_mz", "cpml_a_mz",
+            "Psi_eyx", "Psi_ezx", "Psi_hyx", "Psi_hzx", "cpsi_eyx", "cpsi_ezx", "cpsi_hyx", "cpsi_hzx",
+            "Psi_exy", "Psi_ezy", "Psi_hxy", "Psi_hzy", "cpsi_exy", "cpsi_ezy", "cpsi_hxy", "cpsi_hzy",
+            "Psi_exz", "Psi_eyz", "Psi_hxz", "Psi_hyz", "cpsi_exz", "cpsi_eyz", "cpsi_hxz", "cpsi_hyz"};
+        for (int q = 0; q < 96; ++q) { P[q] = A(order[q]); a.push_back(&P[q]); }
+        a.push_back(&NX); a.push_back(&NY); a.push_back(&NZ_N);
+        if (!launch(K_SETZERO, grid3d(), block3d(), a)) { free_all(); return -1; }
+    }
+    // setBrick per box (fdtdrav.h:1524, called at 4104-4128)
+    for (int b = 0; b < s->nbricks; ++b) {
+        const int* bx = s->brick_box + 6 * b;
+        const float* bm = s->brick_mat + 4 * b;
+        int is = bx[0], js = bx[1], ks = bx[2], ie = bx[3], je = bx[4], ke = bx[5];
+        float se = bm[1], ep = bm[0], sm = bm[3], mu = bm[2];
+        static float* P[12];
+        const char* order[] = {"mat_eps_x", "mat_eps_y", "mat_eps_z", "mat_sigma_e_x", "mat_sigma_e_y", "mat_sigma_e_z",
+                               "mat_mu_x", "mat_mu_y", "mat_mu_z", "mat_sigma_m_x", "mat_sigma_m_y", "mat_sigma_m_z"};
+        std::vector<void*> a = {&NX, &NY, &NZ, &NZ_N, &off};
+        for (int q = 0; q < 12; ++q) { P[q] = A(order[q]); a.push_back(&P[q]); }
+        a.push_back(&is); a.push_back(&js); a.push_back(&ks); a.push_back(&ie); a.push_back(&je); a.push_back(&ke);
+        a.push_back(&se); a.push_back(&se); a.push_back(&se); a.push_back(&ep); a.push_back(&ep); a.push_back(&ep);
+        a.push_back(&sm); a.push_back(&sm); a.push_back(&sm); a.push_back(&mu); a.push_back(&mu); a.push_back(&mu);
+        if (!launch(K_SETBRICK, grid3d(), block3d(), a)) { free_all(); return -1; }
+    }
+    // setSigmaEpsSigmaMu (fdtdrav.h:1097, called at 4133-4150)
+    {
+        static float* P[24];
+        const char* order[] = {"mat_eps_x", "mat_eps_y", "mat_eps_z", "mat_sigma_e_x", "mat_sigma_e_y", "mat_sigma_e_z",
+                               "mat_mu_x", "mat_mu_y", "mat_mu_z", "mat_sigma_m_x", "mat_sigma_m_y", "mat_sigma_m_z",
+                               "eps_r_x", "sigma_e_x", "eps_r_y", "sigma_e_y", "eps_r_z", "sigma_e_z",
+                               "mu_r_x", "sigma_m_x", "mu_r_y", "sigma_m_y", "mu_r_z", "sigma_m_z"};
+        std::vector<void*> a = {&NX, &NY, &NZ, &NZ_N, &off};
+        for (int q = 0; q < 24; ++q) { P[q] = A(order[q]); a.push_back(&P[q]); }
+        if (!launch(K_SETSIGMA, grid3d(), block3d(), a)) { free_all(); return -1; }
+    }
+    // setCoefficients (fdtdrav.h:1223, called at 4213-4230)
+    {
+        static float* P[36];
+        const char* order[] = {
+            "Cexe", "Cexhz", "Cexhy", "Cexj", "eps_r_x", "sigma_e_x",
+            "Ceye", "Ceyhx", "Ceyhz", "Ceyj", "eps_r_y", "sigma_e_y",
+            "Ceze", "Cezhy", "Cezhx", "Cezj", "eps_r_z", "sigma_e_z",
+            "Chxh", "Chxey", "Chxez", "Chxm", "mu_r_x", "sigma_m_x",
+            "Chyh", "Chyez", "Chyex", "Chym", "mu_r_y", "sigma_m_y",
+            "Chzh", "Chzex", "Chzey", "Chzm", "mu_r_z", "sigma_m_z"};
+        std::vector<void*> a = {&NX, &NXX, &NY, &NYY, &NZ, &NZ_N, &off};
+        for (int q = 0; q < 36; ++q) { P[q] = A(order[q]); a.push_back(&P[q]); }
+        a.push_back(&g_d.dx); a.push_back(&g_d.dy); a.push_back(&g_d.dz); a.push_back(&g_d.dt);
+        a.push_back(&g_d.eps0); a.push_back(&g_d.pi); a.push_back(&g_d.mu0);
+        if (!launch(K_SETCOEF, grid3d(), block3d(), a)) { free_all(); return -1; }
+    }
+    // setABCPML (fdtdrav.h:1747, called at 4237-4258); the pml sizes are float parameters there
+    {
+        static float* P[36];
+        static float pf[6];
+        const char* order[] = {
+            "cpml_b_ex", "cpml_a_ex", "cpml_b_mx", "cpml_a_mx", "cpml_b_ey", "cpml_a_ey", "cpml_b_my", "cpml_a_my",
+            "cpml_b_ez", "cpml_a_ez", "cpml_b_mz", "cpml_a_mz",
+            "cpsi_eyx", "cpsi_ezx", "cpsi_hyx", "cpsi_hzx", "cpsi_exy", "cpsi_ezy", "cpsi_hxy", "cpsi_hzy",
+            "cpsi_exz", "cpsi_eyz", "cpsi_hxz", "cpsi_hyz",
+            "Cexhz", "Cexhy", "Ceyhx", "Ceyhz", "Cezhy", "Cezhx", "Chxey", "Chxez", "Chyez", "Chyex", "Chzex", "Chzey"};
+        std::vector<void*> a = {&NX, &NXX, &NY, &NYY, &NZ, &NZ_N, &off};
+        for (int q = 0; q < 36; ++q) { P[q] = A(order[q]); a.push_back(&P[q]); }
+        // call order: pml_x_n, pml_y_n, pml_z_n, pml_x_p, pml_y_p, pml_z_p (fdtdrav.h:4255)
+        pf[0] = (float)d.pml[0]; pf[1] = (float)d.pml[2]; pf[2] = (float)d.pml[4];
+        pf[3] = (float)d.pml[1]; pf[4] = (float)d.pml[3]; pf[5] = (float)d.pml[5];
+        for (int q = 0; q < 6; ++q) a.push_back(&pf[q]);
+        a.push_back(&g_d.dx); a.push_back(&g_d.dy); a.push_back(&g_d.dz); a.push_back(&g_d.dt);
+        a.push_back(&g_d.eps0); a.push_back(&g_d.pi); a.push_back(&g_d.mu0);
+        if (!launch(K_SETABCPML, grid3d(), block3d(), a)) { free_all(); return -1; }
+    }
+    // defineSourceZ per source (fdtdrav.h:1368, called at 4275-4277)
+    g_src_box.clear();
+    for (int q = 0; q < s->nsources; ++q) {
+        const int* bx = s->src_box + 6 * q;
+        g_src_box.push_back(std::vector<int>(bx, bx + 6));
+        int is = bx[0], js = bx[1], ks = bx[2], ie = bx[3], je = bx[4], ke = bx[5];
+        float rs = s->src_r[q];
+        static float* P[6];
+        const char* order[] = {"Ceze", "Cezhy", "Cezhx", "Cezj", "eps_r_z", "sigma_e_z"};
+        std::vector<void*> a = {&NX, &NXX, &NY, &NYY, &NZ, &NZ_N, &off, &is, &js, &ks, &ie, &je, &ke};
+        for (int r = 0; r < 6; ++r) { P[r] = A(order[r]); a.push_back(&P[r]); }
+        a.push_back(&rs); a.push_back(&g_d.dx); a.push_back(&g_d.dy); a.push_back(&g_d.dz); a.push_back(&g_d.dt);
+        a.push_back(&g_d.eps0);
+        if (!launch(K_SRCZ, grid3d(), block3d(), a)) { free_all(); return -1; }
+    }
+    // defineResistor per resistor (fdtdrav.h:1429, called at 4295-4309)
+    for (int q = 0; q < s->nres; ++q) {
+        const int* bx = s->res_box + 6 * q;
+        int is = bx[0], js = bx[1], ks = bx[2], ie = bx[3], je = bx[4], ke = bx[5], dir = 3;
+        float rs = s->res_r[q];
+        static float* P[5];
+        const char* order[] = {"Ceze", "Cezhy", "Cezhx", "eps_r_z", "sigma_e_z"};
+        std::vector<void*> a = {&NX, &NXX, &NY, &NYY, &NZ, &NZ_N, &off, &is, &js, &ks, &ie, &je, &ke, &dir};
+        for (int r = 0; r < 5; ++r) { P[r] = A(order[r]); a.push_back(&P[r]); }
+        a.push_back(&rs); a.push_back(&g_d.dx); a.push_back(&g_d.dy); a.push_back(&g_d.dz); a.push_back(&g_d.dt);
+        a.push_back(&g_d.eps0);
+        if (!launch(K_RES, grid3d(), block3d(), a)) { free_all(); return -1; }
+    }
+    if (!ck(cudaDeviceSynchronize(), "setup sync")) { free_all(); return -1; }
+    g_ready = true;
+    return 0;
+}
+
+// Copy a reference array to the host. Volume arrays are returned as the (nz, nyy, nxx) region
+// (x fastest), 1-D arrays as their first `len` entries.
+int rh_get(const char* name, float* out, long long len) {
+    auto it = g_arr.find(name);
+    if (it == g_arr.end()) { g_err = std::string("unknown array ") + name; return -1; }
+    bool vol = false;
+    for (const char* n : kVolumeNames) vol |= (strcmp(n, name) == 0);
+    if (!vol) return ck(cudaMemcpy(out, it->second, (size_t)len * sizeof(float), cudaMemcpyDeviceToHost), "rh_get") ? 0 : -1;
+    for (int k = 0; k < g_d.NZ; ++k)  // rows of one z-plane are contiguous, planes are NX*NY apart
+        if (!ck(cudaMemcpy2D(out + (size_t)k * g_d.NXX * g_d.NYY, (size_t)g_d.NXX * sizeof(float),
+                             it->second + (size_t)k * g_plane, (size_t)g_d.NX * sizeof(float),
+                             (size_t)g_d.NXX * sizeof(float), (size_t)g_d.NYY, cudaMemcpyDeviceToHost), "rh_get 2D"))
+            return -1;
+    return 0;
+}
+
+// Overwrite a volume array's (nz, nyy, nxx) region from the host (used to seed random states).
+int rh_set(const char* name, const float* in) {
+    auto it = g_arr.find(name);
+    if (it == g_arr.end()) { g_err = std::string("unknown array ") + name; return -1; }
+    for (int k = 0; k < g_d.NZ; ++k)
+        if (!ck(cudaMemcpy2D(it->second + (size_t)k * g_plane, (size_t)g_d.NX * sizeof(float),
+                             in + (size_t)k * g_d.NXX * g_d.NYY, (size_t)g_d.NXX * sizeof(float),
+                             (size_t)g_d.NXX * sizeof(float), (size_t)g_d.NYY, cudaMemcpyHostToDevice), "rh_set 2D"))
+            return -1;
+    return 0;
+}
+
+static bool ensure_signal(const float* sig, long long n) {
+    if ((size_t)n > g_signal_cap) {
+        if (g_signal_dev) cudaFree(g_signal_dev);
+        g_signal_dev = nullptr;
+        if (!ck(cudaMalloc(&g_signal_dev, (size_t)n * sizeof(float)), "cudaMalloc signal")) return false;
+        g_signal_cap = (size_t)n;
+    }
+    return ck(cudaMemcpy(g_signal_dev, sig, (size_t)n * sizeof(float), cudaMemcpyHostToDevice), "signal H2D");
+}
+
+static bool do_calc_e(int m, int src_slot) {
+    int NX = g_d.NX, NXX = g_d.NXX, NY = g_d.NY, NYY = g_d.NYY, NZ = g_d.NZ, NZ_N = g_d.NZ_N, off = 0, voff = 0;
+    int* pml = g_d.pml;  // x_n, x_p, y_n, y_p, z_n, z_p (calc_e parameter order)
+    static int sbox[6];
+    if (src_slot >= 0) for (int q = 0; q < 6; ++q) sbox[q] = g_src_box[src_slot][q];
+    else { sbox[0] = sbox[1] = sbox[2] = -10; sbox[3] = sbox[4] = sbox[5] = -10; }
+    static int vbox[6] = {-10, -10, -10, -10, -10, -10};
+    static int vn[3] = {1, 1, 1};
+    static float* P[57];
+    const char* order[] = {
+        "Ex", "Jx", "Cexe", "Cexhz", "Cexhy", "Cexj", "Ey", "Jy", "Ceye", "Ceyhx", "Ceyhz", "Ceyj",
+        "Ez", "Jz", "Ceze", "Cezhy", "Cezhx", "Cezj", "Hx", "Mx", "Hy", "My", "Hz", "Mz", "gHx", "gHy",
+        "cpml_b_ex", "cpml_a_ex", "cpml_b_ey", "cpml_a_ey", "cpml_b_ez", "cpml_a_ez",
+        "Psi_eyx", "Psi_ezx", "Psi_hyx", "Psi_hzx", "cpsi_eyx", "cpsi_ezx", "cpsi_hyx", "cpsi_hzx",
+        "Psi_exy", "Psi_ezy", "Psi_hxy", "Psi_hzy", "cpsi_exy", "cpsi_ezy", "cpsi_hxy", "cpsi_hzy",
+        "Psi_exz", "Psi_eyz", "Psi_hxz", "Psi_hyz", "cpsi_exz", "cpsi_eyz", "cpsi_hxz", "cpsi_hyz"};
+    std::vector<void*> a = {&NX, &NXX, &NY, &NYY, &NZ, &NZ_N, &off, &voff};
+    for (int q = 0; q < 6; ++q) a.push_back(&pml[q]);
+    for (int q = 0; q < 56; ++q) { P[q] = A(order[q]); a.push_back(&P[q]); }
+    P[56] = g_signal_dev ? g_signal_dev : A("sampE");
+    a.push_back(&P[56]);
+    for (int q = 0; q < 6; ++q) a.push_back(&sbox[q]);
+    for (int q = 0; q < 6; ++q) a.push_back(&vbox[q]);
+    for (int q = 0; q < 3; ++q) a.push_back(&vn[q]);
+    static int mm; mm = m; a.push_back(&mm);
+    static float* PE; PE = A("sampE"); a.push_back(&PE);
+    return launch(K_CALCE, grid3d(), block3d(), a);
+}
+
+static bool do_calc_h(int m) {
+    int NX = g_d.NX, NXX = g_d.NXX, NY = g_d.NY, NYY = g_d.NYY, NZ = g_d.NZ, NZ_N = g_d.NZ_N, off = 0;
+    int* pml = g_d.pml;
+    static int cbox[6] = {-10, -10, -10, -10, -10, -10};
+    static int cn[3] = {1, 1, 1};
+    static float* P[56];
+    const char* order[] = {
+        "Ex", "Jx", "Ey", "Jy", "Ez", "Jz", "gEx", "gEy",
+        "Hx", "Mx", "Chxh", "Chxey", "Chxez", "Chxm", "Hy", "My", "Chyh", "Chyez", "Chyex", "Chym",
+        "Hz", "Mz", "Chzh", "Chzex", "Chzey", "Chzm",
+        "cpml_b_mx", "cpml_a_mx", "cpml_b_my", "cpml_a_my", "cpml_b_mz", "cpml_a_mz",
+        "Psi_eyx", "Psi_ezx", "Psi_hyx", "Psi_hzx", "cpsi_eyx", "cpsi_ezx", "cpsi_hyx", "cpsi_hzx",
+        "Psi_exy", "Psi_ezy", "Psi_hxy", "Psi_hzy", "cpsi_exy", "cpsi_ezy", "cpsi_hxy", "cpsi_hzy",
+        "Psi_exz", "Psi_eyz", "Psi_hxz", "Psi_hyz", "cpsi_exz", "cpsi_eyz", "cpsi_hxz", "cpsi_hyz"};
+    std::vector<void*> a = {&NX, &NXX, &NY, &NYY, &NZ, &NZ_N, &off};
+    for (int q = 0; q < 6; ++q) a.push_back(&pml[q]);
+    for (int q = 0; q < 56; ++q) { P[q] = A(order[q]); a.push_back(&P[q]); }
+    for (int q = 0; q < 6; ++q) a.push_back(&cbox[q]);
+    for (int q = 0; q < 3; ++q) a.push_back(&cn[q]);
+    static int mm; mm = m; a.push_back(&mm);
+    static float* PH[3]; PH[0] = A("sampHx"); PH[1] = A("sampHy"); PH[2] = A("sampHz");
+    a.push_back(&PH[0]); a.push_back(&PH[1]); a.push_back(&PH[2]);
+    return launch(K_CALCH, grid3d(), block3d(), a);
+}
+
+// One reference E half-step (calc_e) at time index m with source slot src_slot (-1: none).
+int rh_calc_e(int m, int src_slot, const float* signal, long long nsig) {
+    if (!g_ready) { g_err = "not set up"; return -1; }
+    if (signal && !ensure_signal(signal, nsig)) return -1;
+    if (!do_calc_e(m, src_slot)) return -1;
+    return ck(cudaDeviceSynchronize(), "calc_e sync") ? 0 : -1;
+}
+
+int rh_calc_h(int m) {
+    if (!g_ready) { g_err = "not set up"; return -1; }
+    if (!do_calc_h(m)) return -1;
+    return ck(cudaDeviceSynchronize(), "calc_h sync") ? 0 : -1;
+}
+
+// Run n_steps reference steps m0 .. m0+n_steps-1 (calc_e then calc_h each step). If nprobes > 0,
+// probe values (component 0..5 = Ex,Ey,Ez,Hx,Hy,Hz at node i,j,k) are gathered after each step
+// into probe_out[step][probe]. elapsed_ms receives the device time of the whole loop (CUDA events).
+int rh_run(int m0, int n_steps, int src_slot, const float* signal, long long nsig,
+           int nprobes, const int* pcomp, const int* pi, const int* pj, const int* pk,
+           float* probe_out, float* elapsed_ms) {
+    if (!g_ready) { g_err = "not set up"; return -1; }
+    if (signal && !ensure_signal(signal, nsig)) return -1;
+    if (nprobes > 0) {
+        if (nprobes > g_probe_cap) {
+            if (g_probe_comp_dev) cudaFree(g_probe_comp_dev);
+            if (g_probe_idx_dev) cudaFree(g_probe_idx_dev);
+            g_probe_comp_dev = nullptr; g_probe_idx_dev = nullptr;
+            if (!ck(cudaMalloc(&g_probe_comp_dev, nprobes * sizeof(int)), "probe comp") ||
+                !ck(cudaMalloc(&g_probe_idx_dev, nprobes * sizeof(long long)), "probe idx")) return -1;
+            g_probe_cap = nprobes;
+        }
+        std::vector<long long> idx(nprobes);
+        for (int p = 0; p < nprobes; ++p)
+            idx[p] = (long long)pi[p] + (long long)pj[p] * g_d.NX + (long long)pk[p] * g_d.NX * g_d.NY;
+        cudaMemcpy(g_probe_comp_dev, pcomp, nprobes * sizeof(int), cudaMemcpyHostToDevice);
+        cudaMemcpy(g_probe_idx_dev, idx.data(), nprobes * sizeof(long long), cudaMemcpyHostToDevice);
+        if (g_probe_dev) cudaFree(g_probe_dev);
+        g_probe_dev = nullptr;
+        if (!ck(cudaMalloc(&g_probe_dev, (size_t)nprobes * n_steps * sizeof(float)), "probe buf")) return -1;
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0); cudaEventCreate(&e1);
+    cudaEventRecord(e0, 0);
+    for (int m = m0; m < m0 + n_steps; ++m) {
+        if (!do_calc_e(m, src_slot)) return -1;
+        if (!do_calc_h(m)) return -1;
+        if (nprobes > 0) {
+            float* outp = g_probe_dev + (size_t)(m - m0) * nprobes;
+            std::vector<void*> a = {&g_gather_fields, &g_probe_comp_dev, &g_probe_idx_dev, &outp, &nprobes};
+            if (!launch(K_GATHER, dim3((nprobes + 127) / 128), dim3(128), a)) return -1;
+        }
+    }
+    cudaEventRecord(e1, 0);
+    if (!ck(cudaEventSynchronize(e1), "run sync")) return -1;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    if (elapsed_ms) *elapsed_ms = ms;
+    if (nprobes > 0 && probe_out)
+        if (!ck(cudaMemcpy(probe_out, g_probe_dev, (size_t)nprobes * n_steps * sizeof(float), cudaMemcpyDeviceToHost),
+                "probe D2H")) return -1;
+    return 0;
+}
+
+long long rh_padded_dims(int* nx, int* ny) { *nx = g_d.NX; *ny = g_d.NY; return (long long)g_vol; }
+
+void rh_free(void) { free_all(); }
+
+}  // extern "C"

@@ -1,0 +1,155 @@
+"""Python driver for the reference-kernel harness (test infrastructure only).
+
+Runs the reference's own setup kernels and calc_e / calc_h (fdtdrav.h, compiled unmodified except
+for its barrier calls, see ref_kernels.cu) on a single slab through ``librefharness.so``. Used to
+generate golden fixtures, to compare coefficient arrays and single steps, and as the timed
+reference arm of the benchmark. Never imported by the product package.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_DIR = os.path.join(os.path.dirname(HERE), "_ref")
+CUBIN = os.path.join(REF_DIR, "fdtdrav_sm103a.cubin")
+RUNNER = os.path.join(REF_DIR, "librefharness.so")
+
+_i = ctypes.c_int
+_f = ctypes.c_float
+_pi = ctypes.POINTER(ctypes.c_int)
+_pf = ctypes.POINTER(ctypes.c_float)
+
+
+class _Scenario(ctypes.Structure):
+    _fields_ = [("nxx", _i), ("nyy", _i), ("nz", _i), ("pml", _i * 6),
+                ("dx", _f), ("dy", _f), ("dz", _f), ("dt", _f), ("eps0", _f), ("pi", _f), ("mu0", _f),
+                ("nbricks", _i), ("brick_box", _pi), ("brick_mat", _pf),
+                ("nsources", _i), ("src_box", _pi), ("src_r", _pf),
+                ("nres", _i), ("res_box", _pi), ("res_r", _pf)]
+
+
+def available() -> bool:
+    return os.path.exists(CUBIN) and os.path.exists(RUNNER)
+
+
+class RefHarness:
+    """One reference simulation on the current GPU (single slab, NUMDEV = 1)."""
+
+    def __init__(self, cubin: str = CUBIN, runner: str = RUNNER):
+        if not os.path.exists(cubin):
+            raise FileNotFoundError(f"reference cubin missing: {cubin}")
+        self.lib = ctypes.CDLL(runner)
+        L = self.lib
+        L.rh_error.restype = ctypes.c_char_p
+        L.rh_load.argtypes = [ctypes.c_char_p]
+        L.rh_setup.argtypes = [ctypes.POINTER(_Scenario)]
+        L.rh_get.argtypes = [ctypes.c_char_p, _pf, ctypes.c_longlong]
+        L.rh_set.argtypes = [ctypes.c_char_p, _pf]
+        L.rh_calc_e.argtypes = [_i, _i, _pf, ctypes.c_longlong]
+        L.rh_calc_h.argtypes = [_i]
+        L.rh_run.argtypes = [_i, _i, _i, _pf, ctypes.c_longlong, _i, _pi, _pi, _pi, _pi, _pf, _pf]
+        self._check(L.rh_load(cubin.encode()))
+        self.sc = None
+
+    def _check(self, rc):
+        if rc != 0:
+            raise RuntimeError("reference harness: " + self.lib.rh_error().decode())
+
+    def setup(self, sc) -> None:
+        """Run the reference setup sequence for a ``fdtd_gb300.scenario.Scenario``."""
+        self.sc = sc
+        s = _Scenario()
+        s.nxx, s.nyy, s.nz = sc.nx, sc.ny, sc.nz
+        for q in range(6):
+            s.pml[q] = sc.pml[q]
+        s.dx, s.dy, s.dz, s.dt = sc.dx, sc.dy, sc.dz, sc.dt
+        s.eps0, s.pi, s.mu0 = sc.eps0, sc.pi, sc.mu0
+        tab = sc.material_table()
+        bb = np.array([b.box for b in sc.bricks], dtype=np.int32).reshape(-1, 6)
+        bm = np.array([tab[b.material] for b in sc.bricks], dtype=np.float32).reshape(-1, 4)
+        sb = np.array([x.box for x in sc.sources], dtype=np.int32).reshape(-1, 6)
+        sr = np.array([x.resistance for x in sc.sources], dtype=np.float32)
+        rb = np.array([x.box for x in sc.resistors], dtype=np.int32).reshape(-1, 6)
+        rr = np.array([x.resistance for x in sc.resistors], dtype=np.float32)
+        self._keep = [np.ascontiguousarray(a) for a in (bb, bm, sb, sr, rb, rr)]
+        bb, bm, sb, sr, rb, rr = self._keep
+        s.nbricks, s.brick_box, s.brick_mat = len(sc.bricks), bb.ctypes.data_as(_pi), bm.ctypes.data_as(_pf)
+        s.nsources, s.src_box, s.src_r = len(sc.sources), sb.ctypes.data_as(_pi), sr.ctypes.data_as(_pf)
+        s.nres, s.res_box, s.res_r = len(sc.resistors), rb.ctypes.data_as(_pi), rr.ctypes.data_as(_pf)
+        self._check(self.lib.rh_setup(ctypes.byref(s)))
+
+    def get(self, name: str, length: Optional[int] = None) -> np.ndarray:
+        """A reference array: volume arrays come back as (nz, ny, nx) float32, 1-D arrays as ``length``."""
+        if length is None:
+            out = np.empty((self.sc.nz, self.sc.ny, self.sc.nx), dtype=np.float32)
+            n = out.size
+        else:
+            out = np.empty(length, dtype=np.float32)
+            n = length
+        self._check(self.lib.rh_get(name.encode(), out.ctypes.data_as(_pf), n))
+        return out
+
+    def set(self, name: str, arr: np.ndarray) -> None:
+        a = np.ascontiguousarray(arr, dtype=np.float32).reshape(self.sc.nz, self.sc.ny, self.sc.nx)
+        self._check(self.lib.rh_set(name.encode(), a.ctypes.data_as(_pf)))
+
+    def calc_e(self, m: int, src_slot: int = -1, signal: Optional[np.ndarray] = None) -> None:
+        sig = None if signal is None else np.ascontiguousarray(signal, dtype=np.float32)
+        self._check(self.lib.rh_calc_e(m, src_slot, None if sig is None else sig.ctypes.data_as(_pf),
+                                       0 if sig is None else sig.size))
+
+    def calc_h(self, m: int) -> None:
+        self._check(self.lib.rh_calc_h(m))
+
+    def run(self, steps: int, m0: int = 0, src_slot: int = -1, signal: Optional[np.ndarray] = None,
+            probes: Sequence = ()) -> tuple:
+        """Run ``steps`` reference steps; returns (probe array (steps, n_probes), elapsed ms)."""
+        sig = None if signal is None else np.ascontiguousarray(signal, dtype=np.float32)
+        n = len(probes)
+        pc = np.array([p.component for p in probes], dtype=np.int32)
+        pi = np.array([p.i for p in probes], dtype=np.int32)
+        pj = np.array([p.j for p in probes], dtype=np.int32)
+        pk = np.array([p.k for p in probes], dtype=np.int32)
+        out = np.zeros((steps, max(n, 1)), dtype=np.float32)
+        ms = _f(0.0)
+        self._check(self.lib.rh_run(m0, steps, src_slot,
+                                    None if sig is None else sig.ctypes.data_as(_pf), 0 if sig is None else sig.size,
+                                    n, pc.ctypes.data_as(_pi), pi.ctypes.data_as(_pi), pj.ctypes.data_as(_pi),
+                                    pk.ctypes.data_as(_pi), out.ctypes.data_as(_pf), ctypes.byref(ms)))
+        return out[:, :n], ms.value
+
+    def fields(self) -> dict:
+        return {n: self.get(n) for n in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")}
+
+    def close(self) -> None:
+        self.lib.rh_free()
+
+
+def run_reference(sc, steps: Optional[int] = None, with_fields: bool = True):
+    """Full reference run of a scenario. Several sources are run one at a time and summed
+    (the reference's calc_e injects a single source box per launch, fdtdrav.h:726)."""
+    steps = sc.steps if steps is None else steps
+    h = RefHarness()
+    try:
+        if not sc.sources:
+            h.setup(sc)
+            probes, _ = h.run(steps, probes=sc.probes)
+            return probes, (h.fields() if with_fields else None)
+        tot_p, tot_f = None, None
+        for s in range(len(sc.sources)):
+            h.setup(sc)
+            p, _ = h.run(steps, src_slot=s, signal=sc.signal_per_node(s), probes=sc.probes)
+            f = h.fields() if with_fields else None
+            if tot_p is None:
+                tot_p, tot_f = p, f
+            else:
+                tot_p = tot_p + p
+                if with_fields:
+                    tot_f = {k: tot_f[k] + f[k] for k in tot_f}
+        return tot_p, tot_f
+    finally:
+        h.close()

@@ -1,0 +1,84 @@
+"""Scenarios behind the golden fixtures in this directory (shared by make_golden.py and the tests).
+
+Every scenario is rebuilt deterministically from these definitions, so a fixture only stores the
+reference's outputs. Sizes are small enough for the CPU oracle to finish in seconds, except the
+64^3 vacuum case, whose fixture keeps probe series, field norms and a mid-plane slice only.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+from fdtd_gb300 import scenario as S  # noqa: E402
+
+ONESTEP_M = 7
+
+
+def onestep_signal():
+    """Per-edge source signal for the single-step fixture: large enough (|Cezj*s| ~ O(1)) that the
+    rounding of the lumped-source term shows in the result."""
+    import numpy as np
+    return (np.random.default_rng(1234).standard_normal(ONESTEP_M + 1) * 1e-3).astype(np.float32)
+
+
+def vacuum64():
+    """64^3 vacuum workload with extra probes of every component (all outside the CPML)."""
+    sc = S.vacuum_cube(64, 1000, name="vacuum64")
+    sc.probes += [S.Probe(S.EZ, 32, 32, 40), S.Probe(S.HX, 32, 40, 32), S.Probe(S.HY, 40, 32, 32),
+                  S.Probe(S.EX, 36, 36, 36), S.Probe(S.EY, 30, 34, 32), S.Probe(S.HZ, 28, 28, 33)]
+    return sc
+
+
+def small_vacuum():
+    """32x28x24 vacuum, asymmetric CPML, one centred source, 80 steps (pulse still inside)."""
+    sc = S.vacuum_cube(32, 80, pml=5, name="small_vacuum")
+    sc.nx, sc.ny, sc.nz = 32, 28, 24
+    sc.pml = (6, 5, 4, 6, 5, 4)
+    wf = sc.sources[0].waveform
+    sc.sources = [S.LumpedSource((15, 13, 11, 15, 13, 12), 50.0, wf)]
+    sc.probes = [S.Probe(S.EZ, 20, 13, 11), S.Probe(S.HX, 15, 16, 12), S.Probe(S.HY, 12, 13, 14),
+                 S.Probe(S.EX, 17, 15, 13), S.Probe(S.EY, 14, 11, 10), S.Probe(S.HZ, 16, 12, 9)]
+    return sc
+
+
+def boxes_scenario():
+    """32x30x26 random dielectric boxes plus one magnetic box, one source, one resistor, 400 steps."""
+    sc = S.scaled_boxes(32, 30, 26, 400, seed=11, pml=5, n_boxes=10, n_sources=1, n_probes=8,
+                        name="small_boxes")
+    sc.pml = (5, 6, 4, 5, 6, 4)
+    sc.materials.append(S.Material(eps_r=3.0, sigma_e=0.01, mu_r=2.0, sigma_m=2e4))
+    sc.bricks.append(S.Brick((9, 8, 9, 17, 14, 15), len(sc.materials) - 1))
+    s = sc.sources[0].box
+    sc.resistors = [S.Resistor((s[0] + 3, s[1] - 2, s[2], s[0] + 3, s[1] - 2, s[5] + 1), 75.0)]
+    return sc
+
+
+def two_sources():
+    """32x28x24 vacuum with two delayed sources (reference runs once per source and sums), 90 steps."""
+    sc = small_vacuum()
+    sc.name = "two_sources"
+    sc.steps = 90
+    sc.sources[0].waveform = S.gaussian_derivative(sc.steps, sc.dt, 30e9, 1e-3)
+    dt = sc.dt
+    wf2 = S.gaussian_derivative(sc.steps, dt, 30e9, 1e-3, delay_steps=17.0, amp=0.5)
+    sc.sources.append(S.LumpedSource((10, 16, 12, 10, 16, 14), 50.0, wf2))
+    return sc
+
+
+def onestep_scenario():
+    """24x20x18 random boxes with a magnetic box, 4-cell CPML, one source: single-step checks."""
+    sc = S.scaled_boxes(24, 20, 18, 16, seed=5, pml=4, n_boxes=6, n_sources=1, n_probes=2,
+                        name="onestep")
+    sc.pml = (4, 3, 4, 3, 4, 3)
+    sc.materials.append(S.Material(eps_r=2.0, sigma_e=0.02, mu_r=3.0, sigma_m=5e3))
+    sc.bricks.append(S.Brick((6, 5, 5, 12, 11, 10), len(sc.materials) - 1))
+    return sc
+
+
+def fixture_scenarios():
+    """(scenario, keep full fields?) for every run fixture."""
+    return [(vacuum64(), False), (small_vacuum(), True), (boxes_scenario(), True), (two_sources(), True)]

@@ -1,0 +1,122 @@
+"""Generate golden fixtures by running the reference's own kernels (needs a GPU and the
+reference-kernel harness built under oracle/_ref by oracle/build_ref.sh).
+
+    python tests/golden/make_golden.py --out <dir> [--analysis <dir>]
+
+Writes one compressed .npz per scenario: the probe series of every step and, for the small grids,
+the six final fields; plus ``onestep.npz`` (one calc_e and one calc_h applied to a seeded random
+state) and ``coefs.npz`` (the reference's per-edge coefficients and 1-D CPML profiles for the
+random-box scenario). The scenarios are defined in golden_scenarios.py so the tests rebuild them
+bit-for-bit without running this script.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle", "ref_harness"))
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+
+import refharness  # noqa: E402
+import golden_scenarios as gs  # noqa: E402
+
+COEF_NAMES = ["Cexe", "Cexhz", "Cexhy", "Ceye", "Ceyhx", "Ceyhz", "Ceze", "Cezhy", "Cezhx", "Cezj",
+              "Chxh", "Chxey", "Chxez", "Chyh", "Chyez", "Chyex", "Chzh", "Chzex", "Chzey",
+              "eps_r_x", "sigma_e_x", "eps_r_y", "sigma_e_y", "eps_r_z", "sigma_e_z",
+              "mu_r_x", "sigma_m_x", "mu_r_y", "sigma_m_y", "mu_r_z", "sigma_m_z",
+              "cpsi_eyx", "cpsi_ezx", "cpsi_hyx", "cpsi_hzx", "cpsi_exy", "cpsi_ezy", "cpsi_hxy", "cpsi_hzy",
+              "cpsi_exz", "cpsi_eyz", "cpsi_hxz", "cpsi_hyz"]
+LINE_NAMES = [("cpml_b_ex", "x"), ("cpml_a_ex", "x"), ("cpml_b_mx", "x"), ("cpml_a_mx", "x"),
+              ("cpml_b_ey", "y"), ("cpml_a_ey", "y"), ("cpml_b_my", "y"), ("cpml_a_my", "y"),
+              ("cpml_b_ez", "z"), ("cpml_a_ez", "z"), ("cpml_b_mz", "z"), ("cpml_a_mz", "z")]
+PSI_E = ["Psi_eyx", "Psi_ezx", "Psi_exy", "Psi_ezy", "Psi_exz", "Psi_eyz"]
+PSI_H = ["Psi_hyx", "Psi_hzx", "Psi_hxy", "Psi_hzy", "Psi_hxz", "Psi_hyz"]
+
+
+def line_len(sc, axis):
+    return {"x": sc.nx, "y": sc.ny, "z": sc.nz}[axis]
+
+
+def run_scenario(sc, full_fields: bool):
+    t0 = time.time()
+    probes, fields = refharness.run_reference(sc, with_fields=True)
+    out = {"probes": probes}
+    if full_fields:
+        for k, v in fields.items():
+            out[k] = v
+    else:
+        for k, v in fields.items():
+            out[k + "_l2"] = np.array(np.linalg.norm(v.astype(np.float64)))
+            out[k + "_zmid"] = v[sc.nz // 2].copy()
+    print(f"{sc.name}: {sc.nx}x{sc.ny}x{sc.nz} x {sc.steps} steps, {len(sc.sources)} source(s) "
+          f"in {time.time() - t0:.1f}s", flush=True)
+    return out
+
+
+def coef_dump(sc):
+    h = refharness.RefHarness()
+    try:
+        h.setup(sc)
+        out = {n: h.get(n) for n in COEF_NAMES}
+        for n, ax in LINE_NAMES:
+            out[n] = h.get(n, line_len(sc, ax))
+        return out
+    finally:
+        h.close()
+
+
+def onestep(sc, seed=99):
+    """Seeded random E and H, one reference calc_e (source slot 0 at step m) then one calc_h."""
+    rng = np.random.default_rng(seed)
+    shape = (sc.nz, sc.ny, sc.nx)
+    state = {n: rng.standard_normal(shape).astype(np.float32) for n in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")}
+    m = gs.ONESTEP_M
+    h = refharness.RefHarness()
+    try:
+        h.setup(sc)
+        for n, v in state.items():
+            h.set(n, v)
+        sig = gs.onestep_signal()
+        h.calc_e(m, 0, sig)
+        out = {n + "_after_e": h.get(n) for n in ("Ex", "Ey", "Ez")}
+        out["signal"] = sig
+        for n in PSI_E:
+            out[n] = h.get(n)
+        h.calc_h(m)
+        for n in ("Hx", "Hy", "Hz"):
+            out[n + "_after_h"] = h.get(n)
+        for n in PSI_H:
+            out[n] = h.get(n)
+        return out
+    finally:
+        h.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", required=True)
+    ap.add_argument("--analysis", default=None, help="also write large analysis-only dumps here")
+    args = ap.parse_args()
+    os.makedirs(args.out, exist_ok=True)
+    for sc, full in gs.fixture_scenarios():
+        np.savez_compressed(os.path.join(args.out, sc.name + ".npz"), **run_scenario(sc, full))
+    np.savez_compressed(os.path.join(args.out, "onestep.npz"), **onestep(gs.onestep_scenario()))
+    np.savez_compressed(os.path.join(args.out, "coefs_onestep.npz"), **coef_dump(gs.onestep_scenario()))
+    if args.analysis:
+        os.makedirs(args.analysis, exist_ok=True)
+        np.savez_compressed(os.path.join(args.analysis, "coefs_boxes.npz"), **coef_dump(gs.boxes_scenario()))
+        sc = gs.boxes_scenario()
+        for n in (39, 41, 45):
+            _, f = refharness.run_reference(sc, steps=n)
+            np.savez_compressed(os.path.join(args.analysis, f"boxes_fields_{n}.npz"), **f)
+    print("golden fixtures written to", args.out)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,136 @@
+"""GPU behaviour of the C ABI: checkpoint/resume, the probe ring buffer, streams, errors."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import golden_scenarios as gs
+from conftest import bitwise_equal
+from fdtd_gb300 import scenario as S
+
+pytestmark = pytest.mark.gpu
+
+
+def small():
+    sc = S.scaled_boxes(28, 24, 20, 60, seed=21, pml=4, n_boxes=5, n_sources=1, n_probes=4, name="api")
+    return sc
+
+
+def test_save_load_state_roundtrip(gpu_lib):
+    import torch
+    from fdtd_gb300 import solver
+    sc = small()
+    with solver.Simulation.from_scenario(sc) as sim:
+        sim.step(20)
+        buf = torch.empty(sim.state_bytes(), dtype=torch.uint8, device="cuda")
+        torch.cuda.synchronize()
+        sim.save_state(buf.data_ptr())
+        sim.step(25)
+        sim.synchronize()
+        a = sim.fields()
+        pa = sim.read_probes(20, 25)
+        sim.load_state(buf.data_ptr())
+        assert sim.current_step == 20
+        sim.step(25)
+        sim.synchronize()
+        b = sim.fields()
+        pb = sim.read_probes(20, 25)
+    assert bitwise_equal(a, b) and bitwise_equal(pa, pb)
+
+
+def test_probe_ring_wraps(gpu_lib):
+    from fdtd_gb300 import solver
+    sc = small()
+    with solver.Simulation.from_scenario(sc, probe_capacity=7) as sim:
+        sim.step(30)
+        sim.synchronize()
+        last = sim.read_probes(23, 7)
+        with pytest.raises(solver.FDTDError) as e:
+            sim.read_probes(10, 5)
+        assert e.value.code == 5  # FDTD_ERR_RANGE
+    with solver.Simulation.from_scenario(sc, probe_capacity=64) as sim:
+        sim.step(30)
+        sim.synchronize()
+        full = sim.read_probes(0, 30)
+    assert bitwise_equal(last, full[23:30])
+
+
+def test_steps_in_chunks_equal_one_call(gpu_lib):
+    from fdtd_gb300 import solver
+    sc = small()
+    with solver.Simulation.from_scenario(sc) as sim:
+        for _ in range(6):
+            sim.step(5)
+        sim.synchronize()
+        a = sim.fields()
+    with solver.Simulation.from_scenario(sc) as sim:
+        sim.step(30)
+        sim.synchronize()
+        b = sim.fields()
+    assert bitwise_equal(a, b)
+
+
+def test_caller_stream(gpu_lib):
+    import torch
+    from fdtd_gb300 import solver
+    sc = small()
+    s = torch.cuda.Stream()
+    with solver.Simulation.from_scenario(sc) as sim:
+        sim.set_stream(s.cuda_stream)
+        sim.step(30)
+        sim.synchronize()
+        a = sim.fields()
+    with solver.Simulation.from_scenario(sc) as sim:
+        sim.step(30)
+        sim.synchronize()
+        b = sim.fields()
+    assert bitwise_equal(a, b)
+
+
+def test_device_field_copies(gpu_lib):
+    import torch
+    from fdtd_gb300 import solver
+    sc = small()
+    with solver.Simulation.from_scenario(sc) as sim:
+        sim.step(12)
+        t = torch.empty(sim.shape, dtype=torch.float32, device="cuda")
+        sim.get_field_device(2, t.data_ptr())
+        sim.synchronize()
+        assert bitwise_equal(t.cpu().numpy(), sim.get_field(2))
+        t.mul_(0.5)
+        torch.cuda.synchronize()
+        sim.set_field_device(2, t.data_ptr())
+        sim.synchronize()
+        assert bitwise_equal(sim.get_field(2), t.cpu().numpy())
+
+
+def test_argument_errors(gpu_lib):
+    from fdtd_gb300 import solver
+    sc = small()
+    with solver.Simulation.from_scenario(sc) as sim:
+        with pytest.raises(solver.FDTDError):
+            sim.add_source((0, 5, 5, 0, 5, 6), 50.0, np.zeros(4, np.float32))  # on the PEC wall
+        with pytest.raises(solver.FDTDError):
+            sim.add_source((5, 5, 5, 5, 5, 5), 50.0, np.zeros(4, np.float32))  # empty k range
+        with pytest.raises(solver.FDTDError):
+            sim.add_source(sc.sources[0].box, 50.0, np.zeros(4, np.float32))  # shares an edge
+        with pytest.raises(solver.FDTDError):
+            sim.add_probe(7, 1, 1, 1)
+        with pytest.raises(solver.FDTDError):
+            sim.set_materials(np.array([[1, 0, 1, 0]], np.float32))  # sigma_m = 0 gives 0/0
+        bad = np.zeros(sim.shape, np.uint8)
+        bad[0, 0, 0] = 200
+        with pytest.raises(solver.FDTDError):
+            sim.set_material_index(bad)
+
+
+def test_no_source_keeps_initial_state(gpu_lib):
+    """Without excitation every node stays at the scale of the reference's initial 1.2e-38."""
+    from fdtd_gb300 import solver
+    sc = small()
+    sc.sources = []
+    with solver.Simulation.from_scenario(sc) as sim:
+        sim.step(10)
+        sim.synchronize()
+        f = sim.fields()
+    assert np.all(np.abs(f) < np.float32(1e-36))

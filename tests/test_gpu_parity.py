@@ -1,0 +1,145 @@
+"""GPU parity: the CUDA solver against the reference's own kernels (golden fixtures) and against
+the CPU oracle, through the C ABI."""
+import numpy as np
+import pytest
+
+import golden_scenarios as gs
+import oracle
+from conftest import REL_L2_TOL, bitwise_equal, golden, rel_l2, rel_l2_group
+from fdtd_gb300 import scenario as S
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")
+SCHEDULES = [1]  # two-pass; the fused sweep is added to this list where it is built
+
+
+def run_gpu(sc, steps=None, schedule=0, material_index=False, fields=True):
+    from fdtd_gb300 import solver
+    steps = sc.steps if steps is None else steps
+    mi = sc.material_index() if material_index else None
+    with solver.Simulation.from_scenario(sc, schedule, material_index=mi, probe_capacity=max(steps, 1)) as sim:
+        sim.step(steps)
+        sim.synchronize()
+        p = sim.read_probes(0, steps)
+        f = sim.fields() if fields else None
+        prof = sim.cpml_profiles()
+    return p, f, prof
+
+
+def scenarios():
+    return dict((s.name, (s, full)) for s, full in gs.fixture_scenarios())
+
+
+@pytest.mark.parametrize("schedule", SCHEDULES)
+@pytest.mark.parametrize("name", ["small_vacuum", "small_boxes", "vacuum64"])
+def test_matches_reference_kernels_bitwise(gpu_lib, name, schedule):
+    """Single-source scenarios: probe series and final fields equal the reference's bit for bit."""
+    sc, full = scenarios()[name]
+    fix = golden(name)
+    p, f, _ = run_gpu(sc, schedule=schedule)
+    assert bitwise_equal(p, fix["probes"]), rel_l2(p, fix["probes"])
+    for c, n in enumerate(FIELDS):
+        if full:
+            assert bitwise_equal(f[c], fix[n]), (n, rel_l2(f[c], fix[n]))
+        else:
+            assert bitwise_equal(f[c][sc.nz // 2], fix[n + "_zmid"]), n
+            assert abs(np.linalg.norm(f[c].astype(np.float64)) - float(fix[n + "_l2"])) <= 1e-12 * float(fix[n + "_l2"])
+
+
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_two_sources_vs_reference(gpu_lib, schedule):
+    """The reference injects one source per calc_e launch, so its two-source fixture is the sum of
+    two runs; linear superposition holds to FP32 rounding."""
+    sc, _ = scenarios()["two_sources"]
+    fix = golden("two_sources")
+    p, f, _ = run_gpu(sc, schedule=schedule)
+    assert rel_l2(p, fix["probes"]) < REL_L2_TOL
+    ref = [fix[n] for n in FIELDS]
+    for c, n in enumerate(FIELDS):
+        assert rel_l2_group(f, ref, c) < REL_L2_TOL, n
+
+
+def test_cpml_profiles_equal_reference(gpu_lib):
+    sc = gs.onestep_scenario()
+    fix = golden("coefs_onestep")
+    _, _, prof = run_gpu(sc, steps=0, fields=False)
+    for a in oracle.PROFILE_NAMES:
+        kind = a[:3]  # b_e / a_e / b_m / a_m
+        got = prof[kind + a[-1]]
+        assert bitwise_equal(got, fix["cpml_" + a][: got.size]), a
+
+
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_onestep_bitwise(gpu_lib, schedule):
+    """One step from a seeded random state, with a large source signal: bit-exact against one
+    reference calc_e + calc_h."""
+    from fdtd_gb300 import solver
+    sc = gs.onestep_scenario()
+    fix = golden("onestep")
+    sig = fix["signal"] if "signal" in fix.files else sc.signal_per_node(0)
+    sc.sources[0].waveform = np.asarray(sig[gs.ONESTEP_M:], dtype=np.float32)  # step 0 injects sig[m]
+    rng = np.random.default_rng(99)
+    shape = (sc.nz, sc.ny, sc.nx)
+    state = {n: rng.standard_normal(shape).astype(np.float32) for n in FIELDS}
+    with solver.Simulation.from_scenario(sc, schedule) as sim:
+        for c, n in enumerate(FIELDS):
+            sim.set_field(c, state[n])
+        sim.step(1)
+        sim.synchronize()
+        out = sim.fields()
+    for c, n in enumerate(FIELDS):
+        key = n + ("_after_e" if c < 3 else "_after_h")
+        assert bitwise_equal(out[c], fix[key]), (key, rel_l2(out[c], fix[key]))
+
+
+def edge_cases():
+    """Small scenarios that exercise masks, padding, faces and lumped elements."""
+    cases = []
+    # odd sizes (row pitch > nx), asymmetric CPML, probes of every component incl. inside CPML
+    sc = S.vacuum_cube(17, 45, pml=2, name="odd17")
+    sc.nx, sc.ny, sc.nz = 17, 13, 11
+    sc.pml = (3, 2, 2, 3, 1, 2)
+    sc.sources = [S.LumpedSource((8, 6, 5, 8, 6, 6), 50.0, sc.sources[0].waveform)]
+    sc.probes = [S.Probe(c, 8 + c % 2, 6, 5) for c in range(6)] + [S.Probe(S.EZ, 1, 6, 5), S.Probe(S.HY, 15, 1, 9)]
+    cases.append(sc)
+    # random boxes with magnetic material, two sources and two resistors, boxes reaching into CPML
+    sc = S.scaled_boxes(40, 33, 29, 60, seed=3, pml=4, n_boxes=9, n_sources=2, n_probes=6, name="boxes40")
+    sc.materials.append(S.Material(eps_r=4.0, sigma_e=0.03, mu_r=1.5, sigma_m=1e4))
+    sc.bricks.append(S.Brick((0, 0, 10, 40, 12, 16), len(sc.materials) - 1))
+    sc.resistors = [S.Resistor((20, 5, 3, 21, 5, 5), 100.0), S.Resistor((30, 25, 20, 30, 26, 22), 25.0)]
+    cases.append(sc)
+    # PEC walls (zero-thickness CPML on some faces), source inside a CPML slab
+    sc = S.vacuum_cube(24, 30, pml=3, name="pec_faces")
+    sc.pml = (0, 4, 0, 4, 3, 0)
+    sc.sources = [S.LumpedSource((21, 12, 12, 21, 12, 13), 50.0, sc.sources[0].waveform)]
+    sc.probes = [S.Probe(S.EZ, 5, 12, 12), S.Probe(S.HX, 20, 3, 2)]
+    cases.append(sc)
+    # x extent a multiple of the row pitch, multi-edge source box
+    sc = S.vacuum_cube(32, 35, pml=4, name="pitch32")
+    sc.sources = [S.LumpedSource((15, 15, 14, 16, 16, 17), 50.0, sc.sources[0].waveform)]
+    sc.probes = [S.Probe(S.EZ, 22, 16, 15), S.Probe(S.HZ, 10, 10, 10)]
+    cases.append(sc)
+    return cases
+
+
+@pytest.mark.parametrize("schedule", SCHEDULES)
+@pytest.mark.parametrize("case", range(4))
+def test_vs_oracle(gpu_lib, case, schedule):
+    """Bit-exact against the oracle when the oracle uses the GPU's CPML profiles; within the FP32
+    parity bar with the oracle's own (host libm) profiles."""
+    sc = edge_cases()[case]
+    p, f, prof = run_gpu(sc, schedule=schedule)
+    po, fo = oracle.run(sc, profile_override=prof)
+    assert bitwise_equal(p, po), rel_l2(p, po)
+    for c, n in enumerate(FIELDS):
+        assert bitwise_equal(f[c], fo[c]), (n, rel_l2(f[c], fo[c]))
+    po2, fo2 = oracle.run(sc)
+    assert rel_l2(p, po2) < REL_L2_TOL
+
+
+def test_material_index_equals_bricks(gpu_lib):
+    sc = edge_cases()[1]
+    p1, f1, _ = run_gpu(sc, steps=20)
+    p2, f2, _ = run_gpu(sc, steps=20, material_index=True)
+    assert bitwise_equal(p1, p2) and bitwise_equal(f1, f2)

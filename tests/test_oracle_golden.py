@@ -1,0 +1,86 @@
+"""The CPU oracle against the golden fixtures produced by the reference's own kernels.
+
+These pin the oracle: coefficient arrays and single steps must be bit-exact, full runs within the
+FP32 parity bar, and the FP64 build states the FP32 error of the reference itself.
+"""
+import numpy as np
+import pytest
+
+import golden_scenarios as gs
+import oracle
+from conftest import REL_L2_TOL, bitwise_equal, golden, rel_l2, rel_l2_group
+
+COEF_MAP = {"eps_r_x": "eps_x", "sigma_e_x": "sig_x", "eps_r_y": "eps_y", "sigma_e_y": "sig_y",
+            "eps_r_z": "eps_z", "sigma_e_z": "sig_z", "mu_r_x": "mu_x", "sigma_m_x": "sm_x",
+            "mu_r_y": "mu_y", "sigma_m_y": "sm_y", "mu_r_z": "mu_z", "sigma_m_z": "sm_z"}
+FIELDS = ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")
+
+
+def ref_profiles(fix):
+    return {a: fix["cpml_" + a] for a in oracle.PROFILE_NAMES}
+
+
+@pytest.fixture(scope="module")
+def coefs():
+    return golden("coefs_onestep")
+
+
+def test_coefficients_bitwise(coefs):
+    """Every per-edge array of setSigmaEpsSigmaMu / setCoefficients / setABCPML / defineSourceZ."""
+    sc = gs.onestep_scenario()
+    for name in coefs.files:
+        if name.startswith("cpml_"):
+            continue
+        o = oracle.coef(sc, COEF_MAP.get(name, name))
+        assert bitwise_equal(o, coefs[name]), name
+
+
+def test_cpml_profiles_close(coefs):
+    """1-D CPML profiles: the oracle uses the host libm's powf/expf, the reference CUDA's; the b
+    values agree to a few ulp and a = (b-1)*... inherits that through the cancellation in b-1."""
+    sc = gs.onestep_scenario()
+    for name in oracle.PROFILE_NAMES:
+        r = coefs["cpml_" + name]
+        o = oracle.coef(sc, name)[: r.size]
+        ulp = np.abs(r.view(np.int32).astype(np.int64) - o.view(np.int32).astype(np.int64)).max()
+        assert ulp <= (2 if name.startswith("b") else 64), (name, ulp)
+
+
+def test_onestep_bitwise():
+    """calc_e then calc_h from a seeded random state, with the reference's own 1-D profiles."""
+    sc = gs.onestep_scenario()
+    fix = golden("onestep")
+    if "signal" in fix.files:
+        sig = fix["signal"]
+        sc.sources[0].waveform = np.asarray(sig, dtype=np.float32) * np.float32(sc.sources[0].box[5] - sc.sources[0].box[2])
+        sc.steps = sig.size
+    rng = np.random.default_rng(99)
+    shape = (sc.nz, sc.ny, sc.nx)
+    state = {n: rng.standard_normal(shape).astype(np.float32) for n in FIELDS}
+    init = np.stack([state[n] for n in FIELDS])
+    out = oracle.onestep(sc, gs.ONESTEP_M, init, profile_override=ref_profiles(golden("coefs_onestep")))
+    for c, n in enumerate(FIELDS):
+        key = n + ("_after_e" if c < 3 else "_after_h")
+        assert bitwise_equal(out[c], fix[key]), key
+
+
+@pytest.mark.parametrize("name", ["small_vacuum", "small_boxes", "two_sources", "vacuum64"])
+def test_full_runs(name):
+    sc = dict((s.name, s) for s, _ in gs.fixture_scenarios())[name]
+    fix = golden(name)
+    probes, fields = oracle.run(sc)
+    assert rel_l2(probes, fix["probes"]) < REL_L2_TOL
+    if name != "vacuum64":
+        ref = [fix[n] for n in FIELDS]
+        for c, n in enumerate(FIELDS):
+            assert rel_l2_group(fields, ref, c) < REL_L2_TOL, n
+
+
+def test_fp64_error_statement():
+    """The FP64 build of the same update at small size: the reference's FP32 probe error against it
+    is small but nonzero (it is the FP32 rounding error of the scheme, reported in DESIGN)."""
+    sc = gs.small_vacuum()
+    fix = golden("small_vacuum")
+    p64, _ = oracle.run(sc, precision="f64")
+    err = rel_l2(fix["probes"], p64)
+    assert 0 < err < 1e-4
