@@ -39,7 +39,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", choices=["512", "64", "hbm"], default="512")
+    ap.add_argument("--config", choices=["512", "256", "64", "hbm"], default="512")
     ap.add_argument("--schedule", type=int, default=0, help="0 auto, 1 two-pass, 2 fused")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -50,6 +50,9 @@ def scenario_for(cfg: str):
     from fdtd_gb300 import scenario as S
     if cfg == "64":
         return S.config_small(), "vacuum 64^3, 10-cell CPML, 1 z-edge source, 1 Ez probe"
+    if cfg == "256":
+        return (S.random_boxes(256, 256, 256, 1000, seed=256, edge=(8, 64), name="boxes256"),
+                "256^3 random boxes (64 boxes, uint8 index), 10-cell CPML, 4 sources, 16 probes")
     if cfg == "hbm":
         return S.config_hbm(), ("1024x1024x896 random boxes (64 boxes, 65 materials, uint8 index), "
                                 "10-cell CPML, 4 sources, 16 probes")
@@ -217,7 +220,7 @@ def bench_ours(args, rank, world):
     sim.prepare()
     sim.step(args.warmup)
     sim.synchronize()
-    launches_per_step = 1 if args.schedule == 2 else 2
+    launches_per_step = 2 if args.schedule == 1 else 1  # auto runs the fused sweep
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     clocks = ClockSampler(torch.cuda.current_device())

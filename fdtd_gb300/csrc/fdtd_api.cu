@@ -52,13 +52,19 @@ struct fdtd_handle {
     int schedule = FDTD_SCHEDULE_AUTO;
     int device = 0;
 
-    // device state
-    float* field[6] = {};
+    // device state: two field buffers and two CPML memory sets; `cur` holds the current step.
+    // The two-pass schedule updates buffer `cur` in place, the fused sweep reads `cur` and writes
+    // the other one (allocated on first use).
+    float* field[2][6] = {};
+    PsiSet psi[2] = {};
+    int cur = 0;
+    bool have_second = false;
+    FusedMaps maps[2];
+    int kc = 0;  // planes per CTA chunk of the fused sweep
     uint8_t* mat = nullptr;
     MatProps* props = nullptr;
     MatCoef* coef = nullptr;
     float* prof[18] = {};
-    PsiSet psi{};
     std::vector<void*> allocs;
     long long psi_elems[6] = {};  // elements per psi array of each face
 
@@ -153,6 +159,70 @@ int validate_grid(const fdtd_grid* g) {
 
 int ensure_prepared(fdtd_handle* h);
 
+// One set of CPML memory slabs (4 arrays per face), initialised to 1.2e-38.
+int alloc_psi_set(fdtd_handle* h, int s) {
+    for (int f = 0; f < 6; ++f) {
+        const long long n = h->psi_elems[f];
+        float* arr[4] = {nullptr, nullptr, nullptr, nullptr};
+        for (int q = 0; q < 4 && n > 0; ++q) {
+            if (h->alloc((void**)&arr[q], sizeof(float) * n) != cudaSuccess) return fail(FDTD_ERR_OOM, "CPML memory allocation failed");
+            if (launch_fill(arr[q], n, kTiny, nullptr) != cudaSuccess) return fail(FDTD_ERR_CUDA, "fill failed");
+        }
+        h->psi[s].f[f].e[0] = arr[0]; h->psi[s].f[f].e[1] = arr[1];
+        h->psi[s].f[f].h[0] = arr[2]; h->psi[s].f[f].h[1] = arr[3];
+    }
+    return FDTD_OK;
+}
+
+float* const* psi_arrays(fdtd_handle* h, int s, int f, float* out[4]) {
+    out[0] = h->psi[s].f[f].e[0]; out[1] = h->psi[s].f[f].e[1];
+    out[2] = h->psi[s].f[f].h[0]; out[3] = h->psi[s].f[f].h[1];
+    return out;
+}
+
+void* tensor_map_encoder() {
+    static void* fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            fn = nullptr;
+    }
+    return fn;
+}
+
+// Second field buffer, second CPML set and the TMA tensor maps of both buffers for the fused sweep.
+int ensure_fused(fdtd_handle* h) {
+    if (h->have_second) return FDTD_OK;
+    const long long V = vol(h);
+    for (int c = 0; c < 6; ++c) {
+        CUDA_TRY(h->alloc((void**)&h->field[1][c], (size_t)V * sizeof(float)));
+        CUDA_TRY(cudaMemcpyAsync(h->field[1][c], h->field[0][c], (size_t)V * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
+    }
+    int rc = alloc_psi_set(h, 1);
+    if (rc) return rc;
+    void* enc = tensor_map_encoder();
+    if (!enc) return fail(FDTD_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    for (int b = 0; b < 2; ++b) {
+        float* hh[3] = {h->field[b][3], h->field[b][4], h->field[b][5]};
+        float* ee[3] = {h->field[b][0], h->field[b][1], h->field[b][2]};
+        if (encode_fused_maps(&h->maps[b], h->g, hh, ee, h->mat, enc) != 0)
+            return fail(FDTD_ERR_CUDA, "tensor map encoding failed");
+    }
+    CUDA_TRY(fused_configure());
+    // planes per CTA chunk: whole columns unless that leaves too few CTAs to fill the GPU
+    const long long tiles = (long long)((h->g.nx + fused_tile_x() - 1) / fused_tile_x()) *
+                            ((h->g.ny + fused_tile_y() - 1) / fused_tile_y());
+    int kc = h->g.nz;
+    while (kc > 16 && tiles * ((h->g.nz + kc - 1) / kc) < 4096) kc = (kc + 1) / 2;
+    h->kc = kc;
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    h->have_second = true;
+    return FDTD_OK;
+}
+
+bool use_fused(const fdtd_handle* h) { return h->schedule == FDTD_SCHEDULE_FUSED || h->schedule == FDTD_SCHEDULE_AUTO; }
+
 }  // namespace
 
 extern "C" {
@@ -178,7 +248,7 @@ int fdtd_create(const fdtd_grid* grid, fdtd_handle** out) {
     auto cleanup = [&](int code) { fdtd_destroy(h); return code; };
     const long long V = vol(h);
     for (int c = 0; c < 6; ++c) {
-        cudaError_t e = h->alloc((void**)&h->field[c], (size_t)V * sizeof(float));
+        cudaError_t e = h->alloc((void**)&h->field[0][c], (size_t)V * sizeof(float));
         if (e != cudaSuccess) return cleanup(fail(FDTD_ERR_OOM, "field allocation failed: " + std::string(cudaGetErrorString(e))));
     }
     if (h->alloc((void**)&h->mat, (size_t)V) != cudaSuccess) return cleanup(fail(FDTD_ERR_OOM, "material index allocation failed"));
@@ -199,24 +269,12 @@ int fdtd_create(const fdtd_grid* grid, fdtd_handle** out) {
         else if (f < 4) n = (long long)g.nz * P[f] * g.pitch;
         else n = (long long)P[f] * g.ny * g.pitch;
         h->psi_elems[f] = n;
-        for (int s = 0; s < 2; ++s) {
-            float* pe = nullptr; float* ph = nullptr;
-            if (n > 0) {
-                if (h->alloc((void**)&pe, sizeof(float) * n) != cudaSuccess || h->alloc((void**)&ph, sizeof(float) * n) != cudaSuccess)
-                    return cleanup(fail(FDTD_ERR_OOM, "CPML memory allocation failed"));
-            }
-            h->psi.f[f].e[s] = pe;
-            h->psi.f[f].h[s] = ph;
-        }
     }
+    rc = alloc_psi_set(h, 0);
+    if (rc) return cleanup(rc);
     // initial state of setZero: fields and psi 1.2e-38, material 0 everywhere
     for (int c = 0; c < 6; ++c)
-        if (launch_fill(h->field[c], V, kTiny, nullptr) != cudaSuccess) return cleanup(fail(FDTD_ERR_CUDA, "fill failed"));
-    for (int f = 0; f < 6; ++f)
-        for (int s = 0; s < 2; ++s) {
-            launch_fill(h->psi.f[f].e[s], h->psi_elems[f], kTiny, nullptr);
-            launch_fill(h->psi.f[f].h[s], h->psi_elems[f], kTiny, nullptr);
-        }
+        if (launch_fill(h->field[0][c], V, kTiny, nullptr) != cudaSuccess) return cleanup(fail(FDTD_ERR_CUDA, "fill failed"));
     if (cudaMemset(h->mat, 0, (size_t)V) != cudaSuccess || cudaMemset(h->status, 0, sizeof(int)) != cudaSuccess)
         return cleanup(fail(FDTD_ERR_CUDA, "memset failed"));
     h->materials.push_back(fdtd_material{1.0f, kTiny, 1.0f, kTiny});
@@ -245,7 +303,6 @@ int fdtd_set_stream(fdtd_handle* h, void* s) {
 int fdtd_set_schedule(fdtd_handle* h, int32_t schedule) {
     if (!h) return fail(FDTD_ERR_INVALID, "handle is NULL");
     if (schedule < FDTD_SCHEDULE_AUTO || schedule > FDTD_SCHEDULE_FUSED) return fail(FDTD_ERR_INVALID, "unknown schedule");
-    if (schedule == FDTD_SCHEDULE_FUSED) return fail(FDTD_ERR_INVALID, "fused schedule not available in this build");
     h->schedule = schedule;
     return FDTD_OK;
 }
@@ -375,9 +432,22 @@ int fdtd_step(fdtd_handle* h, int64_t n) {
     int rc = ensure_prepared(h);
     if (rc) return rc;
     StepParams p = make_params(h);
-    FieldPtrs f{h->field[0], h->field[1], h->field[2], h->field[3], h->field[4], h->field[5]};
+    if (use_fused(h)) {
+        rc = ensure_fused(h);
+        if (rc) return rc;
+        for (int64_t s = 0; s < n; ++s) {
+            const int a = h->cur, b = 1 - h->cur;
+            FieldPtrs fo{h->field[b][0], h->field[b][1], h->field[b][2], h->field[b][3], h->field[b][4], h->field[b][5]};
+            CUDA_TRY(launch_fused(h->maps[a], p, fo, h->psi[a], h->psi[b], h->step, h->kc, h->stream));
+            h->cur = b;
+            ++h->step;
+        }
+        return FDTD_OK;
+    }
+    const int a = h->cur;
+    FieldPtrs f{h->field[a][0], h->field[a][1], h->field[a][2], h->field[a][3], h->field[a][4], h->field[a][5]};
     for (int64_t s = 0; s < n; ++s) {
-        CUDA_TRY(launch_two_pass(p, f, h->psi, h->step, h->stream));
+        CUDA_TRY(launch_two_pass(p, f, h->psi[a], h->step, h->stream));
         ++h->step;
     }
     return FDTD_OK;
@@ -417,7 +487,7 @@ int fdtd_get_field(fdtd_handle* h, int32_t comp, float* out) {
     if (!h || !out) return fail(FDTD_ERR_INVALID, "NULL argument");
     if (comp < 0 || comp > 5) return fail(FDTD_ERR_INVALID, "component must be 0..5");
     const DeviceGrid& g = h->g;
-    CUDA_TRY(cudaMemcpy2DAsync(out, (size_t)g.nx * 4, h->field[comp], (size_t)g.pitch * 4, (size_t)g.nx * 4,
+    CUDA_TRY(cudaMemcpy2DAsync(out, (size_t)g.nx * 4, h->field[h->cur][comp], (size_t)g.pitch * 4, (size_t)g.nx * 4,
                                (size_t)g.ny * g.nz, cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     return FDTD_OK;
@@ -427,8 +497,9 @@ int fdtd_set_field(fdtd_handle* h, int32_t comp, const float* in) {
     if (!h || !in) return fail(FDTD_ERR_INVALID, "NULL argument");
     if (comp < 0 || comp > 5) return fail(FDTD_ERR_INVALID, "component must be 0..5");
     const DeviceGrid& g = h->g;
-    CUDA_TRY(cudaMemcpy2DAsync(h->field[comp], (size_t)g.pitch * 4, in, (size_t)g.nx * 4, (size_t)g.nx * 4,
-                               (size_t)g.ny * g.nz, cudaMemcpyHostToDevice, h->stream));
+    for (int b = 0; b < (h->have_second ? 2 : 1); ++b)
+        CUDA_TRY(cudaMemcpy2DAsync(h->field[b][comp], (size_t)g.pitch * 4, in, (size_t)g.nx * 4, (size_t)g.nx * 4,
+                                   (size_t)g.ny * g.nz, cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     return FDTD_OK;
 }
@@ -437,7 +508,7 @@ int fdtd_get_field_device(fdtd_handle* h, int32_t comp, float* out) {
     if (!h || !out) return fail(FDTD_ERR_INVALID, "NULL argument");
     if (comp < 0 || comp > 5) return fail(FDTD_ERR_INVALID, "component must be 0..5");
     const DeviceGrid& g = h->g;
-    CUDA_TRY(cudaMemcpy2DAsync(out, (size_t)g.nx * 4, h->field[comp], (size_t)g.pitch * 4, (size_t)g.nx * 4,
+    CUDA_TRY(cudaMemcpy2DAsync(out, (size_t)g.nx * 4, h->field[h->cur][comp], (size_t)g.pitch * 4, (size_t)g.nx * 4,
                                (size_t)g.ny * g.nz, cudaMemcpyDeviceToDevice, h->stream));
     return FDTD_OK;
 }
@@ -446,8 +517,9 @@ int fdtd_set_field_device(fdtd_handle* h, int32_t comp, const float* in) {
     if (!h || !in) return fail(FDTD_ERR_INVALID, "NULL argument");
     if (comp < 0 || comp > 5) return fail(FDTD_ERR_INVALID, "component must be 0..5");
     const DeviceGrid& g = h->g;
-    CUDA_TRY(cudaMemcpy2DAsync(h->field[comp], (size_t)g.pitch * 4, in, (size_t)g.nx * 4, (size_t)g.nx * 4,
-                               (size_t)g.ny * g.nz, cudaMemcpyDeviceToDevice, h->stream));
+    for (int b = 0; b < (h->have_second ? 2 : 1); ++b)
+        CUDA_TRY(cudaMemcpy2DAsync(h->field[b][comp], (size_t)g.pitch * 4, in, (size_t)g.nx * 4, (size_t)g.nx * 4,
+                                   (size_t)g.ny * g.nz, cudaMemcpyDeviceToDevice, h->stream));
     return FDTD_OK;
 }
 
@@ -462,10 +534,12 @@ int fdtd_save_state(fdtd_handle* h, void* buf) {
     if (!h || !buf) return fail(FDTD_ERR_INVALID, "NULL argument");
     char* p = (char*)buf;
     const size_t V = (size_t)vol(h) * sizeof(float);
-    for (int c = 0; c < 6; ++c, p += V) CUDA_TRY(cudaMemcpyAsync(p, h->field[c], V, cudaMemcpyDeviceToDevice, h->stream));
+    const int a = h->cur;
+    for (int c = 0; c < 6; ++c, p += V) CUDA_TRY(cudaMemcpyAsync(p, h->field[a][c], V, cudaMemcpyDeviceToDevice, h->stream));
     for (int f = 0; f < 6; ++f) {
         const size_t n = (size_t)h->psi_elems[f] * sizeof(float);
-        float* arr[4] = {h->psi.f[f].e[0], h->psi.f[f].e[1], h->psi.f[f].h[0], h->psi.f[f].h[1]};
+        float* arr[4];
+        psi_arrays(h, a, f, arr);
         for (int q = 0; q < 4; ++q, p += n)
             if (n) CUDA_TRY(cudaMemcpyAsync(p, arr[q], n, cudaMemcpyDeviceToDevice, h->stream));
     }
@@ -479,18 +553,25 @@ int fdtd_load_state(fdtd_handle* h, const void* buf) {
     if (!h || !buf) return fail(FDTD_ERR_INVALID, "NULL argument");
     const char* p = (const char*)buf;
     const size_t V = (size_t)vol(h) * sizeof(float);
-    for (int c = 0; c < 6; ++c, p += V) CUDA_TRY(cudaMemcpyAsync(h->field[c], p, V, cudaMemcpyDeviceToDevice, h->stream));
+    {
+        long long hdr[8];
+        const size_t off = 6 * V + [&] { size_t t = 0; for (int f = 0; f < 6; ++f) t += 4 * (size_t)h->psi_elems[f] * sizeof(float); return t; }();
+        CUDA_TRY(cudaMemcpyAsync(hdr, p + off, sizeof(hdr), cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+        if (hdr[1] != h->g.nx || hdr[2] != h->g.ny || hdr[3] != h->g.nz) return fail(FDTD_ERR_INVALID, "state belongs to another grid");
+        h->step = hdr[0];
+    }
+    const int nb = h->have_second ? 2 : 1;
+    for (int c = 0; c < 6; ++c, p += V)
+        for (int b = 0; b < nb; ++b) CUDA_TRY(cudaMemcpyAsync(h->field[b][c], p, V, cudaMemcpyDeviceToDevice, h->stream));
     for (int f = 0; f < 6; ++f) {
         const size_t n = (size_t)h->psi_elems[f] * sizeof(float);
-        float* arr[4] = {h->psi.f[f].e[0], h->psi.f[f].e[1], h->psi.f[f].h[0], h->psi.f[f].h[1]};
+        float* arr[4];
+        psi_arrays(h, h->cur, f, arr);
         for (int q = 0; q < 4; ++q, p += n)
             if (n) CUDA_TRY(cudaMemcpyAsync(arr[q], p, n, cudaMemcpyDeviceToDevice, h->stream));
     }
-    long long hdr[8];
-    CUDA_TRY(cudaMemcpyAsync(hdr, p, sizeof(hdr), cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
-    if (hdr[1] != h->g.nx || hdr[2] != h->g.ny || hdr[3] != h->g.nz) return fail(FDTD_ERR_INVALID, "state belongs to another grid");
-    h->step = hdr[0];
     return FDTD_OK;
 }
 

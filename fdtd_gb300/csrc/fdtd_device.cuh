@@ -105,6 +105,10 @@ __device__ __forceinline__ float upd4(float c1, float v, float c2, float d2, flo
 __device__ __forceinline__ float psi_upd(float b, float psi, float a, float d) {
     return __fmaf_rn(b, psi, __fmul_rn(a, d));
 }
+// The reference's Psi_hyz statement (fdtdrav.h:537) is contracted with b*psi as the addend.
+__device__ __forceinline__ float psi_upd_hyz(float b, float psi, float a, float d) {
+    return __fmaf_rn(a, d, __fmul_rn(b, psi));
+}
 // f = f + cpsi*psi (e.g. fdtdrav.h:410)
 __device__ __forceinline__ float psi_add(float f, float cpsi, float psi) {
     return __fmaf_rn(cpsi, psi, f);

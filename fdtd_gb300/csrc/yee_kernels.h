@@ -1,6 +1,8 @@
 // Launch interface of the update kernels (host-visible declarations).
 #pragma once
 
+#include <cuda.h>
+
 #include "fdtd_device.cuh"
 
 namespace fdtd {
@@ -17,6 +19,23 @@ struct PsiSet {
 // One time step m with the two-pass schedule (E pass then H pass, in place).
 cudaError_t launch_two_pass(const StepParams& p, const FieldPtrs& f, const PsiSet& ps, long long m,
                             cudaStream_t st);
+
+// Fused z-marching sweep (yee_fused.cu): reads fields through TMA tensor maps of buffer A (H with
+// halo, old E, material index) and writes buffer B; CPML memory psi_in -> psi_out.
+struct FusedMaps {
+    CUtensorMap h[3];
+    CUtensorMap e[3];
+    CUtensorMap mat;
+};
+cudaError_t fused_configure();
+int fused_smem_bytes();
+int fused_tile_x();
+int fused_tile_y();
+cudaError_t launch_fused(const FusedMaps& maps, const StepParams& p, const FieldPtrs& fo, const PsiSet& psi_in,
+                         const PsiSet& psi_out, long long m, int kc, cudaStream_t st);
+// encode_fn: the driver's cuTensorMapEncodeTiled. Returns 0 on success.
+int encode_fused_maps(FusedMaps* out, const DeviceGrid& g, float* const h[3], float* const e[3], const uint8_t* mat,
+                      void* encode_fn);
 
 // Setup kernels (setup_kernels.cu).
 cudaError_t launch_cpml_profiles(const DeviceGrid& g, float pi, float* const prof[18], cudaStream_t st);

@@ -393,7 +393,8 @@ void calc_h(Sim<R>& s, R* row) {
                 if (i < NX && j < NY && ((k < s.pzn) || (k > NZ - s.pzp - 1 && k < NZ - 1))) {
                     if (k + 1 < NZ) {
                         s.Psi_hxz[n] = FMA<R>(s.b_mz[k], s.Psi_hxz[n], s.a_mz[k] * (s.Ey[n + sz] - s.Ey[n]));
-                        s.Psi_hyz[n] = FMA<R>(s.b_mz[k], s.Psi_hyz[n], s.a_mz[k] * (s.Ex[n + sz] - s.Ex[n]));
+                        // the reference's Psi_hyz statement (fdtdrav.h:537) is contracted with b*psi as the addend
+                        s.Psi_hyz[n] = FMA<R>(s.a_mz[k], s.Ex[n + sz] - s.Ex[n], s.b_mz[k] * s.Psi_hyz[n]);
                     }
                     if (j < NY - 1) s.Hx[n] = FMA<R>(s.cpsi_hxz[n], s.Psi_hxz[n], s.Hx[n]);
                     if (i < NX - 1) s.Hy[n] = FMA<R>(s.cpsi_hyz[n], s.Psi_hyz[n], s.Hy[n]);
@@ -407,9 +408,18 @@ std::vector<R>* field(Sim<R>& s, int c) {
     return f[c];
 }
 
+// The 12 psi arrays in the reference's order: E x, y, z faces then H x, y, z faces.
+template <class R>
+std::vector<R>* psi_arr(Sim<R>& s, int q) {
+    std::vector<R>* a[12] = {&s.Psi_eyx, &s.Psi_ezx, &s.Psi_exy, &s.Psi_ezy, &s.Psi_exz, &s.Psi_eyz,
+                             &s.Psi_hyx, &s.Psi_hzx, &s.Psi_hxy, &s.Psi_hzy, &s.Psi_hxz, &s.Psi_hyz};
+    return a[q];
+}
+
 template <class R>
 int run(const or_scenario* sc, int steps, const float* signal_per_node, int n_sig,
-        const float* init_fields, R* probes_out, R* fields_out, int nthreads, int onestep_m) {
+        const float* init_fields, R* probes_out, R* fields_out, int nthreads, int onestep_m,
+        const float* init_psi = nullptr, R* psi_out = nullptr) {
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
@@ -418,6 +428,9 @@ int run(const or_scenario* sc, int steps, const float* signal_per_node, int n_si
     if (init_fields)
         for (int c = 0; c < 6; ++c)
             for (size_t n = 0; n < s.N; ++n) (*field(s, c))[n] = (R)init_fields[(size_t)c * s.N + n];
+    if (init_psi)
+        for (int q = 0; q < 12; ++q)
+            for (size_t n = 0; n < s.N; ++n) (*psi_arr(s, q))[n] = (R)init_psi[(size_t)q * s.N + n];
     const size_t np = s.probes.size();
     std::vector<R> row(np ? np : 1);
     if (onestep_m >= 0) {  // one calc_e then one calc_h at time index onestep_m
@@ -425,6 +438,7 @@ int run(const or_scenario* sc, int steps, const float* signal_per_node, int n_si
         if (fields_out) for (int c = 0; c < 3; ++c) std::memcpy(fields_out + (size_t)c * s.N, field(s, c)->data(), s.N * sizeof(R));
         calc_h<R>(s, row.data());
         if (fields_out) for (int c = 3; c < 6; ++c) std::memcpy(fields_out + (size_t)c * s.N, field(s, c)->data(), s.N * sizeof(R));
+        if (psi_out) for (int q = 0; q < 12; ++q) std::memcpy(psi_out + (size_t)q * s.N, psi_arr(s, q)->data(), s.N * sizeof(R));
         return 0;
     }
     for (int m = 0; m < steps; ++m) {
@@ -451,9 +465,11 @@ int or_run_f64(const or_scenario* sc, int steps, const float* sig, int n_sig, co
     return run<double>(sc, steps, sig, n_sig, init_fields, probes_out, fields_out, nthreads, -1);
 }
 // One calc_e (fields_out[0..2] after it) then one calc_h (fields_out[3..5]) from init_fields.
+// init_psi / psi_out: 12 (nz,ny,nx) arrays in the order eyx, ezx, exy, ezy, exz, eyz, hyx, hzx,
+// hxy, hzy, hxz, hyz (either may be NULL).
 int or_onestep_f32(const or_scenario* sc, int m, const float* sig, int n_sig, const float* init_fields,
-                   float* fields_out) {
-    return run<float>(sc, 0, sig, n_sig, init_fields, nullptr, fields_out, 1, m);
+                   float* fields_out, const float* init_psi, float* psi_out) {
+    return run<float>(sc, 0, sig, n_sig, init_fields, nullptr, fields_out, 1, m, init_psi, psi_out);
 }
 
 // Per-edge coefficient arrays after the full setup, by reference name (volume (nz,ny,nx) or 1-D).

@@ -62,7 +62,7 @@ def lib():
         L.or_error.restype = ctypes.c_char_p
         L.or_run_f32.argtypes = [ctypes.POINTER(_Scenario), _i, _pf, _i, _pf, _pf, _pf, _i]
         L.or_run_f64.argtypes = [ctypes.POINTER(_Scenario), _i, _pf, _i, _pf, _pd, _pd, _i]
-        L.or_onestep_f32.argtypes = [ctypes.POINTER(_Scenario), _i, _pf, _i, _pf, _pf]
+        L.or_onestep_f32.argtypes = [ctypes.POINTER(_Scenario), _i, _pf, _i, _pf, _pf, _pf, _pf]
         L.or_coef_f32.argtypes = [ctypes.POINTER(_Scenario), ctypes.c_char_p, _pf]
         _lib = L
     return _lib
@@ -136,17 +136,27 @@ def run(sc, steps: Optional[int] = None, precision: str = "f32", init_fields: Op
     return pout[:, :p.n_probes], fout
 
 
-def onestep(sc, m: int, init_fields: np.ndarray, profile_override: Optional[dict] = None) -> np.ndarray:
-    """One calc_e then one calc_h from ``init_fields`` (6, nz, ny, nx); returns the 6 fields after."""
+# Order of the 12 psi arrays in onestep's init_psi / psi output.
+PSI_NAMES = ["Psi_eyx", "Psi_ezx", "Psi_exy", "Psi_ezy", "Psi_exz", "Psi_eyz",
+             "Psi_hyx", "Psi_hzx", "Psi_hxy", "Psi_hzy", "Psi_hxz", "Psi_hyz"]
+
+
+def onestep(sc, m: int, init_fields: np.ndarray, profile_override: Optional[dict] = None,
+            init_psi: Optional[np.ndarray] = None, return_psi: bool = False):
+    """One calc_e then one calc_h from ``init_fields`` (6, nz, ny, nx) and optionally ``init_psi``
+    (12, nz, ny, nx, order PSI_NAMES); returns the 6 fields after (and the 12 psi arrays)."""
     p = _Prepared(sc, profile_override)
     init = np.ascontiguousarray(init_fields, dtype=np.float32)
     out = np.zeros((6, sc.nz, sc.ny, sc.nx), dtype=np.float32)
+    ipsi = None if init_psi is None else np.ascontiguousarray(init_psi, dtype=np.float32)
+    psi = np.zeros((12, sc.nz, sc.ny, sc.nx), dtype=np.float32) if return_psi else None
     L = lib()
     rc = L.or_onestep_f32(ctypes.byref(p.s), m, p.sig.ctypes.data_as(_pf), p.n_sig, init.ctypes.data_as(_pf),
-                          out.ctypes.data_as(_pf))
+                          out.ctypes.data_as(_pf), None if ipsi is None else ipsi.ctypes.data_as(_pf),
+                          None if psi is None else psi.ctypes.data_as(_pf))
     if rc != 0:
         raise RuntimeError("oracle: " + L.or_error().decode())
-    return out
+    return (out, psi) if return_psi else out
 
 
 def coef(sc, name: str, profile_override: Optional[dict] = None) -> np.ndarray:

@@ -54,6 +54,13 @@ def run_scenario(sc, full_fields: bool):
         for k, v in fields.items():
             out[k + "_l2"] = np.array(np.linalg.norm(v.astype(np.float64)))
             out[k + "_zmid"] = v[sc.nz // 2].copy()
+    h = refharness.RefHarness()
+    try:
+        h.setup(sc)
+        for n, ax in LINE_NAMES:
+            out[n] = h.get(n, line_len(sc, ax))
+    finally:
+        h.close()
     print(f"{sc.name}: {sc.nx}x{sc.ny}x{sc.nz} x {sc.steps} steps, {len(sc.sources)} source(s) "
           f"in {time.time() - t0:.1f}s", flush=True)
     return out
@@ -98,6 +105,34 @@ def onestep(sc, seed=99):
         h.close()
 
 
+def onestep_psi(sc, seed=77):
+    """Seeded random E, H and all 12 CPML psi arrays, one reference calc_e then one calc_h: pins
+    the rounding of the psi recurrences and of the psi corrections."""
+    rng = np.random.default_rng(seed)
+    shape = (sc.nz, sc.ny, sc.nx)
+    names = ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz") + tuple(PSI_E) + tuple(PSI_H)
+    state = {n: rng.standard_normal(shape).astype(np.float32) for n in names}
+    m = gs.ONESTEP_M
+    h = refharness.RefHarness()
+    try:
+        h.setup(sc)
+        for n, v in state.items():
+            h.set(n, v)
+        sig = gs.onestep_signal()
+        h.calc_e(m, 0, sig)
+        out = {n + "_after_e": h.get(n) for n in ("Ex", "Ey", "Ez")}
+        for n in PSI_E:
+            out[n + "_after"] = h.get(n)
+        h.calc_h(m)
+        for n in ("Hx", "Hy", "Hz"):
+            out[n + "_after_h"] = h.get(n)
+        for n in PSI_H:
+            out[n + "_after"] = h.get(n)
+        return out
+    finally:
+        h.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
@@ -108,6 +143,7 @@ def main():
         np.savez_compressed(os.path.join(args.out, sc.name + ".npz"), **run_scenario(sc, full))
     np.savez_compressed(os.path.join(args.out, "onestep.npz"), **onestep(gs.onestep_scenario()))
     np.savez_compressed(os.path.join(args.out, "coefs_onestep.npz"), **coef_dump(gs.onestep_scenario()))
+    np.savez_compressed(os.path.join(args.out, "onestep_psi.npz"), **onestep_psi(gs.onestep_scenario()))
     if args.analysis:
         os.makedirs(args.analysis, exist_ok=True)
         np.savez_compressed(os.path.join(args.analysis, "coefs_boxes.npz"), **coef_dump(gs.boxes_scenario()))

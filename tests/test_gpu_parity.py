@@ -11,7 +11,7 @@ from fdtd_gb300 import scenario as S
 pytestmark = pytest.mark.gpu
 
 FIELDS = ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")
-SCHEDULES = [1]  # two-pass; the fused sweep is added to this list where it is built
+SCHEDULES = [1, 2]  # two-pass, fused sweep
 
 
 def run_gpu(sc, steps=None, schedule=0, material_index=False, fields=True):
@@ -143,3 +143,88 @@ def test_material_index_equals_bricks(gpu_lib):
     p1, f1, _ = run_gpu(sc, steps=20)
     p2, f2, _ = run_gpu(sc, steps=20, material_index=True)
     assert bitwise_equal(p1, p2) and bitwise_equal(f1, f2)
+
+
+def pack_state(sc, fields, psi, step):
+    """State buffer of fdtd_save_state / fdtd_load_state built from dense arrays: 6 fields padded to
+    the 32-float row pitch, then per CPML face (x_n, x_p, y_n, y_p, z_n, z_p) the slabs
+    e0, e1, h0, h1, then an 8 x int64 header (step, nx, ny, nz)."""
+    nz, ny, nx = sc.nz, sc.ny, sc.nx
+    pitch = (nx + 31) // 32 * 32
+    parts = []
+    for c in range(6):
+        a = np.zeros((nz, ny, pitch), np.float32)
+        a[:, :, :nx] = fields[c]
+        parts.append(a.ravel())
+    P = sc.pml
+    names = {0: ("Psi_eyx", "Psi_ezx", "Psi_hyx", "Psi_hzx"), 1: ("Psi_exy", "Psi_ezy", "Psi_hxy", "Psi_hzy"),
+             2: ("Psi_exz", "Psi_eyz", "Psi_hxz", "Psi_hyz")}
+    for f in range(6):
+        ax, side = f // 2, f % 2
+        n = P[f]
+        for nm in names[ax]:
+            v = psi[nm]
+            if ax == 0:
+                sl = v[:, :, :n] if side == 0 else v[:, :, nx - n:]
+                parts.append(np.ascontiguousarray(sl).ravel())
+            elif ax == 1:
+                a = np.zeros((nz, n, pitch), np.float32)
+                a[:, :, :nx] = v[:, :n, :] if side == 0 else v[:, ny - n:, :]
+                parts.append(a.ravel())
+            else:
+                a = np.zeros((n, ny, pitch), np.float32)
+                a[:, :, :nx] = v[:n] if side == 0 else v[nz - n:]
+                parts.append(a.ravel())
+    hdr = np.zeros(8, np.int64)
+    hdr[:4] = (step, nx, ny, nz)
+    return np.concatenate([np.concatenate(parts).view(np.uint8), hdr.view(np.uint8)])
+
+
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_onestep_random_psi_bitwise(gpu_lib, schedule):
+    """One step from random fields and random CPML memory (loaded through the state API): fields
+    bit-exact against one reference calc_e + calc_h, which pins every psi recurrence."""
+    import torch
+    from fdtd_gb300 import solver
+    sc = gs.onestep_scenario()
+    fix = golden("onestep_psi")
+    sc.sources[0].waveform = gs.onestep_signal()  # single-edge source: per-edge signal = V
+    rng = np.random.default_rng(77)
+    shape = (sc.nz, sc.ny, sc.nx)
+    names = FIELDS + tuple(oracle.PSI_NAMES)
+    st = {n: rng.standard_normal(shape).astype(np.float32) for n in names}
+    buf = pack_state(sc, [st[n] for n in FIELDS], st, gs.ONESTEP_M)
+    with solver.Simulation.from_scenario(sc, schedule) as sim:
+        assert buf.size == sim.state_bytes()
+        dev = torch.from_numpy(buf).cuda()
+        torch.cuda.synchronize()
+        sim.load_state(dev.data_ptr())
+        assert sim.current_step == gs.ONESTEP_M
+        sim.step(1)
+        sim.synchronize()
+        out = sim.fields()
+    for c, n in enumerate(FIELDS):
+        key = n + ("_after_e" if c < 3 else "_after_h")
+        assert bitwise_equal(out[c], fix[key]), (key, rel_l2(out[c], fix[key]))
+
+
+@pytest.mark.parametrize("dims", [(70, 45, 80), (33, 13, 40), (100, 17, 16)])
+def test_fused_equals_two_pass(gpu_lib, dims):
+    """Ragged tiles in x and y, several z-chunks per column: the fused sweep reproduces the two-pass
+    schedule bit for bit (probes and all fields), and switching schedules mid-run changes nothing."""
+    from fdtd_gb300 import solver
+    nx, ny, nz = dims
+    sc = S.scaled_boxes(nx, ny, nz, 30, seed=nx + ny, pml=3, n_boxes=8, n_sources=1, n_probes=6, name="ragged")
+    p1, f1, _ = run_gpu(sc, schedule=1)
+    p2, f2, _ = run_gpu(sc, schedule=2)
+    assert bitwise_equal(p1, p2), rel_l2(p2, p1)
+    assert bitwise_equal(f1, f2), rel_l2(f2, f1)
+    with solver.Simulation.from_scenario(sc, 2, probe_capacity=30) as sim:
+        sim.step(11)
+        sim.set_schedule(1)
+        sim.step(7)
+        sim.set_schedule(2)
+        sim.step(12)
+        sim.synchronize()
+        assert bitwise_equal(sim.read_probes(0, 30), p1)
+        assert bitwise_equal(sim.fields(), f1)

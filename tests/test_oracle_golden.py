@@ -76,6 +76,24 @@ def test_full_runs(name):
             assert rel_l2_group(fields, ref, c) < REL_L2_TOL, n
 
 
+@pytest.mark.parametrize("name", ["small_vacuum", "small_boxes"])
+def test_full_runs_bitwise_with_reference_profiles(name):
+    """With the reference's own 1-D CPML b / a profiles (CUDA expf), single-source runs are
+    bit-exact: probes of every step and the final fields. The CPML stretching kappa is still the
+    oracle's (host powf); for these thin CPMLs it equals CUDA's, so the runs match exactly."""
+    sc = dict((s.name, s) for s, _ in gs.fixture_scenarios())[name]
+    fix = golden(name)
+    if "cpml_b_ex" not in fix.files:
+        pytest.skip("fixture predates the stored profiles")
+    probes, fields = oracle.run(sc, profile_override=ref_profiles(fix))
+    assert bitwise_equal(probes, fix["probes"])
+    for c, n in enumerate(FIELDS):
+        if n in fix.files:
+            assert bitwise_equal(fields[c], fix[n]), n
+        else:
+            assert bitwise_equal(fields[c][sc.nz // 2], fix[n + "_zmid"]), n
+
+
 def test_fp64_error_statement():
     """The FP64 build of the same update at small size: the reference's FP32 probe error against it
     is small but nonzero (it is the FP32 rounding error of the scheme, reported in DESIGN)."""
@@ -84,3 +102,24 @@ def test_fp64_error_statement():
     p64, _ = oracle.run(sc, precision="f64")
     err = rel_l2(fix["probes"], p64)
     assert 0 < err < 1e-4
+
+
+def test_onestep_random_psi_bitwise():
+    """Random fields and random CPML memory: every field and every psi array after one calc_e +
+    calc_h equals the reference's (this pins the psi recurrences and corrections)."""
+    sc = gs.onestep_scenario()
+    fix = golden("onestep_psi")
+    sc.sources[0].waveform = gs.onestep_signal()
+    sc.steps = gs.ONESTEP_M + 1
+    rng = np.random.default_rng(77)
+    shape = (sc.nz, sc.ny, sc.nx)
+    names = FIELDS + tuple(oracle.PSI_NAMES)
+    st = {n: rng.standard_normal(shape).astype(np.float32) for n in names}
+    out, psi = oracle.onestep(sc, gs.ONESTEP_M, np.stack([st[n] for n in FIELDS]),
+                              profile_override=ref_profiles(golden("coefs_onestep")),
+                              init_psi=np.stack([st[n] for n in oracle.PSI_NAMES]), return_psi=True)
+    for c, n in enumerate(FIELDS):
+        key = n + ("_after_e" if c < 3 else "_after_h")
+        assert bitwise_equal(out[c], fix[key]), key
+    for q, n in enumerate(oracle.PSI_NAMES):
+        assert bitwise_equal(psi[q], fix[n + "_after"]), n
