@@ -22,10 +22,11 @@ constexpr int kMaxMaterials = 256;
 constexpr int kDefaultEntry = kMaxMaterials;  // H coefficient of faces the reference never averages
 
 // Per-material coefficients for an edge whose surrounding cells all hold the same material.
-// e[c] = {Ca, Cb_plus, Cb_minus} for Ex, Ey, Ez; h[c] = {Ch, Cb_plus, Cb_minus} for Hx, Hy, Hz.
+// e[c] = {Ca, Cb_plus, Cb_minus, 0} for Ex, Ey, Ez; h[c] = {Ch, Cb_plus, Cb_minus, 0} for Hx, Hy,
+// Hz (one 16-byte load per component).
 struct MatCoef {
-    float e[3][3];
-    float h[3][3];
+    float4 e[3];
+    float4 h[3];
 };
 
 struct MatProps {
@@ -59,6 +60,20 @@ struct DeviceGrid {
     float dx, dy, dz, dt, eps0, mu0;
 };
 
+// Curl coefficients of one material (the CPML background) divided by the CPML stretching kappa
+// at every node of each axis, the value setABCPML leaves in the per-edge arrays
+// (fdtdrav.h:1893-1906); outside the slabs kappa = 1 and the entries equal the undivided
+// coefficient. Index [axis][slot] with the slots
+//   x: {Ey minus, Ez plus}   y: {Ex plus, Ez minus}   z: {Ex minus, Ey plus}
+// for E and
+//   x: {Hy plus, Hz minus}   y: {Hx minus, Hz plus}   z: {Hx plus, Hy minus}
+// for H.
+struct BgCurl {
+    int mat;
+    const float* e[3][2];
+    const float* h[3][2];
+};
+
 // Everything an update kernel reads besides the fields.
 struct StepParams {
     DeviceGrid g;
@@ -81,6 +96,7 @@ struct StepParams {
     int n_probes;
     long long ring_cap;
     int* status;                 // device error word
+    BgCurl bg;                   // kappa-divided curl coefficients of the CPML background material
 };
 
 // ------------------------------------------------------------------------------------------

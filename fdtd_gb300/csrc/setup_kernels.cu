@@ -91,9 +91,9 @@ __global__ void k_material_tables(const MatProps* props, int n, MatCoef* coef, D
     const float dp_h[3] = {g.dz, g.dx, g.dy}, dm_h[3] = {g.dy, g.dz, g.dx};
     for (int q = 0; q < 3; ++q) {
         Coef3 e = coef3(eps, sig, g.dt, g.eps0, dp_e[q], dm_e[q]);
-        c.e[q][0] = e.a; c.e[q][1] = e.bp; c.e[q][2] = e.bm;
+        c.e[q] = make_float4(e.a, e.bp, e.bm, 0.0f);
         Coef3 h = coef3(mu, sm, g.dt, g.mu0, dp_h[q], dm_h[q]);
-        c.h[q][0] = h.a; c.h[q][1] = h.bp; c.h[q][2] = h.bm;
+        c.h[q] = make_float4(h.a, h.bp, h.bm, 0.0f);
     }
     coef[m] = c;
 }
@@ -140,6 +140,35 @@ cudaError_t launch_lumped_coefs(const DeviceGrid& g, const uint8_t* mat, const M
                                 int n_edges, cudaStream_t st) {
     if (n_edges == 0) return cudaSuccess;
     k_lumped_coefs<<<(n_edges + 127) / 128, 128, 0, st>>>(g, mat, props, edges, boxes, resist, owner, n_edges);
+    return cudaGetLastError();
+}
+
+// Kappa-divided curl coefficients of material `bg` along each axis (the division setABCPML applies
+// in its slabs, fdtdrav.h:1893-1906; kappa = 1 elsewhere leaves the coefficient unchanged).
+// out[axis][slot]: E then H slots as documented on BgCurl.
+__global__ void k_bg_curl(const MatCoef* coef, int bg, DeviceGrid g, const float* const* kappa, float* const* out) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int a = blockIdx.y;
+    const int n = a == 0 ? g.nx : a == 1 ? g.ny : g.nz;
+    if (q >= n) return;
+    const MatCoef c = coef[bg];
+    const float ke = kappa[2 * a][q], km = kappa[2 * a + 1][q];
+    // E slots: x {Ey minus, Ez plus}, y {Ex plus, Ez minus}, z {Ex minus, Ey plus}
+    const float e0[3] = {c.e[1].z, c.e[0].y, c.e[0].z};
+    const float e1[3] = {c.e[2].y, c.e[2].z, c.e[1].y};
+    // H slots: x {Hy plus, Hz minus}, y {Hx minus, Hz plus}, z {Hx plus, Hy minus}
+    const float h0[3] = {c.h[1].y, c.h[0].z, c.h[0].y};
+    const float h1[3] = {c.h[2].z, c.h[2].y, c.h[1].z};
+    out[4 * a + 0][q] = __fdiv_rn(e0[a], ke);
+    out[4 * a + 1][q] = __fdiv_rn(e1[a], ke);
+    out[4 * a + 2][q] = __fdiv_rn(h0[a], km);
+    out[4 * a + 3][q] = __fdiv_rn(h1[a], km);
+}
+
+cudaError_t launch_bg_curl(const DeviceGrid& g, const MatCoef* coef, int bg, const float* const* kappa_dev,
+                           float* const* out_dev, cudaStream_t st) {
+    const int nmax = max(g.nx, max(g.ny, g.nz));
+    k_bg_curl<<<dim3((nmax + 127) / 128, 3), 128, 0, st>>>(coef, bg, g, kappa_dev, out_dev);
     return cudaGetLastError();
 }
 

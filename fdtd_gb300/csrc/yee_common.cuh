@@ -2,8 +2,14 @@
 //
 // e_update / h_update compute one node's three E (or H) components from a neighbourhood struct
 // that the caller fills, from global memory (two-pass schedule) or from shared-memory plane tiles
-// (fused sweep). The coefficient reconstruction, the masks, the lumped-element override, the CPML
+// (fused sweep). Coefficient reconstruction, masks, the lumped-element override, the CPML
 // recurrences and every rounding step live here only, so all schedules produce identical bits.
+//
+// The function is written so that the common case costs little and the special cases diverge per
+// component only: an edge whose surrounding cells hold one material takes its coefficients from
+// the material table (the reference's averaging formula, with its divisions, runs only at material
+// interfaces); in CPML slabs filled with the background material the kappa-divided coefficient
+// comes from a per-axis table; components a boundary mask excludes keep their old value.
 #pragma once
 
 #include "fdtd_device.cuh"
@@ -14,57 +20,101 @@ namespace fdtd {
 // fdtdrav.h:1860, 1912, 1960, 1993, 2059, 2107).
 __device__ __forceinline__ bool in_slab(int q, int n, int pn, int pp) { return q < pn || q >= n - pp; }
 
-// Slab index of psi for node (i,j,k) on the x / y / z faces; `side` = 0 on the n face, 1 on the p face.
-__device__ __forceinline__ long long psi_index_x(const DeviceGrid& g, int i, int j, int k, int& side) {
-    if (i < g.pxn) { side = 0; return ((long long)k * g.ny + j) * g.pxn + i; }
+// Offset of psi for node (i,j,k) in the x / y / z face slabs; `side` = 0 on the n face, 1 on the p face.
+__device__ __forceinline__ int psi_off_x(const DeviceGrid& g, int i, int j, int k, int& side) {
+    if (i < g.pxn) { side = 0; return (k * g.ny + j) * g.pxn + i; }
     side = 1;
-    return ((long long)k * g.ny + j) * g.pxp + (i - (g.nx - g.pxp));
+    return (k * g.ny + j) * g.pxp + (i - (g.nx - g.pxp));
 }
-__device__ __forceinline__ long long psi_index_y(const DeviceGrid& g, int i, int j, int k, int& side) {
-    if (j < g.pyn) { side = 0; return ((long long)k * g.pyn + j) * g.pitch + i; }
+__device__ __forceinline__ int psi_off_y(const DeviceGrid& g, int i, int j, int k, int& side) {
+    if (j < g.pyn) { side = 0; return (k * g.pyn + j) * g.pitch + i; }
     side = 1;
-    return ((long long)k * g.pyp + (j - (g.ny - g.pyp))) * g.pitch + i;
+    return (k * g.pyp + (j - (g.ny - g.pyp))) * g.pitch + i;
 }
-__device__ __forceinline__ long long psi_index_z(const DeviceGrid& g, int i, int j, int k, int& side) {
-    if (k < g.pzn) { side = 0; return ((long long)k * g.ny + j) * g.pitch + i; }
+__device__ __forceinline__ int psi_off_z(const DeviceGrid& g, int i, int j, int k, int& side) {
+    if (k < g.pzn) { side = 0; return (k * g.ny + j) * g.pitch + i; }
     side = 1;
-    return ((long long)(k - (g.nz - g.pzp)) * g.ny + j) * g.pitch + i;
+    return ((k - (g.nz - g.pzp)) * g.ny + j) * g.pitch + i;
 }
 
-// E-edge coefficients from the four cells around the edge, in the reference's summation order
-// (setSigmaEpsSigmaMu fdtdrav.h:1135, 1153, 1170). comp: 0 = Ex, 1 = Ey, 2 = Ez.
-__device__ __forceinline__ Coef3 e_coef(const StepParams& p, int comp, int m0, int m1, int m2, int m3) {
-    if (m0 == m1 && m0 == m2 && m0 == m3) {
-        const float* c = p.coef[m0].e[comp];
-        return Coef3{__ldg(c), __ldg(c + 1), __ldg(c + 2)};
+// Coefficients of an edge between different materials: the edge averages of setSigmaEpsSigmaMu
+// (fdtdrav.h:1135, 1153, 1170, reference summation order) and setCoefficients' expressions. Out of
+// line with scalar arguments: it runs only at material interfaces and keeps its divisions out of
+// the hot loop's instruction footprint.
+static __device__ __noinline__ Coef3 e_coef_mixed(const MatProps* props, int m0, int m1, int m2, int m3, float dt,
+                                                  float eps0, float dp, float dm) {
+    const MatProps a = props[m0], b = props[m1], c = props[m2], d = props[m3];
+    return coef3(avg4(a.eps, b.eps, c.eps, d.eps), avg4(a.sig, b.sig, c.sig, d.sig), dt, eps0, dp, dm);
+}
+// Harmonic means of two cells for an H face (fdtdrav.h:1183-1213).
+static __device__ __noinline__ Coef3 h_coef_mixed(const MatProps* props, int m0, int m1, float dt, float mu0,
+                                                  float dp, float dm) {
+    const MatProps a = props[m0], b = props[m1];
+    return coef3(harm2(a.mu, b.mu), harm2(a.sigm, b.sigm), dt, mu0, dp, dm);
+}
+// A curl coefficient divided by the CPML kappa (setABCPML, fdtdrav.h:1903-1906 and mirrors).
+static __device__ __noinline__ float kappa_div(float c, float kappa) { return __fdiv_rn(c, kappa); }
+
+// E-edge coefficients (setCoefficients, fdtdrav.h:1280-1303). `uni`: the four cells around the
+// edge hold material m0, so the table entry applies. comp: 0 = Ex, 1 = Ey, 2 = Ez; the Cb cell
+// sizes are Ex (dy, dz), Ey (dz, dx), Ez (dx, dy).
+__device__ __forceinline__ Coef3 e_coef(const StepParams& p, int comp, bool uni, int m0, int m1, int m2, int m3) {
+    if (uni) {
+        const float4 c = __ldg(&p.coef[m0].e[comp]);
+        return Coef3{c.x, c.y, c.z};
     }
-    const MatProps a = p.props[m0], b = p.props[m1], c = p.props[m2], d = p.props[m3];
-    const float eps = avg4(a.eps, b.eps, c.eps, d.eps);
-    const float sig = avg4(a.sig, b.sig, c.sig, d.sig);
     const DeviceGrid& g = p.g;
-    // (Cb_plus, Cb_minus) cell sizes: Ex (dy, dz), Ey (dz, dx), Ez (dx, dy) (fdtdrav.h:1280-1303)
     const float dp = comp == 0 ? g.dy : comp == 1 ? g.dz : g.dx;
     const float dm = comp == 0 ? g.dz : comp == 1 ? g.dx : g.dy;
-    return coef3(eps, sig, g.dt, g.eps0, dp, dm);
+    return e_coef_mixed(p.props, m0, m1, m2, m3, g.dt, g.eps0, dp, dm);
 }
 
-// H-face coefficients from the two cells sharing the face (harmonic means, fdtdrav.h:1183-1213).
-// `edge` is true on the low face of the axis (i = 0 for Hx, ...), where the reference keeps its
-// initial mu = 1, sigma_m = 1.2e-38.
-__device__ __forceinline__ Coef3 h_coef(const StepParams& p, int comp, bool edge, int m0, int m1) {
-    const int e = edge ? kDefaultEntry : m0;
-    if (edge || m0 == m1) {
-        const float* c = p.coef[e].h[comp];
-        return Coef3{__ldg(c), __ldg(c + 1), __ldg(c + 2)};
+// H-face coefficients (fdtdrav.h:1250-1272). `edge`: the low face of the axis (i = 0 for Hx, ...),
+// where the reference keeps its initial mu = 1, sigma_m = 1.2e-38 (setSigmaEpsSigmaMu masks,
+// fdtdrav.h:1181-1213); `uni`: both cells hold m0. Cb cell sizes: Hx (dz, dy), Hy (dx, dz), Hz (dy, dx).
+__device__ __forceinline__ Coef3 h_coef(const StepParams& p, int comp, bool edge, bool uni, int m0, int m1) {
+    if (edge || uni) {
+        const float4 c = __ldg(&p.coef[edge ? kDefaultEntry : m0].h[comp]);
+        return Coef3{c.x, c.y, c.z};
     }
-    const MatProps a = p.props[m0], b = p.props[m1];
-    const float mu = harm2(a.mu, b.mu);
-    const float sm = harm2(a.sigm, b.sigm);
     const DeviceGrid& g = p.g;
-    // Hx (dz, dy), Hy (dx, dz), Hz (dy, dx) (fdtdrav.h:1250-1272)
     const float dp = comp == 0 ? g.dz : comp == 1 ? g.dx : g.dy;
     const float dm = comp == 0 ? g.dy : comp == 1 ? g.dz : g.dx;
-    return coef3(mu, sm, g.dt, g.mu0, dp, dm);
+    return h_coef_mixed(p.props, m0, m1, g.dt, g.mu0, dp, dm);
+}
+
+// Curl coefficient divided by the CPML kappa of its derivative axis. `bg_ok`: the coefficient is
+// the table entry of the background material, whose divided values are tabulated per node (same
+// division); otherwise divide here.
+__device__ __forceinline__ float kdiv(float c, bool bg_ok, const float* bg_table, const float* kappa, int q) {
+    return bg_ok ? __ldg(bg_table + q) : kappa_div(c, __ldg(kappa + q));
+}
+
+// Interior range of an axis: nodes that are neither on the two boundary planes nor in a CPML slab.
+__device__ __forceinline__ bool interior(int q, int n, int pn, int pp) {
+    return q >= (pn > 1 ? pn : 1) && q <= (n - 1 - pp < n - 2 ? n - 1 - pp : n - 2);
+}
+
+// Interior fast path: a node with every component updated, outside every CPML slab and lumped
+// edge, whose surrounding cells all hold one material: table coefficients, no corrections.
+// Same bits as e_update / h_update for such nodes.
+__device__ __forceinline__ void e_update_interior(const StepParams& p, int m0, float ex, float ey, float ez,
+                                                  float dHz_j, float dHy_k, float dHx_k, float dHz_i, float dHy_i,
+                                                  float dHx_j, float out[3]) {
+    const MatCoef* mc = p.coef + m0;
+    const float4 a = __ldg(&mc->e[0]), b = __ldg(&mc->e[1]), c = __ldg(&mc->e[2]);
+    out[0] = upd3(a.x, ex, a.y, dHz_j, a.z, dHy_k);
+    out[1] = upd3(b.x, ey, b.y, dHx_k, b.z, dHz_i);
+    out[2] = upd3(c.x, ez, c.y, dHy_i, c.z, dHx_j);
+}
+__device__ __forceinline__ void h_update_interior(const StepParams& p, int m0, float hx, float hy, float hz,
+                                                  float dEy_k, float dEz_j, float dEz_i, float dEx_k, float dEx_j,
+                                                  float dEy_i, float out[3]) {
+    const MatCoef* mc = p.coef + m0;
+    const float4 a = __ldg(&mc->h[0]), b = __ldg(&mc->h[1]), c = __ldg(&mc->h[2]);
+    out[0] = upd3_hx(a.x, hx, a.y, dEy_k, a.z, dEz_j);
+    out[1] = upd3(b.x, hy, b.y, dEz_i, b.z, dEx_k);
+    out[2] = upd3(c.x, hz, c.y, dEx_j, c.z, dEy_i);
 }
 
 // Lumped-edge override for node (i,j) among the edges bucketed in plane k.
@@ -108,6 +158,23 @@ struct HNbr {
     int m0, mi, mj, mk;  // cells (i,j,k) (i-1,j,k) (i,j-1,k) (i,j,k-1)
 };
 
+__device__ __forceinline__ bool e_uniform(const ENbr& n) {
+    return n.m0 == n.mi && n.m0 == n.mj && n.m0 == n.mk && n.m0 == n.mij && n.m0 == n.mik && n.m0 == n.mjk;
+}
+__device__ __forceinline__ bool h_uniform(const HNbr& n) { return n.m0 == n.mi && n.m0 == n.mj && n.m0 == n.mk; }
+
+// The interior fast paths applied to a filled neighbourhood.
+__device__ __forceinline__ void e_update_interior(const StepParams& p, const ENbr& n, float out[3]) {
+    e_update_interior(p, n.m0, n.ex, n.ey, n.ez, __fsub_rn(n.hz, n.hz_jm), __fsub_rn(n.hy, n.hy_km),
+                      __fsub_rn(n.hx, n.hx_km), __fsub_rn(n.hz, n.hz_im), __fsub_rn(n.hy, n.hy_im),
+                      __fsub_rn(n.hx, n.hx_jm), out);
+}
+__device__ __forceinline__ void h_update_interior(const StepParams& p, const HNbr& n, float out[3]) {
+    h_update_interior(p, n.m0, n.hx, n.hy, n.hz, __fsub_rn(n.ey_kp, n.ey), __fsub_rn(n.ez_jp, n.ez),
+                      __fsub_rn(n.ez_ip, n.ez), __fsub_rn(n.ex_kp, n.ex), __fsub_rn(n.ex_jp, n.ex),
+                      __fsub_rn(n.ey_ip, n.ey), out);
+}
+
 // CPML memory of one time level: read from `in`, written to `out` (the same set for in-place
 // schedules). write = false computes with the old psi without storing (halo recomputation).
 struct PsiIO {
@@ -117,203 +184,144 @@ struct PsiIO {
 };
 
 template <bool kHyz = false>
-__device__ __forceinline__ float psi_step(const float* in, float* out, long long q, bool write,
+__device__ __forceinline__ float psi_step(const float* in, float* out, int q, bool write,
                                           float b, float a, float d, float f, float cpsi) {
-    const float s = kHyz ? psi_upd_hyz(b, in[q], a, d) : psi_upd(b, in[q], a, d);
+    const float s = kHyz ? psi_upd_hyz(b, __ldg(in + q), a, d) : psi_upd(b, __ldg(in + q), a, d);
     if (write) out[q] = s;
     return psi_add(f, cpsi, s);
 }
 
-// Fast path for an E node strictly inside the grid, outside every CPML slab and lumped element,
-// whose seven surrounding cells hold one material m: every coefficient is the table entry of m and
-// no correction follows the main update. Gives the same bits as e_update for such a node.
-__device__ __forceinline__ bool e_fast_ok(const ENbr& n) {
-    return n.m0 == n.mi && n.m0 == n.mj && n.m0 == n.mk && n.m0 == n.mij && n.m0 == n.mik && n.m0 == n.mjk;
-}
-__device__ __forceinline__ void e_update_fast(const StepParams& p, const ENbr& n, float out[3]) {
-    const float* c = p.coef[n.m0].e[0];
-    out[0] = upd3(__ldg(c + 0), n.ex, __ldg(c + 1), __fsub_rn(n.hz, n.hz_jm), __ldg(c + 2), __fsub_rn(n.hy, n.hy_km));
-    out[1] = upd3(__ldg(c + 3), n.ey, __ldg(c + 4), __fsub_rn(n.hx, n.hx_km), __ldg(c + 5), __fsub_rn(n.hz, n.hz_im));
-    out[2] = upd3(__ldg(c + 6), n.ez, __ldg(c + 7), __fsub_rn(n.hy, n.hy_im), __ldg(c + 8), __fsub_rn(n.hx, n.hx_jm));
-}
-// Same for an H node with i, j, k >= 1 (no reference-default faces) and four equal cells.
-__device__ __forceinline__ bool h_fast_ok(const HNbr& n) { return n.m0 == n.mi && n.m0 == n.mj && n.m0 == n.mk; }
-__device__ __forceinline__ void h_update_fast(const StepParams& p, const HNbr& n, float out[3]) {
-    const float* c = p.coef[n.m0].h[0];
-    out[0] = upd3_hx(__ldg(c + 0), n.hx, __ldg(c + 1), __fsub_rn(n.ey_kp, n.ey), __ldg(c + 2), __fsub_rn(n.ez_jp, n.ez));
-    out[1] = upd3(__ldg(c + 3), n.hy, __ldg(c + 4), __fsub_rn(n.ez_ip, n.ez), __ldg(c + 5), __fsub_rn(n.ex_kp, n.ex));
-    out[2] = upd3(__ldg(c + 6), n.hz, __ldg(c + 7), __fsub_rn(n.ex_jp, n.ex), __ldg(c + 8), __fsub_rn(n.ey_ip, n.ey));
-}
-
-// One E node (calc_e fdtdrav.h:577-915): main updates with masks and the lumped override, then the
-// CPML corrections in the reference's order (x, y, z per component). pre[] receives the values
-// between the main update and the CPML corrections (the sampleField values).
+// One E node (calc_e fdtdrav.h:577-915): main updates with their masks and the lumped override,
+// then the CPML corrections in the reference's order (x, y, z). pre[] receives the values between
+// the main update and the CPML corrections (the sampleField values, fdtdrav.h:740).
+// plane_lumped: some lumped edge lies in plane k (uniform across a CTA).
 __device__ __forceinline__ void e_update(const StepParams& p, const ENbr& n, int i, int j, int k, long long m,
-                                         const PsiIO& ps, float out[3], float pre[3]) {
+                                         bool plane_lumped, const PsiIO& ps, float out[3], float pre[3]) {
     const DeviceGrid& g = p.g;
-    out[0] = n.ex; out[1] = n.ey; out[2] = n.ez;
-    pre[0] = n.ex; pre[1] = n.ey; pre[2] = n.ez;
     const bool in_x = i > 0 && i < g.nx - 1, in_y = j > 0 && j < g.ny - 1, in_z = k > 0 && k < g.nz - 1;
-    const bool ex_m = i < g.nx - 1 && in_y && in_z;
-    const bool ey_m = in_x && j < g.ny - 1 && in_z;
-    const bool ez_m = in_x && in_y && k < g.nz - 1;
-    if (!(ex_m || ey_m || ez_m)) return;
+    const bool ex_m = i < g.nx - 1 && in_y && in_z;  // fdtdrav.h:665
+    const bool ey_m = in_x && j < g.ny - 1 && in_z;  // fdtdrav.h:696
+    const bool ez_m = in_x && in_y && k < g.nz - 1;  // fdtdrav.h:720
     const bool xs = in_slab(i, g.nx, g.pxn, g.pxp);
     const bool ys = in_slab(j, g.ny, g.pyn, g.pyp);
     const bool zs = in_slab(k, g.nz, g.pzn, g.pzp);
-    int side;
-    if (ex_m) {  // Ex (fdtdrav.h:665-676); CPML y (790-808) then z (829-850)
-        const Coef3 c = e_coef(p, 0, n.m0, n.mj, n.mk, n.mjk);
-        float cy = c.bp, cz = c.bm;
-        if (ys) cy = __fdiv_rn(c.bp, p.key[j]);
-        if (zs) cz = __fdiv_rn(c.bm, p.kez[k]);
-        const float dHz = __fsub_rn(n.hz, n.hz_jm);
-        const float dHy = __fsub_rn(n.hy, n.hy_km);
-        float v = upd3(c.a, n.ex, cy, dHz, cz, dHy);
-        pre[0] = v;
-        if (ys) {
-            const long long q = psi_index_y(g, i, j, k, side);
-            v = psi_step(ps.in[2 + side].e[0], ps.out[2 + side].e[0], q, ps.write, p.bey[j], p.aey[j], dHz, v,
-                         __fmul_rn(c.bp, g.dy));
-        }
-        if (zs) {
-            const long long q = psi_index_z(g, i, j, k, side);
-            v = psi_step(ps.in[4 + side].e[0], ps.out[4 + side].e[0], q, ps.write, p.bez[k], p.aez[k], dHy, v,
-                         __fmul_rn(c.bm, g.dz));
-        }
-        out[0] = v;
-    }
-    if (ey_m) {  // Ey (fdtdrav.h:696-707); CPML x then z
-        const Coef3 c = e_coef(p, 1, n.m0, n.mi, n.mk, n.mik);
-        float cz = c.bp, cx = c.bm;
-        if (zs) cz = __fdiv_rn(c.bp, p.kez[k]);
-        if (xs) cx = __fdiv_rn(c.bm, p.kex[i]);
-        const float dHx = __fsub_rn(n.hx, n.hx_km);
-        const float dHz = __fsub_rn(n.hz, n.hz_im);
-        float v = upd3(c.a, n.ey, cz, dHx, cx, dHz);
-        pre[1] = v;
-        if (xs) {
-            const long long q = psi_index_x(g, i, j, k, side);
-            v = psi_step(ps.in[side].e[0], ps.out[side].e[0], q, ps.write, p.bex[i], p.aex[i], dHz, v,
-                         __fmul_rn(c.bm, g.dx));
-        }
-        if (zs) {
-            const long long q = psi_index_z(g, i, j, k, side);
-            v = psi_step(ps.in[4 + side].e[1], ps.out[4 + side].e[1], q, ps.write, p.bez[k], p.aez[k], dHx, v,
-                         __fmul_rn(c.bp, g.dz));
-        }
-        out[1] = v;
-    }
-    if (ez_m) {  // Ez with lumped elements (fdtdrav.h:720-741); CPML x then y
-        const Coef3 c = e_coef(p, 2, n.m0, n.mi, n.mj, n.mij);
-        float cx = c.bp, cy = c.bm;
-        if (xs) cx = __fdiv_rn(c.bp, p.kex[i]);
-        if (ys) cy = __fdiv_rn(c.bm, p.key[j]);
-        const float dHy = __fsub_rn(n.hy, n.hy_im);
-        const float dHx = __fsub_rn(n.hx, n.hx_jm);
-        float v;
-        const LumpedEdge* L = (p.lumped_k[k] < p.lumped_k[k + 1]) ? find_lumped(p, i, j, k) : nullptr;
-        if (L) {
-            if (L->source >= 0) {
-                const float s = m < p.wave_len[L->source] ? p.waves[L->source][m] : 0.f;
-                v = upd4(L->ceze, n.ez, L->cezhy, dHy, L->cezhx, dHx, L->cezj, s);
-            } else {
-                v = upd3(L->ceze, n.ez, L->cezhy, dHy, L->cezhx, dHx);
-            }
+    const int bg = p.bg.mat;
+    const bool ux = n.m0 == n.mj && n.m0 == n.mk && n.m0 == n.mjk;
+    const bool uy = n.m0 == n.mi && n.m0 == n.mk && n.m0 == n.mik;
+    const bool uz = n.m0 == n.mi && n.m0 == n.mj && n.m0 == n.mij;
+    const Coef3 cx = e_coef(p, 0, ux, n.m0, n.mj, n.mk, n.mjk);
+    const Coef3 cy = e_coef(p, 1, uy, n.m0, n.mi, n.mk, n.mik);
+    const Coef3 cz = e_coef(p, 2, uz, n.m0, n.mi, n.mj, n.mij);
+    const float dHz_j = __fsub_rn(n.hz, n.hz_jm), dHy_k = __fsub_rn(n.hy, n.hy_km);
+    const float dHx_k = __fsub_rn(n.hx, n.hx_km), dHz_i = __fsub_rn(n.hz, n.hz_im);
+    const float dHy_i = __fsub_rn(n.hy, n.hy_im), dHx_j = __fsub_rn(n.hx, n.hx_jm);
+    const BgCurl& B = p.bg;
+    // Ex (fdtdrav.h:665-676)
+    float vx = upd3(cx.a, n.ex, ys ? kdiv(cx.bp, ux && n.m0 == bg, B.e[1][0], p.key, j) : cx.bp, dHz_j,
+                    zs ? kdiv(cx.bm, ux && n.m0 == bg, B.e[2][0], p.kez, k) : cx.bm, dHy_k);
+    // Ey (fdtdrav.h:696-707)
+    float vy = upd3(cy.a, n.ey, zs ? kdiv(cy.bp, uy && n.m0 == bg, B.e[2][1], p.kez, k) : cy.bp, dHx_k,
+                    xs ? kdiv(cy.bm, uy && n.m0 == bg, B.e[0][0], p.kex, i) : cy.bm, dHz_i);
+    // Ez with lumped elements (fdtdrav.h:720-741)
+    float vz;
+    const LumpedEdge* L = plane_lumped ? find_lumped(p, i, j, k) : nullptr;
+    if (L) {
+        if (L->source >= 0) {
+            const float s = m < p.wave_len[L->source] ? p.waves[L->source][m] : 0.f;
+            vz = upd4(L->ceze, n.ez, L->cezhy, dHy_i, L->cezhx, dHx_j, L->cezj, s);
         } else {
-            v = upd3(c.a, n.ez, cx, dHy, cy, dHx);
+            vz = upd3(L->ceze, n.ez, L->cezhy, dHy_i, L->cezhx, dHx_j);
         }
-        pre[2] = v;
-        if (xs) {
-            const long long q = psi_index_x(g, i, j, k, side);
-            v = psi_step(ps.in[side].e[1], ps.out[side].e[1], q, ps.write, p.bex[i], p.aex[i], dHy, v,
-                         __fmul_rn(c.bp, g.dx));
-        }
-        if (ys) {
-            const long long q = psi_index_y(g, i, j, k, side);
-            v = psi_step(ps.in[2 + side].e[1], ps.out[2 + side].e[1], q, ps.write, p.bey[j], p.aey[j], dHx, v,
-                         __fmul_rn(c.bm, g.dy));
-        }
-        out[2] = v;
+    } else {
+        vz = upd3(cz.a, n.ez, xs ? kdiv(cz.bp, uz && n.m0 == bg, B.e[0][1], p.kex, i) : cz.bp, dHy_i,
+                  ys ? kdiv(cz.bm, uz && n.m0 == bg, B.e[1][1], p.key, j) : cz.bm, dHx_j);
     }
+    pre[0] = ex_m ? vx : n.ex;
+    pre[1] = ey_m ? vy : n.ey;
+    pre[2] = ez_m ? vz : n.ez;
+    int side;
+    // CPML, per component in the reference's block order: x (fdtdrav.h:752-785), y (790-827),
+    // z (829-911). The psi regions of the reference equal the component masks restricted to the
+    // slabs, so psi is updated exactly where a correction is applied.
+    if (xs && (ey_m || ez_m)) {
+        const int q = psi_off_x(g, i, j, k, side);
+        const float bb = __ldg(p.bex + i), aa = __ldg(p.aex + i);
+        if (ey_m) vy = psi_step(ps.in[side].e[0], ps.out[side].e[0], q, ps.write, bb, aa, dHz_i, vy, __fmul_rn(cy.bm, g.dx));
+        if (ez_m) vz = psi_step(ps.in[side].e[1], ps.out[side].e[1], q, ps.write, bb, aa, dHy_i, vz, __fmul_rn(cz.bp, g.dx));
+    }
+    if (ys && (ex_m || ez_m)) {
+        const int q = psi_off_y(g, i, j, k, side);
+        const float bb = __ldg(p.bey + j), aa = __ldg(p.aey + j);
+        if (ex_m) vx = psi_step(ps.in[2 + side].e[0], ps.out[2 + side].e[0], q, ps.write, bb, aa, dHz_j, vx, __fmul_rn(cx.bp, g.dy));
+        if (ez_m) vz = psi_step(ps.in[2 + side].e[1], ps.out[2 + side].e[1], q, ps.write, bb, aa, dHx_j, vz, __fmul_rn(cz.bm, g.dy));
+    }
+    if (zs && (ex_m || ey_m)) {
+        const int q = psi_off_z(g, i, j, k, side);
+        const float bb = __ldg(p.bez + k), aa = __ldg(p.aez + k);
+        if (ex_m) vx = psi_step(ps.in[4 + side].e[0], ps.out[4 + side].e[0], q, ps.write, bb, aa, dHy_k, vx, __fmul_rn(cx.bm, g.dz));
+        if (ey_m) vy = psi_step(ps.in[4 + side].e[1], ps.out[4 + side].e[1], q, ps.write, bb, aa, dHx_k, vy, __fmul_rn(cy.bp, g.dz));
+    }
+    out[0] = ex_m ? vx : n.ex;
+    out[1] = ey_m ? vy : n.ey;
+    out[2] = ez_m ? vz : n.ez;
 }
 
 // One H node (calc_h fdtdrav.h:249-573).
 __device__ __forceinline__ void h_update(const StepParams& p, const HNbr& n, int i, int j, int k,
                                          const PsiIO& ps, float out[3], float pre[3]) {
     const DeviceGrid& g = p.g;
-    out[0] = n.hx; out[1] = n.hy; out[2] = n.hz;
-    pre[0] = n.hx; pre[1] = n.hy; pre[2] = n.hz;
-    const bool hx_m = j < g.ny - 1 && k < g.nz - 1;
-    const bool hy_m = i < g.nx - 1 && k < g.nz - 1;
-    const bool hz_m = i < g.nx - 1 && j < g.ny - 1;
+    const bool hx_m = j < g.ny - 1 && k < g.nz - 1;  // fdtdrav.h:328
+    const bool hy_m = i < g.nx - 1 && k < g.nz - 1;  // fdtdrav.h:357
+    const bool hz_m = i < g.nx - 1 && j < g.ny - 1;  // fdtdrav.h:382
     const bool xs = in_slab(i, g.nx, g.pxn, g.pxp);
     const bool ys = in_slab(j, g.ny, g.pyn, g.pyp);
     const bool zs = in_slab(k, g.nz, g.pzn, g.pzp);
+    const int bg = p.bg.mat;
+    const bool ux = n.m0 == n.mi, uy = n.m0 == n.mj, uz = n.m0 == n.mk;
+    const Coef3 cx = h_coef(p, 0, i == 0, ux, n.m0, n.mi);
+    const Coef3 cy = h_coef(p, 1, j == 0, uy, n.m0, n.mj);
+    const Coef3 cz = h_coef(p, 2, k == 0, uz, n.m0, n.mk);
+    // the tabulated kappa-divided values belong to the background material's table entry
+    const bool bx = i != 0 && ux && n.m0 == bg, by = j != 0 && uy && n.m0 == bg, bz = k != 0 && uz && n.m0 == bg;
+    const float dEy_k = __fsub_rn(n.ey_kp, n.ey), dEz_j = __fsub_rn(n.ez_jp, n.ez);
+    const float dEz_i = __fsub_rn(n.ez_ip, n.ez), dEx_k = __fsub_rn(n.ex_kp, n.ex);
+    const float dEx_j = __fsub_rn(n.ex_jp, n.ex), dEy_i = __fsub_rn(n.ey_ip, n.ey);
+    const BgCurl& B = p.bg;
+    // Hx (fdtdrav.h:331-338)
+    float vx = upd3_hx(cx.a, n.hx, zs ? kdiv(cx.bp, bx, B.h[2][0], p.kmz, k) : cx.bp, dEy_k,
+                       ys ? kdiv(cx.bm, bx, B.h[1][0], p.kmy, j) : cx.bm, dEz_j);
+    // Hy (fdtdrav.h:360-366)
+    float vy = upd3(cy.a, n.hy, xs ? kdiv(cy.bp, by, B.h[0][0], p.kmx, i) : cy.bp, dEz_i,
+                    zs ? kdiv(cy.bm, by, B.h[2][1], p.kmz, k) : cy.bm, dEx_k);
+    // Hz (fdtdrav.h:385)
+    float vz = upd3(cz.a, n.hz, ys ? kdiv(cz.bp, bz, B.h[1][1], p.kmy, j) : cz.bp, dEx_j,
+                    xs ? kdiv(cz.bm, bz, B.h[0][1], p.kmx, i) : cz.bm, dEy_i);
+    pre[0] = hx_m ? vx : n.hx;
+    pre[1] = hy_m ? vy : n.hy;
+    pre[2] = hz_m ? vz : n.hz;
     int side;
-    if (hx_m) {  // Hx (fdtdrav.h:328-348); CPML y (445-486) then z (489-528)
-        const Coef3 c = h_coef(p, 0, i == 0, n.m0, n.mi);
-        float cz = c.bp, cy = c.bm;
-        if (zs) cz = __fdiv_rn(c.bp, p.kmz[k]);
-        if (ys) cy = __fdiv_rn(c.bm, p.kmy[j]);
-        const float dEy = __fsub_rn(n.ey_kp, n.ey);
-        const float dEz = __fsub_rn(n.ez_jp, n.ez);
-        float v = upd3_hx(c.a, n.hx, cz, dEy, cy, dEz);
-        pre[0] = v;
-        if (ys) {
-            const long long q = psi_index_y(g, i, j, k, side);
-            v = psi_step(ps.in[2 + side].h[0], ps.out[2 + side].h[0], q, ps.write, p.bmy[j], p.amy[j], dEz, v,
-                         __fmul_rn(c.bm, g.dy));
-        }
-        if (zs) {
-            const long long q = psi_index_z(g, i, j, k, side);
-            v = psi_step(ps.in[4 + side].h[0], ps.out[4 + side].h[0], q, ps.write, p.bmz[k], p.amz[k], dEy, v,
-                         __fmul_rn(c.bp, g.dz));
-        }
-        out[0] = v;
+    // CPML x (fdtdrav.h:401-442), y (445-486), z (489-562)
+    if (xs && (hy_m || hz_m)) {
+        const int q = psi_off_x(g, i, j, k, side);
+        const float bb = __ldg(p.bmx + i), aa = __ldg(p.amx + i);
+        if (hy_m) vy = psi_step(ps.in[side].h[0], ps.out[side].h[0], q, ps.write, bb, aa, dEz_i, vy, __fmul_rn(cy.bp, g.dx));
+        if (hz_m) vz = psi_step(ps.in[side].h[1], ps.out[side].h[1], q, ps.write, bb, aa, dEy_i, vz, __fmul_rn(cz.bm, g.dx));
     }
-    if (hy_m) {  // Hy (fdtdrav.h:357-373); CPML x then z
-        const Coef3 c = h_coef(p, 1, j == 0, n.m0, n.mj);
-        float cx = c.bp, cz = c.bm;
-        if (xs) cx = __fdiv_rn(c.bp, p.kmx[i]);
-        if (zs) cz = __fdiv_rn(c.bm, p.kmz[k]);
-        const float dEz = __fsub_rn(n.ez_ip, n.ez);
-        const float dEx = __fsub_rn(n.ex_kp, n.ex);
-        float v = upd3(c.a, n.hy, cx, dEz, cz, dEx);
-        pre[1] = v;
-        if (xs) {
-            const long long q = psi_index_x(g, i, j, k, side);
-            v = psi_step(ps.in[side].h[0], ps.out[side].h[0], q, ps.write, p.bmx[i], p.amx[i], dEz, v,
-                         __fmul_rn(c.bp, g.dx));
-        }
-        if (zs) {
-            const long long q = psi_index_z(g, i, j, k, side);
-            v = psi_step<true>(ps.in[4 + side].h[1], ps.out[4 + side].h[1], q, ps.write, p.bmz[k], p.amz[k], dEx, v,
-                               __fmul_rn(c.bm, g.dz));
-        }
-        out[1] = v;
+    if (ys && (hx_m || hz_m)) {
+        const int q = psi_off_y(g, i, j, k, side);
+        const float bb = __ldg(p.bmy + j), aa = __ldg(p.amy + j);
+        if (hx_m) vx = psi_step(ps.in[2 + side].h[0], ps.out[2 + side].h[0], q, ps.write, bb, aa, dEz_j, vx, __fmul_rn(cx.bm, g.dy));
+        if (hz_m) vz = psi_step(ps.in[2 + side].h[1], ps.out[2 + side].h[1], q, ps.write, bb, aa, dEx_j, vz, __fmul_rn(cz.bp, g.dy));
     }
-    if (hz_m) {  // Hz (fdtdrav.h:382-392); CPML x then y
-        const Coef3 c = h_coef(p, 2, k == 0, n.m0, n.mk);
-        float cy = c.bp, cx = c.bm;
-        if (ys) cy = __fdiv_rn(c.bp, p.kmy[j]);
-        if (xs) cx = __fdiv_rn(c.bm, p.kmx[i]);
-        const float dEx = __fsub_rn(n.ex_jp, n.ex);
-        const float dEy = __fsub_rn(n.ey_ip, n.ey);
-        float v = upd3(c.a, n.hz, cy, dEx, cx, dEy);
-        pre[2] = v;
-        if (xs) {
-            const long long q = psi_index_x(g, i, j, k, side);
-            v = psi_step(ps.in[side].h[1], ps.out[side].h[1], q, ps.write, p.bmx[i], p.amx[i], dEy, v,
-                         __fmul_rn(c.bm, g.dx));
-        }
-        if (ys) {
-            const long long q = psi_index_y(g, i, j, k, side);
-            v = psi_step(ps.in[2 + side].h[1], ps.out[2 + side].h[1], q, ps.write, p.bmy[j], p.amy[j], dEx, v,
-                         __fmul_rn(c.bp, g.dy));
-        }
-        out[2] = v;
+    if (zs && (hx_m || hy_m)) {
+        const int q = psi_off_z(g, i, j, k, side);
+        const float bb = __ldg(p.bmz + k), aa = __ldg(p.amz + k);
+        if (hx_m) vx = psi_step(ps.in[4 + side].h[0], ps.out[4 + side].h[0], q, ps.write, bb, aa, dEy_k, vx, __fmul_rn(cx.bp, g.dz));
+        if (hy_m) vy = psi_step<true>(ps.in[4 + side].h[1], ps.out[4 + side].h[1], q, ps.write, bb, aa, dEx_k, vy, __fmul_rn(cy.bm, g.dz));
     }
+    out[0] = hx_m ? vx : n.hx;
+    out[1] = hy_m ? vy : n.hy;
+    out[2] = hz_m ? vz : n.hz;
 }
 
 }  // namespace fdtd

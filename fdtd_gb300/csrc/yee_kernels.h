@@ -3,6 +3,8 @@
 
 #include <cuda.h>
 
+#include <vector>
+
 #include "fdtd_device.cuh"
 
 namespace fdtd {
@@ -27,12 +29,21 @@ struct FusedMaps {
     CUtensorMap e[3];
     CUtensorMap mat;
 };
+// Work items of one sweep (device arrays of int4 {x0, y0, k0, k1}), split into interior and
+// general items (plan_fused).
+struct FusedWork {
+    const int4* interior;
+    int n_interior;
+    const int4* general;
+    int n_general;
+};
 cudaError_t fused_configure();
 int fused_smem_bytes();
 int fused_tile_x();
 int fused_tile_y();
+void plan_fused(const DeviceGrid& g, int kc, std::vector<int4>& interior_items, std::vector<int4>& general_items);
 cudaError_t launch_fused(const FusedMaps& maps, const StepParams& p, const FieldPtrs& fo, const PsiSet& psi_in,
-                         const PsiSet& psi_out, long long m, int kc, cudaStream_t st);
+                         const PsiSet& psi_out, long long m, const FusedWork& w, cudaStream_t st);
 // encode_fn: the driver's cuTensorMapEncodeTiled. Returns 0 on success.
 int encode_fused_maps(FusedMaps* out, const DeviceGrid& g, float* const h[3], float* const e[3], const uint8_t* mat,
                       void* encode_fn);
@@ -44,6 +55,10 @@ cudaError_t launch_material_tables(const DeviceGrid& g, const MatProps* props, i
 cudaError_t launch_lumped_coefs(const DeviceGrid& g, const uint8_t* mat, const MatProps* props,
                                 LumpedEdge* edges, const int* boxes, const float* resist, const int* owner,
                                 int n_edges, cudaStream_t st);
+// kappa_dev: device array of 6 pointers {kappa_e x, kappa_m x, kappa_e y, kappa_m y, kappa_e z,
+// kappa_m z}; out_dev: device array of 12 pointers, per axis {E slot 0, E slot 1, H slot 0, H slot 1}.
+cudaError_t launch_bg_curl(const DeviceGrid& g, const MatCoef* coef, int bg, const float* const* kappa_dev,
+                           float* const* out_dev, cudaStream_t st);
 cudaError_t launch_fill(float* p, long long n, float v, cudaStream_t st);
 cudaError_t launch_paint(uint8_t* mat, const DeviceGrid& g, const int box[6], uint8_t value, cudaStream_t st);
 

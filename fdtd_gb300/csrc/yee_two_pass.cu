@@ -8,7 +8,8 @@
 
 namespace fdtd {
 
-__global__ void __launch_bounds__(256) k_update_e(StepParams p, FieldPtrs f, PsiSet ps, long long m) {
+__global__ void __launch_bounds__(256) k_update_e(const __grid_constant__ StepParams p, FieldPtrs f,
+                                                  const __grid_constant__ PsiSet ps, long long m) {
     const DeviceGrid& g = p.g;
     const int i = blockIdx.x * 32 + threadIdx.x;
     const int j = blockIdx.y * 8 + threadIdx.y;
@@ -34,15 +35,14 @@ __global__ void __launch_bounds__(256) k_update_e(StepParams p, FieldPtrs f, Psi
     nb.mik = (i > 0 && k > 0) ? mat[n - 1 - P] : 0;
     nb.mjk = (j > 0 && k > 0) ? mat[n - R - P] : 0;
     float out[3], pre[3];
-    const bool fast = i >= 1 && i <= g.nx - 2 && j >= 1 && j <= g.ny - 2 && k >= 1 && k <= g.nz - 2 &&
-                      !in_slab(i, g.nx, g.pxn, g.pxp) && !in_slab(j, g.ny, g.pyn, g.pyp) &&
-                      !in_slab(k, g.nz, g.pzn, g.pzp) && p.lumped_k[k] == p.lumped_k[k + 1] && e_fast_ok(nb);
-    if (fast) {
-        e_update_fast(p, nb, out);
+    const PsiIO io{ps.f, ps.f, true};
+    const bool plane_lumped = p.lumped_k[k] < p.lumped_k[k + 1];
+    if (!plane_lumped && interior(i, g.nx, g.pxn, g.pxp) && interior(j, g.ny, g.pyn, g.pyp) &&
+        interior(k, g.nz, g.pzn, g.pzp) && e_uniform(nb)) {
+        e_update_interior(p, nb, out);
         pre[0] = out[0]; pre[1] = out[1]; pre[2] = out[2];
     } else {
-        const PsiIO io{ps.f, ps.f, true};
-        e_update(p, nb, i, j, k, m, io, out, pre);
+        e_update(p, nb, i, j, k, m, plane_lumped, io, out, pre);
     }
     f.ex[n] = out[0]; f.ey[n] = out[1]; f.ez[n] = out[2];
     if (p.probe_k[k] < p.probe_k[k + 1]) {
@@ -51,7 +51,8 @@ __global__ void __launch_bounds__(256) k_update_e(StepParams p, FieldPtrs f, Psi
     }
 }
 
-__global__ void __launch_bounds__(256) k_update_h(StepParams p, FieldPtrs f, PsiSet ps, long long m) {
+__global__ void __launch_bounds__(256) k_update_h(const __grid_constant__ StepParams p, FieldPtrs f,
+                                                  const __grid_constant__ PsiSet ps, long long m) {
     const DeviceGrid& g = p.g;
     const int i = blockIdx.x * 32 + threadIdx.x;
     const int j = blockIdx.y * 8 + threadIdx.y;
@@ -74,14 +75,12 @@ __global__ void __launch_bounds__(256) k_update_h(StepParams p, FieldPtrs f, Psi
     nb.mj = j > 0 ? mat[n - R] : 0;
     nb.mk = k > 0 ? mat[n - P] : 0;
     float out[3], pre[3];
-    const bool fast = i >= 1 && i <= g.nx - 2 && j >= 1 && j <= g.ny - 2 && k >= 1 && k <= g.nz - 2 &&
-                      !in_slab(i, g.nx, g.pxn, g.pxp) && !in_slab(j, g.ny, g.pyn, g.pyp) &&
-                      !in_slab(k, g.nz, g.pzn, g.pzp) && h_fast_ok(nb);
-    if (fast) {
-        h_update_fast(p, nb, out);
+    const PsiIO io{ps.f, ps.f, true};
+    if (interior(i, g.nx, g.pxn, g.pxp) && interior(j, g.ny, g.pyn, g.pyp) && interior(k, g.nz, g.pzn, g.pzp) &&
+        h_uniform(nb)) {
+        h_update_interior(p, nb, out);
         pre[0] = out[0]; pre[1] = out[1]; pre[2] = out[2];
     } else {
-        const PsiIO io{ps.f, ps.f, true};
         h_update(p, nb, i, j, k, io, out, pre);
     }
     f.hx[n] = out[0]; f.hy[n] = out[1]; f.hz[n] = out[2];

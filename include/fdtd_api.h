@@ -36,7 +36,7 @@ enum { FDTD_EX = 0, FDTD_EY = 1, FDTD_EZ = 2, FDTD_HX = 3, FDTD_HY = 4, FDTD_HZ 
 
 /* Update-kernel schedules (fdtd_set_schedule). */
 enum {
-    FDTD_SCHEDULE_AUTO = 0,   /* fused sweep when the grid allows it, otherwise two passes   */
+    FDTD_SCHEDULE_AUTO = 0,   /* the fastest schedule measured on GB300: currently two passes */
     FDTD_SCHEDULE_TWO_PASS = 1, /* E pass then H pass per step, in place (the reference's order) */
     FDTD_SCHEDULE_FUSED = 2   /* one z-marching sweep per step over ping-pong field buffers   */
 };

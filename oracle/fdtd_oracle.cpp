@@ -62,6 +62,10 @@ typedef struct {
     // optional 1-D profile override: 18 arrays, per axis x, y, z: b_e, a_e, b_m, a_m, kappa_e,
     // kappa_m (length n_axis); NULL entries keep the oracle's own values
     const float* const* profile_override;
+    // optional design region: cells [d0,d3) x [d1,d4) x [d2,d5) take eps_r from design_eps
+    // ((d5-d2), (d4-d1), (d3-d0) array, x fastest) instead of the material table
+    int design_box[6];
+    const double* design_eps;
 } or_scenario;
 
 const char* or_error(void) { return g_err.c_str(); }
@@ -158,6 +162,13 @@ int setup(Sim<R>& s, const or_scenario* sc, const float* signal_per_node, int n_
     for (size_t n = 0; n < N; ++n) {
         const float* t = sc->table + 4 * sc->mat[n];
         ceps[n] = t[0]; csig[n] = t[1]; cmu[n] = t[2]; csm[n] = t[3];
+    }
+    if (sc->design_eps) {
+        const int* d = sc->design_box;
+        for (int k = d[2]; k < d[5]; ++k)
+            for (int j = d[1]; j < d[4]; ++j)
+                for (int i = d[0]; i < d[3]; ++i)
+                    ceps[s.id(i, j, k)] = (R)sc->design_eps[((size_t)(k - d[2]) * (d[4] - d[1]) + (j - d[1])) * (d[3] - d[0]) + (i - d[0])];
     }
     s.eps_x.assign(N, 1); s.eps_y.assign(N, 1); s.eps_z.assign(N, 1);
     s.mu_x.assign(N, 1); s.mu_y.assign(N, 1); s.mu_z.assign(N, 1);
@@ -451,9 +462,218 @@ int run(const or_scenario* sc, int steps, const float* signal_per_node, int n_si
     return 0;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Discrete adjoint of the update above (the reference has none; this is the checker of the GPU
+// adjoint). Figure of merit J = sum_m dt * Ez(p)^2 over the samples of steps m = 0..N-1 at an Ez
+// probe outside the CPML. The adjoint state holds dJ/d(field) and dJ/d(psi) at a point of the
+// forward sequence; reverse_h undoes calc_h, reverse_e undoes calc_e (transposes of the exact
+// linear maps, CPML recurrences and lumped-edge coefficients included).
+// ---------------------------------------------------------------------------------------------
+
+template <class R>
+struct Adj {
+    std::vector<R> ex, ey, ez, hx, hy, hz;
+    std::vector<R> psi_eyx, psi_ezx, psi_exy, psi_ezy, psi_exz, psi_eyz;
+    std::vector<R> psi_hyx, psi_hzx, psi_hxy, psi_hzy, psi_hxz, psi_hyz;
+    explicit Adj(size_t N) {
+        for (std::vector<R>* v : {&ex, &ey, &ez, &hx, &hy, &hz, &psi_eyx, &psi_ezx, &psi_exy, &psi_ezy, &psi_exz, &psi_eyz,
+                                  &psi_hyx, &psi_hzx, &psi_hxy, &psi_hzy, &psi_hxz, &psi_hyz})
+            v->assign(N, (R)0);
+    }
+};
+
+template <class R>
+void reverse_h(const Sim<R>& s, Adj<R>& a) {
+    const int NX = s.NX, NY = s.NY, NZ = s.NZ;
+    const size_t sx = 1, sy = (size_t)NX, sz = (size_t)NX * NY;
+    for (int k = 0; k < NZ; ++k)
+        for (int j = 0; j < NY; ++j)
+            for (int i = 0; i < NX; ++i) {
+                const size_t n = s.id(i, j, k);
+                const bool xs = (i < s.pxn) || (i > NX - s.pxp - 1 && i < NX - 1);
+                const bool ys = (j < s.pyn) || (j > NY - s.pyp - 1 && j < NY - 1);
+                const bool zs = (k < s.pzn) || (k > NZ - s.pzp - 1 && k < NZ - 1);
+                if (j < NY - 1 && k < NZ - 1) {  // Hx
+                    const R L = a.hx[n];
+                    const R my = ys ? a.psi_hxy[n] + s.cpsi_hxy[n] * L : 0;
+                    const R mz = zs ? a.psi_hxz[n] + s.cpsi_hxz[n] * L : 0;
+                    if (ys) a.psi_hxy[n] = s.b_my[j] * my;
+                    if (zs) a.psi_hxz[n] = s.b_mz[k] * mz;
+                    const R gy = s.Chxey[n] * L + (zs ? s.a_mz[k] * mz : 0);
+                    const R gz = s.Chxez[n] * L + (ys ? s.a_my[j] * my : 0);
+                    a.ey[n + sz] += gy; a.ey[n] -= gy;
+                    a.ez[n + sy] += gz; a.ez[n] -= gz;
+                    a.hx[n] = s.Chxh[n] * L;
+                }
+                if (i < NX - 1 && k < NZ - 1) {  // Hy
+                    const R L = a.hy[n];
+                    const R mx = xs ? a.psi_hyx[n] + s.cpsi_hyx[n] * L : 0;
+                    const R mz = zs ? a.psi_hyz[n] + s.cpsi_hyz[n] * L : 0;
+                    if (xs) a.psi_hyx[n] = s.b_mx[i] * mx;
+                    if (zs) a.psi_hyz[n] = s.b_mz[k] * mz;
+                    const R gz = s.Chyez[n] * L + (xs ? s.a_mx[i] * mx : 0);
+                    const R gx = s.Chyex[n] * L + (zs ? s.a_mz[k] * mz : 0);
+                    a.ez[n + sx] += gz; a.ez[n] -= gz;
+                    a.ex[n + sz] += gx; a.ex[n] -= gx;
+                    a.hy[n] = s.Chyh[n] * L;
+                }
+                if (i < NX - 1 && j < NY - 1) {  // Hz
+                    const R L = a.hz[n];
+                    const R mx = xs ? a.psi_hzx[n] + s.cpsi_hzx[n] * L : 0;
+                    const R my = ys ? a.psi_hzy[n] + s.cpsi_hzy[n] * L : 0;
+                    if (xs) a.psi_hzx[n] = s.b_mx[i] * mx;
+                    if (ys) a.psi_hzy[n] = s.b_my[j] * my;
+                    const R gx = s.Chzex[n] * L + (ys ? s.a_my[j] * my : 0);
+                    const R gy = s.Chzey[n] * L + (xs ? s.a_mx[i] * mx : 0);
+                    a.ex[n + sy] += gx; a.ex[n] -= gx;
+                    a.ey[n + sx] += gy; a.ey[n] -= gy;
+                    a.hz[n] = s.Chzh[n] * L;
+                }
+            }
+}
+
+template <class R>
+void reverse_e(const Sim<R>& s, Adj<R>& a) {
+    const int NX = s.NX, NY = s.NY, NZ = s.NZ;
+    const size_t sx = 1, sy = (size_t)NX, sz = (size_t)NX * NY;
+    for (int k = 0; k < NZ; ++k)
+        for (int j = 0; j < NY; ++j)
+            for (int i = 0; i < NX; ++i) {
+                const size_t n = s.id(i, j, k);
+                const bool xs = (i > 0 && i < s.pxn) || (i > NX - s.pxp - 1 && i < NX - 1);
+                const bool ys = (j > 0 && j < s.pyn) || (j > NY - s.pyp - 1 && j < NY - 1);
+                const bool zs = (k > 0 && k < s.pzn) || (k > NZ - s.pzp - 1 && k < NZ - 1);
+                if (i < NX - 1 && j > 0 && j < NY - 1 && k > 0 && k < NZ - 1) {  // Ex
+                    const R L = a.ex[n];
+                    const R my = ys ? a.psi_exy[n] + s.cpsi_exy[n] * L : 0;
+                    const R mz = zs ? a.psi_exz[n] + s.cpsi_exz[n] * L : 0;
+                    if (ys) a.psi_exy[n] = s.b_ey[j] * my;
+                    if (zs) a.psi_exz[n] = s.b_ez[k] * mz;
+                    const R gz = s.Cexhz[n] * L + (ys ? s.a_ey[j] * my : 0);
+                    const R gy = s.Cexhy[n] * L + (zs ? s.a_ez[k] * mz : 0);
+                    a.hz[n] += gz; a.hz[n - sy] -= gz;
+                    a.hy[n] += gy; a.hy[n - sz] -= gy;
+                    a.ex[n] = s.Cexe[n] * L;
+                }
+                if (i > 0 && i < NX - 1 && j < NY - 1 && k > 0 && k < NZ - 1) {  // Ey
+                    const R L = a.ey[n];
+                    const R mx = xs ? a.psi_eyx[n] + s.cpsi_eyx[n] * L : 0;
+                    const R mz = zs ? a.psi_eyz[n] + s.cpsi_eyz[n] * L : 0;
+                    if (xs) a.psi_eyx[n] = s.b_ex[i] * mx;
+                    if (zs) a.psi_eyz[n] = s.b_ez[k] * mz;
+                    const R gx = s.Ceyhx[n] * L + (zs ? s.a_ez[k] * mz : 0);
+                    const R gz = s.Ceyhz[n] * L + (xs ? s.a_ex[i] * mx : 0);
+                    a.hx[n] += gx; a.hx[n - sz] -= gx;
+                    a.hz[n] += gz; a.hz[n - sx] -= gz;
+                    a.ey[n] = s.Ceye[n] * L;
+                }
+                if (i > 0 && i < NX - 1 && j > 0 && j < NY - 1 && k < NZ - 1) {  // Ez
+                    const R L = a.ez[n];
+                    const R mx = xs ? a.psi_ezx[n] + s.cpsi_ezx[n] * L : 0;
+                    const R my = ys ? a.psi_ezy[n] + s.cpsi_ezy[n] * L : 0;
+                    if (xs) a.psi_ezx[n] = s.b_ex[i] * mx;
+                    if (ys) a.psi_ezy[n] = s.b_ey[j] * my;
+                    const R gy = s.Cezhy[n] * L + (xs ? s.a_ex[i] * mx : 0);
+                    const R gx = s.Cezhx[n] * L + (ys ? s.a_ey[j] * my : 0);
+                    a.hy[n] += gy; a.hy[n - sx] -= gy;
+                    a.hx[n] += gx; a.hx[n - sy] -= gx;
+                    a.ez[n] = s.Ceze[n] * L;
+                }
+            }
+}
+
+// dJ/deps_r of the design cells: for every E edge whose four surrounding cells touch the design
+// region, lambda(edge) * dE'/d(eps_avg), shared as 1/4 by each surrounding cell. E^m, H^m are the
+// fields before the step; lam the adjoint of E^{m+1}. Coefficients from the averaged eps/sigma.
+template <class R>
+void accumulate_grad(const Sim<R>& s, const Adj<R>& a, const std::vector<R>* Em[3], const std::vector<R>* Hm[3],
+                     const int* d, double* grad) {
+    const int NX = s.NX, NY = s.NY, NZ = s.NZ;
+    const size_t sx = 1, sy = (size_t)NX, sz = (size_t)NX * NY;
+    const int gx = d[3] - d[0], gy = d[4] - d[1];
+    auto add = [&](int ci, int cj, int ck, double v) {
+        if (ci < d[0] || ci >= d[3] || cj < d[1] || cj >= d[4] || ck < d[2] || ck >= d[5]) return;
+        grad[((size_t)(ck - d[2]) * gy + (cj - d[1])) * gx + (ci - d[0])] += 0.25 * v;
+    };
+    const R two = 2, four = 4;
+    for (int k = std::max(d[2], 1); k <= std::min(d[5], NZ - 2); ++k)
+        for (int j = std::max(d[1], 1); j <= std::min(d[4], NY - 2); ++j)
+            for (int i = std::max(d[0], 1); i <= std::min(d[3], NX - 2); ++i) {
+                const size_t n = s.id(i, j, k);
+                {   // Ex(i,j,k): cells (i,j,k) (i,j-1,k) (i,j,k-1) (i,j-1,k-1)
+                    const R den = two * s.eps_x[n] * s.eps0 + s.dt * s.sig_x[n];
+                    const R dca = four * s.eps0 * s.dt * s.sig_x[n] / (den * den);
+                    const R curl = s.Cexhz[n] * ((*Hm[2])[n] - (*Hm[2])[n - sy]) + s.Cexhy[n] * ((*Hm[1])[n] - (*Hm[1])[n - sz]);
+                    const double v = (double)(a.ex[n] * (dca * (*Em[0])[n] - two * s.eps0 / den * curl));
+                    add(i, j, k, v); add(i, j - 1, k, v); add(i, j, k - 1, v); add(i, j - 1, k - 1, v);
+                }
+                {   // Ey(i,j,k): cells (i,j,k) (i-1,j,k) (i,j,k-1) (i-1,j,k-1)
+                    const R den = two * s.eps_y[n] * s.eps0 + s.dt * s.sig_y[n];
+                    const R dca = four * s.eps0 * s.dt * s.sig_y[n] / (den * den);
+                    const R curl = s.Ceyhx[n] * ((*Hm[0])[n] - (*Hm[0])[n - sz]) + s.Ceyhz[n] * ((*Hm[2])[n] - (*Hm[2])[n - sx]);
+                    const double v = (double)(a.ey[n] * (dca * (*Em[1])[n] - two * s.eps0 / den * curl));
+                    add(i, j, k, v); add(i - 1, j, k, v); add(i, j, k - 1, v); add(i - 1, j, k - 1, v);
+                }
+                {   // Ez(i,j,k): cells (i,j,k) (i-1,j,k) (i,j-1,k) (i-1,j-1,k)
+                    const R den = two * s.eps_z[n] * s.eps0 + s.dt * s.sig_z[n];
+                    const R dca = four * s.eps0 * s.dt * s.sig_z[n] / (den * den);
+                    const R curl = s.Cezhy[n] * ((*Hm[1])[n] - (*Hm[1])[n - sx]) + s.Cezhx[n] * ((*Hm[0])[n] - (*Hm[0])[n - sy]);
+                    const double v = (double)(a.ez[n] * (dca * (*Em[2])[n] - two * s.eps0 / den * curl));
+                    add(i, j, k, v); add(i - 1, j, k, v); add(i, j - 1, k, v); add(i - 1, j - 1, k, v);
+                }
+            }
+}
+
+// FoM and (optionally) its adjoint gradient. Stores the whole field history (small grids only).
+template <class R>
+int fom_and_grad(const or_scenario* sc, int steps, const float* sig, int n_sig, int pi, int pj, int pk,
+                 double* J_out, double* grad_out) {
+    Sim<R> s;
+    if (setup<R>(s, sc, sig, n_sig)) return -1;
+    const size_t n_p = s.id(pi, pj, pk);
+    std::vector<R> row(std::max<size_t>(s.probes.size(), 1));
+    std::vector<std::vector<R>> hist;  // E^m, H^m for m = 0..steps-1 (6 arrays each) when needed
+    std::vector<R> ezp(steps);
+    for (int m = 0; m < steps; ++m) {
+        if (grad_out)
+            for (int c = 0; c < 6; ++c) hist.push_back(*field(s, c));
+        calc_e<R>(s, m, row.data());
+        ezp[m] = s.Ez[n_p];  // Ez after step m's E update (probe outside the CPML)
+        calc_h<R>(s, row.data());
+    }
+    const double dt = (double)s.dt;
+    double J = 0;
+    for (int m = 0; m < steps; ++m) J += dt * (double)ezp[m] * (double)ezp[m];
+    *J_out = J;
+    if (!grad_out) return 0;
+    const int* d = sc->design_box;
+    std::fill(grad_out, grad_out + (size_t)(d[3] - d[0]) * (d[4] - d[1]) * (d[5] - d[2]), 0.0);
+    Adj<R> a(s.N);
+    for (int m = steps - 1; m >= 0; --m) {
+        a.ez[n_p] += (R)(2.0 * dt) * ezp[m];  // dJ/dEz(p) of the sample taken in step m
+        reverse_h<R>(s, a);
+        const std::vector<R>* Em[3] = {&hist[6 * m + 0], &hist[6 * m + 1], &hist[6 * m + 2]};
+        const std::vector<R>* Hm[3] = {&hist[6 * m + 3], &hist[6 * m + 4], &hist[6 * m + 5]};
+        accumulate_grad<R>(s, a, Em, Hm, d, grad_out);
+        reverse_e<R>(s, a);
+    }
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
+
+// FP64 figure of merit J = sum_m dt Ez(pi,pj,pk)^2 and, when grad is non-NULL, dJ/deps_r over the
+// scenario's design region (from the discrete adjoint).
+int or_fom_grad_f64(const or_scenario* sc, int steps, const float* sig, int n_sig, int pi, int pj, int pk,
+                    double* J, double* grad) {
+    return fom_and_grad<double>(sc, steps, sig, n_sig, pi, pj, pk, J, grad);
+}
+int or_fom_grad_f32(const or_scenario* sc, int steps, const float* sig, int n_sig, int pi, int pj, int pk,
+                    double* J, double* grad) {
+    return fom_and_grad<float>(sc, steps, sig, n_sig, pi, pj, pk, J, grad);
+}
 
 // Full run: probes_out (steps, nprobe), fields_out (6, nz, ny, nx). signal_per_node (nsrc, n_sig).
 int or_run_f32(const or_scenario* sc, int steps, const float* sig, int n_sig, const float* init_fields,

@@ -39,7 +39,8 @@ class _Scenario(ctypes.Structure):
                 ("nsrc", _i), ("src_box", _pi), ("src_r", _pf),
                 ("nres", _i), ("res_box", _pi), ("res_r", _pf),
                 ("nprobe", _i), ("probe", _pi),
-                ("profile_override", ctypes.POINTER(_pf))]
+                ("profile_override", ctypes.POINTER(_pf)),
+                ("design_box", _i * 6), ("design_eps", ctypes.POINTER(ctypes.c_double))]
 
 
 def build(force: bool = False) -> str:
@@ -64,14 +65,24 @@ def lib():
         L.or_run_f64.argtypes = [ctypes.POINTER(_Scenario), _i, _pf, _i, _pf, _pd, _pd, _i]
         L.or_onestep_f32.argtypes = [ctypes.POINTER(_Scenario), _i, _pf, _i, _pf, _pf, _pf, _pf]
         L.or_coef_f32.argtypes = [ctypes.POINTER(_Scenario), ctypes.c_char_p, _pf]
+        for fn in (L.or_fom_grad_f64, L.or_fom_grad_f32):
+            fn.argtypes = [ctypes.POINTER(_Scenario), _i, _pf, _i, _i, _i, _i, _pd, _pd]
         _lib = L
     return _lib
 
 
 class _Prepared:
-    def __init__(self, sc, profile_override: Optional[dict] = None, probes: Optional[Sequence] = None):
+    def __init__(self, sc, profile_override: Optional[dict] = None, probes: Optional[Sequence] = None,
+                 design=None):
         self.keep = []
         s = _Scenario()
+        if design is not None:  # (box (6 ints), eps array (nz_d, ny_d, nx_d) float64)
+            box, eps = design
+            e = np.ascontiguousarray(eps, dtype=np.float64)
+            self.keep.append(e)
+            for q in range(6):
+                s.design_box[q] = int(box[q])
+            s.design_eps = e.ctypes.data_as(_pd)
         s.nx, s.ny, s.nz = sc.nx, sc.ny, sc.nz
         for q in range(6):
             s.pml[q] = sc.pml[q]
@@ -171,3 +182,21 @@ def coef(sc, name: str, profile_override: Optional[dict] = None) -> np.ndarray:
     if L.or_coef_f32(ctypes.byref(p.s), name.encode(), out.ctypes.data_as(_pf)) != 0:
         raise RuntimeError("oracle: " + L.or_error().decode())
     return out
+
+
+def fom_grad(sc, probe, design_box, design_eps, steps: Optional[int] = None, precision: str = "f64",
+             grad: bool = True):
+    """Figure of merit J = sum_m dt * Ez(probe)^2 over ``steps`` and, if ``grad``, the discrete-adjoint
+    gradient dJ/deps_r of the design cells (array shaped like ``design_eps``). The design region
+    ``design_box`` = (i0, j0, k0, i1, j1, k1) overrides the cells' eps_r with ``design_eps``."""
+    steps = sc.steps if steps is None else steps
+    p = _Prepared(sc, design=(design_box, design_eps))
+    g = np.zeros(np.shape(design_eps), dtype=np.float64) if grad else None
+    J = ctypes.c_double(0.0)
+    L = lib()
+    fn = L.or_fom_grad_f64 if precision == "f64" else L.or_fom_grad_f32
+    rc = fn(ctypes.byref(p.s), steps, p.sig.ctypes.data_as(_pf), p.n_sig, int(probe[0]), int(probe[1]), int(probe[2]),
+            ctypes.byref(J), None if g is None else g.ctypes.data_as(_pd))
+    if rc != 0:
+        raise RuntimeError("oracle: " + L.or_error().decode())
+    return (J.value, g) if grad else J.value
