@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -98,6 +99,10 @@ struct fdtd_handle {
 
     long long step = 0;
     long long bytes = 0;
+
+    // host-side work list of fdtd_step_static_scratch (interior items first), planned on first use
+    std::vector<int4> static_items;
+    int static_n_interior = -1;
 
     cudaError_t alloc(void** p, size_t n) {
         cudaError_t e = cudaMalloc(p, n);
@@ -749,3 +754,161 @@ int ensure_prepared(fdtd_handle* h) {
 }
 
 }  // namespace
+
+// ---------------------------------------------------------------------------------------------
+// fdtd_step_static_scratch: the fused sweep with its ping-pong target in a static device array.
+//
+// fdtd_step under FDTD_SCHEDULE_FUSED allocates a second field set, a second CPML set and the work
+// list on its first call. Callers that cannot allocate while stepping (device memory reserved in
+// full by their own pool; loops that must not let cudaMalloc / cudaFree synchronise the device)
+// use this entry point instead: the same kernels alternate between the handle's buffers and a
+// fixed array of FDTD_STEP_STATIC_SCRATCH_BYTES, and no device memory is allocated.
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kStaticScratchBytes = FDTD_STEP_STATIC_SCRATCH_BYTES;
+constexpr size_t kScratchAlign = 256;  // TMA needs 16-byte aligned bases; keep each piece on 256 B
+constexpr int kMaxScratchDevices = 64;
+
+// One per device and process; zero-initialised at module load, but no call relies on its contents.
+static __device__ __align__(256) unsigned char g_step_scratch[kStaticScratchBytes];
+
+std::mutex g_scratch_mu;
+unsigned char* g_scratch_addr[kMaxScratchDevices] = {};
+bool g_scratch_configured[kMaxScratchDevices] = {};
+
+size_t align_up(size_t v) { return (v + kScratchAlign - 1) / kScratchAlign * kScratchAlign; }
+
+// Offsets of the pieces of the scratch for handle h: 6 fields, 24 CPML arrays, work list.
+struct ScratchLayout {
+    size_t field[6];
+    size_t psi[6][4];
+    size_t items;
+    size_t total;
+};
+
+ScratchLayout scratch_layout(const fdtd_handle* h, size_t n_items) {
+    ScratchLayout L{};
+    size_t off = 0;
+    const size_t fb = align_up((size_t)vol(h) * sizeof(float));
+    for (int c = 0; c < 6; ++c, off += fb) L.field[c] = off;
+    for (int f = 0; f < 6; ++f) {
+        const size_t pb = align_up((size_t)h->psi_elems[f] * sizeof(float));
+        for (int q = 0; q < 4; ++q, off += pb) L.psi[f][q] = off;
+    }
+    L.items = off;
+    off += align_up(n_items * sizeof(int4));
+    L.total = off;
+    return L;
+}
+
+// Address of the scratch on `dev` (the current device) and the sweep's shared-memory limit, set
+// once per device.
+int scratch_setup(int dev, unsigned char** base) {
+    if (dev < 0 || dev >= kMaxScratchDevices) return fail(FDTD_ERR_STATE, "device ordinal outside the static scratch table");
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_addr[dev]) {
+        void* a = nullptr;
+        CUDA_TRY(cudaGetSymbolAddress(&a, g_step_scratch));
+        g_scratch_addr[dev] = (unsigned char*)a;
+    }
+    if (!g_scratch_configured[dev]) {
+        CUDA_TRY(fused_configure());
+        g_scratch_configured[dev] = true;
+    }
+    *base = g_scratch_addr[dev];
+    return FDTD_OK;
+}
+
+}  // namespace
+
+extern "C" int fdtd_step_static_scratch(fdtd_handle* h, int64_t n) {
+    if (!h) return fail(FDTD_ERR_INVALID, "handle is NULL");
+    if (n < 0) return fail(FDTD_ERR_INVALID, "negative step count");
+    // preparation allocates (coefficient, lumped and probe tables): it must be done already
+    if (!h->prepared || h->dirty_materials || h->dirty_lumped || h->dirty_probes)
+        return fail(FDTD_ERR_STATE, "fdtd_step_static_scratch needs a prepared handle: call fdtd_prepare after the last "
+                                    "change to materials, lumped elements or probes");
+    int dev = -1;
+    CUDA_TRY(cudaGetDevice(&dev));
+    if (dev != h->device) return fail(FDTD_ERR_STATE, "the current device is not the handle's device");
+    if (h->static_n_interior < 0) {  // host-only planning (kc rule of the fused schedule)
+        const long long tiles = (long long)((h->g.nx + fused_tile_x() - 1) / fused_tile_x()) *
+                                ((h->g.ny + fused_tile_y() - 1) / fused_tile_y());
+        int kc = h->g.nz;
+        while (kc > 16 && tiles * ((h->g.nz + kc - 1) / kc) < 4096) kc = (kc + 1) / 2;
+        std::vector<int4> wi, wg;
+        plan_fused(h->g, kc, wi, wg);
+        h->static_n_interior = (int)wi.size();
+        wi.insert(wi.end(), wg.begin(), wg.end());
+        h->static_items.swap(wi);
+    }
+    const ScratchLayout L = scratch_layout(h, h->static_items.size());
+    if (L.total > kStaticScratchBytes)
+        return fail(FDTD_ERR_RANGE, "grid needs " + std::to_string(L.total) + " bytes of step scratch; the static scratch holds " +
+                                        std::to_string(kStaticScratchBytes) + " (about a 64^3 grid with 10-cell CPML)");
+    unsigned char* base = nullptr;
+    int rc = scratch_setup(dev, &base);
+    if (rc) return rc;
+    if (n == 0) return FDTD_OK;
+
+    void* enc = tensor_map_encoder();
+    if (!enc) return fail(FDTD_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    const int a = h->cur;
+    float* sf[6];
+    for (int c = 0; c < 6; ++c) sf[c] = (float*)(base + L.field[c]);
+    PsiSet sp{};
+    for (int f = 0; f < 6; ++f) {
+        sp.f[f].e[0] = h->psi_elems[f] ? (float*)(base + L.psi[f][0]) : nullptr;
+        sp.f[f].e[1] = h->psi_elems[f] ? (float*)(base + L.psi[f][1]) : nullptr;
+        sp.f[f].h[0] = h->psi_elems[f] ? (float*)(base + L.psi[f][2]) : nullptr;
+        sp.f[f].h[1] = h->psi_elems[f] ? (float*)(base + L.psi[f][3]) : nullptr;
+    }
+    FusedMaps maps_h, maps_s;  // tensor maps (host structs) of the handle's buffer and the scratch
+    {
+        float* hh[3] = {h->field[a][3], h->field[a][4], h->field[a][5]};
+        float* ee[3] = {h->field[a][0], h->field[a][1], h->field[a][2]};
+        float* sh[3] = {sf[3], sf[4], sf[5]};
+        float* se[3] = {sf[0], sf[1], sf[2]};
+        if (encode_fused_maps(&maps_h, h->g, hh, ee, h->mat, enc) != 0 || encode_fused_maps(&maps_s, h->g, sh, se, h->mat, enc) != 0)
+            return fail(FDTD_ERR_CUDA, "tensor map encoding failed");
+    }
+    int4* d_items = (int4*)(base + L.items);
+    const size_t n_items = h->static_items.size();
+    if (n_items) CUDA_TRY(cudaMemcpyAsync(d_items, h->static_items.data(), n_items * sizeof(int4), cudaMemcpyHostToDevice, h->stream));
+    const FusedWork w{d_items, h->static_n_interior, d_items + h->static_n_interior, (int)n_items - h->static_n_interior};
+    // the scratch's CPML arrays start as copies of the handle's, so that the elements no step
+    // writes agree when the result is copied back
+    for (int f = 0; f < 6; ++f) {
+        const size_t nb = (size_t)h->psi_elems[f] * sizeof(float);
+        if (!nb) continue;
+        float* src[4];
+        psi_arrays(h, a, f, src);
+        const float* dst[4] = {sp.f[f].e[0], sp.f[f].e[1], sp.f[f].h[0], sp.f[f].h[1]};
+        for (int q = 0; q < 4; ++q) CUDA_TRY(cudaMemcpyAsync((void*)dst[q], src[q], nb, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    const StepParams p = make_params(h);
+    const FieldPtrs fh{h->field[a][0], h->field[a][1], h->field[a][2], h->field[a][3], h->field[a][4], h->field[a][5]};
+    const FieldPtrs fs{sf[0], sf[1], sf[2], sf[3], sf[4], sf[5]};
+    for (int64_t s = 0; s < n; ++s) {
+        if ((s & 1) == 0) CUDA_TRY(launch_fused(maps_h, p, fs, h->psi[a], sp, h->step, w, h->stream));
+        else CUDA_TRY(launch_fused(maps_s, p, fh, sp, h->psi[a], h->step, w, h->stream));
+        ++h->step;
+    }
+    if (n & 1) {  // the last step wrote the scratch: copy the state back into the handle's buffers
+        // only the nx columns of each row: the sweep never writes the row padding
+        const DeviceGrid& g = h->g;
+        for (int c = 0; c < 6; ++c)
+            CUDA_TRY(cudaMemcpy2DAsync(h->field[a][c], (size_t)g.pitch * 4, sf[c], (size_t)g.pitch * 4, (size_t)g.nx * 4,
+                                       (size_t)g.ny * g.nz, cudaMemcpyDeviceToDevice, h->stream));
+        for (int f = 0; f < 6; ++f) {
+            const size_t nb = (size_t)h->psi_elems[f] * sizeof(float);
+            if (!nb) continue;
+            float* dst[4];
+            psi_arrays(h, a, f, dst);
+            const float* src[4] = {sp.f[f].e[0], sp.f[f].e[1], sp.f[f].h[0], sp.f[f].h[1]};
+            for (int q = 0; q < 4; ++q) CUDA_TRY(cudaMemcpyAsync(dst[q], src[q], nb, cudaMemcpyDeviceToDevice, h->stream));
+        }
+    }
+    return FDTD_OK;
+}

@@ -76,6 +76,7 @@ SIGNATURES = {
     "fdtd_load_state": (ctypes.c_int, [_vp, _vp]),
     "fdtd_get_cpml_profile": (ctypes.c_int, [_vp, _i32, _i32, _pf]),
     "fdtd_device_bytes": (_i64, [_vp]),
+    "fdtd_step_static_scratch": (ctypes.c_int, [_vp, _i64]),
 }
 
 _lib = None
@@ -196,6 +197,10 @@ class Simulation:
     # -- run ------------------------------------------------------------------------------------
     def step(self, n: int = 1) -> None:
         _check(_lib.fdtd_step(self._h, n))
+
+    def step_static_scratch(self, n: int = 1) -> None:
+        """n fused steps that allocate no device memory (the handle must be prepared; small grids)."""
+        _check(_lib.fdtd_step_static_scratch(self._h, n))
 
     def synchronize(self) -> None:
         _check(_lib.fdtd_synchronize(self._h))

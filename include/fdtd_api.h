@@ -142,6 +142,37 @@ int fdtd_get_cpml_profile(fdtd_handle* h, int32_t axis, int32_t kind, float* hos
 /* Bytes of device memory the handle holds. */
 int64_t fdtd_device_bytes(const fdtd_handle* h);
 
+/* Maximum bytes of FDTD_STEP_STATIC_SCRATCH: one second field set, one second CPML memory set and
+ * the sweep's work list. Enough for a 64^3 grid with 10-cell CPML on all faces (about 9.8 MiB). */
+#define FDTD_STEP_STATIC_SCRATCH_BYTES (16u << 20)
+
+/* No reference counterpart (the reference allocates all of its arrays in marchingLoop before the
+ * loop and has no fused schedule). Advances n steps with the fused sweep like fdtd_step under
+ * FDTD_SCHEDULE_FUSED, with bit-identical fields, CPML memory and probe samples. This call
+ * allocates no device memory. fdtd_step allocates a second field set and CPML set (plus the
+ * sweep's work list) the first time it runs the fused sweep. The ping-pong target here is instead
+ * a fixed static device array of FDTD_STEP_STATIC_SCRATCH_BYTES inside the library.
+ * It is for callers that cannot allocate while stepping: callers whose device memory is reserved
+ * in full up front (by their own pool) so that a lazy allocation would fail, and callers that must
+ * not let a step call synchronise the device (cudaMalloc / cudaFree may).
+ *  - The handle must be prepared (fdtd_prepare after the last change to materials, lumped elements
+ *    or probes), because preparation allocates; otherwise FDTD_ERR_STATE. The calling thread's
+ *    current device must be the handle's device.
+ *  - Grids whose scratch exceeds FDTD_STEP_STATIC_SCRATCH_BYTES are rejected with
+ *    FDTD_ERR_RANGE, and the message gives the bytes needed.
+ *  - The first call on each device looks up the array's address (cudaGetSymbolAddress) and sets
+ *    the sweep kernels' shared-memory limit; these are not stream operations. A call with n = 0
+ *    does only this set-up; make it once per device before a section that must issue nothing
+ *    but stream work.
+ *  - Nothing in the scratch needs to start at zero or to survive between calls: each call first
+ *    copies the handle's CPML memory into it, every scratch element a step reads was written
+ *    earlier in the same call, and the result is back in the handle's own buffers when the call's
+ *    stream work completes.
+ *  - The scratch is one per device and per process. Calls whose stream work overlaps on the device
+ *    (other handles, other streams, other threads) race on it and corrupt each other's results;
+ *    order them (one stream, or events), as with any shared buffer. */
+int fdtd_step_static_scratch(fdtd_handle* h, int64_t n);
+
 #ifdef __cplusplus
 }
 #endif
