@@ -64,6 +64,8 @@ struct fdtd_handle {
     int kc = 0;  // planes per CTA chunk of the fused sweep
     FusedWork work{};
     uint8_t* mat = nullptr;
+    uint8_t* cls = nullptr;  // node classes, built by ensure_prepared
+    int n_lumped_edges = 0;
     MatProps* props = nullptr;
     MatCoef* coef = nullptr;
     float* prof[18] = {};
@@ -128,6 +130,7 @@ StepParams make_params(fdtd_handle* h) {
     StepParams p{};
     p.g = h->g;
     p.mat = h->mat;
+    p.cls = h->cls;
     p.props = h->props;
     p.coef = h->coef;
     const float* const* P = h->prof;
@@ -221,15 +224,11 @@ int ensure_fused(fdtd_handle* h) {
     for (int b = 0; b < 2; ++b) {
         float* hh[3] = {h->field[b][3], h->field[b][4], h->field[b][5]};
         float* ee[3] = {h->field[b][0], h->field[b][1], h->field[b][2]};
-        if (encode_fused_maps(&h->maps[b], h->g, hh, ee, h->mat, enc) != 0)
+        if (encode_fused_maps(&h->maps[b], h->g, hh, ee, h->cls, enc) != 0)
             return fail(FDTD_ERR_CUDA, "tensor map encoding failed");
     }
     CUDA_TRY(fused_configure());
-    // planes per CTA chunk: whole columns unless that leaves too few CTAs to fill the GPU
-    const long long tiles = (long long)((h->g.nx + fused_tile_x() - 1) / fused_tile_x()) *
-                            ((h->g.ny + fused_tile_y() - 1) / fused_tile_y());
-    int kc = h->g.nz;
-    while (kc > 16 && tiles * ((h->g.nz + kc - 1) / kc) < 4096) kc = (kc + 1) / 2;
+    const int kc = fused_chunk(h->g);
     h->kc = kc;
     // work items of the sweep: interior items (lean kernel) and the rest (general kernel)
     std::vector<int4> wi, wg;
@@ -244,8 +243,8 @@ int ensure_fused(fdtd_handle* h) {
     return FDTD_OK;
 }
 
-// AUTO takes the two-pass schedule: on GB300 it is faster than the fused sweep at every size measured
-// (512^3 random boxes: 50.7 against 37.7 Gcell/s).
+// AUTO takes the two-pass schedule: on GB300 it is faster than the fused schedule on the random-box
+// workloads measured (512^3 random boxes with 10-cell CPML: 53.1 against 47.2 Gcell/s).
 bool use_fused(const fdtd_handle* h) { return h->schedule == FDTD_SCHEDULE_FUSED; }
 
 }  // namespace
@@ -476,8 +475,9 @@ int fdtd_step(fdtd_handle* h, int64_t n) {
         if (rc) return rc;
         for (int64_t s = 0; s < n; ++s) {
             const int a = h->cur, b = 1 - h->cur;
+            FieldPtrs fi{h->field[a][0], h->field[a][1], h->field[a][2], h->field[a][3], h->field[a][4], h->field[a][5]};
             FieldPtrs fo{h->field[b][0], h->field[b][1], h->field[b][2], h->field[b][3], h->field[b][4], h->field[b][5]};
-            CUDA_TRY(launch_fused(h->maps[a], p, fo, h->psi[a], h->psi[b], h->step, h->work, h->stream));
+            CUDA_TRY(launch_fused(h->maps[a], p, fi, fo, h->psi[a], h->psi[b], h->step, h->work, h->stream));
             h->cur = b;
             ++h->step;
         }
@@ -661,6 +661,7 @@ int build_lumped(fdtd_handle* h) {
     for (const LumpedEdge& e : se) koff[e.k + 1]++;
     for (int k = 0; k < g.nz; ++k) koff[k + 1] += koff[k];
     const size_t ne = se.size();
+    h->n_lumped_edges = (int)ne;
     CUDA_TRY(h->alloc((void**)&h->d_lumped_k, sizeof(int) * (g.nz + 1)));
     CUDA_TRY(cudaMemcpy(h->d_lumped_k, koff.data(), sizeof(int) * (g.nz + 1), cudaMemcpyHostToDevice));
     CUDA_TRY(h->alloc((void**)&h->d_lumped, sizeof(LumpedEdge) * std::max<size_t>(ne, 1)));
@@ -743,6 +744,12 @@ int ensure_prepared(fdtd_handle* h) {
     if (h->dirty_lumped) {
         int rc = build_lumped(h);
         if (rc) return rc;
+        // node classes depend on the material index and the lumped edges
+        if (!h->cls) {
+            CUDA_TRY(h->alloc((void**)&h->cls, (size_t)vol(h)));
+            CUDA_TRY(cudaMemsetAsync(h->cls, kGeneral, (size_t)vol(h), h->stream));
+        }
+        CUDA_TRY(launch_node_class(h->g, h->mat, h->d_lumped, h->n_lumped_edges, h->cls, h->stream));
     }
     if (h->dirty_probes) {
         int rc = build_probes(h);
@@ -832,13 +839,9 @@ extern "C" int fdtd_step_static_scratch(fdtd_handle* h, int64_t n) {
     int dev = -1;
     CUDA_TRY(cudaGetDevice(&dev));
     if (dev != h->device) return fail(FDTD_ERR_STATE, "the current device is not the handle's device");
-    if (h->static_n_interior < 0) {  // host-only planning (kc rule of the fused schedule)
-        const long long tiles = (long long)((h->g.nx + fused_tile_x() - 1) / fused_tile_x()) *
-                                ((h->g.ny + fused_tile_y() - 1) / fused_tile_y());
-        int kc = h->g.nz;
-        while (kc > 16 && tiles * ((h->g.nz + kc - 1) / kc) < 4096) kc = (kc + 1) / 2;
+    if (h->static_n_interior < 0) {  // host-only planning, as for the fused schedule
         std::vector<int4> wi, wg;
-        plan_fused(h->g, kc, wi, wg);
+        plan_fused(h->g, fused_chunk(h->g), wi, wg);
         h->static_n_interior = (int)wi.size();
         wi.insert(wi.end(), wg.begin(), wg.end());
         h->static_items.swap(wi);
@@ -870,7 +873,7 @@ extern "C" int fdtd_step_static_scratch(fdtd_handle* h, int64_t n) {
         float* ee[3] = {h->field[a][0], h->field[a][1], h->field[a][2]};
         float* sh[3] = {sf[3], sf[4], sf[5]};
         float* se[3] = {sf[0], sf[1], sf[2]};
-        if (encode_fused_maps(&maps_h, h->g, hh, ee, h->mat, enc) != 0 || encode_fused_maps(&maps_s, h->g, sh, se, h->mat, enc) != 0)
+        if (encode_fused_maps(&maps_h, h->g, hh, ee, h->cls, enc) != 0 || encode_fused_maps(&maps_s, h->g, sh, se, h->cls, enc) != 0)
             return fail(FDTD_ERR_CUDA, "tensor map encoding failed");
     }
     int4* d_items = (int4*)(base + L.items);
@@ -891,8 +894,8 @@ extern "C" int fdtd_step_static_scratch(fdtd_handle* h, int64_t n) {
     const FieldPtrs fh{h->field[a][0], h->field[a][1], h->field[a][2], h->field[a][3], h->field[a][4], h->field[a][5]};
     const FieldPtrs fs{sf[0], sf[1], sf[2], sf[3], sf[4], sf[5]};
     for (int64_t s = 0; s < n; ++s) {
-        if ((s & 1) == 0) CUDA_TRY(launch_fused(maps_h, p, fs, h->psi[a], sp, h->step, w, h->stream));
-        else CUDA_TRY(launch_fused(maps_s, p, fh, sp, h->psi[a], h->step, w, h->stream));
+        if ((s & 1) == 0) CUDA_TRY(launch_fused(maps_h, p, fh, fs, h->psi[a], sp, h->step, w, h->stream));
+        else CUDA_TRY(launch_fused(maps_s, p, fs, fh, sp, h->psi[a], h->step, w, h->stream));
         ++h->step;
     }
     if (n & 1) {  // the last step wrote the scratch: copy the state back into the handle's buffers

@@ -20,6 +20,7 @@ namespace fdtd {
 constexpr float kTiny = 1.2e-38f;  // setZero's initial value for fields, psi and conductivities
 constexpr int kMaxMaterials = 256;
 constexpr int kDefaultEntry = kMaxMaterials;  // H coefficient of faces the reference never averages
+constexpr int kGeneral = 255;                 // node class of nodes that take the general path
 
 // Per-material coefficients for an edge whose surrounding cells all hold the same material.
 // e[c] = {Ca, Cb_plus, Cb_minus, 0} for Ex, Ey, Ez; h[c] = {Ch, Cb_plus, Cb_minus, 0} for Hx, Hy,
@@ -78,6 +79,10 @@ struct BgCurl {
 struct StepParams {
     DeviceGrid g;
     const uint8_t* mat;          // (nz, ny, pitch)
+    // Node class (nz, ny, pitch): the material id when the node takes the fast path (every
+    // component updated, outside the CPML slabs, no lumped edge, the seven cells of its three E
+    // edge averages all of that material), kGeneral otherwise. Built by launch_node_class.
+    const uint8_t* cls;
     const MatProps* props;       // kMaxMaterials entries
     const MatCoef* coef;         // kMaxMaterials + 1 entries (last = reference default for H faces)
     // 1-D CPML profiles per axis (length nx, ny, nz): b/a for E and H, kappa for E and H

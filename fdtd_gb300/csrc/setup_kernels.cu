@@ -204,3 +204,41 @@ cudaError_t launch_paint(uint8_t* mat, const DeviceGrid& g, const int box[6], ui
 }
 
 }  // namespace fdtd
+
+namespace fdtd {
+
+// Node class (StepParams::cls): material id of nodes that take the fast path, kGeneral otherwise.
+// The seven cells are those the three E edge averages read, (i,j,k) (i-1,j,k) (i,j-1,k) (i,j,k-1)
+// (i-1,j-1,k) (i-1,j,k-1) (i,j-1,k-1); the four cells of the H faces are among them.
+__global__ void k_node_class(const uint8_t* __restrict__ mat, uint8_t* __restrict__ cls, DeviceGrid g) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= g.nx || j >= g.ny) return;
+    const long long n = (long long)k * g.plane + (long long)j * g.pitch + i;
+    uint8_t c = kGeneral;
+    if (interior(i, g.nx, g.pxn, g.pxp) && interior(j, g.ny, g.pyn, g.pyp) && interior(k, g.nz, g.pzn, g.pzp)) {
+        const long long R = g.pitch, P = g.plane;
+        const uint8_t m0 = mat[n];
+        if (mat[n - 1] == m0 && mat[n - R] == m0 && mat[n - P] == m0 && mat[n - 1 - R] == m0 && mat[n - 1 - P] == m0 &&
+            mat[n - R - P] == m0)
+            c = m0;  // m0 == kGeneral stays general
+    }
+    cls[n] = c;
+}
+
+__global__ void k_class_lumped(uint8_t* cls, DeviceGrid g, const LumpedEdge* edges, int n_edges) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n_edges) cls[(long long)edges[q].k * g.plane + (long long)edges[q].j * g.pitch + edges[q].i] = kGeneral;
+}
+
+cudaError_t launch_node_class(const DeviceGrid& g, const uint8_t* mat, const LumpedEdge* edges, int n_edges, uint8_t* cls,
+                              cudaStream_t st) {
+    dim3 block(32, 8, 1);
+    dim3 grid((g.nx + 31) / 32, (g.ny + 7) / 8, g.nz);
+    k_node_class<<<grid, block, 0, st>>>(mat, cls, g);
+    if (n_edges > 0) k_class_lumped<<<(n_edges + 127) / 128, 128, 0, st>>>(cls, g, edges, n_edges);
+    return cudaGetLastError();
+}
+
+}  // namespace fdtd

@@ -1,24 +1,22 @@
-// Fused schedule: one z-marching sweep per time step over ping-pong field buffers.
+// Fused schedule: per time step, one z-marching sweep over the interior plus two passes over the
+// shell (CPML slabs and boundary planes), all reading buffer A and writing buffer B.
 //
-// A work item is a 32 x 8 column of nodes and a range of planes [k0, k1). Planes stream through a
-// 5-stage shared-memory ring filled by TMA (cp.async.bulk.tensor, 3-D tiles from this GPU's HBM,
-// two planes ahead of the one being computed). At plane k the CTA
-//   1. computes E(k) on the tile plus one column / row beyond its high x / y edges (the H update of
-//      the tile needs those E values; the extra ones are recomputed from the old fields instead of
-//      being exchanged), storing only the tile's own nodes;
+// Interior sweep. A work item is a 32 x 16 column of nodes and a plane range [k0, k1) inside the
+// interior (no CPML, no boundary planes). Planes stream through a 3-stage shared-memory ring
+// filled by TMA (cp.async.bulk.tensor, 3-D tiles of this GPU's HBM, one plane ahead of the one
+// computed): H with a one-node halo, old E, and the node-class byte. At plane k the CTA
+//   1. computes E(k) on its tile plus one column / row beyond the high x / y edges (the H update
+//      needs those E values; they are recomputed from the old fields instead of being exchanged),
+//      storing only its own nodes;
 //   2. computes H(k-1) of its own nodes from E(k-1), E(k) (shared memory) and H(k-1) (the ring).
-// Old fields and old CPML memory are read from buffer A, new ones written to buffer B, so any
-// partition of the grid into items is valid and CTAs never see each other's partial results. Each
-// field value crosses HBM once per step in each direction: 24 B read + 24 B written per cell, plus
-// the uint8 material index and the CPML memory.
-//
-// Two instantiations split the items: the interior kernel covers items whose every node is away
-// from the grid boundary and the CPML slabs (table coefficients, an out-of-line call at material
-// interfaces, the lumped-source override); the general kernel covers the rest with e_update /
-// h_update. Keeping the general code out of the interior kernel halves the interior kernel's
-// registers and instruction footprint. Both use the arithmetic of yee_common.cuh, so the result is
-// bit-identical to the two-pass schedule. All waits on the TMA barriers are bounded: on timeout
-// the kernel records an error in the status word, drains its own copies (again bounded) and exits.
+// Each thread owns two nodes of a plane (rows ty and ty + 8), which gives every warp two
+// independent update chains and halves the per-plane overhead per node. Each field value crosses
+// HBM once per step in each direction (24 B read + 24 B written per cell) plus the class byte.
+// Nodes of class kGeneral (material interfaces, lumped edges) leave the fast path through an
+// out-of-line call. The shell passes (yee_two_pass.cu) run before (E) and after (H) the sweep.
+// All schedules use the arithmetic of yee_common.cuh, so the results are bit-identical. Every
+// wait on a TMA barrier is bounded: on timeout the kernel records an error in the status word,
+// drains its own copies (again bounded) and exits.
 #include <cuda.h>
 
 #include "yee_common.cuh"
@@ -28,13 +26,15 @@ namespace fdtd {
 
 namespace {
 
-constexpr int TX = 32, TY = 8;              // tile of nodes owned by a CTA
-constexpr int NTH = TX * TY;                // one thread per owned node
-constexpr int NSTAGE = 5;                   // planes resident in the ring
-constexpr int AHEAD = 2;                    // planes loaded ahead of the one computed (<= NSTAGE - 3)
+constexpr int TX = 32, TY = 16;             // tile of nodes owned by a CTA (and shell item size)
+constexpr int NTH = 256;                    // threads per CTA
+constexpr int ROWS = TX * TY / NTH;         // nodes per thread per plane (rows ty, ty + 8)
+constexpr int RSTEP = NTH / TX;             // row distance between a thread's nodes
+constexpr int NSTAGE = 3;                   // planes resident in the ring
+constexpr int AHEAD = 1;                    // planes loaded ahead of the one computed (<= NSTAGE - 2)
 constexpr int HW = TX + 8, HH = TY + 2;     // H tile: x in [x0-4, x0+TX+4), y in [y0-1, y0+TY+1)
 constexpr int EW = TX + 4, EH = TY + 1;     // old-E tile: x in [x0, x0+TX+4), y in [y0, y0+TY+1)
-constexpr int MW = TX + 32, MH = TY + 2;    // material tile: x in [x0-16, x0+TX+16), y in [y0-1, ...)
+constexpr int MW = TX + 32, MH = TY + 2;    // class tile: x in [x0-16, x0+TX+16), y in [y0-1, ...)
 constexpr int NW = TX + 1, NH = TY + 1;     // new-E plane: x in [x0, x0+TX], y in [y0, y0+TY]
 
 constexpr int round128(int b) { return (b + 127) / 128 * 128; }
@@ -45,8 +45,11 @@ constexpr int STAGE_BYTES = 3 * H_BYTES + 3 * E_BYTES + M_BYTES;
 constexpr unsigned TX_BYTES = 3u * HW * HH * 4 + 3u * EW * EH * 4 + MW * MH;  // bytes the TMA boxes carry
 constexpr int N_FLOATS = NW * NH;
 constexpr int ENEW_BYTES = 2 * 3 * N_FLOATS * 4;
-constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + ENEW_BYTES + NSTAGE * 8;
-constexpr int NWARP = NTH / 32, NHALO = N_FLOATS - NTH;
+constexpr int NHALO = TX + TY + 1;  // row y0 + TY (warp 0) and column x0 + TX (warp 1)
+constexpr int kMaxItemPlanes = 512;  // planes streamed by one item (chunk + 2); bounds the flag array
+constexpr int SMEM_INTERIOR = NSTAGE * STAGE_BYTES + ENEW_BYTES + NSTAGE * 8 + kMaxItemPlanes;
+static_assert(NSTAGE >= AHEAD + 2, "the ring recycles the stage of plane k - 2 at plane k");
+static_assert(NHALO <= 64, "halo nodes live on the first two warps");
 
 constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
 
@@ -85,7 +88,7 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
 }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-// Arrays of one ring stage: H tile (3), old-E tile (3), material tile, at fixed offsets.
+// Arrays of one ring stage: H tile (3), old-E tile (3), class tile, at fixed offsets.
 struct StageView {
     const unsigned char* base;
     __device__ explicit StageView(const unsigned char* b) : base(b) {}
@@ -94,94 +97,173 @@ struct StageView {
     __device__ const uint8_t* m() const { return base + 3 * H_BYTES + 3 * E_BYTES; }
 };
 
-// E update of an interior node (all three components updated, no CPML) with the lumped override.
-__device__ __forceinline__ void e_interior(const StepParams& p, const ENbr& n, int i, int j, int k, long long m,
-                                           bool plane_lumped, float out[3]) {
+// Slow paths of the interior kernel, out of line: nodes at a material interface or on a lumped
+// edge (node class kGeneral). The cell materials come from the index in global memory; the
+// coefficients are the table entry where the cells of an edge agree and the reference's averages
+// otherwise (e_coef_mixed / h_coef_mixed), then the lumped override (calc_e fdtdrav.h:720-741).
+static __device__ __noinline__ float3 e_slow(const StepParams* pp, int i, int j, int k, long long m, int plane_lumped,
+                                             float ex, float ey, float ez, float dHz_j, float dHy_k, float dHx_k,
+                                             float dHz_i, float dHy_i, float dHx_j) {
+    const StepParams& p = *pp;
     const DeviceGrid& g = p.g;
-    const float dHz_j = __fsub_rn(n.hz, n.hz_jm), dHy_k = __fsub_rn(n.hy, n.hy_km);
-    const float dHx_k = __fsub_rn(n.hx, n.hx_km), dHz_i = __fsub_rn(n.hz, n.hz_im);
-    const float dHy_i = __fsub_rn(n.hy, n.hy_im), dHx_j = __fsub_rn(n.hx, n.hx_jm);
-    const MatCoef* mc = p.coef + n.m0;
+    const long long R = g.pitch, P = g.plane, n = (long long)k * P + (long long)j * R + i;
+    const uint8_t* mat = p.mat;
+    const int m0 = mat[n], mi = mat[n - 1], mj = mat[n - R], mk = mat[n - P];
+    const int mij = mat[n - 1 - R], mik = mat[n - 1 - P], mjk = mat[n - R - P];
+    const MatCoef* mc = p.coef + m0;
     Coef3 cx, cy, cz;
-    if (n.m0 == n.mj && n.m0 == n.mk && n.m0 == n.mjk) { const float4 c = __ldg(&mc->e[0]); cx = Coef3{c.x, c.y, c.z}; }
-    else cx = e_coef_mixed(p.props, n.m0, n.mj, n.mk, n.mjk, g.dt, g.eps0, g.dy, g.dz);
-    if (n.m0 == n.mi && n.m0 == n.mk && n.m0 == n.mik) { const float4 c = __ldg(&mc->e[1]); cy = Coef3{c.x, c.y, c.z}; }
-    else cy = e_coef_mixed(p.props, n.m0, n.mi, n.mk, n.mik, g.dt, g.eps0, g.dz, g.dx);
-    if (n.m0 == n.mi && n.m0 == n.mj && n.m0 == n.mij) { const float4 c = __ldg(&mc->e[2]); cz = Coef3{c.x, c.y, c.z}; }
-    else cz = e_coef_mixed(p.props, n.m0, n.mi, n.mj, n.mij, g.dt, g.eps0, g.dx, g.dy);
-    out[0] = upd3(cx.a, n.ex, cx.bp, dHz_j, cx.bm, dHy_k);
-    out[1] = upd3(cy.a, n.ey, cy.bp, dHx_k, cy.bm, dHz_i);
+    if (m0 == mj && m0 == mk && m0 == mjk) { const float4 c = __ldg(&mc->e[0]); cx = Coef3{c.x, c.y, c.z}; }
+    else cx = e_coef_mixed(p.props, m0, mj, mk, mjk, g.dt, g.eps0, g.dy, g.dz);
+    if (m0 == mi && m0 == mk && m0 == mik) { const float4 c = __ldg(&mc->e[1]); cy = Coef3{c.x, c.y, c.z}; }
+    else cy = e_coef_mixed(p.props, m0, mi, mk, mik, g.dt, g.eps0, g.dz, g.dx);
+    if (m0 == mi && m0 == mj && m0 == mij) { const float4 c = __ldg(&mc->e[2]); cz = Coef3{c.x, c.y, c.z}; }
+    else cz = e_coef_mixed(p.props, m0, mi, mj, mij, g.dt, g.eps0, g.dx, g.dy);
+    float3 r;
+    r.x = upd3(cx.a, ex, cx.bp, dHz_j, cx.bm, dHy_k);
+    r.y = upd3(cy.a, ey, cy.bp, dHx_k, cy.bm, dHz_i);
     const LumpedEdge* L = plane_lumped ? find_lumped(p, i, j, k) : nullptr;
     if (L) {
         if (L->source >= 0) {
             const float s = m < p.wave_len[L->source] ? p.waves[L->source][m] : 0.f;
-            out[2] = upd4(L->ceze, n.ez, L->cezhy, dHy_i, L->cezhx, dHx_j, L->cezj, s);
+            r.z = upd4(L->ceze, ez, L->cezhy, dHy_i, L->cezhx, dHx_j, L->cezj, s);
         } else {
-            out[2] = upd3(L->ceze, n.ez, L->cezhy, dHy_i, L->cezhx, dHx_j);
+            r.z = upd3(L->ceze, ez, L->cezhy, dHy_i, L->cezhx, dHx_j);
         }
     } else {
-        out[2] = upd3(cz.a, n.ez, cz.bp, dHy_i, cz.bm, dHx_j);
+        r.z = upd3(cz.a, ez, cz.bp, dHy_i, cz.bm, dHx_j);
     }
+    return r;
 }
 
-// H update of an interior node (no reference-default faces, no CPML).
-__device__ __forceinline__ void h_interior(const StepParams& p, const HNbr& n, float out[3]) {
+static __device__ __noinline__ float3 h_slow(const StepParams* pp, int i, int j, int k, float hx, float hy, float hz,
+                                             float dEy_k, float dEz_j, float dEz_i, float dEx_k, float dEx_j,
+                                             float dEy_i) {
+    const StepParams& p = *pp;
     const DeviceGrid& g = p.g;
-    const MatCoef* mc = p.coef + n.m0;
+    const long long n = (long long)k * g.plane + (long long)j * g.pitch + i;
+    const int m0 = p.mat[n], mi = p.mat[n - 1], mj = p.mat[n - g.pitch], mk = p.mat[n - g.plane];
+    const MatCoef* mc = p.coef + m0;
     Coef3 cx, cy, cz;
-    if (n.m0 == n.mi) { const float4 c = __ldg(&mc->h[0]); cx = Coef3{c.x, c.y, c.z}; }
-    else cx = h_coef_mixed(p.props, n.m0, n.mi, g.dt, g.mu0, g.dz, g.dy);
-    if (n.m0 == n.mj) { const float4 c = __ldg(&mc->h[1]); cy = Coef3{c.x, c.y, c.z}; }
-    else cy = h_coef_mixed(p.props, n.m0, n.mj, g.dt, g.mu0, g.dx, g.dz);
-    if (n.m0 == n.mk) { const float4 c = __ldg(&mc->h[2]); cz = Coef3{c.x, c.y, c.z}; }
-    else cz = h_coef_mixed(p.props, n.m0, n.mk, g.dt, g.mu0, g.dy, g.dx);
-    out[0] = upd3_hx(cx.a, n.hx, cx.bp, __fsub_rn(n.ey_kp, n.ey), cx.bm, __fsub_rn(n.ez_jp, n.ez));
-    out[1] = upd3(cy.a, n.hy, cy.bp, __fsub_rn(n.ez_ip, n.ez), cy.bm, __fsub_rn(n.ex_kp, n.ex));
-    out[2] = upd3(cz.a, n.hz, cz.bp, __fsub_rn(n.ex_jp, n.ex), cz.bm, __fsub_rn(n.ey_ip, n.ey));
+    if (m0 == mi) { const float4 c = __ldg(&mc->h[0]); cx = Coef3{c.x, c.y, c.z}; }
+    else cx = h_coef_mixed(p.props, m0, mi, g.dt, g.mu0, g.dz, g.dy);
+    if (m0 == mj) { const float4 c = __ldg(&mc->h[1]); cy = Coef3{c.x, c.y, c.z}; }
+    else cy = h_coef_mixed(p.props, m0, mj, g.dt, g.mu0, g.dx, g.dz);
+    if (m0 == mk) { const float4 c = __ldg(&mc->h[2]); cz = Coef3{c.x, c.y, c.z}; }
+    else cz = h_coef_mixed(p.props, m0, mk, g.dt, g.mu0, g.dy, g.dx);
+    return make_float3(upd3_hx(cx.a, hx, cx.bp, dEy_k, cx.bm, dEz_j), upd3(cy.a, hy, cy.bp, dEz_i, cy.bm, dEx_k),
+                       upd3(cz.a, hz, cz.bp, dEx_j, cz.bm, dEy_i));
+}
+
+// Inputs of one E node read from the ring: old E, the six H differences and the node class.
+struct EIn {
+    float ex, ey, ez, dHz_j, dHy_k, dHx_k, dHz_i, dHy_i, dHx_j;
+    int c;
+};
+__device__ __forceinline__ EIn e_load(const StageView& cur, const StageView& prv, int hi, int ei, int mi) {
+    const float* H0 = cur.h(0);
+    const float* H1 = cur.h(1);
+    const float* H2 = cur.h(2);
+    const float hx = H0[hi], hy = H1[hi], hz = H2[hi];
+    EIn r;
+    r.dHz_j = __fsub_rn(hz, H2[hi - HW]); r.dHy_k = __fsub_rn(hy, prv.h(1)[hi]);
+    r.dHx_k = __fsub_rn(hx, prv.h(0)[hi]); r.dHz_i = __fsub_rn(hz, H2[hi - 1]);
+    r.dHy_i = __fsub_rn(hy, H1[hi - 1]); r.dHx_j = __fsub_rn(hx, H0[hi - HW]);
+    r.ex = cur.e(0)[ei]; r.ey = cur.e(1)[ei]; r.ez = cur.e(2)[ei];
+    r.c = cur.m()[mi];
+    return r;
+}
+__device__ __forceinline__ float3 e_fast(const StepParams& p, const EIn& a) {
+    const MatCoef* mc = p.coef + a.c;
+    const float4 x = __ldg(&mc->e[0]), y = __ldg(&mc->e[1]), z = __ldg(&mc->e[2]);
+    return make_float3(upd3(x.x, a.ex, x.y, a.dHz_j, x.z, a.dHy_k), upd3(y.x, a.ey, y.y, a.dHx_k, y.z, a.dHz_i),
+                       upd3(z.x, a.ez, z.y, a.dHy_i, z.z, a.dHx_j));
+}
+__device__ __forceinline__ float3 e_any(const StepParams& p, const EIn& a, int i, int j, int k, long long m, int lumped) {
+    if (a.c != kGeneral) return e_fast(p, a);
+    return e_slow(&p, i, j, k, m, lumped, a.ex, a.ey, a.ez, a.dHz_j, a.dHy_k, a.dHx_k, a.dHz_i, a.dHy_i, a.dHx_j);
+}
+
+// Inputs of one H node: old H, the six new-E differences (from the E planes k-1 and k in shared
+// memory) and the node class.
+struct HIn {
+    float hx, hy, hz, dEy_k, dEz_j, dEz_i, dEx_k, dEx_j, dEy_i;
+    int c;
+};
+__device__ __forceinline__ HIn h_load(const StageView& prv, const float* en_prv, const float* en_cur, int hi, int mi, int ni) {
+    HIn r;
+    const float ex = en_prv[ni], ey = en_prv[N_FLOATS + ni], ez = en_prv[2 * N_FLOATS + ni];
+    r.dEy_k = __fsub_rn(en_cur[N_FLOATS + ni], ey); r.dEz_j = __fsub_rn(en_prv[2 * N_FLOATS + ni + NW], ez);
+    r.dEz_i = __fsub_rn(en_prv[2 * N_FLOATS + ni + 1], ez); r.dEx_k = __fsub_rn(en_cur[ni], ex);
+    r.dEx_j = __fsub_rn(en_prv[ni + NW], ex); r.dEy_i = __fsub_rn(en_prv[N_FLOATS + ni + 1], ey);
+    r.hx = prv.h(0)[hi]; r.hy = prv.h(1)[hi]; r.hz = prv.h(2)[hi];
+    r.c = prv.m()[mi];
+    return r;
+}
+__device__ __forceinline__ float3 h_fast(const StepParams& p, const HIn& a) {
+    const MatCoef* mc = p.coef + a.c;
+    const float4 x = __ldg(&mc->h[0]), y = __ldg(&mc->h[1]), z = __ldg(&mc->h[2]);
+    return make_float3(upd3_hx(x.x, a.hx, x.y, a.dEy_k, x.z, a.dEz_j), upd3(y.x, a.hy, y.y, a.dEz_i, y.z, a.dEx_k),
+                       upd3(z.x, a.hz, z.y, a.dEx_j, z.z, a.dEy_i));
+}
+__device__ __forceinline__ float3 h_any(const StepParams& p, const HIn& a, int i, int j, int k) {
+    if (a.c != kGeneral) return h_fast(p, a);
+    return h_slow(&p, i, j, k, a.hx, a.hy, a.hz, a.dEy_k, a.dEz_j, a.dEz_i, a.dEx_k, a.dEx_j, a.dEy_i);
+}
+
+__device__ __forceinline__ void store3(float* a, float* b, float* c, long long n, float3 v) {
+    a[n] = v.x; b[n] = v.y; c[n] = v.z;
 }
 
 }  // namespace
 
-// One sweep over the items of `items` (int4 {x0, y0, k0, k1}, one per CTA). INTERIOR selects the
-// interior instantiation (all nodes of its items are interior by construction of the list).
-template <bool INTERIOR>
-__global__ void __launch_bounds__(NTH, 4)
-k_fused(const __grid_constant__ FusedMaps maps, const __grid_constant__ StepParams p, FieldPtrs fo,
-        const __grid_constant__ PsiSet psi_in, const __grid_constant__ PsiSet psi_out,
-        const int4* __restrict__ items, long long m) {
+// Interior sweep over `items` (int4 {x0, y0, k0, k1}, one per CTA; plan_fused puts only interior
+// tiles and planes here). Per-thread ring offsets are fixed for the whole item, nothing is bounds-
+// checked, and the per-plane lumped / probe flags are read once into shared memory.
+__global__ void __launch_bounds__(NTH, 3)
+k_sweep_interior(const __grid_constant__ FusedMaps maps, const __grid_constant__ StepParams p, FieldPtrs fo,
+                 const int4* __restrict__ items, long long m) {
     extern __shared__ __align__(128) unsigned char smem[];
     float* enew = reinterpret_cast<float*>(smem + NSTAGE * STAGE_BYTES);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + NSTAGE * STAGE_BYTES + ENEW_BYTES);
+    uint8_t* pflags = reinterpret_cast<uint8_t*>(bars + NSTAGE);  // per plane: bit 0 lumped edges, bit 1 probes
     const DeviceGrid& g = p.g;
     const int tid = threadIdx.x;
     const int tx = tid % TX, ty = tid / TX;
     const int4 it = items[blockIdx.x];
     const int x0 = it.x, y0 = it.y, k0 = it.z, k1 = it.w;
-    const int kfirst = k0 - 1, klast = k1;  // planes streamed through the ring
+    const int kfirst = k0 - 1, klast = k1;
     const long long row = m % p.ring_cap;
+    // own nodes (tx, ty + r * RSTEP); ring / new-E offsets of row r are these plus r * RSTEP rows
+    const int i = x0 + tx, j = y0 + ty;
+    const int hi = (ty + 1) * HW + tx + 4, ei = ty * EW + tx, mi = (ty + 1) * MW + tx + 16, ni = ty * NW + tx;
+    // halo node of the first NHALO threads: row y0 + TY (warp 0), column x0 + TX (warp 1)
+    const bool halo = tid < NHALO;
+    const int hpx = tid < TX ? tid : TX, hpy = tid < TX ? TY : tid - TX;
+    const int hhi = (hpy + 1) * HW + hpx + 4, hei = hpy * EW + hpx, hmi = (hpy + 1) * MW + hpx + 16, hni = hpy * NW + hpx;
+    const long long n_own = (long long)j * g.pitch + i;
+    const long long n_row = (long long)RSTEP * g.pitch;
 
     if (tid == 0) {
         for (int s = 0; s < NSTAGE; ++s) mbar_init(&bars[s], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    for (int q = tid; q <= klast - kfirst; q += NTH) {  // klast - kfirst < kMaxItemPlanes (fused_chunk)
+        const int k = kfirst + q;
+        pflags[q] = (p.lumped_k[k] < p.lumped_k[k + 1] ? 1 : 0) | (p.probe_k[k] < p.probe_k[k + 1] ? 2 : 0);
+    }
     __syncthreads();
-
     auto issue = [&](int k, int s) {
         unsigned char* st = smem + s * STAGE_BYTES;
         mbar_expect_tx(&bars[s], TX_BYTES);
         for (int c = 0; c < 3; ++c) tma_load_3d(st + c * H_BYTES, &maps.h[c], &bars[s], x0 - 4, y0 - 1, k);
         for (int c = 0; c < 3; ++c) tma_load_3d(st + 3 * H_BYTES + c * E_BYTES, &maps.e[c], &bars[s], x0, y0, k);
-        tma_load_3d(st + 3 * H_BYTES + 3 * E_BYTES, &maps.mat, &bars[s], x0 - 16, y0 - 1, k);
+        tma_load_3d(st + 3 * H_BYTES + 3 * E_BYTES, &maps.cls, &bars[s], x0 - 16, y0 - 1, k);
     };
-    // stage of plane k is (k - kfirst) % NSTAGE: kept as rotating counters
     if (tid == 0)
         for (int q = 0; q < AHEAD && kfirst + q <= klast; ++q) issue(kfirst + q, q);
 
-    const PsiIO io_core{psi_in.f, psi_out.f, true};
-    const PsiIO io_halo{psi_in.f, psi_out.f, false};
-    int s_cur = 0, s_prv = NSTAGE - 1, s_pp = NSTAGE - 2, s_next = AHEAD % NSTAGE;
+    int s_cur = 0, s_prv = NSTAGE - 1, s_next = AHEAD % NSTAGE;
     uint32_t parity = 0;
-
     for (int k = kfirst; k <= klast; ++k) {
         if (tid == 0 && k + AHEAD <= klast) {
             fence_proxy_async();  // generic reads of the recycled stage precede the async writes
@@ -192,87 +274,60 @@ k_fused(const __grid_constant__ FusedMaps maps, const __grid_constant__ StepPara
         const StageView prv(smem + s_prv * STAGE_BYTES);
         float* en_cur = enew + (k & 1) * 3 * N_FLOATS;
         const float* en_prv = enew + ((k - 1) & 1) * 3 * N_FLOATS;
-
-        // ---- E(k) on the tile and its high-x column / high-y row ----
-        if (k >= k0 && k < g.nz) {
-            const bool store = k < k1;
-            const bool plane_lumped = p.lumped_k[k] < p.lumped_k[k + 1];
-            const bool plane_probe = p.probe_k[k] < p.probe_k[k + 1];
-            // pass 0: the thread's own node; pass 1: one of the TX + TY + 1 halo positions, dealt
-            // round-robin over the warps (halo h -> lane h / NWARP of warp h % NWARP)
-            for (int pass = 0; pass < 2; ++pass) {
-                int px, py;
-                if (pass == 0) { px = tx; py = ty; }
-                else {
-                    const int h = (tid % 32) * NWARP + tid / 32;
-                    if (h >= NHALO) break;
-                    if (h < TY + 1) { px = TX; py = h; } else { px = h - (TY + 1); py = TY; }
-                }
-                const int i = x0 + px, j = y0 + py;
-                if (i >= g.nx || j >= g.ny) continue;
-                const int hi = (py + 1) * HW + px + 4;   // (i, j) in the H tile
-                const int ei = py * EW + px;             // (i, j) in the old-E tile
-                const int mi = (py + 1) * MW + px + 16;  // cell (i, j) in the material tile
-                ENbr nb;
-                nb.ex = cur.e(0)[ei]; nb.ey = cur.e(1)[ei]; nb.ez = cur.e(2)[ei];
-                nb.hx = cur.h(0)[hi]; nb.hy = cur.h(1)[hi]; nb.hz = cur.h(2)[hi];
-                nb.hx_jm = cur.h(0)[hi - HW]; nb.hx_km = prv.h(0)[hi];
-                nb.hy_im = cur.h(1)[hi - 1]; nb.hy_km = prv.h(1)[hi];
-                nb.hz_im = cur.h(2)[hi - 1]; nb.hz_jm = cur.h(2)[hi - HW];
-                nb.m0 = cur.m()[mi]; nb.mi = cur.m()[mi - 1]; nb.mj = cur.m()[mi - MW]; nb.mij = cur.m()[mi - MW - 1];
-                nb.mk = prv.m()[mi]; nb.mik = prv.m()[mi - 1]; nb.mjk = prv.m()[mi - MW];
-                const bool own = store && pass == 0;
-                float out[3], pre[3];
-                if (INTERIOR) {
-                    e_interior(p, nb, i, j, k, m, plane_lumped, out);
-                    pre[0] = out[0]; pre[1] = out[1]; pre[2] = out[2];
-                } else {
-                    e_update(p, nb, i, j, k, m, plane_lumped, own ? io_core : io_halo, out, pre);
-                }
-                const int ni = py * NW + px;
-                en_cur[ni] = out[0]; en_cur[N_FLOATS + ni] = out[1]; en_cur[2 * N_FLOATS + ni] = out[2];
-                if (own) {
-                    const long long n = (long long)k * g.plane + (long long)j * g.pitch + i;
-                    fo.ex[n] = out[0]; fo.ey[n] = out[1]; fo.ez[n] = out[2];
-                    if (plane_probe)
-                        for (int c = 0; c < 3; ++c) sample(p, row, c, i, j, k, pre[c]);
+        if (k >= k0) {
+            // ---- E(k): own nodes (stored below plane k1), then the halo nodes ----
+            const int fl = pflags[k - kfirst];
+            const EIn a0 = e_load(cur, prv, hi, ei, mi);
+            const EIn a1 = e_load(cur, prv, hi + RSTEP * HW, ei + RSTEP * EW, mi + RSTEP * MW);
+            float3 v0, v1;
+            if (a0.c != kGeneral && a1.c != kGeneral) {
+                v0 = e_fast(p, a0);
+                v1 = e_fast(p, a1);
+            } else {
+                v0 = e_any(p, a0, i, j, k, m, fl & 1);
+                v1 = e_any(p, a1, i, j + RSTEP, k, m, fl & 1);
+            }
+            en_cur[ni] = v0.x; en_cur[N_FLOATS + ni] = v0.y; en_cur[2 * N_FLOATS + ni] = v0.z;
+            const int ni1 = ni + RSTEP * NW;
+            en_cur[ni1] = v1.x; en_cur[N_FLOATS + ni1] = v1.y; en_cur[2 * N_FLOATS + ni1] = v1.z;
+            if (k < k1) {
+                const long long n = (long long)k * g.plane + n_own;
+                store3(fo.ex, fo.ey, fo.ez, n, v0);
+                store3(fo.ex, fo.ey, fo.ez, n + n_row, v1);
+                if (fl & 2) {
+                    sample(p, row, 0, i, j, k, v0.x); sample(p, row, 1, i, j, k, v0.y); sample(p, row, 2, i, j, k, v0.z);
+                    sample(p, row, 0, i, j + RSTEP, k, v1.x); sample(p, row, 1, i, j + RSTEP, k, v1.y);
+                    sample(p, row, 2, i, j + RSTEP, k, v1.z);
                 }
             }
-        }
-
-        // ---- H(k-1) on the tile ----
-        const int kh = k - 1;
-        if (kh >= k0 && kh < k1) {
-            const int i = x0 + tx, j = y0 + ty;
-            if (i < g.nx && j < g.ny) {
-                const StageView mst(smem + s_pp * STAGE_BYTES);  // plane kh - 1
-                const int hi = (ty + 1) * HW + tx + 4;
-                const int mi = (ty + 1) * MW + tx + 16;
-                const int ni = ty * NW + tx;
-                HNbr nb;
-                nb.hx = prv.h(0)[hi]; nb.hy = prv.h(1)[hi]; nb.hz = prv.h(2)[hi];
-                nb.ex = en_prv[ni]; nb.ey = en_prv[N_FLOATS + ni]; nb.ez = en_prv[2 * N_FLOATS + ni];
-                nb.ey_kp = en_cur[N_FLOATS + ni];
-                nb.ex_kp = en_cur[ni];
-                nb.ez_jp = en_prv[2 * N_FLOATS + ni + NW];
-                nb.ex_jp = en_prv[ni + NW];
-                nb.ez_ip = en_prv[2 * N_FLOATS + ni + 1];
-                nb.ey_ip = en_prv[N_FLOATS + ni + 1];
-                nb.m0 = prv.m()[mi]; nb.mi = prv.m()[mi - 1]; nb.mj = prv.m()[mi - MW]; nb.mk = mst.m()[mi];
-                float out[3], pre[3];
-                if (INTERIOR) {
-                    h_interior(p, nb, out);
-                    pre[0] = out[0]; pre[1] = out[1]; pre[2] = out[2];
-                } else {
-                    h_update(p, nb, i, j, kh, io_core, out, pre);
-                }
-                const long long n = (long long)kh * g.plane + (long long)j * g.pitch + i;
-                fo.hx[n] = out[0]; fo.hy[n] = out[1]; fo.hz[n] = out[2];
-                if (p.probe_k[kh] < p.probe_k[kh + 1])
-                    for (int c = 0; c < 3; ++c) sample(p, row, 3 + c, i, j, kh, pre[c]);
+            if (halo) {
+                const EIn a = e_load(cur, prv, hhi, hei, hmi);
+                const float3 w = e_any(p, a, x0 + hpx, y0 + hpy, k, m, fl & 1);
+                en_cur[hni] = w.x; en_cur[N_FLOATS + hni] = w.y; en_cur[2 * N_FLOATS + hni] = w.z;
             }
         }
-
+        if (k > k0) {
+            // ---- H(k-1) of the own nodes from E(k-1), E(k) and the old H(k-1) ----
+            const int kh = k - 1;
+            const HIn a0 = h_load(prv, en_prv, en_cur, hi, mi, ni);
+            const HIn a1 = h_load(prv, en_prv, en_cur, hi + RSTEP * HW, mi + RSTEP * MW, ni + RSTEP * NW);
+            float3 v0, v1;
+            if (a0.c != kGeneral && a1.c != kGeneral) {
+                v0 = h_fast(p, a0);
+                v1 = h_fast(p, a1);
+            } else {
+                v0 = h_any(p, a0, i, j, kh);
+                v1 = h_any(p, a1, i, j + RSTEP, kh);
+            }
+            const long long n = (long long)kh * g.plane + n_own;
+            store3(fo.hx, fo.hy, fo.hz, n, v0);
+            store3(fo.hx, fo.hy, fo.hz, n + n_row, v1);
+            if (pflags[kh - kfirst] & 2) {
+                sample(p, row, 3, i, j, kh, v0.x); sample(p, row, 4, i, j, kh, v0.y); sample(p, row, 5, i, j, kh, v0.z);
+                sample(p, row, 3, i, j + RSTEP, kh, v1.x); sample(p, row, 4, i, j + RSTEP, kh, v1.y);
+                sample(p, row, 5, i, j + RSTEP, kh, v1.z);
+            }
+        }
         if (__syncthreads_or(!ok)) {
             // A plane never arrived: record it, wait (bounded) for the copies still in flight, exit.
             if (tid == 0) {
@@ -287,35 +342,43 @@ k_fused(const __grid_constant__ FusedMaps maps, const __grid_constant__ StepPara
             __syncthreads();
             return;
         }
-        // rotate the ring counters
-        s_pp = s_prv; s_prv = s_cur;
+        s_prv = s_cur;
         if (++s_cur == NSTAGE) { s_cur = 0; parity ^= 1u; }
         if (++s_next == NSTAGE) s_next = 0;
     }
 }
 
-int fused_smem_bytes() { return SMEM_BYTES; }
+int fused_smem_bytes() { return SMEM_INTERIOR; }
 int fused_tile_x() { return TX; }
 int fused_tile_y() { return TY; }
 
+// Planes per interior item: whole columns unless that leaves too few CTAs to fill the GPU, and at
+// most kMaxItemPlanes - 2 (the item also streams the plane below and recomputes the one above).
+int fused_chunk(const DeviceGrid& g) {
+    const long long tiles = (long long)((g.nx + TX - 1) / TX) * ((g.ny + TY - 1) / TY);
+    int kc = g.nz;
+    while (kc > 16 && tiles * ((g.nz + kc - 1) / kc) < 4096) kc = (kc + 1) / 2;
+    return kc < kMaxItemPlanes - 2 ? kc : kMaxItemPlanes - 2;
+}
+
 cudaError_t fused_configure() {
-    cudaError_t e = cudaFuncSetAttribute(k_fused<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    return cudaFuncSetAttribute(k_sweep_interior, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_INTERIOR);
+}
+
+// One fused step: shell E (general items), interior sweep, shell H (general items).
+cudaError_t launch_fused(const FusedMaps& maps, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo,
+                         const PsiSet& psi_in, const PsiSet& psi_out, long long m, const FusedWork& w, cudaStream_t st) {
+    cudaError_t e = launch_shell(true, p, fi, fo, psi_in, psi_out, w.general, w.n_general, TY, m, st);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_fused<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (w.n_interior > 0) k_sweep_interior<<<w.n_interior, NTH, SMEM_INTERIOR, st>>>(maps, p, fo, w.interior, m);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return launch_shell(false, p, fi, fo, psi_in, psi_out, w.general, w.n_general, TY, m, st);
 }
 
-cudaError_t launch_fused(const FusedMaps& maps, const StepParams& p, const FieldPtrs& fo, const PsiSet& psi_in,
-                         const PsiSet& psi_out, long long m, const FusedWork& w, cudaStream_t st) {
-    if (w.n_interior > 0)
-        k_fused<true><<<w.n_interior, NTH, SMEM_BYTES, st>>>(maps, p, fo, psi_in, psi_out, w.interior, m);
-    if (w.n_general > 0)
-        k_fused<false><<<w.n_general, NTH, SMEM_BYTES, st>>>(maps, p, fo, psi_in, psi_out, w.general, m);
-    return cudaGetLastError();
-}
-
-// Tensor maps of the buffers a sweep reads: H tiles with a one-node halo (x widened to 16-byte
-// boundaries), old-E tiles, material tiles. Coordinates outside the arrays load as zeros.
-int encode_fused_maps(FusedMaps* out, const DeviceGrid& g, float* const h[3], float* const e[3], const uint8_t* mat,
+// Tensor maps of the buffers the interior sweep reads: H tiles with a one-node halo (x widened to
+// 16-byte boundaries), old-E tiles, node-class tiles. Coordinates outside the arrays load as zeros.
+int encode_fused_maps(FusedMaps* out, const DeviceGrid& g, float* const h[3], float* const e[3], const uint8_t* cls,
                       void* encode_fn) {
     auto encode = reinterpret_cast<CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
@@ -333,7 +396,7 @@ int encode_fused_maps(FusedMaps* out, const DeviceGrid& g, float* const h[3], fl
                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
             return -1;
     }
-    if (encode(&out->mat, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, (void*)mat, dims, mstr, mbox, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+    if (encode(&out->cls, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, (void*)cls, dims, mstr, mbox, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return -1;
     return 0;
@@ -343,7 +406,9 @@ int encode_fused_maps(FusedMaps* out, const DeviceGrid& g, float* const h[3], fl
 // interior get their interior planes as interior items (chunks of at most kc planes); everything
 // else (boundary / CPML tiles, and the z-boundary and z-CPML planes of interior tiles) becomes
 // general items. The E positions of plane k1 of an item are recomputed, so a chunk must also keep
-// its top plane in the interior range to stay interior.
+// its top plane in the interior range to stay interior. The tile grid starts at (ox, oy) <= 0,
+// chosen to put as many nodes as possible in interior tiles; ox is a multiple of 16 so that every
+// TMA box starts on a 16-byte boundary (material box at x0 - 16, one byte per cell).
 void plan_fused(const DeviceGrid& g, int kc, std::vector<int4>& interior_items, std::vector<int4>& general_items) {
     interior_items.clear();
     general_items.clear();
@@ -351,13 +416,27 @@ void plan_fused(const DeviceGrid& g, int kc, std::vector<int4>& interior_items, 
         const int lo = pn > 1 ? pn : 1, hi = (n - 1 - pp < n - 2) ? n - 1 - pp : n - 2;
         return q >= lo && q <= hi;
     };
+    auto interior_tiles = [&](int start, int step, int n, int pn, int pp) {
+        int c = 0;
+        for (int q = start; q < n; q += step) c += inside(q, n, pn, pp) && inside(q + step, n, pn, pp);
+        return c;
+    };
+    int ox = 0, oy = 0, best_x = -1, best_y = -1;
+    for (int o = 0; o > -TX; o -= 16) {
+        const int c = interior_tiles(o, TX, g.nx, g.pxn, g.pxp);
+        if (c > best_x) { best_x = c; ox = o; }
+    }
+    for (int o = 0; o > -TY; --o) {
+        const int c = interior_tiles(o, TY, g.ny, g.pyn, g.pyp);
+        if (c > best_y) { best_y = c; oy = o; }
+    }
     const int zlo = g.pzn > 1 ? g.pzn : 1;
     const int zhi = (g.nz - 1 - g.pzp < g.nz - 2) ? g.nz - 1 - g.pzp : g.nz - 2;  // last interior plane
     auto chunks = [&](std::vector<int4>& out, int x0, int y0, int a, int b) {  // planes [a, b)
         for (int k = a; k < b; k += kc) out.push_back(make_int4(x0, y0, k, k + kc < b ? k + kc : b));
     };
-    for (int y0 = 0; y0 < g.ny; y0 += TY)
-        for (int x0 = 0; x0 < g.nx; x0 += TX) {
+    for (int y0 = oy; y0 < g.ny; y0 += TY)
+        for (int x0 = ox; x0 < g.nx; x0 += TX) {
             const bool tile_int = inside(x0, g.nx, g.pxn, g.pxp) && inside(x0 + TX, g.nx, g.pxn, g.pxp) &&
                                   inside(y0, g.ny, g.pyn, g.pyp) && inside(y0 + TY, g.ny, g.pyn, g.pyp);
             // interior items cover planes [zlo, zhi) so that the recomputed top plane <= zhi

@@ -22,15 +22,21 @@ struct PsiSet {
 cudaError_t launch_two_pass(const StepParams& p, const FieldPtrs& f, const PsiSet& ps, long long m,
                             cudaStream_t st);
 
-// Fused z-marching sweep (yee_fused.cu): reads fields through TMA tensor maps of buffer A (H with
-// halo, old E, material index) and writes buffer B; CPML memory psi_in -> psi_out.
+// Shell passes of the fused schedule (yee_two_pass.cu): E (e_pass) or H of the nodes of `items`,
+// reading fi / pin (buffer A) and writing fo / pout (buffer B).
+cudaError_t launch_shell(bool e_pass, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
+                         const PsiSet& pout, const int4* items, int n_items, int tile_h, long long m, cudaStream_t st);
+
+// Fused schedule (yee_fused.cu): per step the shell E pass, the z-marching interior sweep (TMA
+// tiles of buffer A: H with halo, old E, node class) and the shell H pass; fields A -> B, CPML
+// memory psi_in -> psi_out.
 struct FusedMaps {
     CUtensorMap h[3];
     CUtensorMap e[3];
-    CUtensorMap mat;
+    CUtensorMap cls;
 };
-// Work items of one sweep (device arrays of int4 {x0, y0, k0, k1}), split into interior and
-// general items (plan_fused).
+// Work items of one step (device arrays of int4 {x0, y0, k0, k1}): interior items for the sweep,
+// general items for the shell passes (plan_fused).
 struct FusedWork {
     const int4* interior;
     int n_interior;
@@ -39,13 +45,14 @@ struct FusedWork {
 };
 cudaError_t fused_configure();
 int fused_smem_bytes();
+int fused_chunk(const DeviceGrid& g);
 int fused_tile_x();
 int fused_tile_y();
 void plan_fused(const DeviceGrid& g, int kc, std::vector<int4>& interior_items, std::vector<int4>& general_items);
-cudaError_t launch_fused(const FusedMaps& maps, const StepParams& p, const FieldPtrs& fo, const PsiSet& psi_in,
-                         const PsiSet& psi_out, long long m, const FusedWork& w, cudaStream_t st);
+cudaError_t launch_fused(const FusedMaps& maps, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo,
+                         const PsiSet& psi_in, const PsiSet& psi_out, long long m, const FusedWork& w, cudaStream_t st);
 // encode_fn: the driver's cuTensorMapEncodeTiled. Returns 0 on success.
-int encode_fused_maps(FusedMaps* out, const DeviceGrid& g, float* const h[3], float* const e[3], const uint8_t* mat,
+int encode_fused_maps(FusedMaps* out, const DeviceGrid& g, float* const h[3], float* const e[3], const uint8_t* cls,
                       void* encode_fn);
 
 // Setup kernels (setup_kernels.cu).
@@ -60,6 +67,9 @@ cudaError_t launch_lumped_coefs(const DeviceGrid& g, const uint8_t* mat, const M
 cudaError_t launch_bg_curl(const DeviceGrid& g, const MatCoef* coef, int bg, const float* const* kappa_dev,
                            float* const* out_dev, cudaStream_t st);
 cudaError_t launch_fill(float* p, long long n, float v, cudaStream_t st);
+// Node classes (StepParams::cls) from the material index and the lumped edges.
+cudaError_t launch_node_class(const DeviceGrid& g, const uint8_t* mat, const LumpedEdge* edges, int n_edges, uint8_t* cls,
+                              cudaStream_t st);
 cudaError_t launch_paint(uint8_t* mat, const DeviceGrid& g, const int box[6], uint8_t value, cudaStream_t st);
 
 }  // namespace fdtd

@@ -8,86 +8,143 @@
 
 namespace fdtd {
 
-__global__ void __launch_bounds__(256) k_update_e(const __grid_constant__ StepParams p, FieldPtrs f,
-                                                  const __grid_constant__ PsiSet ps, long long m) {
+// One node's E (or H) update reading the fields `fi` and CPML memory `pin`, writing `fo` / `pout`
+// (the same buffers for the in-place two-pass schedule). Every node loads its twelve field values
+// and its class byte together (one round of memory latency); fast-path nodes (class != kGeneral)
+// then update from the material table, the rest also gather the seven cell materials and take
+// e_update / h_update.
+__device__ __forceinline__ void e_node_global(const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo,
+                                              const PsiSet& pin, const PsiSet& pout, int i, int j, int k, long long m) {
     const DeviceGrid& g = p.g;
-    const int i = blockIdx.x * 32 + threadIdx.x;
-    const int j = blockIdx.y * 8 + threadIdx.y;
-    const int k = blockIdx.z;
-    if (i >= g.nx || j >= g.ny) return;
     const long long n = (long long)k * g.plane + (long long)j * g.pitch + i;
     const long long P = g.plane, R = g.pitch;
-    const uint8_t* mat = p.mat;
     ENbr nb;
-    nb.ex = f.ex[n]; nb.ey = f.ey[n]; nb.ez = f.ez[n];
-    nb.hx = f.hx[n]; nb.hy = f.hy[n]; nb.hz = f.hz[n];
-    nb.hx_jm = j > 0 ? f.hx[n - R] : 0.f;
-    nb.hx_km = k > 0 ? f.hx[n - P] : 0.f;
-    nb.hy_im = i > 0 ? f.hy[n - 1] : 0.f;
-    nb.hy_km = k > 0 ? f.hy[n - P] : 0.f;
-    nb.hz_im = i > 0 ? f.hz[n - 1] : 0.f;
-    nb.hz_jm = j > 0 ? f.hz[n - R] : 0.f;
-    nb.m0 = mat[n];
-    nb.mi = i > 0 ? mat[n - 1] : 0;
-    nb.mj = j > 0 ? mat[n - R] : 0;
-    nb.mk = k > 0 ? mat[n - P] : 0;
-    nb.mij = (i > 0 && j > 0) ? mat[n - 1 - R] : 0;
-    nb.mik = (i > 0 && k > 0) ? mat[n - 1 - P] : 0;
-    nb.mjk = (j > 0 && k > 0) ? mat[n - R - P] : 0;
+    nb.ex = fi.ex[n]; nb.ey = fi.ey[n]; nb.ez = fi.ez[n];
+    nb.hx = fi.hx[n]; nb.hy = fi.hy[n]; nb.hz = fi.hz[n];
+    nb.hx_jm = j > 0 ? fi.hx[n - R] : 0.f;
+    nb.hx_km = k > 0 ? fi.hx[n - P] : 0.f;
+    nb.hy_im = i > 0 ? fi.hy[n - 1] : 0.f;
+    nb.hy_km = k > 0 ? fi.hy[n - P] : 0.f;
+    nb.hz_im = i > 0 ? fi.hz[n - 1] : 0.f;
+    nb.hz_jm = j > 0 ? fi.hz[n - R] : 0.f;
+    const int c = p.cls[n];
     float out[3], pre[3];
-    const PsiIO io{ps.f, ps.f, true};
-    const bool plane_lumped = p.lumped_k[k] < p.lumped_k[k + 1];
-    if (!plane_lumped && interior(i, g.nx, g.pxn, g.pxp) && interior(j, g.ny, g.pyn, g.pyp) &&
-        interior(k, g.nz, g.pzn, g.pzp) && e_uniform(nb)) {
-        e_update_interior(p, nb, out);
+    if (c != kGeneral) {
+        e_update_interior(p, c, nb.ex, nb.ey, nb.ez, __fsub_rn(nb.hz, nb.hz_jm), __fsub_rn(nb.hy, nb.hy_km),
+                          __fsub_rn(nb.hx, nb.hx_km), __fsub_rn(nb.hz, nb.hz_im), __fsub_rn(nb.hy, nb.hy_im),
+                          __fsub_rn(nb.hx, nb.hx_jm), out);
         pre[0] = out[0]; pre[1] = out[1]; pre[2] = out[2];
     } else {
+        const uint8_t* mat = p.mat;
+        nb.m0 = mat[n];
+        nb.mi = i > 0 ? mat[n - 1] : 0;
+        nb.mj = j > 0 ? mat[n - R] : 0;
+        nb.mk = k > 0 ? mat[n - P] : 0;
+        nb.mij = (i > 0 && j > 0) ? mat[n - 1 - R] : 0;
+        nb.mik = (i > 0 && k > 0) ? mat[n - 1 - P] : 0;
+        nb.mjk = (j > 0 && k > 0) ? mat[n - R - P] : 0;
+        const PsiIO io{pin.f, pout.f, true};
+        const bool plane_lumped = p.lumped_k[k] < p.lumped_k[k + 1];
         e_update(p, nb, i, j, k, m, plane_lumped, io, out, pre);
     }
-    f.ex[n] = out[0]; f.ey[n] = out[1]; f.ez[n] = out[2];
+    fo.ex[n] = out[0]; fo.ey[n] = out[1]; fo.ez[n] = out[2];
     if (p.probe_k[k] < p.probe_k[k + 1]) {
         const long long row = m % p.ring_cap;
-        for (int c = 0; c < 3; ++c) sample(p, row, c, i, j, k, pre[c]);
+        for (int q = 0; q < 3; ++q) sample(p, row, q, i, j, k, pre[q]);
     }
+}
+
+// H reads the old H from `fi` and the new E from `fe`.
+__device__ __forceinline__ void h_node_global(const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fe,
+                                              const FieldPtrs& fo, const PsiSet& pin, const PsiSet& pout, int i, int j,
+                                              int k, long long m) {
+    const DeviceGrid& g = p.g;
+    const long long n = (long long)k * g.plane + (long long)j * g.pitch + i;
+    const long long P = g.plane, R = g.pitch;
+    HNbr nb;
+    nb.hx = fi.hx[n]; nb.hy = fi.hy[n]; nb.hz = fi.hz[n];
+    nb.ex = fe.ex[n]; nb.ey = fe.ey[n]; nb.ez = fe.ez[n];
+    nb.ey_kp = k < g.nz - 1 ? fe.ey[n + P] : 0.f;
+    nb.ez_jp = j < g.ny - 1 ? fe.ez[n + R] : 0.f;
+    nb.ez_ip = i < g.nx - 1 ? fe.ez[n + 1] : 0.f;
+    nb.ex_kp = k < g.nz - 1 ? fe.ex[n + P] : 0.f;
+    nb.ex_jp = j < g.ny - 1 ? fe.ex[n + R] : 0.f;
+    nb.ey_ip = i < g.nx - 1 ? fe.ey[n + 1] : 0.f;
+    const int c = p.cls[n];
+    float out[3], pre[3];
+    if (c != kGeneral) {
+        h_update_interior(p, c, nb.hx, nb.hy, nb.hz, __fsub_rn(nb.ey_kp, nb.ey), __fsub_rn(nb.ez_jp, nb.ez),
+                          __fsub_rn(nb.ez_ip, nb.ez), __fsub_rn(nb.ex_kp, nb.ex), __fsub_rn(nb.ex_jp, nb.ex),
+                          __fsub_rn(nb.ey_ip, nb.ey), out);
+        pre[0] = out[0]; pre[1] = out[1]; pre[2] = out[2];
+    } else {
+        const uint8_t* mat = p.mat;
+        nb.m0 = mat[n];
+        nb.mi = i > 0 ? mat[n - 1] : 0;
+        nb.mj = j > 0 ? mat[n - R] : 0;
+        nb.mk = k > 0 ? mat[n - P] : 0;
+        const PsiIO io{pin.f, pout.f, true};
+        h_update(p, nb, i, j, k, io, out, pre);
+    }
+    fo.hx[n] = out[0]; fo.hy[n] = out[1]; fo.hz[n] = out[2];
+    if (p.probe_k[k] < p.probe_k[k + 1]) {
+        const long long row = m % p.ring_cap;
+        for (int q = 0; q < 3; ++q) sample(p, row, 3 + q, i, j, k, pre[q]);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_update_e(const __grid_constant__ StepParams p, FieldPtrs f,
+                                                  const __grid_constant__ PsiSet ps, long long m) {
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    if (i >= p.g.nx || j >= p.g.ny) return;
+    e_node_global(p, f, f, ps, ps, i, j, blockIdx.z, m);
 }
 
 __global__ void __launch_bounds__(256) k_update_h(const __grid_constant__ StepParams p, FieldPtrs f,
                                                   const __grid_constant__ PsiSet ps, long long m) {
-    const DeviceGrid& g = p.g;
     const int i = blockIdx.x * 32 + threadIdx.x;
     const int j = blockIdx.y * 8 + threadIdx.y;
-    const int k = blockIdx.z;
-    if (i >= g.nx || j >= g.ny) return;
-    const long long n = (long long)k * g.plane + (long long)j * g.pitch + i;
-    const long long P = g.plane, R = g.pitch;
-    const uint8_t* mat = p.mat;
-    HNbr nb;
-    nb.hx = f.hx[n]; nb.hy = f.hy[n]; nb.hz = f.hz[n];
-    nb.ex = f.ex[n]; nb.ey = f.ey[n]; nb.ez = f.ez[n];
-    nb.ey_kp = k < g.nz - 1 ? f.ey[n + P] : 0.f;
-    nb.ez_jp = j < g.ny - 1 ? f.ez[n + R] : 0.f;
-    nb.ez_ip = i < g.nx - 1 ? f.ez[n + 1] : 0.f;
-    nb.ex_kp = k < g.nz - 1 ? f.ex[n + P] : 0.f;
-    nb.ex_jp = j < g.ny - 1 ? f.ex[n + R] : 0.f;
-    nb.ey_ip = i < g.nx - 1 ? f.ey[n + 1] : 0.f;
-    nb.m0 = mat[n];
-    nb.mi = i > 0 ? mat[n - 1] : 0;
-    nb.mj = j > 0 ? mat[n - R] : 0;
-    nb.mk = k > 0 ? mat[n - P] : 0;
-    float out[3], pre[3];
-    const PsiIO io{ps.f, ps.f, true};
-    if (interior(i, g.nx, g.pxn, g.pxp) && interior(j, g.ny, g.pyn, g.pyp) && interior(k, g.nz, g.pzn, g.pzp) &&
-        h_uniform(nb)) {
-        h_update_interior(p, nb, out);
-        pre[0] = out[0]; pre[1] = out[1]; pre[2] = out[2];
-    } else {
-        h_update(p, nb, i, j, k, io, out, pre);
+    if (i >= p.g.nx || j >= p.g.ny) return;
+    h_node_global(p, f, f, f, ps, ps, i, j, blockIdx.z, m);
+}
+
+// Shell passes of the fused schedule: the nodes of the general items (int4 {x0, y0, k0, k1}, a
+// 32 x tile_h tile and a plane range; x0, y0 may be negative) read buffer A (`fi`, `pin`) and
+// write buffer B (`fo`, `pout`). The E pass runs before the interior sweep, the H pass after it,
+// since H reads new E at interior nodes next to the shell.
+__global__ void __launch_bounds__(256) k_shell_e(const __grid_constant__ StepParams p, FieldPtrs fi, FieldPtrs fo,
+                                                 const __grid_constant__ PsiSet pin, const __grid_constant__ PsiSet pout,
+                                                 const int4* __restrict__ items, int tile_h, long long m) {
+    const int4 it = items[blockIdx.x];
+    const int i = it.x + (int)threadIdx.x;
+    if (i < 0 || i >= p.g.nx) return;
+    for (int r = threadIdx.y; r < tile_h; r += 8) {
+        const int j = it.y + r;
+        if (j < 0 || j >= p.g.ny) continue;
+        for (int k = it.z; k < it.w; ++k) e_node_global(p, fi, fo, pin, pout, i, j, k, m);
     }
-    f.hx[n] = out[0]; f.hy[n] = out[1]; f.hz[n] = out[2];
-    if (p.probe_k[k] < p.probe_k[k + 1]) {
-        const long long row = m % p.ring_cap;
-        for (int c = 0; c < 3; ++c) sample(p, row, 3 + c, i, j, k, pre[c]);
+}
+
+__global__ void __launch_bounds__(256) k_shell_h(const __grid_constant__ StepParams p, FieldPtrs fi, FieldPtrs fo,
+                                                 const __grid_constant__ PsiSet pin, const __grid_constant__ PsiSet pout,
+                                                 const int4* __restrict__ items, int tile_h, long long m) {
+    const int4 it = items[blockIdx.x];
+    const int i = it.x + (int)threadIdx.x;
+    if (i < 0 || i >= p.g.nx) return;
+    for (int r = threadIdx.y; r < tile_h; r += 8) {
+        const int j = it.y + r;
+        if (j < 0 || j >= p.g.ny) continue;
+        for (int k = it.z; k < it.w; ++k) h_node_global(p, fi, fo, fo, pin, pout, i, j, k, m);
     }
+}
+
+cudaError_t launch_shell(bool e_pass, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
+                         const PsiSet& pout, const int4* items, int n_items, int tile_h, long long m, cudaStream_t st) {
+    if (n_items <= 0) return cudaSuccess;
+    if (e_pass) k_shell_e<<<n_items, dim3(32, 8, 1), 0, st>>>(p, fi, fo, pin, pout, items, tile_h, m);
+    else k_shell_h<<<n_items, dim3(32, 8, 1), 0, st>>>(p, fi, fo, pin, pout, items, tile_h, m);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_two_pass(const StepParams& p, const FieldPtrs& f, const PsiSet& ps, long long m,
