@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "../../include/fdtd_api.h"
+#include "adjoint.h"
 #include "yee_kernels.h"
 
 using namespace fdtd;
@@ -102,6 +103,31 @@ struct fdtd_handle {
     long long step = 0;
     long long bytes = 0;
 
+    // design region (cells of material kDesign, per-cell eps_r)
+    bool has_design = false;
+    int dbox[6] = {};
+    fdtd_material design_base{};
+    float* d_deps = nullptr;
+
+    // adjoint: buffers of fdtd_adjoint_forward / fdtd_adjoint_backward
+    struct Adjoint {
+        bool ready = false;            // a forward has run and its records are valid
+        long long n = 0, start = 0;    // steps and first step of the forward
+        int K = 0;                     // checkpoint interval (0: design E of every step kept)
+        long long probe = 0;           // node index of the FoM probe
+        AdjState st{};
+        PsiSet psa{};                  // CPML adjoint memory
+        float* samples = nullptr;      // Ez(p) per forward step (device)
+        std::vector<float> host_samples;
+        float* hist = nullptr;         // design-edge-box E snapshots
+        long long hist_slots = 0;
+        char* ckpt = nullptr;          // checkpoints (K > 0) and the final state
+        long long ckpt_slots = 0;
+        double* acc = nullptr;         // per-edge gradient accumulators
+        double* grad = nullptr;        // per-cell gradient
+        std::vector<void*> bufs;       // everything above, for release
+    } adj;
+
     // host-side work list of fdtd_step_static_scratch (interior items first), planned on first use
     std::vector<int4> static_items;
     int static_n_interior = -1;
@@ -126,6 +152,8 @@ namespace {
 
 long long vol(const fdtd_handle* h) { return h->g.plane * (long long)h->g.nz; }
 
+bool in_slab_host(int q, int n, int pn, int pp) { return q < pn || q >= n - pp; }
+
 StepParams make_params(fdtd_handle* h) {
     StepParams p{};
     p.g = h->g;
@@ -148,6 +176,8 @@ StepParams make_params(fdtd_handle* h) {
     p.n_probes = (int)h->probes.size();
     p.ring_cap = h->ring_cap;
     p.status = h->status;
+    p.deps = h->has_design ? h->d_deps : nullptr;
+    for (int q = 0; q < 6; ++q) p.dbox[q] = h->dbox[q];
     p.bg.mat = 0;  // the background material fills the CPML slabs in the usual layouts
     for (int a = 0; a < 3; ++a)
         for (int s = 0; s < 2; ++s) {
@@ -360,6 +390,8 @@ int fdtd_set_materials(fdtd_handle* h, const fdtd_material* table, int32_t n) {
     }
     if (h->prepared && n < (int)h->materials.size())
         return fail(FDTD_ERR_STATE, "cannot shrink the material table after the index uses it");
+    if (h->has_design && n > kDesign)
+        return fail(FDTD_ERR_INVALID, "material index 255 is reserved for the design region: at most 255 materials");
     h->materials.assign(table, table + n);
     h->dirty_materials = true;
     return FDTD_OK;
@@ -562,6 +594,38 @@ int fdtd_set_field_device(fdtd_handle* h, int32_t comp, const float* in) {
     return FDTD_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Copy the dynamic state (6 fields, then the 24 CPML arrays) to or from a device buffer on the
+// handle's stream, without synchronising. Loading writes both field buffers of the fused schedule.
+int state_copy(fdtd_handle* h, void* buf, bool save) {
+    char* p = (char*)buf;
+    const size_t V = (size_t)vol(h) * sizeof(float);
+    const int a = h->cur, nb = h->have_second ? 2 : 1;
+    for (int c = 0; c < 6; ++c, p += V) {
+        if (save) CUDA_TRY(cudaMemcpyAsync(p, h->field[a][c], V, cudaMemcpyDeviceToDevice, h->stream));
+        else
+            for (int b = 0; b < nb; ++b) CUDA_TRY(cudaMemcpyAsync(h->field[b][c], p, V, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    for (int f = 0; f < 6; ++f) {
+        const size_t n = (size_t)h->psi_elems[f] * sizeof(float);
+        float* arr[4];
+        psi_arrays(h, a, f, arr);
+        for (int q = 0; q < 4; ++q, p += n) {
+            if (!n) continue;
+            if (save) CUDA_TRY(cudaMemcpyAsync(p, arr[q], n, cudaMemcpyDeviceToDevice, h->stream));
+            else CUDA_TRY(cudaMemcpyAsync(arr[q], p, n, cudaMemcpyDeviceToDevice, h->stream));
+        }
+    }
+    return FDTD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int64_t fdtd_state_bytes(const fdtd_handle* h) {
     if (!h) return -1;
     long long n = 6 * vol(h);
@@ -731,11 +795,13 @@ int ensure_prepared(fdtd_handle* h) {
     if (h->dirty_materials || !h->prepared) {
         std::vector<MatProps> props(kMaxMaterials);
         for (int q = 0; q < kMaxMaterials; ++q) {
-            const fdtd_material m = q < (int)h->materials.size() ? h->materials[q] : fdtd_material{1.0f, kTiny, 1.0f, kTiny};
+            fdtd_material m = q < (int)h->materials.size() ? h->materials[q] : fdtd_material{1.0f, kTiny, 1.0f, kTiny};
+            if (q == kDesign && h->has_design) m = h->design_base;  // eps_r comes per cell
             props[q] = MatProps{m.eps_r, m.sigma_e, m.mu_r, m.sigma_m};
         }
         CUDA_TRY(cudaMemcpy(h->props, props.data(), sizeof(MatProps) * kMaxMaterials, cudaMemcpyHostToDevice));
-        CUDA_TRY(launch_material_tables(h->g, h->props, (int)h->materials.size(), h->coef, h->stream));
+        const int n_tab = h->has_design ? kMaxMaterials : (int)h->materials.size();
+        CUDA_TRY(launch_material_tables(h->g, h->props, n_tab, h->coef, h->stream));
         if (!h->prepared) CUDA_TRY(launch_cpml_profiles(h->g, h->grid.pi, h->prof, h->stream));
         CUDA_TRY(launch_bg_curl(h->g, h->coef, 0, h->d_kappa_ptrs, h->d_bg_ptrs, h->stream));
         h->dirty_materials = false;
@@ -913,5 +979,206 @@ extern "C" int fdtd_step_static_scratch(fdtd_handle* h, int64_t n) {
             for (int q = 0; q < 4; ++q) CUDA_TRY(cudaMemcpyAsync(dst[q], src[q], nb, cudaMemcpyDeviceToDevice, h->stream));
         }
     }
+    return FDTD_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Design region and discrete adjoint (no reference counterpart).
+// ---------------------------------------------------------------------------------------------
+extern "C" int fdtd_set_design_region(fdtd_handle* h, const int32_t box[6], const fdtd_material* base, const float* eps_r) {
+    if (!h || !box || !base || !eps_r) return fail(FDTD_ERR_INVALID, "NULL argument");
+    const DeviceGrid& g = h->g;
+    const int lo[3] = {std::max(g.pxn, 1), std::max(g.pyn, 1), std::max(g.pzn, 1)};
+    const int hi[3] = {std::min(g.nx - 1 - g.pxp, g.nx - 2), std::min(g.ny - 1 - g.pyp, g.ny - 2),
+                       std::min(g.nz - 1 - g.pzp, g.nz - 2)};
+    // the E edges of the cells [b0, b3) lie on nodes b0..b3 of each axis: all must be interior nodes
+    for (int a = 0; a < 3; ++a)
+        if (box[a] >= box[a + 3] || box[a] < lo[a] || box[a + 3] > hi[a])
+            return fail(FDTD_ERR_INVALID, "design box empty, or its edges reach the CPML slabs or the boundary planes");
+    if (!(base->mu_r > 0.f) || !(base->sigma_e >= 0.f) || !(base->sigma_m > 0.f))
+        return fail(FDTD_ERR_INVALID, "design base material: mu_r > 0, sigma_e >= 0, sigma_m > 0");
+    if ((int)h->materials.size() > kDesign)
+        return fail(FDTD_ERR_INVALID, "material index 255 is reserved for the design region: at most 255 materials");
+    for (const LumpedDef& L : h->lumped) {  // the cells of a lumped Ez edge (i,j): i-1..i, j-1..j
+        const int* b = L.box;
+        if (b[0] - 1 < box[3] && box[0] <= b[3] && b[1] - 1 < box[4] && box[1] <= b[4] && b[2] < box[5] && box[2] < b[5])
+            return fail(FDTD_ERR_INVALID, "a lumped element touches the design region");
+    }
+    const size_t nd = (size_t)(box[3] - box[0]) * (box[4] - box[1]) * (box[5] - box[2]);
+    for (size_t q = 0; q < nd; ++q)
+        if (!(eps_r[q] > 0.f) || !std::isfinite(eps_r[q])) return fail(FDTD_ERR_INVALID, "design eps_r must be positive");
+    const bool same = h->has_design && std::equal(box, box + 6, h->dbox);
+    if (!same) {
+        h->release(h->d_deps);
+        h->d_deps = nullptr;
+        CUDA_TRY(h->alloc((void**)&h->d_deps, nd * sizeof(float)));
+        int b[6];
+        for (int q = 0; q < 6; ++q) b[q] = box[q];
+        CUDA_TRY(launch_paint(h->mat, g, b, (uint8_t)kDesign, h->stream));
+        std::copy(box, box + 6, h->dbox);
+    }
+    CUDA_TRY(cudaMemcpyAsync(h->d_deps, eps_r, nd * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    h->design_base = *base;
+    h->has_design = true;
+    h->dirty_materials = true;  // table entry 255, node classes
+    h->adj.ready = false;
+    return FDTD_OK;
+}
+
+namespace {
+
+int adj_alloc(fdtd_handle* h, void** p, size_t n) {
+    CUDA_TRY(h->alloc(p, n));
+    h->adj.bufs.push_back(*p);
+    return FDTD_OK;
+}
+
+long long edge_box_volume(const int* d) { return (long long)(d[3] - d[0] + 1) * (d[4] - d[1] + 1) * (d[5] - d[2] + 1); }
+
+// Buffers of an adjoint run of n steps with checkpoint interval K.
+int adj_prepare(fdtd_handle* h, long long n, int K) {
+    auto& A = h->adj;
+    for (void* p : A.bufs) h->release(p);
+    A.bufs.clear();
+    A = fdtd_handle::Adjoint{};
+    const size_t V = (size_t)vol(h) * sizeof(float);
+    int rc;
+    for (int c = 0; c < 6; ++c) {
+        if ((rc = adj_alloc(h, (void**)&A.st.l[c], V)) || (rc = adj_alloc(h, (void**)&A.st.ge[c], V)) ||
+            (rc = adj_alloc(h, (void**)&A.st.gh[c], V)))
+            return rc;
+    }
+    for (int f = 0; f < 6; ++f) {
+        const size_t pn = (size_t)h->psi_elems[f] * sizeof(float);
+        float* arr[4] = {nullptr, nullptr, nullptr, nullptr};
+        for (int q = 0; q < 4 && pn; ++q)
+            if ((rc = adj_alloc(h, (void**)&arr[q], pn))) return rc;
+        A.psa.f[f].e[0] = arr[0]; A.psa.f[f].e[1] = arr[1]; A.psa.f[f].h[0] = arr[2]; A.psa.f[f].h[1] = arr[3];
+    }
+    const long long ne = edge_box_volume(h->dbox);
+    A.hist_slots = K > 0 ? K + 1 : n + 1;
+    A.ckpt_slots = K > 0 ? (n + K - 1) / K + 1 : 1;  // + the final state
+    const size_t nd = (size_t)(h->dbox[3] - h->dbox[0]) * (h->dbox[4] - h->dbox[1]) * (h->dbox[5] - h->dbox[2]);
+    if ((rc = adj_alloc(h, (void**)&A.samples, sizeof(float) * (size_t)std::max<long long>(n, 1))) ||
+        (rc = adj_alloc(h, (void**)&A.hist, sizeof(float) * 3 * (size_t)ne * (size_t)A.hist_slots)) ||
+        (rc = adj_alloc(h, (void**)&A.ckpt, (size_t)fdtd_state_bytes(h) * (size_t)A.ckpt_slots)) ||
+        (rc = adj_alloc(h, (void**)&A.acc, sizeof(double) * 3 * (size_t)ne)) ||
+        (rc = adj_alloc(h, (void**)&A.grad, sizeof(double) * nd)))
+        return rc;
+    A.n = n;
+    A.K = K;
+    return FDTD_OK;
+}
+
+float* adj_slot(fdtd_handle* h, long long s) { return h->adj.hist + (size_t)s * 3 * (size_t)edge_box_volume(h->dbox); }
+char* adj_ckpt(fdtd_handle* h, long long s) { return h->adj.ckpt + (size_t)s * (size_t)fdtd_state_bytes(h); }
+
+// One forward step followed by the FoM sample (sample may be NULL) and an optional design snapshot.
+int adj_forward_step(fdtd_handle* h, float* sample, float* snap) {
+    int rc = fdtd_step(h, 1);
+    if (rc) return rc;
+    const int c = h->cur;
+    CUDA_TRY(launch_after_step(h->field[c][0], h->field[c][1], h->field[c][2], h->g, h->adj.probe, sample, h->dbox, snap,
+                               h->stream));
+    return FDTD_OK;
+}
+
+}  // namespace
+
+extern "C" int fdtd_adjoint_forward(fdtd_handle* h, int64_t n, int32_t checkpoint_every, int32_t pi, int32_t pj, int32_t pk,
+                                    double* J) {
+    if (!h || !J) return fail(FDTD_ERR_INVALID, "NULL argument");
+    if (!h->has_design) return fail(FDTD_ERR_STATE, "no design region (fdtd_set_design_region)");
+    if (n < 1 || checkpoint_every < 0) return fail(FDTD_ERR_INVALID, "steps >= 1 and checkpoint interval >= 0 required");
+    const DeviceGrid& g = h->g;
+    if (pi < 1 || pi > g.nx - 2 || pj < 1 || pj > g.ny - 2 || pk < 0 || pk > g.nz - 2)
+        return fail(FDTD_ERR_INVALID, "FoM probe must be an updated Ez edge");
+    if (in_slab_host(pi, g.nx, g.pxn, g.pxp) || in_slab_host(pj, g.ny, g.pyn, g.pyp) || in_slab_host(pk, g.nz, g.pzn, g.pzp))
+        return fail(FDTD_ERR_INVALID, "FoM probe inside the CPML");
+    int rc = ensure_prepared(h);
+    if (rc) return rc;
+    const int K = checkpoint_every;
+    rc = adj_prepare(h, n, K);
+    if (rc) return rc;
+    auto& A = h->adj;
+    A.start = h->step;
+    A.probe = (long long)pk * g.plane + (long long)pj * g.pitch + pi;
+    if (K == 0) {  // design E before the first step
+        const int c = h->cur;
+        CUDA_TRY(launch_after_step(h->field[c][0], h->field[c][1], h->field[c][2], g, A.probe, nullptr, h->dbox, adj_slot(h, 0),
+                                   h->stream));
+    }
+    for (long long s = 0; s < n; ++s) {
+        if (K > 0 && s % K == 0 && (rc = state_copy(h, adj_ckpt(h, s / K), true))) return rc;
+        if ((rc = adj_forward_step(h, A.samples + s, K == 0 ? adj_slot(h, s + 1) : nullptr))) return rc;
+    }
+    if ((rc = state_copy(h, adj_ckpt(h, A.ckpt_slots - 1), true))) return rc;  // final state
+    A.host_samples.resize((size_t)n);
+    CUDA_TRY(cudaMemcpyAsync(A.host_samples.data(), A.samples, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    double sum = 0.0;
+    for (float v : A.host_samples) sum += (double)g.dt * (double)v * (double)v;
+    *J = sum;
+    A.ready = true;
+    return FDTD_OK;
+}
+
+extern "C" int fdtd_adjoint_backward(fdtd_handle* h, double* grad) {
+    if (!h || !grad) return fail(FDTD_ERR_INVALID, "NULL argument");
+    auto& A = h->adj;
+    if (!A.ready) return fail(FDTD_ERR_STATE, "no fdtd_adjoint_forward since the last change");
+    const size_t V = (size_t)vol(h) * sizeof(float);
+    for (int c = 0; c < 6; ++c) {
+        CUDA_TRY(cudaMemsetAsync(A.st.l[c], 0, V, h->stream));
+        CUDA_TRY(cudaMemsetAsync(A.st.ge[c], 0, V, h->stream));
+        CUDA_TRY(cudaMemsetAsync(A.st.gh[c], 0, V, h->stream));
+    }
+    for (int f = 0; f < 6; ++f) {
+        const size_t pn = (size_t)h->psi_elems[f] * sizeof(float);
+        if (!pn) continue;
+        CUDA_TRY(cudaMemsetAsync(A.psa.f[f].e[0], 0, pn, h->stream));
+        CUDA_TRY(cudaMemsetAsync(A.psa.f[f].e[1], 0, pn, h->stream));
+        CUDA_TRY(cudaMemsetAsync(A.psa.f[f].h[0], 0, pn, h->stream));
+        CUDA_TRY(cudaMemsetAsync(A.psa.f[f].h[1], 0, pn, h->stream));
+    }
+    const long long ne = edge_box_volume(h->dbox);
+    CUDA_TRY(cudaMemsetAsync(A.acc, 0, sizeof(double) * 3 * (size_t)ne, h->stream));
+    const StepParams p = make_params(h);
+    const float two_dt = 2.0f * h->g.dt;
+    auto reverse = [&](long long m, const float* e_old, const float* e_new) -> int {
+        const AdjStep st{A.probe, two_dt * A.host_samples[(size_t)m], A.acc, e_old, e_new};
+        CUDA_TRY(launch_adj_step(p, A.st, A.psa, st, h->stream));
+        return FDTD_OK;
+    };
+    int rc;
+    if (A.K == 0) {
+        for (long long m = A.n - 1; m >= 0; --m)
+            if ((rc = reverse(m, adj_slot(h, m), adj_slot(h, m + 1)))) return rc;
+    } else {
+        const long long nseg = (A.n + A.K - 1) / A.K;
+        for (long long sg = nseg - 1; sg >= 0; --sg) {
+            // recompute the segment from its checkpoint, keeping the design E of every step
+            if ((rc = state_copy(h, adj_ckpt(h, sg), false))) return rc;
+            h->step = A.start + sg * A.K;
+            const long long len = std::min<long long>(A.K, A.n - sg * A.K);
+            const int c = h->cur;
+            CUDA_TRY(launch_after_step(h->field[c][0], h->field[c][1], h->field[c][2], h->g, A.probe, nullptr, h->dbox,
+                                       adj_slot(h, 0), h->stream));
+            for (long long t = 0; t < len; ++t)
+                if ((rc = adj_forward_step(h, nullptr, adj_slot(h, t + 1)))) return rc;
+            for (long long t = len - 1; t >= 0; --t)
+                if ((rc = reverse(sg * A.K + t, adj_slot(h, t), adj_slot(h, t + 1)))) return rc;
+        }
+    }
+    CUDA_TRY(launch_grad_finalize(A.acc, h->dbox, A.grad, h->stream));
+    const size_t nd = (size_t)(h->dbox[3] - h->dbox[0]) * (h->dbox[4] - h->dbox[1]) * (h->dbox[5] - h->dbox[2]);
+    CUDA_TRY(cudaMemcpyAsync(grad, A.grad, sizeof(double) * nd, cudaMemcpyDeviceToHost, h->stream));
+    // leave the handle where the forward left it
+    if (A.K > 0) {
+        if ((rc = state_copy(h, adj_ckpt(h, A.ckpt_slots - 1), false))) return rc;
+        h->step = A.start + A.n;
+    }
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
     return FDTD_OK;
 }

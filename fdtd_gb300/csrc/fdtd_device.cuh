@@ -21,6 +21,7 @@ constexpr float kTiny = 1.2e-38f;  // setZero's initial value for fields, psi an
 constexpr int kMaxMaterials = 256;
 constexpr int kDefaultEntry = kMaxMaterials;  // H coefficient of faces the reference never averages
 constexpr int kGeneral = 255;                 // node class of nodes that take the general path
+constexpr int kDesign = 255;                  // material index of design-region cells (per-cell eps_r)
 
 // Per-material coefficients for an edge whose surrounding cells all hold the same material.
 // e[c] = {Ca, Cb_plus, Cb_minus, 0} for Ex, Ey, Ez; h[c] = {Ch, Cb_plus, Cb_minus, 0} for Hx, Hy,
@@ -102,6 +103,10 @@ struct StepParams {
     long long ring_cap;
     int* status;                 // device error word
     BgCurl bg;                   // kappa-divided curl coefficients of the CPML background material
+    // design region: cells of material kDesign inside dbox = [d0,d3) x [d1,d4) x [d2,d5) take eps_r
+    // from deps ((d5-d2), (d4-d1), (d3-d0), x fastest); NULL when the handle has none
+    const float* deps;
+    int dbox[6];
 };
 
 // ------------------------------------------------------------------------------------------

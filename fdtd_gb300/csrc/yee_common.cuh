@@ -55,10 +55,50 @@ static __device__ __noinline__ Coef3 h_coef_mixed(const MatProps* props, int m0,
 // A curl coefficient divided by the CPML kappa (setABCPML, fdtdrav.h:1903-1906 and mirrors).
 static __device__ __noinline__ float kappa_div(float c, float kappa) { return __fdiv_rn(c, kappa); }
 
+// eps_r of cell (ci, cj, ck) holding material m: the design array for design cells.
+__device__ __forceinline__ float cell_eps(const StepParams& p, int m, int ci, int cj, int ck) {
+    if (m == kDesign && p.deps) {
+        const int* d = p.dbox;
+        return p.deps[((long long)(ck - d[2]) * (d[4] - d[1]) + (cj - d[1])) * (d[3] - d[0]) + (ci - d[0])];
+    }
+    return p.props[m].eps;
+}
+// The averaged eps_r and sigma_e of E edge `comp` at node (i, j, k) over its four cells in the
+// reference's summation order: Ex (i,j,k) (i,j-1,k) (i,j,k-1) (i,j-1,k-1); Ey (i,j,k) (i-1,j,k)
+// (i,j,k-1) (i-1,j,k-1); Ez (i,j,k) (i-1,j,k) (i,j-1,k) (i-1,j-1,k). m0..m3 are those cells' materials.
+__device__ __forceinline__ void edge_material(const StepParams& p, int comp, int i, int j, int k, int m0, int m1, int m2,
+                                              int m3, float& eps, float& sig) {
+    int c1i = i, c1j = j, c1k = k, c2i = i, c2j = j, c2k = k - 1, c3i = i, c3j = j, c3k = k - 1;
+    if (comp == 0) { c1j = j - 1; c3j = j - 1; }
+    else if (comp == 1) { c1i = i - 1; c3i = i - 1; }
+    else { c1i = i - 1; c2k = k; c2j = j - 1; c3i = i - 1; c3j = j - 1; c3k = k; }
+    eps = avg4(cell_eps(p, m0, i, j, k), cell_eps(p, m1, c1i, c1j, c1k), cell_eps(p, m2, c2i, c2j, c2k),
+               cell_eps(p, m3, c3i, c3j, c3k));
+    sig = avg4(p.props[m0].sig, p.props[m1].sig, p.props[m2].sig, p.props[m3].sig);
+}
+// Coefficients of an E edge with a design cell among its four cells (setCoefficients on the
+// averages, fdtdrav.h:1280-1303). Out of line: design edges are a small region.
+static __device__ __noinline__ Coef3 e_coef_design(const StepParams* pp, int comp, int i, int j, int k, int m0, int m1,
+                                                   int m2, int m3) {
+    const StepParams& p = *pp;
+    float eps, sig;
+    edge_material(p, comp, i, j, k, m0, m1, m2, m3, eps, sig);
+    const DeviceGrid& g = p.g;
+    const float dp = comp == 0 ? g.dy : comp == 1 ? g.dz : g.dx;
+    const float dm = comp == 0 ? g.dz : comp == 1 ? g.dx : g.dy;
+    return coef3(eps, sig, g.dt, g.eps0, dp, dm);
+}
+__device__ __forceinline__ bool has_design(const StepParams& p, int m0, int m1, int m2, int m3) {
+    return p.deps && (m0 == kDesign || m1 == kDesign || m2 == kDesign || m3 == kDesign);
+}
+
 // E-edge coefficients (setCoefficients, fdtdrav.h:1280-1303). `uni`: the four cells around the
 // edge hold material m0, so the table entry applies. comp: 0 = Ex, 1 = Ey, 2 = Ez; the Cb cell
-// sizes are Ex (dy, dz), Ey (dz, dx), Ez (dx, dy).
-__device__ __forceinline__ Coef3 e_coef(const StepParams& p, int comp, bool uni, int m0, int m1, int m2, int m3) {
+// sizes are Ex (dy, dz), Ey (dz, dx), Ez (dx, dy). Edges touching the design region average the
+// per-cell eps_r.
+__device__ __forceinline__ Coef3 e_coef(const StepParams& p, int comp, bool uni, int m0, int m1, int m2, int m3, int i,
+                                        int j, int k) {
+    if (has_design(p, m0, m1, m2, m3)) return e_coef_design(&p, comp, i, j, k, m0, m1, m2, m3);
     if (uni) {
         const float4 c = __ldg(&p.coef[m0].e[comp]);
         return Coef3{c.x, c.y, c.z};
@@ -209,9 +249,9 @@ __device__ __forceinline__ void e_update(const StepParams& p, const ENbr& n, int
     const bool ux = n.m0 == n.mj && n.m0 == n.mk && n.m0 == n.mjk;
     const bool uy = n.m0 == n.mi && n.m0 == n.mk && n.m0 == n.mik;
     const bool uz = n.m0 == n.mi && n.m0 == n.mj && n.m0 == n.mij;
-    const Coef3 cx = e_coef(p, 0, ux, n.m0, n.mj, n.mk, n.mjk);
-    const Coef3 cy = e_coef(p, 1, uy, n.m0, n.mi, n.mk, n.mik);
-    const Coef3 cz = e_coef(p, 2, uz, n.m0, n.mi, n.mj, n.mij);
+    const Coef3 cx = e_coef(p, 0, ux, n.m0, n.mj, n.mk, n.mjk, i, j, k);
+    const Coef3 cy = e_coef(p, 1, uy, n.m0, n.mi, n.mk, n.mik, i, j, k);
+    const Coef3 cz = e_coef(p, 2, uz, n.m0, n.mi, n.mj, n.mij, i, j, k);
     const float dHz_j = __fsub_rn(n.hz, n.hz_jm), dHy_k = __fsub_rn(n.hy, n.hy_km);
     const float dHx_k = __fsub_rn(n.hx, n.hx_km), dHz_i = __fsub_rn(n.hz, n.hz_im);
     const float dHy_i = __fsub_rn(n.hy, n.hy_im), dHx_j = __fsub_rn(n.hx, n.hx_jm);

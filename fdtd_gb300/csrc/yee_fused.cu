@@ -110,14 +110,9 @@ static __device__ __noinline__ float3 e_slow(const StepParams* pp, int i, int j,
     const uint8_t* mat = p.mat;
     const int m0 = mat[n], mi = mat[n - 1], mj = mat[n - R], mk = mat[n - P];
     const int mij = mat[n - 1 - R], mik = mat[n - 1 - P], mjk = mat[n - R - P];
-    const MatCoef* mc = p.coef + m0;
-    Coef3 cx, cy, cz;
-    if (m0 == mj && m0 == mk && m0 == mjk) { const float4 c = __ldg(&mc->e[0]); cx = Coef3{c.x, c.y, c.z}; }
-    else cx = e_coef_mixed(p.props, m0, mj, mk, mjk, g.dt, g.eps0, g.dy, g.dz);
-    if (m0 == mi && m0 == mk && m0 == mik) { const float4 c = __ldg(&mc->e[1]); cy = Coef3{c.x, c.y, c.z}; }
-    else cy = e_coef_mixed(p.props, m0, mi, mk, mik, g.dt, g.eps0, g.dz, g.dx);
-    if (m0 == mi && m0 == mj && m0 == mij) { const float4 c = __ldg(&mc->e[2]); cz = Coef3{c.x, c.y, c.z}; }
-    else cz = e_coef_mixed(p.props, m0, mi, mj, mij, g.dt, g.eps0, g.dx, g.dy);
+    const Coef3 cx = e_coef(p, 0, m0 == mj && m0 == mk && m0 == mjk, m0, mj, mk, mjk, i, j, k);
+    const Coef3 cy = e_coef(p, 1, m0 == mi && m0 == mk && m0 == mik, m0, mi, mk, mik, i, j, k);
+    const Coef3 cz = e_coef(p, 2, m0 == mi && m0 == mj && m0 == mij, m0, mi, mj, mij, i, j, k);
     float3 r;
     r.x = upd3(cx.a, ex, cx.bp, dHz_j, cx.bm, dHy_k);
     r.y = upd3(cy.a, ey, cy.bp, dHx_k, cy.bm, dHz_i);

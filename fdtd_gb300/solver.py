@@ -77,6 +77,9 @@ SIGNATURES = {
     "fdtd_get_cpml_profile": (ctypes.c_int, [_vp, _i32, _i32, _pf]),
     "fdtd_device_bytes": (_i64, [_vp]),
     "fdtd_step_static_scratch": (ctypes.c_int, [_vp, _i64]),
+    "fdtd_set_design_region": (ctypes.c_int, [_vp, _pi32, ctypes.POINTER(Material), _pf]),
+    "fdtd_adjoint_forward": (ctypes.c_int, [_vp, _i64, _i32, _i32, _i32, _i32, ctypes.POINTER(ctypes.c_double)]),
+    "fdtd_adjoint_backward": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
 }
 
 _lib = None
@@ -259,6 +262,31 @@ class Simulation:
 
     def device_bytes(self) -> int:
         return _lib.fdtd_device_bytes(self._h)
+
+    # -- design region and adjoint ---------------------------------------------------------------
+    def set_design_region(self, box: Sequence[int], eps_r: np.ndarray, sigma_e: float = float(S.REF_TINY),
+                          mu_r: float = 1.0, sigma_m: float = float(S.REF_TINY)) -> None:
+        """Design cells ``box`` = (i0, j0, k0, i1, j1, k1) with per-cell eps_r (shape (k1-k0, j1-j0, i1-i0))."""
+        e = np.ascontiguousarray(eps_r, dtype=np.float32)
+        want = (box[5] - box[2], box[4] - box[1], box[3] - box[0])
+        if e.shape != want:
+            raise ValueError(f"eps_r shape {e.shape} != design box shape {want}")
+        base = Material(1.0, sigma_e, mu_r, sigma_m)
+        _check(_lib.fdtd_set_design_region(self._h, _box(box), ctypes.byref(base), e.ctypes.data_as(_pf)))
+        self._design_shape = want
+
+    def adjoint_forward(self, steps: int, probe: Sequence[int], checkpoint_every: int = 64) -> float:
+        """J = sum_m dt * Ez(probe)^2 over ``steps`` steps, recording for adjoint_backward."""
+        J = ctypes.c_double(0.0)
+        _check(_lib.fdtd_adjoint_forward(self._h, steps, checkpoint_every, int(probe[0]), int(probe[1]), int(probe[2]),
+                                         ctypes.byref(J)))
+        return J.value
+
+    def adjoint_backward(self) -> np.ndarray:
+        """dJ/deps_r of the design cells (float64, shaped like the design eps_r)."""
+        g = np.zeros(self._design_shape, dtype=np.float64)
+        _check(_lib.fdtd_adjoint_backward(self._h, g.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return g
 
     # -- scenarios ------------------------------------------------------------------------------
     @classmethod

@@ -142,6 +142,30 @@ int fdtd_get_cpml_profile(fdtd_handle* h, int32_t axis, int32_t kind, float* hos
 /* Bytes of device memory the handle holds. */
 int64_t fdtd_device_bytes(const fdtd_handle* h);
 
+/* ---- Design region and adjoint gradient (no reference counterpart: the reference has no
+ * gradient; its commented-out differential-evolution optimiser, fdtdrav.h:2758-2986, is the
+ * gradient-free alternative it never finished). ---- */
+
+/* Cells [box[0],box[3]) x [box[1],box[4]) x [box[2],box[5]) become the design region: eps_r per
+ * cell from `eps_r` ((box[5]-box[2]) * (box[4]-box[1]) * (box[3]-box[0]) floats, x fastest),
+ * sigma_e, mu_r and sigma_m from `base` (its eps_r is ignored). The cells get the reserved material
+ * index 255 (so the table may hold at most 255 materials), painted over what they held. The E edges
+ * of the region must be interior nodes (outside the CPML slabs and the boundary planes) and no
+ * lumped element may touch it. Calling again with the same box only replaces eps_r. */
+int fdtd_set_design_region(fdtd_handle* h, const int32_t box[6], const fdtd_material* base, const float* eps_r);
+
+/* Figure of merit J = sum over the next n steps of dt * Ez(i,j,k)^2, Ez sampled after each step's E
+ * update at an Ez edge outside the CPML. Runs the n steps and records what the backward needs:
+ * checkpoint_every = K > 0 keeps the full state every K steps (the backward recomputes each segment
+ * from its checkpoint, keeping only the design-region E); K = 0 keeps the design-region E of every
+ * step instead (no recompute; (n+1) * 3 * (box+1)^3 floats). *J is the FP64 sum. */
+int fdtd_adjoint_forward(fdtd_handle* h, int64_t n, int32_t checkpoint_every, int32_t i, int32_t j, int32_t k, double* J);
+
+/* dJ/d(eps_r) of every design cell for the steps of the last fdtd_adjoint_forward, by the discrete
+ * adjoint of the FP32 update (CPML memory and lumped elements included), accumulated in FP64 into
+ * the host array `grad` (shaped like eps_r). The handle ends in the state the forward left. */
+int fdtd_adjoint_backward(fdtd_handle* h, double* grad);
+
 /* Maximum bytes of FDTD_STEP_STATIC_SCRATCH: one second field set, one second CPML memory set and
  * the sweep's work list. Enough for a 64^3 grid with 10-cell CPML on all faces (about 9.8 MiB). */
 #define FDTD_STEP_STATIC_SCRATCH_BYTES (16u << 20)

@@ -126,10 +126,12 @@ class _Prepared:
 
 
 def run(sc, steps: Optional[int] = None, precision: str = "f32", init_fields: Optional[np.ndarray] = None,
-        profile_override: Optional[dict] = None, threads: int = 0, probes: Optional[Sequence] = None):
-    """Run the oracle. Returns (probes (steps, n_probes), fields (6, nz, ny, nx))."""
+        profile_override: Optional[dict] = None, threads: int = 0, probes: Optional[Sequence] = None,
+        design=None):
+    """Run the oracle. Returns (probes (steps, n_probes), fields (6, nz, ny, nx)). ``design`` =
+    (box, eps_r array) overrides eps_r of the design cells."""
     steps = sc.steps if steps is None else steps
-    p = _Prepared(sc, profile_override, probes)
+    p = _Prepared(sc, profile_override, probes, design)
     dt = np.float32 if precision == "f32" else np.float64
     pout = np.zeros((steps, max(p.n_probes, 1)), dtype=dt)
     fout = np.zeros((6, sc.nz, sc.ny, sc.nx), dtype=dt)

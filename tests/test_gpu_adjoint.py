@@ -1,0 +1,112 @@
+"""GPU design region and discrete adjoint against the oracle.
+
+- the forward with a design region equals the FP32 oracle bit for bit (GPU CPML profiles);
+- the adjoint gradient (checkpointed and resident history) agrees with the oracle's FP64 adjoint
+  and with central finite differences of the FP64 oracle forward (h = 1e-3) within 1e-3 relative;
+- the checkpointed and the resident backward give identical bits;
+- the torch.autograd.Function returns the same gradient through autograd.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import bitwise_equal
+from fdtd_gb300 import scenario as S
+
+pytestmark = pytest.mark.gpu
+
+GRAD_TOL = 1e-3  # relative, per the figure-of-merit gradient requirement
+
+
+def design_case(seed=0, steps=160):
+    sc = S.vacuum_cube(24, steps, pml=4, name="adjoint_gpu")
+    sc.nx, sc.ny, sc.nz = 24, 22, 20
+    sc.sources = [S.LumpedSource((7, 11, 9, 7, 11, 10), 50.0, S.gaussian_derivative(steps, sc.dt, 30e9, 1e-3))]
+    sc.probes = [S.Probe(2, 18, 11, 9)]
+    sc.materials.append(S.Material(eps_r=3.0, sigma_e=0.02))
+    sc.bricks.append(S.Brick((17, 4, 5, 21, 9, 8), 1))  # a lossy dielectric next to the design region
+    box = (10, 8, 7, 16, 14, 11)
+    rng = np.random.default_rng(seed)
+    eps = rng.uniform(1, 12, size=(box[5] - box[2], box[4] - box[1], box[3] - box[0])).astype(np.float32)
+    return sc, box, eps, (18, 11, 9)
+
+
+def gpu_grad(sc, box, eps, probe, K):
+    from fdtd_gb300 import solver
+    with solver.Simulation.from_scenario(sc, probe_capacity=sc.steps) as sim:
+        sim.set_design_region(box, eps)
+        J = sim.adjoint_forward(sc.steps, probe, K)
+        g = sim.adjoint_backward()
+        assert sim.current_step == sc.steps
+    return J, g
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
+
+
+def test_design_forward_bitwise(gpu_lib):
+    from fdtd_gb300 import solver
+    sc, box, eps, probe = design_case()
+    with solver.Simulation.from_scenario(sc, probe_capacity=sc.steps) as sim:
+        sim.set_design_region(box, eps)
+        sim.step(sc.steps)
+        sim.synchronize()
+        f = sim.fields()
+        p = sim.read_probes(0, sc.steps)
+        prof = sim.cpml_profiles()
+    po, fo = oracle.run(sc, profile_override=prof, design=(box, eps.astype(np.float64)))
+    assert bitwise_equal(p, po) and bitwise_equal(f, fo)
+
+
+@pytest.mark.parametrize("K", [0, 16])
+def test_gradient_matches_fp64_adjoint(gpu_lib, K):
+    sc, box, eps, probe = design_case()
+    J, g = gpu_grad(sc, box, eps, probe, K)
+    J64, g64 = oracle.fom_grad(sc, probe, box, eps.astype(np.float64), precision="f64")
+    assert abs(J - J64) <= 1e-4 * abs(J64)
+    assert rel(g, g64) < GRAD_TOL, rel(g, g64)
+
+
+def test_checkpointed_equals_resident(gpu_lib):
+    sc, box, eps, probe = design_case(2)
+    J0, g0 = gpu_grad(sc, box, eps, probe, 0)
+    J1, g1 = gpu_grad(sc, box, eps, probe, 7)  # segments of uneven length
+    assert J0 == J1 and np.array_equal(g0, g1)
+
+
+def test_gradient_matches_central_differences(gpu_lib):
+    sc, box, eps, probe = design_case(1)
+    _, g = gpu_grad(sc, box, eps, probe, 16)
+    e64 = eps.astype(np.float64)
+    rng = np.random.default_rng(5)
+    h = 1e-3
+    for _ in range(6):
+        v = tuple(int(rng.integers(0, s)) for s in eps.shape)
+        e1 = e64.copy(); e1[v] += h
+        e2 = e64.copy(); e2[v] -= h
+        fd = (oracle.fom_grad(sc, probe, box, e1, grad=False) - oracle.fom_grad(sc, probe, box, e2, grad=False)) / (2 * h)
+        assert abs(g[v] - fd) <= GRAD_TOL * abs(fd), (v, g[v], fd)
+
+
+def test_autograd_function(gpu_lib):
+    import torch
+    from fdtd_gb300.adjoint import probe_energy
+    sc, box, eps, probe = design_case(3)
+    x = torch.tensor(eps, dtype=torch.float32, requires_grad=True)
+    J = probe_energy(x, sc, box, probe, sc.steps, checkpoint_every=32)
+    (2.0 * J).backward()
+    _, g = gpu_grad(sc, box, eps, probe, 32)
+    assert np.array_equal(x.grad.numpy(), (2.0 * g).astype(np.float32))
+
+
+def test_design_region_validation(gpu_lib):
+    from fdtd_gb300 import solver
+    sc, box, eps, probe = design_case()
+    with solver.Simulation.from_scenario(sc) as sim:
+        with pytest.raises(solver.FDTDError):
+            sim.set_design_region((2, 8, 7, 8, 14, 11), np.ones((4, 6, 6), np.float32))  # reaches the CPML
+        with pytest.raises(solver.FDTDError):
+            sim.set_design_region((6, 9, 8, 9, 12, 11), np.ones((3, 3, 3), np.float32))  # touches the source edge
+        with pytest.raises(solver.FDTDError):
+            sim.adjoint_forward(10, probe, 4)  # no design region yet
