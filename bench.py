@@ -43,6 +43,7 @@ def parse():
     ap.add_argument("--schedule", type=int, default=0, help="0 auto, 1 two-pass, 2 fused")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     return ap.parse_args()
 
 
@@ -284,6 +285,40 @@ def e2e_ours(args, sc, mat):
             "seconds": round(t1 - t0, 3)}
 
 
+def bench_adjoint():
+    """Adjoint cost on the 128^3 design problem (32x32x16 centred design region, eps_r ~ U[1,12],
+    10-cell CPML, one source, one Ez probe, 4000 steps): plain forward, forward with checkpoints
+    every 64 steps + backward with segment recompute, and the resident-history variant (K = 0).
+    Wall-clock around the synchronous C calls; every run starts from a fresh handle."""
+    import torch
+    from fdtd_gb300 import scenario as S, solver
+    d = S.design_problem()
+    sc = d.scenario
+
+    def fresh():
+        sim = solver.Simulation.from_scenario(sc, probe_capacity=sc.steps)
+        sim.set_design_region(d.box, d.eps)
+        sim.prepare()
+        sim.synchronize()
+        return sim
+
+    sim = fresh(); sim.step(64); sim.synchronize(); sim.close()  # warm-up
+    sim = fresh()
+    t0 = time.perf_counter(); sim.step(sc.steps); sim.synchronize(); t_plain = time.perf_counter() - t0
+    sim.close()
+    out = {"workload": "128^3 vacuum, 10-cell CPML, 32x32x16 design region eps_r~U[1,12], 1 source, 1 Ez probe, "
+                       "FoM sum dt*Ez^2", "steps": sc.steps, "forward_ms": round(t_plain * 1e3, 2)}
+    for K, key in ((64, "checkpoint64"), (0, "resident")):
+        sim = fresh()
+        t0 = time.perf_counter(); J = sim.adjoint_forward(sc.steps, d.probe, K); t1 = time.perf_counter()
+        g = sim.adjoint_backward(); t2 = time.perf_counter()
+        sim.close()
+        out[key] = {"adjoint_forward_ms": round((t1 - t0) * 1e3, 2), "backward_ms": round((t2 - t1) * 1e3, 2),
+                    "ratio": round((t2 - t0) / t_plain, 3), "backward_over_forward": round((t2 - t1) / t_plain, 3),
+                    "J": J, "grad_l2": float(np.linalg.norm(g))}
+    return out
+
+
 def bench_reference(args, rank, world):
     """The reference's own kernels (calc_e + calc_h from fdtdrav.h, built into oracle/_ref) on the
     same workload, single slab on this GPU."""
@@ -338,6 +373,8 @@ def main():
         if not args.no_cpu_baseline:
             sc, _ = scenario_for(args.config)
             out["cpu_baseline"] = cpu_baseline(sc)
+        if not args.no_adjoint and world == 1:
+            out["adjoint"] = bench_adjoint()
         print(json.dumps(out))
 
 

@@ -263,3 +263,28 @@ def scaled_boxes(nx: int, ny: int, nz: int, steps: int, seed: int = 7, pml: int 
     return random_boxes(nx, ny, nz, steps, seed=seed, n_boxes=n_boxes, edge=(e0, e1), pml=pml,
                         n_sources=n_sources, n_probes=n_probes, src_margin=2, max_delay=20,
                         name=name or f"small_boxes{nx}x{ny}x{nz}")
+
+
+@dataclasses.dataclass
+class DesignProblem:
+    """A figure-of-merit problem: scenario, design box (cells), eps_r per design cell, Ez probe."""
+    scenario: Scenario
+    box: Tuple[int, int, int, int, int, int]
+    eps: np.ndarray  # float32, (box[5]-box[2], box[4]-box[1], box[3]-box[0])
+    probe: Tuple[int, int, int]
+
+
+def design_problem(n: int = 128, steps: int = 4000, design=(32, 32, 16), pml: int = 10, seed: int = 4,
+                   delta: float = 1e-3, courant: float = 0.99, fmax: float = 30e9) -> DesignProblem:
+    """Vacuum n^3 with a centred design region of continuous eps_r ~ U[1, 12], one 50-ohm z-edge
+    Gaussian-derivative source a quarter of the way along x and the Ez output probe three quarters
+    of the way, both on the centre line (the 128^3 / 4000-step adjoint workload by default)."""
+    dt = courant_dt(delta, delta, delta, courant)
+    c = n // 2
+    src = LumpedSource((n // 4, c, c, n // 4, c, c + 1), 50.0, gaussian_derivative(steps, dt, fmax, delta))
+    sc = Scenario(f"design{n}", n, n, n, delta, delta, delta, float(dt), (pml,) * 6, steps, [Material()], [], [src], [],
+                  [])
+    dx, dy, dz = design
+    box = (c - dx // 2, c - dy // 2, c - dz // 2, c - dx // 2 + dx, c - dy // 2 + dy, c - dz // 2 + dz)
+    eps = np.random.default_rng(seed).uniform(1.0, 12.0, size=(dz, dy, dx)).astype(np.float32)
+    return DesignProblem(sc, box, eps, (3 * n // 4, c, c))
