@@ -145,9 +145,9 @@ __global__ void __launch_bounds__(256) k_adj_e(const __grid_constant__ StepParam
     const bool ux = m0 == mj && m0 == mk && m0 == mjk;
     const bool uy = m0 == mi && m0 == mk && m0 == mik;
     const bool uz = m0 == mi && m0 == mj && m0 == mij;
-    const Coef3 cx = e_coef(p, 0, ux, m0, mj, mk, mjk, i, j, k);
-    const Coef3 cy = e_coef(p, 1, uy, m0, mi, mk, mik, i, j, k);
-    const Coef3 cz = e_coef(p, 2, uz, m0, mi, mj, mij, i, j, k);
+    const Coef3 cx = e_coef<true>(p, 0, ux, m0, mj, mk, mjk, i, j, k);
+    const Coef3 cy = e_coef<true>(p, 1, uy, m0, mi, mk, mik, i, j, k);
+    const Coef3 cz = e_coef<true>(p, 2, uz, m0, mi, mj, mij, i, j, k);
 
     // design gradient: lambda here is dJ/dE^{m+1}; E^m and E^{m+1} come from the saved design E
     if (st.acc) {

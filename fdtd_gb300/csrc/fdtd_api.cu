@@ -64,6 +64,7 @@ struct fdtd_handle {
     FusedMaps maps[2];
     int kc = 0;  // planes per CTA chunk of the fused sweep
     FusedWork work{};
+    bool replan = false;  // the design region changed since the fused work was planned
     uint8_t* mat = nullptr;
     uint8_t* cls = nullptr;  // node classes, built by ensure_prepared
     int n_lumped_edges = 0;
@@ -239,8 +240,25 @@ void* tensor_map_encoder() {
     return fn;
 }
 
+// Work items of the fused schedule: interior items (TMA sweep) and the rest (shell passes). The
+// design region, if any, stays with the shell; planned again when it changes.
+int plan_work(fdtd_handle* h) {
+    std::vector<int4> wi, wg;
+    plan_fused(h->g, h->kc, h->has_design ? h->dbox : nullptr, wi, wg);
+    h->release((void*)h->work.interior);
+    h->work = FusedWork{};
+    int4* d = nullptr;
+    CUDA_TRY(h->alloc((void**)&d, sizeof(int4) * (wi.size() + wg.size() + 1)));
+    if (!wi.empty()) CUDA_TRY(cudaMemcpy(d, wi.data(), sizeof(int4) * wi.size(), cudaMemcpyHostToDevice));
+    if (!wg.empty()) CUDA_TRY(cudaMemcpy(d + wi.size(), wg.data(), sizeof(int4) * wg.size(), cudaMemcpyHostToDevice));
+    h->work = FusedWork{d, (int)wi.size(), d + wi.size(), (int)wg.size()};
+    h->replan = false;
+    return FDTD_OK;
+}
+
 // Second field buffer, second CPML set and the TMA tensor maps of both buffers for the fused sweep.
 int ensure_fused(fdtd_handle* h) {
+    if (h->have_second && h->replan) return plan_work(h);
     if (h->have_second) return FDTD_OK;
     const long long V = vol(h);
     for (int c = 0; c < 6; ++c) {
@@ -258,16 +276,9 @@ int ensure_fused(fdtd_handle* h) {
             return fail(FDTD_ERR_CUDA, "tensor map encoding failed");
     }
     CUDA_TRY(fused_configure());
-    const int kc = fused_chunk(h->g);
-    h->kc = kc;
-    // work items of the sweep: interior items (lean kernel) and the rest (general kernel)
-    std::vector<int4> wi, wg;
-    plan_fused(h->g, kc, wi, wg);
-    int4* d = nullptr;
-    CUDA_TRY(h->alloc((void**)&d, sizeof(int4) * (wi.size() + wg.size() + 1)));
-    if (!wi.empty()) CUDA_TRY(cudaMemcpy(d, wi.data(), sizeof(int4) * wi.size(), cudaMemcpyHostToDevice));
-    if (!wg.empty()) CUDA_TRY(cudaMemcpy(d + wi.size(), wg.data(), sizeof(int4) * wg.size(), cudaMemcpyHostToDevice));
-    h->work = FusedWork{d, (int)wi.size(), d + wi.size(), (int)wg.size()};
+    h->kc = fused_chunk(h->g);
+    rc = plan_work(h);
+    if (rc) return rc;
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     h->have_second = true;
     return FDTD_OK;
@@ -815,7 +826,8 @@ int ensure_prepared(fdtd_handle* h) {
             CUDA_TRY(h->alloc((void**)&h->cls, (size_t)vol(h)));
             CUDA_TRY(cudaMemsetAsync(h->cls, kGeneral, (size_t)vol(h), h->stream));
         }
-        CUDA_TRY(launch_node_class(h->g, h->mat, h->d_lumped, h->n_lumped_edges, h->cls, h->stream));
+        CUDA_TRY(launch_node_class(h->g, h->mat, h->d_lumped, h->n_lumped_edges, h->has_design ? h->dbox : nullptr, h->cls,
+                                   h->stream));
     }
     if (h->dirty_probes) {
         int rc = build_probes(h);
@@ -907,7 +919,7 @@ extern "C" int fdtd_step_static_scratch(fdtd_handle* h, int64_t n) {
     if (dev != h->device) return fail(FDTD_ERR_STATE, "the current device is not the handle's device");
     if (h->static_n_interior < 0) {  // host-only planning, as for the fused schedule
         std::vector<int4> wi, wg;
-        plan_fused(h->g, fused_chunk(h->g), wi, wg);
+        plan_fused(h->g, fused_chunk(h->g), h->has_design ? h->dbox : nullptr, wi, wg);
         h->static_n_interior = (int)wi.size();
         wi.insert(wi.end(), wg.begin(), wg.end());
         h->static_items.swap(wi);
@@ -1021,6 +1033,8 @@ extern "C" int fdtd_set_design_region(fdtd_handle* h, const int32_t box[6], cons
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     h->design_base = *base;
     h->has_design = true;
+    h->replan = true;            // fused work items
+    h->static_n_interior = -1;   // and those of fdtd_step_static_scratch
     h->dirty_materials = true;  // table entry 255, node classes
     h->adj.ready = false;
     return FDTD_OK;

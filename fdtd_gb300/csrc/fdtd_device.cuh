@@ -21,6 +21,8 @@ constexpr float kTiny = 1.2e-38f;  // setZero's initial value for fields, psi an
 constexpr int kMaxMaterials = 256;
 constexpr int kDefaultEntry = kMaxMaterials;  // H coefficient of faces the reference never averages
 constexpr int kGeneral = 255;                 // node class of nodes that take the general path
+constexpr int kDesignNode = 253;              // node class of the design region's edge box; classes
+                                              // below it are fast-path material ids
 constexpr int kDesign = 255;                  // material index of design-region cells (per-cell eps_r)
 
 // Per-material coefficients for an edge whose surrounding cells all hold the same material.

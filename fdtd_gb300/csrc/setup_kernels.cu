@@ -210,7 +210,9 @@ namespace fdtd {
 // Node class (StepParams::cls): material id of nodes that take the fast path, kGeneral otherwise.
 // The seven cells are those the three E edge averages read, (i,j,k) (i-1,j,k) (i,j-1,k) (i,j,k-1)
 // (i-1,j-1,k) (i-1,j,k-1) (i,j-1,k-1); the four cells of the H faces are among them.
-__global__ void k_node_class(const uint8_t* __restrict__ mat, uint8_t* __restrict__ cls, DeviceGrid g) {
+// Nodes of the design region's edge box [dlo, dhi] get kDesignNode.
+__global__ void k_node_class(const uint8_t* __restrict__ mat, uint8_t* __restrict__ cls, DeviceGrid g, int4 dlo,
+                             int4 dhi) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
@@ -222,8 +224,9 @@ __global__ void k_node_class(const uint8_t* __restrict__ mat, uint8_t* __restric
         const uint8_t m0 = mat[n];
         if (mat[n - 1] == m0 && mat[n - R] == m0 && mat[n - P] == m0 && mat[n - 1 - R] == m0 && mat[n - 1 - P] == m0 &&
             mat[n - R - P] == m0)
-            c = m0;  // m0 == kGeneral stays general
+            c = m0 < kDesignNode ? m0 : kGeneral;  // material ids from kDesignNode up stay general
     }
+    if (i >= dlo.x && i <= dhi.x && j >= dlo.y && j <= dhi.y && k >= dlo.z && k <= dhi.z) c = kDesignNode;
     cls[n] = c;
 }
 
@@ -232,11 +235,13 @@ __global__ void k_class_lumped(uint8_t* cls, DeviceGrid g, const LumpedEdge* edg
     if (q < n_edges) cls[(long long)edges[q].k * g.plane + (long long)edges[q].j * g.pitch + edges[q].i] = kGeneral;
 }
 
-cudaError_t launch_node_class(const DeviceGrid& g, const uint8_t* mat, const LumpedEdge* edges, int n_edges, uint8_t* cls,
-                              cudaStream_t st) {
+cudaError_t launch_node_class(const DeviceGrid& g, const uint8_t* mat, const LumpedEdge* edges, int n_edges,
+                              const int* design_box, uint8_t* cls, cudaStream_t st) {
+    const int4 dlo = design_box ? make_int4(design_box[0], design_box[1], design_box[2], 0) : make_int4(1, 1, 1, 0);
+    const int4 dhi = design_box ? make_int4(design_box[3], design_box[4], design_box[5], 0) : make_int4(0, 0, 0, 0);
     dim3 block(32, 8, 1);
     dim3 grid((g.nx + 31) / 32, (g.ny + 7) / 8, g.nz);
-    k_node_class<<<grid, block, 0, st>>>(mat, cls, g);
+    k_node_class<<<grid, block, 0, st>>>(mat, cls, g, dlo, dhi);
     if (n_edges > 0) k_class_lumped<<<(n_edges + 127) / 128, 128, 0, st>>>(cls, g, edges, n_edges);
     return cudaGetLastError();
 }

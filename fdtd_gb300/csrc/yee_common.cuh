@@ -94,11 +94,13 @@ __device__ __forceinline__ bool has_design(const StepParams& p, int m0, int m1, 
 
 // E-edge coefficients (setCoefficients, fdtdrav.h:1280-1303). `uni`: the four cells around the
 // edge hold material m0, so the table entry applies. comp: 0 = Ex, 1 = Ey, 2 = Ez; the Cb cell
-// sizes are Ex (dy, dz), Ey (dz, dx), Ez (dx, dy). Edges touching the design region average the
-// per-cell eps_r.
+// sizes are Ex (dy, dz), Ey (dz, dx), Ez (dx, dy). kDesignAware: edges touching the design region
+// average the per-cell eps_r. The update kernels compile without it (their registers, and with
+// them their occupancy, would grow); the design region's E is then redone by k_design_e.
+template <bool kDesignAware = false>
 __device__ __forceinline__ Coef3 e_coef(const StepParams& p, int comp, bool uni, int m0, int m1, int m2, int m3, int i,
                                         int j, int k) {
-    if (has_design(p, m0, m1, m2, m3)) return e_coef_design(&p, comp, i, j, k, m0, m1, m2, m3);
+    if (kDesignAware && has_design(p, m0, m1, m2, m3)) return e_coef_design(&p, comp, i, j, k, m0, m1, m2, m3);
     if (uni) {
         const float4 c = __ldg(&p.coef[m0].e[comp]);
         return Coef3{c.x, c.y, c.z};
@@ -235,6 +237,7 @@ __device__ __forceinline__ float psi_step(const float* in, float* out, int q, bo
 // then the CPML corrections in the reference's order (x, y, z). pre[] receives the values between
 // the main update and the CPML corrections (the sampleField values, fdtdrav.h:740).
 // plane_lumped: some lumped edge lies in plane k (uniform across a CTA).
+template <bool kDesignAware = false>
 __device__ __forceinline__ void e_update(const StepParams& p, const ENbr& n, int i, int j, int k, long long m,
                                          bool plane_lumped, const PsiIO& ps, float out[3], float pre[3]) {
     const DeviceGrid& g = p.g;
@@ -249,9 +252,9 @@ __device__ __forceinline__ void e_update(const StepParams& p, const ENbr& n, int
     const bool ux = n.m0 == n.mj && n.m0 == n.mk && n.m0 == n.mjk;
     const bool uy = n.m0 == n.mi && n.m0 == n.mk && n.m0 == n.mik;
     const bool uz = n.m0 == n.mi && n.m0 == n.mj && n.m0 == n.mij;
-    const Coef3 cx = e_coef(p, 0, ux, n.m0, n.mj, n.mk, n.mjk, i, j, k);
-    const Coef3 cy = e_coef(p, 1, uy, n.m0, n.mi, n.mk, n.mik, i, j, k);
-    const Coef3 cz = e_coef(p, 2, uz, n.m0, n.mi, n.mj, n.mij, i, j, k);
+    const Coef3 cx = e_coef<kDesignAware>(p, 0, ux, n.m0, n.mj, n.mk, n.mjk, i, j, k);
+    const Coef3 cy = e_coef<kDesignAware>(p, 1, uy, n.m0, n.mi, n.mk, n.mik, i, j, k);
+    const Coef3 cz = e_coef<kDesignAware>(p, 2, uz, n.m0, n.mi, n.mj, n.mij, i, j, k);
     const float dHz_j = __fsub_rn(n.hz, n.hz_jm), dHy_k = __fsub_rn(n.hy, n.hy_km);
     const float dHx_k = __fsub_rn(n.hx, n.hx_km), dHz_i = __fsub_rn(n.hz, n.hz_im);
     const float dHy_i = __fsub_rn(n.hy, n.hy_im), dHx_j = __fsub_rn(n.hx, n.hx_jm);

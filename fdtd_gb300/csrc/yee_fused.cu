@@ -174,7 +174,7 @@ __device__ __forceinline__ float3 e_fast(const StepParams& p, const EIn& a) {
                        upd3(z.x, a.ez, z.y, a.dHy_i, z.z, a.dHx_j));
 }
 __device__ __forceinline__ float3 e_any(const StepParams& p, const EIn& a, int i, int j, int k, long long m, int lumped) {
-    if (a.c != kGeneral) return e_fast(p, a);
+    if (a.c < kDesignNode) return e_fast(p, a);
     return e_slow(&p, i, j, k, m, lumped, a.ex, a.ey, a.ez, a.dHz_j, a.dHy_k, a.dHx_k, a.dHz_i, a.dHy_i, a.dHx_j);
 }
 
@@ -201,7 +201,7 @@ __device__ __forceinline__ float3 h_fast(const StepParams& p, const HIn& a) {
                        upd3(z.x, a.hz, z.y, a.dEx_j, z.z, a.dEy_i));
 }
 __device__ __forceinline__ float3 h_any(const StepParams& p, const HIn& a, int i, int j, int k) {
-    if (a.c != kGeneral) return h_fast(p, a);
+    if (a.c < kDesignNode) return h_fast(p, a);
     return h_slow(&p, i, j, k, a.hx, a.hy, a.hz, a.dEy_k, a.dEz_j, a.dEz_i, a.dEx_k, a.dEx_j, a.dEy_i);
 }
 
@@ -275,7 +275,7 @@ k_sweep_interior(const __grid_constant__ FusedMaps maps, const __grid_constant__
             const EIn a0 = e_load(cur, prv, hi, ei, mi);
             const EIn a1 = e_load(cur, prv, hi + RSTEP * HW, ei + RSTEP * EW, mi + RSTEP * MW);
             float3 v0, v1;
-            if (a0.c != kGeneral && a1.c != kGeneral) {
+            if (a0.c < kDesignNode && a1.c < kDesignNode) {
                 v0 = e_fast(p, a0);
                 v1 = e_fast(p, a1);
             } else {
@@ -307,7 +307,7 @@ k_sweep_interior(const __grid_constant__ FusedMaps maps, const __grid_constant__
             const HIn a0 = h_load(prv, en_prv, en_cur, hi, mi, ni);
             const HIn a1 = h_load(prv, en_prv, en_cur, hi + RSTEP * HW, mi + RSTEP * MW, ni + RSTEP * NW);
             float3 v0, v1;
-            if (a0.c != kGeneral && a1.c != kGeneral) {
+            if (a0.c < kDesignNode && a1.c < kDesignNode) {
                 v0 = h_fast(p, a0);
                 v1 = h_fast(p, a1);
             } else {
@@ -364,6 +364,7 @@ cudaError_t fused_configure() {
 cudaError_t launch_fused(const FusedMaps& maps, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo,
                          const PsiSet& psi_in, const PsiSet& psi_out, long long m, const FusedWork& w, cudaStream_t st) {
     cudaError_t e = launch_shell(true, p, fi, fo, psi_in, psi_out, w.general, w.n_general, TY, m, st);
+    if (e == cudaSuccess) e = launch_design_e(p, fi, fo, psi_in, psi_out, m, st);
     if (e != cudaSuccess) return e;
     if (w.n_interior > 0) k_sweep_interior<<<w.n_interior, NTH, SMEM_INTERIOR, st>>>(maps, p, fo, w.interior, m);
     e = cudaGetLastError();
@@ -404,7 +405,8 @@ int encode_fused_maps(FusedMaps* out, const DeviceGrid& g, float* const h[3], fl
 // its top plane in the interior range to stay interior. The tile grid starts at (ox, oy) <= 0,
 // chosen to put as many nodes as possible in interior tiles; ox is a multiple of 16 so that every
 // TMA box starts on a 16-byte boundary (material box at x0 - 16, one byte per cell).
-void plan_fused(const DeviceGrid& g, int kc, std::vector<int4>& interior_items, std::vector<int4>& general_items) {
+void plan_fused(const DeviceGrid& g, int kc, const int* design_box, std::vector<int4>& interior_items,
+                std::vector<int4>& general_items) {
     interior_items.clear();
     general_items.clear();
     auto inside = [](int q, int n, int pn, int pp) {
@@ -432,8 +434,12 @@ void plan_fused(const DeviceGrid& g, int kc, std::vector<int4>& interior_items, 
     };
     for (int y0 = oy; y0 < g.ny; y0 += TY)
         for (int x0 = ox; x0 < g.nx; x0 += TX) {
-            const bool tile_int = inside(x0, g.nx, g.pxn, g.pxp) && inside(x0 + TX, g.nx, g.pxn, g.pxp) &&
-                                  inside(y0, g.ny, g.pyn, g.pyp) && inside(y0 + TY, g.ny, g.pyn, g.pyp);
+            bool tile_int = inside(x0, g.nx, g.pxn, g.pxp) && inside(x0 + TX, g.nx, g.pxn, g.pxp) &&
+                            inside(y0, g.ny, g.pyn, g.pyp) && inside(y0 + TY, g.ny, g.pyn, g.pyp);
+            // the design region's edge box [d0, d3] x [d1, d4] (all planes) stays with the shell
+            if (design_box && x0 <= design_box[3] && design_box[0] <= x0 + TX && y0 <= design_box[4] &&
+                design_box[1] <= y0 + TY)
+                tile_int = false;
             // interior items cover planes [zlo, zhi) so that the recomputed top plane <= zhi
             if (tile_int && zhi > zlo) {
                 chunks(general_items, x0, y0, 0, zlo);

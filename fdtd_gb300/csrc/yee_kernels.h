@@ -22,6 +22,11 @@ struct PsiSet {
 cudaError_t launch_two_pass(const StepParams& p, const FieldPtrs& f, const PsiSet& ps, long long m,
                             cudaStream_t st);
 
+// E of the design region's nodes, fi/pin -> fo/pout, after a schedule's E kernels; nothing
+// without a design region.
+cudaError_t launch_design_e(const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
+                            const PsiSet& pout, long long m, cudaStream_t st);
+
 // Shell passes of the fused schedule (yee_two_pass.cu): E (e_pass) or H of the nodes of `items`,
 // reading fi / pin (buffer A) and writing fo / pout (buffer B).
 cudaError_t launch_shell(bool e_pass, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
@@ -48,7 +53,10 @@ int fused_smem_bytes();
 int fused_chunk(const DeviceGrid& g);
 int fused_tile_x();
 int fused_tile_y();
-void plan_fused(const DeviceGrid& g, int kc, std::vector<int4>& interior_items, std::vector<int4>& general_items);
+// design_box: the design region's cells (box[6]) or NULL; tiles whose nodes or E halo reach its
+// edge box go to the general items.
+void plan_fused(const DeviceGrid& g, int kc, const int* design_box, std::vector<int4>& interior_items,
+                std::vector<int4>& general_items);
 cudaError_t launch_fused(const FusedMaps& maps, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo,
                          const PsiSet& psi_in, const PsiSet& psi_out, long long m, const FusedWork& w, cudaStream_t st);
 // encode_fn: the driver's cuTensorMapEncodeTiled. Returns 0 on success.
@@ -68,8 +76,9 @@ cudaError_t launch_bg_curl(const DeviceGrid& g, const MatCoef* coef, int bg, con
                            float* const* out_dev, cudaStream_t st);
 cudaError_t launch_fill(float* p, long long n, float v, cudaStream_t st);
 // Node classes (StepParams::cls) from the material index and the lumped edges.
-cudaError_t launch_node_class(const DeviceGrid& g, const uint8_t* mat, const LumpedEdge* edges, int n_edges, uint8_t* cls,
-                              cudaStream_t st);
+// design_box: the design region's cells or NULL (its edge box gets class kDesignNode).
+cudaError_t launch_node_class(const DeviceGrid& g, const uint8_t* mat, const LumpedEdge* edges, int n_edges,
+                              const int* design_box, uint8_t* cls, cudaStream_t st);
 cudaError_t launch_paint(uint8_t* mat, const DeviceGrid& g, const int box[6], uint8_t value, cudaStream_t st);
 
 }  // namespace fdtd

@@ -12,7 +12,9 @@ namespace fdtd {
 // (the same buffers for the in-place two-pass schedule). Every node loads its twelve field values
 // and its class byte together (one round of memory latency); fast-path nodes (class != kGeneral)
 // then update from the material table, the rest also gather the seven cell materials and take
-// e_update / h_update.
+// e_update / h_update. kDesign (k_design_e only): skip the class test and average the per-cell
+// eps_r of design cells.
+template <bool kDesign = false>
 __device__ __forceinline__ void e_node_global(const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo,
                                               const PsiSet& pin, const PsiSet& pout, int i, int j, int k, long long m) {
     const DeviceGrid& g = p.g;
@@ -27,9 +29,9 @@ __device__ __forceinline__ void e_node_global(const StepParams& p, const FieldPt
     nb.hy_km = k > 0 ? fi.hy[n - P] : 0.f;
     nb.hz_im = i > 0 ? fi.hz[n - 1] : 0.f;
     nb.hz_jm = j > 0 ? fi.hz[n - R] : 0.f;
-    const int c = p.cls[n];
+    const int c = kDesign ? kGeneral : p.cls[n];
     float out[3], pre[3];
-    if (c != kGeneral) {
+    if (c < kDesignNode) {
         e_update_interior(p, c, nb.ex, nb.ey, nb.ez, __fsub_rn(nb.hz, nb.hz_jm), __fsub_rn(nb.hy, nb.hy_km),
                           __fsub_rn(nb.hx, nb.hx_km), __fsub_rn(nb.hz, nb.hz_im), __fsub_rn(nb.hy, nb.hy_im),
                           __fsub_rn(nb.hx, nb.hx_jm), out);
@@ -45,8 +47,9 @@ __device__ __forceinline__ void e_node_global(const StepParams& p, const FieldPt
         nb.mjk = (j > 0 && k > 0) ? mat[n - R - P] : 0;
         const PsiIO io{pin.f, pout.f, true};
         const bool plane_lumped = p.lumped_k[k] < p.lumped_k[k + 1];
-        e_update(p, nb, i, j, k, m, plane_lumped, io, out, pre);
+        e_update<kDesign>(p, nb, i, j, k, m, plane_lumped, io, out, pre);
     }
+    if (!kDesign && c == kDesignNode) return;  // k_design_e writes the design region's E
     fo.ex[n] = out[0]; fo.ey[n] = out[1]; fo.ez[n] = out[2];
     if (p.probe_k[k] < p.probe_k[k + 1]) {
         const long long row = m % p.ring_cap;
@@ -72,7 +75,7 @@ __device__ __forceinline__ void h_node_global(const StepParams& p, const FieldPt
     nb.ey_ip = i < g.nx - 1 ? fe.ey[n + 1] : 0.f;
     const int c = p.cls[n];
     float out[3], pre[3];
-    if (c != kGeneral) {
+    if (c < kDesignNode) {
         h_update_interior(p, c, nb.hx, nb.hy, nb.hz, __fsub_rn(nb.ey_kp, nb.ey), __fsub_rn(nb.ez_jp, nb.ez),
                           __fsub_rn(nb.ez_ip, nb.ez), __fsub_rn(nb.ex_kp, nb.ex), __fsub_rn(nb.ex_jp, nb.ex),
                           __fsub_rn(nb.ey_ip, nb.ey), out);
@@ -147,11 +150,36 @@ cudaError_t launch_shell(bool e_pass, const StepParams& p, const FieldPtrs& fi, 
     return cudaGetLastError();
 }
 
+// E of the nodes of the design region's edge box [d0, d3] x [d1, d4] x [d2, d5] (node class
+// kDesignNode, which the other E kernels do not store), with the per-cell eps_r of the design
+// cells. Design nodes are interior: no CPML memory, no lumped edge.
+__global__ void __launch_bounds__(256) k_design_e(const __grid_constant__ StepParams p, FieldPtrs fi, FieldPtrs fo,
+                                                  const __grid_constant__ PsiSet pin,
+                                                  const __grid_constant__ PsiSet pout, long long m) {
+    const int* d = p.dbox;
+    const int i = d[0] + blockIdx.x * 32 + threadIdx.x;
+    const int j = d[1] + blockIdx.y * 8 + threadIdx.y;
+    const int k = d[2] + blockIdx.z;
+    if (i > d[3] || j > d[4]) return;
+    e_node_global<true>(p, fi, fo, pin, pout, i, j, k, m);
+}
+
+cudaError_t launch_design_e(const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
+                            const PsiSet& pout, long long m, cudaStream_t st) {
+    if (!p.deps) return cudaSuccess;
+    const int* d = p.dbox;
+    const dim3 grid((d[3] - d[0] + 32) / 32, (d[4] - d[1] + 8) / 8, d[5] - d[2] + 1);
+    k_design_e<<<grid, dim3(32, 8, 1), 0, st>>>(p, fi, fo, pin, pout, m);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_two_pass(const StepParams& p, const FieldPtrs& f, const PsiSet& ps, long long m,
                             cudaStream_t st) {
     dim3 block(32, 8, 1);
     dim3 grid((p.g.nx + 31) / 32, (p.g.ny + 7) / 8, p.g.nz);
     k_update_e<<<grid, block, 0, st>>>(p, f, ps, m);
+    cudaError_t e = launch_design_e(p, f, f, ps, ps, m, st);
+    if (e != cudaSuccess) return e;
     k_update_h<<<grid, block, 0, st>>>(p, f, ps, m);
     return cudaGetLastError();
 }
