@@ -203,6 +203,18 @@ def cpu_baseline(sc_full, seconds_budget=20.0):
                       "6 steps (difference of an 8-step and a 2-step run, setup excluded)"}
 
 
+# DRAM bytes per cell update of one two-pass step (k_update_e + k_update_h), from an ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum) of the 256^3 random-box case: 78.15 B. Larger
+# grids are scaled by cells (an upper bound: their CPML share is smaller).
+TWO_PASS_DRAM_BYTES_PER_CELL = 78.15
+
+
+def measured_traffic(args, cells):
+    if args.schedule == 2:
+        return None  # the fused schedule has no capture of its own
+    return round(TWO_PASS_DRAM_BYTES_PER_CELL * cells)
+
+
 def bench_ours(args, rank, world):
     import torch
     from fdtd_gb300 import solver
@@ -253,7 +265,7 @@ def bench_ours(args, rank, world):
                       "schedule": {0: "auto", 1: "two-pass", 2: "fused"}[args.schedule],
                       "l2": "inputs larger than L2 (fields 24 B/cell x 134M cells)", "parallelism": f"replicas{world}"},
            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                        "frac": round(achieved / peak, 4), "traffic": None,
+                        "frac": round(achieved / peak, 4), "traffic": measured_traffic(args, N),
                         "bytes_per_cell_update": round(B, 3), "peak_source": peak_kind,
                         "kernel": "one full time step (all update launches of the step)"},
            "gpu_launches": launches_per_step * args.steps, "clocks": clk}
