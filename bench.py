@@ -44,6 +44,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     return ap.parse_args()
 
 
@@ -331,6 +332,48 @@ def bench_adjoint():
     return out
 
 
+def bench_batched(steps=2000):
+    """256 independent instances (per-axis sizes U{32..96}, 8-cell CPML, 8 dielectric boxes, one
+    source and one probe each): the same instances run one by one through fdtd_step, then together
+    through the batched persistent launch (autotuned, one CUDA-graph launch). Handle creation and
+    setup are outside both timings; both advance every instance by `steps` steps."""
+    import torch
+    from fdtd_gb300 import scenario as S, solver
+    scs = S.batch_instances(256, steps=2 * steps + 16)
+    cells = sum(sc.cells for sc in scs)
+    sims = [solver.Simulation.from_scenario(sc, probe_capacity=2 * steps + 16) for sc in scs]
+    for s in sims:
+        s.prepare()
+        s.step(2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in sims:
+        s.step(steps)
+    for s in sims:
+        s.synchronize()
+    t_seq = time.perf_counter() - t0
+    with solver.Batch(sims) as b:
+        tune_ms = b.tune(5)
+        b.step(2)
+        b.synchronize()
+        t0 = time.perf_counter()
+        b.step(steps)
+        b.synchronize()
+        t_bat = time.perf_counter() - t0
+        cfg = b.config
+    for s in sims:
+        s.close()
+    seq = cells * steps / t_seq / 1e9
+    bat = cells * steps / t_bat / 1e9
+    return {"workload": "256 instances, per-axis sizes U{32..96}, 8-cell CPML, 8 boxes eps_r~U[1,12], 1 source + "
+                        "1 probe each", "instances": len(scs), "cells": cells, "steps": steps,
+            "sequential": {"value": round(seq, 3), "unit": "Gcell-updates/s", "seconds": round(t_seq, 3),
+                           "gpu_launches": 2 * steps * len(scs)},
+            "batched": {"value": round(bat, 3), "unit": "Gcell-updates/s", "seconds": round(t_bat, 3),
+                        "gpu_launches": 1, "config": cfg, "tune_ms_5_steps": round(tune_ms, 2)},
+            "speedup": round(bat / seq, 2)}
+
+
 def bench_reference(args, rank, world):
     """The reference's own kernels (calc_e + calc_h from fdtdrav.h, built into oracle/_ref) on the
     same workload, single slab on this GPU."""
@@ -387,6 +430,8 @@ def main():
             out["cpu_baseline"] = cpu_baseline(sc)
         if not args.no_adjoint and world == 1:
             out["adjoint"] = bench_adjoint()
+        if not args.no_batched and world == 1:
+            out["batched"] = bench_batched()
         print(json.dumps(out))
 
 

@@ -1,0 +1,28 @@
+// Launch interface of the batched persistent kernel (batch.cu).
+#pragma once
+
+#include "fdtd_device.cuh"
+#include "yee_kernels.h"
+
+namespace fdtd {
+
+// One instance of a batch: its step parameters, field and CPML pointers (the handle's in-place
+// two-pass buffers) and its current step, which the kernel advances.
+struct __align__(16) BatchInstance {
+    StepParams p;
+    FieldPtrs f;
+    PsiSet ps;
+    long long step;
+};
+static_assert(sizeof(BatchInstance) % 16 == 0, "copied to shared memory in 16-byte words");
+
+// CTA sizes with a kernel instantiation (128, 256, 512 threads).
+bool batch_threads_supported(int threads);
+// Clusters of `cluster` CTAs of `threads` threads that fit on the device at once.
+cudaError_t batch_max_clusters(int cluster, int threads, int* out);
+// Advance every instance by `steps` steps: the queue is reset, then one launch of n_clusters
+// clusters takes the instances in `order` (indices into inst, longest first).
+cudaError_t launch_batch(BatchInstance* inst, const int* order, int n_inst, int* queue, long long steps, int cluster,
+                         int threads, int n_clusters, cudaStream_t st);
+
+}  // namespace fdtd

@@ -17,6 +17,7 @@
 
 #include "../../include/fdtd_api.h"
 #include "adjoint.h"
+#include "batch.h"
 #include "yee_kernels.h"
 
 using namespace fdtd;
@@ -1195,4 +1196,237 @@ extern "C" int fdtd_adjoint_backward(fdtd_handle* h, double* grad) {
     }
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     return FDTD_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Batched persistent launch (no reference counterpart).
+// ---------------------------------------------------------------------------------------------
+struct fdtd_batch {
+    std::vector<fdtd_handle*> hs;
+    int device = 0;
+    cudaStream_t stream = nullptr;      // launch stream (graph capture needs a non-default one)
+    cudaStream_t own_stream = nullptr;
+    std::vector<BatchInstance> inst;    // host copy, refreshed before each launch
+    BatchInstance* d_inst = nullptr;
+    int* d_order = nullptr;
+    int* d_queue = nullptr;
+    int cluster = 4, threads = 256, n_clusters = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long graph_steps = -1;
+    int graph_cfg[3] = {0, 0, 0};
+};
+
+namespace {
+
+void batch_drop_graph(fdtd_batch* b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    b->graph_steps = -1;
+}
+
+// Instance descriptors from the handles' current in-place buffers and steps.
+int batch_refresh(fdtd_batch* b) {
+    for (size_t q = 0; q < b->hs.size(); ++q) {
+        fdtd_handle* h = b->hs[q];
+        int rc = ensure_prepared(h);
+        if (rc) return rc;
+        if (h->stream != b->stream) CUDA_TRY(cudaStreamSynchronize(h->stream));  // the handle's own work first
+        const int a = h->cur;
+        BatchInstance& I = b->inst[q];
+        I.p = make_params(h);
+        I.f = FieldPtrs{h->field[a][0], h->field[a][1], h->field[a][2], h->field[a][3], h->field[a][4], h->field[a][5]};
+        I.ps = h->psi[a];
+        I.step = h->step;
+    }
+    CUDA_TRY(cudaMemcpyAsync(b->d_inst, b->inst.data(), sizeof(BatchInstance) * b->inst.size(), cudaMemcpyHostToDevice,
+                             b->stream));
+    return FDTD_OK;
+}
+
+int batch_set_config(fdtd_batch* b, int cluster, int threads) {
+    if (!batch_threads_supported(threads) || (cluster != 1 && cluster != 2 && cluster != 4 && cluster != 8))
+        return fail(FDTD_ERR_INVALID, "cluster size 1, 2, 4 or 8 and 128, 256 or 512 threads per CTA");
+    int n = 0;
+    CUDA_TRY(batch_max_clusters(cluster, threads, &n));
+    if (n < 1) return fail(FDTD_ERR_CUDA, "no cluster of this shape fits on the device");
+    b->cluster = cluster;
+    b->threads = threads;
+    b->n_clusters = std::min<int>(n, (int)b->hs.size());
+    return FDTD_OK;
+}
+
+// Run `steps` steps on every instance (refresh, one graph launch), then advance the step counters.
+int batch_run(fdtd_batch* b, long long steps) {
+    int rc = batch_refresh(b);
+    if (rc) return rc;
+    const int cfg[3] = {b->cluster, b->threads, b->n_clusters};
+    if (b->graph_steps != steps || !std::equal(cfg, cfg + 3, b->graph_cfg)) {
+        batch_drop_graph(b);
+        CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = launch_batch(b->d_inst, b->d_order, (int)b->hs.size(), b->d_queue, steps, b->cluster, b->threads,
+                                     b->n_clusters, b->stream);
+        cudaGraph_t g = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+        if (e != cudaSuccess || e2 != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return fail(FDTD_ERR_CUDA, std::string("batch graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+        }
+        b->graph = g;
+        CUDA_TRY(cudaGraphInstantiate(&b->exec, b->graph, 0));
+        b->graph_steps = steps;
+        std::copy(cfg, cfg + 3, b->graph_cfg);
+    }
+    CUDA_TRY(cudaGraphLaunch(b->exec, b->stream));
+    for (fdtd_handle* h : b->hs) h->step += steps;
+    return FDTD_OK;
+}
+
+}  // namespace
+
+extern "C" int fdtd_batch_create(fdtd_handle* const* handles, int32_t n, fdtd_batch** out) {
+    if (!handles || !out || n < 1) return fail(FDTD_ERR_INVALID, "NULL argument or empty batch");
+    *out = nullptr;
+    int dev = -1;
+    CUDA_TRY(cudaGetDevice(&dev));
+    for (int q = 0; q < n; ++q) {
+        if (!handles[q]) return fail(FDTD_ERR_INVALID, "NULL handle in the batch");
+        if (handles[q]->device != dev) return fail(FDTD_ERR_INVALID, "batch handles must live on the current device");
+        if (handles[q]->has_design) return fail(FDTD_ERR_INVALID, "handles with a design region cannot join a batch");
+        for (int r = 0; r < q; ++r)
+            if (handles[r] == handles[q]) return fail(FDTD_ERR_INVALID, "a handle appears twice in the batch");
+    }
+    fdtd_batch* b = new fdtd_batch();
+    b->hs.assign(handles, handles + n);
+    b->device = dev;
+    b->inst.resize(n);
+    auto cleanup = [&](int rc) { fdtd_batch_destroy(b); return rc; };
+    if (cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return cleanup(fail(FDTD_ERR_CUDA, "batch stream"));
+    b->stream = b->own_stream;
+    if (cudaMalloc((void**)&b->d_inst, sizeof(BatchInstance) * n) != cudaSuccess ||
+        cudaMalloc((void**)&b->d_order, sizeof(int) * n) != cudaSuccess || cudaMalloc((void**)&b->d_queue, sizeof(int)) != cudaSuccess)
+        return cleanup(fail(FDTD_ERR_OOM, "batch tables"));
+    // longest first: clusters that finish early pick up the short instances
+    std::vector<int> order(n);
+    for (int q = 0; q < n; ++q) order[q] = q;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return vol(b->hs[x]) > vol(b->hs[y]); });
+    if (cudaMemcpy(b->d_order, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice) != cudaSuccess)
+        return cleanup(fail(FDTD_ERR_CUDA, "batch order upload"));
+    int rc = batch_set_config(b, 4, 256);
+    if (rc) return cleanup(rc);
+    *out = b;
+    return FDTD_OK;
+}
+
+extern "C" int fdtd_batch_destroy(fdtd_batch* b) {
+    if (!b) return FDTD_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    batch_drop_graph(b);
+    if (b->own_stream) cudaStreamDestroy(b->own_stream);
+    cudaFree(b->d_inst);
+    cudaFree(b->d_order);
+    cudaFree(b->d_queue);
+    delete b;
+    return FDTD_OK;
+}
+
+extern "C" int fdtd_batch_set_stream(fdtd_batch* b, void* stream) {
+    if (!b) return fail(FDTD_ERR_INVALID, "batch is NULL");
+    if (!stream) return fail(FDTD_ERR_INVALID, "the batch needs a created stream (graph capture)");
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    b->stream = (cudaStream_t)stream;
+    batch_drop_graph(b);
+    return FDTD_OK;
+}
+
+extern "C" int fdtd_batch_set_config(fdtd_batch* b, int32_t cluster, int32_t threads) {
+    if (!b) return fail(FDTD_ERR_INVALID, "batch is NULL");
+    return batch_set_config(b, cluster, threads);
+}
+
+extern "C" int fdtd_batch_get_config(const fdtd_batch* b, int32_t* cluster, int32_t* threads, int32_t* n_clusters) {
+    if (!b || !cluster || !threads || !n_clusters) return fail(FDTD_ERR_INVALID, "NULL argument");
+    *cluster = b->cluster;
+    *threads = b->threads;
+    *n_clusters = b->n_clusters;
+    return FDTD_OK;
+}
+
+extern "C" int fdtd_batch_step(fdtd_batch* b, int64_t steps) {
+    if (!b) return fail(FDTD_ERR_INVALID, "batch is NULL");
+    if (steps < 0) return fail(FDTD_ERR_INVALID, "negative step count");
+    if (steps == 0) return FDTD_OK;
+    return batch_run(b, steps);
+}
+
+extern "C" int fdtd_batch_synchronize(fdtd_batch* b) {
+    if (!b) return fail(FDTD_ERR_INVALID, "batch is NULL");
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+    for (fdtd_handle* h : b->hs) {
+        int st = 0;
+        CUDA_TRY(cudaMemcpy(&st, h->status, sizeof(int), cudaMemcpyDeviceToHost));
+        if (st) return fail(FDTD_ERR_DEVICE, "device status word " + std::to_string(st));
+    }
+    return FDTD_OK;
+}
+
+extern "C" int fdtd_batch_tune(fdtd_batch* b, int64_t steps, double* best_ms) {
+    if (!b) return fail(FDTD_ERR_INVALID, "batch is NULL");
+    if (steps < 1) return fail(FDTD_ERR_INVALID, "tuning needs at least one step");
+    // every candidate runs from the same state: save all instances, restore after each trial
+    const size_t nh = b->hs.size();
+    std::vector<void*> saved(nh, nullptr);
+    std::vector<long long> steps0(nh);
+    std::vector<cudaStream_t> streams(nh);
+    for (size_t q = 0; q < nh; ++q) streams[q] = b->hs[q]->stream;
+    auto restore_all = [&]() {
+        for (void* p : saved) cudaFree(p);
+        for (size_t q = 0; q < nh; ++q) b->hs[q]->stream = streams[q];
+    };
+    for (size_t q = 0; q < nh; ++q) {
+        fdtd_handle* h = b->hs[q];
+        int rc = ensure_prepared(h);
+        if (!rc && h->stream != b->stream && cudaStreamSynchronize(h->stream) != cudaSuccess) rc = fail(FDTD_ERR_CUDA, "sync");
+        if (!rc && cudaMalloc(&saved[q], (size_t)fdtd_state_bytes(h)) != cudaSuccess) rc = fail(FDTD_ERR_OOM, "tuning state copies");
+        h->stream = b->stream;  // the state copies go on the batch stream during tuning
+        if (!rc) rc = state_copy(h, saved[q], true);
+        if (rc) { restore_all(); return rc; }
+        steps0[q] = h->step;
+    }
+    const int clusters[4] = {1, 2, 4, 8}, threads[3] = {128, 256, 512};
+    double best = 1e300;
+    int best_c = b->cluster, best_t = b->threads;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int rc = FDTD_OK;
+    for (int c : clusters) {
+        for (int t : threads) {
+            if (batch_set_config(b, c, t) != FDTD_OK) continue;  // shape does not fit: skip it
+            cudaEventRecord(e0, b->stream);
+            if ((rc = batch_run(b, steps))) break;
+            cudaEventRecord(e1, b->stream);
+            if (cudaEventSynchronize(e1) != cudaSuccess) { rc = fail(FDTD_ERR_CUDA, "tuning run failed"); break; }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best) { best = ms; best_c = c; best_t = t; }
+            for (size_t q = 0; q < nh && !rc; ++q) {
+                rc = state_copy(b->hs[q], saved[q], false);
+                b->hs[q]->step = steps0[q];
+            }
+            if (rc) break;
+        }
+        if (rc) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamSynchronize(b->stream);
+    restore_all();
+    if (rc) return rc;
+    rc = batch_set_config(b, best_c, best_t);
+    if (best_ms) *best_ms = best;
+    return rc;
 }

@@ -3,98 +3,9 @@
 // This is the reference's own order of work (calc_e then calc_h, solver fdtdrav.h:3222-3333)
 // expressed over the compact data layout. It runs at any grid size and is the schedule the fused
 // sweep is checked against bit for bit; both call the same e_update / h_update.
-#include "yee_common.cuh"
-#include "yee_kernels.h"
+#include "node_global.cuh"
 
 namespace fdtd {
-
-// One node's E (or H) update reading the fields `fi` and CPML memory `pin`, writing `fo` / `pout`
-// (the same buffers for the in-place two-pass schedule). Every node loads its twelve field values
-// and its class byte together (one round of memory latency); fast-path nodes (class != kGeneral)
-// then update from the material table, the rest also gather the seven cell materials and take
-// e_update / h_update. kDesign (k_design_e only): skip the class test and average the per-cell
-// eps_r of design cells.
-template <bool kDesign = false>
-__device__ __forceinline__ void e_node_global(const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo,
-                                              const PsiSet& pin, const PsiSet& pout, int i, int j, int k, long long m) {
-    const DeviceGrid& g = p.g;
-    const long long n = (long long)k * g.plane + (long long)j * g.pitch + i;
-    const long long P = g.plane, R = g.pitch;
-    ENbr nb;
-    nb.ex = fi.ex[n]; nb.ey = fi.ey[n]; nb.ez = fi.ez[n];
-    nb.hx = fi.hx[n]; nb.hy = fi.hy[n]; nb.hz = fi.hz[n];
-    nb.hx_jm = j > 0 ? fi.hx[n - R] : 0.f;
-    nb.hx_km = k > 0 ? fi.hx[n - P] : 0.f;
-    nb.hy_im = i > 0 ? fi.hy[n - 1] : 0.f;
-    nb.hy_km = k > 0 ? fi.hy[n - P] : 0.f;
-    nb.hz_im = i > 0 ? fi.hz[n - 1] : 0.f;
-    nb.hz_jm = j > 0 ? fi.hz[n - R] : 0.f;
-    const int c = kDesign ? kGeneral : p.cls[n];
-    float out[3], pre[3];
-    if (c < kDesignNode) {
-        e_update_interior(p, c, nb.ex, nb.ey, nb.ez, __fsub_rn(nb.hz, nb.hz_jm), __fsub_rn(nb.hy, nb.hy_km),
-                          __fsub_rn(nb.hx, nb.hx_km), __fsub_rn(nb.hz, nb.hz_im), __fsub_rn(nb.hy, nb.hy_im),
-                          __fsub_rn(nb.hx, nb.hx_jm), out);
-        pre[0] = out[0]; pre[1] = out[1]; pre[2] = out[2];
-    } else {
-        const uint8_t* mat = p.mat;
-        nb.m0 = mat[n];
-        nb.mi = i > 0 ? mat[n - 1] : 0;
-        nb.mj = j > 0 ? mat[n - R] : 0;
-        nb.mk = k > 0 ? mat[n - P] : 0;
-        nb.mij = (i > 0 && j > 0) ? mat[n - 1 - R] : 0;
-        nb.mik = (i > 0 && k > 0) ? mat[n - 1 - P] : 0;
-        nb.mjk = (j > 0 && k > 0) ? mat[n - R - P] : 0;
-        const PsiIO io{pin.f, pout.f, true};
-        const bool plane_lumped = p.lumped_k[k] < p.lumped_k[k + 1];
-        e_update<kDesign>(p, nb, i, j, k, m, plane_lumped, io, out, pre);
-    }
-    if (!kDesign && c == kDesignNode) return;  // k_design_e writes the design region's E
-    fo.ex[n] = out[0]; fo.ey[n] = out[1]; fo.ez[n] = out[2];
-    if (p.probe_k[k] < p.probe_k[k + 1]) {
-        const long long row = m % p.ring_cap;
-        for (int q = 0; q < 3; ++q) sample(p, row, q, i, j, k, pre[q]);
-    }
-}
-
-// H reads the old H from `fi` and the new E from `fe`.
-__device__ __forceinline__ void h_node_global(const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fe,
-                                              const FieldPtrs& fo, const PsiSet& pin, const PsiSet& pout, int i, int j,
-                                              int k, long long m) {
-    const DeviceGrid& g = p.g;
-    const long long n = (long long)k * g.plane + (long long)j * g.pitch + i;
-    const long long P = g.plane, R = g.pitch;
-    HNbr nb;
-    nb.hx = fi.hx[n]; nb.hy = fi.hy[n]; nb.hz = fi.hz[n];
-    nb.ex = fe.ex[n]; nb.ey = fe.ey[n]; nb.ez = fe.ez[n];
-    nb.ey_kp = k < g.nz - 1 ? fe.ey[n + P] : 0.f;
-    nb.ez_jp = j < g.ny - 1 ? fe.ez[n + R] : 0.f;
-    nb.ez_ip = i < g.nx - 1 ? fe.ez[n + 1] : 0.f;
-    nb.ex_kp = k < g.nz - 1 ? fe.ex[n + P] : 0.f;
-    nb.ex_jp = j < g.ny - 1 ? fe.ex[n + R] : 0.f;
-    nb.ey_ip = i < g.nx - 1 ? fe.ey[n + 1] : 0.f;
-    const int c = p.cls[n];
-    float out[3], pre[3];
-    if (c < kDesignNode) {
-        h_update_interior(p, c, nb.hx, nb.hy, nb.hz, __fsub_rn(nb.ey_kp, nb.ey), __fsub_rn(nb.ez_jp, nb.ez),
-                          __fsub_rn(nb.ez_ip, nb.ez), __fsub_rn(nb.ex_kp, nb.ex), __fsub_rn(nb.ex_jp, nb.ex),
-                          __fsub_rn(nb.ey_ip, nb.ey), out);
-        pre[0] = out[0]; pre[1] = out[1]; pre[2] = out[2];
-    } else {
-        const uint8_t* mat = p.mat;
-        nb.m0 = mat[n];
-        nb.mi = i > 0 ? mat[n - 1] : 0;
-        nb.mj = j > 0 ? mat[n - R] : 0;
-        nb.mk = k > 0 ? mat[n - P] : 0;
-        const PsiIO io{pin.f, pout.f, true};
-        h_update(p, nb, i, j, k, io, out, pre);
-    }
-    fo.hx[n] = out[0]; fo.hy[n] = out[1]; fo.hz[n] = out[2];
-    if (p.probe_k[k] < p.probe_k[k + 1]) {
-        const long long row = m % p.ring_cap;
-        for (int q = 0; q < 3; ++q) sample(p, row, 3 + q, i, j, k, pre[q]);
-    }
-}
 
 __global__ void __launch_bounds__(256) k_update_e(const __grid_constant__ StepParams p, FieldPtrs f,
                                                   const __grid_constant__ PsiSet ps, long long m) {

@@ -288,3 +288,28 @@ def design_problem(n: int = 128, steps: int = 4000, design=(32, 32, 16), pml: in
     box = (c - dx // 2, c - dy // 2, c - dz // 2, c - dx // 2 + dx, c - dy // 2 + dy, c - dz // 2 + dz)
     eps = np.random.default_rng(seed).uniform(1.0, 12.0, size=(dz, dy, dx)).astype(np.float32)
     return DesignProblem(sc, box, eps, (3 * n // 4, c, c))
+
+
+def batch_instances(n: int = 256, size=(32, 96), steps: int = 2000, pml: int = 8, n_boxes: int = 8, seed: int = 5,
+                    delta: float = 1e-3, courant: float = 0.99, fmax: float = 30e9) -> List[Scenario]:
+    """Independent instances with per-axis sizes uniform in ``size`` (inclusive), ``pml``-cell
+    CPML, ``n_boxes`` random dielectric boxes (eps_r ~ U[1, 12], lossless), one 50-ohm z-edge
+    source and one Ez probe each (the 256-instance batched workload by default)."""
+    rng = np.random.default_rng(seed)
+    dt = courant_dt(delta, delta, delta, courant)
+    out = []
+    for q in range(n):
+        dims = [int(v) for v in rng.integers(size[0], size[1] + 1, size=3)]
+        mats = [Material()]
+        bricks = []
+        for b in range(n_boxes):
+            lo = [int(rng.integers(pml, m - pml - 2)) for m in dims]
+            hi = [min(lo[a] + int(rng.integers(4, max(5, dims[a] // 3))), dims[a] - pml) for a in range(3)]
+            mats.append(Material(eps_r=float(rng.uniform(1.0, 12.0))))
+            bricks.append(Brick((lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]), len(mats) - 1))
+        i, j, k = (int(rng.integers(pml + 2, m - pml - 3)) for m in dims)
+        src = LumpedSource((i, j, k, i, j, k + 1), 50.0, gaussian_derivative(steps, dt, fmax, delta))
+        pi_, pj, pk = (int(rng.integers(pml + 2, m - pml - 2)) for m in dims)
+        out.append(Scenario(f"batch{q}", dims[0], dims[1], dims[2], delta, delta, delta, float(dt), (pml,) * 6, steps,
+                            mats, bricks, [src], [], [Probe(EZ, pi_, pj, pk)], seed=seed))
+    return out

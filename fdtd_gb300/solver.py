@@ -80,6 +80,14 @@ SIGNATURES = {
     "fdtd_set_design_region": (ctypes.c_int, [_vp, _pi32, ctypes.POINTER(Material), _pf]),
     "fdtd_adjoint_forward": (ctypes.c_int, [_vp, _i64, _i32, _i32, _i32, _i32, ctypes.POINTER(ctypes.c_double)]),
     "fdtd_adjoint_backward": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
+    "fdtd_batch_create": (ctypes.c_int, [ctypes.POINTER(_vp), _i32, ctypes.POINTER(_vp)]),
+    "fdtd_batch_destroy": (ctypes.c_int, [_vp]),
+    "fdtd_batch_set_stream": (ctypes.c_int, [_vp, _vp]),
+    "fdtd_batch_set_config": (ctypes.c_int, [_vp, _i32, _i32]),
+    "fdtd_batch_get_config": (ctypes.c_int, [_vp, _pi32, _pi32, _pi32]),
+    "fdtd_batch_tune": (ctypes.c_int, [_vp, _i64, ctypes.POINTER(ctypes.c_double)]),
+    "fdtd_batch_step": (ctypes.c_int, [_vp, _i64]),
+    "fdtd_batch_synchronize": (ctypes.c_int, [_vp]),
 }
 
 _lib = None
@@ -309,6 +317,59 @@ class Simulation:
         if probe_capacity is not None:
             sim.set_probe_capacity(probe_capacity)
         return sim
+
+
+class Batch:
+    """Many simulations advanced together by one persistent launch per step call (fdtd_batch_*).
+    The simulations stay usable on their own (fields, probes, state); the batch only refers to them."""
+
+    def __init__(self, sims: Sequence[Simulation]):
+        self._sims = list(sims)
+        arr = (_vp * len(self._sims))(*[s.handle for s in self._sims])
+        h = _vp()
+        _check(_lib.fdtd_batch_create(arr, len(self._sims), ctypes.byref(h)))
+        self._b = h
+
+    def close(self) -> None:
+        if getattr(self, "_b", None):
+            _lib.fdtd_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_stream(self, stream_ptr: int) -> None:
+        _check(_lib.fdtd_batch_set_stream(self._b, _vp(stream_ptr)))
+
+    def set_config(self, cluster: int, threads: int) -> None:
+        _check(_lib.fdtd_batch_set_config(self._b, cluster, threads))
+
+    @property
+    def config(self) -> dict:
+        c, t, n = _i32(), _i32(), _i32()
+        _check(_lib.fdtd_batch_get_config(self._b, ctypes.byref(c), ctypes.byref(t), ctypes.byref(n)))
+        return {"cluster": c.value, "threads": t.value, "n_clusters": n.value}
+
+    def tune(self, steps: int = 10) -> float:
+        """Autotune the cluster and CTA size on `steps` steps (states restored); returns the best time."""
+        ms = ctypes.c_double(0.0)
+        _check(_lib.fdtd_batch_tune(self._b, steps, ctypes.byref(ms)))
+        return ms.value
+
+    def step(self, n: int = 1) -> None:
+        _check(_lib.fdtd_batch_step(self._b, n))
+
+    def synchronize(self) -> None:
+        _check(_lib.fdtd_batch_synchronize(self._b))
 
 
 def run_scenario(sc: "S.Scenario", steps: Optional[int] = None, schedule: int = SCHEDULE_AUTO,

@@ -166,6 +166,33 @@ int fdtd_adjoint_forward(fdtd_handle* h, int64_t n, int32_t checkpoint_every, in
  * the host array `grad` (shaped like eps_r). The handle ends in the state the forward left. */
 int fdtd_adjoint_backward(fdtd_handle* h, double* grad);
 
+/* ---- Batched persistent launch (no reference counterpart: the reference runs one domain per
+ * process). A batch advances many independent handles of any sizes with one kernel launch per
+ * fdtd_batch_step, captured in a CUDA graph: each instance is owned by a thread-block cluster
+ * for all of its steps (E update, cluster barrier, H update, cluster barrier), instances are taken
+ * longest first from a queue, and every instance produces the bits fdtd_step would produce. ---- */
+typedef struct fdtd_batch fdtd_batch;
+
+/* A batch over n distinct handles on the current device (none with a design region). The handles
+ * keep their state, tables and probe rings; between fdtd_batch_create and fdtd_batch_destroy they
+ * may still be read, saved or stepped alone: every launch picks up each handle's current buffers
+ * and step, after waiting for the handle's own stream. */
+int fdtd_batch_create(fdtd_handle* const* handles, int32_t n, fdtd_batch** out);
+int fdtd_batch_destroy(fdtd_batch* b);
+/* Stream of the batch launches: a created stream, not the legacy default stream (the launch is
+ * captured in a CUDA graph). By default the batch uses a stream of its own. */
+int fdtd_batch_set_stream(fdtd_batch* b, void* stream);
+/* Cluster size (1, 2, 4 or 8 CTAs per instance) and CTA size (128, 256 or 512 threads). */
+int fdtd_batch_set_config(fdtd_batch* b, int32_t cluster, int32_t threads);
+int fdtd_batch_get_config(const fdtd_batch* b, int32_t* cluster, int32_t* threads, int32_t* n_clusters);
+/* Autotuner: times `steps` steps of the whole batch for every cluster and CTA size, restores every
+ * instance's state after each trial, keeps the fastest shape (its time in *best_ms if not NULL). */
+int fdtd_batch_tune(fdtd_batch* b, int64_t steps, double* best_ms);
+/* Advance every instance by `steps` steps (one graph launch, asynchronous on the batch stream). */
+int fdtd_batch_step(fdtd_batch* b, int64_t steps);
+/* Wait for the batch stream; FDTD_ERR_DEVICE if an instance's kernel reported an error. */
+int fdtd_batch_synchronize(fdtd_batch* b);
+
 /* Maximum bytes of FDTD_STEP_STATIC_SCRATCH: one second field set, one second CPML memory set and
  * the sweep's work list. Enough for a 64^3 grid with 10-cell CPML on all faces (about 9.8 MiB). */
 #define FDTD_STEP_STATIC_SCRATCH_BYTES (16u << 20)
