@@ -68,7 +68,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(8, len(cmds))) as ex:
         list(ex.map(run, cmds))
     tmp = LIB + ".tmp"
-    run([nv, "-shared", "-o", tmp] + objs + ARCH + ["-Xcompiler", "-fPIC", "-lcudart"])
+    cuda_lib = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nv))), "lib64")
+    run([nv, "-shared", "-o", tmp] + objs + ARCH + ["-Xcompiler", "-fPIC", "-lcudart", "-lcufft",
+                                                    "-Xlinker", "-rpath," + cuda_lib])
     os.replace(tmp, LIB)
     return LIB
 

@@ -18,6 +18,7 @@
 #include "../../include/fdtd_api.h"
 #include "adjoint.h"
 #include "batch.h"
+#include "ports.h"
 #include "yee_kernels.h"
 
 using namespace fdtd;
@@ -44,6 +45,15 @@ struct LumpedDef {
     int box[6];
     float resistance;
     int source;  // waveform index or -1
+};
+
+// A z-directed port: the point probes of its voltage edges (k outer, then j, then i, as voltMgpu
+// sums them) followed by its current loop at plane ke - 1 of the current box: Hx at j = js - 1
+// (i = is..ie), Hx at j = je, Hy at i = ie (j = js..je), Hy at i = is - 1.
+struct PortDef {
+    int vbox[6], ibox[6];
+    int first;  // probe id of the first voltage edge
+    int n_v, n_x, n_y;
 };
 
 }  // namespace
@@ -83,6 +93,7 @@ struct fdtd_handle {
     std::vector<LumpedDef> lumped;
     std::vector<std::vector<float>> waves;  // per source, per-edge signal
     std::vector<Probe> probes;
+    std::vector<PortDef> ports;
 
     // prepared device tables
     bool prepared = false;
@@ -1429,4 +1440,102 @@ extern "C" int fdtd_batch_tune(fdtd_batch* b, int64_t steps, double* best_ms) {
     rc = batch_set_config(b, best_c, best_t);
     if (best_ms) *best_ms = best;
     return rc;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Port voltage and current (voltMgpu, currMgpu, fdtdrav.h:2185-2488), z direction.
+// ---------------------------------------------------------------------------------------------
+extern "C" int fdtd_add_port(fdtd_handle* h, int32_t axis, const int32_t vbox[6], const int32_t ibox[6], int32_t* id_out) {
+    if (!h || !vbox || !ibox) return fail(FDTD_ERR_INVALID, "NULL argument");
+    if (axis != 2) return fail(FDTD_ERR_INVALID, "only z-directed ports (axis 2) are supported");
+    if (h->step > 0) return fail(FDTD_ERR_STATE, "ports must be added before the first step");
+    const DeviceGrid& g = h->g;
+    const int* v = vbox;
+    const int* c = ibox;
+    if (v[0] < 0 || v[3] >= g.nx || v[0] > v[3] || v[1] < 0 || v[4] >= g.ny || v[1] > v[4] || v[2] < 0 || v[5] > g.nz ||
+        v[2] >= v[5])
+        return fail(FDTD_ERR_INVALID, "voltage box outside the grid or empty (k range is half-open)");
+    if (c[0] < 1 || c[3] >= g.nx || c[0] > c[3] || c[1] < 1 || c[4] >= g.ny || c[1] > c[4] || c[5] < 1 || c[5] > g.nz)
+        return fail(FDTD_ERR_INVALID, "current box must leave one node on its low x / y sides inside the grid");
+    PortDef P{};
+    std::copy(v, v + 6, P.vbox);
+    std::copy(c, c + 6, P.ibox);
+    P.first = (int)h->probes.size();
+    for (int k = v[2]; k < v[5]; ++k)
+        for (int j = v[1]; j <= v[4]; ++j)
+            for (int i = v[0]; i <= v[3]; ++i) h->probes.push_back(Probe{FDTD_EZ, i, j, k});
+    P.n_v = (int)h->probes.size() - P.first;
+    const int kc = c[5] - 1;
+    for (int i = c[0]; i <= c[3]; ++i) h->probes.push_back(Probe{FDTD_HX, i, c[1] - 1, kc});
+    for (int i = c[0]; i <= c[3]; ++i) h->probes.push_back(Probe{FDTD_HX, i, c[4], kc});
+    P.n_x = c[3] - c[0] + 1;
+    for (int j = c[1]; j <= c[4]; ++j) h->probes.push_back(Probe{FDTD_HY, c[3], j, kc});
+    for (int j = c[1]; j <= c[4]; ++j) h->probes.push_back(Probe{FDTD_HY, c[0] - 1, j, kc});
+    P.n_y = c[4] - c[1] + 1;
+    h->ports.push_back(P);
+    h->dirty_probes = true;
+    if (id_out) *id_out = (int32_t)h->ports.size() - 1;
+    return FDTD_OK;
+}
+
+extern "C" int fdtd_read_port(fdtd_handle* h, int32_t id, int64_t first, int64_t n, int32_t time_average,
+                              float* voltage, float* current) {
+    if (!h || (n > 0 && (!voltage || !current))) return fail(FDTD_ERR_INVALID, "NULL argument");
+    if (id < 0 || id >= (int)h->ports.size()) return fail(FDTD_ERR_INVALID, "no such port");
+    if (n == 0) return FDTD_OK;
+    const int np = (int)h->probes.size();
+    std::vector<float> rows((size_t)n * np);
+    int rc = fdtd_read_probes(h, first, n, rows.data());
+    if (rc) return rc;
+    const PortDef& P = h->ports[id];
+    const float dx = h->g.dx, dy = h->g.dy, dz = h->g.dz;
+    // voltMgpu case 3: csuf = -dz / ((ie - is + 1) (je - js + 1)) with float box bounds
+    const float is = (float)P.vbox[0], js = (float)P.vbox[1], ie = (float)P.vbox[3], je = (float)P.vbox[4];
+    const float csuf = (-dz) / ((ie - is + 1) * (je - js + 1));
+    for (int64_t t = 0; t < n; ++t) {
+        const float* r = rows.data() + (size_t)t * np + P.first;
+        float volt = 0.f;
+        for (int q = 0; q < P.n_v; ++q) volt = volt + r[q];
+        voltage[t] = volt * csuf;
+        const float* hx = r + P.n_v;
+        const float* hy = hx + 2 * P.n_x;
+        float xp = 0.f, xn = 0.f, yp = 0.f, yn = 0.f;
+        for (int q = 0; q < P.n_x; ++q) { xp = xp + hx[q]; xn = xn + hx[P.n_x + q]; }
+        for (int q = 0; q < P.n_y; ++q) { yp = yp + hy[q]; yn = yn + hy[P.n_y + q]; }
+        // currMgpu case 3: the Ampere loop around the z edges, dy*yp + dx*xp - dy*yn - dx*xn as the
+        // reference's compiled expression contracts it (dx*xp fused with dy*yp as the addend, then
+        // the two subtractions as FMAs)
+        current[t] = std::fmaf(-dx, xn, std::fmaf(-dy, yn, std::fmaf(dx, xp, dy * yp)));
+    }
+    if (time_average && n > 1) {
+        // correcI averages in place, one thread per step: I(t) = (I(t) + I(t+1)) / 2 from the
+        // unaveraged neighbour, and the last step (I(t) + I(t-1)) / 2 from the already averaged
+        // one (its branch diverges from its neighbour's inside the warp and runs after it)
+        for (int64_t t = 0; t + 1 < n; ++t) current[t] = (current[t] + current[t + 1]) / 2;
+        current[n - 1] = (current[n - 1] + current[n - 2]) / 2;
+    }
+    return FDTD_OK;
+}
+
+extern "C" int fdtd_port_spectrum(fdtd_handle* h, int32_t id, int64_t first, int64_t n, float z0_re, float z0_im,
+                                  float* v_spectrum, float* i_spectrum, float* s11, float* zin) {
+    if (!h) return fail(FDTD_ERR_INVALID, "NULL argument");
+    if (n < 2 || n > INT32_MAX) return fail(FDTD_ERR_INVALID, "the spectrum needs 2 .. 2^31-1 steps");
+    if (!(z0_re > 0.f)) return fail(FDTD_ERR_INVALID, "Re z0 must be positive");
+    std::vector<float> v((size_t)n), c((size_t)n);
+    int rc = fdtd_read_port(h, id, first, n, 1, v.data(), c.data());
+    if (rc) return rc;
+    std::string err;
+    rc = port_spectra(h->stream, (int)n, v.data(), c.data(), z0_re, z0_im, v_spectrum, i_spectrum, s11, zin, &err);
+    return rc ? fail(rc, err) : FDTD_OK;
+}
+
+extern "C" int fdtd_port_zin(int64_t n_bins, const float* v_spectrum, const float* i_spectrum, float z0_re,
+                             float z0_im, float* s11, float* zin) {
+    if (n_bins < 1 || n_bins > INT32_MAX / 4) return fail(FDTD_ERR_INVALID, "n_bins must be 1 .. 2^29-1");
+    if (!v_spectrum || !i_spectrum) return fail(FDTD_ERR_INVALID, "NULL spectrum");
+    if (!(z0_re > 0.f)) return fail(FDTD_ERR_INVALID, "Re z0 must be positive");
+    std::string err;
+    const int rc = port_zin(nullptr, (int)n_bins, v_spectrum, i_spectrum, z0_re, z0_im, s11, zin, &err);
+    return rc ? fail(rc, err) : FDTD_OK;
 }

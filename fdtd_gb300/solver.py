@@ -80,6 +80,10 @@ SIGNATURES = {
     "fdtd_set_design_region": (ctypes.c_int, [_vp, _pi32, ctypes.POINTER(Material), _pf]),
     "fdtd_adjoint_forward": (ctypes.c_int, [_vp, _i64, _i32, _i32, _i32, _i32, ctypes.POINTER(ctypes.c_double)]),
     "fdtd_adjoint_backward": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
+    "fdtd_add_port": (ctypes.c_int, [_vp, _i32, _pi32, _pi32, _pi32]),
+    "fdtd_read_port": (ctypes.c_int, [_vp, _i32, _i64, _i64, _i32, _pf, _pf]),
+    "fdtd_port_spectrum": (ctypes.c_int, [_vp, _i32, _i64, _i64, ctypes.c_float, ctypes.c_float, _pf, _pf, _pf, _pf]),
+    "fdtd_port_zin": (ctypes.c_int, [_i64, _pf, _pf, ctypes.c_float, ctypes.c_float, _pf, _pf]),
     "fdtd_batch_create": (ctypes.c_int, [ctypes.POINTER(_vp), _i32, ctypes.POINTER(_vp)]),
     "fdtd_batch_destroy": (ctypes.c_int, [_vp]),
     "fdtd_batch_set_stream": (ctypes.c_int, [_vp, _vp]),
@@ -136,6 +140,7 @@ class Simulation:
         _check(lib.fdtd_create(ctypes.byref(g), ctypes.byref(h)))
         self._h = h
         self.shape = (nz, ny, nx)
+        self.dt = float(np.float32(dt))
         self.n_probes = 0
         if schedule != SCHEDULE_AUTO:
             _check(lib.fdtd_set_schedule(self._h, schedule))
@@ -198,6 +203,35 @@ class Simulation:
         _check(_lib.fdtd_add_probe(self._h, component, i, j, k, ctypes.byref(out)))
         self.n_probes = out.value + 1
         return out.value
+
+    def add_port(self, voltage_box: Sequence[int], current_box: Sequence[int], axis: int = 2) -> int:
+        """A z-directed port (voltage edges and current loop); returns its id."""
+        pid = _i32(-1)
+        _check(_lib.fdtd_add_port(self._h, axis, _box(voltage_box), _box(current_box), ctypes.byref(pid)))
+        self.n_probes = _lib.fdtd_probe_count(self._h)
+        return pid.value
+
+    def read_port(self, pid: int, first: int = 0, n: Optional[int] = None, time_average: bool = True):
+        """(V(t), I(t)) float32 arrays of the port's steps [first, first + n); I(t) time-averaged
+        over the window unless ``time_average`` is False."""
+        n = self.current_step - first if n is None else n
+        v = np.zeros(n, dtype=np.float32)
+        i = np.zeros(n, dtype=np.float32)
+        _check(_lib.fdtd_read_port(self._h, pid, first, n, int(time_average), v.ctypes.data_as(_pf),
+                                   i.ctypes.data_as(_pf)))
+        return v, i
+
+    def port_spectrum(self, pid: int, z0: complex = 50.0, first: int = 0, n: Optional[int] = None) -> dict:
+        """Spectra of a port over steps [first, first + n): complex64 arrays ``v``, ``i``, ``s11``,
+        ``zin`` of n // 2 + 1 bins and ``freq`` (Hz, bin f at f / (n dt))."""
+        n = self.current_step - first if n is None else n
+        nf = n // 2 + 1
+        out = {k: np.zeros(nf, dtype=np.complex64) for k in ("v", "i", "s11", "zin")}
+        z = complex(z0)
+        _check(_lib.fdtd_port_spectrum(self._h, pid, first, n, z.real, z.imag,
+                                       *(out[k].ctypes.data_as(_pf) for k in ("v", "i", "s11", "zin"))))
+        out["freq"] = np.arange(nf, dtype=np.float64) / (n * float(self.dt))
+        return out
 
     def set_probe_capacity(self, steps: int) -> None:
         _check(_lib.fdtd_set_probe_capacity(self._h, steps))
@@ -317,6 +351,20 @@ class Simulation:
         if probe_capacity is not None:
             sim.set_probe_capacity(probe_capacity)
         return sim
+
+
+def port_zin(v_spectrum: np.ndarray, i_spectrum: np.ndarray, z0: complex = 50.0):
+    """s11 and zin (complex64) of given V and I spectra for reference impedance z0 (fdtd_port_zin)."""
+    v = np.ascontiguousarray(v_spectrum, dtype=np.complex64)
+    i = np.ascontiguousarray(i_spectrum, dtype=np.complex64)
+    if v.shape != i.shape or v.ndim != 1:
+        raise ValueError("spectra must be 1-D arrays of equal length")
+    s11 = np.zeros_like(v)
+    zin = np.zeros_like(v)
+    z = complex(z0)
+    _check(load_library().fdtd_port_zin(v.size, v.ctypes.data_as(_pf), i.ctypes.data_as(_pf), z.real, z.imag,
+                                        s11.ctypes.data_as(_pf), zin.ctypes.data_as(_pf)))
+    return s11, zin
 
 
 class Batch:

@@ -142,6 +142,37 @@ int fdtd_get_cpml_profile(fdtd_handle* h, int32_t axis, int32_t kind, float* hos
 /* Bytes of device memory the handle holds. */
 int64_t fdtd_device_bytes(const fdtd_handle* h);
 
+/* Port voltage and current (z direction). Registers the point probes of a port: the Ez edges of
+ * the voltage box i in [is,ie], j in [js,je], k in [ks,ke), and the current loop of the current
+ * box at plane ke-1 (Hx at j = js-1 and j = je for i in [is,ie], Hy at i = ie and i = is-1 for
+ * j in [js,je]). Replaces the voltage / current sample boxes of sampleField and the reductions
+ * voltMgpu / currMgpu (fdtdrav.h:2185-2488, case 3). Add ports before the first step; their
+ * probes also appear as columns of fdtd_read_probes. */
+int fdtd_add_port(fdtd_handle* h, int32_t axis, const int32_t voltage_box[6], const int32_t current_box[6],
+                  int32_t* id_out);
+/* V(t) = -dz / (n_i n_j) * sum of the voltage edges' Ez and I(t) = dy (Hy(ie) sum) + dx (Hx(js-1)
+ * sum) - dy (Hy(is-1) sum) - dx (Hx(je) sum) for steps [first_step, first_step+n_steps), summed in
+ * the reference's order (host memory; voltMgpu / currMgpu, fdtdrav.h:2185-2488). With time_average
+ * set, I(t) becomes (I(t) + I(t+1)) / 2 over the window from the unaveraged I(t+1), and the last
+ * step (I(t) + I'(t-1)) / 2 from the averaged I'(t-1), as the reference's in-place correcI produces
+ * them (fdtdrav.h:2490-2508, called by calcVoltCurrent, fdtdrav.h:3129-3186). */
+int fdtd_read_port(fdtd_handle* h, int32_t id, int64_t first_step, int64_t n_steps, int32_t time_average,
+                   float* voltage, float* current);
+/* Frequency response of a port over steps [first_step, first_step+n_steps): real-to-complex FFTs
+ * (cuFFT, n_steps/2+1 bins, unnormalised) of V(t) and the time-averaged I(t), then per bin
+ * a = (V + z0 I) / (2 sqrt(Re z0)), b = (V - z0 I) / (2 sqrt(Re z0)), s11 = b / a and
+ * zin = z0 (1 + s11) / (1 - s11). Outputs are host arrays of n_steps/2+1 interleaved complex
+ * floats; any may be NULL. Bin f is the frequency f / (n_steps dt). Replaces calc_otm / calc_otm2
+ * (fdtdrav.h:2988-3127) and c_zinS11 (fdtdrav.h:2510-2548). Synchronises the handle's stream. */
+int fdtd_port_spectrum(fdtd_handle* h, int32_t id, int64_t first_step, int64_t n_steps, float z0_re, float z0_im,
+                       float* v_spectrum, float* i_spectrum, float* s11, float* zin);
+/* The per-bin step of fdtd_port_spectrum on spectra the caller already holds (host arrays of
+ * n_bins interleaved complex floats): s11 and zin for reference impedance z0, on the current
+ * device's default stream. Replaces c_zinS11 (fdtdrav.h:2510-2548) as calc_otm2 uses it on
+ * precomputed spectra (fdtdrav.h:3054-3127). */
+int fdtd_port_zin(int64_t n_bins, const float* v_spectrum, const float* i_spectrum, float z0_re, float z0_im,
+                  float* s11, float* zin);
+
 /* ---- Design region and adjoint gradient (no reference counterpart: the reference has no
  * gradient; its commented-out differential-evolution optimiser, fdtdrav.h:2758-2986, is the
  * gradient-free alternative it never finished). ---- */

@@ -692,6 +692,49 @@ int or_onestep_f32(const or_scenario* sc, int m, const float* sig, int n_sig, co
     return run<float>(sc, 0, sig, n_sig, init_fields, nullptr, fields_out, 1, m, init_psi, psi_out);
 }
 
+// Port voltage and current of a z-directed port from sampled series (steps rows of `stride` floats,
+// the port's columns from col0): the voltage box's Ez edges (k in [ks,ke) outer, then j, then i),
+// Hx at j = js-1 and at j = je (i = is..ie), Hy at i = ie and at i = is-1 (j = js..je) of the
+// current box at plane ke-1. Restates voltMgpu case 3 (fdtdrav.h:2268-2290): a float sum in that
+// order times csuf = -dz / ((ie-is+1)(je-js+1)); currMgpu case 3 (fdtdrav.h:2427-2480): four float
+// sums and dy*yp + dx*xp - dy*yn - dx*xn, contracted as the reference's compiled expression is
+// (dx*xp fused with dy*yp as the addend, then two FMAs; found by comparing the candidate
+// contractions against the reference's outputs); and, with time_average, correcI
+// (fdtdrav.h:2490-2508) in the order its in-place threads produced their results.
+int or_port_vi(const float* series, int steps, int stride, int col0, const int* vbox, const int* cbox,
+               float dx, float dy, float dz, int time_average, float* V, float* I) {
+    const int nv = (vbox[3] - vbox[0] + 1) * (vbox[4] - vbox[1] + 1) * (vbox[5] - vbox[2]);
+    const int nx = cbox[3] - cbox[0] + 1, ny = cbox[4] - cbox[1] + 1;
+    if (nv <= 0 || nx <= 0 || ny <= 0 || col0 + nv + 2 * nx + 2 * ny > stride) {
+        g_err = "port columns outside the series";
+        return -1;
+    }
+    const float is = (float)vbox[0], js = (float)vbox[1], ie = (float)vbox[3], je = (float)vbox[4];
+    const float csuf = (-dz) / ((ie - is + 1) * (je - js + 1));
+    for (int t = 0; t < steps; ++t) {
+        const float* r = series + (size_t)t * stride + col0;
+        float v = 0.f;
+        for (int q = 0; q < nv; ++q) v = v + r[q];
+        V[t] = v * csuf;
+        const float* hx = r + nv;
+        const float* hy = hx + 2 * nx;
+        float xp = 0.f, xn = 0.f, yp = 0.f, yn = 0.f;
+        for (int q = 0; q < nx; ++q) xp = xp + hx[q];
+        for (int q = 0; q < nx; ++q) xn = xn + hx[nx + q];
+        for (int q = 0; q < ny; ++q) yp = yp + hy[q];
+        for (int q = 0; q < ny; ++q) yn = yn + hy[ny + q];
+        I[t] = std::fmaf(-dx, xn, std::fmaf(-dy, yn, std::fmaf(dx, xp, dy * yp)));
+    }
+    if (time_average && steps > 1) {
+        // each step from its unaveraged successor; the last step from its averaged predecessor
+        // (the order in which the reference's in-place kernel produced its results)
+        std::vector<float> raw(I, I + steps);
+        for (int t = 0; t + 1 < steps; ++t) I[t] = (raw[t] + raw[t + 1]) / 2;
+        I[steps - 1] = (raw[steps - 1] + I[steps - 2]) / 2;
+    }
+    return 0;
+}
+
 // Per-edge coefficient arrays after the full setup, by reference name (volume (nz,ny,nx) or 1-D).
 int or_coef_f32(const or_scenario* sc, const char* name, float* out) {
     Sim<float> s;

@@ -65,6 +65,7 @@ def lib():
         L.or_run_f64.argtypes = [ctypes.POINTER(_Scenario), _i, _pf, _i, _pf, _pd, _pd, _i]
         L.or_onestep_f32.argtypes = [ctypes.POINTER(_Scenario), _i, _pf, _i, _pf, _pf, _pf, _pf]
         L.or_coef_f32.argtypes = [ctypes.POINTER(_Scenario), ctypes.c_char_p, _pf]
+        L.or_port_vi.argtypes = [_pf, _i, _i, _i, _pi, _pi, _f, _f, _f, _i, _pf, _pf]
         for fn in (L.or_fom_grad_f64, L.or_fom_grad_f32):
             fn.argtypes = [ctypes.POINTER(_Scenario), _i, _pf, _i, _i, _i, _i, _pd, _pd]
         _lib = L
@@ -202,3 +203,56 @@ def fom_grad(sc, probe, design_box, design_eps, steps: Optional[int] = None, pre
     if rc != 0:
         raise RuntimeError("oracle: " + L.or_error().decode())
     return (J.value, g) if grad else J.value
+
+
+def port_probes(voltage_box: Sequence[int], current_box: Sequence[int]) -> list:
+    """Point probes (component, i, j, k) that a z-directed port samples, in the order or_port_vi
+    reads them: Ez of the voltage box (k in [ks, ke) outer, j, i), then Hx at j = js-1 and at
+    j = je (i = is..ie), Hy at i = ie and at i = is-1 (j = js..je), at plane ke-1 of the current box."""
+    from fdtd_gb300 import scenario as S
+    v, c = [int(x) for x in voltage_box], [int(x) for x in current_box]
+    out = [S.Probe(S.EZ, i, j, k) for k in range(v[2], v[5]) for j in range(v[1], v[4] + 1)
+           for i in range(v[0], v[3] + 1)]
+    kc = c[5] - 1
+    out += [S.Probe(S.HX, i, c[1] - 1, kc) for i in range(c[0], c[3] + 1)]
+    out += [S.Probe(S.HX, i, c[4], kc) for i in range(c[0], c[3] + 1)]
+    out += [S.Probe(S.HY, c[3], j, kc) for j in range(c[1], c[4] + 1)]
+    out += [S.Probe(S.HY, c[0] - 1, j, kc) for j in range(c[1], c[4] + 1)]
+    return out
+
+
+def port_vi(series: np.ndarray, voltage_box: Sequence[int], current_box: Sequence[int], sc, col0: int = 0,
+            time_average: bool = True):
+    """(V(t), I(t)) float32 of a z-directed port from probe series (steps, n) whose columns from
+    ``col0`` are ``port_probes(voltage_box, current_box)``."""
+    a = np.ascontiguousarray(series, dtype=np.float32)
+    steps, stride = a.shape
+    vb = np.ascontiguousarray(voltage_box, dtype=np.int32)
+    cb = np.ascontiguousarray(current_box, dtype=np.int32)
+    V = np.zeros(steps, dtype=np.float32)
+    I = np.zeros(steps, dtype=np.float32)
+    L = lib()
+    if L.or_port_vi(a.ctypes.data_as(_pf), steps, stride, col0, vb.ctypes.data_as(_pi), cb.ctypes.data_as(_pi),
+                    sc.dx, sc.dy, sc.dz, int(time_average), V.ctypes.data_as(_pf), I.ctypes.data_as(_pf)) != 0:
+        raise RuntimeError("oracle: " + L.or_error().decode())
+    return V, I
+
+
+def port_spectra(V: np.ndarray, I: np.ndarray, z0: complex = 50.0) -> dict:
+    """FP64 restatement of calc_otm + c_zinS11 (fdtdrav.h:2988-3051, 2510-2548): unnormalised real
+    FFTs of V and the time-averaged I (n // 2 + 1 bins), a = (V + z0 I) / (2 sqrt(Re z0)),
+    b = (V - z0 I) / (2 sqrt(Re z0)), s11 = b / a, zin = z0 (1 + s11) / (1 - s11)."""
+    z0 = complex(z0)
+    Vf = np.fft.rfft(np.asarray(V, dtype=np.float64))
+    If = np.fft.rfft(np.asarray(I, dtype=np.float64))
+    return dict(v=Vf, i=If, **zin_s11(Vf, If, z0))
+
+
+def zin_s11(Vf: np.ndarray, If: np.ndarray, z0: complex = 50.0) -> dict:
+    """The per-bin part of port_spectra in complex128."""
+    z0 = complex(z0)
+    scale = 2.0 * np.sqrt(z0.real)
+    a = (Vf + z0 * If) / scale
+    b = (Vf - z0 * If) / scale
+    s11 = b / a
+    return {"a": a, "b": b, "s11": s11, "zin": z0 * (1 + s11) / (1 - s11)}

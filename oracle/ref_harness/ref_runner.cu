@@ -33,12 +33,14 @@ std::string g_err;
 cudaLibrary_t g_lib = nullptr;
 
 struct Kern { const char* name; cudaKernel_t k; };
-enum { K_SETZERO, K_SETBRICK, K_SETSIGMA, K_SETCOEF, K_SETABCPML, K_SRCZ, K_RES, K_CALCE, K_CALCH, K_GATHER, K_COUNT };
+enum { K_SETZERO, K_SETBRICK, K_SETSIGMA, K_SETCOEF, K_SETABCPML, K_SRCZ, K_RES, K_CALCE, K_CALCH,
+       K_VOLT, K_CURR, K_CORREC, K_ZIN, K_GATHER, K_COUNT };
 Kern g_k[K_COUNT] = {
     {"_Z7setZero", nullptr}, {"_Z8setBrick", nullptr}, {"_Z18setSigmaEpsSigmaMu", nullptr},
     {"_Z15setCoefficients", nullptr}, {"_Z9setABCPML", nullptr}, {"_Z13defineSourceZ", nullptr},
     {"_Z14defineResistor", nullptr}, {"_Z6calc_e", nullptr}, {"_Z6calc_h", nullptr},
-    {"harness_gather", nullptr}};
+    {"_Z8voltMgpu", nullptr}, {"_Z8currMgpu", nullptr}, {"_Z7correcI", nullptr},
+    {"_Z8c_zinS11P6float2S0_iS0_S0_S0_S0_S_f", nullptr}, {"harness_gather", nullptr}};
 
 // Itanium-ABI names of the reference kernels: the parameter lists of fdtdrav.h reduce to runs of
 // int (i), float (f) and float* (Pf, then the substitution S_).
@@ -78,6 +80,12 @@ size_t g_signal_cap = 0;
 int g_probe_cap = 0;
 
 std::vector<std::vector<int>> g_src_box;
+
+// The reference's own voltage / current sample boxes (calc_e / calc_h arguments). Outside the grid
+// unless rh_set_port placed them; g_port_steps bounds the time index the sample arrays hold.
+int g_vbox[6] = {-10, -10, -10, -10, -10, -10}, g_vn[3] = {1, 1, 1};
+int g_cbox[6] = {-10, -10, -10, -10, -10, -10}, g_cn[3] = {1, 1, 1};
+int g_port_steps = 0;
 
 const char* kVolumeNames[] = {
     "Ex", "Jx", "Cexe", "Cexhz", "Cexhy", "Cexj", "eps_r_x", "sigma_e_x",
@@ -127,6 +135,9 @@ void free_all() {
     g_gather_fields = nullptr; g_probe_dev = nullptr; g_probe_comp_dev = nullptr;
     g_probe_idx_dev = nullptr; g_signal_dev = nullptr; g_signal_cap = 0; g_probe_cap = 0;
     g_ready = false;
+    for (int q = 0; q < 6; ++q) g_vbox[q] = g_cbox[q] = -10;
+    for (int q = 0; q < 3; ++q) g_vn[q] = g_cn[q] = 1;
+    g_port_steps = 0;
 }
 
 }  // namespace
@@ -158,9 +169,12 @@ int rh_load(const char* cubin_path) {
         "14i5p6f",                     // defineResistor
         "14i57p16i1p",                 // calc_e
         "13i56p10i3p",                 // calc_h
-        nullptr};
+        "11i2p3f2i",                   // voltMgpu
+        "11i4p3f2i",                   // currMgpu
+        "1p1i",                        // correcI
+        nullptr, nullptr};             // c_zinS11 (float2 parameters, full name above), gather
     for (int k = 0; k < K_COUNT; ++k) {
-        std::string nm = specs[k] ? mangled(g_k[k].name, specs[k]) : std::string(g_k[k].name);
+        std::string nm = (k < K_COUNT && specs[k]) ? mangled(g_k[k].name, specs[k]) : std::string(g_k[k].name);
         if (!ck(cudaLibraryGetKernel(&g_k[k].k, g_lib, nm.c_str()), nm.c_str())) return -1;
     }
     return 0;
@@ -371,8 +385,9 @@ static bool do_calc_e(int m, int src_slot) {
     static int sbox[6];
     if (src_slot >= 0) for (int q = 0; q < 6; ++q) sbox[q] = g_src_box[src_slot][q];
     else { sbox[0] = sbox[1] = sbox[2] = -10; sbox[3] = sbox[4] = sbox[5] = -10; }
-    static int vbox[6] = {-10, -10, -10, -10, -10, -10};
-    static int vn[3] = {1, 1, 1};
+    static int vbox[6], vn[3];
+    for (int q = 0; q < 6; ++q) vbox[q] = g_vbox[q];
+    for (int q = 0; q < 3; ++q) vn[q] = g_vn[q];
     static float* P[57];
     const char* order[] = {
         "Ex", "Jx", "Cexe", "Cexhz", "Cexhy", "Cexj", "Ey", "Jy", "Ceye", "Ceyhx", "Ceyhz", "Ceyj",
@@ -397,8 +412,9 @@ static bool do_calc_e(int m, int src_slot) {
 static bool do_calc_h(int m) {
     int NX = g_d.NX, NXX = g_d.NXX, NY = g_d.NY, NYY = g_d.NYY, NZ = g_d.NZ, NZ_N = g_d.NZ_N, off = 0;
     int* pml = g_d.pml;
-    static int cbox[6] = {-10, -10, -10, -10, -10, -10};
-    static int cn[3] = {1, 1, 1};
+    static int cbox[6], cn[3];
+    for (int q = 0; q < 6; ++q) cbox[q] = g_cbox[q];
+    for (int q = 0; q < 3; ++q) cn[q] = g_cn[q];
     static float* P[56];
     const char* order[] = {
         "Ex", "Jx", "Ey", "Jy", "Ez", "Jz", "gEx", "gEy",
@@ -422,6 +438,7 @@ static bool do_calc_h(int m) {
 // One reference E half-step (calc_e) at time index m with source slot src_slot (-1: none).
 int rh_calc_e(int m, int src_slot, const float* signal, long long nsig) {
     if (!g_ready) { g_err = "not set up"; return -1; }
+    if (g_port_steps > 0) { g_err = "single half-steps are not used with a port"; return -1; }
     if (signal && !ensure_signal(signal, nsig)) return -1;
     if (!do_calc_e(m, src_slot)) return -1;
     return ck(cudaDeviceSynchronize(), "calc_e sync") ? 0 : -1;
@@ -429,6 +446,7 @@ int rh_calc_e(int m, int src_slot, const float* signal, long long nsig) {
 
 int rh_calc_h(int m) {
     if (!g_ready) { g_err = "not set up"; return -1; }
+    if (g_port_steps > 0) { g_err = "single half-steps are not used with a port"; return -1; }
     if (!do_calc_h(m)) return -1;
     return ck(cudaDeviceSynchronize(), "calc_h sync") ? 0 : -1;
 }
@@ -440,6 +458,7 @@ int rh_run(int m0, int n_steps, int src_slot, const float* signal, long long nsi
            int nprobes, const int* pcomp, const int* pi, const int* pj, const int* pk,
            float* probe_out, float* elapsed_ms) {
     if (!g_ready) { g_err = "not set up"; return -1; }
+    if (g_port_steps > 0 && (m0 < 0 || m0 + n_steps > g_port_steps)) { g_err = "steps beyond the port sample arrays"; return -1; }
     if (signal && !ensure_signal(signal, nsig)) return -1;
     if (nprobes > 0) {
         if (nprobes > g_probe_cap) {
@@ -486,5 +505,102 @@ int rh_run(int m0, int n_steps, int src_slot, const float* signal, long long nsi
 long long rh_padded_dims(int* nx, int* ny) { *nx = g_d.NX; *ny = g_d.NY; return (long long)g_vol; }
 
 void rh_free(void) { free_all(); }
+
+static bool realloc_sample(const char* name, size_t n) {
+    float*& p = g_arr[name];
+    if (p) cudaFree(p);
+    p = nullptr;
+    if (!ck(cudaMalloc(&p, n * sizeof(float)), "cudaMalloc port sample")) return false;
+    return ck(cudaMemset(p, 0, n * sizeof(float)), "memset port sample");
+}
+
+// Place the reference's voltage and current sample boxes (z-directed port, fdtdrav.h:3628-3652
+// sizes) for runs of at most n_steps steps starting at m = 0. Boxes are checked to lie inside the
+// grid with the current box's low x / y neighbours, so every sampleField write stays in bounds.
+int rh_set_port(const int* vbox, const int* cbox, int n_steps) {
+    if (!g_ready) { g_err = "not set up"; return -1; }
+    const int* v = vbox; const int* c = cbox;
+    if (n_steps < 2 || v[0] < 0 || v[3] >= g_d.NXX || v[0] > v[3] || v[1] < 0 || v[4] >= g_d.NYY || v[1] > v[4] ||
+        v[2] < 0 || v[5] >= g_d.NZ || v[2] >= v[5] || c[0] < 1 || c[3] >= g_d.NXX || c[0] > c[3] || c[1] < 1 ||
+        c[4] >= g_d.NYY || c[1] > c[4] || c[2] < 1 || c[5] >= g_d.NZ || c[2] > c[5]) {
+        g_err = "port boxes outside the grid"; return -1;
+    }
+    int vnx = v[3] - v[0] + 1, vny = v[4] - v[1] + 1, cnx = c[3] - c[0] + 2, cny = c[4] - c[1] + 2;
+    if (!realloc_sample("sampE", (size_t)vnx * vny * g_d.NZ_N * n_steps)) return -1;
+    for (const char* n : {"sampHx", "sampHy", "sampHz"})
+        if (!realloc_sample(n, (size_t)cnx * cny * g_d.NZ_N * n_steps)) return -1;
+    for (int q = 0; q < 6; ++q) { g_vbox[q] = v[q]; g_cbox[q] = c[q]; }
+    g_vn[0] = vnx; g_vn[1] = vny; g_vn[2] = g_d.NZ_N;
+    g_cn[0] = cnx; g_cn[1] = cny; g_cn[2] = g_d.NZ_N;
+    g_port_steps = n_steps;
+    return 0;
+}
+
+// The reference's port reductions on its own samples, launched as calcVoltCurrent does
+// (fdtdrav.h:3129-3186, NUMDEV = 1, 1-D blocks of 512): voltMgpu and currMgpu (direction 3),
+// then correcI in place. Returns V(t), I(t) before correcI and I(t) after it.
+int rh_port_reduce(int n_steps, float* volt, float* curr_raw, float* curr_avg) {
+    if (g_port_steps <= 0 || n_steps != g_port_steps) { g_err = "rh_set_port first, same n_steps"; return -1; }
+    float *dv = nullptr, *di = nullptr;
+    if (!ck(cudaMalloc(&dv, n_steps * sizeof(float)), "cudaMalloc V") ||
+        !ck(cudaMalloc(&di, n_steps * sizeof(float)), "cudaMalloc I")) { cudaFree(dv); return -1; }
+    int block = 512, grid = n_steps / block + ((n_steps % block) == 0 ? 0 : 1);
+    int off = 0, dir = 3, n = n_steps;
+    static int vb[6], cb[6], vn[4], cn[4];
+    for (int q = 0; q < 6; ++q) { vb[q] = g_vbox[q]; cb[q] = g_cbox[q]; }
+    vn[0] = g_vn[0]; vn[1] = g_vn[1]; vn[2] = g_d.NZ; vn[3] = g_d.NZ_N;
+    cn[0] = g_cn[0]; cn[1] = g_cn[1]; cn[2] = g_d.NZ; cn[3] = g_d.NZ_N;
+    static float* P[5];
+    bool ok = true;
+    {
+        P[0] = dv; P[1] = A("sampE");
+        std::vector<void*> a = {&vn[0], &vn[1], &vn[2], &vn[3], &off};
+        for (int q = 0; q < 6; ++q) a.push_back(&vb[q]);
+        a.push_back(&P[0]); a.push_back(&P[1]);
+        a.push_back(&g_d.dx); a.push_back(&g_d.dy); a.push_back(&g_d.dz); a.push_back(&n); a.push_back(&dir);
+        ok = ok && launch(K_VOLT, dim3(grid), dim3(block), a);
+    }
+    {
+        P[0] = di; P[2] = A("sampHx"); P[3] = A("sampHy"); P[4] = A("sampHz");
+        std::vector<void*> a = {&cn[0], &cn[1], &cn[2], &cn[3], &off};
+        for (int q = 0; q < 6; ++q) a.push_back(&cb[q]);
+        a.push_back(&P[0]); a.push_back(&P[2]); a.push_back(&P[3]); a.push_back(&P[4]);
+        a.push_back(&g_d.dx); a.push_back(&g_d.dy); a.push_back(&g_d.dz); a.push_back(&n); a.push_back(&dir);
+        ok = ok && launch(K_CURR, dim3(grid), dim3(block), a);
+    }
+    ok = ok && ck(cudaDeviceSynchronize(), "port reduce sync") &&
+         ck(cudaMemcpy(volt, dv, n_steps * sizeof(float), cudaMemcpyDeviceToHost), "V D2H") &&
+         ck(cudaMemcpy(curr_raw, di, n_steps * sizeof(float), cudaMemcpyDeviceToHost), "I D2H");
+    if (ok) {
+        std::vector<void*> a = {&P[0], &n};
+        ok = launch(K_CORREC, dim3(grid), dim3(block), a) && ck(cudaDeviceSynchronize(), "correcI sync") &&
+             ck(cudaMemcpy(curr_avg, di, n_steps * sizeof(float), cudaMemcpyDeviceToHost), "I avg D2H");
+    }
+    cudaFree(dv); cudaFree(di);
+    return ok ? 0 : -1;
+}
+
+// The reference's c_zinS11 (fdtdrav.h:2510-2548) on given spectra of n_t_steps/2 + 1 bins
+// (interleaved complex): returns s11 and zin, launched as calc_otm2 does (blocks of 1024).
+int rh_zin(int n_t_steps, const float* V, const float* I, float z0_re, float z0_im, float* s11, float* zin) {
+    if (!g_lib) { g_err = "rh_load not called"; return -1; }
+    size_t nf = (size_t)n_t_steps / 2 + 1, bytes = nf * 2 * sizeof(float);
+    float* d[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    bool ok = true;
+    for (int q = 0; q < 6 && ok; ++q) ok = ck(cudaMalloc(&d[q], bytes), "cudaMalloc zin");
+    ok = ok && ck(cudaMemcpy(d[0], V, bytes, cudaMemcpyHostToDevice), "V H2D") &&
+         ck(cudaMemcpy(d[1], I, bytes, cudaMemcpyHostToDevice), "I H2D");
+    if (ok) {
+        int threads = 1024, grid = (int)((nf + threads - 1) / threads), n = n_t_steps;
+        struct { float x, y; } z0 = {z0_re, z0_im};
+        float dt = g_d.dt;
+        std::vector<void*> a = {&d[0], &d[1], &n, &d[2], &d[3], &d[4], &d[5], &z0, &dt};
+        ok = launch(K_ZIN, dim3(grid), dim3(threads), a) && ck(cudaDeviceSynchronize(), "zin sync") &&
+             ck(cudaMemcpy(s11, d[4], bytes, cudaMemcpyDeviceToHost), "s11 D2H") &&
+             ck(cudaMemcpy(zin, d[5], bytes, cudaMemcpyDeviceToHost), "zin D2H");
+    }
+    for (int q = 0; q < 6; ++q) cudaFree(d[q]);
+    return ok ? 0 : -1;
+}
 
 }  // extern "C"

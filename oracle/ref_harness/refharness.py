@@ -52,6 +52,9 @@ class RefHarness:
         L.rh_calc_e.argtypes = [_i, _i, _pf, ctypes.c_longlong]
         L.rh_calc_h.argtypes = [_i]
         L.rh_run.argtypes = [_i, _i, _i, _pf, ctypes.c_longlong, _i, _pi, _pi, _pi, _pi, _pf, _pf]
+        L.rh_set_port.argtypes = [_pi, _pi, _i]
+        L.rh_port_reduce.argtypes = [_i, _pf, _pf, _pf]
+        L.rh_zin.argtypes = [_i, _pf, _pf, _f, _f, _pf, _pf]
         self._check(L.rh_load(cubin.encode()))
         self.sc = None
 
@@ -121,6 +124,33 @@ class RefHarness:
                                     n, pc.ctypes.data_as(_pi), pi.ctypes.data_as(_pi), pj.ctypes.data_as(_pi),
                                     pk.ctypes.data_as(_pi), out.ctypes.data_as(_pf), ctypes.byref(ms)))
         return out[:, :n], ms.value
+
+    def set_port(self, voltage_box: Sequence[int], current_box: Sequence[int], steps: int) -> None:
+        """Place the reference's own z-directed voltage / current sample boxes for a run of
+        ``steps`` steps from m = 0 (after ``setup``, before ``run``)."""
+        v = np.ascontiguousarray(voltage_box, dtype=np.int32)
+        c = np.ascontiguousarray(current_box, dtype=np.int32)
+        self._check(self.lib.rh_set_port(v.ctypes.data_as(_pi), c.ctypes.data_as(_pi), steps))
+
+    def port_reduce(self, steps: int) -> tuple:
+        """The reference's voltMgpu / currMgpu / correcI on its samples: (V, I before correcI,
+        I after correcI), float32 arrays of ``steps``."""
+        out = [np.zeros(steps, dtype=np.float32) for _ in range(3)]
+        self._check(self.lib.rh_port_reduce(steps, *(o.ctypes.data_as(_pf) for o in out)))
+        return tuple(out)
+
+    def zin(self, n_t_steps: int, V: np.ndarray, I: np.ndarray, z0: complex) -> tuple:
+        """The reference's c_zinS11 on spectra V, I (complex64, n_t_steps // 2 + 1 bins)."""
+        nf = n_t_steps // 2 + 1
+        v = np.ascontiguousarray(V, dtype=np.complex64)
+        i = np.ascontiguousarray(I, dtype=np.complex64)
+        assert v.size == nf and i.size == nf
+        s11 = np.zeros(nf, dtype=np.complex64)
+        zin = np.zeros(nf, dtype=np.complex64)
+        self._check(self.lib.rh_zin(n_t_steps, v.ctypes.data_as(_pf), i.ctypes.data_as(_pf),
+                                    complex(z0).real, complex(z0).imag, s11.ctypes.data_as(_pf),
+                                    zin.ctypes.data_as(_pf)))
+        return s11, zin
 
     def fields(self) -> dict:
         return {n: self.get(n) for n in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")}

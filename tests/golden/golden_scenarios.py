@@ -79,6 +79,25 @@ def onestep_scenario():
     return sc
 
 
+def port_scenario():
+    """30x28x24 grid with a dielectric slab under a 2x2-edge lumped port (source, voltage and
+    current boxes on the same edges), 700 steps: more than one 512-thread block of the
+    reference's time-series kernels."""
+    steps = 700
+    sc = S.vacuum_cube(30, steps, pml=5, name="port")
+    sc.nx, sc.ny, sc.nz = 30, 28, 24
+    sc.pml = (5, 6, 5, 6, 5, 4)
+    sc.materials.append(S.Material(eps_r=4.4, sigma_e=0.005))
+    sc.bricks.append(S.Brick((8, 7, 6, 22, 21, 9), len(sc.materials) - 1))
+    sc.sources = [S.LumpedSource(PORT_BOX, 50.0, S.gaussian_derivative(steps, sc.dt, 20e9, 1e-3))]
+    sc.probes = [S.Probe(S.EZ, 20, 14, 10), S.Probe(S.HY, 13, 14, 11)]
+    return sc
+
+
+# voltage box: i, j closed, k half-open (voltMgpu case 3); current box: loop at plane ke - 1
+PORT_BOX = (14, 13, 9, 15, 14, 12)
+
+
 def fixture_scenarios():
     """(scenario, keep full fields?) for every run fixture."""
     return [(vacuum64(), False), (small_vacuum(), True), (boxes_scenario(), True), (two_sources(), True)]

@@ -6,7 +6,9 @@ reference-kernel harness built under oracle/_ref by oracle/build_ref.sh).
 Writes one compressed .npz per scenario: the probe series of every step and, for the small grids,
 the six final fields; plus ``onestep.npz`` (one calc_e and one calc_h applied to a seeded random
 state) and ``coefs.npz`` (the reference's per-edge coefficients and 1-D CPML profiles for the
-random-box scenario). The scenarios are defined in golden_scenarios.py so the tests rebuild them
+random-box scenario); ``port.npz`` (the reference's own port sampling and time-series kernels,
+voltMgpu / currMgpu / correcI, on the port scenario, plus c_zinS11 on seeded spectra). The
+scenarios are defined in golden_scenarios.py so the tests rebuild them
 bit-for-bit without running this script.
 """
 from __future__ import annotations
@@ -133,12 +135,44 @@ def onestep_psi(sc, seed=77):
         h.close()
 
 
+def port_fixture():
+    """Port V(t) / I(t) of the reference's own sampling (calc_e / calc_h sample boxes) and
+    reductions; and c_zinS11 applied to seeded random spectra (n = 700, 351 bins)."""
+    sc = gs.port_scenario()
+    h = refharness.RefHarness()
+    try:
+        h.setup(sc)
+        h.set_port(gs.PORT_BOX, gs.PORT_BOX, sc.steps)
+        probes, _ = h.run(sc.steps, src_slot=0, signal=sc.signal_per_node(0), probes=sc.probes)
+        v, i_raw, i_avg = h.port_reduce(sc.steps)
+        rng = np.random.default_rng(321)
+        nf = sc.steps // 2 + 1
+        sv = (rng.standard_normal(nf) + 1j * rng.standard_normal(nf)).astype(np.complex64)
+        si = (rng.standard_normal(nf) + 1j * rng.standard_normal(nf)).astype(np.complex64) * np.float32(0.02)
+        z0 = complex(50.0, 0.0)
+        s11, zin = h.zin(sc.steps, sv, si, z0)
+        z1 = complex(75.0, -12.5)
+        s11b, zinb = h.zin(sc.steps, sv, si, z1)
+        lines = {n: h.get(n, line_len(sc, ax)) for n, ax in LINE_NAMES}
+    finally:
+        h.close()
+    return {"probes": probes, "voltage": v, "current_raw": i_raw, "current_avg": i_avg,
+            "spec_v": sv, "spec_i": si, "z0": np.array([z0, z1], dtype=np.complex64),
+            "s11": np.stack([s11, s11b]), "zin": np.stack([zin, zinb]), **lines}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
     ap.add_argument("--analysis", default=None, help="also write large analysis-only dumps here")
+    ap.add_argument("--only", default=None, choices=["port"], help="write one fixture only")
     args = ap.parse_args()
     os.makedirs(args.out, exist_ok=True)
+    if args.only == "port":
+        np.savez_compressed(os.path.join(args.out, "port.npz"), **port_fixture())
+        print("port fixture written to", args.out)
+        return
+    np.savez_compressed(os.path.join(args.out, "port.npz"), **port_fixture())
     for sc, full in gs.fixture_scenarios():
         np.savez_compressed(os.path.join(args.out, sc.name + ".npz"), **run_scenario(sc, full))
     np.savez_compressed(os.path.join(args.out, "onestep.npz"), **onestep(gs.onestep_scenario()))
