@@ -30,8 +30,17 @@ constexpr int TX = 32, TY = 16;             // tile of nodes owned by a CTA (and
 constexpr int NTH = 256;                    // threads per CTA
 constexpr int ROWS = TX * TY / NTH;         // nodes per thread per plane (rows ty, ty + 8)
 constexpr int RSTEP = NTH / TX;             // row distance between a thread's nodes
-constexpr int NSTAGE = 3;                   // planes resident in the ring
-constexpr int AHEAD = 1;                    // planes loaded ahead of the one computed (<= NSTAGE - 2)
+#ifndef FDTD_FUSED_NSTAGE
+#define FDTD_FUSED_NSTAGE 3
+#endif
+#ifndef FDTD_FUSED_AHEAD
+#define FDTD_FUSED_AHEAD 1
+#endif
+#ifndef FDTD_FUSED_MIN_BLOCKS
+#define FDTD_FUSED_MIN_BLOCKS 3
+#endif
+constexpr int NSTAGE = FDTD_FUSED_NSTAGE;   // planes resident in the ring
+constexpr int AHEAD = FDTD_FUSED_AHEAD;     // planes loaded ahead of the one computed (<= NSTAGE - 2)
 constexpr int HW = TX + 8, HH = TY + 2;     // H tile: x in [x0-4, x0+TX+4), y in [y0-1, y0+TY+1)
 constexpr int EW = TX + 4, EH = TY + 1;     // old-E tile: x in [x0, x0+TX+4), y in [y0, y0+TY+1)
 constexpr int MW = TX + 32, MH = TY + 2;    // class tile: x in [x0-16, x0+TX+16), y in [y0-1, ...)
@@ -50,6 +59,9 @@ constexpr int kMaxItemPlanes = 512;  // planes streamed by one item (chunk + 2);
 constexpr int SMEM_INTERIOR = NSTAGE * STAGE_BYTES + ENEW_BYTES + NSTAGE * 8 + kMaxItemPlanes;
 static_assert(NSTAGE >= AHEAD + 2, "the ring recycles the stage of plane k - 2 at plane k");
 static_assert(NHALO <= 64, "halo nodes live on the first two warps");
+
+constexpr int kShellRows = 8;  // rows of a shell item (the shell kernels' block is 32 x 8)
+static_assert(TY % kShellRows == 0, "shell items split a tile into whole halves");
 
 constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
 
@@ -214,7 +226,7 @@ __device__ __forceinline__ void store3(float* a, float* b, float* c, long long n
 // Interior sweep over `items` (int4 {x0, y0, k0, k1}, one per CTA; plan_fused puts only interior
 // tiles and planes here). Per-thread ring offsets are fixed for the whole item, nothing is bounds-
 // checked, and the per-plane lumped / probe flags are read once into shared memory.
-__global__ void __launch_bounds__(NTH, 3)
+__global__ void __launch_bounds__(NTH, FDTD_FUSED_MIN_BLOCKS)
 k_sweep_interior(const __grid_constant__ FusedMaps maps, const __grid_constant__ StepParams p, FieldPtrs fo,
                  const int4* __restrict__ items, long long m) {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -363,13 +375,13 @@ cudaError_t fused_configure() {
 // One fused step: shell E (general items), interior sweep, shell H (general items).
 cudaError_t launch_fused(const FusedMaps& maps, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo,
                          const PsiSet& psi_in, const PsiSet& psi_out, long long m, const FusedWork& w, cudaStream_t st) {
-    cudaError_t e = launch_shell(true, p, fi, fo, psi_in, psi_out, w.general, w.n_general, TY, m, st);
+    cudaError_t e = launch_shell(true, p, fi, fo, psi_in, psi_out, w.general, w.n_general, m, st);
     if (e == cudaSuccess) e = launch_design_e(p, fi, fo, psi_in, psi_out, m, st);
     if (e != cudaSuccess) return e;
     if (w.n_interior > 0) k_sweep_interior<<<w.n_interior, NTH, SMEM_INTERIOR, st>>>(maps, p, fo, w.interior, m);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    return launch_shell(false, p, fi, fo, psi_in, psi_out, w.general, w.n_general, TY, m, st);
+    return launch_shell(false, p, fi, fo, psi_in, psi_out, w.general, w.n_general, m, st);
 }
 
 // Tensor maps of the buffers the interior sweep reads: H tiles with a one-node halo (x widened to
@@ -401,7 +413,7 @@ int encode_fused_maps(FusedMaps* out, const DeviceGrid& g, float* const h[3], fl
 // Split the grid into items: tiles whose E positions (x0..x0+TX, y0..y0+TY) lie in the x / y
 // interior get their interior planes as interior items (chunks of at most kc planes); everything
 // else (boundary / CPML tiles, and the z-boundary and z-CPML planes of interior tiles) becomes
-// general items. The E positions of plane k1 of an item are recomputed, so a chunk must also keep
+// shell items of one plane and half a tile. The E positions of plane k1 of an item are recomputed, so a chunk must also keep
 // its top plane in the interior range to stay interior. The tile grid starts at (ox, oy) <= 0,
 // chosen to put as many nodes as possible in interior tiles; ox is a multiple of 16 so that every
 // TMA box starts on a 16-byte boundary (material box at x0 - 16, one byte per cell).
@@ -429,8 +441,15 @@ void plan_fused(const DeviceGrid& g, int kc, const int* design_box, std::vector<
     }
     const int zlo = g.pzn > 1 ? g.pzn : 1;
     const int zhi = (g.nz - 1 - g.pzp < g.nz - 2) ? g.nz - 1 - g.pzp : g.nz - 2;  // last interior plane
-    auto chunks = [&](std::vector<int4>& out, int x0, int y0, int a, int b) {  // planes [a, b)
+    auto chunks = [&](std::vector<int4>& out, int x0, int y0, int a, int b) {  // interior planes [a, b)
         for (int k = a; k < b; k += kc) out.push_back(make_int4(x0, y0, k, k + kc < b ? k + kc : b));
+    };
+    // shell items: the 32 x 8 halves of a tile, one plane each, one node per thread (halves with no
+    // node inside the grid are left out)
+    auto shell = [&](int x0, int y0, int a, int b) {
+        for (int k = a; k < b; ++k)
+            for (int h = 0; h < TY; h += kShellRows)
+                if (y0 + h + kShellRows > 0 && y0 + h < g.ny) general_items.push_back(make_int4(x0, y0 + h, k, 0));
     };
     for (int y0 = oy; y0 < g.ny; y0 += TY)
         for (int x0 = ox; x0 < g.nx; x0 += TX) {
@@ -442,11 +461,11 @@ void plan_fused(const DeviceGrid& g, int kc, const int* design_box, std::vector<
                 tile_int = false;
             // interior items cover planes [zlo, zhi) so that the recomputed top plane <= zhi
             if (tile_int && zhi > zlo) {
-                chunks(general_items, x0, y0, 0, zlo);
+                shell(x0, y0, 0, zlo);
                 chunks(interior_items, x0, y0, zlo, zhi);
-                chunks(general_items, x0, y0, zhi, g.nz);
+                shell(x0, y0, zhi, g.nz);
             } else {
-                chunks(general_items, x0, y0, 0, g.nz);
+                shell(x0, y0, 0, g.nz);
             }
         }
 }

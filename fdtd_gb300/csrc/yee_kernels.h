@@ -30,7 +30,7 @@ cudaError_t launch_design_e(const StepParams& p, const FieldPtrs& fi, const Fiel
 // Shell passes of the fused schedule (yee_two_pass.cu): E (e_pass) or H of the nodes of `items`,
 // reading fi / pin (buffer A) and writing fo / pout (buffer B).
 cudaError_t launch_shell(bool e_pass, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
-                         const PsiSet& pout, const int4* items, int n_items, int tile_h, long long m, cudaStream_t st);
+                         const PsiSet& pout, const int4* items, int n_items, long long m, cudaStream_t st);
 
 // Fused schedule (yee_fused.cu): per step the shell E pass, the z-marching interior sweep (TMA
 // tiles of buffer A: H with halo, old E, node class) and the shell H pass; fields A -> B, CPML
@@ -40,8 +40,9 @@ struct FusedMaps {
     CUtensorMap e[3];
     CUtensorMap cls;
 };
-// Work items of one step (device arrays of int4 {x0, y0, k0, k1}): interior items for the sweep,
-// general items for the shell passes (plan_fused).
+// Work items of one step (device arrays of int4): interior items {x0, y0, k0, k1} for the sweep
+// (a 32 x 16 column over planes [k0, k1)), general items {x0, y0, k, 0} for the shell passes
+// (32 x 8 nodes of plane k) (plan_fused).
 struct FusedWork {
     const int4* interior;
     int n_interior;

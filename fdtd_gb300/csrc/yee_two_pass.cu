@@ -23,41 +23,33 @@ __global__ void __launch_bounds__(256) k_update_h(const __grid_constant__ StepPa
     h_node_global(p, f, f, f, ps, ps, i, j, blockIdx.z, m);
 }
 
-// Shell passes of the fused schedule: the nodes of the general items (int4 {x0, y0, k0, k1}, a
-// 32 x tile_h tile and a plane range; x0, y0 may be negative) read buffer A (`fi`, `pin`) and
-// write buffer B (`fo`, `pout`). The E pass runs before the interior sweep, the H pass after it,
-// since H reads new E at interior nodes next to the shell.
+// Shell passes of the fused schedule: the nodes of the shell items (int4 {x0, y0, k, -}, a 32 x 8
+// block of plane k; x0, y0 may be negative) read buffer A (`fi`, `pin`) and write buffer B (`fo`,
+// `pout`), one node per thread as in the two-pass kernels. The E pass runs before the interior
+// sweep, the H pass after it, since H reads new E at interior nodes next to the shell.
 __global__ void __launch_bounds__(256) k_shell_e(const __grid_constant__ StepParams p, FieldPtrs fi, FieldPtrs fo,
                                                  const __grid_constant__ PsiSet pin, const __grid_constant__ PsiSet pout,
-                                                 const int4* __restrict__ items, int tile_h, long long m) {
+                                                 const int4* __restrict__ items, long long m) {
     const int4 it = items[blockIdx.x];
-    const int i = it.x + (int)threadIdx.x;
-    if (i < 0 || i >= p.g.nx) return;
-    for (int r = threadIdx.y; r < tile_h; r += 8) {
-        const int j = it.y + r;
-        if (j < 0 || j >= p.g.ny) continue;
-        for (int k = it.z; k < it.w; ++k) e_node_global(p, fi, fo, pin, pout, i, j, k, m);
-    }
+    const int i = it.x + (int)threadIdx.x, j = it.y + (int)threadIdx.y;
+    if (i < 0 || i >= p.g.nx || j < 0 || j >= p.g.ny) return;
+    e_node_global(p, fi, fo, pin, pout, i, j, it.z, m);
 }
 
 __global__ void __launch_bounds__(256) k_shell_h(const __grid_constant__ StepParams p, FieldPtrs fi, FieldPtrs fo,
                                                  const __grid_constant__ PsiSet pin, const __grid_constant__ PsiSet pout,
-                                                 const int4* __restrict__ items, int tile_h, long long m) {
+                                                 const int4* __restrict__ items, long long m) {
     const int4 it = items[blockIdx.x];
-    const int i = it.x + (int)threadIdx.x;
-    if (i < 0 || i >= p.g.nx) return;
-    for (int r = threadIdx.y; r < tile_h; r += 8) {
-        const int j = it.y + r;
-        if (j < 0 || j >= p.g.ny) continue;
-        for (int k = it.z; k < it.w; ++k) h_node_global(p, fi, fo, fo, pin, pout, i, j, k, m);
-    }
+    const int i = it.x + (int)threadIdx.x, j = it.y + (int)threadIdx.y;
+    if (i < 0 || i >= p.g.nx || j < 0 || j >= p.g.ny) return;
+    h_node_global(p, fi, fo, fo, pin, pout, i, j, it.z, m);
 }
 
 cudaError_t launch_shell(bool e_pass, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
-                         const PsiSet& pout, const int4* items, int n_items, int tile_h, long long m, cudaStream_t st) {
+                         const PsiSet& pout, const int4* items, int n_items, long long m, cudaStream_t st) {
     if (n_items <= 0) return cudaSuccess;
-    if (e_pass) k_shell_e<<<n_items, dim3(32, 8, 1), 0, st>>>(p, fi, fo, pin, pout, items, tile_h, m);
-    else k_shell_h<<<n_items, dim3(32, 8, 1), 0, st>>>(p, fi, fo, pin, pout, items, tile_h, m);
+    if (e_pass) k_shell_e<<<n_items, dim3(32, 8, 1), 0, st>>>(p, fi, fo, pin, pout, items, m);
+    else k_shell_h<<<n_items, dim3(32, 8, 1), 0, st>>>(p, fi, fo, pin, pout, items, m);
     return cudaGetLastError();
 }
 
