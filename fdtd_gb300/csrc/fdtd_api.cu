@@ -47,6 +47,14 @@ struct LumpedDef {
     int source;  // waveform index or -1
 };
 
+// A zero-thickness plate (definePlateX / Y / Z): normal axis, box, sigma_e of its two tangential
+// components in axis order.
+struct PlateDef {
+    int axis;
+    int box[6];
+    float sigma[2];
+};
+
 // A z-directed port: the point probes of its voltage edges (k outer, then j, then i, as voltMgpu
 // sums them) followed by its current loop at plane ke - 1 of the current box: Hx at j = js - 1
 // (i = is..ie), Hx at j = je, Hy at i = ie (j = js..je), Hy at i = is - 1.
@@ -100,6 +108,11 @@ struct fdtd_handle {
     bool dirty_lumped = true, dirty_probes = true, dirty_materials = true;
     LumpedEdge* d_lumped = nullptr;
     int* d_lumped_k = nullptr;
+    std::vector<PlateDef> plates;
+    PlateEdges* d_plates = nullptr;
+    int* d_plate_k = nullptr;
+    int4* d_plate_nodes = nullptr;
+    int n_plate_nodes = 0;
     Probe* d_probes = nullptr;
     int* d_probe_k = nullptr;
     int* d_probe_ids = nullptr;
@@ -191,6 +204,10 @@ StepParams make_params(fdtd_handle* h) {
     p.status = h->status;
     p.deps = h->has_design ? h->d_deps : nullptr;
     for (int q = 0; q < 6; ++q) p.dbox[q] = h->dbox[q];
+    p.plates = h->plates.empty() ? nullptr : h->d_plates;
+    p.plate_k = h->plates.empty() ? nullptr : h->d_plate_k;
+    p.plate_nodes = h->d_plate_nodes;
+    p.n_plate_nodes = h->plates.empty() ? 0 : h->n_plate_nodes;
     p.bg.mat = 0;  // the background material fills the CPML slabs in the usual layouts
     for (int a = 0; a < 3; ++a)
         for (int s = 0; s < 2; ++s) {
@@ -494,6 +511,23 @@ int fdtd_add_resistor(fdtd_handle* h, int32_t axis, const int32_t box[6], float 
     return FDTD_OK;
 }
 
+int fdtd_add_plate(fdtd_handle* h, int32_t normal_axis, const int32_t box[6], float sigma_1, float sigma_2) {
+    if (!h || !box) return fail(FDTD_ERR_INVALID, "NULL argument");
+    if (normal_axis < 0 || normal_axis > 2) return fail(FDTD_ERR_INVALID, "normal axis must be 0 (x), 1 (y) or 2 (z)");
+    if (h->step > 0) return fail(FDTD_ERR_STATE, "plates must be added before the first step");
+    if (h->has_design) return fail(FDTD_ERR_STATE, "plates cannot be combined with a design region");
+    const DeviceGrid& g = h->g;
+    const int n[3] = {g.nx, g.ny, g.nz};
+    for (int a = 0; a < 3; ++a)
+        if (box[a] < 0 || box[a] > box[a + 3] || box[a] >= n[a])
+            return fail(FDTD_ERR_INVALID, "plate box outside the grid or reversed");
+    if (!(sigma_1 >= 0.f) || !(sigma_2 >= 0.f)) return fail(FDTD_ERR_INVALID, "plate conductivities must be >= 0");
+    PlateDef P{normal_axis, {box[0], box[1], box[2], box[3], box[4], box[5]}, {sigma_1, sigma_2}};
+    h->plates.push_back(P);
+    h->dirty_lumped = true;  // node classes and plate tables are rebuilt with the lumped tables
+    return FDTD_OK;
+}
+
 int fdtd_add_probe(fdtd_handle* h, int32_t comp, int32_t i, int32_t j, int32_t k, int32_t* id_out) {
     if (!h) return fail(FDTD_ERR_INVALID, "handle is NULL");
     if (comp < 0 || comp > 5) return fail(FDTD_ERR_INVALID, "component must be 0..5");
@@ -787,6 +821,93 @@ int build_lumped(fdtd_handle* h) {
     return FDTD_OK;
 }
 
+// The E edges each plate covers, per component and plane, in the order of definePlateX / Y / Z
+// (fdtdrav.h:1574-1679), clipped to the grid: X plate at i = is: Ey j in [js, je), k in [ks, ke];
+// Ez j in [js, je], k in [ks, ke). Y plate at j = js: Ez i in [is, ie], k in [ks, ke); Ex i in
+// [is, ie), k in [ks, ke]. Z plate at k = ks: Ex i in [is, ie), j in [js, je]; Ey i in [is, ie],
+// j in [js, je).
+struct PlateRange {
+    int comp;
+    int lo[3], hi[3];  // inclusive node ranges
+    float sigma;
+};
+std::vector<PlateRange> plate_ranges(const DeviceGrid& g, const PlateDef& P) {
+    const int* b = P.box;
+    std::vector<PlateRange> out;
+    auto add = [&](int comp, int i0, int i1, int j0, int j1, int k0, int k1, float s) {
+        PlateRange r{comp, {std::max(i0, 0), std::max(j0, 0), std::max(k0, 0)},
+                     {std::min(i1, g.nx - 1), std::min(j1, g.ny - 1), std::min(k1, g.nz - 1)}, s};
+        if (r.lo[0] <= r.hi[0] && r.lo[1] <= r.hi[1] && r.lo[2] <= r.hi[2]) out.push_back(r);
+    };
+    if (P.axis == 0) {
+        add(1, b[0], b[0], b[1], b[4] - 1, b[2], b[5], P.sigma[0]);
+        add(2, b[0], b[0], b[1], b[4], b[2], b[5] - 1, P.sigma[1]);
+    } else if (P.axis == 1) {
+        add(2, b[0], b[3], b[1], b[1], b[2], b[5] - 1, P.sigma[1]);
+        add(0, b[0], b[3] - 1, b[1], b[1], b[2], b[5], P.sigma[0]);
+    } else {
+        add(0, b[0], b[3] - 1, b[1], b[4], b[2], b[2], P.sigma[0]);
+        add(1, b[0], b[3], b[1], b[4] - 1, b[2], b[2], P.sigma[1]);
+    }
+    return out;
+}
+
+// Plate tables: edge ranges bucketed by plane (plate order kept within a plane, so the last plate
+// wins as in the reference), and the list of nodes with a covered edge (node class kPlateNode).
+int build_plates(fdtd_handle* h) {
+    h->release(h->d_plates); h->release(h->d_plate_k); h->release(h->d_plate_nodes);
+    h->d_plates = nullptr; h->d_plate_k = nullptr; h->d_plate_nodes = nullptr;
+    h->n_plate_nodes = 0;
+    if (h->plates.empty()) return FDTD_OK;
+    const DeviceGrid& g = h->g;
+    std::vector<std::vector<PlateEdges>> per_k(g.nz);
+    std::vector<long long> nodes;
+    for (const PlateDef& P : h->plates)
+        for (const PlateRange& r : plate_ranges(g, P))
+            for (int k = r.lo[2]; k <= r.hi[2]; ++k) {
+                per_k[k].push_back(PlateEdges{r.comp, r.lo[0], r.hi[0], r.lo[1], r.hi[1], r.sigma});
+                for (int j = r.lo[1]; j <= r.hi[1]; ++j)
+                    for (int i = r.lo[0]; i <= r.hi[0]; ++i) nodes.push_back(((long long)k * g.ny + j) * g.nx + i);
+            }
+    std::sort(nodes.begin(), nodes.end());
+    nodes.erase(std::unique(nodes.begin(), nodes.end()), nodes.end());
+    // lumped Ez edges take their own coefficients from the cells' materials: no plate may cover one
+    std::vector<long long> lumped_ez;
+    for (const LumpedDef& L : h->lumped)
+        for (int k = L.box[2]; k < L.box[5]; ++k)
+            for (int j = L.box[1]; j <= L.box[4]; ++j)
+                for (int i = L.box[0]; i <= L.box[3]; ++i) lumped_ez.push_back(((long long)k * g.ny + j) * g.nx + i);
+    std::sort(lumped_ez.begin(), lumped_ez.end());
+    for (const PlateDef& P : h->plates)
+        for (const PlateRange& r : plate_ranges(g, P)) {
+            if (r.comp != 2) continue;
+            for (int k = r.lo[2]; k <= r.hi[2]; ++k)
+                for (int j = r.lo[1]; j <= r.hi[1]; ++j)
+                    for (int i = r.lo[0]; i <= r.hi[0]; ++i)
+                        if (std::binary_search(lumped_ez.begin(), lumped_ez.end(), ((long long)k * g.ny + j) * g.nx + i))
+                            return fail(FDTD_ERR_INVALID, "a plate covers the Ez edge of a lumped element");
+        }
+    std::vector<PlateEdges> flat;
+    std::vector<int> koff(g.nz + 1, 0);
+    for (int k = 0; k < g.nz; ++k) {
+        flat.insert(flat.end(), per_k[k].begin(), per_k[k].end());
+        koff[k + 1] = (int)flat.size();
+    }
+    std::vector<int4> list(nodes.size());
+    for (size_t q = 0; q < nodes.size(); ++q) {
+        const long long v = nodes[q];
+        list[q] = make_int4((int)(v % g.nx), (int)((v / g.nx) % g.ny), (int)(v / ((long long)g.nx * g.ny)), 0);
+    }
+    CUDA_TRY(h->alloc((void**)&h->d_plates, sizeof(PlateEdges) * std::max<size_t>(flat.size(), 1)));
+    CUDA_TRY(h->alloc((void**)&h->d_plate_k, sizeof(int) * (g.nz + 1)));
+    CUDA_TRY(h->alloc((void**)&h->d_plate_nodes, sizeof(int4) * std::max<size_t>(list.size(), 1)));
+    if (!flat.empty()) CUDA_TRY(cudaMemcpy(h->d_plates, flat.data(), sizeof(PlateEdges) * flat.size(), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(h->d_plate_k, koff.data(), sizeof(int) * (g.nz + 1), cudaMemcpyHostToDevice));
+    if (!list.empty()) CUDA_TRY(cudaMemcpy(h->d_plate_nodes, list.data(), sizeof(int4) * list.size(), cudaMemcpyHostToDevice));
+    h->n_plate_nodes = (int)list.size();
+    return FDTD_OK;
+}
+
 int build_probes(fdtd_handle* h) {
     h->release(h->d_probes); h->release(h->d_probe_k); h->release(h->d_probe_ids); h->release(h->ring);
     h->d_probes = nullptr; h->d_probe_k = nullptr; h->d_probe_ids = nullptr; h->ring = nullptr;
@@ -840,6 +961,9 @@ int ensure_prepared(fdtd_handle* h) {
         }
         CUDA_TRY(launch_node_class(h->g, h->mat, h->d_lumped, h->n_lumped_edges, h->has_design ? h->dbox : nullptr, h->cls,
                                    h->stream));
+        rc = build_plates(h);
+        if (rc) return rc;
+        if (h->n_plate_nodes > 0) CUDA_TRY(launch_class_nodes(h->g, h->d_plate_nodes, h->n_plate_nodes, kPlateNode, h->cls, h->stream));
     }
     if (h->dirty_probes) {
         int rc = build_probes(h);
@@ -1023,6 +1147,7 @@ extern "C" int fdtd_set_design_region(fdtd_handle* h, const int32_t box[6], cons
         return fail(FDTD_ERR_INVALID, "design base material: mu_r > 0, sigma_e >= 0, sigma_m > 0");
     if ((int)h->materials.size() > kDesign)
         return fail(FDTD_ERR_INVALID, "material index 255 is reserved for the design region: at most 255 materials");
+    if (!h->plates.empty()) return fail(FDTD_ERR_STATE, "a design region cannot be combined with plates");
     for (const LumpedDef& L : h->lumped) {  // the cells of a lumped Ez edge (i,j): i-1..i, j-1..j
         const int* b = L.box;
         if (b[0] - 1 < box[3] && box[0] <= b[3] && b[1] - 1 < box[4] && box[1] <= b[4] && b[2] < box[5] && box[2] < b[5])
@@ -1306,6 +1431,7 @@ extern "C" int fdtd_batch_create(fdtd_handle* const* handles, int32_t n, fdtd_ba
         if (!handles[q]) return fail(FDTD_ERR_INVALID, "NULL handle in the batch");
         if (handles[q]->device != dev) return fail(FDTD_ERR_INVALID, "batch handles must live on the current device");
         if (handles[q]->has_design) return fail(FDTD_ERR_INVALID, "handles with a design region cannot join a batch");
+        if (!handles[q]->plates.empty()) return fail(FDTD_ERR_INVALID, "handles with plates cannot join a batch");
         for (int r = 0; r < q; ++r)
             if (handles[r] == handles[q]) return fail(FDTD_ERR_INVALID, "a handle appears twice in the batch");
     }

@@ -21,6 +21,7 @@ constexpr float kTiny = 1.2e-38f;  // setZero's initial value for fields, psi an
 constexpr int kMaxMaterials = 256;
 constexpr int kDefaultEntry = kMaxMaterials;  // H coefficient of faces the reference never averages
 constexpr int kGeneral = 255;                 // node class of nodes that take the general path
+constexpr int kPlateNode = 254;              // node class of nodes with a plate-covered E edge
 constexpr int kDesignNode = 253;              // node class of the design region's edge box; classes
                                               // below it are fast-path material ids
 constexpr int kDesign = 255;                  // material index of design-region cells (per-cell eps_r)
@@ -51,6 +52,15 @@ struct LumpedEdge {
     int i, j, k;
     int source;         // index of the driving waveform, -1 for a resistor
     float ceze, cezhy, cezhx, cezj;
+};
+
+// E edges of one component that a zero-thickness plate covers in the planes it is bucketed under
+// (definePlateX / Y / Z, fdtdrav.h:1574-1679): i in [i0, i1], j in [j0, j1]; their sigma_e is
+// replaced by the plate's.
+struct PlateEdges {
+    int comp;
+    int i0, i1, j0, j1;
+    float sigma;
 };
 
 struct Probe {
@@ -109,6 +119,12 @@ struct StepParams {
     // from deps ((d5-d2), (d4-d1), (d3-d0), x fastest); NULL when the handle has none
     const float* deps;
     int dbox[6];
+    // plate edges bucketed by plane k (CSR offsets, nz + 1 entries, in the order the plates were
+    // added); NULL when the handle has none
+    const PlateEdges* plates;
+    const int* plate_k;
+    const int4* plate_nodes;     // nodes of class kPlateNode {i, j, k, 0} (updated by k_plate_e)
+    int n_plate_nodes;
 };
 
 // ------------------------------------------------------------------------------------------

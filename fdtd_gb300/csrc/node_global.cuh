@@ -12,8 +12,9 @@ namespace fdtd {
 // and its class byte together (one round of memory latency); fast-path nodes (class != kGeneral)
 // then update from the material table, the rest also gather the seven cell materials and take
 // e_update / h_update. kDesign (k_design_e only): skip the class test and average the per-cell
-// eps_r of design cells.
-template <bool kDesign = false, bool kCoherent = false>
+// eps_r of design cells. kPlate (k_plate_e only): plate-covered edges take the plate's sigma_e;
+// the other kernels leave plate nodes (class kPlateNode) alone, CPML memory included.
+template <bool kDesign = false, bool kCoherent = false, bool kPlate = false>
 __device__ __forceinline__ void e_node_global(const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo,
                                               const PsiSet& pin, const PsiSet& pout, int i, int j, int k, long long m) {
     const DeviceGrid& g = p.g;
@@ -44,11 +45,13 @@ __device__ __forceinline__ void e_node_global(const StepParams& p, const FieldPt
         nb.mij = (i > 0 && j > 0) ? mat[n - 1 - R] : 0;
         nb.mik = (i > 0 && k > 0) ? mat[n - 1 - P] : 0;
         nb.mjk = (j > 0 && k > 0) ? mat[n - R - P] : 0;
-        const PsiIO io{pin.f, pout.f, true};
+        // plate nodes are k_plate_e's, CPML memory included: the other kernels store nothing of them
+        const PsiIO io{pin.f, pout.f, kPlate || c != kPlateNode};
         const bool plane_lumped = p.lumped_k[k] < p.lumped_k[k + 1];
-        e_update<kDesign, kCoherent>(p, nb, i, j, k, m, plane_lumped, io, out, pre);
+        e_update<kDesign, kCoherent, kPlate>(p, nb, i, j, k, m, plane_lumped, io, out, pre);
     }
-    if (!kDesign && c == kDesignNode) return;  // k_design_e writes the design region's E
+    // k_design_e writes the design region's E, k_plate_e the plate nodes' E
+    if (!kDesign && !kPlate && (c == kDesignNode || c == kPlateNode)) return;
     fo.ex[n] = out[0]; fo.ey[n] = out[1]; fo.ez[n] = out[2];
     if (p.probe_k[k] < p.probe_k[k + 1]) {
         const long long row = m % p.ring_cap;

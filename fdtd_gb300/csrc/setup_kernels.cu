@@ -235,6 +235,17 @@ __global__ void k_class_lumped(uint8_t* cls, DeviceGrid g, const LumpedEdge* edg
     if (q < n_edges) cls[(long long)edges[q].k * g.plane + (long long)edges[q].j * g.pitch + edges[q].i] = kGeneral;
 }
 
+__global__ void k_class_nodes(uint8_t* cls, DeviceGrid g, const int4* nodes, int n, uint8_t value) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n) cls[(long long)nodes[q].z * g.plane + (long long)nodes[q].y * g.pitch + nodes[q].x] = value;
+}
+
+cudaError_t launch_class_nodes(const DeviceGrid& g, const int4* nodes, int n, int value, uint8_t* cls, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_class_nodes<<<(n + 127) / 128, 128, 0, st>>>(cls, g, nodes, n, (uint8_t)value);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_node_class(const DeviceGrid& g, const uint8_t* mat, const LumpedEdge* edges, int n_edges,
                               const int* design_box, uint8_t* cls, cudaStream_t st) {
     const int4 dlo = design_box ? make_int4(design_box[0], design_box[1], design_box[2], 0) : make_int4(1, 1, 1, 0);

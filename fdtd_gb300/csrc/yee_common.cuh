@@ -92,6 +92,41 @@ __device__ __forceinline__ bool has_design(const StepParams& p, int m0, int m1, 
     return p.deps && (m0 == kDesign || m1 == kDesign || m2 == kDesign || m3 == kDesign);
 }
 
+// Zero-thickness plates (definePlateX / Y / Z, fdtdrav.h:1574-1679, applied after the edge averages
+// and before setCoefficients): for each E component of node (i, j, k) that a plate covers, the
+// coefficients from the edge's averaged eps_r and the plate's sigma_e (the last plate listed
+// wins, as the reference writes them in order). Returns a bit per overridden component and
+// writes its coefficients to c[comp]. Out of line: it runs only in planes holding a plate.
+static __device__ __noinline__ int e_plate(const StepParams* pp, int i, int j, int k, int m0, int mi, int mj, int mk,
+                                           int mij, int mik, int mjk, Coef3* c) {
+    const StepParams& p = *pp;
+    const int b = p.plate_k[k], e = p.plate_k[k + 1];
+    float sig[3];
+    int hit = 0;
+    for (int q = b; q < e; ++q) {
+        const PlateEdges& P = p.plates[q];
+        if (i >= P.i0 && i <= P.i1 && j >= P.j0 && j <= P.j1) {
+            sig[P.comp] = P.sigma;
+            hit |= 1 << P.comp;
+        }
+    }
+    const DeviceGrid& g = p.g;
+    for (int comp = 0; comp < 3; ++comp) {
+        if (!(hit & (1 << comp))) continue;
+        float eps, s_avg;
+        if (comp == 0) edge_material(p, 0, i, j, k, m0, mj, mk, mjk, eps, s_avg);
+        else if (comp == 1) edge_material(p, 1, i, j, k, m0, mi, mk, mik, eps, s_avg);
+        else edge_material(p, 2, i, j, k, m0, mi, mj, mij, eps, s_avg);
+        const float dp = comp == 0 ? g.dy : comp == 1 ? g.dz : g.dx;
+        const float dm = comp == 0 ? g.dz : comp == 1 ? g.dx : g.dy;
+        c[comp] = coef3(eps, sig[comp], g.dt, g.eps0, dp, dm);
+    }
+    return hit;
+}
+__device__ __forceinline__ bool plane_has_plate(const StepParams& p, int k) {
+    return p.plate_k && p.plate_k[k] < p.plate_k[k + 1];
+}
+
 // E-edge coefficients (setCoefficients, fdtdrav.h:1280-1303). `uni`: the four cells around the
 // edge hold material m0, so the table entry applies. comp: 0 = Ex, 1 = Ey, 2 = Ez; the Cb cell
 // sizes are Ex (dy, dz), Ey (dz, dx), Ez (dx, dy). kDesignAware: edges touching the design region
@@ -241,7 +276,9 @@ __device__ __forceinline__ float psi_step(const float* in, float* out, int q, bo
 // then the CPML corrections in the reference's order (x, y, z). pre[] receives the values between
 // the main update and the CPML corrections (the sampleField values, fdtdrav.h:740).
 // plane_lumped: some lumped edge lies in plane k (uniform across a CTA).
-template <bool kDesignAware = false, bool kCoherent = false>
+// kPlate: plate-covered edges take the plate's sigma_e (only k_plate_e, which updates the nodes of
+// node class kPlateNode, instantiates it).
+template <bool kDesignAware = false, bool kCoherent = false, bool kPlate = false>
 __device__ __forceinline__ void e_update(const StepParams& p, const ENbr& n, int i, int j, int k, long long m,
                                          bool plane_lumped, const PsiIO& ps, float out[3], float pre[3]) {
     const DeviceGrid& g = p.g;
@@ -256,19 +293,31 @@ __device__ __forceinline__ void e_update(const StepParams& p, const ENbr& n, int
     const bool ux = n.m0 == n.mj && n.m0 == n.mk && n.m0 == n.mjk;
     const bool uy = n.m0 == n.mi && n.m0 == n.mk && n.m0 == n.mik;
     const bool uz = n.m0 == n.mi && n.m0 == n.mj && n.m0 == n.mij;
-    const Coef3 cx = e_coef<kDesignAware>(p, 0, ux, n.m0, n.mj, n.mk, n.mjk, i, j, k);
-    const Coef3 cy = e_coef<kDesignAware>(p, 1, uy, n.m0, n.mi, n.mk, n.mik, i, j, k);
-    const Coef3 cz = e_coef<kDesignAware>(p, 2, uz, n.m0, n.mi, n.mj, n.mij, i, j, k);
+    Coef3 cx = e_coef<kDesignAware>(p, 0, ux, n.m0, n.mj, n.mk, n.mjk, i, j, k);
+    Coef3 cy = e_coef<kDesignAware>(p, 1, uy, n.m0, n.mi, n.mk, n.mik, i, j, k);
+    Coef3 cz = e_coef<kDesignAware>(p, 2, uz, n.m0, n.mi, n.mj, n.mij, i, j, k);
+    // plate-covered components (kPlate only): plate coefficients, and the background's tabulated
+    // kappa-divided values (which belong to its table coefficients) no longer apply
+    int pm = 0;
+    if constexpr (kPlate) {
+        if (plane_has_plate(p, k)) {
+            Coef3 pc[3];
+            pm = e_plate(&p, i, j, k, n.m0, n.mi, n.mj, n.mk, n.mij, n.mik, n.mjk, pc);
+            if (pm & 1) cx = pc[0];
+            if (pm & 2) cy = pc[1];
+            if (pm & 4) cz = pc[2];
+        }
+    }
     const float dHz_j = __fsub_rn(n.hz, n.hz_jm), dHy_k = __fsub_rn(n.hy, n.hy_km);
     const float dHx_k = __fsub_rn(n.hx, n.hx_km), dHz_i = __fsub_rn(n.hz, n.hz_im);
     const float dHy_i = __fsub_rn(n.hy, n.hy_im), dHx_j = __fsub_rn(n.hx, n.hx_jm);
     const BgCurl& B = p.bg;
     // Ex (fdtdrav.h:665-676)
-    float vx = upd3(cx.a, n.ex, ys ? kdiv(cx.bp, ux && n.m0 == bg, B.e[1][0], p.key, j) : cx.bp, dHz_j,
-                    zs ? kdiv(cx.bm, ux && n.m0 == bg, B.e[2][0], p.kez, k) : cx.bm, dHy_k);
+    float vx = upd3(cx.a, n.ex, ys ? kdiv(cx.bp, ux && n.m0 == bg && !(pm & 1), B.e[1][0], p.key, j) : cx.bp, dHz_j,
+                    zs ? kdiv(cx.bm, ux && n.m0 == bg && !(pm & 1), B.e[2][0], p.kez, k) : cx.bm, dHy_k);
     // Ey (fdtdrav.h:696-707)
-    float vy = upd3(cy.a, n.ey, zs ? kdiv(cy.bp, uy && n.m0 == bg, B.e[2][1], p.kez, k) : cy.bp, dHx_k,
-                    xs ? kdiv(cy.bm, uy && n.m0 == bg, B.e[0][0], p.kex, i) : cy.bm, dHz_i);
+    float vy = upd3(cy.a, n.ey, zs ? kdiv(cy.bp, uy && n.m0 == bg && !(pm & 2), B.e[2][1], p.kez, k) : cy.bp, dHx_k,
+                    xs ? kdiv(cy.bm, uy && n.m0 == bg && !(pm & 2), B.e[0][0], p.kex, i) : cy.bm, dHz_i);
     // Ez with lumped elements (fdtdrav.h:720-741)
     float vz;
     const LumpedEdge* L = plane_lumped ? find_lumped(p, i, j, k) : nullptr;
@@ -280,8 +329,8 @@ __device__ __forceinline__ void e_update(const StepParams& p, const ENbr& n, int
             vz = upd3(L->ceze, n.ez, L->cezhy, dHy_i, L->cezhx, dHx_j);
         }
     } else {
-        vz = upd3(cz.a, n.ez, xs ? kdiv(cz.bp, uz && n.m0 == bg, B.e[0][1], p.kex, i) : cz.bp, dHy_i,
-                  ys ? kdiv(cz.bm, uz && n.m0 == bg, B.e[1][1], p.key, j) : cz.bm, dHx_j);
+        vz = upd3(cz.a, n.ez, xs ? kdiv(cz.bp, uz && n.m0 == bg && !(pm & 4), B.e[0][1], p.kex, i) : cz.bp, dHy_i,
+                  ys ? kdiv(cz.bm, uz && n.m0 == bg && !(pm & 4), B.e[1][1], p.key, j) : cz.bm, dHx_j);
     }
     pre[0] = ex_m ? vx : n.ex;
     pre[1] = ey_m ? vy : n.ey;

@@ -122,9 +122,16 @@ static __device__ __noinline__ float3 e_slow(const StepParams* pp, int i, int j,
     const uint8_t* mat = p.mat;
     const int m0 = mat[n], mi = mat[n - 1], mj = mat[n - R], mk = mat[n - P];
     const int mij = mat[n - 1 - R], mik = mat[n - 1 - P], mjk = mat[n - R - P];
-    const Coef3 cx = e_coef(p, 0, m0 == mj && m0 == mk && m0 == mjk, m0, mj, mk, mjk, i, j, k);
-    const Coef3 cy = e_coef(p, 1, m0 == mi && m0 == mk && m0 == mik, m0, mi, mk, mik, i, j, k);
-    const Coef3 cz = e_coef(p, 2, m0 == mi && m0 == mj && m0 == mij, m0, mi, mj, mij, i, j, k);
+    Coef3 cx = e_coef(p, 0, m0 == mj && m0 == mk && m0 == mjk, m0, mj, mk, mjk, i, j, k);
+    Coef3 cy = e_coef(p, 1, m0 == mi && m0 == mk && m0 == mik, m0, mi, mk, mik, i, j, k);
+    Coef3 cz = e_coef(p, 2, m0 == mi && m0 == mj && m0 == mij, m0, mi, mj, mij, i, j, k);
+    if (plane_has_plate(p, k)) {
+        Coef3 pc[3];
+        const int hit = e_plate(&p, i, j, k, m0, mi, mj, mk, mij, mik, mjk, pc);
+        if (hit & 1) cx = pc[0];
+        if (hit & 2) cy = pc[1];
+        if (hit & 4) cz = pc[2];
+    }
     float3 r;
     r.x = upd3(cx.a, ex, cx.bp, dHz_j, cx.bm, dHy_k);
     r.y = upd3(cy.a, ey, cy.bp, dHx_k, cy.bm, dHz_i);
@@ -377,6 +384,7 @@ cudaError_t launch_fused(const FusedMaps& maps, const StepParams& p, const Field
                          const PsiSet& psi_in, const PsiSet& psi_out, long long m, const FusedWork& w, cudaStream_t st) {
     cudaError_t e = launch_shell(true, p, fi, fo, psi_in, psi_out, w.general, w.n_general, m, st);
     if (e == cudaSuccess) e = launch_design_e(p, fi, fo, psi_in, psi_out, m, st);
+    if (e == cudaSuccess) e = launch_plate_e(p, fi, fo, psi_in, psi_out, m, st);
     if (e != cudaSuccess) return e;
     if (w.n_interior > 0) k_sweep_interior<<<w.n_interior, NTH, SMEM_INTERIOR, st>>>(maps, p, fo, w.interior, m);
     e = cudaGetLastError();

@@ -27,6 +27,10 @@ cudaError_t launch_two_pass(const StepParams& p, const FieldPtrs& f, const PsiSe
 cudaError_t launch_design_e(const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
                             const PsiSet& pout, long long m, cudaStream_t st);
 
+// E of the plate nodes (StepParams::plate_nodes), fi/pin -> fo/pout, after a schedule's E kernels.
+cudaError_t launch_plate_e(const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
+                           const PsiSet& pout, long long m, cudaStream_t st);
+
 // Shell passes of the fused schedule (yee_two_pass.cu): E (e_pass) or H of the nodes of `items`,
 // reading fi / pin (buffer A) and writing fo / pout (buffer B).
 cudaError_t launch_shell(bool e_pass, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
@@ -78,6 +82,8 @@ cudaError_t launch_bg_curl(const DeviceGrid& g, const MatCoef* coef, int bg, con
 cudaError_t launch_fill(float* p, long long n, float v, cudaStream_t st);
 // Node classes (StepParams::cls) from the material index and the lumped edges.
 // design_box: the design region's cells or NULL (its edge box gets class kDesignNode).
+// Set the node class of the listed nodes ({i, j, k, -}) to `value`.
+cudaError_t launch_class_nodes(const DeviceGrid& g, const int4* nodes, int n, int value, uint8_t* cls, cudaStream_t st);
 cudaError_t launch_node_class(const DeviceGrid& g, const uint8_t* mat, const LumpedEdge* edges, int n_edges,
                               const int* design_box, uint8_t* cls, cudaStream_t st);
 cudaError_t launch_paint(uint8_t* mat, const DeviceGrid& g, const int box[6], uint8_t value, cudaStream_t st);

@@ -67,6 +67,24 @@ __global__ void __launch_bounds__(256) k_design_e(const __grid_constant__ StepPa
     e_node_global<true>(p, fi, fo, pin, pout, i, j, k, m);
 }
 
+// E of the nodes with a plate-covered edge (node class kPlateNode, which the other E kernels leave
+// alone): one thread per listed node, plate-aware coefficients.
+__global__ void __launch_bounds__(128) k_plate_e(const __grid_constant__ StepParams p, FieldPtrs fi, FieldPtrs fo,
+                                                 const __grid_constant__ PsiSet pin,
+                                                 const __grid_constant__ PsiSet pout, long long m) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= p.n_plate_nodes) return;
+    const int4 v = p.plate_nodes[q];
+    e_node_global<false, false, true>(p, fi, fo, pin, pout, v.x, v.y, v.z, m);
+}
+
+cudaError_t launch_plate_e(const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
+                           const PsiSet& pout, long long m, cudaStream_t st) {
+    if (p.n_plate_nodes <= 0) return cudaSuccess;
+    k_plate_e<<<(p.n_plate_nodes + 127) / 128, 128, 0, st>>>(p, fi, fo, pin, pout, m);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_design_e(const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
                             const PsiSet& pout, long long m, cudaStream_t st) {
     if (!p.deps) return cudaSuccess;
@@ -82,6 +100,7 @@ cudaError_t launch_two_pass(const StepParams& p, const FieldPtrs& f, const PsiSe
     dim3 grid((p.g.nx + 31) / 32, (p.g.ny + 7) / 8, p.g.nz);
     k_update_e<<<grid, block, 0, st>>>(p, f, ps, m);
     cudaError_t e = launch_design_e(p, f, f, ps, ps, m, st);
+    if (e == cudaSuccess) e = launch_plate_e(p, f, f, ps, ps, m, st);
     if (e != cudaSuccess) return e;
     k_update_h<<<grid, block, 0, st>>>(p, f, ps, m);
     return cudaGetLastError();

@@ -88,6 +88,14 @@ class Resistor:
 
 
 @dataclasses.dataclass
+class Plate:
+    axis: int                                 # normal axis: 0 x, 1 y, 2 z (plate at the box's low coordinate)
+    box: Tuple[int, int, int, int, int, int]  # is, js, ks, ie, je, ke (definePlateX / Y / Z)
+    sigma_1: float                            # sigma_e of the first tangential component (axis order)
+    sigma_2: float                            # sigma_e of the second
+
+
+@dataclasses.dataclass
 class Probe:
     component: int
     i: int
@@ -112,6 +120,7 @@ class Scenario:
     sources: List[LumpedSource] = dataclasses.field(default_factory=list)
     resistors: List[Resistor] = dataclasses.field(default_factory=list)
     probes: List[Probe] = dataclasses.field(default_factory=list)
+    plates: List[Plate] = dataclasses.field(default_factory=list)
     eps0: float = float(REF_EPS0)
     mu0: float = float(REF_MU0)
     pi: float = float(REF_PI)

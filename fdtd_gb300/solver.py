@@ -80,6 +80,7 @@ SIGNATURES = {
     "fdtd_set_design_region": (ctypes.c_int, [_vp, _pi32, ctypes.POINTER(Material), _pf]),
     "fdtd_adjoint_forward": (ctypes.c_int, [_vp, _i64, _i32, _i32, _i32, _i32, ctypes.POINTER(ctypes.c_double)]),
     "fdtd_adjoint_backward": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
+    "fdtd_add_plate": (ctypes.c_int, [_vp, _i32, _pi32, ctypes.c_float, ctypes.c_float]),
     "fdtd_add_port": (ctypes.c_int, [_vp, _i32, _pi32, _pi32, _pi32]),
     "fdtd_read_port": (ctypes.c_int, [_vp, _i32, _i64, _i64, _i32, _pf, _pf]),
     "fdtd_port_spectrum": (ctypes.c_int, [_vp, _i32, _i64, _i64, ctypes.c_float, ctypes.c_float, _pf, _pf, _pf, _pf]),
@@ -203,6 +204,10 @@ class Simulation:
         _check(_lib.fdtd_add_probe(self._h, component, i, j, k, ctypes.byref(out)))
         self.n_probes = out.value + 1
         return out.value
+
+    def add_plate(self, normal_axis: int, box: Sequence[int], sigma_1: float, sigma_2: float) -> None:
+        """Zero-thickness plate normal to ``normal_axis`` (fdtd_add_plate)."""
+        _check(_lib.fdtd_add_plate(self._h, normal_axis, _box(box), sigma_1, sigma_2))
 
     def add_port(self, voltage_box: Sequence[int], current_box: Sequence[int], axis: int = 2) -> int:
         """A z-directed port (voltage edges and current loop); returns its id."""
@@ -346,6 +351,8 @@ class Simulation:
             sim.add_source(s.box, s.resistance, s.waveform)
         for r in sc.resistors:
             sim.add_resistor(r.box, r.resistance)
+        for q in sc.plates:
+            sim.add_plate(q.axis, q.box, q.sigma_1, q.sigma_2)
         for p in sc.probes:
             sim.add_probe(p.component, p.i, p.j, p.k)
         if probe_capacity is not None:

@@ -94,6 +94,18 @@ int fdtd_add_lumped_source(fdtd_handle* h, int32_t axis, const int32_t box[6], f
 /* Lumped resistor on the same kind of edge box (defineResistor, fdtdrav.h:1429-1483). */
 int fdtd_add_resistor(fdtd_handle* h, int32_t axis, const int32_t box[6], float resistance);
 
+/* Zero-thickness conducting plate normal to `normal_axis` (0 x, 1 y, 2 z) at the box's low
+ * coordinate on that axis: the sigma_e of the E edges it covers becomes sigma_1 / sigma_2 for its
+ * two tangential components in axis order (x plate: y, z; y plate: x, z; z plate: x, y), after
+ * the edge averages and before the update coefficients, later plates overriding earlier ones.
+ * Covered edges, box = {is,js,ks,ie,je,ke}: x plate at i = is: Ey j in [js,je), k in [ks,ke];
+ * Ez j in [js,je], k in [ks,ke). y plate at j = js: Ez i in [is,ie], k in [ks,ke); Ex i in
+ * [is,ie), k in [ks,ke]. z plate at k = ks: Ex i in [is,ie), j in [js,je]; Ey i in [is,ie],
+ * j in [js,je). Replaces definePlateX / definePlateY / definePlateZ (fdtdrav.h:1574-1679,
+ * applied at fdtdrav.h:4162-4182). A plate may not cover the Ez edge of a lumped element, and
+ * handles with plates take no design region and join no batch. */
+int fdtd_add_plate(fdtd_handle* h, int32_t normal_axis, const int32_t box[6], float sigma_1, float sigma_2);
+
 /* Point probe of one field component at node (i,j,k): records, every step, the value right after
  * the component's main update and before its CPML correction, as sampleField does
  * (fdtdrav.h:234-246, called at 347, 372, 391, 740). Returns the probe's column in

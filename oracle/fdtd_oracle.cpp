@@ -66,6 +66,9 @@ typedef struct {
     // ((d5-d2), (d4-d1), (d3-d0) array, x fastest) instead of the material table
     int design_box[6];
     const double* design_eps;
+    // zero-thickness plates, applied in order: (nplate, 7) ints axis, is, js, ks, ie, je, ke and
+    // (nplate, 2) floats sigma_e of the two tangential components in axis order
+    int nplate; const int* plate; const float* plate_sig;
 } or_scenario;
 
 const char* or_error(void) { return g_err.c_str(); }
@@ -199,6 +202,28 @@ int setup(Sim<R>& s, const or_scenario* sc, const float* signal_per_node, int n_
                 if (j > 0) { size_t b = s.id(i, j - 1, k); s.mu_y[n] = harm(cmu[n], cmu[b]); s.sm_y[n] = harm(csm[n], csm[b]); }
                 if (k > 0) { size_t b = s.id(i, j, k - 1); s.mu_z[n] = harm(cmu[n], cmu[b]); s.sm_z[n] = harm(csm[n], csm[b]); }
             }
+    // definePlateX / Y / Z (fdtdrav.h:1574-1679, applied between the averages and setCoefficients,
+    // fdtdrav.h:4162-4182): each plate sets sigma_e of the edges its kernel's conditions select
+    for (int q = 0; q < sc->nplate; ++q) {
+        const int* pl = sc->plate + 7 * q;
+        const int axis = pl[0], is = pl[1], js = pl[2], ks = pl[3], ie = pl[4], je = pl[5], ke = pl[6];
+        const R sa = (R)sc->plate_sig[2 * q], sb = (R)sc->plate_sig[2 * q + 1];
+        for (int k = 0; k < NZ; ++k)
+            for (int j = 0; j < NY; ++j)
+                for (int i = 0; i < NX; ++i) {
+                    const size_t n = s.id(i, j, k);
+                    if (axis == 0) {
+                        if (i == is && j >= js && j < je && k >= ks && k <= ke) s.sig_y[n] = sa;
+                        if (i == is && j >= js && j <= je && k >= ks && k < ke) s.sig_z[n] = sb;
+                    } else if (axis == 1) {
+                        if (i >= is && i <= ie && j == js && k >= ks && k < ke) s.sig_z[n] = sb;
+                        if (i >= is && i < ie && j == js && k >= ks && k <= ke) s.sig_x[n] = sa;
+                    } else {
+                        if (i >= is && i < ie && j >= js && j <= je && k == ks) s.sig_x[n] = sa;
+                        if (i >= is && i <= ie && j >= js && j < je && k == ks) s.sig_y[n] = sb;
+                    }
+                }
+    }
     // setCoefficients with its masks
     const R dt = s.dt, dx = s.dx, dy = s.dy, dz = s.dz;
     for (int k = 0; k < NZ; ++k)

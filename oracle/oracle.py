@@ -40,7 +40,8 @@ class _Scenario(ctypes.Structure):
                 ("nres", _i), ("res_box", _pi), ("res_r", _pf),
                 ("nprobe", _i), ("probe", _pi),
                 ("profile_override", ctypes.POINTER(_pf)),
-                ("design_box", _i * 6), ("design_eps", ctypes.POINTER(ctypes.c_double))]
+                ("design_box", _i * 6), ("design_eps", ctypes.POINTER(ctypes.c_double)),
+                ("nplate", _i), ("plate", _pi), ("plate_sig", _pf)]
 
 
 def build(force: bool = False) -> str:
@@ -97,7 +98,11 @@ class _Prepared:
         rr = np.array([x.resistance for x in sc.resistors], dtype=np.float32)
         probes = sc.probes if probes is None else probes
         pr = np.array([[p.component, p.i, p.j, p.k] for p in probes], dtype=np.int32).reshape(-1, 4)
-        self.keep += [mat, tab, sb, sr, rb, rr, pr]
+        plates = getattr(sc, "plates", [])
+        pl = np.array([[q.axis, *q.box] for q in plates], dtype=np.int32).reshape(-1, 7)
+        ps = np.array([[q.sigma_1, q.sigma_2] for q in plates], dtype=np.float32).reshape(-1, 2)
+        self.keep += [mat, tab, sb, sr, rb, rr, pr, pl, ps]
+        s.nplate, s.plate, s.plate_sig = len(plates), pl.ctypes.data_as(_pi), ps.ctypes.data_as(_pf)
         s.mat, s.table, s.n_mat = mat.ctypes.data_as(_pu8), tab.ctypes.data_as(_pf), tab.shape[0]
         s.nsrc, s.src_box, s.src_r = len(sc.sources), sb.ctypes.data_as(_pi), sr.ctypes.data_as(_pf)
         s.nres, s.res_box, s.res_r = len(sc.resistors), rb.ctypes.data_as(_pi), rr.ctypes.data_as(_pf)

@@ -34,12 +34,13 @@ cudaLibrary_t g_lib = nullptr;
 
 struct Kern { const char* name; cudaKernel_t k; };
 enum { K_SETZERO, K_SETBRICK, K_SETSIGMA, K_SETCOEF, K_SETABCPML, K_SRCZ, K_RES, K_CALCE, K_CALCH,
-       K_VOLT, K_CURR, K_CORREC, K_ZIN, K_GATHER, K_COUNT };
+       K_VOLT, K_CURR, K_CORREC, K_PLATEX, K_PLATEY, K_PLATEZ, K_ZIN, K_GATHER, K_COUNT };
 Kern g_k[K_COUNT] = {
     {"_Z7setZero", nullptr}, {"_Z8setBrick", nullptr}, {"_Z18setSigmaEpsSigmaMu", nullptr},
     {"_Z15setCoefficients", nullptr}, {"_Z9setABCPML", nullptr}, {"_Z13defineSourceZ", nullptr},
     {"_Z14defineResistor", nullptr}, {"_Z6calc_e", nullptr}, {"_Z6calc_h", nullptr},
     {"_Z8voltMgpu", nullptr}, {"_Z8currMgpu", nullptr}, {"_Z7correcI", nullptr},
+    {"_Z12definePlateX", nullptr}, {"_Z12definePlateY", nullptr}, {"_Z12definePlateZ", nullptr},
     {"_Z8c_zinS11P6float2S0_iS0_S0_S0_S0_S_f", nullptr}, {"harness_gather", nullptr}};
 
 // Itanium-ABI names of the reference kernels: the parameter lists of fdtdrav.h reduce to runs of
@@ -151,6 +152,7 @@ typedef struct {
     int nbricks; const int* brick_box; const float* brick_mat;  // box is,js,ks,ie,je,ke; eps_r, sigma_e, mu_r, sigma_m
     int nsources; const int* src_box; const float* src_r;       // box is,js,ks,ie,je,ke
     int nres; const int* res_box; const float* res_r;
+    int nplates; const int* plate; const float* plate_sig;  // (n, 7): axis, box; (n, 2): sigma_e pair
 } rh_scenario;
 
 const char* rh_error(void) { return g_err.c_str(); }
@@ -172,6 +174,9 @@ int rh_load(const char* cubin_path) {
         "11i2p3f2i",                   // voltMgpu
         "11i4p3f2i",                   // currMgpu
         "1p1i",                        // correcI
+        "5i2p2f6i",                    // definePlateX
+        "5i2p2f6i",                    // definePlateY
+        "5i2p2f6i",                    // definePlateZ
         nullptr, nullptr};             // c_zinS11 (float2 parameters, full name above), gather
     for (int k = 0; k < K_COUNT; ++k) {
         std::string nm = (k < K_COUNT && specs[k]) ? mangled(g_k[k].name, specs[k]) : std::string(g_k[k].name);
@@ -271,6 +276,20 @@ int rh_setup(const rh_scenario* s) {
         std::vector<void*> a = {&NX, &NY, &NZ, &NZ_N, &off};
         for (int q = 0; q < 24; ++q) { P[q] = A(order[q]); a.push_back(&P[q]); }
         if (!launch(K_SETSIGMA, grid3d(), block3d(), a)) { free_all(); return -1; }
+    }
+    // definePlateX / Y / Z per plate, in order (fdtdrav.h:1574-1679, called at 4162-4182)
+    for (int q = 0; q < s->nplates; ++q) {
+        const int* pl = s->plate + 7 * q;
+        int is = pl[1], js = pl[2], ks = pl[3], ie = pl[4], je = pl[5], ke = pl[6];
+        float sa = s->plate_sig[2 * q], sb = s->plate_sig[2 * q + 1];
+        static float* P[2];
+        const int kid = pl[0] == 0 ? K_PLATEX : pl[0] == 1 ? K_PLATEY : K_PLATEZ;
+        if (pl[0] == 0) { P[0] = A("sigma_e_y"); P[1] = A("sigma_e_z"); }
+        else if (pl[0] == 1) { P[0] = A("sigma_e_x"); P[1] = A("sigma_e_z"); }
+        else { P[0] = A("sigma_e_x"); P[1] = A("sigma_e_y"); }
+        std::vector<void*> a = {&NX, &NY, &NZ, &NZ_N, &off, &P[0], &P[1], &sa, &sb,
+                                &is, &js, &ks, &ie, &je, &ke};
+        if (!launch(kid, grid3d(), block3d(), a)) { free_all(); return -1; }
     }
     // setCoefficients (fdtdrav.h:1223, called at 4213-4230)
     {

@@ -29,7 +29,8 @@ class _Scenario(ctypes.Structure):
                 ("dx", _f), ("dy", _f), ("dz", _f), ("dt", _f), ("eps0", _f), ("pi", _f), ("mu0", _f),
                 ("nbricks", _i), ("brick_box", _pi), ("brick_mat", _pf),
                 ("nsources", _i), ("src_box", _pi), ("src_r", _pf),
-                ("nres", _i), ("res_box", _pi), ("res_r", _pf)]
+                ("nres", _i), ("res_box", _pi), ("res_r", _pf),
+                ("nplates", _i), ("plate", _pi), ("plate_sig", _pf)]
 
 
 def available() -> bool:
@@ -78,8 +79,12 @@ class RefHarness:
         sr = np.array([x.resistance for x in sc.sources], dtype=np.float32)
         rb = np.array([x.box for x in sc.resistors], dtype=np.int32).reshape(-1, 6)
         rr = np.array([x.resistance for x in sc.resistors], dtype=np.float32)
-        self._keep = [np.ascontiguousarray(a) for a in (bb, bm, sb, sr, rb, rr)]
-        bb, bm, sb, sr, rb, rr = self._keep
+        plates = getattr(sc, "plates", [])
+        pl = np.array([[q.axis, *q.box] for q in plates], dtype=np.int32).reshape(-1, 7)
+        ps = np.array([[q.sigma_1, q.sigma_2] for q in plates], dtype=np.float32).reshape(-1, 2)
+        self._keep = [np.ascontiguousarray(a) for a in (bb, bm, sb, sr, rb, rr, pl, ps)]
+        bb, bm, sb, sr, rb, rr, pl, ps = self._keep
+        s.nplates, s.plate, s.plate_sig = len(plates), pl.ctypes.data_as(_pi), ps.ctypes.data_as(_pf)
         s.nbricks, s.brick_box, s.brick_mat = len(sc.bricks), bb.ctypes.data_as(_pi), bm.ctypes.data_as(_pf)
         s.nsources, s.src_box, s.src_r = len(sc.sources), sb.ctypes.data_as(_pi), sr.ctypes.data_as(_pf)
         s.nres, s.res_box, s.res_r = len(sc.resistors), rb.ctypes.data_as(_pi), rr.ctypes.data_as(_pf)

@@ -94,10 +94,34 @@ def port_scenario():
     return sc
 
 
+def plates_scenario():
+    """40x36x26 microstrip-like case: a substrate slab on a ground plate (reaching into the CPML),
+    a strip plate with a second plate overlapping it (the later one wins), an x- and a y-normal
+    plate, a lumped source and a resistor between ground and strip, 300 steps."""
+    steps = 300
+    sc = S.vacuum_cube(40, steps, pml=5, name="plates")
+    sc.nx, sc.ny, sc.nz = 40, 36, 26
+    sc.pml = (5, 6, 5, 6, 4, 5)
+    sc.materials.append(S.Material(eps_r=4.4, sigma_e=0.002))
+    sc.bricks.append(S.Brick((5, 6, 5, 35, 30, 9), len(sc.materials) - 1))
+    sc.plates = [S.Plate(2, (3, 3, 5, 37, 33, 5), 1e10, 1e10),
+                 S.Plate(2, (10, 14, 9, 30, 18, 9), 5.8e7, 5.8e7),
+                 S.Plate(2, (25, 15, 9, 33, 20, 9), 5e6, 3e6),
+                 S.Plate(0, (8, 10, 6, 8, 20, 12), 1e7, 2e7),
+                 S.Plate(1, (12, 25, 7, 24, 25, 13), 3e5, 4e5)]
+    sc.sources = [S.LumpedSource((12, 16, 5, 12, 16, 9), 50.0, S.gaussian_derivative(steps, sc.dt, 20e9, 1e-3))]
+    sc.resistors = [S.Resistor((28, 16, 5, 28, 16, 9), 50.0)]
+    sc.probes = [S.Probe(S.EZ, 20, 16, 7), S.Probe(S.EX, 18, 16, 10), S.Probe(S.EY, 20, 19, 9),
+                 S.Probe(S.HX, 20, 17, 8), S.Probe(S.HY, 15, 16, 9), S.Probe(S.EZ, 8, 12, 8),
+                 S.Probe(S.EX, 2, 10, 5), S.Probe(S.EZ, 16, 25, 9)]
+    return sc
+
+
 # voltage box: i, j closed, k half-open (voltMgpu case 3); current box: loop at plane ke - 1
 PORT_BOX = (14, 13, 9, 15, 14, 12)
 
 
 def fixture_scenarios():
     """(scenario, keep full fields?) for every run fixture."""
-    return [(vacuum64(), False), (small_vacuum(), True), (boxes_scenario(), True), (two_sources(), True)]
+    return [(vacuum64(), False), (small_vacuum(), True), (boxes_scenario(), True), (two_sources(), True),
+            (plates_scenario(), True)]

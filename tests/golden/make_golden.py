@@ -165,12 +165,16 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
     ap.add_argument("--analysis", default=None, help="also write large analysis-only dumps here")
-    ap.add_argument("--only", default=None, choices=["port"], help="write one fixture only")
+    ap.add_argument("--only", default=None, choices=["port", "plates"], help="write one fixture only")
     args = ap.parse_args()
     os.makedirs(args.out, exist_ok=True)
     if args.only == "port":
         np.savez_compressed(os.path.join(args.out, "port.npz"), **port_fixture())
         print("port fixture written to", args.out)
+        return
+    if args.only == "plates":
+        np.savez_compressed(os.path.join(args.out, "plates.npz"), **run_scenario(gs.plates_scenario(), True))
+        print("plates fixture written to", args.out)
         return
     np.savez_compressed(os.path.join(args.out, "port.npz"), **port_fixture())
     for sc, full in gs.fixture_scenarios():

@@ -1,11 +1,13 @@
 """GPU parity: the CUDA solver against the reference's own kernels (golden fixtures) and against
 the CPU oracle, through the C ABI."""
+import os
+
 import numpy as np
 import pytest
 
 import golden_scenarios as gs
 import oracle
-from conftest import REL_L2_TOL, bitwise_equal, golden, rel_l2, rel_l2_group
+from conftest import GOLDEN, REL_L2_TOL, bitwise_equal, golden, rel_l2, rel_l2_group
 from fdtd_gb300 import scenario as S
 
 pytestmark = pytest.mark.gpu
@@ -32,10 +34,12 @@ def scenarios():
 
 
 @pytest.mark.parametrize("schedule", SCHEDULES)
-@pytest.mark.parametrize("name", ["small_vacuum", "small_boxes", "vacuum64"])
+@pytest.mark.parametrize("name", ["small_vacuum", "small_boxes", "vacuum64", "plates"])
 def test_matches_reference_kernels_bitwise(gpu_lib, name, schedule):
     """Single-source scenarios: probe series and final fields equal the reference's bit for bit."""
     sc, full = scenarios()[name]
+    if not os.path.exists(os.path.join(GOLDEN, name + ".npz")):
+        pytest.skip("fixture not generated")
     fix = golden(name)
     p, f, _ = run_gpu(sc, schedule=schedule)
     assert bitwise_equal(p, fix["probes"]), rel_l2(p, fix["probes"])
