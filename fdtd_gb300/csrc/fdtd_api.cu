@@ -55,13 +55,15 @@ struct PlateDef {
     float sigma[2];
 };
 
-// A z-directed port: the point probes of its voltage edges (k outer, then j, then i, as voltMgpu
-// sums them) followed by its current loop at plane ke - 1 of the current box: Hx at j = js - 1
-// (i = is..ie), Hx at j = je, Hy at i = ie (j = js..je), Hy at i = is - 1.
+// A port: the point probes of its voltage edges (Ez, k outer, then j, then i, as voltMgpu sums
+// them), then four groups of H probes s1..s4 of its current loop; I = a1 s1 + a2 s2 - a1 s3 - a2 s4
+// (currMgpu, the groups and cell sizes per direction in port_groups).
 struct PortDef {
     int vbox[6], ibox[6];
+    int current_axis;
     int first;  // probe id of the first voltage edge
-    int n_v, n_x, n_y;
+    int n_v;
+    int n[4];   // probes of s1..s4
 };
 
 }  // namespace
@@ -314,10 +316,15 @@ int ensure_fused(fdtd_handle* h) {
 }
 
 // AUTO takes the two-pass schedule: on GB300 it is faster than the fused schedule on the random-box
-// workloads measured (512^3 random boxes with 10-cell CPML: 53.1 against 47.2 Gcell/s).
+// workload with sources and probes (512^3, 64 boxes, 10-cell CPML: 49.3 against 47.2 Gcell/s).
 bool use_fused(const fdtd_handle* h) { return h->schedule == FDTD_SCHEDULE_FUSED; }
 
 }  // namespace
+
+namespace fdtd {
+// The calling thread's error message for entry points defined in other translation units.
+int report_error(int code, const char* msg) { return fail(code, msg); }
+}  // namespace fdtd
 
 extern "C" {
 
@@ -1569,11 +1576,45 @@ extern "C" int fdtd_batch_tune(fdtd_batch* b, int64_t steps, double* best_ms) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// Port voltage and current (voltMgpu, currMgpu, fdtdrav.h:2185-2488), z direction.
+// Port voltage and current (voltMgpu, currMgpu, fdtdrav.h:2185-2488).
 // ---------------------------------------------------------------------------------------------
-extern "C" int fdtd_add_port(fdtd_handle* h, int32_t axis, const int32_t vbox[6], const int32_t ibox[6], int32_t* id_out) {
+namespace {
+
+// The current loop of currMgpu for direction `axis` (0 x, 1 y, 2 z; cases 1, 2, 3 of
+// fdtdrav.h:2318-2480) on the current box c, as four groups of H probes in summation order, and
+// the cell sizes a1, a2 of I = a1 s1 + a2 s2 - a1 s3 - a2 s4.
+//   x: s1 Hy(ie-1, j, ks-1), s2 Hz(ie-1, je, k), s3 Hy(ie-1, j, ke), s4 Hz(ie-1, js-1, k); a1 dy, a2 dz
+//   y: s1 Hz(is-1, je-1, k), s2 Hx(i, je-1, ke), s3 Hz(ie, je-1, k), s4 Hx(i, je-1, ks-1); a1 dz, a2 dx
+//   z: s1 Hy(ie, j, ke-1), s2 Hx(i, js-1, ke-1), s3 Hy(is-1, j, ke-1), s4 Hx(i, je, ke-1); a1 dy, a2 dx
+// with i in [is, ie], j in [js, je], k in [ks, ke].
+void port_groups(int axis, const int* c, std::vector<Probe> g[4]) {
+    for (int q = 0; q < 4; ++q) g[q].clear();
+    if (axis == 0) {
+        for (int j = c[1]; j <= c[4]; ++j) g[0].push_back(Probe{FDTD_HY, c[3] - 1, j, c[2] - 1});
+        for (int k = c[2]; k <= c[5]; ++k) g[1].push_back(Probe{FDTD_HZ, c[3] - 1, c[4], k});
+        for (int j = c[1]; j <= c[4]; ++j) g[2].push_back(Probe{FDTD_HY, c[3] - 1, j, c[5]});
+        for (int k = c[2]; k <= c[5]; ++k) g[3].push_back(Probe{FDTD_HZ, c[3] - 1, c[1] - 1, k});
+    } else if (axis == 1) {
+        for (int k = c[2]; k <= c[5]; ++k) g[0].push_back(Probe{FDTD_HZ, c[0] - 1, c[4] - 1, k});
+        for (int i = c[0]; i <= c[3]; ++i) g[1].push_back(Probe{FDTD_HX, i, c[4] - 1, c[5]});
+        for (int k = c[2]; k <= c[5]; ++k) g[2].push_back(Probe{FDTD_HZ, c[3], c[4] - 1, k});
+        for (int i = c[0]; i <= c[3]; ++i) g[3].push_back(Probe{FDTD_HX, i, c[4] - 1, c[2] - 1});
+    } else {
+        const int kc = c[5] - 1;
+        for (int j = c[1]; j <= c[4]; ++j) g[0].push_back(Probe{FDTD_HY, c[3], j, kc});
+        for (int i = c[0]; i <= c[3]; ++i) g[1].push_back(Probe{FDTD_HX, i, c[1] - 1, kc});
+        for (int j = c[1]; j <= c[4]; ++j) g[2].push_back(Probe{FDTD_HY, c[0] - 1, j, kc});
+        for (int i = c[0]; i <= c[3]; ++i) g[3].push_back(Probe{FDTD_HX, i, c[4], kc});
+    }
+}
+
+}  // namespace
+
+extern "C" int fdtd_add_port(fdtd_handle* h, int32_t voltage_axis, const int32_t vbox[6], int32_t current_axis,
+                             const int32_t ibox[6], int32_t* id_out) {
     if (!h || !vbox || !ibox) return fail(FDTD_ERR_INVALID, "NULL argument");
-    if (axis != 2) return fail(FDTD_ERR_INVALID, "only z-directed ports (axis 2) are supported");
+    if (voltage_axis != 2) return fail(FDTD_ERR_INVALID, "only z-directed port voltages (axis 2) are supported");
+    if (current_axis < 0 || current_axis > 2) return fail(FDTD_ERR_INVALID, "current axis must be 0, 1 or 2");
     if (h->step > 0) return fail(FDTD_ERR_STATE, "ports must be added before the first step");
     const DeviceGrid& g = h->g;
     const int* v = vbox;
@@ -1581,23 +1622,27 @@ extern "C" int fdtd_add_port(fdtd_handle* h, int32_t axis, const int32_t vbox[6]
     if (v[0] < 0 || v[3] >= g.nx || v[0] > v[3] || v[1] < 0 || v[4] >= g.ny || v[1] > v[4] || v[2] < 0 || v[5] > g.nz ||
         v[2] >= v[5])
         return fail(FDTD_ERR_INVALID, "voltage box outside the grid or empty (k range is half-open)");
-    if (c[0] < 1 || c[3] >= g.nx || c[0] > c[3] || c[1] < 1 || c[4] >= g.ny || c[1] > c[4] || c[5] < 1 || c[5] > g.nz)
-        return fail(FDTD_ERR_INVALID, "current box must leave one node on its low x / y sides inside the grid");
+    if (c[0] > c[3] || c[1] > c[4] || c[2] > c[5] || (current_axis == 2 && c[5] < 1))
+        return fail(FDTD_ERR_INVALID, "current box empty or reversed");
+    std::vector<Probe> grp[4];
+    port_groups(current_axis, c, grp);
+    for (int q = 0; q < 4; ++q)
+        for (const Probe& pr : grp[q])
+            if (pr.i < 0 || pr.i >= g.nx || pr.j < 0 || pr.j >= g.ny || pr.k < 0 || pr.k >= g.nz)
+                return fail(FDTD_ERR_INVALID, "the current loop of the box leaves the grid");
     PortDef P{};
     std::copy(v, v + 6, P.vbox);
     std::copy(c, c + 6, P.ibox);
+    P.current_axis = current_axis;
     P.first = (int)h->probes.size();
     for (int k = v[2]; k < v[5]; ++k)
         for (int j = v[1]; j <= v[4]; ++j)
             for (int i = v[0]; i <= v[3]; ++i) h->probes.push_back(Probe{FDTD_EZ, i, j, k});
     P.n_v = (int)h->probes.size() - P.first;
-    const int kc = c[5] - 1;
-    for (int i = c[0]; i <= c[3]; ++i) h->probes.push_back(Probe{FDTD_HX, i, c[1] - 1, kc});
-    for (int i = c[0]; i <= c[3]; ++i) h->probes.push_back(Probe{FDTD_HX, i, c[4], kc});
-    P.n_x = c[3] - c[0] + 1;
-    for (int j = c[1]; j <= c[4]; ++j) h->probes.push_back(Probe{FDTD_HY, c[3], j, kc});
-    for (int j = c[1]; j <= c[4]; ++j) h->probes.push_back(Probe{FDTD_HY, c[0] - 1, j, kc});
-    P.n_y = c[4] - c[1] + 1;
+    for (int q = 0; q < 4; ++q) {
+        h->probes.insert(h->probes.end(), grp[q].begin(), grp[q].end());
+        P.n[q] = (int)grp[q].size();
+    }
     h->ports.push_back(P);
     h->dirty_probes = true;
     if (id_out) *id_out = (int32_t)h->ports.size() - 1;
@@ -1615,6 +1660,7 @@ extern "C" int fdtd_read_port(fdtd_handle* h, int32_t id, int64_t first, int64_t
     if (rc) return rc;
     const PortDef& P = h->ports[id];
     const float dx = h->g.dx, dy = h->g.dy, dz = h->g.dz;
+    const float a1 = P.current_axis == 1 ? dz : dy, a2 = P.current_axis == 0 ? dz : dx;
     // voltMgpu case 3: csuf = -dz / ((ie - is + 1) (je - js + 1)) with float box bounds
     const float is = (float)P.vbox[0], js = (float)P.vbox[1], ie = (float)P.vbox[3], je = (float)P.vbox[4];
     const float csuf = (-dz) / ((ie - is + 1) * (je - js + 1));
@@ -1623,15 +1669,19 @@ extern "C" int fdtd_read_port(fdtd_handle* h, int32_t id, int64_t first, int64_t
         float volt = 0.f;
         for (int q = 0; q < P.n_v; ++q) volt = volt + r[q];
         voltage[t] = volt * csuf;
-        const float* hx = r + P.n_v;
-        const float* hy = hx + 2 * P.n_x;
-        float xp = 0.f, xn = 0.f, yp = 0.f, yn = 0.f;
-        for (int q = 0; q < P.n_x; ++q) { xp = xp + hx[q]; xn = xn + hx[P.n_x + q]; }
-        for (int q = 0; q < P.n_y; ++q) { yp = yp + hy[q]; yn = yn + hy[P.n_y + q]; }
-        // currMgpu case 3: the Ampere loop around the z edges, dy*yp + dx*xp - dy*yn - dx*xn as the
-        // reference's compiled expression contracts it (dx*xp fused with dy*yp as the addend, then
-        // the two subtractions as FMAs)
-        current[t] = std::fmaf(-dx, xn, std::fmaf(-dy, yn, std::fmaf(dx, xp, dy * yp)));
+        const float* h4 = r + P.n_v;
+        float sum[4];
+        for (int q = 0; q < 4; ++q) {
+            float acc = 0.f;
+            for (int e = 0; e < P.n[q]; ++e) acc = acc + h4[e];
+            sum[q] = acc;
+            h4 += P.n[q];
+        }
+        // a1 s1 + a2 s2 - a1 s3 - a2 s4 as the reference's compiled expressions contract it: one
+        // product fused with the other as the addend (the first fused in the x loop, the second in
+        // the y and z loops), then the two subtractions as FMAs
+        const float lead = P.current_axis == 0 ? std::fmaf(a1, sum[0], a2 * sum[1]) : std::fmaf(a2, sum[1], a1 * sum[0]);
+        current[t] = std::fmaf(-a2, sum[3], std::fmaf(-a1, sum[2], lead));
     }
     if (time_average && n > 1) {
         // correcI averages in place, one thread per step: I(t) = (I(t) + I(t+1)) / 2 from the

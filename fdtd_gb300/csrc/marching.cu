@@ -1,0 +1,157 @@
+// Whole-run entry point with marchingLoop's parameter list (fdtdrav.h:3425-4387), and the source
+// waveforms of setGauss / setSine (fdtdrav.h:1486-1520).
+//
+// fdtd_marching_loop is what the reference's driver (source.cu) calls, rebuilt on the C ABI: the
+// metre-to-index conversion and grid sizes of marchingLoop, bricks, PEC plates, the lumped source
+// and resistor, the voltage / current sample boxes as a port, the time loop, and calcVoltCurrent's
+// V(t) / I(t), returned in host arrays instead of the reference's result files.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <vector>
+
+#include "fdtd_api.h"
+
+namespace fdtd {
+int report_error(int code, const char* msg);
+}
+using fdtd::report_error;
+
+namespace {
+
+// Source waveforms as the reference's kernels evaluate them, on the device so that expf / sinf
+// are CUDA's: type 1 Gaussian amp * exp(-((m dt - t0)^2) / tau^2), type 3 sine
+// amp * sin(2 pi f dt m), type 2 none (zero).
+__global__ void k_source_waveform(int type, float amp, float freq, float dt, float t_0, float tau, float pi, int n,
+                                  float* out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    float v = 0.f;
+    if (type == 1) v = amp * expf((-(((t * dt) - t_0) * ((t * dt) - t_0)) / (tau * tau)));
+    else if (type == 3) v = amp * sinf(2 * pi * freq * dt * t);
+    out[t] = v;
+}
+
+// calc_index (fdtdrav.h:198-206): metres to a node index, rounded half away from zero, in float.
+int calc_index(float coordinate, float dxyz) { return (int)std::round((coordinate - 0) / dxyz); }
+
+struct HandleGuard {
+    fdtd_handle* h = nullptr;
+    ~HandleGuard() {
+        if (h) fdtd_destroy(h);
+    }
+};
+
+}  // namespace
+
+extern "C" int fdtd_source_waveform(int32_t type, float amp, float freq, float dt, float t_0, float tau, float pi,
+                                    int64_t n, float* out) {
+    if (!out || n < 1 || n > (1LL << 30)) return report_error(FDTD_ERR_INVALID, "NULL output or n outside 1 .. 2^30");
+    if (type < 1 || type > 3) return report_error(FDTD_ERR_INVALID, "waveform type must be 1 (Gaussian), 2 (none) or 3 (sine)");
+    float* d = nullptr;
+    if (cudaMalloc(&d, (size_t)n * sizeof(float)) != cudaSuccess) return report_error(FDTD_ERR_OOM, "waveform buffer");
+    k_source_waveform<<<(unsigned)((n + 255) / 256), 256>>>(type, amp, freq, dt, t_0, tau, pi, (int)n, d);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(out, d, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e == cudaSuccess ? FDTD_OK : report_error(FDTD_ERR_CUDA, cudaGetErrorString(e));
+}
+
+extern "C" int fdtd_marching_loop(
+    const int NUMDEV, float eps_0, float pi, float mu_0, float c, float dx, float dy, float dz, float dt, int X, int Y,
+    int Z, int n_t_steps, int pml_x_n, int pml_y_n, int pml_z_n, int pml_x_p, int pml_y_p, int pml_z_p, int air_buff_x_n,
+    int air_buff_y_n, int air_buff_z_n, int air_buff_x_p, int air_buff_y_p, int air_buff_z_p, int source_tp,
+    float source_freq, float source_amp, float source_min_x, float source_min_y, float source_min_z, float source_max_x,
+    float source_max_y, float source_max_z, int source_direction, float rs, float nc, float tau, float t_0,
+    const float* brick_min_x, const float* brick_min_y, const float* brick_min_z, const float* brick_max_x,
+    const float* brick_max_y, const float* brick_max_z, const float* brick_sigma_e_x, const float* brick_sigma_e_y,
+    const float* brick_sigma_e_z, const float* brick_eps_r_x, const float* brick_eps_r_y, const float* brick_eps_r_z,
+    const float* brick_sigma_m_x, const float* brick_sigma_m_y, const float* brick_sigma_m_z, const float* brick_mu_r_x,
+    const float* brick_mu_r_y, const float* brick_mu_r_z, int brick_opt, int brick_num, const float* pec_min_x,
+    const float* pec_min_y, const float* pec_min_z, const float* pec_max_x, const float* pec_max_y,
+    const float* pec_max_z, const float* pec_sigma_e_x, const float* pec_sigma_e_y, const float* pec_sigma_e_z,
+    int pec_opt, int pec_num, float resistor_min_x, float resistor_min_y, float resistor_min_z, float resistor_max_x,
+    float resistor_max_y, float resistor_max_z, float resistor_resist, int resistor_direction, int resistor_opt,
+    float sampled_voltage_min_x, float sampled_voltage_min_y, float sampled_voltage_min_z, float sampled_voltage_max_x,
+    float sampled_voltage_max_y, float sampled_voltage_max_z, int voltage_direction, float sampled_current_min_x,
+    float sampled_current_min_y, float sampled_current_min_z, float sampled_current_max_x, float sampled_current_max_y,
+    float sampled_current_max_z, int current_direction, float* voltage, float* current) {
+    (void)c;
+    (void)nc;
+    (void)pec_sigma_e_z;         // a z plate has no z edges (definePlateZ takes x and y only)
+    (void)resistor_direction;    // defineResistor always acts on z edges (fdtdrav.h:1429-1483)
+    if (!voltage || !current || n_t_steps < 2 || NUMDEV < 1)
+        return report_error(FDTD_ERR_INVALID, "NULL output, fewer than 2 steps or NUMDEV < 1");
+    if (source_direction != 3 || voltage_direction != 3 || current_direction < 1 || current_direction > 3)
+        return report_error(FDTD_ERR_INVALID, "z-directed source and voltage only (direction 3); current direction 1, 2 or 3");
+    // domain size (fdtdrav.h:3485-3503); NZ is rounded up to a multiple of NUMDEV as the reference
+    // does, then the whole domain runs on one GPU
+    const int NXX = X + air_buff_x_n + air_buff_x_p + pml_x_n + pml_x_p;
+    const int NYY = Y + air_buff_y_n + air_buff_y_p + pml_y_n + pml_y_p;
+    int NZ = Z + air_buff_z_n + air_buff_z_p + pml_z_n + pml_z_p;
+    NZ = (NZ % NUMDEV == 0) ? NZ : (NZ / NUMDEV + 1) * NUMDEV;
+    const int ox = air_buff_x_n + pml_x_n, oy = air_buff_y_n + pml_y_n, oz = air_buff_z_n + pml_z_n;
+    auto box = [&](float x0, float y0, float z0, float x1, float y1, float z1, int32_t* b) {
+        b[0] = ox + calc_index(x0, dx); b[1] = oy + calc_index(y0, dy); b[2] = oz + calc_index(z0, dz);
+        b[3] = ox + calc_index(x1, dx); b[4] = oy + calc_index(y1, dy); b[5] = oz + calc_index(z1, dz);
+    };
+    fdtd_grid g{};
+    g.nx = NXX; g.ny = NYY; g.nz = NZ;
+    g.dx = dx; g.dy = dy; g.dz = dz; g.dt = dt;
+    g.eps0 = eps_0; g.mu0 = mu_0; g.pi = pi;
+    g.pml[0] = pml_x_n; g.pml[1] = pml_x_p; g.pml[2] = pml_y_n; g.pml[3] = pml_y_p; g.pml[4] = pml_z_n; g.pml[5] = pml_z_p;
+    HandleGuard hg;
+    int rc = fdtd_create(&g, &hg.h);
+    if (rc) return rc;
+    fdtd_handle* h = hg.h;
+    // bricks in order (setBrick, fdtdrav.h:4104-4128); material 0 is the background
+    const int nb = brick_opt != 0 ? brick_num : 0;
+    std::vector<fdtd_material> mats(1 + nb);
+    mats[0] = fdtd_material{1.0f, 1.2e-38f, 1.0f, 1.2e-38f};
+    for (int b = 0; b < nb; ++b) {
+        if (brick_eps_r_y[b] != brick_eps_r_x[b] || brick_eps_r_z[b] != brick_eps_r_x[b] ||
+            brick_sigma_e_y[b] != brick_sigma_e_x[b] || brick_sigma_e_z[b] != brick_sigma_e_x[b] ||
+            brick_mu_r_y[b] != brick_mu_r_x[b] || brick_mu_r_z[b] != brick_mu_r_x[b] ||
+            brick_sigma_m_y[b] != brick_sigma_m_x[b] || brick_sigma_m_z[b] != brick_sigma_m_x[b])
+            return report_error(FDTD_ERR_INVALID, "per-axis (anisotropic) brick materials are not supported");
+        mats[1 + b] = fdtd_material{brick_eps_r_x[b], brick_sigma_e_x[b], brick_mu_r_x[b], brick_sigma_m_x[b]};
+    }
+    if ((rc = fdtd_set_materials(h, mats.data(), (int32_t)mats.size()))) return rc;
+    for (int b = 0; b < nb; ++b) {
+        int32_t bx[6];
+        box(brick_min_x[b], brick_min_y[b], brick_min_z[b], brick_max_x[b], brick_max_y[b], brick_max_z[b], bx);
+        if ((rc = fdtd_add_brick(h, bx, 1 + b))) return rc;
+    }
+    // PEC plates: definePlateZ per plate (fdtdrav.h:4162-4182)
+    const int np = pec_opt != 0 ? pec_num : 0;
+    for (int q = 0; q < np; ++q) {
+        int32_t bx[6];
+        box(pec_min_x[q], pec_min_y[q], pec_min_z[q], pec_max_x[q], pec_max_y[q], pec_max_z[q], bx);
+        if ((rc = fdtd_add_plate(h, 2, bx, pec_sigma_e_x[q], pec_sigma_e_y[q]))) return rc;
+    }
+    // the lumped source with its waveform (setGauss / setSine, defineSourceZ)
+    int32_t sb[6];
+    box(source_min_x, source_min_y, source_min_z, source_max_x, source_max_y, source_max_z, sb);
+    std::vector<float> wave(n_t_steps, 0.f);
+    if (source_tp == 1 || source_tp == 3) {
+        if ((rc = fdtd_source_waveform(source_tp, source_amp, source_freq, dt, t_0, tau, pi, n_t_steps, wave.data())))
+            return rc;
+    }
+    if ((rc = fdtd_add_lumped_source(h, 2, sb, rs, wave.data(), n_t_steps, nullptr))) return rc;
+    if (resistor_opt != 0) {
+        int32_t rb[6];
+        box(resistor_min_x, resistor_min_y, resistor_min_z, resistor_max_x, resistor_max_y, resistor_max_z, rb);
+        if ((rc = fdtd_add_resistor(h, 2, rb, resistor_resist))) return rc;
+    }
+    int32_t vb[6], cb[6], port = -1;
+    box(sampled_voltage_min_x, sampled_voltage_min_y, sampled_voltage_min_z, sampled_voltage_max_x,
+        sampled_voltage_max_y, sampled_voltage_max_z, vb);
+    box(sampled_current_min_x, sampled_current_min_y, sampled_current_min_z, sampled_current_max_x,
+        sampled_current_max_y, sampled_current_max_z, cb);
+    if ((rc = fdtd_add_port(h, 2, vb, current_direction - 1, cb, &port))) return rc;
+    if ((rc = fdtd_set_probe_capacity(h, n_t_steps))) return rc;
+    // the time loop (fdtdrav.h:4320-4355) and calcVoltCurrent (fdtdrav.h:3129-3186)
+    if ((rc = fdtd_step(h, n_t_steps))) return rc;
+    if ((rc = fdtd_synchronize(h))) return rc;
+    return fdtd_read_port(h, port, 0, n_t_steps, 1, voltage, current);
+}

@@ -322,3 +322,84 @@ def batch_instances(n: int = 256, size=(32, 96), steps: int = 2000, pml: int = 8
         out.append(Scenario(f"batch{q}", dims[0], dims[1], dims[2], delta, delta, delta, float(dt), (pml,) * 6, steps,
                             mats, bricks, [src], [], [Probe(EZ, pi_, pj, pk)], seed=seed))
     return out
+
+
+# ---------------------------------------------------------------------------------------------
+# marchingLoop's parameter list (fdtdrav.h:3425-3453) and its metre-to-index set-up
+# ---------------------------------------------------------------------------------------------
+_BRICK_ARRAYS = ["brick_min_x", "brick_min_y", "brick_min_z", "brick_max_x", "brick_max_y", "brick_max_z",
+                 "brick_sigma_e_x", "brick_sigma_e_y", "brick_sigma_e_z", "brick_eps_r_x", "brick_eps_r_y",
+                 "brick_eps_r_z", "brick_sigma_m_x", "brick_sigma_m_y", "brick_sigma_m_z", "brick_mu_r_x",
+                 "brick_mu_r_y", "brick_mu_r_z"]
+_PEC_ARRAYS = ["pec_min_x", "pec_min_y", "pec_min_z", "pec_max_x", "pec_max_y", "pec_max_z",
+               "pec_sigma_e_x", "pec_sigma_e_y", "pec_sigma_e_z"]
+# (name, kind): i int, f float, a float array; in the order of the reference's signature
+MARCHING_PARAMS = (
+    [("NUMDEV", "i"), ("eps_0", "f"), ("pi", "f"), ("mu_0", "f"), ("c", "f"), ("dx", "f"), ("dy", "f"), ("dz", "f"),
+     ("dt", "f"), ("X", "i"), ("Y", "i"), ("Z", "i"), ("n_t_steps", "i")]
+    + [(n, "i") for n in ("pml_x_n", "pml_y_n", "pml_z_n", "pml_x_p", "pml_y_p", "pml_z_p",
+                          "air_buff_x_n", "air_buff_y_n", "air_buff_z_n", "air_buff_x_p", "air_buff_y_p", "air_buff_z_p")]
+    + [("source_tp", "i"), ("source_freq", "f"), ("source_amp", "f")]
+    + [(n, "f") for n in ("source_min_x", "source_min_y", "source_min_z", "source_max_x", "source_max_y", "source_max_z")]
+    + [("source_direction", "i"), ("rs", "f"), ("nc", "f"), ("tau", "f"), ("t_0", "f")]
+    + [(n, "a") for n in _BRICK_ARRAYS] + [("brick_opt", "i"), ("brick_num", "i")]
+    + [(n, "a") for n in _PEC_ARRAYS] + [("pec_opt", "i"), ("pec_num", "i")]
+    + [(n, "f") for n in ("resistor_min_x", "resistor_min_y", "resistor_min_z", "resistor_max_x", "resistor_max_y",
+                          "resistor_max_z", "resistor_resist")]
+    + [("resistor_direction", "i"), ("resistor_opt", "i")]
+    + [(n, "f") for n in ("sampled_voltage_min_x", "sampled_voltage_min_y", "sampled_voltage_min_z",
+                          "sampled_voltage_max_x", "sampled_voltage_max_y", "sampled_voltage_max_z")]
+    + [("voltage_direction", "i")]
+    + [(n, "f") for n in ("sampled_current_min_x", "sampled_current_min_y", "sampled_current_min_z",
+                          "sampled_current_max_x", "sampled_current_max_y", "sampled_current_max_z")]
+    + [("current_direction", "i")])
+
+
+def marching_indices(a: dict) -> dict:
+    """Grid size and index boxes of marchingLoop (fdtdrav.h:3485-3653) for parameters ``a`` (names
+    of MARCHING_PARAMS): node counts nx, ny, nz (nz rounded up to a multiple of NUMDEV) and the
+    boxes of bricks, plates, source, resistor, voltage and current samples."""
+    f32 = np.float32
+    nx = a["X"] + a["air_buff_x_n"] + a["air_buff_x_p"] + a["pml_x_n"] + a["pml_x_p"]
+    ny = a["Y"] + a["air_buff_y_n"] + a["air_buff_y_p"] + a["pml_y_n"] + a["pml_y_p"]
+    nz = a["Z"] + a["air_buff_z_n"] + a["air_buff_z_p"] + a["pml_z_n"] + a["pml_z_p"]
+    nd = a["NUMDEV"]
+    nz = nz if nz % nd == 0 else (nz // nd + 1) * nd
+    o = (a["air_buff_x_n"] + a["pml_x_n"], a["air_buff_y_n"] + a["pml_y_n"], a["air_buff_z_n"] + a["pml_z_n"])
+    d = (f32(a["dx"]), f32(a["dy"]), f32(a["dz"]))
+
+    def box(lo, hi):
+        return tuple([o[q] + calc_index(lo[q], d[q]) for q in range(3)] + [o[q] + calc_index(hi[q], d[q]) for q in range(3)])
+
+    def named(prefix, q=None):
+        g = (lambda n: a[n][q]) if q is not None else (lambda n: a[n])
+        return box([g(prefix + "_min_" + c) for c in "xyz"], [g(prefix + "_max_" + c) for c in "xyz"])
+
+    out = {"nx": nx, "ny": ny, "nz": nz,
+           "bricks": [named("brick", q) for q in range(a["brick_num"] if a["brick_opt"] else 0)],
+           "pecs": [named("pec", q) for q in range(a["pec_num"] if a["pec_opt"] else 0)],
+           "source": named("source"), "resistor": named("resistor") if a["resistor_opt"] else None,
+           "voltage": named("sampled_voltage"), "current": named("sampled_current")}
+    return out
+
+
+def marching_scenario(a: dict, waveform: np.ndarray) -> Tuple[Scenario, Tuple[int, ...], Tuple[int, ...]]:
+    """The scenario marchingLoop builds from ``a`` (isotropic bricks, z plates, z source and
+    resistor), with the source voltage ``waveform``; returns it with the voltage and current boxes."""
+    ix = marching_indices(a)
+    mats = [Material()]
+    bricks = []
+    for q, b in enumerate(ix["bricks"]):
+        mats.append(Material(eps_r=float(a["brick_eps_r_x"][q]), sigma_e=float(a["brick_sigma_e_x"][q]),
+                             mu_r=float(a["brick_mu_r_x"][q]), sigma_m=float(a["brick_sigma_m_x"][q])))
+        bricks.append(Brick(b, q + 1))
+    sc = Scenario(name="marching", nx=ix["nx"], ny=ix["ny"], nz=ix["nz"], dx=float(a["dx"]), dy=float(a["dy"]),
+                  dz=float(a["dz"]), dt=float(a["dt"]),
+                  pml=(a["pml_x_n"], a["pml_x_p"], a["pml_y_n"], a["pml_y_p"], a["pml_z_n"], a["pml_z_p"]),
+                  steps=a["n_t_steps"], materials=mats, bricks=bricks, eps0=float(a["eps_0"]), mu0=float(a["mu_0"]),
+                  pi=float(a["pi"]))
+    sc.plates = [Plate(2, b, float(a["pec_sigma_e_x"][q]), float(a["pec_sigma_e_y"][q])) for q, b in enumerate(ix["pecs"])]
+    sc.sources = [LumpedSource(ix["source"], float(a["rs"]), np.asarray(waveform, dtype=np.float32))]
+    if ix["resistor"] is not None:
+        sc.resistors = [Resistor(ix["resistor"], float(a["resistor_resist"]))]
+    return sc, ix["voltage"], ix["current"]

@@ -81,10 +81,14 @@ SIGNATURES = {
     "fdtd_adjoint_forward": (ctypes.c_int, [_vp, _i64, _i32, _i32, _i32, _i32, ctypes.POINTER(ctypes.c_double)]),
     "fdtd_adjoint_backward": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
     "fdtd_add_plate": (ctypes.c_int, [_vp, _i32, _pi32, ctypes.c_float, ctypes.c_float]),
-    "fdtd_add_port": (ctypes.c_int, [_vp, _i32, _pi32, _pi32, _pi32]),
+    "fdtd_add_port": (ctypes.c_int, [_vp, _i32, _pi32, _i32, _pi32, _pi32]),
     "fdtd_read_port": (ctypes.c_int, [_vp, _i32, _i64, _i64, _i32, _pf, _pf]),
     "fdtd_port_spectrum": (ctypes.c_int, [_vp, _i32, _i64, _i64, ctypes.c_float, ctypes.c_float, _pf, _pf, _pf, _pf]),
     "fdtd_port_zin": (ctypes.c_int, [_i64, _pf, _pf, ctypes.c_float, ctypes.c_float, _pf, _pf]),
+    "fdtd_source_waveform": (ctypes.c_int, [_i32, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                            ctypes.c_float, ctypes.c_float, _i64, _pf]),
+    "fdtd_marching_loop": (ctypes.c_int, [{"i": ctypes.c_int, "f": ctypes.c_float, "a": _pf}[k]
+                                          for _, k in S.MARCHING_PARAMS] + [_pf, _pf]),
     "fdtd_batch_create": (ctypes.c_int, [ctypes.POINTER(_vp), _i32, ctypes.POINTER(_vp)]),
     "fdtd_batch_destroy": (ctypes.c_int, [_vp]),
     "fdtd_batch_set_stream": (ctypes.c_int, [_vp, _vp]),
@@ -209,10 +213,12 @@ class Simulation:
         """Zero-thickness plate normal to ``normal_axis`` (fdtd_add_plate)."""
         _check(_lib.fdtd_add_plate(self._h, normal_axis, _box(box), sigma_1, sigma_2))
 
-    def add_port(self, voltage_box: Sequence[int], current_box: Sequence[int], axis: int = 2) -> int:
-        """A z-directed port (voltage edges and current loop); returns its id."""
+    def add_port(self, voltage_box: Sequence[int], current_box: Sequence[int], current_axis: int = 2,
+                 voltage_axis: int = 2) -> int:
+        """A port (z-directed voltage edges, current loop around ``current_axis``); returns its id."""
         pid = _i32(-1)
-        _check(_lib.fdtd_add_port(self._h, axis, _box(voltage_box), _box(current_box), ctypes.byref(pid)))
+        _check(_lib.fdtd_add_port(self._h, voltage_axis, _box(voltage_box), current_axis, _box(current_box),
+                                  ctypes.byref(pid)))
         self.n_probes = _lib.fdtd_probe_count(self._h)
         return pid.value
 
@@ -358,6 +364,33 @@ class Simulation:
         if probe_capacity is not None:
             sim.set_probe_capacity(probe_capacity)
         return sim
+
+
+def source_waveform(type_: int, amp: float, freq: float, dt: float, t_0: float, tau: float, pi: float, n: int):
+    """setGauss (type 1) / setSine (type 3) voltage waveform of n steps, float32 (fdtd_source_waveform)."""
+    out = np.zeros(n, dtype=np.float32)
+    _check(load_library().fdtd_source_waveform(type_, amp, freq, dt, t_0, tau, pi, n, out.ctypes.data_as(_pf)))
+    return out
+
+
+def marching_loop(params: dict):
+    """The reference's whole run (fdtd_marching_loop) for marchingLoop's parameters ``params`` (the
+    names of scenario.MARCHING_PARAMS): returns (V(t), I(t)) float32."""
+    lib = load_library()
+    keep, args = [], []
+    for name, kind in S.MARCHING_PARAMS:
+        v = params[name]
+        if kind == "a":
+            arr = np.ascontiguousarray(np.asarray(v, dtype=np.float32).reshape(-1))
+            keep.append(arr)
+            args.append(arr.ctypes.data_as(_pf))
+        else:
+            args.append(v)
+    n = int(params["n_t_steps"])
+    V = np.zeros(n, dtype=np.float32)
+    I = np.zeros(n, dtype=np.float32)
+    _check(lib.fdtd_marching_loop(*args, V.ctypes.data_as(_pf), I.ctypes.data_as(_pf)))
+    return V, I
 
 
 def port_zin(v_spectrum: np.ndarray, i_spectrum: np.ndarray, z0: complex = 50.0):

@@ -154,17 +154,23 @@ int fdtd_get_cpml_profile(fdtd_handle* h, int32_t axis, int32_t kind, float* hos
 /* Bytes of device memory the handle holds. */
 int64_t fdtd_device_bytes(const fdtd_handle* h);
 
-/* Port voltage and current (z direction). Registers the point probes of a port: the Ez edges of
- * the voltage box i in [is,ie], j in [js,je], k in [ks,ke), and the current loop of the current
- * box at plane ke-1 (Hx at j = js-1 and j = je for i in [is,ie], Hy at i = ie and i = is-1 for
- * j in [js,je]). Replaces the voltage / current sample boxes of sampleField and the reductions
- * voltMgpu / currMgpu (fdtdrav.h:2185-2488, case 3). Add ports before the first step; their
- * probes also appear as columns of fdtd_read_probes. */
-int fdtd_add_port(fdtd_handle* h, int32_t axis, const int32_t voltage_box[6], const int32_t current_box[6],
-                  int32_t* id_out);
-/* V(t) = -dz / (n_i n_j) * sum of the voltage edges' Ez and I(t) = dy (Hy(ie) sum) + dx (Hx(js-1)
- * sum) - dy (Hy(is-1) sum) - dx (Hx(je) sum) for steps [first_step, first_step+n_steps), summed in
- * the reference's order (host memory; voltMgpu / currMgpu, fdtdrav.h:2185-2488). With time_average
+/* Port voltage and current. Registers the point probes of a port: the Ez edges of the voltage
+ * box i in [is,ie], j in [js,je], k in [ks,ke) (voltage_axis 2; the reference's other voltage
+ * directions sum the same sampled Ez array, fdtdrav.h:2214-2262, and are not provided), and the
+ * current loop of currMgpu around the current box for current_axis 0 / 1 / 2 (x / y / z,
+ * fdtdrav.h:2318-2480, cases 1 / 2 / 3):
+ *   x: Hy(ie-1, j, ks-1), Hz(ie-1, je, k), Hy(ie-1, j, ke), Hz(ie-1, js-1, k)
+ *   y: Hz(is-1, je-1, k), Hx(i, je-1, ke), Hz(ie, je-1, k), Hx(i, je-1, ks-1)
+ *   z: Hy(ie, j, ke-1), Hx(i, js-1, ke-1), Hy(is-1, j, ke-1), Hx(i, je, ke-1)
+ * for i in [is,ie], j in [js,je], k in [ks,ke] of the current box. Replaces the voltage / current
+ * sample boxes of sampleField and the reductions voltMgpu / currMgpu (fdtdrav.h:2185-2488). Add
+ * ports before the first step; their probes also appear as columns of fdtd_read_probes. */
+int fdtd_add_port(fdtd_handle* h, int32_t voltage_axis, const int32_t voltage_box[6], int32_t current_axis,
+                  const int32_t current_box[6], int32_t* id_out);
+/* V(t) = -dz / (n_i n_j) * sum of the voltage edges' Ez and I(t) = a1 s1 + a2 s2 - a1 s3 - a2 s4
+ * over the four probe groups above in order (a1, a2 = dy, dz for x; dz, dx for y; dy, dx for z)
+ * for steps [first_step, first_step+n_steps), summed in the reference's order (host memory;
+ * voltMgpu / currMgpu, fdtdrav.h:2185-2488). With time_average
  * set, I(t) becomes (I(t) + I(t+1)) / 2 over the window from the unaveraged I(t+1), and the last
  * step (I(t) + I'(t-1)) / 2 from the averaged I'(t-1), as the reference's in-place correcI produces
  * them (fdtdrav.h:2490-2508, called by calcVoltCurrent, fdtdrav.h:3129-3186). */
@@ -184,6 +190,43 @@ int fdtd_port_spectrum(fdtd_handle* h, int32_t id, int64_t first_step, int64_t n
  * precomputed spectra (fdtdrav.h:3054-3127). */
 int fdtd_port_zin(int64_t n_bins, const float* v_spectrum, const float* i_spectrum, float z0_re, float z0_im,
                   float* s11, float* zin);
+
+/* ---- The reference's whole run ------------------------------------------------------------ */
+
+/* Source waveform of setGauss / setSine (fdtdrav.h:1486-1520), evaluated on the current device so
+ * that expf / sinf are CUDA's: type 1 out[m] = amp exp(-((m dt - t_0)^2) / tau^2), type 3
+ * out[m] = amp sin(2 pi freq dt m), type 2 zero (the reference leaves that signal unset).
+ * n values to host memory. */
+int fdtd_source_waveform(int32_t type, float amp, float freq, float dt, float t_0, float tau, float pi, int64_t n,
+                         float* out);
+
+/* marchingLoop (fdtdrav.h:3425-4387) with its parameter list, plus the host arrays voltage and
+ * current (n_t_steps floats each) that receive V(t) and the time-averaged I(t) which the reference
+ * computes in calcVoltCurrent and writes to its result files. Geometry in metres is converted to
+ * node indices as the reference does (calc_index, offsets of CPML and air buffer, NZ rounded up to
+ * a multiple of NUMDEV); the whole domain then runs on the current device. Bricks (isotropic:
+ * equal x / y / z values), z plates (pec_*), the z-directed lumped source with its waveform
+ * (source_tp 1 Gaussian, 3 sine, 2 none), the resistor (z edges, as defineResistor) and the port
+ * (voltage direction 3, current direction 1 / 2 / 3). c and nc are unused, as in the reference. */
+int fdtd_marching_loop(
+    const int NUMDEV, float eps_0, float pi, float mu_0, float c, float dx, float dy, float dz, float dt, int X, int Y,
+    int Z, int n_t_steps, int pml_x_n, int pml_y_n, int pml_z_n, int pml_x_p, int pml_y_p, int pml_z_p, int air_buff_x_n,
+    int air_buff_y_n, int air_buff_z_n, int air_buff_x_p, int air_buff_y_p, int air_buff_z_p, int source_tp,
+    float source_freq, float source_amp, float source_min_x, float source_min_y, float source_min_z, float source_max_x,
+    float source_max_y, float source_max_z, int source_direction, float rs, float nc, float tau, float t_0,
+    const float* brick_min_x, const float* brick_min_y, const float* brick_min_z, const float* brick_max_x,
+    const float* brick_max_y, const float* brick_max_z, const float* brick_sigma_e_x, const float* brick_sigma_e_y,
+    const float* brick_sigma_e_z, const float* brick_eps_r_x, const float* brick_eps_r_y, const float* brick_eps_r_z,
+    const float* brick_sigma_m_x, const float* brick_sigma_m_y, const float* brick_sigma_m_z, const float* brick_mu_r_x,
+    const float* brick_mu_r_y, const float* brick_mu_r_z, int brick_opt, int brick_num, const float* pec_min_x,
+    const float* pec_min_y, const float* pec_min_z, const float* pec_max_x, const float* pec_max_y,
+    const float* pec_max_z, const float* pec_sigma_e_x, const float* pec_sigma_e_y, const float* pec_sigma_e_z,
+    int pec_opt, int pec_num, float resistor_min_x, float resistor_min_y, float resistor_min_z, float resistor_max_x,
+    float resistor_max_y, float resistor_max_z, float resistor_resist, int resistor_direction, int resistor_opt,
+    float sampled_voltage_min_x, float sampled_voltage_min_y, float sampled_voltage_min_z, float sampled_voltage_max_x,
+    float sampled_voltage_max_y, float sampled_voltage_max_z, int voltage_direction, float sampled_current_min_x,
+    float sampled_current_min_y, float sampled_current_min_z, float sampled_current_max_x, float sampled_current_max_y,
+    float sampled_current_max_z, int current_direction, float* voltage, float* current);
 
 /* ---- Design region and adjoint gradient (no reference counterpart: the reference has no
  * gradient; its commented-out differential-evolution optimiser, fdtdrav.h:2758-2986, is the

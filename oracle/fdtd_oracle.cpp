@@ -717,20 +717,27 @@ int or_onestep_f32(const or_scenario* sc, int m, const float* sig, int n_sig, co
     return run<float>(sc, 0, sig, n_sig, init_fields, nullptr, fields_out, 1, m, init_psi, psi_out);
 }
 
-// Port voltage and current of a z-directed port from sampled series (steps rows of `stride` floats,
-// the port's columns from col0): the voltage box's Ez edges (k in [ks,ke) outer, then j, then i),
-// Hx at j = js-1 and at j = je (i = is..ie), Hy at i = ie and at i = is-1 (j = js..je) of the
-// current box at plane ke-1. Restates voltMgpu case 3 (fdtdrav.h:2268-2290): a float sum in that
-// order times csuf = -dz / ((ie-is+1)(je-js+1)); currMgpu case 3 (fdtdrav.h:2427-2480): four float
-// sums and dy*yp + dx*xp - dy*yn - dx*xn, contracted as the reference's compiled expression is
-// (dx*xp fused with dy*yp as the addend, then two FMAs; found by comparing the candidate
-// contractions against the reference's outputs); and, with time_average, correcI
+// Port voltage and current from sampled series (steps rows of `stride` floats, the port's columns
+// from col0): the voltage box's Ez edges (k in [ks,ke) outer, then j, then i), then four groups of
+// H samples s1..s4 of the current loop for current direction `axis` (0 x, 1 y, 2 z; the groups
+// of fdtd_gb300's port_groups, in summation order). Restates voltMgpu case 3
+// (fdtdrav.h:2268-2290): a float sum in that order times csuf = -dz / ((ie-is+1)(je-js+1));
+// currMgpu cases 1-3 (fdtdrav.h:2318-2480): four float sums and a1*s1 + a2*s2 - a1*s3 - a2*s4
+// (a1, a2 = dy, dz / dz, dx / dy, dx), contracted as the reference's compiled expressions are
+// (x loop: a1*s1 fused with a2*s2 as the addend; y, z loops: a2*s2 fused with a1*s1 as the
+// addend; then two FMAs; found by comparing the candidate contractions against the reference's
+// outputs); and, with time_average, correcI
 // (fdtdrav.h:2490-2508) in the order its in-place threads produced their results.
-int or_port_vi(const float* series, int steps, int stride, int col0, const int* vbox, const int* cbox,
+int or_port_vi(const float* series, int steps, int stride, int col0, const int* vbox, const int* cbox, int axis,
                float dx, float dy, float dz, int time_average, float* V, float* I) {
     const int nv = (vbox[3] - vbox[0] + 1) * (vbox[4] - vbox[1] + 1) * (vbox[5] - vbox[2]);
-    const int nx = cbox[3] - cbox[0] + 1, ny = cbox[4] - cbox[1] + 1;
-    if (nv <= 0 || nx <= 0 || ny <= 0 || col0 + nv + 2 * nx + 2 * ny > stride) {
+    const int ni = cbox[3] - cbox[0] + 1, nj = cbox[4] - cbox[1] + 1, nk = cbox[5] - cbox[2] + 1;
+    int n[4];
+    float a1, a2;
+    if (axis == 0) { n[0] = nj; n[1] = nk; n[2] = nj; n[3] = nk; a1 = dy; a2 = dz; }
+    else if (axis == 1) { n[0] = nk; n[1] = ni; n[2] = nk; n[3] = ni; a1 = dz; a2 = dx; }
+    else { n[0] = nj; n[1] = ni; n[2] = nj; n[3] = ni; a1 = dy; a2 = dx; }
+    if (nv <= 0 || ni <= 0 || nj <= 0 || nk <= 0 || col0 + nv + n[0] + n[1] + n[2] + n[3] > stride) {
         g_err = "port columns outside the series";
         return -1;
     }
@@ -741,14 +748,16 @@ int or_port_vi(const float* series, int steps, int stride, int col0, const int* 
         float v = 0.f;
         for (int q = 0; q < nv; ++q) v = v + r[q];
         V[t] = v * csuf;
-        const float* hx = r + nv;
-        const float* hy = hx + 2 * nx;
-        float xp = 0.f, xn = 0.f, yp = 0.f, yn = 0.f;
-        for (int q = 0; q < nx; ++q) xp = xp + hx[q];
-        for (int q = 0; q < nx; ++q) xn = xn + hx[nx + q];
-        for (int q = 0; q < ny; ++q) yp = yp + hy[q];
-        for (int q = 0; q < ny; ++q) yn = yn + hy[ny + q];
-        I[t] = std::fmaf(-dx, xn, std::fmaf(-dy, yn, std::fmaf(dx, xp, dy * yp)));
+        const float* hs = r + nv;
+        float sum[4];
+        for (int g = 0; g < 4; ++g) {
+            float acc = 0.f;
+            for (int q = 0; q < n[g]; ++q) acc = acc + hs[q];
+            sum[g] = acc;
+            hs += n[g];
+        }
+        const float lead = axis == 0 ? std::fmaf(a1, sum[0], a2 * sum[1]) : std::fmaf(a2, sum[1], a1 * sum[0]);
+        I[t] = std::fmaf(-a2, sum[3], std::fmaf(-a1, sum[2], lead));
     }
     if (time_average && steps > 1) {
         // each step from its unaveraged successor; the last step from its averaged predecessor

@@ -34,13 +34,14 @@ cudaLibrary_t g_lib = nullptr;
 
 struct Kern { const char* name; cudaKernel_t k; };
 enum { K_SETZERO, K_SETBRICK, K_SETSIGMA, K_SETCOEF, K_SETABCPML, K_SRCZ, K_RES, K_CALCE, K_CALCH,
-       K_VOLT, K_CURR, K_CORREC, K_PLATEX, K_PLATEY, K_PLATEZ, K_ZIN, K_GATHER, K_COUNT };
+       K_VOLT, K_CURR, K_CORREC, K_PLATEX, K_PLATEY, K_PLATEZ, K_GAUSS, K_SINE, K_ZIN, K_GATHER, K_COUNT };
 Kern g_k[K_COUNT] = {
     {"_Z7setZero", nullptr}, {"_Z8setBrick", nullptr}, {"_Z18setSigmaEpsSigmaMu", nullptr},
     {"_Z15setCoefficients", nullptr}, {"_Z9setABCPML", nullptr}, {"_Z13defineSourceZ", nullptr},
     {"_Z14defineResistor", nullptr}, {"_Z6calc_e", nullptr}, {"_Z6calc_h", nullptr},
     {"_Z8voltMgpu", nullptr}, {"_Z8currMgpu", nullptr}, {"_Z7correcI", nullptr},
     {"_Z12definePlateX", nullptr}, {"_Z12definePlateY", nullptr}, {"_Z12definePlateZ", nullptr},
+    {"_Z8setGauss", nullptr}, {"_Z7setSine", nullptr},
     {"_Z8c_zinS11P6float2S0_iS0_S0_S0_S0_S_f", nullptr}, {"harness_gather", nullptr}};
 
 // Itanium-ABI names of the reference kernels: the parameter lists of fdtdrav.h reduce to runs of
@@ -177,6 +178,8 @@ int rh_load(const char* cubin_path) {
         "5i2p2f6i",                    // definePlateX
         "5i2p2f6i",                    // definePlateY
         "5i2p2f6i",                    // definePlateZ
+        "2p1f1i3f1i",                  // setGauss
+        "2p1i4f1i",                    // setSine
         nullptr, nullptr};             // c_zinS11 (float2 parameters, full name above), gather
     for (int k = 0; k < K_COUNT; ++k) {
         std::string nm = (k < K_COUNT && specs[k]) ? mangled(g_k[k].name, specs[k]) : std::string(g_k[k].name);
@@ -525,6 +528,26 @@ long long rh_padded_dims(int* nx, int* ny) { *nx = g_d.NX; *ny = g_d.NY; return 
 
 void rh_free(void) { free_all(); }
 
+// The reference's source waveform kernels as marchingLoop launches them (fdtdrav.h:4068-4086,
+// 1-D blocks of 512): type 1 setGauss, type 3 setSine. Returns d_signal and d_signal_per_node.
+int rh_waveform(int type, float amp, int v_mag_factor, float freq, float dt, float t_0, float tau, float pi, int n,
+                float* signal, float* per_node) {
+    if (!g_lib) { g_err = "rh_load not called"; return -1; }
+    if (type != 1 && type != 3) { g_err = "waveform type 1 or 3"; return -1; }
+    float *ds = nullptr, *dn = nullptr;
+    if (!ck(cudaMalloc(&ds, n * sizeof(float)), "cudaMalloc signal") ||
+        !ck(cudaMalloc(&dn, n * sizeof(float)), "cudaMalloc per node")) { cudaFree(ds); return -1; }
+    int block = 512, grid = n / block + ((n % block) == 0 ? 0 : 1);
+    std::vector<void*> a;
+    if (type == 1) a = {&ds, &dn, &amp, &v_mag_factor, &dt, &t_0, &tau, &n};
+    else a = {&ds, &dn, &v_mag_factor, &amp, &freq, &dt, &pi, &n};
+    bool ok = launch(type == 1 ? K_GAUSS : K_SINE, dim3(grid), dim3(block), a) && ck(cudaDeviceSynchronize(), "waveform sync") &&
+              ck(cudaMemcpy(signal, ds, n * sizeof(float), cudaMemcpyDeviceToHost), "signal D2H") &&
+              ck(cudaMemcpy(per_node, dn, n * sizeof(float), cudaMemcpyDeviceToHost), "per node D2H");
+    cudaFree(ds); cudaFree(dn);
+    return ok ? 0 : -1;
+}
+
 static bool realloc_sample(const char* name, size_t n) {
     float*& p = g_arr[name];
     if (p) cudaFree(p);
@@ -556,15 +579,17 @@ int rh_set_port(const int* vbox, const int* cbox, int n_steps) {
 }
 
 // The reference's port reductions on its own samples, launched as calcVoltCurrent does
-// (fdtdrav.h:3129-3186, NUMDEV = 1, 1-D blocks of 512): voltMgpu and currMgpu (direction 3),
-// then correcI in place. Returns V(t), I(t) before correcI and I(t) after it.
-int rh_port_reduce(int n_steps, float* volt, float* curr_raw, float* curr_avg) {
+// (fdtdrav.h:3129-3186, NUMDEV = 1, 1-D blocks of 512): voltMgpu (direction 3) and currMgpu
+// (current_direction 1, 2 or 3), then correcI in place. Returns V(t), I(t) before correcI and
+// I(t) after it.
+int rh_port_reduce(int n_steps, int current_direction, float* volt, float* curr_raw, float* curr_avg) {
     if (g_port_steps <= 0 || n_steps != g_port_steps) { g_err = "rh_set_port first, same n_steps"; return -1; }
     float *dv = nullptr, *di = nullptr;
     if (!ck(cudaMalloc(&dv, n_steps * sizeof(float)), "cudaMalloc V") ||
         !ck(cudaMalloc(&di, n_steps * sizeof(float)), "cudaMalloc I")) { cudaFree(dv); return -1; }
     int block = 512, grid = n_steps / block + ((n_steps % block) == 0 ? 0 : 1);
-    int off = 0, dir = 3, n = n_steps;
+    int off = 0, dir = 3, cdir = current_direction, n = n_steps;
+    if (cdir < 1 || cdir > 3) { g_err = "current direction must be 1, 2 or 3"; cudaFree(dv); cudaFree(di); return -1; }
     static int vb[6], cb[6], vn[4], cn[4];
     for (int q = 0; q < 6; ++q) { vb[q] = g_vbox[q]; cb[q] = g_cbox[q]; }
     vn[0] = g_vn[0]; vn[1] = g_vn[1]; vn[2] = g_d.NZ; vn[3] = g_d.NZ_N;
@@ -584,7 +609,7 @@ int rh_port_reduce(int n_steps, float* volt, float* curr_raw, float* curr_avg) {
         std::vector<void*> a = {&cn[0], &cn[1], &cn[2], &cn[3], &off};
         for (int q = 0; q < 6; ++q) a.push_back(&cb[q]);
         a.push_back(&P[0]); a.push_back(&P[2]); a.push_back(&P[3]); a.push_back(&P[4]);
-        a.push_back(&g_d.dx); a.push_back(&g_d.dy); a.push_back(&g_d.dz); a.push_back(&n); a.push_back(&dir);
+        a.push_back(&g_d.dx); a.push_back(&g_d.dy); a.push_back(&g_d.dz); a.push_back(&n); a.push_back(&cdir);
         ok = ok && launch(K_CURR, dim3(grid), dim3(block), a);
     }
     ok = ok && ck(cudaDeviceSynchronize(), "port reduce sync") &&

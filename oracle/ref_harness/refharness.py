@@ -54,8 +54,9 @@ class RefHarness:
         L.rh_calc_h.argtypes = [_i]
         L.rh_run.argtypes = [_i, _i, _i, _pf, ctypes.c_longlong, _i, _pi, _pi, _pi, _pi, _pf, _pf]
         L.rh_set_port.argtypes = [_pi, _pi, _i]
-        L.rh_port_reduce.argtypes = [_i, _pf, _pf, _pf]
+        L.rh_port_reduce.argtypes = [_i, _i, _pf, _pf, _pf]
         L.rh_zin.argtypes = [_i, _pf, _pf, _f, _f, _pf, _pf]
+        L.rh_waveform.argtypes = [_i, _f, _i, _f, _f, _f, _f, _f, _i, _pf, _pf]
         self._check(L.rh_load(cubin.encode()))
         self.sc = None
 
@@ -137,11 +138,11 @@ class RefHarness:
         c = np.ascontiguousarray(current_box, dtype=np.int32)
         self._check(self.lib.rh_set_port(v.ctypes.data_as(_pi), c.ctypes.data_as(_pi), steps))
 
-    def port_reduce(self, steps: int) -> tuple:
+    def port_reduce(self, steps: int, current_direction: int = 3) -> tuple:
         """The reference's voltMgpu / currMgpu / correcI on its samples: (V, I before correcI,
-        I after correcI), float32 arrays of ``steps``."""
+        I after correcI), float32 arrays of ``steps``; current_direction 1 / 2 / 3 = x / y / z."""
         out = [np.zeros(steps, dtype=np.float32) for _ in range(3)]
-        self._check(self.lib.rh_port_reduce(steps, *(o.ctypes.data_as(_pf) for o in out)))
+        self._check(self.lib.rh_port_reduce(steps, current_direction, *(o.ctypes.data_as(_pf) for o in out)))
         return tuple(out)
 
     def zin(self, n_t_steps: int, V: np.ndarray, I: np.ndarray, z0: complex) -> tuple:
@@ -156,6 +157,15 @@ class RefHarness:
                                     complex(z0).real, complex(z0).imag, s11.ctypes.data_as(_pf),
                                     zin.ctypes.data_as(_pf)))
         return s11, zin
+
+    def waveform(self, type_: int, amp: float, v_mag_factor: int, freq: float, dt: float, t_0: float, tau: float,
+                 pi: float, n: int) -> tuple:
+        """The reference's setGauss (type 1) / setSine (type 3): (signal, signal per node) float32."""
+        sig = np.zeros(n, dtype=np.float32)
+        per = np.zeros(n, dtype=np.float32)
+        self._check(self.lib.rh_waveform(type_, amp, v_mag_factor, freq, dt, t_0, tau, pi, n,
+                                         sig.ctypes.data_as(_pf), per.ctypes.data_as(_pf)))
+        return sig, per
 
     def fields(self) -> dict:
         return {n: self.get(n) for n in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")}

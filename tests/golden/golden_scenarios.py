@@ -117,8 +117,55 @@ def plates_scenario():
     return sc
 
 
+def marching_params(n_t_steps=500, current_direction=2, numdev=1, source_tp=1, resistor_opt=0):
+    """marchingLoop's parameters for a reduced version of the reference driver's microstrip case
+    (substrate brick on a ground plate, a feed strip and a wider patch plate, a Gaussian source at
+    the feed, voltage and current sampled on the feed line): its cell sizes and constants,
+    a 40 x 60 x 6-cell structure, 6-cell CPML, 4-cell air buffers."""
+    import numpy as np
+    f = np.float32
+    eps_0 = f(8.854187817e-12)
+    pi = f(3.1415)
+    mu_0 = f(np.float64(f(4) * pi) * 1e-7)
+    c = f(1) / np.sqrt(mu_0 * eps_0)
+    dx, dy, dz = f(0.389e-3), f(0.4e-3), f(0.265e-3)
+    dt = f(1 / (np.float64(c) * np.sqrt(1 / np.float64(dx) ** 2 + 1 / np.float64(dy) ** 2 + 1 / np.float64(dz) ** 2)))
+    nc = f(20)
+    tau = (nc * dy) / (f(2) * c)
+    a = dict(NUMDEV=numdev, eps_0=eps_0, pi=pi, mu_0=mu_0, c=c, dx=dx, dy=dy, dz=dz, dt=dt, X=40, Y=60, Z=6,
+             n_t_steps=n_t_steps, pml_x_n=6, pml_y_n=6, pml_z_n=6, pml_x_p=6, pml_y_p=6, pml_z_p=6,
+             air_buff_x_n=4, air_buff_y_n=4, air_buff_z_n=4, air_buff_x_p=4, air_buff_y_p=4, air_buff_z_p=4,
+             source_tp=source_tp, source_freq=f(2e9), source_amp=f(1),
+             source_min_x=f(16) * dx, source_min_y=f(0), source_min_z=f(0),
+             source_max_x=f(22) * dx, source_max_y=f(0), source_max_z=f(3) * dz,
+             source_direction=3, rs=f(50), nc=nc, tau=tau, t_0=f(3) * tau)
+    a.update(brick_min_x=[0.0], brick_min_y=[0.0], brick_min_z=[0.0], brick_max_x=[f(40) * dx],
+             brick_max_y=[f(60) * dy], brick_max_z=[f(3) * dz], brick_sigma_e_x=[4e-4], brick_sigma_e_y=[4e-4],
+             brick_sigma_e_z=[4e-4], brick_eps_r_x=[2.2], brick_eps_r_y=[2.2], brick_eps_r_z=[2.2],
+             brick_sigma_m_x=[1.2e-38], brick_sigma_m_y=[1.2e-38], brick_sigma_m_z=[1.2e-38], brick_mu_r_x=[1.0],
+             brick_mu_r_y=[1.0], brick_mu_r_z=[1.0], brick_opt=1, brick_num=1)
+    a.update(pec_min_x=[0.0, f(16) * dx, f(10) * dx], pec_min_y=[0.0, 0.0, f(30) * dy],
+             pec_min_z=[0.0, f(3) * dz, f(3) * dz], pec_max_x=[f(40) * dx, f(22) * dx, f(30) * dx],
+             pec_max_y=[f(60) * dy, f(30) * dy, f(50) * dy], pec_max_z=[0.0, f(3) * dz, f(3) * dz],
+             pec_sigma_e_x=[1e10] * 3, pec_sigma_e_y=[1e10] * 3, pec_sigma_e_z=[1e10] * 3, pec_opt=1, pec_num=3)
+    a.update(resistor_min_x=f(30) * dx, resistor_min_y=f(50) * dy, resistor_min_z=f(0), resistor_max_x=f(30) * dx,
+             resistor_max_y=f(50) * dy, resistor_max_z=f(3) * dz, resistor_resist=f(50), resistor_direction=3,
+             resistor_opt=resistor_opt)
+    a.update(sampled_voltage_min_x=f(16) * dx, sampled_voltage_min_y=f(10) * dy, sampled_voltage_min_z=f(0),
+             sampled_voltage_max_x=f(22) * dx, sampled_voltage_max_y=f(10) * dy, sampled_voltage_max_z=f(3) * dz,
+             voltage_direction=3)
+    a.update(sampled_current_min_x=f(16) * dx, sampled_current_min_y=f(10) * dy, sampled_current_min_z=f(3) * dz,
+             sampled_current_max_x=f(22) * dx, sampled_current_max_y=f(10) * dy, sampled_current_max_z=f(3) * dz,
+             current_direction=current_direction)
+    if current_direction == 3:  # a z loop needs ks < ke: around the feed's vertical edges
+        a.update(sampled_current_min_z=f(0), sampled_current_max_z=f(3) * dz)
+    return a
+
+
 # voltage box: i, j closed, k half-open (voltMgpu case 3); current box: loop at plane ke - 1
 PORT_BOX = (14, 13, 9, 15, 14, 12)
+# a current box whose x, y and z loops (currMgpu cases 1, 2, 3) all lie inside the grid
+PORT_CURRENT_BOX = (13, 12, 8, 16, 15, 11)
 
 
 def fixture_scenarios():

@@ -145,6 +145,13 @@ def port_fixture():
         h.set_port(gs.PORT_BOX, gs.PORT_BOX, sc.steps)
         probes, _ = h.run(sc.steps, src_slot=0, signal=sc.signal_per_node(0), probes=sc.probes)
         v, i_raw, i_avg = h.port_reduce(sc.steps)
+        # the same run with the current box that all three loop directions fit
+        h.setup(sc)
+        h.set_port(gs.PORT_BOX, gs.PORT_CURRENT_BOX, sc.steps)
+        h.run(sc.steps, src_slot=0, signal=sc.signal_per_node(0))
+        loops = {}
+        for d in (1, 2, 3):
+            _, loops[f"current_raw_d{d}"], loops[f"current_avg_d{d}"] = h.port_reduce(sc.steps, d)
         rng = np.random.default_rng(321)
         nf = sc.steps // 2 + 1
         sv = (rng.standard_normal(nf) + 1j * rng.standard_normal(nf)).astype(np.complex64)
@@ -158,19 +165,46 @@ def port_fixture():
         h.close()
     return {"probes": probes, "voltage": v, "current_raw": i_raw, "current_avg": i_avg,
             "spec_v": sv, "spec_i": si, "z0": np.array([z0, z1], dtype=np.complex64),
-            "s11": np.stack([s11, s11b]), "zin": np.stack([zin, zinb]), **lines}
+            "s11": np.stack([s11, s11b]), "zin": np.stack([zin, zinb]), **lines, **loops}
+
+
+def marching_fixture():
+    """The reference's own pipeline on the reduced microstrip case (marchingLoop's index set-up
+    restated in fdtd_gb300.scenario): setGauss, the setup kernels, calc_e / calc_h with its sample
+    boxes, voltMgpu / currMgpu (y loop) / correcI."""
+    from fdtd_gb300 import scenario as S
+    a = gs.marching_params()
+    n = a["n_t_steps"]
+    h = refharness.RefHarness()
+    try:
+        ix = S.marching_indices(a)
+        src = ix["source"]
+        sig, per = h.waveform(1, a["source_amp"], src[5] - src[2], a["source_freq"], a["dt"], a["t_0"], a["tau"],
+                              a["pi"], n)
+        sc, vbox, cbox = S.marching_scenario(a, sig)
+        h.setup(sc)
+        h.set_port(vbox, cbox, n)
+        h.run(n, src_slot=0, signal=per)
+        v, i_raw, i_avg = h.port_reduce(n, a["current_direction"])
+    finally:
+        h.close()
+    return {"signal": sig, "voltage": v, "current_raw": i_raw, "current_avg": i_avg}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
     ap.add_argument("--analysis", default=None, help="also write large analysis-only dumps here")
-    ap.add_argument("--only", default=None, choices=["port", "plates"], help="write one fixture only")
+    ap.add_argument("--only", default=None, choices=["port", "plates", "marching"], help="write one fixture only")
     args = ap.parse_args()
     os.makedirs(args.out, exist_ok=True)
     if args.only == "port":
         np.savez_compressed(os.path.join(args.out, "port.npz"), **port_fixture())
         print("port fixture written to", args.out)
+        return
+    if args.only == "marching":
+        np.savez_compressed(os.path.join(args.out, "marching.npz"), **marching_fixture())
+        print("marching fixture written to", args.out)
         return
     if args.only == "plates":
         np.savez_compressed(os.path.join(args.out, "plates.npz"), **run_scenario(gs.plates_scenario(), True))

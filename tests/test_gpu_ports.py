@@ -59,6 +59,24 @@ def test_port_vi_bitwise_vs_reference(gpu_lib, schedule):
     assert bitwise_equal(Vo, V) and bitwise_equal(Io, Iavg)
 
 
+@pytest.mark.parametrize("schedule", [1, 2])
+def test_current_loops_bitwise_vs_reference(gpu_lib, schedule):
+    """x, y and z current loops (currMgpu cases 1, 2, 3) on one run."""
+    from fdtd_gb300 import solver
+    sc = gs.port_scenario()
+    fix = golden("port")
+    with solver.Simulation.from_scenario(sc, schedule, probe_capacity=sc.steps) as sim:
+        ids = [sim.add_port(gs.PORT_BOX, gs.PORT_CURRENT_BOX, current_axis=a) for a in (0, 1, 2)]
+        sim.step(sc.steps)
+        sim.synchronize()
+        for a, pid in enumerate(ids):
+            V, Iraw = sim.read_port(pid, time_average=False)
+            _, Iavg = sim.read_port(pid)
+            assert bitwise_equal(V, fix["voltage"])
+            assert bitwise_equal(Iraw, fix[f"current_raw_d{a + 1}"]), a
+            assert bitwise_equal(Iavg, fix[f"current_avg_d{a + 1}"]), a
+
+
 def test_port_columns_in_probe_series(gpu_lib):
     from fdtd_gb300 import solver
     sc = gs.port_scenario()
@@ -117,7 +135,7 @@ def test_port_validation(gpu_lib):
                 sim.add_port(vbox, cbox)
             assert e.value.code == FDTD_ERR_INVALID
         with pytest.raises(solver.FDTDError) as e:
-            sim.add_port(gs.PORT_BOX, gs.PORT_BOX, axis=0)
+            sim.add_port(gs.PORT_BOX, gs.PORT_BOX, voltage_axis=0)
         assert e.value.code == FDTD_ERR_INVALID
         pid = sim.add_port(gs.PORT_BOX, gs.PORT_BOX)
         sim.step(4)

@@ -54,8 +54,14 @@ def test_port_probe_layout():
     nv = (ie - is_ + 1) * (je - js + 1) * (ke - ks)
     assert len(p) == nv + 2 * (ie - is_ + 1) + 2 * (je - js + 1)
     assert (p[0].i, p[0].j, p[0].k) == (is_, js, ks) and (p[1].i, p[1].j, p[1].k) == (is_ + 1, js, ks)
-    assert (p[nv].component, p[nv].i, p[nv].j, p[nv].k) == (3, is_, js - 1, ke - 1)
-    assert (p[-1].component, p[-1].i, p[-1].j, p[-1].k) == (4, is_ - 1, je, ke - 1)
+    # z loop: Hy(ie, j) first, Hx(i, je) last, at plane ke - 1
+    assert (p[nv].component, p[nv].i, p[nv].j, p[nv].k) == (4, ie, js, ke - 1)
+    assert (p[-1].component, p[-1].i, p[-1].j, p[-1].k) == (3, ie, je, ke - 1)
+    # y loop (source.cu's current direction): Hz(is-1, je-1, k) first, Hx(i, je-1, ks-1) last
+    q = oracle.port_probes(gs.PORT_BOX, (14, 13, 9, 15, 13, 11), current_axis=1)
+    assert (q[nv].component, q[nv].i, q[nv].j, q[nv].k) == (5, 13, 12, 9)
+    assert (q[-1].component, q[-1].i, q[-1].j, q[-1].k) == (3, 15, 12, 8)
+    assert len(q) == nv + 2 * 3 + 2 * 2
 
 
 def test_oracle_port_vi_equals_reference():
@@ -77,6 +83,25 @@ def test_oracle_time_average_equals_correcI():
     t = t[t + 1 < raw.size]
     alt = (raw[t] + (raw[t + 1] + raw[np.minimum(t + 2, raw.size - 1)]) / np.float32(2)) / np.float32(2)
     assert np.any(alt != fix["current_avg"][t])
+
+
+@pytest.mark.parametrize("axis", [0, 1, 2])
+def test_oracle_current_loops_equal_reference(axis):
+    """currMgpu's x, y and z loops (cases 1, 2, 3) on the reference's own samples."""
+    sc = gs.port_scenario()
+    fix = golden("port")
+    key = f"current_raw_d{axis + 1}"
+    if key not in fix.files:
+        pytest.skip("fixture predates the three loop directions")
+    prof = {k: fix[v] for k, v in PROFILE_KEYS.items()}
+    probes = list(sc.probes) + oracle.port_probes(gs.PORT_BOX, gs.PORT_CURRENT_BOX, axis)
+    series, _ = oracle.run(sc, profile_override=prof, probes=probes)
+    for avg, name in ((False, key), (True, f"current_avg_d{axis + 1}")):
+        V, I = oracle.port_vi(series, gs.PORT_BOX, gs.PORT_CURRENT_BOX, sc, col0=len(sc.probes),
+                              time_average=avg, current_axis=axis)
+        assert bitwise_equal(V, fix["voltage"])
+        assert bitwise_equal(I, fix[name]), name
+        assert np.abs(I).max() > 0
 
 
 def test_zin_s11_formulas_against_reference():
