@@ -342,8 +342,9 @@ def bench_adjoint():
 def bench_batched(steps=2000):
     """256 independent instances (per-axis sizes U{32..96}, 8-cell CPML, 8 dielectric boxes, one
     source and one probe each): the same instances run one by one through fdtd_step, then together
-    through the batched persistent launch (autotuned, one CUDA-graph launch). Handle creation and
-    setup are outside both timings; both advance every instance by `steps` steps."""
+    through the batched launch (autotuned over the flat and the persistent forms, CUDA graphs).
+    Handle creation and setup are outside both timings; both advance every instance by `steps`
+    steps."""
     import torch
     from fdtd_gb300 import scenario as S, solver
     scs = S.batch_instances(256, steps=2 * steps + 16)
@@ -377,7 +378,10 @@ def bench_batched(steps=2000):
             "sequential": {"value": round(seq, 3), "unit": "Gcell-updates/s", "seconds": round(t_seq, 3),
                            "gpu_launches": 2 * steps * len(scs)},
             "batched": {"value": round(bat, 3), "unit": "Gcell-updates/s", "seconds": round(t_bat, 3),
-                        "gpu_launches": 1, "config": cfg, "tune_ms_5_steps": round(tune_ms, 2)},
+                        "gpu_launches": 3 * steps if cfg["cluster"] == 0 else 1, "config": cfg,
+                        "form": "flat (E, H, step-counter kernels per step)" if cfg["cluster"] == 0
+                        else "persistent clusters",
+                        "tune_ms_5_steps": round(tune_ms, 2)},
             "speedup": round(bat / seq, 2)}
 
 

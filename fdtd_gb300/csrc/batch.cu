@@ -67,6 +67,56 @@ k_batch(BatchInstance* __restrict__ inst, const int* __restrict__ order, int n_i
     }
 }
 
+// Flat form: per step one E kernel and one H kernel over the tiles of every instance (item
+// {instance, x0, y0, k}: a 32 x 8 block of plane k), then the step counters advance. Every CTA
+// copies its instance's descriptor to shared memory first. The GPU is filled by all instances
+// at once with one node per thread, as in the two-pass schedule, instead of a cluster marching
+// through one instance; the per-node updates are the same, so the bits are too.
+__global__ void __launch_bounds__(256) k_batch_flat_e(const BatchInstance* __restrict__ inst,
+                                                      const int4* __restrict__ items) {
+    __shared__ __align__(16) BatchInstance s;
+    const int4 it = items[blockIdx.x];
+    {
+        const int4* src = reinterpret_cast<const int4*>(inst + it.x);
+        int4* dst = reinterpret_cast<int4*>(&s);
+        const int t = threadIdx.y * 32 + threadIdx.x;
+        for (int w = t; w < (int)(sizeof(BatchInstance) / sizeof(int4)); w += 256) dst[w] = src[w];
+    }
+    __syncthreads();
+    const int i = it.y + (int)threadIdx.x, j = it.z + (int)threadIdx.y;
+    if (i < s.p.g.nx && j < s.p.g.ny) e_node_global(s.p, s.f, s.f, s.ps, s.ps, i, j, it.w, s.step);
+}
+
+__global__ void __launch_bounds__(256) k_batch_flat_h(const BatchInstance* __restrict__ inst,
+                                                      const int4* __restrict__ items) {
+    __shared__ __align__(16) BatchInstance s;
+    const int4 it = items[blockIdx.x];
+    {
+        const int4* src = reinterpret_cast<const int4*>(inst + it.x);
+        int4* dst = reinterpret_cast<int4*>(&s);
+        const int t = threadIdx.y * 32 + threadIdx.x;
+        for (int w = t; w < (int)(sizeof(BatchInstance) / sizeof(int4)); w += 256) dst[w] = src[w];
+    }
+    __syncthreads();
+    const int i = it.y + (int)threadIdx.x, j = it.z + (int)threadIdx.y;
+    if (i < s.p.g.nx && j < s.p.g.ny) h_node_global(s.p, s.f, s.f, s.f, s.ps, s.ps, i, j, it.w, s.step);
+}
+
+__global__ void k_batch_advance(BatchInstance* inst, int n) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n) inst[q].step += 1;
+}
+
+cudaError_t launch_batch_flat(BatchInstance* inst, int n_inst, const int4* items, int n_items, long long steps,
+                              cudaStream_t st) {
+    for (long long s = 0; s < steps; ++s) {
+        k_batch_flat_e<<<n_items, dim3(32, 8, 1), 0, st>>>(inst, items);
+        k_batch_flat_h<<<n_items, dim3(32, 8, 1), 0, st>>>(inst, items);
+        k_batch_advance<<<(n_inst + 127) / 128, 128, 0, st>>>(inst, n_inst);
+    }
+    return cudaGetLastError();
+}
+
 // CTA sizes the autotuner may pick, with register budgets that keep several CTAs per SM.
 using BatchKernel = void (*)(BatchInstance*, const int*, int, int*, long long);
 static BatchKernel kernel_for(int threads) {

@@ -25,4 +25,9 @@ cudaError_t batch_max_clusters(int cluster, int threads, int* out);
 cudaError_t launch_batch(BatchInstance* inst, const int* order, int n_inst, int* queue, long long steps, int cluster,
                          int threads, int n_clusters, cudaStream_t st);
 
+// Flat form: `steps` times an E kernel and an H kernel over `items` ({instance, x0, y0, k}, 32 x 8
+// nodes of plane k of an instance), then the step counters of the instances advance by one.
+cudaError_t launch_batch_flat(BatchInstance* inst, int n_inst, const int4* items, int n_items, long long steps,
+                              cudaStream_t st);
+
 }  // namespace fdtd

@@ -1353,21 +1353,26 @@ struct fdtd_batch {
     BatchInstance* d_inst = nullptr;
     int* d_order = nullptr;
     int* d_queue = nullptr;
-    int cluster = 4, threads = 256, n_clusters = 0;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    long long graph_steps = -1;
-    int graph_cfg[3] = {0, 0, 0};
+    int cluster = 4, threads = 256, n_clusters = 0;  // cluster 0: the flat per-step form
+    int4* d_items = nullptr;            // flat form: {instance, x0, y0, k} per 32 x 8 block
+    int n_items = 0;
+    struct Graph {
+        long long steps;
+        int cfg[3];
+        cudaGraph_t graph;
+        cudaGraphExec_t exec;
+    };
+    std::vector<Graph> graphs;          // captured launches by step count and configuration
 };
 
 namespace {
 
 void batch_drop_graph(fdtd_batch* b) {
-    if (b->exec) cudaGraphExecDestroy(b->exec);
-    if (b->graph) cudaGraphDestroy(b->graph);
-    b->exec = nullptr;
-    b->graph = nullptr;
-    b->graph_steps = -1;
+    for (auto& G : b->graphs) {
+        if (G.exec) cudaGraphExecDestroy(G.exec);
+        if (G.graph) cudaGraphDestroy(G.graph);
+    }
+    b->graphs.clear();
 }
 
 // Instance descriptors from the handles' current in-place buffers and steps.
@@ -1390,8 +1395,15 @@ int batch_refresh(fdtd_batch* b) {
 }
 
 int batch_set_config(fdtd_batch* b, int cluster, int threads) {
+    if (cluster == 0) {  // flat per-step kernels: 256 threads per CTA
+        if (threads != 256) return fail(FDTD_ERR_INVALID, "the flat form (cluster 0) runs 256 threads per CTA");
+        b->cluster = 0;
+        b->threads = 256;
+        b->n_clusters = 0;
+        return FDTD_OK;
+    }
     if (!batch_threads_supported(threads) || (cluster != 1 && cluster != 2 && cluster != 4 && cluster != 8))
-        return fail(FDTD_ERR_INVALID, "cluster size 1, 2, 4 or 8 and 128, 256 or 512 threads per CTA");
+        return fail(FDTD_ERR_INVALID, "cluster size 0 (flat), 1, 2, 4 or 8 and 128, 256 or 512 threads per CTA");
     int n = 0;
     CUDA_TRY(batch_max_clusters(cluster, threads, &n));
     if (n < 1) return fail(FDTD_ERR_CUDA, "no cluster of this shape fits on the device");
@@ -1401,28 +1413,56 @@ int batch_set_config(fdtd_batch* b, int cluster, int threads) {
     return FDTD_OK;
 }
 
-// Run `steps` steps on every instance (refresh, one graph launch), then advance the step counters.
+// The captured launch of `steps` steps under the current configuration (captured on first use).
+int batch_graph(fdtd_batch* b, long long steps, cudaGraphExec_t* out) {
+    const int cfg[3] = {b->cluster, b->threads, b->n_clusters};
+    for (auto& G : b->graphs)
+        if (G.steps == steps && std::equal(cfg, cfg + 3, G.cfg)) {
+            *out = G.exec;
+            return FDTD_OK;
+        }
+    if (b->graphs.size() >= 4) batch_drop_graph(b);
+    CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = b->cluster == 0
+                        ? launch_batch_flat(b->d_inst, (int)b->hs.size(), b->d_items, b->n_items, steps, b->stream)
+                        : launch_batch(b->d_inst, b->d_order, (int)b->hs.size(), b->d_queue, steps, b->cluster,
+                                       b->threads, b->n_clusters, b->stream);
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return fail(FDTD_ERR_CUDA, std::string("batch graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+    }
+    fdtd_batch::Graph G{steps, {cfg[0], cfg[1], cfg[2]}, g, nullptr};
+    if (cudaGraphInstantiate(&G.exec, g, 0) != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return fail(FDTD_ERR_CUDA, "batch graph instantiation");
+    }
+    b->graphs.push_back(G);
+    *out = G.exec;
+    return FDTD_OK;
+}
+
+// Run `steps` steps on every instance (refresh, graph launches), then advance the step counters.
+// The persistent form is one launch of `steps` steps; the flat form replays a graph of
+// kFlatChunk steps (three kernels per step) and one of the remainder.
+constexpr long long kFlatChunk = 32;
 int batch_run(fdtd_batch* b, long long steps) {
     int rc = batch_refresh(b);
     if (rc) return rc;
-    const int cfg[3] = {b->cluster, b->threads, b->n_clusters};
-    if (b->graph_steps != steps || !std::equal(cfg, cfg + 3, b->graph_cfg)) {
-        batch_drop_graph(b);
-        CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-        cudaError_t e = launch_batch(b->d_inst, b->d_order, (int)b->hs.size(), b->d_queue, steps, b->cluster, b->threads,
-                                     b->n_clusters, b->stream);
-        cudaGraph_t g = nullptr;
-        cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
-        if (e != cudaSuccess || e2 != cudaSuccess) {
-            if (g) cudaGraphDestroy(g);
-            return fail(FDTD_ERR_CUDA, std::string("batch graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+    cudaGraphExec_t ex = nullptr;
+    if (b->cluster == 0) {
+        const long long chunk = std::min(steps, kFlatChunk), full = steps / chunk, rem = steps % chunk;
+        if ((rc = batch_graph(b, chunk, &ex))) return rc;
+        for (long long q = 0; q < full; ++q) CUDA_TRY(cudaGraphLaunch(ex, b->stream));
+        if (rem) {
+            if ((rc = batch_graph(b, rem, &ex))) return rc;
+            CUDA_TRY(cudaGraphLaunch(ex, b->stream));
         }
-        b->graph = g;
-        CUDA_TRY(cudaGraphInstantiate(&b->exec, b->graph, 0));
-        b->graph_steps = steps;
-        std::copy(cfg, cfg + 3, b->graph_cfg);
+    } else {
+        if ((rc = batch_graph(b, steps, &ex))) return rc;
+        CUDA_TRY(cudaGraphLaunch(ex, b->stream));
     }
-    CUDA_TRY(cudaGraphLaunch(b->exec, b->stream));
     for (fdtd_handle* h : b->hs) h->step += steps;
     return FDTD_OK;
 }
@@ -1459,7 +1499,21 @@ extern "C" int fdtd_batch_create(fdtd_handle* const* handles, int32_t n, fdtd_ba
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return vol(b->hs[x]) > vol(b->hs[y]); });
     if (cudaMemcpy(b->d_order, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice) != cudaSuccess)
         return cleanup(fail(FDTD_ERR_CUDA, "batch order upload"));
-    int rc = batch_set_config(b, 4, 256);
+    // flat form: every 32 x 8 block of every plane of every instance
+    std::vector<int4> items;
+    for (int q = 0; q < n; ++q) {
+        const DeviceGrid& g = b->hs[q]->g;
+        for (int k = 0; k < g.nz; ++k)
+            for (int y0 = 0; y0 < g.ny; y0 += 8)
+                for (int x0 = 0; x0 < g.nx; x0 += 32) items.push_back(make_int4(q, x0, y0, k));
+    }
+    if (items.size() > (size_t)INT32_MAX) return cleanup(fail(FDTD_ERR_INVALID, "batch too large for the flat form"));
+    b->n_items = (int)items.size();
+    if (cudaMalloc((void**)&b->d_items, sizeof(int4) * std::max<size_t>(items.size(), 1)) != cudaSuccess)
+        return cleanup(fail(FDTD_ERR_OOM, "batch work list"));
+    if (cudaMemcpy(b->d_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        return cleanup(fail(FDTD_ERR_CUDA, "batch work list upload"));
+    int rc = batch_set_config(b, 0, 256);
     if (rc) return cleanup(rc);
     *out = b;
     return FDTD_OK;
@@ -1473,6 +1527,7 @@ extern "C" int fdtd_batch_destroy(fdtd_batch* b) {
     cudaFree(b->d_inst);
     cudaFree(b->d_order);
     cudaFree(b->d_queue);
+    cudaFree(b->d_items);
     delete b;
     return FDTD_OK;
 }
@@ -1540,7 +1595,7 @@ extern "C" int fdtd_batch_tune(fdtd_batch* b, int64_t steps, double* best_ms) {
         if (rc) { restore_all(); return rc; }
         steps0[q] = h->step;
     }
-    const int clusters[4] = {1, 2, 4, 8}, threads[3] = {128, 256, 512};
+    const int clusters[5] = {0, 1, 2, 4, 8}, threads[3] = {128, 256, 512};
     double best = 1e300;
     int best_c = b->cluster, best_t = b->threads;
     cudaEvent_t e0, e1;
@@ -1549,6 +1604,7 @@ extern "C" int fdtd_batch_tune(fdtd_batch* b, int64_t steps, double* best_ms) {
     int rc = FDTD_OK;
     for (int c : clusters) {
         for (int t : threads) {
+            if (c == 0 && t != 256) continue;
             if (batch_set_config(b, c, t) != FDTD_OK) continue;  // shape does not fit: skip it
             cudaEventRecord(e0, b->stream);
             if ((rc = batch_run(b, steps))) break;

@@ -448,7 +448,8 @@ class Batch:
         return {"cluster": c.value, "threads": t.value, "n_clusters": n.value}
 
     def tune(self, steps: int = 10) -> float:
-        """Autotune the cluster and CTA size on `steps` steps (states restored); returns the best time."""
+        """Autotune the form (flat, or persistent with its cluster and CTA size) on `steps` steps
+        (states restored); returns the best time."""
         ms = ctypes.c_double(0.0)
         _check(_lib.fdtd_batch_tune(self._b, steps, ctypes.byref(ms)))
         return ms.value

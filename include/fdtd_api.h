@@ -252,11 +252,14 @@ int fdtd_adjoint_forward(fdtd_handle* h, int64_t n, int32_t checkpoint_every, in
  * the host array `grad` (shaped like eps_r). The handle ends in the state the forward left. */
 int fdtd_adjoint_backward(fdtd_handle* h, double* grad);
 
-/* ---- Batched persistent launch (no reference counterpart: the reference runs one domain per
- * process). A batch advances many independent handles of any sizes with one kernel launch per
- * fdtd_batch_step, captured in a CUDA graph: each instance is owned by a thread-block cluster
- * for all of its steps (E update, cluster barrier, H update, cluster barrier), instances are taken
- * longest first from a queue, and every instance produces the bits fdtd_step would produce. ---- */
+/* ---- Batched launch (no reference counterpart: the reference runs one domain per process). A
+ * batch advances many independent handles of any sizes together, its launches captured in CUDA
+ * graphs, in one of two forms: flat (cluster 0, the default): per step one E kernel and one H
+ * kernel over the 32 x 8 blocks of every plane of every instance, one node per thread;
+ * persistent (cluster 1, 2, 4 or 8): one kernel for all steps, each instance owned by a
+ * thread-block cluster for all of its steps (E update, cluster barrier, H update, cluster
+ * barrier), instances taken longest first from a queue. Every instance produces the bits
+ * fdtd_step would produce. ---- */
 typedef struct fdtd_batch fdtd_batch;
 
 /* A batch over n distinct handles on the current device (none with a design region). The handles
@@ -268,13 +271,15 @@ int fdtd_batch_destroy(fdtd_batch* b);
 /* Stream of the batch launches: a created stream, not the legacy default stream (the launch is
  * captured in a CUDA graph). By default the batch uses a stream of its own. */
 int fdtd_batch_set_stream(fdtd_batch* b, void* stream);
-/* Cluster size (1, 2, 4 or 8 CTAs per instance) and CTA size (128, 256 or 512 threads). */
+/* Form and shape: cluster 0 = flat (256 threads per CTA), or the persistent form's cluster size
+ * (1, 2, 4 or 8 CTAs per instance) with its CTA size (128, 256 or 512 threads). */
 int fdtd_batch_set_config(fdtd_batch* b, int32_t cluster, int32_t threads);
 int fdtd_batch_get_config(const fdtd_batch* b, int32_t* cluster, int32_t* threads, int32_t* n_clusters);
-/* Autotuner: times `steps` steps of the whole batch for every cluster and CTA size, restores every
- * instance's state after each trial, keeps the fastest shape (its time in *best_ms if not NULL). */
+/* Autotuner: times `steps` steps of the whole batch in the flat form and for every cluster and CTA
+ * size of the persistent form, restores every instance's state after each trial, keeps the
+ * fastest (its time in *best_ms if not NULL). */
 int fdtd_batch_tune(fdtd_batch* b, int64_t steps, double* best_ms);
-/* Advance every instance by `steps` steps (one graph launch, asynchronous on the batch stream). */
+/* Advance every instance by `steps` steps (graph launches, asynchronous on the batch stream). */
 int fdtd_batch_step(fdtd_batch* b, int64_t steps);
 /* Wait for the batch stream; FDTD_ERR_DEVICE if an instance's kernel reported an error. */
 int fdtd_batch_synchronize(fdtd_batch* b);

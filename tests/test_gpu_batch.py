@@ -1,5 +1,6 @@
-"""Batched persistent launch: every instance equals its own sequential run bit for bit, for every
-cluster / CTA shape, after autotuning, and when handles are also stepped on their own."""
+"""Batched launch: every instance equals its own sequential run bit for bit, in the flat form and
+for every cluster / CTA shape of the persistent form, after autotuning, and when handles are also
+stepped on their own."""
 import numpy as np
 import pytest
 
@@ -48,7 +49,7 @@ def same(a, b):
     return all(bitwise_equal(x[0], y[0]) and bitwise_equal(x[1], y[1]) for x, y in zip(a, b))
 
 
-@pytest.mark.parametrize("config", [(1, 256), (2, 128), (4, 256), (8, 512)])
+@pytest.mark.parametrize("config", [(0, 256), (1, 256), (2, 128), (4, 256), (8, 512)])
 def test_batch_equals_sequential(gpu_lib, config):
     scs = instances()
     assert same(batched(scs, [25, 35], config), sequential(scs, 60))
