@@ -21,6 +21,9 @@ constexpr float kTiny = 1.2e-38f;  // setZero's initial value for fields, psi an
 constexpr int kMaxMaterials = 256;
 constexpr int kDefaultEntry = kMaxMaterials;  // H coefficient of faces the reference never averages
 constexpr int kGeneral = 255;                 // node class of nodes that take the general path
+constexpr int kUniformGeneral = 128;         // classes below: fast-path nodes (the material id);
+                                             // kUniformGeneral + m: general nodes whose seven cells
+                                             // all hold material m (m < kDesignNode - kUniformGeneral)
 constexpr int kPlateNode = 254;              // node class of nodes with a plate-covered E edge
 constexpr int kDesignNode = 253;              // node class of the design region's edge box; classes
                                               // below it are fast-path material ids

@@ -31,20 +31,24 @@ __device__ __forceinline__ void e_node_global(const StepParams& p, const FieldPt
     nb.hz_jm = j > 0 ? fi.hz[n - R] : 0.f;
     const int c = kDesign ? kGeneral : p.cls[n];
     float out[3], pre[3];
-    if (c < kDesignNode) {
+    if (c < kUniformGeneral) {
         e_update_interior(p, c, nb.ex, nb.ey, nb.ez, __fsub_rn(nb.hz, nb.hz_jm), __fsub_rn(nb.hy, nb.hy_km),
                           __fsub_rn(nb.hx, nb.hx_km), __fsub_rn(nb.hz, nb.hz_im), __fsub_rn(nb.hy, nb.hy_im),
                           __fsub_rn(nb.hx, nb.hx_jm), out);
         pre[0] = out[0]; pre[1] = out[1]; pre[2] = out[2];
     } else {
-        const uint8_t* mat = p.mat;
-        nb.m0 = mat[n];
-        nb.mi = i > 0 ? mat[n - 1] : 0;
-        nb.mj = j > 0 ? mat[n - R] : 0;
-        nb.mk = k > 0 ? mat[n - P] : 0;
-        nb.mij = (i > 0 && j > 0) ? mat[n - 1 - R] : 0;
-        nb.mik = (i > 0 && k > 0) ? mat[n - 1 - P] : 0;
-        nb.mjk = (j > 0 && k > 0) ? mat[n - R - P] : 0;
+        if (c >= kUniformGeneral && c < kDesignNode) {  // seven cells of one material: no loads
+            nb.m0 = nb.mi = nb.mj = nb.mk = nb.mij = nb.mik = nb.mjk = c - kUniformGeneral;
+        } else {
+            const uint8_t* mat = p.mat;
+            nb.m0 = mat[n];
+            nb.mi = i > 0 ? mat[n - 1] : 0;
+            nb.mj = j > 0 ? mat[n - R] : 0;
+            nb.mk = k > 0 ? mat[n - P] : 0;
+            nb.mij = (i > 0 && j > 0) ? mat[n - 1 - R] : 0;
+            nb.mik = (i > 0 && k > 0) ? mat[n - 1 - P] : 0;
+            nb.mjk = (j > 0 && k > 0) ? mat[n - R - P] : 0;
+        }
         // plate nodes are k_plate_e's, CPML memory included: the other kernels store nothing of them
         const PsiIO io{pin.f, pout.f, kPlate || c != kPlateNode};
         const bool plane_lumped = p.lumped_k[k] < p.lumped_k[k + 1];
@@ -78,17 +82,21 @@ __device__ __forceinline__ void h_node_global(const StepParams& p, const FieldPt
     nb.ey_ip = i < g.nx - 1 ? fe.ey[n + 1] : 0.f;
     const int c = p.cls[n];
     float out[3], pre[3];
-    if (c < kDesignNode) {
+    if (c < kUniformGeneral) {
         h_update_interior(p, c, nb.hx, nb.hy, nb.hz, __fsub_rn(nb.ey_kp, nb.ey), __fsub_rn(nb.ez_jp, nb.ez),
                           __fsub_rn(nb.ez_ip, nb.ez), __fsub_rn(nb.ex_kp, nb.ex), __fsub_rn(nb.ex_jp, nb.ex),
                           __fsub_rn(nb.ey_ip, nb.ey), out);
         pre[0] = out[0]; pre[1] = out[1]; pre[2] = out[2];
     } else {
-        const uint8_t* mat = p.mat;
-        nb.m0 = mat[n];
-        nb.mi = i > 0 ? mat[n - 1] : 0;
-        nb.mj = j > 0 ? mat[n - R] : 0;
-        nb.mk = k > 0 ? mat[n - P] : 0;
+        if (c >= kUniformGeneral && c < kDesignNode) {
+            nb.m0 = nb.mi = nb.mj = nb.mk = c - kUniformGeneral;
+        } else {
+            const uint8_t* mat = p.mat;
+            nb.m0 = mat[n];
+            nb.mi = i > 0 ? mat[n - 1] : 0;
+            nb.mj = j > 0 ? mat[n - R] : 0;
+            nb.mk = k > 0 ? mat[n - P] : 0;
+        }
         const PsiIO io{pin.f, pout.f, true};
         h_update<kCoherent>(p, nb, i, j, k, io, out, pre);
     }

@@ -207,7 +207,9 @@ cudaError_t launch_paint(uint8_t* mat, const DeviceGrid& g, const int box[6], ui
 
 namespace fdtd {
 
-// Node class (StepParams::cls): material id of nodes that take the fast path, kGeneral otherwise.
+// Node class (StepParams::cls): material id of nodes that take the fast path (interior, seven cells
+// of one material below kUniformGeneral), kUniformGeneral + m for the other nodes whose seven cells
+// all hold material m, kGeneral otherwise.
 // The seven cells are those the three E edge averages read, (i,j,k) (i-1,j,k) (i,j-1,k) (i,j,k-1)
 // (i-1,j-1,k) (i-1,j,k-1) (i,j-1,k-1); the four cells of the H faces are among them.
 // Nodes of the design region's edge box [dlo, dhi] get kDesignNode.
@@ -219,12 +221,19 @@ __global__ void k_node_class(const uint8_t* __restrict__ mat, uint8_t* __restric
     if (i >= g.nx || j >= g.ny) return;
     const long long n = (long long)k * g.plane + (long long)j * g.pitch + i;
     uint8_t c = kGeneral;
-    if (interior(i, g.nx, g.pxn, g.pxp) && interior(j, g.ny, g.pyn, g.pyp) && interior(k, g.nz, g.pzn, g.pzp)) {
-        const long long R = g.pitch, P = g.plane;
-        const uint8_t m0 = mat[n];
-        if (mat[n - 1] == m0 && mat[n - R] == m0 && mat[n - P] == m0 && mat[n - 1 - R] == m0 && mat[n - 1 - P] == m0 &&
-            mat[n - R - P] == m0)
-            c = m0 < kDesignNode ? m0 : kGeneral;  // material ids from kDesignNode up stay general
+    // the seven cells as the general path reads them (cells outside the grid count as material 0)
+    const long long R = g.pitch, P = g.plane;
+    const int m0 = mat[n];
+    const int mi = i > 0 ? mat[n - 1] : 0, mj = j > 0 ? mat[n - R] : 0, mk = k > 0 ? mat[n - P] : 0;
+    const int mij = (i > 0 && j > 0) ? mat[n - 1 - R] : 0, mik = (i > 0 && k > 0) ? mat[n - 1 - P] : 0;
+    const int mjk = (j > 0 && k > 0) ? mat[n - R - P] : 0;
+    const bool uniform = mi == m0 && mj == m0 && mk == m0 && mij == m0 && mik == m0 && mjk == m0;
+    if (uniform) {
+        if (interior(i, g.nx, g.pxn, g.pxp) && interior(j, g.ny, g.pyn, g.pyp) && interior(k, g.nz, g.pzn, g.pzp) &&
+            m0 < kUniformGeneral)
+            c = (uint8_t)m0;  // fast path
+        else if (m0 < kDesignNode - kUniformGeneral)
+            c = (uint8_t)(kUniformGeneral + m0);  // general path without the cell-material loads
     }
     if (i >= dlo.x && i <= dhi.x && j >= dlo.y && j <= dhi.y && k >= dlo.z && k <= dhi.z) c = kDesignNode;
     cls[n] = c;

@@ -193,7 +193,7 @@ __device__ __forceinline__ float3 e_fast(const StepParams& p, const EIn& a) {
                        upd3(z.x, a.ez, z.y, a.dHy_i, z.z, a.dHx_j));
 }
 __device__ __forceinline__ float3 e_any(const StepParams& p, const EIn& a, int i, int j, int k, long long m, int lumped) {
-    if (a.c < kDesignNode) return e_fast(p, a);
+    if (a.c < kUniformGeneral) return e_fast(p, a);
     return e_slow(&p, i, j, k, m, lumped, a.ex, a.ey, a.ez, a.dHz_j, a.dHy_k, a.dHx_k, a.dHz_i, a.dHy_i, a.dHx_j);
 }
 
@@ -220,7 +220,7 @@ __device__ __forceinline__ float3 h_fast(const StepParams& p, const HIn& a) {
                        upd3(z.x, a.hz, z.y, a.dEx_j, z.z, a.dEy_i));
 }
 __device__ __forceinline__ float3 h_any(const StepParams& p, const HIn& a, int i, int j, int k) {
-    if (a.c < kDesignNode) return h_fast(p, a);
+    if (a.c < kUniformGeneral) return h_fast(p, a);
     return h_slow(&p, i, j, k, a.hx, a.hy, a.hz, a.dEy_k, a.dEz_j, a.dEz_i, a.dEx_k, a.dEx_j, a.dEy_i);
 }
 
@@ -294,7 +294,7 @@ k_sweep_interior(const __grid_constant__ FusedMaps maps, const __grid_constant__
             const EIn a0 = e_load(cur, prv, hi, ei, mi);
             const EIn a1 = e_load(cur, prv, hi + RSTEP * HW, ei + RSTEP * EW, mi + RSTEP * MW);
             float3 v0, v1;
-            if (a0.c < kDesignNode && a1.c < kDesignNode) {
+            if (a0.c < kUniformGeneral && a1.c < kUniformGeneral) {
                 v0 = e_fast(p, a0);
                 v1 = e_fast(p, a1);
             } else {
@@ -326,7 +326,7 @@ k_sweep_interior(const __grid_constant__ FusedMaps maps, const __grid_constant__
             const HIn a0 = h_load(prv, en_prv, en_cur, hi, mi, ni);
             const HIn a1 = h_load(prv, en_prv, en_cur, hi + RSTEP * HW, mi + RSTEP * MW, ni + RSTEP * NW);
             float3 v0, v1;
-            if (a0.c < kDesignNode && a1.c < kDesignNode) {
+            if (a0.c < kUniformGeneral && a1.c < kUniformGeneral) {
                 v0 = h_fast(p, a0);
                 v1 = h_fast(p, a1);
             } else {
