@@ -61,7 +61,12 @@ __device__ __forceinline__ long long node(const DeviceGrid& g, int i, int j, int
 // ---- transpose of calc_h (h_update) -------------------------------------------------------
 // G_E slots (written by k_adj_e): 0 Ex->Hz, 1 Ex->Hy, 2 Ey->Hx, 3 Ey->Hz, 4 Ez->Hy, 5 Ez->Hx.
 // G_H slots (written here):        0 Hx->Ey, 1 Hx->Ez, 2 Hy->Ez, 3 Hy->Ex, 4 Hz->Ex, 5 Hz->Ey.
-__global__ void __launch_bounds__(256) k_adj_h(const __grid_constant__ StepParams p, AdjState a,
+// 5 CTAs of 256 per SM (48 registers; k_adj_e spills a few words): measured 14 % faster for the
+// reverse sweep at 128^3 than the compiler's own 80 registers (3 CTAs).
+#ifndef FDTD_ADJ_MIN_BLOCKS
+#define FDTD_ADJ_MIN_BLOCKS 5
+#endif
+__global__ void __launch_bounds__(256, FDTD_ADJ_MIN_BLOCKS) k_adj_h(const __grid_constant__ StepParams p, AdjState a,
                                                const __grid_constant__ PsiSet psa) {
     const DeviceGrid& g = p.g;
     const int i = blockIdx.x * 32 + threadIdx.x;
@@ -118,7 +123,7 @@ __global__ void __launch_bounds__(256) k_adj_h(const __grid_constant__ StepParam
 }
 
 // ---- transpose of calc_e (e_update), FoM source and design gradient ------------------------
-__global__ void __launch_bounds__(256) k_adj_e(const __grid_constant__ StepParams p, AdjState a,
+__global__ void __launch_bounds__(256, FDTD_ADJ_MIN_BLOCKS) k_adj_e(const __grid_constant__ StepParams p, AdjState a,
                                                const __grid_constant__ PsiSet psa, AdjStep st) {
     const DeviceGrid& g = p.g;
     const int i = blockIdx.x * 32 + threadIdx.x;

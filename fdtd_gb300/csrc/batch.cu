@@ -72,7 +72,11 @@ k_batch(BatchInstance* __restrict__ inst, const int* __restrict__ order, int n_i
 // copies its instance's descriptor to shared memory first. The GPU is filled by all instances
 // at once with one node per thread, as in the two-pass schedule, instead of a cluster marching
 // through one instance; the per-node updates are the same, so the bits are too.
-__global__ void __launch_bounds__(256) k_batch_flat_e(const BatchInstance* __restrict__ inst,
+// 6 CTAs of 256 per SM (40 registers), as the two-pass kernels
+#ifndef FDTD_BATCH_FLAT_MIN_BLOCKS
+#define FDTD_BATCH_FLAT_MIN_BLOCKS 6
+#endif
+__global__ void __launch_bounds__(256, FDTD_BATCH_FLAT_MIN_BLOCKS) k_batch_flat_e(const BatchInstance* __restrict__ inst,
                                                       const int4* __restrict__ items) {
     __shared__ __align__(16) BatchInstance s;
     const int4 it = items[blockIdx.x];
@@ -87,7 +91,7 @@ __global__ void __launch_bounds__(256) k_batch_flat_e(const BatchInstance* __res
     if (i < s.p.g.nx && j < s.p.g.ny) e_node_global(s.p, s.f, s.f, s.ps, s.ps, i, j, it.w, s.step);
 }
 
-__global__ void __launch_bounds__(256) k_batch_flat_h(const BatchInstance* __restrict__ inst,
+__global__ void __launch_bounds__(256, FDTD_BATCH_FLAT_MIN_BLOCKS) k_batch_flat_h(const BatchInstance* __restrict__ inst,
                                                       const int4* __restrict__ items) {
     __shared__ __align__(16) BatchInstance s;
     const int4 it = items[blockIdx.x];
