@@ -1215,7 +1215,9 @@ int adj_prepare(fdtd_handle* h, long long n, int K) {
         A.psa.f[f].e[0] = arr[0]; A.psa.f[f].e[1] = arr[1]; A.psa.f[f].h[0] = arr[2]; A.psa.f[f].h[1] = arr[3];
     }
     const long long ne = edge_box_volume(h->dbox);
-    A.hist_slots = K > 0 ? K + 1 : n + 1;
+    // K > 0: two segments of snapshots, so that the backward recomputes one segment while it
+    // reverses the next
+    A.hist_slots = K > 0 ? 2 * ((long long)K + 1) : n + 1;
     A.ckpt_slots = K > 0 ? (n + K - 1) / K + 1 : 1;  // + the final state
     const size_t nd = (size_t)(h->dbox[3] - h->dbox[0]) * (h->dbox[4] - h->dbox[1]) * (h->dbox[5] - h->dbox[2]);
     if ((rc = adj_alloc(h, (void**)&A.samples, sizeof(float) * (size_t)std::max<long long>(n, 1))) ||
@@ -1314,20 +1316,60 @@ extern "C" int fdtd_adjoint_backward(fdtd_handle* h, double* grad) {
         for (long long m = A.n - 1; m >= 0; --m)
             if ((rc = reverse(m, adj_slot(h, m), adj_slot(h, m + 1)))) return rc;
     } else {
+        // Segments are recomputed on the handle's stream (forward fields) and reversed on a second
+        // stream (adjoint state), one segment apart: the recompute of segment sg - 1 runs while
+        // segment sg is reversed. Snapshot buffers alternate by segment parity; events order a
+        // reversal after its recompute and a recompute after the reversal that last read its
+        // buffer.
         const long long nseg = (A.n + A.K - 1) / A.K;
-        for (long long sg = nseg - 1; sg >= 0; --sg) {
-            // recompute the segment from its checkpoint, keeping the design E of every step
-            if ((rc = state_copy(h, adj_ckpt(h, sg), false))) return rc;
+        const long long half = (long long)A.K + 1;
+        auto slot = [&](long long sg, long long t) { return adj_slot(h, (sg & 1) * half + t); };
+        struct Sync {
+            cudaStream_t rev = nullptr;
+            cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // rec[2], rev[2], start
+            ~Sync() {
+                for (cudaEvent_t e : ev)
+                    if (e) cudaEventDestroy(e);
+                if (rev) cudaStreamDestroy(rev);
+            }
+        } S;
+        CUDA_TRY(cudaStreamCreateWithFlags(&S.rev, cudaStreamNonBlocking));
+        for (cudaEvent_t& e : S.ev) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        cudaEvent_t* ev_rec = S.ev;
+        cudaEvent_t* ev_rev = S.ev + 2;
+        CUDA_TRY(cudaEventRecord(S.ev[4], h->stream));  // the adjoint state is cleared
+        CUDA_TRY(cudaStreamWaitEvent(S.rev, S.ev[4], 0));
+        auto recompute = [&](long long sg) -> int {
+            int r = state_copy(h, adj_ckpt(h, sg), false);
+            if (r) return r;
             h->step = A.start + sg * A.K;
             const long long len = std::min<long long>(A.K, A.n - sg * A.K);
             const int c = h->cur;
             CUDA_TRY(launch_after_step(h->field[c][0], h->field[c][1], h->field[c][2], h->g, A.probe, nullptr, h->dbox,
-                                       adj_slot(h, 0), h->stream));
+                                       slot(sg, 0), h->stream));
             for (long long t = 0; t < len; ++t)
-                if ((rc = adj_forward_step(h, nullptr, adj_slot(h, t + 1)))) return rc;
-            for (long long t = len - 1; t >= 0; --t)
-                if ((rc = reverse(sg * A.K + t, adj_slot(h, t), adj_slot(h, t + 1)))) return rc;
+                if ((r = adj_forward_step(h, nullptr, slot(sg, t + 1)))) return r;
+            CUDA_TRY(cudaEventRecord(ev_rec[sg & 1], h->stream));
+            return FDTD_OK;
+        };
+        if ((rc = recompute(nseg - 1))) return rc;
+        for (long long sg = nseg - 1; sg >= 0; --sg) {
+            CUDA_TRY(cudaStreamWaitEvent(S.rev, ev_rec[sg & 1], 0));
+            const long long len = std::min<long long>(A.K, A.n - sg * A.K);
+            for (long long t = len - 1; t >= 0; --t) {
+                const AdjStep st{A.probe, two_dt * A.host_samples[(size_t)(sg * A.K + t)], A.acc, slot(sg, t), slot(sg, t + 1)};
+                CUDA_TRY(launch_adj_step(p, A.st, A.psa, st, S.rev));
+            }
+            CUDA_TRY(cudaEventRecord(ev_rev[sg & 1], S.rev));
+            if (sg > 0) {
+                // segment sg - 1 reuses the buffers segment sg + 1 was reversed from
+                if (sg + 1 < nseg) CUDA_TRY(cudaStreamWaitEvent(h->stream, ev_rev[(sg + 1) & 1], 0));
+                if ((rc = recompute(sg - 1))) return rc;
+            }
         }
+        CUDA_TRY(cudaEventRecord(S.ev[4], S.rev));
+        CUDA_TRY(cudaStreamWaitEvent(h->stream, S.ev[4], 0));
+        CUDA_TRY(cudaStreamSynchronize(S.rev));
     }
     CUDA_TRY(launch_grad_finalize(A.acc, h->dbox, A.grad, h->stream));
     const size_t nd = (size_t)(h->dbox[3] - h->dbox[0]) * (h->dbox[4] - h->dbox[1]) * (h->dbox[5] - h->dbox[2]);
