@@ -88,7 +88,8 @@ __global__ void __launch_bounds__(256, FDTD_BATCH_FLAT_MIN_BLOCKS) k_batch_flat_
     }
     __syncthreads();
     const int i = it.y + (int)threadIdx.x, j = it.z + (int)threadIdx.y;
-    if (i < s.p.g.nx && j < s.p.g.ny) e_node_global(s.p, s.f, s.f, s.ps, s.ps, i, j, it.w, s.step);
+    // instances are small enough for 32-bit node offsets (checked when the batch is created)
+    if (i < s.p.g.nx && j < s.p.g.ny) e_node_global<false, false, false, uint32_t>(s.p, s.f, s.f, s.ps, s.ps, i, j, it.w, s.step);
 }
 
 __global__ void __launch_bounds__(256, FDTD_BATCH_FLAT_MIN_BLOCKS) k_batch_flat_h(const BatchInstance* __restrict__ inst,
@@ -103,7 +104,7 @@ __global__ void __launch_bounds__(256, FDTD_BATCH_FLAT_MIN_BLOCKS) k_batch_flat_
     }
     __syncthreads();
     const int i = it.y + (int)threadIdx.x, j = it.z + (int)threadIdx.y;
-    if (i < s.p.g.nx && j < s.p.g.ny) h_node_global(s.p, s.f, s.f, s.f, s.ps, s.ps, i, j, it.w, s.step);
+    if (i < s.p.g.nx && j < s.p.g.ny) h_node_global<false, uint32_t>(s.p, s.f, s.f, s.f, s.ps, s.ps, i, j, it.w, s.step);
 }
 
 __global__ void k_batch_advance(BatchInstance* inst, int n) {

@@ -1545,6 +1545,8 @@ extern "C" int fdtd_batch_create(fdtd_handle* const* handles, int32_t n, fdtd_ba
     std::vector<int4> items;
     for (int q = 0; q < n; ++q) {
         const DeviceGrid& g = b->hs[q]->g;
+        if (g.plane * (long long)(g.nz + 1) >= (1LL << 31))
+            return cleanup(fail(FDTD_ERR_INVALID, "batch instances must hold fewer than 2^31 nodes"));
         for (int k = 0; k < g.nz; ++k)
             for (int y0 = 0; y0 < g.ny; y0 += 8)
                 for (int x0 = 0; x0 < g.nx; x0 += 32) items.push_back(make_int4(q, x0, y0, k));

@@ -14,12 +14,14 @@ namespace fdtd {
 // e_update / h_update. kDesign (k_design_e only): skip the class test and average the per-cell
 // eps_r of design cells. kPlate (k_plate_e only): plate-covered edges take the plate's sigma_e;
 // the other kernels leave plate nodes (class kPlateNode) alone, CPML memory included.
-template <bool kDesign = false, bool kCoherent = false, bool kPlate = false>
+// Idx: the integer type of node offsets; uint32_t when the field arrays hold fewer than 2^31
+// elements, which saves the 64-bit address arithmetic of every load and store.
+template <bool kDesign = false, bool kCoherent = false, bool kPlate = false, typename Idx = long long>
 __device__ __forceinline__ void e_node_global(const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo,
                                               const PsiSet& pin, const PsiSet& pout, int i, int j, int k, long long m) {
     const DeviceGrid& g = p.g;
-    const long long n = (long long)k * g.plane + (long long)j * g.pitch + i;
-    const long long P = g.plane, R = g.pitch;
+    const Idx n = (Idx)k * (Idx)g.plane + (Idx)j * (Idx)g.pitch + (Idx)i;
+    const Idx P = (Idx)g.plane, R = (Idx)g.pitch;
     ENbr nb;
     nb.ex = fi.ex[n]; nb.ey = fi.ey[n]; nb.ez = fi.ez[n];
     nb.hx = fi.hx[n]; nb.hy = fi.hy[n]; nb.hz = fi.hz[n];
@@ -64,13 +66,13 @@ __device__ __forceinline__ void e_node_global(const StepParams& p, const FieldPt
 }
 
 // H reads the old H from `fi` and the new E from `fe`.
-template <bool kCoherent = false>
+template <bool kCoherent = false, typename Idx = long long>
 __device__ __forceinline__ void h_node_global(const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fe,
                                               const FieldPtrs& fo, const PsiSet& pin, const PsiSet& pout, int i, int j,
                                               int k, long long m) {
     const DeviceGrid& g = p.g;
-    const long long n = (long long)k * g.plane + (long long)j * g.pitch + i;
-    const long long P = g.plane, R = g.pitch;
+    const Idx n = (Idx)k * (Idx)g.plane + (Idx)j * (Idx)g.pitch + (Idx)i;
+    const Idx P = (Idx)g.plane, R = (Idx)g.pitch;
     HNbr nb;
     nb.hx = fi.hx[n]; nb.hy = fi.hy[n]; nb.hz = fi.hz[n];
     nb.ex = fe.ex[n]; nb.ey = fe.ey[n]; nb.ez = fe.ez[n];

@@ -16,49 +16,59 @@ namespace fdtd {
 #ifndef FDTD_SHELL_MIN_BLOCKS
 #define FDTD_SHELL_MIN_BLOCKS 6
 #endif
+template <typename Idx>
 __global__ void __launch_bounds__(256, FDTD_TWO_PASS_MIN_BLOCKS) k_update_e(const __grid_constant__ StepParams p, FieldPtrs f,
                                                   const __grid_constant__ PsiSet ps, long long m) {
     const int i = blockIdx.x * 32 + threadIdx.x;
     const int j = blockIdx.y * 8 + threadIdx.y;
     if (i >= p.g.nx || j >= p.g.ny) return;
-    e_node_global(p, f, f, ps, ps, i, j, blockIdx.z, m);
+    e_node_global<false, false, false, Idx>(p, f, f, ps, ps, i, j, blockIdx.z, m);
 }
 
+template <typename Idx>
 __global__ void __launch_bounds__(256, FDTD_TWO_PASS_MIN_BLOCKS) k_update_h(const __grid_constant__ StepParams p, FieldPtrs f,
                                                   const __grid_constant__ PsiSet ps, long long m) {
     const int i = blockIdx.x * 32 + threadIdx.x;
     const int j = blockIdx.y * 8 + threadIdx.y;
     if (i >= p.g.nx || j >= p.g.ny) return;
-    h_node_global(p, f, f, f, ps, ps, i, j, blockIdx.z, m);
+    h_node_global<false, Idx>(p, f, f, f, ps, ps, i, j, blockIdx.z, m);
 }
 
 // Shell passes of the fused schedule: the nodes of the shell items (int4 {x0, y0, k, -}, a 32 x 8
 // block of plane k; x0, y0 may be negative) read buffer A (`fi`, `pin`) and write buffer B (`fo`,
 // `pout`), one node per thread as in the two-pass kernels. The E pass runs before the interior
 // sweep, the H pass after it, since H reads new E at interior nodes next to the shell.
+template <typename Idx>
 __global__ void __launch_bounds__(256, FDTD_SHELL_MIN_BLOCKS) k_shell_e(const __grid_constant__ StepParams p, FieldPtrs fi, FieldPtrs fo,
                                                  const __grid_constant__ PsiSet pin, const __grid_constant__ PsiSet pout,
                                                  const int4* __restrict__ items, long long m) {
     const int4 it = items[blockIdx.x];
     const int i = it.x + (int)threadIdx.x, j = it.y + (int)threadIdx.y;
     if (i < 0 || i >= p.g.nx || j < 0 || j >= p.g.ny) return;
-    e_node_global(p, fi, fo, pin, pout, i, j, it.z, m);
+    e_node_global<false, false, false, Idx>(p, fi, fo, pin, pout, i, j, it.z, m);
 }
 
+template <typename Idx>
 __global__ void __launch_bounds__(256, FDTD_SHELL_MIN_BLOCKS) k_shell_h(const __grid_constant__ StepParams p, FieldPtrs fi, FieldPtrs fo,
                                                  const __grid_constant__ PsiSet pin, const __grid_constant__ PsiSet pout,
                                                  const int4* __restrict__ items, long long m) {
     const int4 it = items[blockIdx.x];
     const int i = it.x + (int)threadIdx.x, j = it.y + (int)threadIdx.y;
     if (i < 0 || i >= p.g.nx || j < 0 || j >= p.g.ny) return;
-    h_node_global(p, fi, fo, fo, pin, pout, i, j, it.z, m);
+    h_node_global<false, Idx>(p, fi, fo, fo, pin, pout, i, j, it.z, m);
 }
 
 cudaError_t launch_shell(bool e_pass, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
                          const PsiSet& pout, const int4* items, int n_items, long long m, cudaStream_t st) {
     if (n_items <= 0) return cudaSuccess;
-    if (e_pass) k_shell_e<<<n_items, dim3(32, 8, 1), 0, st>>>(p, fi, fo, pin, pout, items, m);
-    else k_shell_h<<<n_items, dim3(32, 8, 1), 0, st>>>(p, fi, fo, pin, pout, items, m);
+    const dim3 b(32, 8, 1);
+    if (p.g.plane * (long long)(p.g.nz + 1) < (1LL << 31)) {
+        if (e_pass) k_shell_e<uint32_t><<<n_items, b, 0, st>>>(p, fi, fo, pin, pout, items, m);
+        else k_shell_h<uint32_t><<<n_items, b, 0, st>>>(p, fi, fo, pin, pout, items, m);
+    } else {
+        if (e_pass) k_shell_e<long long><<<n_items, b, 0, st>>>(p, fi, fo, pin, pout, items, m);
+        else k_shell_h<long long><<<n_items, b, 0, st>>>(p, fi, fo, pin, pout, items, m);
+    }
     return cudaGetLastError();
 }
 
@@ -107,11 +117,15 @@ cudaError_t launch_two_pass(const StepParams& p, const FieldPtrs& f, const PsiSe
                             cudaStream_t st) {
     dim3 block(32, 8, 1);
     dim3 grid((p.g.nx + 31) / 32, (p.g.ny + 7) / 8, p.g.nz);
-    k_update_e<<<grid, block, 0, st>>>(p, f, ps, m);
+    // 32-bit node offsets when every offset (plus one plane of lookahead) fits
+    const bool idx32 = p.g.plane * (long long)(p.g.nz + 1) < (1LL << 31);
+    if (idx32) k_update_e<uint32_t><<<grid, block, 0, st>>>(p, f, ps, m);
+    else k_update_e<long long><<<grid, block, 0, st>>>(p, f, ps, m);
     cudaError_t e = launch_design_e(p, f, f, ps, ps, m, st);
     if (e == cudaSuccess) e = launch_plate_e(p, f, f, ps, ps, m, st);
     if (e != cudaSuccess) return e;
-    k_update_h<<<grid, block, 0, st>>>(p, f, ps, m);
+    if (idx32) k_update_h<uint32_t><<<grid, block, 0, st>>>(p, f, ps, m);
+    else k_update_h<long long><<<grid, block, 0, st>>>(p, f, ps, m);
     return cudaGetLastError();
 }
 
