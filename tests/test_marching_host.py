@@ -1,0 +1,46 @@
+"""Host-side restatement of marchingLoop's set-up (no GPU): grid size, NZ rounding for NUMDEV,
+metre-to-index conversion and the scenario built from it."""
+import numpy as np
+
+import golden_scenarios as gs
+from fdtd_gb300 import scenario as S
+
+
+def test_indices_of_the_reduced_microstrip():
+    a = gs.marching_params()
+    ix = S.marching_indices(a)
+    # 40 x 60 x 6 cells + 2 x (4 air + 6 CPML) per axis
+    assert (ix["nx"], ix["ny"], ix["nz"]) == (60, 80, 26)
+    o = 10
+    assert ix["source"] == (o + 16, o, o, o + 22, o, o + 3)
+    assert ix["voltage"] == (o + 16, o + 10, o, o + 22, o + 10, o + 3)
+    assert ix["current"] == (o + 16, o + 10, o + 3, o + 22, o + 10, o + 3)
+    assert ix["pecs"][0] == (o, o, o, o + 40, o + 60, o)
+    assert ix["bricks"] == [(o, o, o, o + 40, o + 60, o + 3)]
+    assert ix["resistor"] is None
+
+
+def test_numdev_rounds_nz_up():
+    for numdev, nz in ((1, 26), (2, 26), (3, 27), (4, 28), (8, 32)):
+        assert S.marching_indices(gs.marching_params(numdev=numdev))["nz"] == nz
+
+
+def test_calc_index_rounds_half_away_from_zero_in_float():
+    d = np.float32(0.4e-3)
+    assert S.calc_index(np.float32(10) * d, d) == 10
+    assert S.calc_index(np.float32(2.5) * d, d) == 3
+    assert S.calc_index(-np.float32(2.5) * d, d) == -3
+    # 7.535e-3 / 0.389e-3 = 19.37 -> 19 (the reference driver's feed position)
+    assert S.calc_index(7.535e-3, np.float32(0.389e-3)) == 19
+
+
+def test_marching_scenario_structure():
+    a = gs.marching_params(resistor_opt=1)
+    wave = np.linspace(0, 1, a["n_t_steps"], dtype=np.float32)
+    sc, vbox, cbox = S.marching_scenario(a, wave)
+    assert len(sc.plates) == 3 and all(p.axis == 2 for p in sc.plates)
+    assert sc.plates[0].sigma_1 == 1e10
+    assert len(sc.materials) == 2 and abs(sc.materials[1].eps_r - 2.2) < 1e-6
+    assert len(sc.resistors) == 1 and sc.sources[0].resistance == 50.0
+    assert sc.pml == (6, 6, 6, 6, 6, 6)
+    assert vbox[2] < vbox[5]
