@@ -53,8 +53,12 @@ __device__ __forceinline__ void e_node_global(const StepParams& p, const FieldPt
         }
         // plate nodes are k_plate_e's, CPML memory included: the other kernels store nothing of them
         const PsiIO io{pin.f, pout.f, kPlate || c != kPlateNode};
-        const bool plane_lumped = p.lumped_k[k] < p.lumped_k[k + 1];
-        e_update<kDesign, kCoherent, kPlate>(p, nb, i, j, k, m, plane_lumped, io, out, pre);
+        if (!kDesign && !kPlate && c == kUniformGeneral + p.bg.mat) {  // CPML / boundary background node
+            e_update<false, kCoherent, false, true>(p, nb, i, j, k, m, false, io, out, pre);
+        } else {
+            const bool plane_lumped = p.lumped_k[k] < p.lumped_k[k + 1];
+            e_update<kDesign, kCoherent, kPlate>(p, nb, i, j, k, m, plane_lumped, io, out, pre);
+        }
     }
     // k_design_e writes the design region's E, k_plate_e the plate nodes' E
     if (!kDesign && !kPlate && (c == kDesignNode || c == kPlateNode)) return;
@@ -100,7 +104,8 @@ __device__ __forceinline__ void h_node_global(const StepParams& p, const FieldPt
             nb.mk = k > 0 ? mat[n - P] : 0;
         }
         const PsiIO io{pin.f, pout.f, true};
-        h_update<kCoherent>(p, nb, i, j, k, io, out, pre);
+        if (c == kUniformGeneral + p.bg.mat) h_update<kCoherent, true>(p, nb, i, j, k, io, out, pre);  // background node
+        else h_update<kCoherent>(p, nb, i, j, k, io, out, pre);
     }
     fo.hx[n] = out[0]; fo.hy[n] = out[1]; fo.hz[n] = out[2];
     if (p.probe_k[k] < p.probe_k[k + 1]) {

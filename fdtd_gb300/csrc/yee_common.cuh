@@ -277,8 +277,10 @@ __device__ __forceinline__ float psi_step(const float* in, float* out, int q, bo
 // the main update and the CPML corrections (the sampleField values, fdtdrav.h:740).
 // plane_lumped: some lumped edge lies in plane k (uniform across a CTA).
 // kPlate: plate-covered edges take the plate's sigma_e (only k_plate_e, which updates the nodes of
-// node class kPlateNode, instantiates it).
-template <bool kDesignAware = false, bool kCoherent = false, bool kPlate = false>
+// node class kPlateNode, instantiates it). kBg: a node whose seven cells all hold the background
+// material and that carries no lumped edge (node class kUniformGeneral + background): the same
+// arithmetic with the uniformity, background and lumped tests decided at compile time.
+template <bool kDesignAware = false, bool kCoherent = false, bool kPlate = false, bool kBg = false>
 __device__ __forceinline__ void e_update(const StepParams& p, const ENbr& n, int i, int j, int k, long long m,
                                          bool plane_lumped, const PsiIO& ps, float out[3], float pre[3]) {
     const DeviceGrid& g = p.g;
@@ -290,12 +292,14 @@ __device__ __forceinline__ void e_update(const StepParams& p, const ENbr& n, int
     const bool ys = in_slab(j, g.ny, g.pyn, g.pyp);
     const bool zs = in_slab(k, g.nz, g.pzn, g.pzp);
     const int bg = p.bg.mat;
-    const bool ux = n.m0 == n.mj && n.m0 == n.mk && n.m0 == n.mjk;
-    const bool uy = n.m0 == n.mi && n.m0 == n.mk && n.m0 == n.mik;
-    const bool uz = n.m0 == n.mi && n.m0 == n.mj && n.m0 == n.mij;
-    Coef3 cx = e_coef<kDesignAware>(p, 0, ux, n.m0, n.mj, n.mk, n.mjk, i, j, k);
-    Coef3 cy = e_coef<kDesignAware>(p, 1, uy, n.m0, n.mi, n.mk, n.mik, i, j, k);
-    Coef3 cz = e_coef<kDesignAware>(p, 2, uz, n.m0, n.mi, n.mj, n.mij, i, j, k);
+    const int m0 = kBg ? bg : n.m0;
+    const bool ux = kBg || (n.m0 == n.mj && n.m0 == n.mk && n.m0 == n.mjk);
+    const bool uy = kBg || (n.m0 == n.mi && n.m0 == n.mk && n.m0 == n.mik);
+    const bool uz = kBg || (n.m0 == n.mi && n.m0 == n.mj && n.m0 == n.mij);
+    const bool on_bg = kBg || n.m0 == bg;
+    Coef3 cx = e_coef<kDesignAware>(p, 0, ux, m0, n.mj, n.mk, n.mjk, i, j, k);
+    Coef3 cy = e_coef<kDesignAware>(p, 1, uy, m0, n.mi, n.mk, n.mik, i, j, k);
+    Coef3 cz = e_coef<kDesignAware>(p, 2, uz, m0, n.mi, n.mj, n.mij, i, j, k);
     // plate-covered components (kPlate only): plate coefficients, and the background's tabulated
     // kappa-divided values (which belong to its table coefficients) no longer apply
     int pm = 0;
@@ -313,14 +317,14 @@ __device__ __forceinline__ void e_update(const StepParams& p, const ENbr& n, int
     const float dHy_i = __fsub_rn(n.hy, n.hy_im), dHx_j = __fsub_rn(n.hx, n.hx_jm);
     const BgCurl& B = p.bg;
     // Ex (fdtdrav.h:665-676)
-    float vx = upd3(cx.a, n.ex, ys ? kdiv(cx.bp, ux && n.m0 == bg && !(pm & 1), B.e[1][0], p.key, j) : cx.bp, dHz_j,
-                    zs ? kdiv(cx.bm, ux && n.m0 == bg && !(pm & 1), B.e[2][0], p.kez, k) : cx.bm, dHy_k);
+    float vx = upd3(cx.a, n.ex, ys ? kdiv(cx.bp, ux && on_bg && !(pm & 1), B.e[1][0], p.key, j) : cx.bp, dHz_j,
+                    zs ? kdiv(cx.bm, ux && on_bg && !(pm & 1), B.e[2][0], p.kez, k) : cx.bm, dHy_k);
     // Ey (fdtdrav.h:696-707)
-    float vy = upd3(cy.a, n.ey, zs ? kdiv(cy.bp, uy && n.m0 == bg && !(pm & 2), B.e[2][1], p.kez, k) : cy.bp, dHx_k,
-                    xs ? kdiv(cy.bm, uy && n.m0 == bg && !(pm & 2), B.e[0][0], p.kex, i) : cy.bm, dHz_i);
+    float vy = upd3(cy.a, n.ey, zs ? kdiv(cy.bp, uy && on_bg && !(pm & 2), B.e[2][1], p.kez, k) : cy.bp, dHx_k,
+                    xs ? kdiv(cy.bm, uy && on_bg && !(pm & 2), B.e[0][0], p.kex, i) : cy.bm, dHz_i);
     // Ez with lumped elements (fdtdrav.h:720-741)
     float vz;
-    const LumpedEdge* L = plane_lumped ? find_lumped(p, i, j, k) : nullptr;
+    const LumpedEdge* L = (!kBg && plane_lumped) ? find_lumped(p, i, j, k) : nullptr;
     if (L) {
         if (L->source >= 0) {
             const float s = m < p.wave_len[L->source] ? p.waves[L->source][m] : 0.f;
@@ -329,8 +333,8 @@ __device__ __forceinline__ void e_update(const StepParams& p, const ENbr& n, int
             vz = upd3(L->ceze, n.ez, L->cezhy, dHy_i, L->cezhx, dHx_j);
         }
     } else {
-        vz = upd3(cz.a, n.ez, xs ? kdiv(cz.bp, uz && n.m0 == bg && !(pm & 4), B.e[0][1], p.kex, i) : cz.bp, dHy_i,
-                  ys ? kdiv(cz.bm, uz && n.m0 == bg && !(pm & 4), B.e[1][1], p.key, j) : cz.bm, dHx_j);
+        vz = upd3(cz.a, n.ez, xs ? kdiv(cz.bp, uz && on_bg && !(pm & 4), B.e[0][1], p.kex, i) : cz.bp, dHy_i,
+                  ys ? kdiv(cz.bm, uz && on_bg && !(pm & 4), B.e[1][1], p.key, j) : cz.bm, dHx_j);
     }
     pre[0] = ex_m ? vx : n.ex;
     pre[1] = ey_m ? vy : n.ey;
@@ -363,7 +367,7 @@ __device__ __forceinline__ void e_update(const StepParams& p, const ENbr& n, int
 }
 
 // One H node (calc_h fdtdrav.h:249-573).
-template <bool kCoherent = false>
+template <bool kCoherent = false, bool kBg = false>
 __device__ __forceinline__ void h_update(const StepParams& p, const HNbr& n, int i, int j, int k,
                                          const PsiIO& ps, float out[3], float pre[3]) {
     const DeviceGrid& g = p.g;
@@ -374,12 +378,14 @@ __device__ __forceinline__ void h_update(const StepParams& p, const HNbr& n, int
     const bool ys = in_slab(j, g.ny, g.pyn, g.pyp);
     const bool zs = in_slab(k, g.nz, g.pzn, g.pzp);
     const int bg = p.bg.mat;
-    const bool ux = n.m0 == n.mi, uy = n.m0 == n.mj, uz = n.m0 == n.mk;
-    const Coef3 cx = h_coef(p, 0, i == 0, ux, n.m0, n.mi);
-    const Coef3 cy = h_coef(p, 1, j == 0, uy, n.m0, n.mj);
-    const Coef3 cz = h_coef(p, 2, k == 0, uz, n.m0, n.mk);
+    const int m0 = kBg ? bg : n.m0;
+    const bool ux = kBg || n.m0 == n.mi, uy = kBg || n.m0 == n.mj, uz = kBg || n.m0 == n.mk;
+    const bool on_bg = kBg || n.m0 == bg;
+    const Coef3 cx = h_coef(p, 0, i == 0, ux, m0, n.mi);
+    const Coef3 cy = h_coef(p, 1, j == 0, uy, m0, n.mj);
+    const Coef3 cz = h_coef(p, 2, k == 0, uz, m0, n.mk);
     // the tabulated kappa-divided values belong to the background material's table entry
-    const bool bx = i != 0 && ux && n.m0 == bg, by = j != 0 && uy && n.m0 == bg, bz = k != 0 && uz && n.m0 == bg;
+    const bool bx = i != 0 && ux && on_bg, by = j != 0 && uy && on_bg, bz = k != 0 && uz && on_bg;
     const float dEy_k = __fsub_rn(n.ey_kp, n.ey), dEz_j = __fsub_rn(n.ez_jp, n.ez);
     const float dEz_i = __fsub_rn(n.ez_ip, n.ez), dEx_k = __fsub_rn(n.ex_kp, n.ex);
     const float dEx_j = __fsub_rn(n.ex_jp, n.ex), dEy_i = __fsub_rn(n.ey_ip, n.ey);
