@@ -342,7 +342,7 @@ def bench_adjoint():
 def bench_batched(steps=2000):
     """256 independent instances (per-axis sizes U{32..96}, 8-cell CPML, 8 dielectric boxes, one
     source and one probe each): the same instances run one by one through fdtd_step, then together
-    through the batched launch (autotuned over the flat and the persistent forms, CUDA graphs).
+    through the batched launch (autotuned over the chain, flat and persistent forms, CUDA graphs).
     Handle creation and setup are outside both timings; both advance every instance by `steps`
     steps."""
     import torch
@@ -362,7 +362,10 @@ def bench_batched(steps=2000):
     t_seq = time.perf_counter() - t0
     with solver.Batch(sims) as b:
         tune_ms = b.tune(5)
-        b.step(2)
+        # capture the graphs the timed run replays (a 32-step chunk and the remainder)
+        b.step(32)
+        if steps % 32:
+            b.step(steps % 32)
         b.synchronize()
         t0 = time.perf_counter()
         b.step(steps)
@@ -378,9 +381,10 @@ def bench_batched(steps=2000):
             "sequential": {"value": round(seq, 3), "unit": "Gcell-updates/s", "seconds": round(t_seq, 3),
                            "gpu_launches": 2 * steps * len(scs)},
             "batched": {"value": round(bat, 3), "unit": "Gcell-updates/s", "seconds": round(t_bat, 3),
-                        "gpu_launches": 3 * steps if cfg["cluster"] == 0 else 1, "config": cfg,
-                        "form": "flat (E, H, step-counter kernels per step)" if cfg["cluster"] == 0
-                        else "persistent clusters",
+                        "gpu_launches": {-1: 2 * steps * len(scs) + -(-steps // 32), 0: 3 * steps}.get(cfg["cluster"], 1),
+                        "config": cfg,
+                        "form": {-1: "chains (each instance's two-pass kernels, concurrent graph branches)",
+                                 0: "flat (E, H, step-counter kernels per step)"}.get(cfg["cluster"], "persistent clusters"),
                         "tune_ms_5_steps": round(tune_ms, 2)},
             "speedup": round(bat / seq, 2)}
 

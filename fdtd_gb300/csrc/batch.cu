@@ -107,9 +107,14 @@ __global__ void __launch_bounds__(256, FDTD_BATCH_FLAT_MIN_BLOCKS) k_batch_flat_
     if (i < s.p.g.nx && j < s.p.g.ny) h_node_global<false, uint32_t>(s.p, s.f, s.f, s.f, s.ps, s.ps, i, j, it.w, s.step);
 }
 
-__global__ void k_batch_advance(BatchInstance* inst, int n) {
+__global__ void k_batch_advance(BatchInstance* inst, int n, int by) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < n) inst[q].step += 1;
+    if (q < n) inst[q].step += by;
+}
+
+cudaError_t launch_batch_advance(BatchInstance* inst, int n_inst, int by, cudaStream_t st) {
+    k_batch_advance<<<(n_inst + 127) / 128, 128, 0, st>>>(inst, n_inst, by);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_batch_flat(BatchInstance* inst, int n_inst, const int4* items, int n_items, long long steps,
@@ -117,7 +122,7 @@ cudaError_t launch_batch_flat(BatchInstance* inst, int n_inst, const int4* items
     for (long long s = 0; s < steps; ++s) {
         k_batch_flat_e<<<n_items, dim3(32, 8, 1), 0, st>>>(inst, items);
         k_batch_flat_h<<<n_items, dim3(32, 8, 1), 0, st>>>(inst, items);
-        k_batch_advance<<<(n_inst + 127) / 128, 128, 0, st>>>(inst, n_inst);
+        k_batch_advance<<<(n_inst + 127) / 128, 128, 0, st>>>(inst, n_inst, 1);
     }
     return cudaGetLastError();
 }

@@ -30,4 +30,7 @@ cudaError_t launch_batch(BatchInstance* inst, const int* order, int n_inst, int*
 cudaError_t launch_batch_flat(BatchInstance* inst, int n_inst, const int4* items, int n_items, long long steps,
                               cudaStream_t st);
 
+// Add `by` to the step counter of every instance.
+cudaError_t launch_batch_advance(BatchInstance* inst, int n_inst, int by, cudaStream_t st);
+
 }  // namespace fdtd

@@ -1395,7 +1395,7 @@ struct fdtd_batch {
     BatchInstance* d_inst = nullptr;
     int* d_order = nullptr;
     int* d_queue = nullptr;
-    int cluster = 4, threads = 256, n_clusters = 0;  // cluster 0: the flat per-step form
+    int cluster = 4, threads = 256, n_clusters = 0;  // cluster 0: flat per-step form; -1: chains
     int4* d_items = nullptr;            // flat form: {instance, x0, y0, k} per 32 x 8 block
     int n_items = 0;
     struct Graph {
@@ -1405,6 +1405,11 @@ struct fdtd_batch {
         cudaGraphExec_t exec;
     };
     std::vector<Graph> graphs;          // captured launches by step count and configuration
+    // chain form: one stream per instance while capturing, the events that fork and join them,
+    // and a signature of the descriptors the captured graphs bake in
+    std::vector<cudaStream_t> chain_streams;
+    std::vector<cudaEvent_t> chain_events;  // [0]: fork, [1 + q]: join of instance q
+    unsigned long long chain_sig = 0;
 };
 
 namespace {
@@ -1437,6 +1442,13 @@ int batch_refresh(fdtd_batch* b) {
 }
 
 int batch_set_config(fdtd_batch* b, int cluster, int threads) {
+    if (cluster == -1) {  // chains: each instance's own two-pass kernels, instances concurrent
+        if (threads != 256) return fail(FDTD_ERR_INVALID, "the chain form (cluster -1) runs 256 threads per CTA");
+        b->cluster = -1;
+        b->threads = 256;
+        b->n_clusters = 0;
+        return FDTD_OK;
+    }
     if (cluster == 0) {  // flat per-step kernels: 256 threads per CTA
         if (threads != 256) return fail(FDTD_ERR_INVALID, "the flat form (cluster 0) runs 256 threads per CTA");
         b->cluster = 0;
@@ -1464,11 +1476,33 @@ int batch_graph(fdtd_batch* b, long long steps, cudaGraphExec_t* out) {
             return FDTD_OK;
         }
     if (b->graphs.size() >= 4) batch_drop_graph(b);
+    const int n = (int)b->hs.size();
+    if (b->cluster == -1 && b->chain_streams.empty()) {
+        b->chain_streams.assign(n, nullptr);
+        b->chain_events.assign(n + 1, nullptr);
+        for (int q = 0; q < n; ++q) CUDA_TRY(cudaStreamCreateWithFlags(&b->chain_streams[q], cudaStreamNonBlocking));
+        for (int q = 0; q <= n; ++q) CUDA_TRY(cudaEventCreateWithFlags(&b->chain_events[q], cudaEventDisableTiming));
+    }
     CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = b->cluster == 0
-                        ? launch_batch_flat(b->d_inst, (int)b->hs.size(), b->d_items, b->n_items, steps, b->stream)
-                        : launch_batch(b->d_inst, b->d_order, (int)b->hs.size(), b->d_queue, steps, b->cluster,
-                                       b->threads, b->n_clusters, b->stream);
+    cudaError_t e = cudaSuccess;
+    if (b->cluster == -1) {
+        // fork one chain per instance, `steps` two-pass steps each, join, advance the counters
+        e = cudaEventRecord(b->chain_events[0], b->stream);
+        for (int q = 0; q < n && e == cudaSuccess; ++q) {
+            const BatchInstance& I = b->inst[q];
+            cudaStream_t cs = b->chain_streams[q];
+            e = cudaStreamWaitEvent(cs, b->chain_events[0], 0);
+            for (long long t = 0; t < steps && e == cudaSuccess; ++t)
+                e = launch_two_pass_rel(I.p, I.f, I.ps, &b->d_inst[q].step, (int)t, cs);
+            if (e == cudaSuccess) e = cudaEventRecord(b->chain_events[1 + q], cs);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->chain_events[1 + q], 0);
+        }
+        if (e == cudaSuccess) e = launch_batch_advance(b->d_inst, n, (int)steps, b->stream);
+    } else if (b->cluster == 0) {
+        e = launch_batch_flat(b->d_inst, n, b->d_items, b->n_items, steps, b->stream);
+    } else {
+        e = launch_batch(b->d_inst, b->d_order, n, b->d_queue, steps, b->cluster, b->threads, b->n_clusters, b->stream);
+    }
     cudaGraph_t g = nullptr;
     cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
     if (e != cudaSuccess || e2 != cudaSuccess) {
@@ -1486,14 +1520,31 @@ int batch_graph(fdtd_batch* b, long long steps, cudaGraphExec_t* out) {
 }
 
 // Run `steps` steps on every instance (refresh, graph launches), then advance the step counters.
-// The persistent form is one launch of `steps` steps; the flat form replays a graph of
-// kFlatChunk steps (three kernels per step) and one of the remainder.
+// The persistent form is one launch of `steps` steps; the flat and chain forms replay a graph of
+// kFlatChunk steps and one of the remainder. The chain form's graphs bake the descriptors in, so
+// they are captured again when a descriptor changes (a handle stepped alone under the fused
+// schedule, tables rebuilt).
 constexpr long long kFlatChunk = 32;
+unsigned long long descriptor_signature(const fdtd_batch* b) {
+    unsigned long long h = 1469598103934665603ULL;  // FNV-1a over the descriptors without their steps
+    for (const BatchInstance& I : b->inst) {
+        const unsigned char* c = reinterpret_cast<const unsigned char*>(&I);
+        for (size_t q = 0; q < offsetof(BatchInstance, step); ++q) h = (h ^ c[q]) * 1099511628211ULL;
+    }
+    return h;
+}
 int batch_run(fdtd_batch* b, long long steps) {
     int rc = batch_refresh(b);
     if (rc) return rc;
+    if (b->cluster == -1) {
+        const unsigned long long sig = descriptor_signature(b);
+        if (sig != b->chain_sig) {
+            batch_drop_graph(b);
+            b->chain_sig = sig;
+        }
+    }
     cudaGraphExec_t ex = nullptr;
-    if (b->cluster == 0) {
+    if (b->cluster <= 0) {
         const long long chunk = std::min(steps, kFlatChunk), full = steps / chunk, rem = steps % chunk;
         if ((rc = batch_graph(b, chunk, &ex))) return rc;
         for (long long q = 0; q < full; ++q) CUDA_TRY(cudaGraphLaunch(ex, b->stream));
@@ -1557,7 +1608,7 @@ extern "C" int fdtd_batch_create(fdtd_handle* const* handles, int32_t n, fdtd_ba
         return cleanup(fail(FDTD_ERR_OOM, "batch work list"));
     if (cudaMemcpy(b->d_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice) != cudaSuccess)
         return cleanup(fail(FDTD_ERR_CUDA, "batch work list upload"));
-    int rc = batch_set_config(b, 0, 256);
+    int rc = batch_set_config(b, -1, 256);
     if (rc) return cleanup(rc);
     *out = b;
     return FDTD_OK;
@@ -1568,6 +1619,10 @@ extern "C" int fdtd_batch_destroy(fdtd_batch* b) {
     if (b->stream) cudaStreamSynchronize(b->stream);
     batch_drop_graph(b);
     if (b->own_stream) cudaStreamDestroy(b->own_stream);
+    for (cudaStream_t cs : b->chain_streams)
+        if (cs) cudaStreamDestroy(cs);
+    for (cudaEvent_t ev : b->chain_events)
+        if (ev) cudaEventDestroy(ev);
     cudaFree(b->d_inst);
     cudaFree(b->d_order);
     cudaFree(b->d_queue);
@@ -1639,7 +1694,7 @@ extern "C" int fdtd_batch_tune(fdtd_batch* b, int64_t steps, double* best_ms) {
         if (rc) { restore_all(); return rc; }
         steps0[q] = h->step;
     }
-    const int clusters[5] = {0, 1, 2, 4, 8}, threads[3] = {128, 256, 512};
+    const int clusters[6] = {-1, 0, 1, 2, 4, 8}, threads[3] = {128, 256, 512};
     double best = 1e300;
     int best_c = b->cluster, best_t = b->threads;
     cudaEvent_t e0, e1;
@@ -1648,20 +1703,23 @@ extern "C" int fdtd_batch_tune(fdtd_batch* b, int64_t steps, double* best_ms) {
     int rc = FDTD_OK;
     for (int c : clusters) {
         for (int t : threads) {
-            if (c == 0 && t != 256) continue;
+            if (c <= 0 && t != 256) continue;
             if (batch_set_config(b, c, t) != FDTD_OK) continue;  // shape does not fit: skip it
-            cudaEventRecord(e0, b->stream);
-            if ((rc = batch_run(b, steps))) break;
-            cudaEventRecord(e1, b->stream);
-            if (cudaEventSynchronize(e1) != cudaSuccess) { rc = fail(FDTD_ERR_CUDA, "tuning run failed"); break; }
+            // a first run captures the candidate's graphs, the second is timed; states restored after each
             float ms = 0.f;
-            cudaEventElapsedTime(&ms, e0, e1);
-            if (ms < best) { best = ms; best_c = c; best_t = t; }
-            for (size_t q = 0; q < nh && !rc; ++q) {
-                rc = state_copy(b->hs[q], saved[q], false);
-                b->hs[q]->step = steps0[q];
+            for (int rep = 0; rep < 2 && !rc; ++rep) {
+                cudaEventRecord(e0, b->stream);
+                if ((rc = batch_run(b, steps))) break;
+                cudaEventRecord(e1, b->stream);
+                if (cudaEventSynchronize(e1) != cudaSuccess) { rc = fail(FDTD_ERR_CUDA, "tuning run failed"); break; }
+                cudaEventElapsedTime(&ms, e0, e1);
+                for (size_t q = 0; q < nh && !rc; ++q) {
+                    rc = state_copy(b->hs[q], saved[q], false);
+                    b->hs[q]->step = steps0[q];
+                }
             }
             if (rc) break;
+            if (ms < best) { best = ms; best_c = c; best_t = t; }
         }
         if (rc) break;
     }

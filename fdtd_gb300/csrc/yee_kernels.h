@@ -22,6 +22,11 @@ struct PsiSet {
 cudaError_t launch_two_pass(const StepParams& p, const FieldPtrs& f, const PsiSet& ps, long long m,
                             cudaStream_t st);
 
+// One two-pass step whose step index is *base + s (device counter), for graph replay; handles
+// without a design region or plates only.
+cudaError_t launch_two_pass_rel(const StepParams& p, const FieldPtrs& f, const PsiSet& ps, const long long* base, int s,
+                                cudaStream_t st);
+
 // E of the design region's nodes, fi/pin -> fo/pout, after a schedule's E kernels; nothing
 // without a design region.
 cudaError_t launch_design_e(const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,

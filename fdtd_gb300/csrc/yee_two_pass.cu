@@ -113,6 +113,42 @@ cudaError_t launch_design_e(const StepParams& p, const FieldPtrs& fi, const Fiel
     return cudaGetLastError();
 }
 
+// Two-pass kernels whose step index is *base + s: a CUDA graph captured once replays them while
+// a counter on the device advances (the batched chain form).
+template <typename Idx>
+__global__ void __launch_bounds__(256, FDTD_TWO_PASS_MIN_BLOCKS) k_update_e_rel(const __grid_constant__ StepParams p,
+                                                                                 FieldPtrs f,
+                                                                                 const __grid_constant__ PsiSet ps,
+                                                                                 const long long* __restrict__ base, int s) {
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    if (i >= p.g.nx || j >= p.g.ny) return;
+    e_node_global<false, false, false, Idx>(p, f, f, ps, ps, i, j, blockIdx.z, *base + s);
+}
+template <typename Idx>
+__global__ void __launch_bounds__(256, FDTD_TWO_PASS_MIN_BLOCKS) k_update_h_rel(const __grid_constant__ StepParams p,
+                                                                                 FieldPtrs f,
+                                                                                 const __grid_constant__ PsiSet ps,
+                                                                                 const long long* __restrict__ base, int s) {
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    if (i >= p.g.nx || j >= p.g.ny) return;
+    h_node_global<false, Idx>(p, f, f, f, ps, ps, i, j, blockIdx.z, *base + s);
+}
+
+cudaError_t launch_two_pass_rel(const StepParams& p, const FieldPtrs& f, const PsiSet& ps, const long long* base, int s,
+                                cudaStream_t st) {
+    if (p.deps || p.n_plate_nodes > 0) return cudaErrorInvalidValue;  // no design region, no plates
+    dim3 block(32, 8, 1);
+    dim3 grid((p.g.nx + 31) / 32, (p.g.ny + 7) / 8, p.g.nz);
+    const bool idx32 = p.g.plane * (long long)(p.g.nz + 1) < (1LL << 31);
+    if (idx32) k_update_e_rel<uint32_t><<<grid, block, 0, st>>>(p, f, ps, base, s);
+    else k_update_e_rel<long long><<<grid, block, 0, st>>>(p, f, ps, base, s);
+    if (idx32) k_update_h_rel<uint32_t><<<grid, block, 0, st>>>(p, f, ps, base, s);
+    else k_update_h_rel<long long><<<grid, block, 0, st>>>(p, f, ps, base, s);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_two_pass(const StepParams& p, const FieldPtrs& f, const PsiSet& ps, long long m,
                             cudaStream_t st) {
     dim3 block(32, 8, 1);

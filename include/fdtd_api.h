@@ -254,12 +254,13 @@ int fdtd_adjoint_backward(fdtd_handle* h, double* grad);
 
 /* ---- Batched launch (no reference counterpart: the reference runs one domain per process). A
  * batch advances many independent handles of any sizes together, its launches captured in CUDA
- * graphs, in one of two forms: flat (cluster 0, the default): per step one E kernel and one H
- * kernel over the 32 x 8 blocks of every plane of every instance, one node per thread;
- * persistent (cluster 1, 2, 4 or 8): one kernel for all steps, each instance owned by a
- * thread-block cluster for all of its steps (E update, cluster barrier, H update, cluster
- * barrier), instances taken longest first from a queue. Every instance produces the bits
- * fdtd_step would produce. ---- */
+ * graphs, in one of three forms. Chains (cluster -1, the default): each instance runs its own
+ * two-pass kernels on its own branch of the graph, every branch concurrent with the others. Flat
+ * (cluster 0): per step one E kernel and one H kernel over the 32 x 8 blocks of every plane of
+ * every instance, one node per thread. Persistent (cluster 1, 2, 4 or 8): one kernel for all
+ * steps, each instance owned by a thread-block cluster for all of its steps (E update, cluster
+ * barrier, H update, cluster barrier), instances taken longest first from a queue. Every instance
+ * produces the bits fdtd_step would produce. ---- */
 typedef struct fdtd_batch fdtd_batch;
 
 /* A batch over n distinct handles on the current device (none with a design region). The handles
@@ -271,13 +272,14 @@ int fdtd_batch_destroy(fdtd_batch* b);
 /* Stream of the batch launches: a created stream, not the legacy default stream (the launch is
  * captured in a CUDA graph). By default the batch uses a stream of its own. */
 int fdtd_batch_set_stream(fdtd_batch* b, void* stream);
-/* Form and shape: cluster 0 = flat (256 threads per CTA), or the persistent form's cluster size
- * (1, 2, 4 or 8 CTAs per instance) with its CTA size (128, 256 or 512 threads). */
+/* Form and shape: cluster -1 = chains, 0 = flat (both 256 threads per CTA), or the persistent
+ * form's cluster size (1, 2, 4 or 8 CTAs per instance) with its CTA size (128, 256 or 512). */
 int fdtd_batch_set_config(fdtd_batch* b, int32_t cluster, int32_t threads);
 int fdtd_batch_get_config(const fdtd_batch* b, int32_t* cluster, int32_t* threads, int32_t* n_clusters);
-/* Autotuner: times `steps` steps of the whole batch in the flat form and for every cluster and CTA
- * size of the persistent form, restores every instance's state after each trial, keeps the
- * fastest (its time in *best_ms if not NULL). */
+/* Autotuner: times `steps` steps of the whole batch in the chain and flat forms and for every
+ * cluster and CTA size of the persistent form (a first untimed run captures each candidate's
+ * graphs), restores every instance's state after each run, keeps the fastest (its time in
+ * *best_ms if not NULL). */
 int fdtd_batch_tune(fdtd_batch* b, int64_t steps, double* best_ms);
 /* Advance every instance by `steps` steps (graph launches, asynchronous on the batch stream). */
 int fdtd_batch_step(fdtd_batch* b, int64_t steps);

@@ -1,6 +1,6 @@
-"""Batched launch: every instance equals its own sequential run bit for bit, in the flat form and
-for every cluster / CTA shape of the persistent form, after autotuning, and when handles are also
-stepped on their own."""
+"""Batched launch: every instance equals its own sequential run bit for bit, in the chain and flat
+forms and for every cluster / CTA shape of the persistent form, after autotuning, and when handles
+are also stepped on their own (which makes the chain form capture its graphs again)."""
 import numpy as np
 import pytest
 
@@ -49,7 +49,7 @@ def same(a, b):
     return all(bitwise_equal(x[0], y[0]) and bitwise_equal(x[1], y[1]) for x, y in zip(a, b))
 
 
-@pytest.mark.parametrize("config", [(0, 256), (1, 256), (2, 128), (4, 256), (8, 512)])
+@pytest.mark.parametrize("config", [(-1, 256), (0, 256), (1, 256), (2, 128), (4, 256), (8, 512)])
 def test_batch_equals_sequential(gpu_lib, config):
     scs = instances()
     assert same(batched(scs, [25, 35], config), sequential(scs, 60))
@@ -60,13 +60,16 @@ def test_batch_after_tuning(gpu_lib):
     assert same(batched(scs, [40], tune=True), sequential(scs, 40))
 
 
-def test_handles_stepped_alone_between_launches(gpu_lib):
+@pytest.mark.parametrize("config", [None, (-1, 256)])
+def test_handles_stepped_alone_between_launches(gpu_lib, config):
     from fdtd_gb300 import solver
     scs = instances(5, 40, seed=11)
     ref = sequential(scs, 40)
     sims = [solver.Simulation.from_scenario(sc, probe_capacity=40) for sc in scs]
     try:
         with solver.Batch(sims) as b:
+            if config:
+                b.set_config(*config)
             b.step(10)
             b.synchronize()
             sims[2].step(7)        # one instance moves on its own
