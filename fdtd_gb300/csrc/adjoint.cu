@@ -81,8 +81,20 @@ __global__ void __launch_bounds__(256, FDTD_ADJ_MIN_BLOCKS) k_adj_h(const __grid
     float ly = a.l[4][n] + a.ge[1][n] - (kp ? a.ge[1][n + P] : 0.f) + a.ge[4][n] - (ip ? a.ge[4][n + 1] : 0.f);
     float lz = a.l[5][n] + a.ge[0][n] - (jp ? a.ge[0][n + R] : 0.f) + a.ge[3][n] - (ip ? a.ge[3][n + 1] : 0.f);
 
+    const int c = p.cls[n];
+    if (c < kUniformGeneral) {  // fast-path node: table coefficients, every component, no CPML
+        const MatCoef* mc = p.coef + c;
+        const float4 x = __ldg(&mc->h[0]), y = __ldg(&mc->h[1]), z = __ldg(&mc->h[2]);
+        a.l[3][n] = x.x * lx; a.l[4][n] = y.x * ly; a.l[5][n] = z.x * lz;
+        a.gh[0][n] = x.y * lx; a.gh[1][n] = x.z * lx; a.gh[2][n] = y.y * ly;
+        a.gh[3][n] = y.z * ly; a.gh[4][n] = z.y * lz; a.gh[5][n] = z.z * lz;
+        return;
+    }
     const uint8_t* mat = p.mat;
-    const int m0 = mat[n], mi = i > 0 ? mat[n - 1] : 0, mj = j > 0 ? mat[n - R] : 0, mk = k > 0 ? mat[n - P] : 0;
+    const bool one = c < kDesignNode;  // seven cells of one material, given by the class
+    const int m0 = one ? c - kUniformGeneral : mat[n];
+    const int mi = one ? m0 : i > 0 ? mat[n - 1] : 0, mj = one ? m0 : j > 0 ? mat[n - R] : 0;
+    const int mk = one ? m0 : k > 0 ? mat[n - P] : 0;
     const bool hx_m = jp && kp, hy_m = ip && kp, hz_m = ip && jp;
     const bool xs = in_slab(i, g.nx, g.pxn, g.pxp), ys = in_slab(j, g.ny, g.pyn, g.pyp), zs = in_slab(k, g.nz, g.pzn, g.pzp);
     const int bg = p.bg.mat;
@@ -138,11 +150,24 @@ __global__ void __launch_bounds__(256, FDTD_ADJ_MIN_BLOCKS) k_adj_e(const __grid
     float lz = a.l[2][n] + (j > 0 ? a.gh[1][n - R] : 0.f) - a.gh[1][n] + (i > 0 ? a.gh[2][n - 1] : 0.f) - a.gh[2][n];
     if (n == st.probe) lz += st.source;  // dJ/dEz(p) of the sample taken in this step
 
+    const int c = p.cls[n];
+    if (c < kUniformGeneral) {  // fast-path node: table coefficients, every component, no CPML,
+                                // no lumped edge, outside the design edge box
+        const MatCoef* mc = p.coef + c;
+        const float4 x = __ldg(&mc->e[0]), y = __ldg(&mc->e[1]), z = __ldg(&mc->e[2]);
+        a.l[0][n] = x.x * lx; a.l[1][n] = y.x * ly; a.l[2][n] = z.x * lz;
+        a.ge[0][n] = x.y * lx; a.ge[1][n] = x.z * lx; a.ge[2][n] = y.y * ly;
+        a.ge[3][n] = y.z * ly; a.ge[4][n] = z.y * lz; a.ge[5][n] = z.z * lz;
+        return;
+    }
     const uint8_t* mat = p.mat;
-    const int m0 = mat[n];
-    const int mi = i > 0 ? mat[n - 1] : 0, mj = j > 0 ? mat[n - R] : 0, mk = k > 0 ? mat[n - P] : 0;
-    const int mij = (i > 0 && j > 0) ? mat[n - 1 - R] : 0, mik = (i > 0 && k > 0) ? mat[n - 1 - P] : 0;
-    const int mjk = (j > 0 && k > 0) ? mat[n - R - P] : 0;
+    const bool one = c < kDesignNode;  // seven cells of one material, given by the class
+    const int m0 = one ? c - kUniformGeneral : mat[n];
+    const int mi = one ? m0 : i > 0 ? mat[n - 1] : 0, mj = one ? m0 : j > 0 ? mat[n - R] : 0;
+    const int mk = one ? m0 : k > 0 ? mat[n - P] : 0;
+    const int mij = one ? m0 : (i > 0 && j > 0) ? mat[n - 1 - R] : 0;
+    const int mik = one ? m0 : (i > 0 && k > 0) ? mat[n - 1 - P] : 0;
+    const int mjk = one ? m0 : (j > 0 && k > 0) ? mat[n - R - P] : 0;
     const bool in_x = i > 0 && i < g.nx - 1, in_y = j > 0 && j < g.ny - 1, in_z = k > 0 && k < g.nz - 1;
     const bool ex_m = i < g.nx - 1 && in_y && in_z, ey_m = in_x && j < g.ny - 1 && in_z, ez_m = in_x && in_y && k < g.nz - 1;
     const bool xs = in_slab(i, g.nx, g.pxn, g.pxp), ys = in_slab(j, g.ny, g.pyn, g.pyp), zs = in_slab(k, g.nz, g.pzn, g.pzp);
