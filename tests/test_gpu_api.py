@@ -55,6 +55,23 @@ def test_probe_ring_wraps(gpu_lib):
     assert bitwise_equal(last, full[23:30])
 
 
+def test_device_bytes_follow_reallocation(gpu_lib):
+    """Buffers rebuilt with another size (the probe ring here) leave fdtd_device_bytes counting
+    what the handle holds now, not what it ever allocated."""
+    from fdtd_gb300 import solver
+    sc = small()
+    with solver.Simulation.from_scenario(sc, probe_capacity=16) as sim:
+        sim.prepare()
+        base = sim.device_bytes()
+        sim.set_probe_capacity(1 << 16)
+        sim.prepare()
+        big = sim.device_bytes()
+        assert big > base
+        sim.set_probe_capacity(16)
+        sim.prepare()
+        assert sim.device_bytes() == base
+
+
 def test_steps_in_chunks_equal_one_call(gpu_lib):
     from fdtd_gb300 import solver
     sc = small()
