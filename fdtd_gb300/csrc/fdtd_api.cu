@@ -311,7 +311,7 @@ int ensure_fused(fdtd_handle* h) {
     for (int b = 0; b < 2; ++b) {
         float* hh[3] = {h->field[b][3], h->field[b][4], h->field[b][5]};
         float* ee[3] = {h->field[b][0], h->field[b][1], h->field[b][2]};
-        if (encode_fused_maps(&h->maps[b], h->g, hh, ee, h->cls, enc) != 0)
+        if (encode_fused_maps(&h->maps[b], h->g, hh, ee, h->cls, h->mat, enc) != 0)
             return fail(FDTD_ERR_CUDA, "tensor map encoding failed");
     }
     CUDA_TRY(fused_configure());
@@ -1103,7 +1103,8 @@ extern "C" int fdtd_step_static_scratch(fdtd_handle* h, int64_t n) {
         float* ee[3] = {h->field[a][0], h->field[a][1], h->field[a][2]};
         float* sh[3] = {sf[3], sf[4], sf[5]};
         float* se[3] = {sf[0], sf[1], sf[2]};
-        if (encode_fused_maps(&maps_h, h->g, hh, ee, h->cls, enc) != 0 || encode_fused_maps(&maps_s, h->g, sh, se, h->cls, enc) != 0)
+        if (encode_fused_maps(&maps_h, h->g, hh, ee, h->cls, h->mat, enc) != 0 ||
+            encode_fused_maps(&maps_s, h->g, sh, se, h->cls, h->mat, enc) != 0)
             return fail(FDTD_ERR_CUDA, "tensor map encoding failed");
     }
     int4* d_items = (int4*)(base + L.items);

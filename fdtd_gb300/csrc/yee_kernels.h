@@ -48,6 +48,7 @@ struct FusedMaps {
     CUtensorMap h[3];
     CUtensorMap e[3];
     CUtensorMap cls;
+    CUtensorMap mat;  // material index (same box as cls), read by the interface-node path
 };
 // Work items of one step (device arrays of int4): interior items {x0, y0, k0, k1} for the sweep
 // (a 32 x 16 column over planes [k0, k1)), general items {x0, y0, k, 0} for the shell passes
@@ -71,7 +72,7 @@ cudaError_t launch_fused(const FusedMaps& maps, const StepParams& p, const Field
                          const PsiSet& psi_in, const PsiSet& psi_out, long long m, const FusedWork& w, cudaStream_t st);
 // encode_fn: the driver's cuTensorMapEncodeTiled. Returns 0 on success.
 int encode_fused_maps(FusedMaps* out, const DeviceGrid& g, float* const h[3], float* const e[3], const uint8_t* cls,
-                      void* encode_fn);
+                      const uint8_t* mat, void* encode_fn);
 
 // Setup kernels (setup_kernels.cu).
 cudaError_t launch_cpml_profiles(const DeviceGrid& g, float pi, float* const prof[18], cudaStream_t st);
