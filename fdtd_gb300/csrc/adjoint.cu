@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(256, FDTD_ADJ_MIN_BLOCKS) k_adj_h(const __grid
         return;
     }
     const uint8_t* mat = p.mat;
-    const bool one = c < kDesignNode;  // seven cells of one material, given by the class
+    const bool one = c < kInterfaceNode;  // seven cells of one material, given by the class
     const int m0 = one ? c - kUniformGeneral : mat[n];
     const int mi = one ? m0 : i > 0 ? mat[n - 1] : 0, mj = one ? m0 : j > 0 ? mat[n - R] : 0;
     const int mk = one ? m0 : k > 0 ? mat[n - P] : 0;
@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(256, FDTD_ADJ_MIN_BLOCKS) k_adj_e(const __grid
         return;
     }
     const uint8_t* mat = p.mat;
-    const bool one = c < kDesignNode;  // seven cells of one material, given by the class
+    const bool one = c < kInterfaceNode;  // seven cells of one material, given by the class
     const int m0 = one ? c - kUniformGeneral : mat[n];
     const int mi = one ? m0 : i > 0 ? mat[n - 1] : 0, mj = one ? m0 : j > 0 ? mat[n - R] : 0;
     const int mk = one ? m0 : k > 0 ? mat[n - P] : 0;

@@ -88,6 +88,9 @@ struct fdtd_handle {
     bool replan = false;  // the design region changed since the fused work was planned
     uint8_t* mat = nullptr;
     uint8_t* cls = nullptr;  // node classes, built by ensure_prepared
+    uint16_t* rec = nullptr;          // coefficient row per node, built with the classes
+    MatCoef* coef_rows = nullptr;     // material rows then interface rows (StepParams::coef)
+    int n_iface_rows = 0;
     int n_lumped_edges = 0;
     MatProps* props = nullptr;
     MatCoef* coef = nullptr;
@@ -195,8 +198,9 @@ StepParams make_params(fdtd_handle* h) {
     p.g = h->g;
     p.mat = h->mat;
     p.cls = h->cls;
+    p.rec = h->rec;
     p.props = h->props;
-    p.coef = h->coef;
+    p.coef = h->coef_rows ? h->coef_rows : h->coef;
     const float* const* P = h->prof;
     p.bex = P[0]; p.aex = P[1]; p.bmx = P[2]; p.amx = P[3]; p.kex = P[4]; p.kmx = P[5];
     p.bey = P[6]; p.aey = P[7]; p.bmy = P[8]; p.amy = P[9]; p.key = P[10]; p.kmy = P[11];
@@ -311,7 +315,7 @@ int ensure_fused(fdtd_handle* h) {
     for (int b = 0; b < 2; ++b) {
         float* hh[3] = {h->field[b][3], h->field[b][4], h->field[b][5]};
         float* ee[3] = {h->field[b][0], h->field[b][1], h->field[b][2]};
-        if (encode_fused_maps(&h->maps[b], h->g, hh, ee, h->cls, h->mat, enc) != 0)
+        if (encode_fused_maps(&h->maps[b], h->g, hh, ee, h->rec, enc) != 0)
             return fail(FDTD_ERR_CUDA, "tensor map encoding failed");
     }
     CUDA_TRY(fused_configure());
@@ -924,6 +928,56 @@ int build_plates(fdtd_handle* h) {
     return FDTD_OK;
 }
 
+// Interface rows (kInterfaceNode nodes): gather the seven-cell keys, sort and unique them here,
+// then write each node's coefficient row and the rows themselves. Runs after the node classes and
+// plates are final.
+int build_interface_rows(fdtd_handle* h) {
+    const DeviceGrid& g = h->g;
+    if (!h->rec) CUDA_TRY(h->alloc((void**)&h->rec, (size_t)vol(h) * sizeof(uint16_t)));
+    unsigned long long* count = nullptr;
+    unsigned long long* keys = nullptr;
+    CUDA_TRY(h->alloc((void**)&count, sizeof(unsigned long long)));
+    struct Temp {
+        fdtd_handle* h;
+        void* a[2];
+        ~Temp() { h->release(a[0]); h->release(a[1]); }
+    } tmp{h, {count, nullptr}};
+    unsigned long long n = 0;
+    CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(n), h->stream));
+    CUDA_TRY(launch_iface_keys(g, h->cls, h->mat, nullptr, count, 0, h->stream));
+    CUDA_TRY(cudaMemcpyAsync(&n, count, sizeof(n), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    std::vector<unsigned long long> hk((size_t)n);
+    if (n > 0) {
+        CUDA_TRY(h->alloc((void**)&keys, (size_t)n * sizeof(unsigned long long)));
+        tmp.a[1] = keys;
+        CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(n), h->stream));
+        CUDA_TRY(launch_iface_keys(g, h->cls, h->mat, keys, count, (long long)n, h->stream));
+        CUDA_TRY(cudaMemcpyAsync(hk.data(), keys, (size_t)n * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+        std::sort(hk.begin(), hk.end());
+        hk.erase(std::unique(hk.begin(), hk.end()), hk.end());
+        if (hk.size() > (size_t)kMaxInterfaceRows) hk.resize((size_t)kMaxInterfaceRows);  // the rest stay general
+        CUDA_TRY(cudaMemcpyAsync(keys, hk.data(), hk.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice, h->stream));
+    }
+    const int n_rows = (int)hk.size();
+    h->release(h->coef_rows);
+    h->coef_rows = nullptr;
+    h->n_iface_rows = 0;
+    CUDA_TRY(h->alloc((void**)&h->coef_rows, sizeof(MatCoef) * (size_t)(kFirstInterfaceRow + n_rows)));
+    CUDA_TRY(cudaMemcpyAsync(h->coef_rows, h->coef, sizeof(MatCoef) * (size_t)kFirstInterfaceRow, cudaMemcpyDeviceToDevice,
+                             h->stream));
+    CUDA_TRY(launch_iface_rows(g, h->cls, h->mat, keys, n_rows, h->rec, h->stream));
+    StepParams p{};  // the rows come from the material rows and properties only
+    p.g = g;
+    p.props = h->props;
+    p.coef = h->coef;
+    CUDA_TRY(launch_iface_coefs(p, keys, n_rows, h->coef_rows, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    h->n_iface_rows = n_rows;
+    return FDTD_OK;
+}
+
 int build_probes(fdtd_handle* h) {
     h->release(h->d_probes); h->release(h->d_probe_k); h->release(h->d_probe_ids); h->release(h->ring);
     h->d_probes = nullptr; h->d_probe_k = nullptr; h->d_probe_ids = nullptr; h->ring = nullptr;
@@ -980,6 +1034,8 @@ int ensure_prepared(fdtd_handle* h) {
         rc = build_plates(h);
         if (rc) return rc;
         if (h->n_plate_nodes > 0) CUDA_TRY(launch_class_nodes(h->g, h->d_plate_nodes, h->n_plate_nodes, kPlateNode, h->cls, h->stream));
+        rc = build_interface_rows(h);
+        if (rc) return rc;
     }
     if (h->dirty_probes) {
         int rc = build_probes(h);
@@ -1103,8 +1159,8 @@ extern "C" int fdtd_step_static_scratch(fdtd_handle* h, int64_t n) {
         float* ee[3] = {h->field[a][0], h->field[a][1], h->field[a][2]};
         float* sh[3] = {sf[3], sf[4], sf[5]};
         float* se[3] = {sf[0], sf[1], sf[2]};
-        if (encode_fused_maps(&maps_h, h->g, hh, ee, h->cls, h->mat, enc) != 0 ||
-            encode_fused_maps(&maps_s, h->g, sh, se, h->cls, h->mat, enc) != 0)
+        if (encode_fused_maps(&maps_h, h->g, hh, ee, h->rec, enc) != 0 ||
+            encode_fused_maps(&maps_s, h->g, sh, se, h->rec, enc) != 0)
             return fail(FDTD_ERR_CUDA, "tensor map encoding failed");
     }
     int4* d_items = (int4*)(base + L.items);

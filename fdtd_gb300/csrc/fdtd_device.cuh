@@ -23,11 +23,21 @@ constexpr int kDefaultEntry = kMaxMaterials;  // H coefficient of faces the refe
 constexpr int kGeneral = 255;                 // node class of nodes that take the general path
 constexpr int kUniformGeneral = 128;         // classes below: fast-path nodes (the material id);
                                              // kUniformGeneral + m: general nodes whose seven cells
-                                             // all hold material m (m < kDesignNode - kUniformGeneral)
+                                             // all hold material m (m < kInterfaceNode - kUniformGeneral)
+constexpr int kInterfaceNode = 252;          // node class of interior nodes at a material interface
+                                             // (no lumped edge): the table-coefficient update with
+                                             // the coefficient row StepParams::rec gives
 constexpr int kPlateNode = 254;              // node class of nodes with a plate-covered E edge
 constexpr int kDesignNode = 253;              // node class of the design region's edge box; classes
                                               // below it are fast-path material ids
 constexpr int kDesign = 255;                  // material index of design-region cells (per-cell eps_r)
+// Coefficient rows: StepParams::coef holds the material rows 0 .. kMaxMaterials (the last one is
+// kDefaultEntry), then one row per distinct seven-cell material combination of the interface
+// nodes, from kFirstInterfaceRow. StepParams::rec holds per node its row, or kRecGeneral | class
+// for nodes on the general path.
+constexpr int kFirstInterfaceRow = kMaxMaterials + 1;
+constexpr int kRecGeneral = 0x8000;
+constexpr int kMaxInterfaceRows = kRecGeneral - kFirstInterfaceRow;
 
 // Per-material coefficients for an edge whose surrounding cells all hold the same material.
 // e[c] = {Ca, Cb_plus, Cb_minus, 0} for Ex, Ey, Ez; h[c] = {Ch, Cb_plus, Cb_minus, 0} for Hx, Hy,
@@ -97,10 +107,16 @@ struct StepParams {
     const uint8_t* mat;          // (nz, ny, pitch)
     // Node class (nz, ny, pitch): the material id when the node takes the fast path (every
     // component updated, outside the CPML slabs, no lumped edge, the seven cells of its three E
-    // edge averages all of that material), kGeneral otherwise. Built by launch_node_class.
+    // edge averages all of that material), kInterfaceNode, kUniformGeneral + m, kDesignNode,
+    // kPlateNode or kGeneral otherwise. Built by launch_node_class.
     const uint8_t* cls;
+    // Coefficient row of each node (nz, ny, pitch): the material id for fast-path nodes, the
+    // interface row for kInterfaceNode nodes, kRecGeneral | class otherwise. Built with cls.
+    const uint16_t* rec;
     const MatProps* props;       // kMaxMaterials entries
-    const MatCoef* coef;         // kMaxMaterials + 1 entries (last = reference default for H faces)
+    // kMaxMaterials + 1 material rows (the last = reference default for H faces), then the
+    // interface rows (kFirstInterfaceRow + q)
+    const MatCoef* coef;
     // 1-D CPML profiles per axis (length nx, ny, nz): b/a for E and H, kappa for E and H
     const float *bex, *aex, *bmx, *amx, *kex, *kmx;
     const float *bey, *aey, *bmy, *amy, *key, *kmy;

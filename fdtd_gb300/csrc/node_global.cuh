@@ -9,8 +9,9 @@ namespace fdtd {
 
 // One node's E (or H) update reading the fields `fi` and CPML memory `pin`, writing `fo` / `pout`
 // (the same buffers for the in-place two-pass schedule). Every node loads its twelve field values
-// and its class byte together (one round of memory latency); fast-path nodes (class != kGeneral)
-// then update from the material table, the rest also gather the seven cell materials and take
+// and its class byte together (one round of memory latency); fast-path nodes (class below
+// kUniformGeneral) then update from the material table, interface nodes from their row of the
+// coefficient table, the rest also gather the seven cell materials and take
 // e_update / h_update. kDesign (k_design_e only): skip the class test and average the per-cell
 // eps_r of design cells. kPlate (k_plate_e only): plate-covered edges take the plate's sigma_e;
 // the other kernels leave plate nodes (class kPlateNode) alone, CPML memory included.
@@ -33,13 +34,15 @@ __device__ __forceinline__ void e_node_global(const StepParams& p, const FieldPt
     nb.hz_jm = j > 0 ? fi.hz[n - R] : 0.f;
     const int c = kDesign ? kGeneral : p.cls[n];
     float out[3], pre[3];
-    if (c < kUniformGeneral) {
-        e_update_interior(p, c, nb.ex, nb.ey, nb.ez, __fsub_rn(nb.hz, nb.hz_jm), __fsub_rn(nb.hy, nb.hy_km),
+    if (c < kUniformGeneral || c == kInterfaceNode) {
+        // an interface node's coefficient row is one more load, taken only by such nodes
+        const int row = c == kInterfaceNode ? (int)p.rec[n] : c;
+        e_update_interior(p, row, nb.ex, nb.ey, nb.ez, __fsub_rn(nb.hz, nb.hz_jm), __fsub_rn(nb.hy, nb.hy_km),
                           __fsub_rn(nb.hx, nb.hx_km), __fsub_rn(nb.hz, nb.hz_im), __fsub_rn(nb.hy, nb.hy_im),
                           __fsub_rn(nb.hx, nb.hx_jm), out);
         pre[0] = out[0]; pre[1] = out[1]; pre[2] = out[2];
     } else {
-        if (c >= kUniformGeneral && c < kDesignNode) {  // seven cells of one material: no loads
+        if (c >= kUniformGeneral && c < kInterfaceNode) {  // seven cells of one material: no loads
             nb.m0 = nb.mi = nb.mj = nb.mk = nb.mij = nb.mik = nb.mjk = c - kUniformGeneral;
         } else {
             const uint8_t* mat = p.mat;
@@ -88,13 +91,14 @@ __device__ __forceinline__ void h_node_global(const StepParams& p, const FieldPt
     nb.ey_ip = i < g.nx - 1 ? fe.ey[n + 1] : 0.f;
     const int c = p.cls[n];
     float out[3], pre[3];
-    if (c < kUniformGeneral) {
-        h_update_interior(p, c, nb.hx, nb.hy, nb.hz, __fsub_rn(nb.ey_kp, nb.ey), __fsub_rn(nb.ez_jp, nb.ez),
+    if (c < kUniformGeneral || c == kInterfaceNode) {
+        const int row = c == kInterfaceNode ? (int)p.rec[n] : c;
+        h_update_interior(p, row, nb.hx, nb.hy, nb.hz, __fsub_rn(nb.ey_kp, nb.ey), __fsub_rn(nb.ez_jp, nb.ez),
                           __fsub_rn(nb.ez_ip, nb.ez), __fsub_rn(nb.ex_kp, nb.ex), __fsub_rn(nb.ex_jp, nb.ex),
                           __fsub_rn(nb.ey_ip, nb.ey), out);
         pre[0] = out[0]; pre[1] = out[1]; pre[2] = out[2];
     } else {
-        if (c >= kUniformGeneral && c < kDesignNode) {
+        if (c >= kUniformGeneral && c < kInterfaceNode) {
             nb.m0 = nb.mi = nb.mj = nb.mk = c - kUniformGeneral;
         } else {
             const uint8_t* mat = p.mat;

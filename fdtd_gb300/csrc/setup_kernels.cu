@@ -208,8 +208,9 @@ cudaError_t launch_paint(uint8_t* mat, const DeviceGrid& g, const int box[6], ui
 namespace fdtd {
 
 // Node class (StepParams::cls): material id of nodes that take the fast path (interior, seven cells
-// of one material below kUniformGeneral), kUniformGeneral + m for the other nodes whose seven cells
-// all hold material m, kGeneral otherwise.
+// of one material below kUniformGeneral), kInterfaceNode for the other interior nodes,
+// kUniformGeneral + m for the other nodes whose seven cells all hold material m, kGeneral
+// otherwise. Lumped edges (k_class_lumped) and plates turn their nodes general afterwards.
 // The seven cells are those the three E edge averages read, (i,j,k) (i-1,j,k) (i,j-1,k) (i,j,k-1)
 // (i-1,j-1,k) (i-1,j,k-1) (i,j-1,k-1); the four cells of the H faces are among them.
 // Nodes of the design region's edge box [dlo, dhi] get kDesignNode.
@@ -228,13 +229,13 @@ __global__ void k_node_class(const uint8_t* __restrict__ mat, uint8_t* __restric
     const int mij = (i > 0 && j > 0) ? mat[n - 1 - R] : 0, mik = (i > 0 && k > 0) ? mat[n - 1 - P] : 0;
     const int mjk = (j > 0 && k > 0) ? mat[n - R - P] : 0;
     const bool uniform = mi == m0 && mj == m0 && mk == m0 && mij == m0 && mik == m0 && mjk == m0;
-    if (uniform) {
-        if (interior(i, g.nx, g.pxn, g.pxp) && interior(j, g.ny, g.pyn, g.pyp) && interior(k, g.nz, g.pzn, g.pzp) &&
-            m0 < kUniformGeneral)
-            c = (uint8_t)m0;  // fast path
-        else if (m0 < kDesignNode - kUniformGeneral)
-            c = (uint8_t)(kUniformGeneral + m0);  // general path without the cell-material loads
-    }
+    const bool inner = interior(i, g.nx, g.pxn, g.pxp) && interior(j, g.ny, g.pyn, g.pyp) && interior(k, g.nz, g.pzn, g.pzp);
+    if (uniform && inner && m0 < kUniformGeneral)
+        c = (uint8_t)m0;  // fast path
+    else if (inner)
+        c = kInterfaceNode;  // table update with the coefficient row of its seven cells
+    else if (uniform && m0 < kInterfaceNode - kUniformGeneral)
+        c = (uint8_t)(kUniformGeneral + m0);  // general path without the cell-material loads
     if (i >= dlo.x && i <= dhi.x && j >= dlo.y && j <= dhi.y && k >= dlo.z && k <= dhi.z) c = kDesignNode;
     cls[n] = c;
 }
@@ -263,6 +264,118 @@ cudaError_t launch_node_class(const DeviceGrid& g, const uint8_t* mat, const Lum
     dim3 grid((g.nx + 31) / 32, (g.ny + 7) / 8, g.nz);
     k_node_class<<<grid, block, 0, st>>>(mat, cls, g, dlo, dhi);
     if (n_edges > 0) k_class_lumped<<<(n_edges + 127) / 128, 128, 0, st>>>(cls, g, edges, n_edges);
+    return cudaGetLastError();
+}
+
+}  // namespace fdtd
+
+namespace fdtd {
+
+// Interface rows. Every kInterfaceNode node is keyed by its seven cell materials, packed one byte
+// each in the order (i,j,k) (i-1,j,k) (i,j-1,k) (i,j,k-1) (i-1,j-1,k) (i-1,j,k-1) (i,j-1,k-1). The
+// keys are gathered, sorted and made unique on the host, and each unique key gets the coefficient
+// row the general path would build for such a node (e_coef / h_coef: table entries where an edge's
+// cells agree, the reference's averages otherwise), so the node's update is the table form with
+// the same bits.
+namespace {
+__device__ __forceinline__ unsigned long long cell_key(const uint8_t* mat, const DeviceGrid& g, long long n) {
+    const long long R = g.pitch, P = g.plane;  // interior nodes: every neighbour cell exists
+    return (unsigned long long)mat[n] | (unsigned long long)mat[n - 1] << 8 | (unsigned long long)mat[n - R] << 16 |
+           (unsigned long long)mat[n - P] << 24 | (unsigned long long)mat[n - 1 - R] << 32 |
+           (unsigned long long)mat[n - 1 - P] << 40 | (unsigned long long)mat[n - R - P] << 48;
+}
+}  // namespace
+
+// Keys of the kInterfaceNode nodes into keys[atomicAdd(count)] (capacity cap; count counts all).
+__global__ void k_iface_keys(const uint8_t* __restrict__ cls, const uint8_t* __restrict__ mat, DeviceGrid g,
+                             unsigned long long* keys, unsigned long long* count, long long cap) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= g.nx || j >= g.ny) return;
+    const long long n = (long long)k * g.plane + (long long)j * g.pitch + i;
+    if (cls[n] != kInterfaceNode) return;
+    const unsigned long long q = atomicAdd(count, 1ull);
+    if ((long long)q < cap) keys[q] = cell_key(mat, g, n);
+}
+
+// Coefficient rows of every node (StepParams::rec): the material id of fast-path nodes, the
+// interface row of kInterfaceNode nodes whose key is among the n_keys sorted unique keys, and
+// kRecGeneral | class for the rest. kInterfaceNode nodes without a row (more distinct keys than
+// kMaxInterfaceRows) become kGeneral.
+__global__ void k_iface_rows(uint8_t* __restrict__ cls, const uint8_t* __restrict__ mat, DeviceGrid g,
+                             const unsigned long long* __restrict__ keys, int n_keys, uint16_t* __restrict__ rec) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= g.nx || j >= g.ny) return;
+    const long long n = (long long)k * g.plane + (long long)j * g.pitch + i;
+    int c = cls[n];
+    int r = kRecGeneral | c;
+    if (c < kUniformGeneral) {
+        r = c;
+    } else if (c == kInterfaceNode) {
+        const unsigned long long key = cell_key(mat, g, n);
+        int lo = 0, hi = n_keys;  // first key >= key
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (keys[mid] < key) lo = mid + 1;
+            else hi = mid;
+        }
+        if (lo < n_keys && keys[lo] == key) {
+            r = kFirstInterfaceRow + lo;
+        } else {
+            cls[n] = kGeneral;
+            r = kRecGeneral | kGeneral;
+        }
+    }
+    rec[n] = (uint16_t)r;
+}
+
+// Coefficient row kFirstInterfaceRow + q of unique key q, from the material rows and properties.
+__global__ void k_iface_coefs(const __grid_constant__ StepParams p, const unsigned long long* __restrict__ keys,
+                              int n_keys, MatCoef* coef) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n_keys) return;
+    const unsigned long long key = keys[q];
+    const int m0 = (int)(key & 0xff), mi = (int)((key >> 8) & 0xff), mj = (int)((key >> 16) & 0xff);
+    const int mk = (int)((key >> 24) & 0xff), mij = (int)((key >> 32) & 0xff), mik = (int)((key >> 40) & 0xff);
+    const int mjk = (int)((key >> 48) & 0xff);
+    // interior node: no design cells (those nodes are kDesignNode), no CPML, no boundary face
+    const Coef3 ex = e_coef(p, 0, m0 == mj && m0 == mk && m0 == mjk, m0, mj, mk, mjk, 1, 1, 1);
+    const Coef3 ey = e_coef(p, 1, m0 == mi && m0 == mk && m0 == mik, m0, mi, mk, mik, 1, 1, 1);
+    const Coef3 ez = e_coef(p, 2, m0 == mi && m0 == mj && m0 == mij, m0, mi, mj, mij, 1, 1, 1);
+    const Coef3 hx = h_coef(p, 0, false, m0 == mi, m0, mi);
+    const Coef3 hy = h_coef(p, 1, false, m0 == mj, m0, mj);
+    const Coef3 hz = h_coef(p, 2, false, m0 == mk, m0, mk);
+    MatCoef c;
+    c.e[0] = make_float4(ex.a, ex.bp, ex.bm, 0.f);
+    c.e[1] = make_float4(ey.a, ey.bp, ey.bm, 0.f);
+    c.e[2] = make_float4(ez.a, ez.bp, ez.bm, 0.f);
+    c.h[0] = make_float4(hx.a, hx.bp, hx.bm, 0.f);
+    c.h[1] = make_float4(hy.a, hy.bp, hy.bm, 0.f);
+    c.h[2] = make_float4(hz.a, hz.bp, hz.bm, 0.f);
+    coef[kFirstInterfaceRow + q] = c;
+}
+
+cudaError_t launch_iface_keys(const DeviceGrid& g, const uint8_t* cls, const uint8_t* mat, unsigned long long* keys,
+                              unsigned long long* count, long long cap, cudaStream_t st) {
+    const dim3 block(32, 8, 1), grid((g.nx + 31) / 32, (g.ny + 7) / 8, g.nz);
+    k_iface_keys<<<grid, block, 0, st>>>(cls, mat, g, keys, count, cap);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_iface_rows(const DeviceGrid& g, uint8_t* cls, const uint8_t* mat, const unsigned long long* keys,
+                              int n_keys, uint16_t* rec, cudaStream_t st) {
+    const dim3 block(32, 8, 1), grid((g.nx + 31) / 32, (g.ny + 7) / 8, g.nz);
+    k_iface_rows<<<grid, block, 0, st>>>(cls, mat, g, keys, n_keys, rec);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_iface_coefs(const StepParams& p, const unsigned long long* keys, int n_keys, MatCoef* coef,
+                               cudaStream_t st) {
+    if (n_keys <= 0) return cudaSuccess;
+    k_iface_coefs<<<(n_keys + 127) / 128, 128, 0, st>>>(p, keys, n_keys, coef);
     return cudaGetLastError();
 }
 

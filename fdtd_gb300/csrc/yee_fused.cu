@@ -4,16 +4,17 @@
 // Interior sweep. A work item is a 32 x 16 column of nodes and a plane range [k0, k1) inside the
 // interior (no CPML, no boundary planes). Planes stream through a 3-stage shared-memory ring
 // filled by TMA (cp.async.bulk.tensor, 3-D tiles of this GPU's HBM, one plane ahead of the one
-// computed): H with a one-node halo, old E, and the node-class byte. At plane k the CTA
+// computed): H with a one-node halo, old E, and the coefficient row of each node (16 bits:
+// StepParams::rec). At plane k the CTA
 //   1. computes E(k) on its tile plus one column / row beyond the high x / y edges (the H update
 //      needs those E values; they are recomputed from the old fields instead of being exchanged),
 //      storing only its own nodes;
 //   2. computes H(k-1) of its own nodes from E(k-1), E(k) (shared memory) and H(k-1) (the ring).
 // Each thread owns two nodes of a plane (rows ty and ty + 8), which gives every warp two
 // independent update chains and halves the per-plane overhead per node. Each field value crosses
-// HBM once per step in each direction (24 B read + 24 B written per cell) plus the class byte.
-// Nodes of class kGeneral (material interfaces, lumped edges) leave the fast path through an
-// out-of-line call. The shell passes (yee_two_pass.cu) run before (E) and after (H) the sweep.
+// HBM once per step in each direction (24 B read + 24 B written per cell) plus the 2-byte row.
+// Fast-path and interface nodes update from their coefficient row; the other nodes (lumped
+// edges, plates) leave the fast path through an out-of-line call. The shell passes (yee_two_pass.cu) run before (E) and after (H) the sweep.
 // All schedules use the arithmetic of yee_common.cuh, so the results are bit-identical. Every
 // wait on a TMA barrier is bounded: on timeout the kernel records an error in the status word,
 // drains its own copies (again bounded) and exits.
@@ -43,27 +44,21 @@ constexpr int NSTAGE = FDTD_FUSED_NSTAGE;   // planes resident in the ring
 constexpr int AHEAD = FDTD_FUSED_AHEAD;     // planes loaded ahead of the one computed (<= NSTAGE - 2)
 constexpr int HW = TX + 8, HH = TY + 2;     // H tile: x in [x0-4, x0+TX+4), y in [y0-1, y0+TY+1)
 constexpr int EW = TX + 4, EH = TY + 1;     // old-E tile: x in [x0, x0+TX+4), y in [y0, y0+TY+1)
-constexpr int MW = TX + 32, MH = TY + 2;    // class tile: x in [x0-16, x0+TX+16), y in [y0-1, ...)
+constexpr int MW = TX + 32, MH = TY + 2;    // row tile: x in [x0-16, x0+TX+16), y in [y0-1, ...)
 constexpr int NW = TX + 1, NH = TY + 1;     // new-E plane: x in [x0, x0+TX], y in [y0, y0+TY]
 
 constexpr int round128(int b) { return (b + 127) / 128 * 128; }
 constexpr int H_BYTES = round128(HW * HH * 4);
 constexpr int E_BYTES = round128(EW * EH * 4);
-constexpr int M_BYTES = round128(MW * MH);
+constexpr int M_BYTES = round128(MW * MH * 2);
 constexpr int STAGE_BYTES = 3 * H_BYTES + 3 * E_BYTES + M_BYTES;
-constexpr unsigned TX_BYTES = 3u * HW * HH * 4 + 3u * EW * EH * 4 + MW * MH;  // bytes the TMA boxes carry
+constexpr unsigned TX_BYTES = 3u * HW * HH * 4 + 3u * EW * EH * 4 + MW * MH * 2;  // bytes the TMA boxes carry
 constexpr int N_FLOATS = NW * NH;
 constexpr int ENEW_BYTES = 2 * 3 * N_FLOATS * 4;
 constexpr int NHALO = TX + TY + 1;  // row y0 + TY (warp 0) and column x0 + TX (warp 1)
 constexpr int kMaxItemPlanes = 512;  // planes streamed by one item (chunk + 2); bounds the flag array
-// Material tiles (same box as the class tile) in a ring of their own: H(k-1) reads the materials of
-// plane k-2, whose ring stage is being refilled with plane k+1 while plane k is computed.
-constexpr int MAT_SLOTS = 4;
-constexpr unsigned MAT_TX_BYTES = MW * MH;
-constexpr int SMEM_INTERIOR = NSTAGE * STAGE_BYTES + MAT_SLOTS * M_BYTES + ENEW_BYTES + NSTAGE * 8 + kMaxItemPlanes;
-static_assert((NSTAGE * STAGE_BYTES + MAT_SLOTS * M_BYTES + ENEW_BYTES) % 8 == 0, "mbarriers need 8-byte alignment");
+constexpr int SMEM_INTERIOR = NSTAGE * STAGE_BYTES + ENEW_BYTES + NSTAGE * 8 + kMaxItemPlanes;
 static_assert(NSTAGE >= AHEAD + 2, "the ring recycles the stage of plane k - 2 at plane k");
-static_assert(MAT_SLOTS >= AHEAD + 3, "material tiles of planes k - 2 .. k + AHEAD are resident at plane k");
 static_assert(NHALO <= 64, "halo nodes live on the first two warps");
 
 constexpr int kShellRows = 8;  // rows of a shell item (the shell kernels' block is 32 x 8)
@@ -106,27 +101,28 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
 }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-// Arrays of one ring stage: H tile (3), old-E tile (3), class tile, at fixed offsets.
+// Arrays of one ring stage: H tile (3), old-E tile (3), coefficient-row tile, at fixed offsets.
 struct StageView {
     const unsigned char* base;
     __device__ explicit StageView(const unsigned char* b) : base(b) {}
     __device__ const float* h(int c) const { return reinterpret_cast<const float*>(base + c * H_BYTES); }
     __device__ const float* e(int c) const { return reinterpret_cast<const float*>(base + 3 * H_BYTES + c * E_BYTES); }
-    __device__ const uint8_t* m() const { return base + 3 * H_BYTES + 3 * E_BYTES; }
+    __device__ const uint16_t* m() const { return reinterpret_cast<const uint16_t*>(base + 3 * H_BYTES + 3 * E_BYTES); }
 };
 
-// Slow paths of the interior kernel, out of line: nodes at a material interface or on a lumped
-// edge (node class kGeneral). The cell materials come from the material tiles in shared memory
-// (packed one byte each: m0 | mi << 8 | mj << 16 | mk << 24, and mij | mik << 8 | mjk << 16 for
-// E); the coefficients are the table entry where the cells of an edge agree and the reference's
-// averages otherwise (e_coef_mixed / h_coef_mixed), then the lumped override (calc_e
-// fdtdrav.h:720-741).
+// Slow paths of the interior kernel, out of line: nodes on the general path (lumped edges, plate
+// nodes, interface nodes beyond the coefficient table's capacity). The cell materials come from the index in global memory; the
+// coefficients are the table entry where the cells of an edge agree and the reference's averages
+// otherwise (e_coef_mixed / h_coef_mixed), then the lumped override (calc_e fdtdrav.h:720-741).
 static __device__ __noinline__ float3 e_slow(const StepParams* pp, int i, int j, int k, long long m, int plane_lumped,
-                                             unsigned mats0, unsigned mats1, float ex, float ey, float ez, float dHz_j,
-                                             float dHy_k, float dHx_k, float dHz_i, float dHy_i, float dHx_j) {
+                                             float ex, float ey, float ez, float dHz_j, float dHy_k, float dHx_k,
+                                             float dHz_i, float dHy_i, float dHx_j) {
     const StepParams& p = *pp;
-    const int m0 = mats0 & 0xff, mi = (mats0 >> 8) & 0xff, mj = (mats0 >> 16) & 0xff, mk = mats0 >> 24;
-    const int mij = mats1 & 0xff, mik = (mats1 >> 8) & 0xff, mjk = (mats1 >> 16) & 0xff;
+    const DeviceGrid& g = p.g;
+    const long long R = g.pitch, P = g.plane, n = (long long)k * P + (long long)j * R + i;
+    const uint8_t* mat = p.mat;
+    const int m0 = mat[n], mi = mat[n - 1], mj = mat[n - R], mk = mat[n - P];
+    const int mij = mat[n - 1 - R], mik = mat[n - 1 - P], mjk = mat[n - R - P];
     Coef3 cx = e_coef(p, 0, m0 == mj && m0 == mk && m0 == mjk, m0, mj, mk, mjk, i, j, k);
     Coef3 cy = e_coef(p, 1, m0 == mi && m0 == mk && m0 == mik, m0, mi, mk, mik, i, j, k);
     Coef3 cz = e_coef(p, 2, m0 == mi && m0 == mj && m0 == mij, m0, mi, mj, mij, i, j, k);
@@ -154,12 +150,13 @@ static __device__ __noinline__ float3 e_slow(const StepParams* pp, int i, int j,
     return r;
 }
 
-static __device__ __noinline__ float3 h_slow(const StepParams* pp, unsigned mats0, float hx, float hy, float hz,
+static __device__ __noinline__ float3 h_slow(const StepParams* pp, int i, int j, int k, float hx, float hy, float hz,
                                              float dEy_k, float dEz_j, float dEz_i, float dEx_k, float dEx_j,
                                              float dEy_i) {
     const StepParams& p = *pp;
     const DeviceGrid& g = p.g;
-    const int m0 = mats0 & 0xff, mi = (mats0 >> 8) & 0xff, mj = (mats0 >> 16) & 0xff, mk = mats0 >> 24;
+    const long long n = (long long)k * g.plane + (long long)j * g.pitch + i;
+    const int m0 = p.mat[n], mi = p.mat[n - 1], mj = p.mat[n - g.pitch], mk = p.mat[n - g.plane];
     const MatCoef* mc = p.coef + m0;
     Coef3 cx, cy, cz;
     if (m0 == mi) { const float4 c = __ldg(&mc->h[0]); cx = Coef3{c.x, c.y, c.z}; }
@@ -172,7 +169,7 @@ static __device__ __noinline__ float3 h_slow(const StepParams* pp, unsigned mats
                        upd3(cz.a, hz, cz.bp, dEx_j, cz.bm, dEy_i));
 }
 
-// Inputs of one E node read from the ring: old E, the six H differences and the node class.
+// Inputs of one E node read from the ring: old E, the six H differences and the coefficient row.
 struct EIn {
     float ex, ey, ez, dHz_j, dHy_k, dHx_k, dHz_i, dHy_i, dHx_j;
     int c;
@@ -196,18 +193,13 @@ __device__ __forceinline__ float3 e_fast(const StepParams& p, const EIn& a) {
     return make_float3(upd3(x.x, a.ex, x.y, a.dHz_j, x.z, a.dHy_k), upd3(y.x, a.ey, y.y, a.dHx_k, y.z, a.dHz_i),
                        upd3(z.x, a.ez, z.y, a.dHy_i, z.z, a.dHx_j));
 }
-// mc / mp: material tiles of planes k and k - 1; t: the node's offset in them.
-__device__ __forceinline__ float3 e_any(const StepParams& p, const EIn& a, int i, int j, int k, long long m, int lumped,
-                                        const uint8_t* mc, const uint8_t* mp, int t) {
-    if (a.c < kUniformGeneral) return e_fast(p, a);
-    const unsigned mats0 = mc[t] | (unsigned)mc[t - 1] << 8 | (unsigned)mc[t - MW] << 16 | (unsigned)mp[t] << 24;
-    const unsigned mats1 = mc[t - 1 - MW] | (unsigned)mp[t - 1] << 8 | (unsigned)mp[t - MW] << 16;
-    return e_slow(&p, i, j, k, m, lumped, mats0, mats1, a.ex, a.ey, a.ez, a.dHz_j, a.dHy_k, a.dHx_k, a.dHz_i, a.dHy_i,
-                  a.dHx_j);
+__device__ __forceinline__ float3 e_any(const StepParams& p, const EIn& a, int i, int j, int k, long long m, int lumped) {
+    if (a.c < kRecGeneral) return e_fast(p, a);
+    return e_slow(&p, i, j, k, m, lumped, a.ex, a.ey, a.ez, a.dHz_j, a.dHy_k, a.dHx_k, a.dHz_i, a.dHy_i, a.dHx_j);
 }
 
 // Inputs of one H node: old H, the six new-E differences (from the E planes k-1 and k in shared
-// memory) and the node class.
+// memory) and the coefficient row.
 struct HIn {
     float hx, hy, hz, dEy_k, dEz_j, dEz_i, dEx_k, dEx_j, dEy_i;
     int c;
@@ -228,11 +220,9 @@ __device__ __forceinline__ float3 h_fast(const StepParams& p, const HIn& a) {
     return make_float3(upd3_hx(x.x, a.hx, x.y, a.dEy_k, x.z, a.dEz_j), upd3(y.x, a.hy, y.y, a.dEz_i, y.z, a.dEx_k),
                        upd3(z.x, a.hz, z.y, a.dEx_j, z.z, a.dEy_i));
 }
-// mc / mp: material tiles of planes kh and kh - 1; t: the node's offset in them.
-__device__ __forceinline__ float3 h_any(const StepParams& p, const HIn& a, const uint8_t* mc, const uint8_t* mp, int t) {
-    if (a.c < kUniformGeneral) return h_fast(p, a);
-    const unsigned mats0 = mc[t] | (unsigned)mc[t - 1] << 8 | (unsigned)mc[t - MW] << 16 | (unsigned)mp[t] << 24;
-    return h_slow(&p, mats0, a.hx, a.hy, a.hz, a.dEy_k, a.dEz_j, a.dEz_i, a.dEx_k, a.dEx_j, a.dEy_i);
+__device__ __forceinline__ float3 h_any(const StepParams& p, const HIn& a, int i, int j, int k) {
+    if (a.c < kRecGeneral) return h_fast(p, a);
+    return h_slow(&p, i, j, k, a.hx, a.hy, a.hz, a.dEy_k, a.dEz_j, a.dEz_i, a.dEx_k, a.dEx_j, a.dEy_i);
 }
 
 __device__ __forceinline__ void store3(float* a, float* b, float* c, long long n, float3 v) {
@@ -248,9 +238,8 @@ __global__ void __launch_bounds__(NTH, FDTD_FUSED_MIN_BLOCKS)
 k_sweep_interior(const __grid_constant__ FusedMaps maps, const __grid_constant__ StepParams p, FieldPtrs fo,
                  const int4* __restrict__ items, long long m) {
     extern __shared__ __align__(128) unsigned char smem[];
-    uint8_t* mring = smem + NSTAGE * STAGE_BYTES;  // material tile of plane q in slot q % MAT_SLOTS
-    float* enew = reinterpret_cast<float*>(mring + MAT_SLOTS * M_BYTES);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(enew) + ENEW_BYTES);
+    float* enew = reinterpret_cast<float*>(smem + NSTAGE * STAGE_BYTES);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + NSTAGE * STAGE_BYTES + ENEW_BYTES);
     uint8_t* pflags = reinterpret_cast<uint8_t*>(bars + NSTAGE);  // per plane: bit 0 lumped edges, bit 1 probes
     const DeviceGrid& g = p.g;
     const int tid = threadIdx.x;
@@ -280,11 +269,10 @@ k_sweep_interior(const __grid_constant__ FusedMaps maps, const __grid_constant__
     __syncthreads();
     auto issue = [&](int k, int s) {
         unsigned char* st = smem + s * STAGE_BYTES;
-        mbar_expect_tx(&bars[s], TX_BYTES + MAT_TX_BYTES);
+        mbar_expect_tx(&bars[s], TX_BYTES);
         for (int c = 0; c < 3; ++c) tma_load_3d(st + c * H_BYTES, &maps.h[c], &bars[s], x0 - 4, y0 - 1, k);
         for (int c = 0; c < 3; ++c) tma_load_3d(st + 3 * H_BYTES + c * E_BYTES, &maps.e[c], &bars[s], x0, y0, k);
-        tma_load_3d(st + 3 * H_BYTES + 3 * E_BYTES, &maps.cls, &bars[s], x0 - 16, y0 - 1, k);
-        tma_load_3d(mring + (k % MAT_SLOTS) * M_BYTES, &maps.mat, &bars[s], x0 - 16, y0 - 1, k);
+        tma_load_3d(st + 3 * H_BYTES + 3 * E_BYTES, &maps.rec, &bars[s], x0 - 16, y0 - 1, k);
     };
     if (tid == 0)
         for (int q = 0; q < AHEAD && kfirst + q <= klast; ++q) issue(kfirst + q, q);
@@ -301,20 +289,18 @@ k_sweep_interior(const __grid_constant__ FusedMaps maps, const __grid_constant__
         const StageView prv(smem + s_prv * STAGE_BYTES);
         float* en_cur = enew + (k & 1) * 3 * N_FLOATS;
         const float* en_prv = enew + ((k - 1) & 1) * 3 * N_FLOATS;
-        const uint8_t* mt_cur = mring + (k % MAT_SLOTS) * M_BYTES;
-        const uint8_t* mt_prv = mring + ((k - 1) % MAT_SLOTS) * M_BYTES;  // k - 1 >= kfirst >= 0
         if (k >= k0) {
             // ---- E(k): own nodes (stored below plane k1), then the halo nodes ----
             const int fl = pflags[k - kfirst];
             const EIn a0 = e_load(cur, prv, hi, ei, mi);
             const EIn a1 = e_load(cur, prv, hi + RSTEP * HW, ei + RSTEP * EW, mi + RSTEP * MW);
             float3 v0, v1;
-            if (a0.c < kUniformGeneral && a1.c < kUniformGeneral) {
+            if (a0.c < kRecGeneral && a1.c < kRecGeneral) {
                 v0 = e_fast(p, a0);
                 v1 = e_fast(p, a1);
             } else {
-                v0 = e_any(p, a0, i, j, k, m, fl & 1, mt_cur, mt_prv, mi);
-                v1 = e_any(p, a1, i, j + RSTEP, k, m, fl & 1, mt_cur, mt_prv, mi + RSTEP * MW);
+                v0 = e_any(p, a0, i, j, k, m, fl & 1);
+                v1 = e_any(p, a1, i, j + RSTEP, k, m, fl & 1);
             }
             en_cur[ni] = v0.x; en_cur[N_FLOATS + ni] = v0.y; en_cur[2 * N_FLOATS + ni] = v0.z;
             const int ni1 = ni + RSTEP * NW;
@@ -331,7 +317,7 @@ k_sweep_interior(const __grid_constant__ FusedMaps maps, const __grid_constant__
             }
             if (halo) {
                 const EIn a = e_load(cur, prv, hhi, hei, hmi);
-                const float3 w = e_any(p, a, x0 + hpx, y0 + hpy, k, m, fl & 1, mt_cur, mt_prv, hmi);
+                const float3 w = e_any(p, a, x0 + hpx, y0 + hpy, k, m, fl & 1);
                 en_cur[hni] = w.x; en_cur[N_FLOATS + hni] = w.y; en_cur[2 * N_FLOATS + hni] = w.z;
             }
         }
@@ -341,13 +327,12 @@ k_sweep_interior(const __grid_constant__ FusedMaps maps, const __grid_constant__
             const HIn a0 = h_load(prv, en_prv, en_cur, hi, mi, ni);
             const HIn a1 = h_load(prv, en_prv, en_cur, hi + RSTEP * HW, mi + RSTEP * MW, ni + RSTEP * NW);
             float3 v0, v1;
-            if (a0.c < kUniformGeneral && a1.c < kUniformGeneral) {
+            if (a0.c < kRecGeneral && a1.c < kRecGeneral) {
                 v0 = h_fast(p, a0);
                 v1 = h_fast(p, a1);
             } else {
-                const uint8_t* mt_pp = mring + ((kh - 1) % MAT_SLOTS) * M_BYTES;  // kh - 1 >= kfirst
-                v0 = h_any(p, a0, mt_prv, mt_pp, mi);
-                v1 = h_any(p, a1, mt_prv, mt_pp, mi + RSTEP * MW);
+                v0 = h_any(p, a0, i, j, kh);
+                v1 = h_any(p, a1, i, j + RSTEP, kh);
             }
             const long long n = (long long)kh * g.plane + n_own;
             store3(fo.hx, fo.hy, fo.hz, n, v0);
@@ -409,16 +394,17 @@ cudaError_t launch_fused(const FusedMaps& maps, const StepParams& p, const Field
 }
 
 // Tensor maps of the buffers the interior sweep reads: H tiles with a one-node halo (x widened to
-// 16-byte boundaries), old-E tiles, node-class tiles. Coordinates outside the arrays load as zeros.
-int encode_fused_maps(FusedMaps* out, const DeviceGrid& g, float* const h[3], float* const e[3], const uint8_t* cls,
-                      const uint8_t* mat, void* encode_fn) {
+// 16-byte boundaries), old-E tiles, coefficient-row tiles. Coordinates outside the arrays load as
+// zeros.
+int encode_fused_maps(FusedMaps* out, const DeviceGrid& g, float* const h[3], float* const e[3], const uint16_t* rec,
+                      void* encode_fn) {
     auto encode = reinterpret_cast<CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
                                                 CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
                                                 CUtensorMapFloatOOBfill)>(encode_fn);
     const cuuint64_t dims[3] = {(cuuint64_t)g.pitch, (cuuint64_t)g.ny, (cuuint64_t)g.nz};
     const cuuint64_t fstr[2] = {(cuuint64_t)g.pitch * 4, (cuuint64_t)g.plane * 4};
-    const cuuint64_t mstr[2] = {(cuuint64_t)g.pitch, (cuuint64_t)g.plane};
+    const cuuint64_t mstr[2] = {(cuuint64_t)g.pitch * 2, (cuuint64_t)g.plane * 2};
     const cuuint32_t hbox[3] = {HW, HH, 1}, ebox[3] = {EW, EH, 1}, mbox[3] = {MW, MH, 1}, es[3] = {1, 1, 1};
     for (int c = 0; c < 3; ++c) {
         if (encode(&out->h[c], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, h[c], dims, fstr, hbox, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -428,10 +414,7 @@ int encode_fused_maps(FusedMaps* out, const DeviceGrid& g, float* const h[3], fl
                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
             return -1;
     }
-    if (encode(&out->cls, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, (void*)cls, dims, mstr, mbox, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-        return -1;
-    if (encode(&out->mat, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, (void*)mat, dims, mstr, mbox, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+    if (encode(&out->rec, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, (void*)rec, dims, mstr, mbox, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return -1;
     return 0;
@@ -442,8 +425,9 @@ int encode_fused_maps(FusedMaps* out, const DeviceGrid& g, float* const h[3], fl
 // else (boundary / CPML tiles, and the z-boundary and z-CPML planes of interior tiles) becomes
 // shell items of one plane and half a tile. The E positions of plane k1 of an item are recomputed, so a chunk must also keep
 // its top plane in the interior range to stay interior. The tile grid starts at (ox, oy) <= 0,
-// chosen to put as many nodes as possible in interior tiles; ox is a multiple of 16 so that every
-// TMA box starts on a 16-byte boundary (material box at x0 - 16, one byte per cell).
+// chosen to put as many nodes as possible in interior tiles; ox is a multiple of 8 so that every
+// TMA box starts on a 16-byte boundary (H box at x0 - 4, four bytes per node; row box at x0 - 16,
+// two bytes per node).
 void plan_fused(const DeviceGrid& g, int kc, const int* design_box, std::vector<int4>& interior_items,
                 std::vector<int4>& general_items) {
     interior_items.clear();
@@ -458,7 +442,7 @@ void plan_fused(const DeviceGrid& g, int kc, const int* design_box, std::vector<
         return c;
     };
     int ox = 0, oy = 0, best_x = -1, best_y = -1;
-    for (int o = 0; o > -TX; o -= 16) {
+    for (int o = 0; o > -TX; o -= 8) {
         const int c = interior_tiles(o, TX, g.nx, g.pxn, g.pxp);
         if (c > best_x) { best_x = c; ox = o; }
     }

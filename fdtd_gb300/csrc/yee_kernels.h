@@ -42,13 +42,12 @@ cudaError_t launch_shell(bool e_pass, const StepParams& p, const FieldPtrs& fi, 
                          const PsiSet& pout, const int4* items, int n_items, long long m, cudaStream_t st);
 
 // Fused schedule (yee_fused.cu): per step the shell E pass, the z-marching interior sweep (TMA
-// tiles of buffer A: H with halo, old E, node class) and the shell H pass; fields A -> B, CPML
+// tiles of buffer A: H with halo, old E, coefficient rows) and the shell H pass; fields A -> B, CPML
 // memory psi_in -> psi_out.
 struct FusedMaps {
     CUtensorMap h[3];
     CUtensorMap e[3];
-    CUtensorMap cls;
-    CUtensorMap mat;  // material index (same box as cls), read by the interface-node path
+    CUtensorMap rec;  // coefficient rows (StepParams::rec)
 };
 // Work items of one step (device arrays of int4): interior items {x0, y0, k0, k1} for the sweep
 // (a 32 x 16 column over planes [k0, k1)), general items {x0, y0, k, 0} for the shell passes
@@ -71,8 +70,8 @@ void plan_fused(const DeviceGrid& g, int kc, const int* design_box, std::vector<
 cudaError_t launch_fused(const FusedMaps& maps, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo,
                          const PsiSet& psi_in, const PsiSet& psi_out, long long m, const FusedWork& w, cudaStream_t st);
 // encode_fn: the driver's cuTensorMapEncodeTiled. Returns 0 on success.
-int encode_fused_maps(FusedMaps* out, const DeviceGrid& g, float* const h[3], float* const e[3], const uint8_t* cls,
-                      const uint8_t* mat, void* encode_fn);
+int encode_fused_maps(FusedMaps* out, const DeviceGrid& g, float* const h[3], float* const e[3], const uint16_t* rec,
+                      void* encode_fn);
 
 // Setup kernels (setup_kernels.cu).
 cudaError_t launch_cpml_profiles(const DeviceGrid& g, float pi, float* const prof[18], cudaStream_t st);
@@ -93,5 +92,15 @@ cudaError_t launch_class_nodes(const DeviceGrid& g, const int4* nodes, int n, in
 cudaError_t launch_node_class(const DeviceGrid& g, const uint8_t* mat, const LumpedEdge* edges, int n_edges,
                               const int* design_box, uint8_t* cls, cudaStream_t st);
 cudaError_t launch_paint(uint8_t* mat, const DeviceGrid& g, const int box[6], uint8_t value, cudaStream_t st);
+// Interface rows (setup_kernels.cu): the seven-cell keys of the kInterfaceNode nodes (at most cap
+// of them into keys, *count = all of them), then, from the sorted unique keys, the per-node
+// coefficient rows (StepParams::rec; nodes without a row become kGeneral) and the rows themselves
+// (p: the handle's parameters with the material rows in place).
+cudaError_t launch_iface_keys(const DeviceGrid& g, const uint8_t* cls, const uint8_t* mat, unsigned long long* keys,
+                              unsigned long long* count, long long cap, cudaStream_t st);
+cudaError_t launch_iface_rows(const DeviceGrid& g, uint8_t* cls, const uint8_t* mat, const unsigned long long* keys,
+                              int n_keys, uint16_t* rec, cudaStream_t st);
+cudaError_t launch_iface_coefs(const StepParams& p, const unsigned long long* keys, int n_keys, MatCoef* coef,
+                               cudaStream_t st);
 
 }  // namespace fdtd
