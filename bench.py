@@ -217,10 +217,14 @@ def cpu_baseline(sc_full, seconds_budget=20.0):
 TWO_PASS_DRAM_BYTES_PER_CELL = 78.15
 
 
-def measured_traffic(args, cells):
-    if args.schedule == 2:
-        return None  # the fused schedule has no capture of its own
-    return round(TWO_PASS_DRAM_BYTES_PER_CELL * cells)
+# DRAM bytes per cell update of one fused step (k_shell_e + k_sweep_interior + k_shell_h), from an
+# ncu capture of the 256^3 random-box case; None until captured.
+FUSED_DRAM_BYTES_PER_CELL = None
+
+
+def measured_traffic(schedule, cells):
+    per_cell = FUSED_DRAM_BYTES_PER_CELL if schedule == 2 else TWO_PASS_DRAM_BYTES_PER_CELL
+    return None if per_cell is None else round(per_cell * cells)
 
 
 def bench_ours(args, rank, world):
@@ -239,9 +243,11 @@ def bench_ours(args, rank, world):
     sim = solver.Simulation.from_scenario(sc, args.schedule, material_index=mat, probe_capacity=total_steps)
     sim.set_stream(stream.cuda_stream)
     sim.prepare()
+    sim.tune_schedule()  # AUTO: time both schedules on this grid (state kept) and keep the faster
     sim.step(args.warmup)
     sim.synchronize()
-    launches_per_step = 2  # two-pass: E and H kernels; fused: interior and general sweeps
+    active = sim.active_schedule
+    launches_per_step = 3 if active == 2 else 2  # fused: shell E, sweep, shell H; two-pass: E and H
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     clocks = ClockSampler(torch.cuda.current_device())
@@ -270,10 +276,12 @@ def bench_ours(args, rank, world):
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (seeded random-box scenario)",
            "config": {"workload": desc, "cells": N, "grid": [sc.nx, sc.ny, sc.nz], "cpml": 10,
-                      "schedule": {0: "auto", 1: "two-pass", 2: "fused"}[args.schedule],
+                      "schedule": {0: "auto", 1: "two-pass", 2: "fused"}[args.schedule] +
+                                  (" (fused)" if args.schedule == 0 and active == 2 else
+                                   " (two-pass)" if args.schedule == 0 else ""),
                       "l2": "inputs larger than L2 (fields 24 B/cell x 134M cells)", "parallelism": f"replicas{world}"},
            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                        "frac": round(achieved / peak, 4), "traffic": measured_traffic(args, N),
+                        "frac": round(achieved / peak, 4), "traffic": measured_traffic(active, N),
                         "bytes_per_cell_update": round(B, 3), "peak_source": peak_kind,
                         "kernel": "one full time step (all update launches of the step)"},
            "gpu_launches": launches_per_step * args.steps, "clocks": clk}

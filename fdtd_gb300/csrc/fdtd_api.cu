@@ -73,6 +73,7 @@ struct fdtd_handle {
     DeviceGrid g{};
     cudaStream_t stream = nullptr;
     int schedule = FDTD_SCHEDULE_AUTO;
+    int auto_choice = FDTD_SCHEDULE_AUTO;  // AUTO: the schedule its trial chose (AUTO = none yet)
     int device = 0;
 
     // device state: two field buffers and two CPML memory sets; `cur` holds the current step.
@@ -327,9 +328,28 @@ int ensure_fused(fdtd_handle* h) {
     return FDTD_OK;
 }
 
-// AUTO takes the two-pass schedule: on GB300 it is faster than the fused schedule on the random-box
-// workload with sources and probes (512^3, 64 boxes, 10-cell CPML: 56.4 against 49.0 Gcell/s).
-bool use_fused(const fdtd_handle* h) { return h->schedule == FDTD_SCHEDULE_FUSED; }
+// AUTO runs two-pass until a trial on the handle's own grid has chosen (auto_trial).
+bool use_fused(const fdtd_handle* h) {
+    return h->schedule == FDTD_SCHEDULE_FUSED ||
+           (h->schedule == FDTD_SCHEDULE_AUTO && h->auto_choice == FDTD_SCHEDULE_FUSED);
+}
+
+// Frees what ensure_fused allocated; the state must be in buffer 0.
+void release_fused(fdtd_handle* h) {
+    for (int c = 0; c < 6; ++c) {
+        h->release(h->field[1][c]);
+        h->field[1][c] = nullptr;
+    }
+    for (int f = 0; f < 6; ++f) {
+        float* a[4];
+        psi_arrays(h, 1, f, a);
+        for (float* x : a) h->release(x);
+        h->psi[1].f[f] = PsiFace{};
+    }
+    h->release((void*)h->work.interior);
+    h->work = FusedWork{};
+    h->have_second = false;
+}
 
 }  // namespace
 
@@ -432,6 +452,7 @@ int fdtd_set_schedule(fdtd_handle* h, int32_t schedule) {
     if (!h) return fail(FDTD_ERR_INVALID, "handle is NULL");
     if (schedule < FDTD_SCHEDULE_AUTO || schedule > FDTD_SCHEDULE_FUSED) return fail(FDTD_ERR_INVALID, "unknown schedule");
     h->schedule = schedule;
+    h->auto_choice = FDTD_SCHEDULE_AUTO;  // AUTO runs its trial again
     return FDTD_OK;
 }
 
@@ -573,25 +594,23 @@ int fdtd_prepare(fdtd_handle* h) {
     return ensure_prepared(h);
 }
 
-int fdtd_step(fdtd_handle* h, int64_t n) {
-    if (!h) return fail(FDTD_ERR_INVALID, "handle is NULL");
-    if (n < 0) return fail(FDTD_ERR_INVALID, "negative step count");
-    int rc = ensure_prepared(h);
+namespace {
+
+int steps_fused(fdtd_handle* h, const StepParams& p, int64_t n) {
+    int rc = ensure_fused(h);
     if (rc) return rc;
-    StepParams p = make_params(h);
-    if (use_fused(h)) {
-        rc = ensure_fused(h);
-        if (rc) return rc;
-        for (int64_t s = 0; s < n; ++s) {
-            const int a = h->cur, b = 1 - h->cur;
-            FieldPtrs fi{h->field[a][0], h->field[a][1], h->field[a][2], h->field[a][3], h->field[a][4], h->field[a][5]};
-            FieldPtrs fo{h->field[b][0], h->field[b][1], h->field[b][2], h->field[b][3], h->field[b][4], h->field[b][5]};
-            CUDA_TRY(launch_fused(h->maps[a], p, fi, fo, h->psi[a], h->psi[b], h->step, h->work, h->stream));
-            h->cur = b;
-            ++h->step;
-        }
-        return FDTD_OK;
+    for (int64_t s = 0; s < n; ++s) {
+        const int a = h->cur, b = 1 - h->cur;
+        FieldPtrs fi{h->field[a][0], h->field[a][1], h->field[a][2], h->field[a][3], h->field[a][4], h->field[a][5]};
+        FieldPtrs fo{h->field[b][0], h->field[b][1], h->field[b][2], h->field[b][3], h->field[b][4], h->field[b][5]};
+        CUDA_TRY(launch_fused(h->maps[a], p, fi, fo, h->psi[a], h->psi[b], h->step, h->work, h->stream));
+        h->cur = b;
+        ++h->step;
     }
+    return FDTD_OK;
+}
+
+int steps_two_pass(fdtd_handle* h, const StepParams& p, int64_t n) {
     const int a = h->cur;
     FieldPtrs f{h->field[a][0], h->field[a][1], h->field[a][2], h->field[a][3], h->field[a][4], h->field[a][5]};
     for (int64_t s = 0; s < n; ++s) {
@@ -599,6 +618,69 @@ int fdtd_step(fdtd_handle* h, int64_t n) {
         ++h->step;
     }
     return FDTD_OK;
+}
+
+// The AUTO trial: on grids of at least kAutoTrialCells cells, the first fdtd_step call of at least
+// 2 * kAutoTrialSteps steps times kAutoTrialSteps fused steps and then as many two-pass steps (real
+// steps: both schedules give the same bits) and keeps the faster schedule for the handle. Which one
+// wins depends on the grid: on GB300 the fused sweep is faster on 384^3 to 512^3 random-box grids,
+// two-pass on smaller ones and on the 1024 x 1024 x 896 one. Smaller grids take two-pass without a
+// trial. The fused buffers are freed when two-pass wins or cannot be allocated.
+constexpr int64_t kAutoTrialSteps = 4;
+constexpr long long kAutoTrialCells = 48LL << 20;
+
+int auto_trial(fdtd_handle* h, const StepParams& p) {
+    if (ensure_fused(h) != FDTD_OK) {  // no room for the second buffers
+        cudaGetLastError();
+        if (h->cur == 0) release_fused(h);
+        h->auto_choice = FDTD_SCHEDULE_TWO_PASS;
+        return FDTD_OK;
+    }
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    struct Guard {
+        cudaEvent_t* e;
+        ~Guard() {
+            for (int q = 0; q < 3; ++q)
+                if (e[q]) cudaEventDestroy(e[q]);
+        }
+    } guard{ev};
+    for (cudaEvent_t& e : ev) CUDA_TRY(cudaEventCreate(&e));
+    CUDA_TRY(cudaEventRecord(ev[0], h->stream));
+    int rc = steps_fused(h, p, kAutoTrialSteps);  // an even count
+    if (rc) return rc;
+    CUDA_TRY(cudaEventRecord(ev[1], h->stream));
+    if ((rc = steps_two_pass(h, p, kAutoTrialSteps))) return rc;
+    CUDA_TRY(cudaEventRecord(ev[2], h->stream));
+    CUDA_TRY(cudaEventSynchronize(ev[2]));
+    float t_fused = 0.f, t_two = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&t_fused, ev[0], ev[1]));
+    CUDA_TRY(cudaEventElapsedTime(&t_two, ev[1], ev[2]));
+    h->auto_choice = t_fused < t_two ? FDTD_SCHEDULE_FUSED : FDTD_SCHEDULE_TWO_PASS;
+    // the fused steps came in pairs, so the state is back in the buffer it started in
+    if (h->auto_choice == FDTD_SCHEDULE_TWO_PASS && h->cur == 0) release_fused(h);
+    return FDTD_OK;
+}
+
+}  // namespace
+
+int fdtd_step(fdtd_handle* h, int64_t n) {
+    if (!h) return fail(FDTD_ERR_INVALID, "handle is NULL");
+    if (n < 0) return fail(FDTD_ERR_INVALID, "negative step count");
+    int rc = ensure_prepared(h);
+    if (rc) return rc;
+    StepParams p = make_params(h);
+    if (h->schedule == FDTD_SCHEDULE_AUTO && h->auto_choice == FDTD_SCHEDULE_AUTO && n >= 2 * kAutoTrialSteps &&
+        (long long)h->g.nx * h->g.ny * h->g.nz >= kAutoTrialCells) {
+        if ((rc = auto_trial(h, p))) return rc;
+        n -= 2 * kAutoTrialSteps;
+    }
+    return use_fused(h) ? steps_fused(h, p, n) : steps_two_pass(h, p, n);
+}
+
+int32_t fdtd_active_schedule(const fdtd_handle* h) {
+    if (!h) return -1;
+    if (h->schedule != FDTD_SCHEDULE_AUTO) return h->schedule;
+    return h->auto_choice == FDTD_SCHEDULE_AUTO ? FDTD_SCHEDULE_TWO_PASS : h->auto_choice;
 }
 
 int fdtd_synchronize(fdtd_handle* h) {
@@ -751,6 +833,38 @@ int fdtd_load_state(fdtd_handle* h, const void* buf) {
         for (int q = 0; q < 4; ++q, p += n)
             if (n) CUDA_TRY(cudaMemcpyAsync(arr[q], p, n, cudaMemcpyDeviceToDevice, h->stream));
     }
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return FDTD_OK;
+}
+
+int fdtd_tune_schedule(fdtd_handle* h) {
+    if (!h) return fail(FDTD_ERR_INVALID, "handle is NULL");
+    int rc = ensure_prepared(h);
+    if (rc) return rc;
+    if (h->schedule != FDTD_SCHEDULE_AUTO || h->auto_choice != FDTD_SCHEDULE_AUTO) return FDTD_OK;
+    if ((long long)h->g.nx * h->g.ny * h->g.nz < kAutoTrialCells) {
+        h->auto_choice = FDTD_SCHEDULE_TWO_PASS;
+        return FDTD_OK;
+    }
+    // the trial's steps are undone: state and probe ring saved before, restored after
+    const size_t ring = sizeof(float) * (size_t)h->ring_cap * std::max<size_t>(h->probes.size(), 1);
+    void* saved = nullptr;
+    if (cudaMalloc(&saved, (size_t)fdtd_state_bytes(h) + ring) != cudaSuccess) {
+        cudaGetLastError();
+        return FDTD_OK;  // no room: the first long fdtd_step call runs the trial instead
+    }
+    struct Free {
+        void* p;
+        ~Free() { cudaFree(p); }
+    } guard{saved};
+    char* ring_copy = (char*)saved + fdtd_state_bytes(h);
+    if ((rc = state_copy(h, saved, true))) return rc;
+    CUDA_TRY(cudaMemcpyAsync(ring_copy, h->ring, ring, cudaMemcpyDeviceToDevice, h->stream));
+    const long long step = h->step;
+    if ((rc = auto_trial(h, make_params(h)))) return rc;
+    if ((rc = state_copy(h, saved, false))) return rc;
+    CUDA_TRY(cudaMemcpyAsync(h->ring, ring_copy, ring, cudaMemcpyDeviceToDevice, h->stream));
+    h->step = step;
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     return FDTD_OK;
 }

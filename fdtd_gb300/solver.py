@@ -65,6 +65,8 @@ SIGNATURES = {
     "fdtd_step": (ctypes.c_int, [_vp, _i64]),
     "fdtd_synchronize": (ctypes.c_int, [_vp]),
     "fdtd_current_step": (_i64, [_vp]),
+    "fdtd_active_schedule": (_i32, [_vp]),
+    "fdtd_tune_schedule": (ctypes.c_int, [_vp]),
     "fdtd_read_probes": (ctypes.c_int, [_vp, _i64, _i64, _pf]),
     "fdtd_probe_count": (_i32, [_vp]),
     "fdtd_get_field": (ctypes.c_int, [_vp, _i32, _pf]),
@@ -264,6 +266,15 @@ class Simulation:
     @property
     def current_step(self) -> int:
         return _lib.fdtd_current_step(self._h)
+
+    def tune_schedule(self) -> None:
+        """Under SCHEDULE_AUTO, choose the schedule now by timing both (the handle's state is kept)."""
+        _check(_lib.fdtd_tune_schedule(self._h))
+
+    @property
+    def active_schedule(self) -> int:
+        """The schedule the next step runs (SCHEDULE_TWO_PASS or SCHEDULE_FUSED; AUTO resolved)."""
+        return _lib.fdtd_active_schedule(self._h)
 
     def read_probes(self, first: int = 0, n: Optional[int] = None) -> np.ndarray:
         n = self.current_step - first if n is None else n

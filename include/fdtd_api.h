@@ -36,7 +36,9 @@ enum { FDTD_EX = 0, FDTD_EY = 1, FDTD_EZ = 2, FDTD_HX = 3, FDTD_HY = 4, FDTD_HZ 
 
 /* Update-kernel schedules (fdtd_set_schedule). */
 enum {
-    FDTD_SCHEDULE_AUTO = 0,   /* the fastest schedule measured on GB300: currently two passes */
+    FDTD_SCHEDULE_AUTO = 0,   /* two passes; on grids of >= 48 Mi cells the first fdtd_step call
+                                 of >= 8 steps times 4 steps of each schedule and keeps the faster
+                                 (that call synchronises the handle's stream) */
     FDTD_SCHEDULE_TWO_PASS = 1, /* E pass then H pass per step, in place (the reference's order) */
     FDTD_SCHEDULE_FUSED = 2   /* one z-marching sweep per step over ping-pong field buffers   */
 };
@@ -72,6 +74,12 @@ int fdtd_destroy(fdtd_handle* h);
 /* Run all device work of this handle on a caller stream (a cudaStream_t); NULL = legacy stream. */
 int fdtd_set_stream(fdtd_handle* h, void* cuda_stream);
 int fdtd_set_schedule(fdtd_handle* h, int32_t schedule);
+/* The schedule the next step runs: TWO_PASS or FUSED (AUTO resolved; -1 for a NULL handle). */
+int32_t fdtd_active_schedule(const fdtd_handle* h);
+/* Under AUTO, run the schedule trial now without advancing the handle: fields, CPML memory, probe
+ * ring and step count are restored afterwards. Nothing to do for other schedules or a trial already
+ * taken. Synchronises the handle's stream. */
+int fdtd_tune_schedule(fdtd_handle* h);
 
 /* Material table (at most 256 entries). Replaces the per-brick material scalars that setBrick
  * paints into 12 per-cell arrays (fdtdrav.h:1524-1571). */

@@ -70,3 +70,4 @@ def test_null_handle_errors(lib):
     assert lib.fdtd_step(None, 1) == 1
     assert lib.fdtd_destroy(None) == 0
     assert lib.fdtd_current_step(None) == -1
+    assert lib.fdtd_active_schedule(None) == -1

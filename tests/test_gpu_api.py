@@ -151,3 +151,45 @@ def test_no_source_keeps_initial_state(gpu_lib):
         sim.synchronize()
         f = sim.fields()
     assert np.all(np.abs(f) < np.float32(1e-36))
+
+
+def test_auto_schedule_trial(gpu_lib):
+    """AUTO on a grid above the trial size: the first long fdtd_step call times both schedules on
+    real steps and keeps one; the state equals a two-pass run bit for bit. Below the trial size
+    AUTO runs two-pass and allocates nothing more."""
+    import torch
+    from fdtd_gb300 import solver
+    sc = S.random_boxes(384, 384, 344, 12, seed=9, n_boxes=16, edge=(16, 96), pml=10, n_sources=2, n_probes=4)
+    states, probes = [], []
+    for schedule, tune in ((solver.SCHEDULE_AUTO, False), (solver.SCHEDULE_AUTO, True), (solver.SCHEDULE_TWO_PASS, False)):
+        with solver.Simulation.from_scenario(sc, schedule, probe_capacity=12) as sim:
+            if tune:  # the trial up front, undone: the run then starts from step 0 with the choice made
+                sim.step(3)
+                sim.tune_schedule()
+                assert sim.current_step == 3
+                sim.step(9)
+            else:
+                sim.step(12)
+            sim.synchronize()
+            assert sim.current_step == 12
+            if schedule == solver.SCHEDULE_AUTO:
+                assert sim.active_schedule in (solver.SCHEDULE_TWO_PASS, solver.SCHEDULE_FUSED)
+            buf = torch.empty(sim.state_bytes(), dtype=torch.uint8, device="cuda")
+            torch.cuda.synchronize()
+            sim.save_state(buf.data_ptr())
+            torch.cuda.synchronize()
+            states.append(buf)
+            probes.append(sim.read_probes(0, 12))
+    for q in (0, 1):
+        assert torch.equal(states[q], states[2])
+        assert bitwise_equal(probes[q], probes[2])
+    small_sc = small()
+    with solver.Simulation.from_scenario(small_sc, probe_capacity=40) as a, \
+            solver.Simulation.from_scenario(small_sc, solver.SCHEDULE_TWO_PASS, probe_capacity=40) as b:
+        a.step(40)
+        b.step(40)
+        a.synchronize()
+        b.synchronize()
+        assert a.active_schedule == solver.SCHEDULE_TWO_PASS
+        assert a.device_bytes() == b.device_bytes()
+        assert bitwise_equal(a.fields(), b.fields())
