@@ -218,8 +218,9 @@ TWO_PASS_DRAM_BYTES_PER_CELL = 78.15
 
 
 # DRAM bytes per cell update of one fused step (k_shell_e + k_sweep_interior + k_shell_h), from an
-# ncu capture of the 256^3 random-box case; None until captured.
-FUSED_DRAM_BYTES_PER_CELL = None
+# ncu capture of the 256^3 random-box case (profiles/yee_step_fused_boxes256_dram.md): 72.77 B,
+# scaled by cells like the two-pass figure (an upper bound: the shell share is smaller at 512^3).
+FUSED_DRAM_BYTES_PER_CELL = 72.77
 
 
 def measured_traffic(schedule, cells):
