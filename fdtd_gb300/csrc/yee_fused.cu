@@ -455,12 +455,20 @@ void plan_fused(const DeviceGrid& g, int kc, const int* design_box, std::vector<
     auto chunks = [&](std::vector<int4>& out, int x0, int y0, int a, int b) {  // interior planes [a, b)
         for (int k = a; k < b; k += kc) out.push_back(make_int4(x0, y0, k, k + kc < b ? k + kc : b));
     };
-    // shell items: the 32 x 8 halves of a tile, one plane each, one node per thread (halves with no
-    // node inside the grid are left out)
+    // shell items, one plane and one node per thread each: the 32 x 8 halves of a tile (halves with
+    // no node inside the grid are left out), or one 16 x 16 block (w = 1) where at most 16 columns
+    // of the tile lie in the grid (the tile columns at the x edges), so that no warp is half empty
     auto shell = [&](int x0, int y0, int a, int b) {
-        for (int k = a; k < b; ++k)
+        const int c0 = x0 > 0 ? x0 : 0, c1 = x0 + TX < g.nx ? x0 + TX : g.nx;
+        static_assert(TY == 16, "a 16 x 16 shell block spans one tile height");
+        for (int k = a; k < b; ++k) {
+            if (c1 - c0 <= 16) {
+                general_items.push_back(make_int4(c0, y0, k, 1));
+                continue;
+            }
             for (int h = 0; h < TY; h += kShellRows)
                 if (y0 + h + kShellRows > 0 && y0 + h < g.ny) general_items.push_back(make_int4(x0, y0 + h, k, 0));
+        }
     };
     for (int y0 = oy; y0 < g.ny; y0 += TY)
         for (int x0 = ox; x0 < g.nx; x0 += TX) {

@@ -34,16 +34,17 @@ __global__ void __launch_bounds__(256, FDTD_TWO_PASS_MIN_BLOCKS) k_update_h(cons
     h_node_global<false, Idx>(p, f, f, f, ps, ps, i, j, blockIdx.z, m);
 }
 
-// Shell passes of the fused schedule: the nodes of the shell items (int4 {x0, y0, k, -}, a 32 x 8
-// block of plane k; x0, y0 may be negative) read buffer A (`fi`, `pin`) and write buffer B (`fo`,
-// `pout`), one node per thread as in the two-pass kernels. The E pass runs before the interior
+// Shell passes of the fused schedule: the nodes of the shell items (int4 {x0, y0, k, w}: a 32 x 8
+// block of plane k for w = 0, a 16 x 16 block for w = 1; x0, y0 may be negative) read buffer A
+// (`fi`, `pin`) and write buffer B (`fo`, `pout`), one node per thread as in the two-pass kernels. The E pass runs before the interior
 // sweep, the H pass after it, since H reads new E at interior nodes next to the shell.
 template <typename Idx>
 __global__ void __launch_bounds__(256, FDTD_SHELL_MIN_BLOCKS) k_shell_e(const __grid_constant__ StepParams p, FieldPtrs fi, FieldPtrs fo,
                                                  const __grid_constant__ PsiSet pin, const __grid_constant__ PsiSet pout,
                                                  const int4* __restrict__ items, long long m) {
     const int4 it = items[blockIdx.x];
-    const int i = it.x + (int)threadIdx.x, j = it.y + (int)threadIdx.y;
+    const int t = (int)(threadIdx.y * 32 + threadIdx.x);
+    const int i = it.x + (it.w ? (t & 15) : (int)threadIdx.x), j = it.y + (it.w ? (t >> 4) : (int)threadIdx.y);
     if (i < 0 || i >= p.g.nx || j < 0 || j >= p.g.ny) return;
     e_node_global<false, false, false, Idx>(p, fi, fo, pin, pout, i, j, it.z, m);
 }
@@ -53,7 +54,8 @@ __global__ void __launch_bounds__(256, FDTD_SHELL_MIN_BLOCKS) k_shell_h(const __
                                                  const __grid_constant__ PsiSet pin, const __grid_constant__ PsiSet pout,
                                                  const int4* __restrict__ items, long long m) {
     const int4 it = items[blockIdx.x];
-    const int i = it.x + (int)threadIdx.x, j = it.y + (int)threadIdx.y;
+    const int t = (int)(threadIdx.y * 32 + threadIdx.x);
+    const int i = it.x + (it.w ? (t & 15) : (int)threadIdx.x), j = it.y + (it.w ? (t >> 4) : (int)threadIdx.y);
     if (i < 0 || i >= p.g.nx || j < 0 || j >= p.g.ny) return;
     h_node_global<false, Idx>(p, fi, fo, fo, pin, pout, i, j, it.z, m);
 }
