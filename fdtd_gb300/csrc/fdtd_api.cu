@@ -623,11 +623,11 @@ int steps_two_pass(fdtd_handle* h, const StepParams& p, int64_t n) {
 // The AUTO trial: on grids of at least kAutoTrialCells cells, the first fdtd_step call of at least
 // 2 * kAutoTrialSteps steps times kAutoTrialSteps fused steps and then as many two-pass steps (real
 // steps: both schedules give the same bits) and keeps the faster schedule for the handle. Which one
-// wins depends on the grid: on GB300 the fused sweep is faster on 384^3 to 512^3 random-box grids,
-// two-pass on smaller ones and on the 1024 x 1024 x 896 one. Smaller grids take two-pass without a
-// trial. The fused buffers are freed when two-pass wins or cannot be allocated.
+// wins depends on the grid: on GB300 random-box cubes with 10-cell CPML, two-pass below about
+// 224^3 and fused above. Smaller grids take two-pass without a trial. The fused buffers are freed
+// when two-pass wins or cannot be allocated.
 constexpr int64_t kAutoTrialSteps = 4;
-constexpr long long kAutoTrialCells = 48LL << 20;
+constexpr long long kAutoTrialCells = 8LL << 20;
 
 int auto_trial(fdtd_handle* h, const StepParams& p) {
     if (ensure_fused(h) != FDTD_OK) {  // no room for the second buffers

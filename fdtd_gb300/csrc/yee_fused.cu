@@ -20,6 +20,8 @@
 // drains its own copies (again bounded) and exits.
 #include <cuda.h>
 
+#include <algorithm>
+
 #include "yee_common.cuh"
 #include "yee_kernels.h"
 
@@ -487,6 +489,12 @@ void plan_fused(const DeviceGrid& g, int kc, const int* design_box, std::vector<
                 shell(x0, y0, 0, g.nz);
             }
         }
+    // plane-major order: CTAs run in item order, so the CTAs in flight then work on neighbouring
+    // planes of many tiles instead of many planes of a few tiles, which keeps the pages they touch
+    // few on large grids
+    auto by_plane = [](const int4& a, const int4& b) { return a.z < b.z; };
+    std::stable_sort(interior_items.begin(), interior_items.end(), by_plane);
+    std::stable_sort(general_items.begin(), general_items.end(), by_plane);
 }
 
 }  // namespace fdtd

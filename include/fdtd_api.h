@@ -36,7 +36,7 @@ enum { FDTD_EX = 0, FDTD_EY = 1, FDTD_EZ = 2, FDTD_HX = 3, FDTD_HY = 4, FDTD_HZ 
 
 /* Update-kernel schedules (fdtd_set_schedule). */
 enum {
-    FDTD_SCHEDULE_AUTO = 0,   /* two passes; on grids of >= 48 Mi cells the first fdtd_step call
+    FDTD_SCHEDULE_AUTO = 0,   /* two passes; on grids of >= 8 Mi cells the first fdtd_step call
                                  of >= 8 steps times 4 steps of each schedule and keeps the faster
                                  (that call synchronises the handle's stream) */
     FDTD_SCHEDULE_TWO_PASS = 1, /* E pass then H pass per step, in place (the reference's order) */

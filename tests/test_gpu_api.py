@@ -159,7 +159,7 @@ def test_auto_schedule_trial(gpu_lib):
     AUTO runs two-pass and allocates nothing more."""
     import torch
     from fdtd_gb300 import solver
-    sc = S.random_boxes(384, 384, 344, 12, seed=9, n_boxes=16, edge=(16, 96), pml=10, n_sources=2, n_probes=4)
+    sc = S.random_boxes(224, 224, 176, 12, seed=9, n_boxes=16, edge=(8, 64), pml=10, n_sources=2, n_probes=4)
     states, probes = [], []
     for schedule, tune in ((solver.SCHEDULE_AUTO, False), (solver.SCHEDULE_AUTO, True), (solver.SCHEDULE_TWO_PASS, False)):
         with solver.Simulation.from_scenario(sc, schedule, probe_capacity=12) as sim:
