@@ -371,10 +371,16 @@ int fused_tile_y() { return TY; }
 
 // Planes per interior item: whole columns unless that leaves too few CTAs to fill the GPU, and at
 // most kMaxItemPlanes - 2 (the item also streams the plane below and recomputes the one above).
+// Interior items to aim for: at least this many (chunks halved until reached). 8192 measured best
+// at 512^3 and 1024 x 1024 x 896 against 2048, 4096 and 16384 (shorter chunks keep the CTAs in
+// flight on fewer planes; each chunk re-reads two planes).
+#ifndef FDTD_FUSED_MIN_ITEMS
+#define FDTD_FUSED_MIN_ITEMS 8192
+#endif
 int fused_chunk(const DeviceGrid& g) {
     const long long tiles = (long long)((g.nx + TX - 1) / TX) * ((g.ny + TY - 1) / TY);
     int kc = g.nz;
-    while (kc > 16 && tiles * ((g.nz + kc - 1) / kc) < 4096) kc = (kc + 1) / 2;
+    while (kc > 16 && tiles * ((g.nz + kc - 1) / kc) < FDTD_FUSED_MIN_ITEMS) kc = (kc + 1) / 2;
     return kc < kMaxItemPlanes - 2 ? kc : kMaxItemPlanes - 2;
 }
 
