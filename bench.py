@@ -217,15 +217,18 @@ def cpu_baseline(sc_full, seconds_budget=20.0):
 TWO_PASS_DRAM_BYTES_PER_CELL = 78.15
 
 
-# DRAM bytes per cell update of one fused step (k_shell_e + k_sweep_interior + k_shell_h), from an
-# ncu capture of the 256^3 random-box case (profiles/yee_step_fused_boxes256_dram.md): 72.77 B,
-# scaled by cells like the two-pass figure (an upper bound: the shell share is smaller at 512^3).
-FUSED_DRAM_BYTES_PER_CELL = 72.77
+# DRAM bytes per cell update of one fused step (k_shell_e + k_sweep_interior + k_shell_h): 62.57 B
+# from an ncu capture of the 512^3 bench workload itself (profiles/yee_step_boxes512_launch_list.md),
+# 72.77 B at 256^3 (profiles/yee_step_fused_boxes256_dram.md), where the shell share is larger.
+FUSED_DRAM_BYTES_PER_CELL = {"512": 62.57, "256": 72.77}
 
 
-def measured_traffic(schedule, cells):
-    per_cell = FUSED_DRAM_BYTES_PER_CELL if schedule == 2 else TWO_PASS_DRAM_BYTES_PER_CELL
-    return None if per_cell is None else round(per_cell * cells)
+def measured_traffic(schedule, cells, config):
+    if schedule == 2:
+        per_cell = FUSED_DRAM_BYTES_PER_CELL.get(config, FUSED_DRAM_BYTES_PER_CELL["512"])
+    else:
+        per_cell = TWO_PASS_DRAM_BYTES_PER_CELL
+    return round(per_cell * cells)
 
 
 def bench_ours(args, rank, world):
@@ -282,7 +285,7 @@ def bench_ours(args, rank, world):
                                    " (two-pass)" if args.schedule == 0 else ""),
                       "l2": "inputs larger than L2 (fields 24 B/cell x 134M cells)", "parallelism": f"replicas{world}"},
            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                        "frac": round(achieved / peak, 4), "traffic": measured_traffic(active, N),
+                        "frac": round(achieved / peak, 4), "traffic": measured_traffic(active, N, args.config),
                         "bytes_per_cell_update": round(B, 3), "peak_source": peak_kind,
                         "kernel": "one full time step (all update launches of the step)"},
            "gpu_launches": launches_per_step * args.steps, "clocks": clk}
