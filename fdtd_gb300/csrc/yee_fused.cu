@@ -31,7 +31,6 @@ namespace {
 
 constexpr int TX = 32, TY = 16;             // tile of nodes owned by a CTA (and shell item size)
 constexpr int NTH = 256;                    // threads per CTA
-constexpr int ROWS = TX * TY / NTH;         // nodes per thread per plane (rows ty, ty + 8)
 constexpr int RSTEP = NTH / TX;             // row distance between a thread's nodes
 #ifndef FDTD_FUSED_NSTAGE
 #define FDTD_FUSED_NSTAGE 3
@@ -46,7 +45,9 @@ constexpr int NSTAGE = FDTD_FUSED_NSTAGE;   // planes resident in the ring
 constexpr int AHEAD = FDTD_FUSED_AHEAD;     // planes loaded ahead of the one computed (<= NSTAGE - 2)
 constexpr int HW = TX + 8, HH = TY + 2;     // H tile: x in [x0-4, x0+TX+4), y in [y0-1, y0+TY+1)
 constexpr int EW = TX + 4, EH = TY + 1;     // old-E tile: x in [x0, x0+TX+4), y in [y0, y0+TY+1)
-constexpr int MW = TX + 32, MH = TY + 2;    // row tile: x in [x0-16, x0+TX+16), y in [y0-1, ...)
+// row tile: x in [xr, xr+MW) with xr = x0 rounded down to a multiple of 8 (the tile's own columns
+// start at offset x0 - xr, 0 for the planner's origins), y in [y0-1, y0+TY+1)
+constexpr int MW = TX + 8, MH = TY + 2;
 constexpr int NW = TX + 1, NH = TY + 1;     // new-E plane: x in [x0, x0+TX], y in [y0, y0+TY]
 
 constexpr int round128(int b) { return (b + 127) / 128 * 128; }
@@ -63,8 +64,11 @@ constexpr int SMEM_INTERIOR = NSTAGE * STAGE_BYTES + ENEW_BYTES + NSTAGE * 8 + k
 static_assert(NSTAGE >= AHEAD + 2, "the ring recycles the stage of plane k - 2 at plane k");
 static_assert(NHALO <= 64, "halo nodes live on the first two warps");
 
-constexpr int kShellRows = 8;  // rows of a shell item (the shell kernels' block is 32 x 8)
-static_assert(TY % kShellRows == 0, "shell items split a tile into whole halves");
+// Shell item block shapes of 256 nodes (the shell kernels' block is 256 threads): widths. Shapes
+// narrower than 16 serve only rectangles narrower than 16 (the boundary planes of grids without
+// CPML), since their warps load short row pieces.
+constexpr int kShapes = 9;
+constexpr int kShapeW[kShapes] = {32, 16, 64, 128, 256, 8, 4, 2, 1};
 
 constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
 
@@ -252,11 +256,12 @@ k_sweep_interior(const __grid_constant__ FusedMaps maps, const __grid_constant__
     const long long row = m % p.ring_cap;
     // own nodes (tx, ty + r * RSTEP); ring / new-E offsets of row r are these plus r * RSTEP rows
     const int i = x0 + tx, j = y0 + ty;
-    const int hi = (ty + 1) * HW + tx + 4, ei = ty * EW + tx, mi = (ty + 1) * MW + tx + 16, ni = ty * NW + tx;
+    const int xoff = x0 & 7;  // column of x0 in the row tile
+    const int hi = (ty + 1) * HW + tx + 4, ei = ty * EW + tx, mi = (ty + 1) * MW + tx + xoff, ni = ty * NW + tx;
     // halo node of the first NHALO threads: row y0 + TY (warp 0), column x0 + TX (warp 1)
     const bool halo = tid < NHALO;
     const int hpx = tid < TX ? tid : TX, hpy = tid < TX ? TY : tid - TX;
-    const int hhi = (hpy + 1) * HW + hpx + 4, hei = hpy * EW + hpx, hmi = (hpy + 1) * MW + hpx + 16, hni = hpy * NW + hpx;
+    const int hhi = (hpy + 1) * HW + hpx + 4, hei = hpy * EW + hpx, hmi = (hpy + 1) * MW + hpx + xoff, hni = hpy * NW + hpx;
     const long long n_own = (long long)j * g.pitch + i;
     const long long n_row = (long long)RSTEP * g.pitch;
 
@@ -274,7 +279,7 @@ k_sweep_interior(const __grid_constant__ FusedMaps maps, const __grid_constant__
         mbar_expect_tx(&bars[s], TX_BYTES);
         for (int c = 0; c < 3; ++c) tma_load_3d(st + c * H_BYTES, &maps.h[c], &bars[s], x0 - 4, y0 - 1, k);
         for (int c = 0; c < 3; ++c) tma_load_3d(st + 3 * H_BYTES + c * E_BYTES, &maps.e[c], &bars[s], x0, y0, k);
-        tma_load_3d(st + 3 * H_BYTES + 3 * E_BYTES, &maps.rec, &bars[s], x0 - 16, y0 - 1, k);
+        tma_load_3d(st + 3 * H_BYTES + 3 * E_BYTES, &maps.rec, &bars[s], x0 - xoff, y0 - 1, k);
     };
     if (tid == 0)
         for (int q = 0; q < AHEAD && kfirst + q <= klast; ++q) issue(kfirst + q, q);
@@ -428,73 +433,88 @@ int encode_fused_maps(FusedMaps* out, const DeviceGrid& g, float* const h[3], fl
     return 0;
 }
 
-// Split the grid into items: tiles whose E positions (x0..x0+TX, y0..y0+TY) lie in the x / y
-// interior get their interior planes as interior items (chunks of at most kc planes); everything
-// else (boundary / CPML tiles, and the z-boundary and z-CPML planes of interior tiles) becomes
-// shell items of one plane and half a tile. The E positions of plane k1 of an item are recomputed, so a chunk must also keep
-// its top plane in the interior range to stay interior. The tile grid starts at (ox, oy) <= 0,
-// chosen to put as many nodes as possible in interior tiles; ox is a multiple of 8 so that every
-// TMA box starts on a 16-byte boundary (H box at x0 - 4, four bytes per node; row box at x0 - 16,
-// two bytes per node).
+// Split the grid into items. Interior tiles (32 x 16 columns whose E positions x0..x0+TX,
+// y0..y0+TY all lie in the x / y interior) get their interior planes as interior items (chunks of
+// at most kc planes; the E positions of an item's top plane are recomputed, so a chunk keeps its
+// top plane in the interior range). Tiles start at the first interior node (x0 rounded up to a
+// multiple of 8: every TMA box then starts on a 16-byte boundary and every warp's row of stores on
+// a 32-byte sector; origins off the sector grid left sectors half written by two CTAs, which
+// measured up to 30 % slower) and step by the tile size; one
+// more tile per axis ends on the last interior node, overlapping its neighbour (both write the same
+// values there). With a design region, tiles that reach its edge box stay out of the sweep and
+// no overlapping tiles are added. Everything else is the shell: per plane a few rectangles (whole
+// planes outside the interior z range; bands around the swept rectangle and the left-out tiles
+// inside it), cut into shell items of 256 nodes in the block shape that wastes the fewest threads.
 void plan_fused(const DeviceGrid& g, int kc, const int* design_box, std::vector<int4>& interior_items,
                 std::vector<int4>& general_items) {
     interior_items.clear();
     general_items.clear();
-    auto inside = [](int q, int n, int pn, int pp) {
-        const int lo = pn > 1 ? pn : 1, hi = (n - 1 - pp < n - 2) ? n - 1 - pp : n - 2;
-        return q >= lo && q <= hi;
-    };
-    auto interior_tiles = [&](int start, int step, int n, int pn, int pp) {
-        int c = 0;
-        for (int q = start; q < n; q += step) c += inside(q, n, pn, pp) && inside(q + step, n, pn, pp);
-        return c;
-    };
-    int ox = 0, oy = 0, best_x = -1, best_y = -1;
-    for (int o = 0; o > -TX; o -= 8) {
-        const int c = interior_tiles(o, TX, g.nx, g.pxn, g.pxp);
-        if (c > best_x) { best_x = c; ox = o; }
-    }
-    for (int o = 0; o > -TY; --o) {
-        const int c = interior_tiles(o, TY, g.ny, g.pyn, g.pyp);
-        if (c > best_y) { best_y = c; oy = o; }
-    }
+    const int xlo = g.pxn > 1 ? g.pxn : 1, xhi = (g.nx - 1 - g.pxp < g.nx - 2) ? g.nx - 1 - g.pxp : g.nx - 2;
+    const int ylo = g.pyn > 1 ? g.pyn : 1, yhi = (g.ny - 1 - g.pyp < g.ny - 2) ? g.ny - 1 - g.pyp : g.ny - 2;
     const int zlo = g.pzn > 1 ? g.pzn : 1;
     const int zhi = (g.nz - 1 - g.pzp < g.nz - 2) ? g.nz - 1 - g.pzp : g.nz - 2;  // last interior plane
-    auto chunks = [&](std::vector<int4>& out, int x0, int y0, int a, int b) {  // interior planes [a, b)
-        for (int k = a; k < b; k += kc) out.push_back(make_int4(x0, y0, k, k + kc < b ? k + kc : b));
+    // tile starts along an axis: from lo (rounded up to `align`) while the tile's far E positions
+    // (start + size) stay <= hi, plus one overlapping tile ending on hi
+    auto starts = [&](int lo, int hi, int size, int align, bool overlap) {
+        std::vector<int> v;
+        const int a0 = (lo + align - 1) / align * align;
+        for (int q = a0; q + size <= hi; q += size) v.push_back(q);
+        if (overlap && !v.empty() && v.back() + size < hi) {
+            const int last = (hi - size) / align * align;
+            if (last > v.back()) v.push_back(last);
+        }
+        return v;
     };
-    // shell items, one plane and one node per thread each: the 32 x 8 halves of a tile (halves with
-    // no node inside the grid are left out), or one 16 x 16 block (w = 1) where at most 16 columns
-    // of the tile lie in the grid (the tile columns at the x edges), so that no warp is half empty
-    auto shell = [&](int x0, int y0, int a, int b) {
-        const int c0 = x0 > 0 ? x0 : 0, c1 = x0 + TX < g.nx ? x0 + TX : g.nx;
-        static_assert(TY == 16, "a 16 x 16 shell block spans one tile height");
-        for (int k = a; k < b; ++k) {
-            if (c1 - c0 <= 16) {
-                general_items.push_back(make_int4(c0, y0, k, 1));
+    const bool overlap = design_box == nullptr;
+    std::vector<int> xs, ys;
+    if (zhi > zlo) {
+        xs = starts(xlo, xhi, TX, 8, overlap);
+        ys = starts(ylo, yhi, TY, 1, overlap);
+    }
+    // shell items of one rectangle [x0, x0+w) x [y0, y0+h) of plane k: block shapes of 256 nodes
+    // (shape s: width kShapeW[s]), the one with the fewest items; {x0, y0, k, s | cols << 4 | rows << 13}
+    auto rect = [&](int x0, int y0, int w, int h, int k) {
+        if (w <= 0 || h <= 0) return;
+        int best = 0, narrowest = 1;
+        while (narrowest < w && narrowest < 16) narrowest *= 2;
+        long long best_n = -1;
+        for (int sh = 0; sh < kShapes; ++sh) {
+            const int bw = kShapeW[sh], bh = 256 / bw;
+            if (bw < narrowest) continue;
+            const long long n = (long long)((w + bw - 1) / bw) * ((h + bh - 1) / bh);
+            if (best_n < 0 || n < best_n) { best_n = n; best = sh; }
+        }
+        const int bw = kShapeW[best], bh = 256 / bw;
+        for (int y = 0; y < h; y += bh)
+            for (int x = 0; x < w; x += bw) {
+                const int cw = w - x < bw ? w - x : bw, ch = h - y < bh ? h - y : bh;
+                general_items.push_back(make_int4(x0 + x, y0 + y, k, best | cw << 4 | ch << 13));
+            }
+    };
+    std::vector<int4> left_out;  // tiles inside the swept rectangle that reach the design edge box
+    for (int y0 : ys)
+        for (int x0 : xs) {
+            if (design_box && x0 <= design_box[3] && design_box[0] <= x0 + TX && y0 <= design_box[4] &&
+                design_box[1] <= y0 + TY) {
+                left_out.push_back(make_int4(x0, y0, 0, 0));
                 continue;
             }
-            for (int h = 0; h < TY; h += kShellRows)
-                if (y0 + h + kShellRows > 0 && y0 + h < g.ny) general_items.push_back(make_int4(x0, y0 + h, k, 0));
+            for (int k = zlo; k < zhi; k += kc) interior_items.push_back(make_int4(x0, y0, k, k + kc < zhi ? k + kc : zhi));
         }
-    };
-    for (int y0 = oy; y0 < g.ny; y0 += TY)
-        for (int x0 = ox; x0 < g.nx; x0 += TX) {
-            bool tile_int = inside(x0, g.nx, g.pxn, g.pxp) && inside(x0 + TX, g.nx, g.pxn, g.pxp) &&
-                            inside(y0, g.ny, g.pyn, g.pyp) && inside(y0 + TY, g.ny, g.pyn, g.pyp);
-            // the design region's edge box [d0, d3] x [d1, d4] (all planes) stays with the shell
-            if (design_box && x0 <= design_box[3] && design_box[0] <= x0 + TX && y0 <= design_box[4] &&
-                design_box[1] <= y0 + TY)
-                tile_int = false;
-            // interior items cover planes [zlo, zhi) so that the recomputed top plane <= zhi
-            if (tile_int && zhi > zlo) {
-                shell(x0, y0, 0, zlo);
-                chunks(interior_items, x0, y0, zlo, zhi);
-                shell(x0, y0, zhi, g.nz);
-            } else {
-                shell(x0, y0, 0, g.nz);
-            }
+    const bool swept = !xs.empty() && !ys.empty();
+    const int X0 = swept ? xs.front() : 0, X1 = swept ? xs.back() + TX : 0;
+    const int Y0 = swept ? ys.front() : 0, Y1 = swept ? ys.back() + TY : 0;
+    for (int k = 0; k < g.nz; ++k) {
+        if (!swept || k < zlo || k >= zhi) {
+            rect(0, 0, g.nx, g.ny, k);
+            continue;
         }
+        rect(0, 0, g.nx, Y0, k);
+        rect(0, Y1, g.nx, g.ny - Y1, k);
+        rect(0, Y0, X0, Y1 - Y0, k);
+        rect(X1, Y0, g.nx - X1, Y1 - Y0, k);
+        for (const int4& t : left_out) rect(t.x, t.y, TX, TY, k);
+    }
     // plane-major order: CTAs run in item order, so the CTAs in flight then work on neighbouring
     // planes of many tiles instead of many planes of a few tiles, which keeps the pages they touch
     // few on large grids

@@ -50,8 +50,9 @@ struct FusedMaps {
     CUtensorMap rec;  // coefficient rows (StepParams::rec)
 };
 // Work items of one step (device arrays of int4): interior items {x0, y0, k0, k1} for the sweep
-// (a 32 x 16 column over planes [k0, k1)), general items {x0, y0, k, w} for the shell passes
-// (32 x 8 nodes of plane k for w = 0, 16 x 16 for w = 1) (plan_fused).
+// (a 32 x 16 column over planes [k0, k1)), general items {x0, y0, k, code} for the shell passes
+// (a block of up to 256 nodes of plane k: shape code & 15, columns (code >> 4) & 511, rows
+// (code >> 13) & 511) (plan_fused).
 struct FusedWork {
     const int4* interior;
     int n_interior;

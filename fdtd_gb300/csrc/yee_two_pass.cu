@@ -34,30 +34,38 @@ __global__ void __launch_bounds__(256, FDTD_TWO_PASS_MIN_BLOCKS) k_update_h(cons
     h_node_global<false, Idx>(p, f, f, f, ps, ps, i, j, blockIdx.z, m);
 }
 
-// Shell passes of the fused schedule: the nodes of the shell items (int4 {x0, y0, k, w}: a 32 x 8
-// block of plane k for w = 0, a 16 x 16 block for w = 1; x0, y0 may be negative) read buffer A
-// (`fi`, `pin`) and write buffer B (`fo`, `pout`), one node per thread as in the two-pass kernels. The E pass runs before the interior
-// sweep, the H pass after it, since H reads new E at interior nodes next to the shell.
+// Shell passes of the fused schedule: the nodes of the shell items (int4 {x0, y0, k, code}: a
+// block of plane k of shape s = code & 15 (widths 32, 16, 64, 128, 256, 8, 4, 2, 1; 256 nodes) of
+// which the first (code >> 4) & 511 columns and (code >> 13) & 511 rows are the item's) read buffer A (`fi`,
+// `pin`) and write buffer B (`fo`, `pout`), one node per thread as in the two-pass kernels. The E
+// pass runs before the interior sweep, the H pass after it, since H reads new E at interior nodes
+// next to the shell.
+__device__ __forceinline__ bool shell_node(const int4& it, const DeviceGrid& g, int& i, int& j) {
+    const int s = it.w & 15;
+    const int lw = s == 0 ? 5 : s == 1 ? 4 : s <= 4 ? s + 4 : 8 - s;  // log2 of the block width
+    const int t = (int)(threadIdx.y * 32 + threadIdx.x);
+    const int tx = t & ((1 << lw) - 1), ty = t >> lw;
+    i = it.x + tx;
+    j = it.y + ty;
+    return tx < ((it.w >> 4) & 511) && ty < ((it.w >> 13) & 511) && i < g.nx && j < g.ny;
+}
+
 template <typename Idx>
 __global__ void __launch_bounds__(256, FDTD_SHELL_MIN_BLOCKS) k_shell_e(const __grid_constant__ StepParams p, FieldPtrs fi, FieldPtrs fo,
                                                  const __grid_constant__ PsiSet pin, const __grid_constant__ PsiSet pout,
                                                  const int4* __restrict__ items, long long m) {
-    const int4 it = items[blockIdx.x];
-    const int t = (int)(threadIdx.y * 32 + threadIdx.x);
-    const int i = it.x + (it.w ? (t & 15) : (int)threadIdx.x), j = it.y + (it.w ? (t >> 4) : (int)threadIdx.y);
-    if (i < 0 || i >= p.g.nx || j < 0 || j >= p.g.ny) return;
-    e_node_global<false, false, false, Idx>(p, fi, fo, pin, pout, i, j, it.z, m);
+    int i, j;
+    if (!shell_node(items[blockIdx.x], p.g, i, j)) return;
+    e_node_global<false, false, false, Idx>(p, fi, fo, pin, pout, i, j, items[blockIdx.x].z, m);
 }
 
 template <typename Idx>
 __global__ void __launch_bounds__(256, FDTD_SHELL_MIN_BLOCKS) k_shell_h(const __grid_constant__ StepParams p, FieldPtrs fi, FieldPtrs fo,
                                                  const __grid_constant__ PsiSet pin, const __grid_constant__ PsiSet pout,
                                                  const int4* __restrict__ items, long long m) {
-    const int4 it = items[blockIdx.x];
-    const int t = (int)(threadIdx.y * 32 + threadIdx.x);
-    const int i = it.x + (it.w ? (t & 15) : (int)threadIdx.x), j = it.y + (it.w ? (t >> 4) : (int)threadIdx.y);
-    if (i < 0 || i >= p.g.nx || j < 0 || j >= p.g.ny) return;
-    h_node_global<false, Idx>(p, fi, fo, fo, pin, pout, i, j, it.z, m);
+    int i, j;
+    if (!shell_node(items[blockIdx.x], p.g, i, j)) return;
+    h_node_global<false, Idx>(p, fi, fo, fo, pin, pout, i, j, items[blockIdx.x].z, m);
 }
 
 cudaError_t launch_shell(bool e_pass, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
