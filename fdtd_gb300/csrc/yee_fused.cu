@@ -67,6 +67,13 @@ static_assert(NHALO <= 64, "halo nodes live on the first two warps");
 // Shell item block shapes of 256 nodes (the shell kernels' block is 256 threads): widths. Shapes
 // narrower than 16 serve only rectangles narrower than 16 (the boundary planes of grids without
 // CPML), since their warps load short row pieces.
+#ifndef FDTD_SHELL_PLANES
+#define FDTD_SHELL_PLANES 4
+#endif
+// planes per shell item (at most 16): 4 measured 5 % faster than 1 and level with 8 on the
+// 512^3 bench workload (fewer, longer CTAs)
+constexpr int kShellPlanes = FDTD_SHELL_PLANES;
+static_assert(kShellPlanes >= 1 && kShellPlanes <= 16, "the plane count takes 4 bits of an item");
 constexpr int kShapes = 9;
 constexpr int kShapeW[kShapes] = {32, 16, 64, 128, 256, 8, 4, 2, 1};
 
@@ -471,9 +478,10 @@ void plan_fused(const DeviceGrid& g, int kc, const int* design_box, std::vector<
         xs = starts(xlo, xhi, TX, 8, overlap);
         ys = starts(ylo, yhi, TY, 1, overlap);
     }
-    // shell items of one rectangle [x0, x0+w) x [y0, y0+h) of plane k: block shapes of 256 nodes
-    // (shape s: width kShapeW[s]), the one with the fewest items; {x0, y0, k, s | cols << 4 | rows << 13}
-    auto rect = [&](int x0, int y0, int w, int h, int k) {
+    // shell items of one rectangle [x0, x0+w) x [y0, y0+h) of planes k .. k+nk-1: block shapes of
+    // 256 nodes (shape s: width kShapeW[s]), the one with the fewest items;
+    // {x0, y0, k, s | cols << 4 | rows << 13 | (nk - 1) << 22}
+    auto rect = [&](int x0, int y0, int w, int h, int k, int nk) {
         if (w <= 0 || h <= 0) return;
         int best = 0, narrowest = 1;
         while (narrowest < w && narrowest < 16) narrowest *= 2;
@@ -488,7 +496,7 @@ void plan_fused(const DeviceGrid& g, int kc, const int* design_box, std::vector<
         for (int y = 0; y < h; y += bh)
             for (int x = 0; x < w; x += bw) {
                 const int cw = w - x < bw ? w - x : bw, ch = h - y < bh ? h - y : bh;
-                general_items.push_back(make_int4(x0 + x, y0 + y, k, best | cw << 4 | ch << 13));
+                general_items.push_back(make_int4(x0 + x, y0 + y, k, best | cw << 4 | ch << 13 | (nk - 1) << 22));
             }
     };
     std::vector<int4> left_out;  // tiles inside the swept rectangle that reach the design edge box
@@ -504,16 +512,21 @@ void plan_fused(const DeviceGrid& g, int kc, const int* design_box, std::vector<
     const bool swept = !xs.empty() && !ys.empty();
     const int X0 = swept ? xs.front() : 0, X1 = swept ? xs.back() + TX : 0;
     const int Y0 = swept ? ys.front() : 0, Y1 = swept ? ys.back() + TY : 0;
-    for (int k = 0; k < g.nz; ++k) {
-        if (!swept || k < zlo || k >= zhi) {
-            rect(0, 0, g.nx, g.ny, k);
-            continue;
+    // runs of up to kShellPlanes planes with the same rectangles share items
+    for (int k = 0; k < g.nz;) {
+        const bool full = !swept || k < zlo || k >= zhi;
+        const int end = full ? (swept && k < zlo ? zlo : g.nz) : zhi;
+        const int nk = end - k < kShellPlanes ? end - k : kShellPlanes;
+        if (full) {
+            rect(0, 0, g.nx, g.ny, k, nk);
+        } else {
+            rect(0, 0, g.nx, Y0, k, nk);
+            rect(0, Y1, g.nx, g.ny - Y1, k, nk);
+            rect(0, Y0, X0, Y1 - Y0, k, nk);
+            rect(X1, Y0, g.nx - X1, Y1 - Y0, k, nk);
+            for (const int4& t : left_out) rect(t.x, t.y, TX, TY, k, nk);
         }
-        rect(0, 0, g.nx, Y0, k);
-        rect(0, Y1, g.nx, g.ny - Y1, k);
-        rect(0, Y0, X0, Y1 - Y0, k);
-        rect(X1, Y0, g.nx - X1, Y1 - Y0, k);
-        for (const int4& t : left_out) rect(t.x, t.y, TX, TY, k);
+        k += nk;
     }
     // plane-major order: CTAs run in item order, so the CTAs in flight then work on neighbouring
     // planes of many tiles instead of many planes of a few tiles, which keeps the pages they touch

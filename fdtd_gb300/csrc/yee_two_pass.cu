@@ -35,8 +35,9 @@ __global__ void __launch_bounds__(256, FDTD_TWO_PASS_MIN_BLOCKS) k_update_h(cons
 }
 
 // Shell passes of the fused schedule: the nodes of the shell items (int4 {x0, y0, k, code}: a
-// block of plane k of shape s = code & 15 (widths 32, 16, 64, 128, 256, 8, 4, 2, 1; 256 nodes) of
-// which the first (code >> 4) & 511 columns and (code >> 13) & 511 rows are the item's) read buffer A (`fi`,
+// block of shape s = code & 15 (widths 32, 16, 64, 128, 256, 8, 4, 2, 1; 256 nodes) of which the
+// first (code >> 4) & 511 columns and (code >> 13) & 511 rows are the item's, in planes k ..
+// k + ((code >> 22) & 15)) read buffer A (`fi`,
 // `pin`) and write buffer B (`fo`, `pout`), one node per thread as in the two-pass kernels. The E
 // pass runs before the interior sweep, the H pass after it, since H reads new E at interior nodes
 // next to the shell.
@@ -55,8 +56,10 @@ __global__ void __launch_bounds__(256, FDTD_SHELL_MIN_BLOCKS) k_shell_e(const __
                                                  const __grid_constant__ PsiSet pin, const __grid_constant__ PsiSet pout,
                                                  const int4* __restrict__ items, long long m) {
     int i, j;
-    if (!shell_node(items[blockIdx.x], p.g, i, j)) return;
-    e_node_global<false, false, false, Idx>(p, fi, fo, pin, pout, i, j, items[blockIdx.x].z, m);
+    const int4 it = items[blockIdx.x];
+    if (!shell_node(it, p.g, i, j)) return;
+    for (int k = it.z, k1 = it.z + ((it.w >> 22) & 15); k <= k1; ++k)
+        e_node_global<false, false, false, Idx>(p, fi, fo, pin, pout, i, j, k, m);
 }
 
 template <typename Idx>
@@ -64,8 +67,10 @@ __global__ void __launch_bounds__(256, FDTD_SHELL_MIN_BLOCKS) k_shell_h(const __
                                                  const __grid_constant__ PsiSet pin, const __grid_constant__ PsiSet pout,
                                                  const int4* __restrict__ items, long long m) {
     int i, j;
-    if (!shell_node(items[blockIdx.x], p.g, i, j)) return;
-    h_node_global<false, Idx>(p, fi, fo, fo, pin, pout, i, j, items[blockIdx.x].z, m);
+    const int4 it = items[blockIdx.x];
+    if (!shell_node(it, p.g, i, j)) return;
+    for (int k = it.z, k1 = it.z + ((it.w >> 22) & 15); k <= k1; ++k)
+        h_node_global<false, Idx>(p, fi, fo, fo, pin, pout, i, j, k, m);
 }
 
 cudaError_t launch_shell(bool e_pass, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
