@@ -217,9 +217,9 @@ def cpu_baseline(sc_full, seconds_budget=20.0):
 TWO_PASS_DRAM_BYTES_PER_CELL = 78.15
 
 
-# DRAM bytes per cell update of one fused step (k_shell_e + k_sweep_interior + k_shell_h): 62.57 B
-# from an ncu capture of the 512^3 bench workload itself (profiles/yee_step_boxes512_launch_list.md),
-# 72.77 B at 256^3 (profiles/yee_step_fused_boxes256_dram.md), where the shell share is larger.
+# DRAM bytes per cell update of one fused step (k_shell_e + k_sweep_interior + k_shell_h),
+# dram__bytes_read.sum + dram__bytes_write.sum from ncu captures: 62.57 B on the 512^3 bench
+# workload itself, 72.77 B at 256^3, where the shell share is larger.
 FUSED_DRAM_BYTES_PER_CELL = {"512": 62.57, "256": 72.77}
 
 
