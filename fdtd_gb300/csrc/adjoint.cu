@@ -66,43 +66,29 @@ __device__ __forceinline__ long long node(const DeviceGrid& g, int i, int j, int
 #ifndef FDTD_ADJ_MIN_BLOCKS
 #define FDTD_ADJ_MIN_BLOCKS 5
 #endif
-__global__ void __launch_bounds__(256, FDTD_ADJ_MIN_BLOCKS) k_adj_h(const __grid_constant__ StepParams p, AdjState a,
-                                               const __grid_constant__ PsiSet psa) {
+// General path of k_adj_h. kBg: a node of class kUniformGeneral + background (CPML slabs and
+// boundary planes in the usual layouts): uniform cells and background tables decided at compile
+// time, as in the forward's specialisation.
+template <bool kBg>
+__device__ __forceinline__ void adj_h_general(const StepParams& p, const AdjState& a, const PsiSet& psa, int i, int j,
+                                              int k, long long n, int c, float lx, float ly, float lz) {
     const DeviceGrid& g = p.g;
-    const int i = blockIdx.x * 32 + threadIdx.x;
-    const int j = blockIdx.y * 8 + threadIdx.y;
-    const int k = blockIdx.z;
-    if (i >= g.nx || j >= g.ny) return;
-    const long long n = node(g, i, j, k);
     const long long P = g.plane, R = g.pitch;
     const bool kp = k < g.nz - 1, jp = j < g.ny - 1, ip = i < g.nx - 1;
-    // finish the transpose of the previous reverse step's calc_e: gather G_E
-    float lx = a.l[3][n] + a.ge[2][n] - (kp ? a.ge[2][n + P] : 0.f) + a.ge[5][n] - (jp ? a.ge[5][n + R] : 0.f);
-    float ly = a.l[4][n] + a.ge[1][n] - (kp ? a.ge[1][n + P] : 0.f) + a.ge[4][n] - (ip ? a.ge[4][n + 1] : 0.f);
-    float lz = a.l[5][n] + a.ge[0][n] - (jp ? a.ge[0][n + R] : 0.f) + a.ge[3][n] - (ip ? a.ge[3][n + 1] : 0.f);
-
-    const int c = p.cls[n];
-    if (c < kUniformGeneral) {  // fast-path node: table coefficients, every component, no CPML
-        const MatCoef* mc = p.coef + c;
-        const float4 x = __ldg(&mc->h[0]), y = __ldg(&mc->h[1]), z = __ldg(&mc->h[2]);
-        a.l[3][n] = x.x * lx; a.l[4][n] = y.x * ly; a.l[5][n] = z.x * lz;
-        a.gh[0][n] = x.y * lx; a.gh[1][n] = x.z * lx; a.gh[2][n] = y.y * ly;
-        a.gh[3][n] = y.z * ly; a.gh[4][n] = z.y * lz; a.gh[5][n] = z.z * lz;
-        return;
-    }
     const uint8_t* mat = p.mat;
-    const bool one = c < kInterfaceNode;  // seven cells of one material, given by the class
-    const int m0 = one ? c - kUniformGeneral : mat[n];
+    const bool one = kBg || c < kInterfaceNode;  // seven cells of one material, given by the class
+    const int m0 = kBg ? p.bg.mat : one ? c - kUniformGeneral : mat[n];
     const int mi = one ? m0 : i > 0 ? mat[n - 1] : 0, mj = one ? m0 : j > 0 ? mat[n - R] : 0;
     const int mk = one ? m0 : k > 0 ? mat[n - P] : 0;
     const bool hx_m = jp && kp, hy_m = ip && kp, hz_m = ip && jp;
     const bool xs = in_slab(i, g.nx, g.pxn, g.pxp), ys = in_slab(j, g.ny, g.pyn, g.pyp), zs = in_slab(k, g.nz, g.pzn, g.pzp);
     const int bg = p.bg.mat;
-    const bool ux = m0 == mi, uy = m0 == mj, uz = m0 == mk;
+    const bool ux = kBg || m0 == mi, uy = kBg || m0 == mj, uz = kBg || m0 == mk;
+    const bool on_bg = kBg || m0 == bg;
     const Coef3 cx = h_coef(p, 0, i == 0, ux, m0, mi);
     const Coef3 cy = h_coef(p, 1, j == 0, uy, m0, mj);
     const Coef3 cz = h_coef(p, 2, k == 0, uz, m0, mk);
-    const bool bx = i != 0 && ux && m0 == bg, by = j != 0 && uy && m0 == bg, bz = k != 0 && uz && m0 == bg;
+    const bool bx = i != 0 && ux && on_bg, by = j != 0 && uy && on_bg, bz = k != 0 && uz && on_bg;
     const BgCurl& B = p.bg;
     int side;
     float g0 = 0.f, g1 = 0.f, g2 = 0.f, g3 = 0.f, g4 = 0.f, g5 = 0.f;
@@ -134,9 +120,8 @@ __global__ void __launch_bounds__(256, FDTD_ADJ_MIN_BLOCKS) k_adj_h(const __grid
     a.gh[0][n] = g0; a.gh[1][n] = g1; a.gh[2][n] = g2; a.gh[3][n] = g3; a.gh[4][n] = g4; a.gh[5][n] = g5;
 }
 
-// ---- transpose of calc_e (e_update), FoM source and design gradient ------------------------
-__global__ void __launch_bounds__(256, FDTD_ADJ_MIN_BLOCKS) k_adj_e(const __grid_constant__ StepParams p, AdjState a,
-                                               const __grid_constant__ PsiSet psa, AdjStep st) {
+__global__ void __launch_bounds__(256, FDTD_ADJ_MIN_BLOCKS) k_adj_h(const __grid_constant__ StepParams p, AdjState a,
+                                               const __grid_constant__ PsiSet psa) {
     const DeviceGrid& g = p.g;
     const int i = blockIdx.x * 32 + threadIdx.x;
     const int j = blockIdx.y * 8 + threadIdx.y;
@@ -144,25 +129,37 @@ __global__ void __launch_bounds__(256, FDTD_ADJ_MIN_BLOCKS) k_adj_e(const __grid
     if (i >= g.nx || j >= g.ny) return;
     const long long n = node(g, i, j, k);
     const long long P = g.plane, R = g.pitch;
-    // finish the transpose of calc_h: gather G_H
-    float lx = a.l[0][n] + (k > 0 ? a.gh[3][n - P] : 0.f) - a.gh[3][n] + (j > 0 ? a.gh[4][n - R] : 0.f) - a.gh[4][n];
-    float ly = a.l[1][n] + (k > 0 ? a.gh[0][n - P] : 0.f) - a.gh[0][n] + (i > 0 ? a.gh[5][n - 1] : 0.f) - a.gh[5][n];
-    float lz = a.l[2][n] + (j > 0 ? a.gh[1][n - R] : 0.f) - a.gh[1][n] + (i > 0 ? a.gh[2][n - 1] : 0.f) - a.gh[2][n];
-    if (n == st.probe) lz += st.source;  // dJ/dEz(p) of the sample taken in this step
+    const bool kp = k < g.nz - 1, jp = j < g.ny - 1, ip = i < g.nx - 1;
+    // finish the transpose of the previous reverse step's calc_e: gather G_E
+    float lx = a.l[3][n] + a.ge[2][n] - (kp ? a.ge[2][n + P] : 0.f) + a.ge[5][n] - (jp ? a.ge[5][n + R] : 0.f);
+    float ly = a.l[4][n] + a.ge[1][n] - (kp ? a.ge[1][n + P] : 0.f) + a.ge[4][n] - (ip ? a.ge[4][n + 1] : 0.f);
+    float lz = a.l[5][n] + a.ge[0][n] - (jp ? a.ge[0][n + R] : 0.f) + a.ge[3][n] - (ip ? a.ge[3][n + 1] : 0.f);
 
     const int c = p.cls[n];
-    if (c < kUniformGeneral) {  // fast-path node: table coefficients, every component, no CPML,
-                                // no lumped edge, outside the design edge box
+    if (c < kUniformGeneral) {  // fast-path node: table coefficients, every component, no CPML
         const MatCoef* mc = p.coef + c;
-        const float4 x = __ldg(&mc->e[0]), y = __ldg(&mc->e[1]), z = __ldg(&mc->e[2]);
-        a.l[0][n] = x.x * lx; a.l[1][n] = y.x * ly; a.l[2][n] = z.x * lz;
-        a.ge[0][n] = x.y * lx; a.ge[1][n] = x.z * lx; a.ge[2][n] = y.y * ly;
-        a.ge[3][n] = y.z * ly; a.ge[4][n] = z.y * lz; a.ge[5][n] = z.z * lz;
+        const float4 x = __ldg(&mc->h[0]), y = __ldg(&mc->h[1]), z = __ldg(&mc->h[2]);
+        a.l[3][n] = x.x * lx; a.l[4][n] = y.x * ly; a.l[5][n] = z.x * lz;
+        a.gh[0][n] = x.y * lx; a.gh[1][n] = x.z * lx; a.gh[2][n] = y.y * ly;
+        a.gh[3][n] = y.z * ly; a.gh[4][n] = z.y * lz; a.gh[5][n] = z.z * lz;
         return;
     }
+    if (c == kUniformGeneral + p.bg.mat) adj_h_general<true>(p, a, psa, i, j, k, n, c, lx, ly, lz);
+    else adj_h_general<false>(p, a, psa, i, j, k, n, c, lx, ly, lz);
+}
+
+// ---- transpose of calc_e (e_update), FoM source and design gradient ------------------------
+// General path of k_adj_e, specialised like adj_h_general (background nodes carry no lumped edge
+// and lie outside the design edge box).
+template <bool kBg>
+__device__ __forceinline__ void adj_e_general(const StepParams& p, const AdjState& a, const PsiSet& psa,
+                                              const AdjStep& st, int i, int j, int k, long long n, int c, float lx,
+                                              float ly, float lz) {
+    const DeviceGrid& g = p.g;
+    const long long P = g.plane, R = g.pitch;
     const uint8_t* mat = p.mat;
-    const bool one = c < kInterfaceNode;  // seven cells of one material, given by the class
-    const int m0 = one ? c - kUniformGeneral : mat[n];
+    const bool one = kBg || c < kInterfaceNode;  // seven cells of one material, given by the class
+    const int m0 = kBg ? p.bg.mat : one ? c - kUniformGeneral : mat[n];
     const int mi = one ? m0 : i > 0 ? mat[n - 1] : 0, mj = one ? m0 : j > 0 ? mat[n - R] : 0;
     const int mk = one ? m0 : k > 0 ? mat[n - P] : 0;
     const int mij = one ? m0 : (i > 0 && j > 0) ? mat[n - 1 - R] : 0;
@@ -172,15 +169,16 @@ __global__ void __launch_bounds__(256, FDTD_ADJ_MIN_BLOCKS) k_adj_e(const __grid
     const bool ex_m = i < g.nx - 1 && in_y && in_z, ey_m = in_x && j < g.ny - 1 && in_z, ez_m = in_x && in_y && k < g.nz - 1;
     const bool xs = in_slab(i, g.nx, g.pxn, g.pxp), ys = in_slab(j, g.ny, g.pyn, g.pyp), zs = in_slab(k, g.nz, g.pzn, g.pzp);
     const int bg = p.bg.mat;
-    const bool ux = m0 == mj && m0 == mk && m0 == mjk;
-    const bool uy = m0 == mi && m0 == mk && m0 == mik;
-    const bool uz = m0 == mi && m0 == mj && m0 == mij;
-    const Coef3 cx = e_coef<true>(p, 0, ux, m0, mj, mk, mjk, i, j, k);
-    const Coef3 cy = e_coef<true>(p, 1, uy, m0, mi, mk, mik, i, j, k);
-    const Coef3 cz = e_coef<true>(p, 2, uz, m0, mi, mj, mij, i, j, k);
+    const bool ux = kBg || (m0 == mj && m0 == mk && m0 == mjk);
+    const bool uy = kBg || (m0 == mi && m0 == mk && m0 == mik);
+    const bool uz = kBg || (m0 == mi && m0 == mj && m0 == mij);
+    const bool on_bg = kBg || m0 == bg;
+    const Coef3 cx = e_coef<!kBg>(p, 0, ux, m0, mj, mk, mjk, i, j, k);
+    const Coef3 cy = e_coef<!kBg>(p, 1, uy, m0, mi, mk, mik, i, j, k);
+    const Coef3 cz = e_coef<!kBg>(p, 2, uz, m0, mi, mj, mij, i, j, k);
 
     // design gradient: lambda here is dJ/dE^{m+1}; E^m and E^{m+1} come from the saved design E
-    if (st.acc) {
+    if (!kBg && st.acc) {  // background nodes lie outside the design edge box
         const int* d = p.dbox;
         const int ei = i - d[0], ej = j - d[1], ek = k - d[2];
         const int bx = d[3] - d[0] + 1, by = d[4] - d[1] + 1, bzz = d[5] - d[2] + 1;
@@ -212,35 +210,64 @@ __global__ void __launch_bounds__(256, FDTD_ADJ_MIN_BLOCKS) k_adj_e(const __grid
         PsiTerm t1{nullptr, 0, 0, 0}, t2{nullptr, 0, 0, 0};
         if (ys) { const int q = psi_off_y(g, i, j, k, side); t1 = PsiTerm{psa.f[2 + side].e[0] + q, p.bey[j], p.aey[j], __fmul_rn(cx.bp, g.dy)}; }
         if (zs) { const int q = psi_off_z(g, i, j, k, side); t2 = PsiTerm{psa.f[4 + side].e[0] + q, p.bez[k], p.aez[k], __fmul_rn(cx.bm, g.dz)}; }
-        const float c1 = ys ? kdiv(cx.bp, ux && m0 == bg, B.e[1][0], p.key, j) : cx.bp;
-        const float c2 = zs ? kdiv(cx.bm, ux && m0 == bg, B.e[2][0], p.kez, k) : cx.bm;
+        const float c1 = ys ? kdiv(cx.bp, ux && on_bg, B.e[1][0], p.key, j) : cx.bp;
+        const float c2 = zs ? kdiv(cx.bm, ux && on_bg, B.e[2][0], p.kez, k) : cx.bm;
         lx = adj_comp(lx, cx.a, c1, c2, t1, t2, g0, g1);
     }
     if (ey_m) {  // Ey: c1 on dHx_k (z CPML), c2 on dHz_i (x CPML)
         PsiTerm t1{nullptr, 0, 0, 0}, t2{nullptr, 0, 0, 0};
         if (zs) { const int q = psi_off_z(g, i, j, k, side); t1 = PsiTerm{psa.f[4 + side].e[1] + q, p.bez[k], p.aez[k], __fmul_rn(cy.bp, g.dz)}; }
         if (xs) { const int q = psi_off_x(g, i, j, k, side); t2 = PsiTerm{psa.f[side].e[0] + q, p.bex[i], p.aex[i], __fmul_rn(cy.bm, g.dx)}; }
-        const float c1 = zs ? kdiv(cy.bp, uy && m0 == bg, B.e[2][1], p.kez, k) : cy.bp;
-        const float c2 = xs ? kdiv(cy.bm, uy && m0 == bg, B.e[0][0], p.kex, i) : cy.bm;
+        const float c1 = zs ? kdiv(cy.bp, uy && on_bg, B.e[2][1], p.kez, k) : cy.bp;
+        const float c2 = xs ? kdiv(cy.bm, uy && on_bg, B.e[0][0], p.kex, i) : cy.bm;
         ly = adj_comp(ly, cy.a, c1, c2, t1, t2, g2, g3);
     }
     if (ez_m) {  // Ez: c1 on dHy_i (x CPML), c2 on dHx_j (y CPML); lumped edges override a, c1, c2
         PsiTerm t1{nullptr, 0, 0, 0}, t2{nullptr, 0, 0, 0};
         if (xs) { const int q = psi_off_x(g, i, j, k, side); t1 = PsiTerm{psa.f[side].e[1] + q, p.bex[i], p.aex[i], __fmul_rn(cz.bp, g.dx)}; }
         if (ys) { const int q = psi_off_y(g, i, j, k, side); t2 = PsiTerm{psa.f[2 + side].e[1] + q, p.bey[j], p.aey[j], __fmul_rn(cz.bm, g.dy)}; }
-        const bool plane_lumped = p.lumped_k[k] < p.lumped_k[k + 1];
+        const bool plane_lumped = !kBg && p.lumped_k[k] < p.lumped_k[k + 1];  // background nodes carry none
         const LumpedEdge* L = plane_lumped ? find_lumped(p, i, j, k) : nullptr;
         float aa, c1, c2;
         if (L) { aa = L->ceze; c1 = L->cezhy; c2 = L->cezhx; }
         else {
             aa = cz.a;
-            c1 = xs ? kdiv(cz.bp, uz && m0 == bg, B.e[0][1], p.kex, i) : cz.bp;
-            c2 = ys ? kdiv(cz.bm, uz && m0 == bg, B.e[1][1], p.key, j) : cz.bm;
+            c1 = xs ? kdiv(cz.bp, uz && on_bg, B.e[0][1], p.kex, i) : cz.bp;
+            c2 = ys ? kdiv(cz.bm, uz && on_bg, B.e[1][1], p.key, j) : cz.bm;
         }
         lz = adj_comp(lz, aa, c1, c2, t1, t2, g4, g5);
     }
     a.l[0][n] = lx; a.l[1][n] = ly; a.l[2][n] = lz;
     a.ge[0][n] = g0; a.ge[1][n] = g1; a.ge[2][n] = g2; a.ge[3][n] = g3; a.ge[4][n] = g4; a.ge[5][n] = g5;
+}
+
+__global__ void __launch_bounds__(256, FDTD_ADJ_MIN_BLOCKS) k_adj_e(const __grid_constant__ StepParams p, AdjState a,
+                                               const __grid_constant__ PsiSet psa, AdjStep st) {
+    const DeviceGrid& g = p.g;
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * 8 + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= g.nx || j >= g.ny) return;
+    const long long n = node(g, i, j, k);
+    const long long P = g.plane, R = g.pitch;
+    // finish the transpose of calc_h: gather G_H
+    float lx = a.l[0][n] + (k > 0 ? a.gh[3][n - P] : 0.f) - a.gh[3][n] + (j > 0 ? a.gh[4][n - R] : 0.f) - a.gh[4][n];
+    float ly = a.l[1][n] + (k > 0 ? a.gh[0][n - P] : 0.f) - a.gh[0][n] + (i > 0 ? a.gh[5][n - 1] : 0.f) - a.gh[5][n];
+    float lz = a.l[2][n] + (j > 0 ? a.gh[1][n - R] : 0.f) - a.gh[1][n] + (i > 0 ? a.gh[2][n - 1] : 0.f) - a.gh[2][n];
+    if (n == st.probe) lz += st.source;  // dJ/dEz(p) of the sample taken in this step
+
+    const int c = p.cls[n];
+    if (c < kUniformGeneral) {  // fast-path node: table coefficients, every component, no CPML,
+                                // no lumped edge, outside the design edge box
+        const MatCoef* mc = p.coef + c;
+        const float4 x = __ldg(&mc->e[0]), y = __ldg(&mc->e[1]), z = __ldg(&mc->e[2]);
+        a.l[0][n] = x.x * lx; a.l[1][n] = y.x * ly; a.l[2][n] = z.x * lz;
+        a.ge[0][n] = x.y * lx; a.ge[1][n] = x.z * lx; a.ge[2][n] = y.y * ly;
+        a.ge[3][n] = y.z * ly; a.ge[4][n] = z.y * lz; a.ge[5][n] = z.z * lz;
+        return;
+    }
+    if (c == kUniformGeneral + p.bg.mat) adj_e_general<true>(p, a, psa, st, i, j, k, n, c, lx, ly, lz);
+    else adj_e_general<false>(p, a, psa, st, i, j, k, n, c, lx, ly, lz);
 }
 
 // After a forward step: the FoM sample Ez(p) and, when `snap` is set, the E components over the
