@@ -218,9 +218,9 @@ TWO_PASS_DRAM_BYTES_PER_CELL = 78.15
 
 
 # DRAM bytes per cell update of one fused step (k_shell_e + k_sweep_interior + k_shell_h),
-# dram__bytes_read.sum + dram__bytes_write.sum from ncu captures: 62.57 B on the 512^3 bench
+# dram__bytes_read.sum + dram__bytes_write.sum from ncu captures: 62.46 B on the 512^3 bench
 # workload itself, 72.77 B at 256^3, where the shell share is larger.
-FUSED_DRAM_BYTES_PER_CELL = {"512": 62.57, "256": 72.77}
+FUSED_DRAM_BYTES_PER_CELL = {"512": 62.46, "256": 72.77}
 
 
 def measured_traffic(schedule, cells, config):
