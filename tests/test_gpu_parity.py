@@ -212,6 +212,20 @@ def test_onestep_random_psi_bitwise(gpu_lib, schedule):
         assert bitwise_equal(out[c], fix[key]), (key, rel_l2(out[c], fix[key]))
 
 
+@pytest.mark.parametrize("dims,pml", [((70, 45, 40), 0), ((61, 50, 30), 1), ((90, 37, 33), 2)])
+def test_fused_thin_shell_equals_two_pass(gpu_lib, dims, pml):
+    """Grids whose shell bands are 1 to 8 nodes wide (no or thin CPML): the fused schedule's shell
+    items take the narrow block shapes, and the result equals the two-pass schedule bit for bit."""
+    import dataclasses
+    nx, ny, nz = dims
+    sc = S.scaled_boxes(nx, ny, nz, 20, seed=nx + pml, pml=3, n_boxes=6, n_sources=1, n_probes=5, name="thin_shell")
+    sc = dataclasses.replace(sc, pml=(pml,) * 6)
+    p1, f1, _ = run_gpu(sc, schedule=1)
+    p2, f2, _ = run_gpu(sc, schedule=2)
+    assert bitwise_equal(p1, p2), rel_l2(p2, p1)
+    assert bitwise_equal(f1, f2), rel_l2(f2, f1)
+
+
 @pytest.mark.parametrize("dims", [(70, 45, 80), (33, 13, 40), (100, 17, 16)])
 def test_fused_equals_two_pass(gpu_lib, dims):
     """Ragged tiles in x and y, several z-chunks per column: the fused sweep reproduces the two-pass
