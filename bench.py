@@ -45,6 +45,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-hbm", action="store_true")
     return ap.parse_args()
 
 
@@ -194,21 +195,60 @@ def replica_value(cells, steps, ms_per_rank, world):
     return world * cells * steps / (ms_per_rank * 1e-3) / 1e9
 
 
-def cpu_baseline(sc_full, seconds_budget=20.0):
-    """The CPU oracle (FP32 restatement of the reference's calc_e/calc_h) on a bounded sample: a
-    256 x 256 x 128 sub-domain of the same generator, timed over a few steps on all host cores."""
+def cpu_baseline():
+    """The CPU oracle (FP32 restatement of the reference's calc_e / calc_h, OpenMP over z-planes)
+    on all host cores, time loop only (setup excluded): a 50-step window of a 512 x 512 x 64 z-slab
+    of the 512^3 generator (same seed, boxes clipped to the slab), median of 3 runs, as the value;
+    the 64^3 vacuum workload in full (1000 steps) beside it."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     from fdtd_gb300 import scenario as S
-    sub = S.random_boxes(256, 256, 128, 8, seed=512, edge=(8, 64), name="cpu_sample")
     cores = os.cpu_count() or 1
-    # setup cost is excluded by timing two runs of different length
-    t0 = time.perf_counter(); oracle.run(sub, steps=2, threads=cores); t1 = time.perf_counter()
-    t2 = time.perf_counter(); oracle.run(sub, steps=8, threads=cores); t3 = time.perf_counter()
-    per_step = max(((t3 - t2) - (t1 - t0)) / 6.0, 1e-9)
-    return {"value": sub.cells / per_step / 1e9, "unit": "Gcell-updates/s", "cores": cores, "kind": "port",
-            "sample": "CPU oracle (FP32, OpenMP) on a 256x256x128 sub-domain of the random-box generator, "
-                      "6 steps (difference of an 8-step and a 2-step run, setup excluded)"}
+    window = S.random_boxes(512, 512, 64, 50, seed=512, name="cpu_window")
+    rates = []
+    for _ in range(3):
+        oracle.run(window, steps=50, threads=cores)
+        rates.append(window.cells * 50 / oracle.last_step_seconds() / 1e9)
+    small = S.config_small()
+    oracle.run(small, threads=cores)
+    t_small = oracle.last_step_seconds()
+    return {"value": float(np.median(rates)), "unit": "Gcell-updates/s", "cores": cores, "kind": "port",
+            "sample": "CPU oracle (FP32, OpenMP, all host cores), time loop only: 50 steps of a 512x512x64 "
+                      "z-slab of the 512^3 random-box generator, median of 3 runs",
+            "runs": [round(r, 4) for r in rates],
+            "vacuum64_full": {"value": round(small.cells * small.steps / t_small / 1e9, 4),
+                              "unit": "Gcell-updates/s", "steps": small.steps, "seconds": round(t_small, 3)}}
+
+
+def fp64_error():
+    """Error of the FP32 solver against an FP64 build of the same update at small size: the 64^3
+    vacuum workload on the GPU (C ABI, AUTO) against the FP64 oracle. Relative L2 of the Ez probe
+    series over the full 1000 steps, and of the final fields after 150 steps, while the pulse is
+    still inside the grid (after 1000 steps the CPML has absorbed it and only residue of the order
+    of the rounding is left)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from fdtd_gb300 import scenario as S, solver
+    sc = S.config_small()
+    cores = os.cpu_count() or 1
+
+    def gpu(steps):
+        with solver.Simulation.from_scenario(sc, probe_capacity=steps) as sim:
+            sim.step(steps)
+            sim.synchronize()
+            return sim.read_probes(0, steps).astype(np.float64), sim.fields().astype(np.float64)
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    p, _ = gpu(sc.steps)
+    p64, _ = oracle.run(sc, precision="f64", threads=cores)
+    _, f = gpu(150)
+    _, f64 = oracle.run(sc, steps=150, precision="f64", threads=cores)
+    return {"workload": "64^3 vacuum, 10-cell CPML, 1 source, 1 Ez probe",
+            "probes_rel_l2": rel(p, p64), "probe_steps": sc.steps,
+            "e_fields_rel_l2": rel(f[:3], f64[:3]), "h_fields_rel_l2": rel(f[3:], f64[3:]), "field_steps": 150,
+            "note": "the solver equals the reference's kernels bit for bit on this workload "
+                    "(tests/golden/vacuum64.npz); this is the FP32 error of the scheme itself"}
 
 
 # DRAM bytes per cell update of one two-pass step (k_update_e + k_update_h), from an ncu capture
@@ -297,7 +337,8 @@ def bench_ours(args, rank, world):
 
 def e2e_ours(args, sc, mat):
     """Same metric through the C ABI from host buffers: handle creation, material table and index
-    upload, waveform upload, K steps, probe read-back, destroy."""
+    upload (pinned), waveform upload, K steps, probe read-back (the handle is destroyed after the
+    timer stops). A second run times each phase with a synchronize after it, destroy included."""
     import torch
     from fdtd_gb300 import solver
     pinned = torch.from_numpy(mat).pin_memory()
@@ -308,13 +349,90 @@ def e2e_ours(args, sc, mat):
     sim = solver.Simulation.from_scenario(sc, args.schedule, material_index=host_mat, probe_capacity=steps)
     sim.step(steps)
     probes = sim.read_probes(0, steps)
-    sim.close()
     t1 = time.perf_counter()
+    sim.close()  # after the result is on the host: not part of the timed job
     h2d = host_mat.nbytes + sum(s.waveform.nbytes for s in sc.sources)
     d2h = probes.nbytes
-    return {"value": sc.cells * steps / (t1 - t0) / 1e9, "unit": "Gcell-updates/s",
-            "h2d_bytes_per_step": round(h2d / steps, 1), "d2h_bytes_per_step": round(d2h / steps, 1),
-            "seconds": round(t1 - t0, 3)}
+    out = {"value": sc.cells * steps / (t1 - t0) / 1e9, "unit": "Gcell-updates/s",
+           "h2d_bytes_per_step": round(h2d / steps, 1), "d2h_bytes_per_step": round(d2h / steps, 1),
+           "seconds": round(t1 - t0, 4), "steps": steps}
+    # phase breakdown (separate run, synchronised between phases)
+    ph = {}
+    t = time.perf_counter()
+
+    def mark(name):
+        nonlocal t
+        torch.cuda.synchronize()
+        now = time.perf_counter()
+        ph[name] = round((now - t) * 1e3, 2)
+        t = now
+    sim = solver.Simulation(sc.nx, sc.ny, sc.nz, sc.dx, sc.dy, sc.dz, sc.dt, sc.pml, sc.eps0, sc.mu0, sc.pi,
+                            args.schedule)
+    mark("create_ms")
+    sim.set_materials(sc.material_table())
+    sim.set_material_index(host_mat)
+    for q in sc.sources:
+        sim.add_source(q.box, q.resistance, q.waveform)
+    for q in sc.probes:
+        sim.add_probe(q.component, q.i, q.j, q.k)
+    sim.set_probe_capacity(steps)
+    mark("upload_ms")
+    sim.prepare()
+    sim.synchronize()
+    mark("prepare_ms")
+    first = min(8, steps)
+    sim.step(first)
+    sim.synchronize()
+    mark("first_8_steps_ms")
+    sim.step(steps - first)
+    sim.synchronize()
+    mark("other_steps_ms")
+    sim.read_probes(0, steps)
+    mark("readback_ms")
+    sim.close()
+    mark("destroy_ms")
+    out["phases"] = ph
+    return out
+
+
+def bench_hbm(warmup=3, steps=20):
+    """The 1024 x 1024 x 896 single domain (939.5 M cells, the same random-box generator, 10-cell
+    CPML, 4 sources, 16 probes): device-timed steps with the grid resident, its own roofline."""
+    import torch
+    from fdtd_gb300 import solver
+    sc, desc = scenario_for("hbm")
+    B = algorithmic_bytes_per_cell(sc)
+    mat = sc.material_index()
+    stream = torch.cuda.Stream()
+    sim = solver.Simulation.from_scenario(sc, 0, material_index=mat, probe_capacity=warmup + steps + 64)
+    del mat
+    sim.set_stream(stream.cuda_stream)
+    sim.prepare()
+    sim.tune_schedule()
+    sim.step(warmup)
+    sim.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    e0.record(stream)
+    sim.step(steps)
+    e1.record(stream)
+    e1.synchronize()
+    clk = clocks.stop()
+    active = sim.active_schedule
+    dev_bytes = sim.device_bytes()
+    sim.close()
+    ms = e0.elapsed_time(e1) / steps
+    peak, peak_kind = measured_peak()
+    achieved = B * sc.cells / (ms * 1e-3) / 1e9
+    return {"workload": desc, "grid": [sc.nx, sc.ny, sc.nz], "cells": sc.cells, "steps": steps, "warmup": warmup,
+            "value": round(sc.cells / (ms * 1e-3) / 1e9, 3), "unit": "Gcell-updates/s", "ms_per_step": round(ms, 4),
+            "schedule": {1: "two-pass", 2: "fused"}.get(active, str(active)), "device_gb": round(dev_bytes / 1e9, 2),
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "bytes_per_cell_update": round(B, 3),
+                         "peak_source": peak_kind},
+            "clocks": clk}
 
 
 def bench_adjoint():
@@ -453,12 +571,15 @@ def main():
     out = bench_ours(args, rank, world)
     if rank == 0:
         if not args.no_cpu_baseline:
-            sc, _ = scenario_for(args.config)
-            out["cpu_baseline"] = cpu_baseline(sc)
+            out["cpu_baseline"] = cpu_baseline()
+        if world == 1:
+            out["fp64_error"] = fp64_error()
         if not args.no_adjoint and world == 1:
             out["adjoint"] = bench_adjoint()
         if not args.no_batched and world == 1:
             out["batched"] = bench_batched()
+        if not args.no_hbm and world == 1 and args.config != "hbm":
+            out["hbm"] = bench_hbm()
         print(json.dumps(out))
 
 

@@ -31,7 +31,7 @@ def nvcc() -> str:
 
 
 def sources():
-    return sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    return sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
 
 
 def _headers():
@@ -54,7 +54,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     objs = []
     cmds = []
     for src in sources():
-        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(BUILD, os.path.splitext(os.path.basename(src))[0] + ".o")
         objs.append(obj)
         cmds.append([nv, "-c", src, "-o", obj] + ARCH + NVCC_FLAGS)
 

@@ -18,6 +18,7 @@
 #include "../../include/fdtd_api.h"
 #include "adjoint.h"
 #include "batch.h"
+#include "planner.h"
 #include "ports.h"
 #include "yee_kernels.h"
 
@@ -92,6 +93,11 @@ struct fdtd_handle {
     uint16_t* rec = nullptr;          // coefficient row per node, built with the classes
     MatCoef* coef_rows = nullptr;     // material rows then interface rows (StepParams::coef)
     int n_iface_rows = 0;
+    // interface-key hash set and its lists (launch_iface_set / launch_iface_rows)
+    unsigned long long* iface_table = nullptr;
+    unsigned long long* iface_keys = nullptr;
+    int* iface_slot_row = nullptr;
+    int* iface_counters = nullptr;
     int n_lumped_edges = 0;
     MatProps* props = nullptr;
     MatCoef* coef = nullptr;
@@ -103,7 +109,7 @@ struct fdtd_handle {
     long long psi_elems[6] = {};  // elements per psi array of each face
 
     // host-side definitions
-    std::vector<fdtd_material> materials;
+    std::vector<fdtd_material_axes> materials;
     std::vector<LumpedDef> lumped;
     std::vector<std::vector<float>> waves;  // per source, per-edge signal
     std::vector<Probe> probes;
@@ -131,6 +137,7 @@ struct fdtd_handle {
     float* ring = nullptr;
     long long ring_cap = 4096;
     int* status = nullptr;
+    int* small = nullptr;  // device scratch of a few ints for results read back by entry points
 
     long long step = 0;
     long long bytes = 0;
@@ -160,9 +167,12 @@ struct fdtd_handle {
         std::vector<void*> bufs;       // everything above, for release
     } adj;
 
-    // host-side work list of fdtd_step_static_scratch (interior items first), planned on first use
-    std::vector<int4> static_items;
-    int static_n_interior = -1;
+    // work list of fdtd_step_static_scratch (interior items first) in pinned host memory, planned
+    // on first use; each call uploads it into the scratch with one asynchronous copy
+    int4* static_items = nullptr;
+    size_t static_n_items = 0;
+    int static_counts[4] = {};     // items per list (interior, wide, narrow, shell)
+    bool static_planned = false;
 
     std::vector<size_t> alloc_sizes;  // bytes of each entry of allocs
 
@@ -191,6 +201,14 @@ struct fdtd_handle {
 namespace {
 
 long long vol(const fdtd_handle* h) { return h->g.plane * (long long)h->g.nz; }
+
+fdtd_material_axes axes_of(const fdtd_material& m) {
+    fdtd_material_axes r;
+    for (int a = 0; a < 3; ++a) {
+        r.eps_r[a] = m.eps_r; r.sigma_e[a] = m.sigma_e; r.mu_r[a] = m.mu_r; r.sigma_m[a] = m.sigma_m;
+    }
+    return r;
+}
 
 bool in_slab_host(int q, int n, int pn, int pp) { return q < pn || q >= n - pp; }
 
@@ -284,18 +302,40 @@ void* tensor_map_encoder() {
     return fn;
 }
 
-// Work items of the fused schedule: interior items (TMA sweep) and the rest (shell passes). The
-// design region, if any, stays with the shell; planned again when it changes.
+PlanGrid plan_grid(const DeviceGrid& g) {
+    return PlanGrid{g.nx, g.ny, g.nz, g.pxn, g.pxp, g.pyn, g.pyp, g.pzn, g.pzp};
+}
+
+// The lists of a plan one after the other (interior, wide, narrow, shell) and their counts.
+std::vector<PlanItem> flatten(const FusedPlan& plan, int counts[4]) {
+    std::vector<PlanItem> all;
+    const std::vector<PlanItem>* lists[4] = {&plan.interior, &plan.wide, &plan.narrow, &plan.shell};
+    for (int q = 0; q < 4; ++q) {
+        counts[q] = (int)lists[q]->size();
+        all.insert(all.end(), lists[q]->begin(), lists[q]->end());
+    }
+    return all;
+}
+
+// The work lists over a device copy of the flattened plan.
+FusedWork work_of(const int4* d, const int counts[4]) {
+    return FusedWork{d, counts[0], d + counts[0], counts[1], d + counts[0] + counts[1], counts[2],
+                     d + counts[0] + counts[1] + counts[2], counts[3]};
+}
+
+// Work items of the fused schedule (planner.cpp). The design region, if any, stays with the shell;
+// planned again when it changes.
 int plan_work(fdtd_handle* h) {
-    std::vector<int4> wi, wg;
-    plan_fused(h->g, h->kc, h->has_design ? h->dbox : nullptr, wi, wg);
+    FusedPlan plan;
+    plan_fused(plan_grid(h->g), h->kc, h->has_design ? h->dbox : nullptr, plan);
+    int counts[4];
+    const std::vector<PlanItem> all = flatten(plan, counts);
     h->release((void*)h->work.interior);
     h->work = FusedWork{};
     int4* d = nullptr;
-    CUDA_TRY(h->alloc((void**)&d, sizeof(int4) * (wi.size() + wg.size() + 1)));
-    if (!wi.empty()) CUDA_TRY(cudaMemcpy(d, wi.data(), sizeof(int4) * wi.size(), cudaMemcpyHostToDevice));
-    if (!wg.empty()) CUDA_TRY(cudaMemcpy(d + wi.size(), wg.data(), sizeof(int4) * wg.size(), cudaMemcpyHostToDevice));
-    h->work = FusedWork{d, (int)wi.size(), d + wi.size(), (int)wg.size()};
+    CUDA_TRY(h->alloc((void**)&d, sizeof(int4) * (all.size() + 1)));
+    if (!all.empty()) CUDA_TRY(cudaMemcpy(d, all.data(), sizeof(int4) * all.size(), cudaMemcpyHostToDevice));
+    h->work = work_of(d, counts);
     h->replan = false;
     return FDTD_OK;
 }
@@ -320,7 +360,7 @@ int ensure_fused(fdtd_handle* h) {
             return fail(FDTD_ERR_CUDA, "tensor map encoding failed");
     }
     CUDA_TRY(fused_configure());
-    h->kc = fused_chunk(h->g);
+    h->kc = plan_chunk(plan_grid(h->g));
     rc = plan_work(h);
     if (rc) return rc;
     CUDA_TRY(cudaStreamSynchronize(h->stream));
@@ -387,7 +427,7 @@ int fdtd_create(const fdtd_grid* grid, fdtd_handle** out) {
     if (h->alloc((void**)&h->mat, (size_t)V) != cudaSuccess) return cleanup(fail(FDTD_ERR_OOM, "material index allocation failed"));
     if (h->alloc((void**)&h->props, sizeof(MatProps) * kMaxMaterials) != cudaSuccess ||
         h->alloc((void**)&h->coef, sizeof(MatCoef) * (kMaxMaterials + 1)) != cudaSuccess ||
-        h->alloc((void**)&h->status, sizeof(int)) != cudaSuccess)
+        h->alloc((void**)&h->status, sizeof(int)) != cudaSuccess || h->alloc((void**)&h->small, 4 * sizeof(int)) != cudaSuccess)
         return cleanup(fail(FDTD_ERR_OOM, "table allocation failed"));
     const int ns[3] = {g.nx, g.ny, g.nz};
     for (int a = 0; a < 3; ++a)
@@ -424,7 +464,7 @@ int fdtd_create(const fdtd_grid* grid, fdtd_handle** out) {
         if (launch_fill(h->field[0][c], V, kTiny, nullptr) != cudaSuccess) return cleanup(fail(FDTD_ERR_CUDA, "fill failed"));
     if (cudaMemset(h->mat, 0, (size_t)V) != cudaSuccess || cudaMemset(h->status, 0, sizeof(int)) != cudaSuccess)
         return cleanup(fail(FDTD_ERR_CUDA, "memset failed"));
-    h->materials.push_back(fdtd_material{1.0f, kTiny, 1.0f, kTiny});
+    h->materials.push_back(axes_of(fdtd_material{1.0f, kTiny, 1.0f, kTiny}));
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return cleanup(fail(FDTD_ERR_CUDA, std::string("init: ") + cudaGetErrorString(e)));
     *out = h;
@@ -438,6 +478,7 @@ int fdtd_destroy(fdtd_handle* h) {
     for (void* p : h->allocs) cudaFree(p);
     h->allocs.clear();
     h->alloc_sizes.clear();
+    if (h->static_items) cudaFreeHost(h->static_items);
     delete h;
     return FDTD_OK;
 }
@@ -456,19 +497,21 @@ int fdtd_set_schedule(fdtd_handle* h, int32_t schedule) {
     return FDTD_OK;
 }
 
-int fdtd_set_materials(fdtd_handle* h, const fdtd_material* table, int32_t n) {
+int fdtd_set_materials_axes(fdtd_handle* h, const fdtd_material_axes* table, int32_t n) {
     if (!h || !table) return fail(FDTD_ERR_INVALID, "NULL argument");
     if (n < 1 || n > kMaxMaterials) return fail(FDTD_ERR_INVALID, "material count must be 1..256");
-    for (int q = 0; q < n; ++q) {
-        const fdtd_material& m = table[q];
-        if (!(m.eps_r > 0.f) || !(m.mu_r > 0.f) || !std::isfinite(m.eps_r) || !std::isfinite(m.mu_r))
-            return fail(FDTD_ERR_INVALID, "material " + std::to_string(q) + ": eps_r and mu_r must be positive");
-        if (!(m.sigma_e >= 0.f) || !std::isfinite(m.sigma_e))
-            return fail(FDTD_ERR_INVALID, "material " + std::to_string(q) + ": sigma_e must be >= 0");
-        // the harmonic mean of two magnetic conductivities (fdtdrav.h:1187) is 0/0 for zeros
-        if (!(m.sigma_m > 0.f) || !std::isfinite(m.sigma_m))
-            return fail(FDTD_ERR_INVALID, "material " + std::to_string(q) + ": sigma_m must be > 0 (use 1.2e-38 for a lossless medium)");
-    }
+    for (int q = 0; q < n; ++q)
+        for (int a = 0; a < 3; ++a) {
+            const fdtd_material_axes& m = table[q];
+            const std::string what = "material " + std::to_string(q) + " axis " + std::to_string(a);
+            if (!(m.eps_r[a] > 0.f) || !(m.mu_r[a] > 0.f) || !std::isfinite(m.eps_r[a]) || !std::isfinite(m.mu_r[a]))
+                return fail(FDTD_ERR_INVALID, what + ": eps_r and mu_r must be positive");
+            if (!(m.sigma_e[a] >= 0.f) || !std::isfinite(m.sigma_e[a]))
+                return fail(FDTD_ERR_INVALID, what + ": sigma_e must be >= 0");
+            // the harmonic mean of two magnetic conductivities (fdtdrav.h:1187) is 0/0 for zeros
+            if (!(m.sigma_m[a] > 0.f) || !std::isfinite(m.sigma_m[a]))
+                return fail(FDTD_ERR_INVALID, what + ": sigma_m must be > 0 (use 1.2e-38 for a lossless medium)");
+        }
     if (h->prepared && n < (int)h->materials.size())
         return fail(FDTD_ERR_STATE, "cannot shrink the material table after the index uses it");
     if (h->has_design && n > kDesign)
@@ -478,16 +521,30 @@ int fdtd_set_materials(fdtd_handle* h, const fdtd_material* table, int32_t n) {
     return FDTD_OK;
 }
 
+int fdtd_set_materials(fdtd_handle* h, const fdtd_material* table, int32_t n) {
+    if (!h || !table) return fail(FDTD_ERR_INVALID, "NULL argument");
+    if (n < 1 || n > kMaxMaterials) return fail(FDTD_ERR_INVALID, "material count must be 1..256");
+    std::vector<fdtd_material_axes> t((size_t)n);
+    for (int q = 0; q < n; ++q) t[q] = axes_of(table[q]);
+    return fdtd_set_materials_axes(h, t.data(), n);
+}
+
 int fdtd_set_material_index(fdtd_handle* h, const uint8_t* cells) {
     if (!h || !cells) return fail(FDTD_ERR_INVALID, "NULL argument");
     const DeviceGrid& g = h->g;
-    const size_t n = (size_t)g.nx * g.ny * g.nz;
-    const uint8_t mx = *std::max_element(cells, cells + n);
-    if ((int)mx >= (int)h->materials.size())
-        return fail(FDTD_ERR_INVALID, "material index " + std::to_string(mx) + " outside the material table");
     CUDA_TRY(cudaMemcpy2DAsync(h->mat, g.pitch, cells, g.nx, g.nx, (size_t)g.ny * g.nz, cudaMemcpyHostToDevice, h->stream));
+    // validated on the device: the largest index of the uploaded cells
+    CUDA_TRY(launch_index_max(h->mat, g, h->small, h->stream));
+    int mx = 0;
+    CUDA_TRY(cudaMemcpyAsync(&mx, h->small, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     h->dirty_lumped = true;
+    if (mx >= (int)h->materials.size()) {  // leave a valid index behind: every cell background
+        CUDA_TRY(cudaMemsetAsync(h->mat, 0, (size_t)vol(h), h->stream));
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+        return fail(FDTD_ERR_INVALID, "material index " + std::to_string(mx) + " outside the material table (the index "
+                                      "is reset to material 0)");
+    }
     return FDTD_OK;
 }
 
@@ -1048,31 +1105,29 @@ int build_plates(fdtd_handle* h) {
 int build_interface_rows(fdtd_handle* h) {
     const DeviceGrid& g = h->g;
     if (!h->rec) CUDA_TRY(h->alloc((void**)&h->rec, (size_t)vol(h) * sizeof(uint16_t)));
-    unsigned long long* count = nullptr;
-    unsigned long long* keys = nullptr;
-    CUDA_TRY(h->alloc((void**)&count, sizeof(unsigned long long)));
-    struct Temp {
-        fdtd_handle* h;
-        void* a[2];
-        ~Temp() { h->release(a[0]); h->release(a[1]); }
-    } tmp{h, {count, nullptr}};
-    unsigned long long n = 0;
-    CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(n), h->stream));
-    CUDA_TRY(launch_iface_keys(g, h->cls, h->mat, nullptr, count, 0, h->stream));
-    CUDA_TRY(cudaMemcpyAsync(&n, count, sizeof(n), cudaMemcpyDeviceToHost, h->stream));
+    if (!h->iface_table) {
+        CUDA_TRY(h->alloc((void**)&h->iface_table, sizeof(unsigned long long) * kIfaceTableSize));
+        CUDA_TRY(h->alloc((void**)&h->iface_keys, sizeof(unsigned long long) * kIfaceTableSize));
+        CUDA_TRY(h->alloc((void**)&h->iface_slot_row, sizeof(int) * kIfaceTableSize));
+        CUDA_TRY(h->alloc((void**)&h->iface_counters, sizeof(int) * 2));
+    }
+    // distinct keys on the device; only they come to the host (two small copies)
+    CUDA_TRY(launch_iface_set(g, h->cls, h->mat, h->iface_table, h->iface_counters, h->iface_keys, h->stream));
+    int counters[2] = {0, 0};
+    CUDA_TRY(cudaMemcpyAsync(counters, h->iface_counters, sizeof(counters), cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(cudaStreamSynchronize(h->stream));
+    const int n = std::min(counters[1], kIfaceTableSize);
     std::vector<unsigned long long> hk((size_t)n);
     if (n > 0) {
-        CUDA_TRY(h->alloc((void**)&keys, (size_t)n * sizeof(unsigned long long)));
-        tmp.a[1] = keys;
-        CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(n), h->stream));
-        CUDA_TRY(launch_iface_keys(g, h->cls, h->mat, keys, count, (long long)n, h->stream));
-        CUDA_TRY(cudaMemcpyAsync(hk.data(), keys, (size_t)n * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(cudaMemcpyAsync(hk.data(), h->iface_keys, (size_t)n * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                 h->stream));
         CUDA_TRY(cudaStreamSynchronize(h->stream));
         std::sort(hk.begin(), hk.end());
         hk.erase(std::unique(hk.begin(), hk.end()), hk.end());
         if (hk.size() > (size_t)kMaxInterfaceRows) hk.resize((size_t)kMaxInterfaceRows);  // the rest stay general
-        CUDA_TRY(cudaMemcpyAsync(keys, hk.data(), hk.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice, h->stream));
+        // pageable source: the copy has taken the data when the call returns
+        CUDA_TRY(cudaMemcpyAsync(h->iface_keys, hk.data(), hk.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                                 h->stream));
     }
     const int n_rows = (int)hk.size();
     h->release(h->coef_rows);
@@ -1081,13 +1136,13 @@ int build_interface_rows(fdtd_handle* h) {
     CUDA_TRY(h->alloc((void**)&h->coef_rows, sizeof(MatCoef) * (size_t)(kFirstInterfaceRow + n_rows)));
     CUDA_TRY(cudaMemcpyAsync(h->coef_rows, h->coef, sizeof(MatCoef) * (size_t)kFirstInterfaceRow, cudaMemcpyDeviceToDevice,
                              h->stream));
-    CUDA_TRY(launch_iface_rows(g, h->cls, h->mat, keys, n_rows, h->rec, h->stream));
+    CUDA_TRY(launch_iface_rows(g, h->cls, h->mat, h->iface_table, h->iface_keys, n_rows, h->iface_slot_row, h->rec,
+                               h->stream));
     StepParams p{};  // the rows come from the material rows and properties only
     p.g = g;
     p.props = h->props;
     p.coef = h->coef;
-    CUDA_TRY(launch_iface_coefs(p, keys, n_rows, h->coef_rows, h->stream));
-    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    CUDA_TRY(launch_iface_coefs(p, h->iface_keys, n_rows, h->coef_rows, h->stream));
     h->n_iface_rows = n_rows;
     return FDTD_OK;
 }
@@ -1123,9 +1178,10 @@ int ensure_prepared(fdtd_handle* h) {
     if (h->dirty_materials || !h->prepared) {
         std::vector<MatProps> props(kMaxMaterials);
         for (int q = 0; q < kMaxMaterials; ++q) {
-            fdtd_material m = q < (int)h->materials.size() ? h->materials[q] : fdtd_material{1.0f, kTiny, 1.0f, kTiny};
-            if (q == kDesign && h->has_design) m = h->design_base;  // eps_r comes per cell
-            props[q] = MatProps{m.eps_r, m.sigma_e, m.mu_r, m.sigma_m};
+            fdtd_material_axes m =
+                q < (int)h->materials.size() ? h->materials[q] : axes_of(fdtd_material{1.0f, kTiny, 1.0f, kTiny});
+            if (q == kDesign && h->has_design) m = axes_of(h->design_base);  // eps_r comes per cell
+            for (int a = 0; a < 3; ++a) props[q].a[a] = MatAxis{m.eps_r[a], m.sigma_e[a], m.mu_r[a], m.sigma_m[a]};
         }
         CUDA_TRY(cudaMemcpy(h->props, props.data(), sizeof(MatProps) * kMaxMaterials, cudaMemcpyHostToDevice));
         const int n_tab = h->has_design ? kMaxMaterials : (int)h->materials.size();
@@ -1239,14 +1295,22 @@ extern "C" int fdtd_step_static_scratch(fdtd_handle* h, int64_t n) {
     int dev = -1;
     CUDA_TRY(cudaGetDevice(&dev));
     if (dev != h->device) return fail(FDTD_ERR_STATE, "the current device is not the handle's device");
-    if (h->static_n_interior < 0) {  // host-only planning, as for the fused schedule
-        std::vector<int4> wi, wg;
-        plan_fused(h->g, fused_chunk(h->g), h->has_design ? h->dbox : nullptr, wi, wg);
-        h->static_n_interior = (int)wi.size();
-        wi.insert(wi.end(), wg.begin(), wg.end());
-        h->static_items.swap(wi);
+    if (!h->static_planned) {  // planning, as for the fused schedule; host memory only
+        FusedPlan plan;
+        const PlanGrid pg = plan_grid(h->g);
+        plan_fused(pg, plan_chunk(pg), h->has_design ? h->dbox : nullptr, plan);
+        const std::vector<PlanItem> all = flatten(plan, h->static_counts);
+        if (h->static_items) CUDA_TRY(cudaFreeHost(h->static_items));
+        h->static_items = nullptr;
+        h->static_n_items = 0;
+        if (!all.empty()) {
+            CUDA_TRY(cudaHostAlloc((void**)&h->static_items, all.size() * sizeof(int4), cudaHostAllocDefault));
+            std::memcpy(h->static_items, all.data(), all.size() * sizeof(int4));
+        }
+        h->static_n_items = all.size();
+        h->static_planned = true;
     }
-    const ScratchLayout L = scratch_layout(h, h->static_items.size());
+    const ScratchLayout L = scratch_layout(h, h->static_n_items);
     if (L.total > kStaticScratchBytes)
         return fail(FDTD_ERR_RANGE, "grid needs " + std::to_string(L.total) + " bytes of step scratch; the static scratch holds " +
                                         std::to_string(kStaticScratchBytes) + " (about a 64^3 grid with 10-cell CPML)");
@@ -1278,12 +1342,13 @@ extern "C" int fdtd_step_static_scratch(fdtd_handle* h, int64_t n) {
             return fail(FDTD_ERR_CUDA, "tensor map encoding failed");
     }
     int4* d_items = (int4*)(base + L.items);
-    const size_t n_items = h->static_items.size();
-    if (n_items) CUDA_TRY(cudaMemcpyAsync(d_items, h->static_items.data(), n_items * sizeof(int4), cudaMemcpyHostToDevice, h->stream));
-    const FusedWork w{d_items, h->static_n_interior, d_items + h->static_n_interior, (int)n_items - h->static_n_interior};
-    // the scratch's CPML arrays start as copies of the handle's, so that the elements no step
-    // writes agree when the result is copied back
-    for (int f = 0; f < 6; ++f) {
+    const size_t n_items = h->static_n_items;
+    if (n_items) CUDA_TRY(cudaMemcpyAsync(d_items, h->static_items, n_items * sizeof(int4), cudaMemcpyHostToDevice, h->stream));
+    const FusedWork w = work_of(d_items, h->static_counts);
+    // With an odd count the result ends in the scratch and is copied back whole, so the scratch's
+    // CPML arrays start as copies of the handle's: the elements no step writes then agree. With an
+    // even count the last step writes the handle's own buffers and the scratch needs no copy.
+    for (int f = 0; f < 6 && (n & 1); ++f) {
         const size_t nb = (size_t)h->psi_elems[f] * sizeof(float);
         if (!nb) continue;
         float* src[4];
@@ -1358,7 +1423,7 @@ extern "C" int fdtd_set_design_region(fdtd_handle* h, const int32_t box[6], cons
     h->design_base = *base;
     h->has_design = true;
     h->replan = true;            // fused work items
-    h->static_n_interior = -1;   // and those of fdtd_step_static_scratch
+    h->static_planned = false;   // and those of fdtd_step_static_scratch
     h->dirty_materials = true;  // table entry 255, node classes
     h->adj.ready = false;
     return FDTD_OK;

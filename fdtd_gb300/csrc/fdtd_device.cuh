@@ -47,8 +47,13 @@ struct MatCoef {
     float4 h[3];
 };
 
-struct MatProps {
+// Cell material of one axis: eps_r, sigma_e, mu_r, sigma_m. A component of E or H averages the
+// values of its own axis (setSigmaEpsSigmaMu, fdtdrav.h:1097-1220: Ex from the x values, ...).
+struct MatAxis {
     float eps, sig, mu, sigm;
+};
+struct MatProps {
+    MatAxis a[3];  // x, y, z
 };
 
 // One face slab of CPML memory per axis side: two E and two H psi arrays.

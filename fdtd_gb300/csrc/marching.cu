@@ -106,17 +106,18 @@ extern "C" int fdtd_marching_loop(
     fdtd_handle* h = hg.h;
     // bricks in order (setBrick, fdtdrav.h:4104-4128); material 0 is the background
     const int nb = brick_opt != 0 ? brick_num : 0;
-    std::vector<fdtd_material> mats(1 + nb);
-    mats[0] = fdtd_material{1.0f, 1.2e-38f, 1.0f, 1.2e-38f};
-    for (int b = 0; b < nb; ++b) {
-        if (brick_eps_r_y[b] != brick_eps_r_x[b] || brick_eps_r_z[b] != brick_eps_r_x[b] ||
-            brick_sigma_e_y[b] != brick_sigma_e_x[b] || brick_sigma_e_z[b] != brick_sigma_e_x[b] ||
-            brick_mu_r_y[b] != brick_mu_r_x[b] || brick_mu_r_z[b] != brick_mu_r_x[b] ||
-            brick_sigma_m_y[b] != brick_sigma_m_x[b] || brick_sigma_m_z[b] != brick_sigma_m_x[b])
-            return report_error(FDTD_ERR_INVALID, "per-axis (anisotropic) brick materials are not supported");
-        mats[1 + b] = fdtd_material{brick_eps_r_x[b], brick_sigma_e_x[b], brick_mu_r_x[b], brick_sigma_m_x[b]};
+    std::vector<fdtd_material_axes> mats(1 + nb);
+    for (int a = 0; a < 3; ++a) {
+        mats[0].eps_r[a] = 1.0f; mats[0].sigma_e[a] = 1.2e-38f; mats[0].mu_r[a] = 1.0f; mats[0].sigma_m[a] = 1.2e-38f;
     }
-    if ((rc = fdtd_set_materials(h, mats.data(), (int32_t)mats.size()))) return rc;
+    for (int b = 0; b < nb; ++b) {  // setBrick's per-axis values
+        fdtd_material_axes& m = mats[1 + b];
+        m.eps_r[0] = brick_eps_r_x[b]; m.eps_r[1] = brick_eps_r_y[b]; m.eps_r[2] = brick_eps_r_z[b];
+        m.sigma_e[0] = brick_sigma_e_x[b]; m.sigma_e[1] = brick_sigma_e_y[b]; m.sigma_e[2] = brick_sigma_e_z[b];
+        m.mu_r[0] = brick_mu_r_x[b]; m.mu_r[1] = brick_mu_r_y[b]; m.mu_r[2] = brick_mu_r_z[b];
+        m.sigma_m[0] = brick_sigma_m_x[b]; m.sigma_m[1] = brick_sigma_m_y[b]; m.sigma_m[2] = brick_sigma_m_z[b];
+    }
+    if ((rc = fdtd_set_materials_axes(h, mats.data(), (int32_t)mats.size()))) return rc;
     for (int b = 0; b < nb; ++b) {
         int32_t bx[6];
         box(brick_min_x[b], brick_min_y[b], brick_min_z[b], brick_max_x[b], brick_max_y[b], brick_max_z[b], bx);
@@ -154,4 +155,69 @@ extern "C" int fdtd_marching_loop(
     if ((rc = fdtd_step(h, n_t_steps))) return rc;
     if ((rc = fdtd_synchronize(h))) return rc;
     return fdtd_read_port(h, port, 0, n_t_steps, 1, voltage, current);
+}
+
+// ---------------------------------------------------------------------------------------------
+// marchingLoop with the reference's exact parameter list and C++ linkage (include/compat/fdtdrav.h):
+// fdtd_marching_loop, then V(t) and the averaged I(t) written as saveTDomain writes them
+// (fdtdrav.h:2704-2719): results1003.dat and results1004.dat, "%e \n" per step.
+// ---------------------------------------------------------------------------------------------
+#include <cstdio>
+
+#include "../../include/compat/fdtdrav.h"
+
+namespace {
+bool save_tdomain(const std::vector<float>& q, int fac) {
+    char name[32];
+    std::snprintf(name, sizeof(name), "results%d.dat", fac);
+    FILE* f = std::fopen(name, "w");
+    if (!f) return false;
+    for (float v : q) std::fprintf(f, "%e \n", v);
+    return std::fclose(f) == 0;
+}
+}  // namespace
+
+void marchingLoop(const int NUMDEV, float eps_0, float pi, float mu_0, float c, float dx, float dy, float dz, float dt,
+                  int X, int Y, int Z, int n_t_steps, int pml_x_n, int pml_y_n, int pml_z_n, int pml_x_p, int pml_y_p,
+                  int pml_z_p, int air_buff_x_n, int air_buff_y_n, int air_buff_z_n, int air_buff_x_p, int air_buff_y_p,
+                  int air_buff_z_p, int source_tp, float source_freq, float source_amp, float source_min_x,
+                  float source_min_y, float source_min_z, float source_max_x, float source_max_y, float source_max_z,
+                  int source_direction, float rs, float nc, float tau, float t_0, float* brick_min_x, float* brick_min_y,
+                  float* brick_min_z, float* brick_max_x, float* brick_max_y, float* brick_max_z, float* brick_sigma_e_x,
+                  float* brick_sigma_e_y, float* brick_sigma_e_z, float* brick_eps_r_x, float* brick_eps_r_y,
+                  float* brick_eps_r_z, float* brick_sigma_m_x, float* brick_sigma_m_y, float* brick_sigma_m_z,
+                  float* brick_mu_r_x, float* brick_mu_r_y, float* brick_mu_r_z, int brick_opt, int brick_num,
+                  float* pec_min_x, float* pec_min_y, float* pec_min_z, float* pec_max_x, float* pec_max_y,
+                  float* pec_max_z, float* pec_sigma_e_x, float* pec_sigma_e_y, float* pec_sigma_e_z, int pec_opt,
+                  int pec_num, float resistor_min_x, float resistor_min_y, float resistor_min_z, float resistor_max_x,
+                  float resistor_max_y, float resistor_max_z, float resistor_resist, int resistor_direction,
+                  int resistor_opt, float sampled_voltage_min_x, float sampled_voltage_min_y,
+                  float sampled_voltage_min_z, float sampled_voltage_max_x, float sampled_voltage_max_y,
+                  float sampled_voltage_max_z, int voltage_direction, float sampled_current_min_x,
+                  float sampled_current_min_y, float sampled_current_min_z, float sampled_current_max_x,
+                  float sampled_current_max_y, float sampled_current_max_z, int current_direction) {
+    if (n_t_steps < 2) {
+        std::fprintf(stderr, "marchingLoop: fewer than 2 time steps\n");
+        return;
+    }
+    std::vector<float> voltage((size_t)n_t_steps), current((size_t)n_t_steps);
+    const int rc = fdtd_marching_loop(
+        NUMDEV, eps_0, pi, mu_0, c, dx, dy, dz, dt, X, Y, Z, n_t_steps, pml_x_n, pml_y_n, pml_z_n, pml_x_p, pml_y_p,
+        pml_z_p, air_buff_x_n, air_buff_y_n, air_buff_z_n, air_buff_x_p, air_buff_y_p, air_buff_z_p, source_tp,
+        source_freq, source_amp, source_min_x, source_min_y, source_min_z, source_max_x, source_max_y, source_max_z,
+        source_direction, rs, nc, tau, t_0, brick_min_x, brick_min_y, brick_min_z, brick_max_x, brick_max_y, brick_max_z,
+        brick_sigma_e_x, brick_sigma_e_y, brick_sigma_e_z, brick_eps_r_x, brick_eps_r_y, brick_eps_r_z, brick_sigma_m_x,
+        brick_sigma_m_y, brick_sigma_m_z, brick_mu_r_x, brick_mu_r_y, brick_mu_r_z, brick_opt, brick_num, pec_min_x,
+        pec_min_y, pec_min_z, pec_max_x, pec_max_y, pec_max_z, pec_sigma_e_x, pec_sigma_e_y, pec_sigma_e_z, pec_opt,
+        pec_num, resistor_min_x, resistor_min_y, resistor_min_z, resistor_max_x, resistor_max_y, resistor_max_z,
+        resistor_resist, resistor_direction, resistor_opt, sampled_voltage_min_x, sampled_voltage_min_y,
+        sampled_voltage_min_z, sampled_voltage_max_x, sampled_voltage_max_y, sampled_voltage_max_z, voltage_direction,
+        sampled_current_min_x, sampled_current_min_y, sampled_current_min_z, sampled_current_max_x, sampled_current_max_y,
+        sampled_current_max_z, current_direction, voltage.data(), current.data());
+    if (rc != FDTD_OK) {
+        std::fprintf(stderr, "marchingLoop: fdtd_marching_loop failed (%d): %s\n", rc, fdtd_last_error());
+        return;
+    }
+    if (!save_tdomain(voltage, 1003) || !save_tdomain(current, 1004))
+        std::fprintf(stderr, "marchingLoop: cannot write results1003.dat / results1004.dat\n");
 }

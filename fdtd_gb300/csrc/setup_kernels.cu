@@ -75,21 +75,15 @@ __global__ void k_material_tables(const MatProps* props, int n, MatCoef* coef, D
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m > kMaxMaterials) return;
     MatCoef c;
-    MatProps a;
-    if (m == kDefaultEntry) {
-        a.eps = 1.0f; a.sig = kTiny; a.mu = 1.0f; a.sigm = kTiny;
-    } else if (m < n) {
-        a = props[m];
-    } else {
-        a.eps = 1.0f; a.sig = kTiny; a.mu = 1.0f; a.sigm = kTiny;
-    }
-    const float eps = avg4(a.eps, a.eps, a.eps, a.eps);
-    const float sig = avg4(a.sig, a.sig, a.sig, a.sig);
-    const float mu = m == kDefaultEntry ? 1.0f : harm2(a.mu, a.mu);
-    const float sm = m == kDefaultEntry ? kTiny : harm2(a.sigm, a.sigm);
     const float dp_e[3] = {g.dy, g.dz, g.dx}, dm_e[3] = {g.dz, g.dx, g.dy};
     const float dp_h[3] = {g.dz, g.dx, g.dy}, dm_h[3] = {g.dy, g.dz, g.dx};
-    for (int q = 0; q < 3; ++q) {
+    for (int q = 0; q < 3; ++q) {  // component q averages the values of axis q
+        MatAxis a{1.0f, kTiny, 1.0f, kTiny};
+        if (m < n && m != kDefaultEntry) a = props[m].a[q];
+        const float eps = avg4(a.eps, a.eps, a.eps, a.eps);
+        const float sig = avg4(a.sig, a.sig, a.sig, a.sig);
+        const float mu = m == kDefaultEntry ? 1.0f : harm2(a.mu, a.mu);
+        const float sm = m == kDefaultEntry ? kTiny : harm2(a.sigm, a.sigm);
         Coef3 e = coef3(eps, sig, g.dt, g.eps0, dp_e[q], dm_e[q]);
         c.e[q] = make_float4(e.a, e.bp, e.bm, 0.0f);
         Coef3 h = coef3(mu, sm, g.dt, g.mu0, dp_h[q], dm_h[q]);
@@ -123,7 +117,8 @@ __global__ void k_lumped_coefs(DeviceGrid g, const uint8_t* mat, const MatProps*
     float rfactor_aux = (r_comp * dx * dy);
     // eps_z / sigma_z of the edge: average of cells (i,j), (i-1,j), (i,j-1), (i-1,j-1) in plane k
     const long long n = (long long)L.k * g.plane + (long long)L.j * g.pitch + L.i;
-    const MatProps a = props[mat[n]], bb = props[mat[n - 1]], c = props[mat[n - g.pitch]], d = props[mat[n - 1 - g.pitch]];
+    const MatAxis a = props[mat[n]].a[2], bb = props[mat[n - 1]].a[2], c = props[mat[n - g.pitch]].a[2],
+                  d = props[mat[n - 1 - g.pitch]].a[2];
     float eps_z = avg4(a.eps, bb.eps, c.eps, d.eps);
     float sig_z = avg4(a.sig, bb.sig, c.sig, d.sig);
     float den = __fadd_rn(__fmaf_rn(2.0f * eps_z, eps_0, __fmul_rn(dt, sig_z)), rfactor);
@@ -191,6 +186,25 @@ __global__ void k_paint(uint8_t* mat, DeviceGrid g, int is, int js, int ks, int 
     const int j = js + blockIdx.y * blockDim.y + threadIdx.y;
     const int k = ks + blockIdx.z;
     if (i < ie && j < je && k < ke) mat[(long long)k * g.plane + (long long)j * g.pitch + i] = v;
+}
+
+// Largest material index of the grid's cells (row padding excluded) into *out (atomicMax; *out
+// starts at 0).
+__global__ void k_index_max(const uint8_t* __restrict__ mat, DeviceGrid g, int* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    int v = (i < g.nx && j < g.ny) ? mat[(long long)k * g.plane + (long long)j * g.pitch + i] : 0;
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0 && v > 0) atomicMax(out, v);
+}
+
+cudaError_t launch_index_max(const uint8_t* mat, const DeviceGrid& g, int* out, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(out, 0, sizeof(int), st);
+    if (e != cudaSuccess) return e;
+    const dim3 block(32, 8, 1), grid((g.nx + 31) / 32, (g.ny + 7) / 8, g.nz);
+    k_index_max<<<grid, block, 0, st>>>(mat, g, out);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_paint(uint8_t* mat, const DeviceGrid& g, const int box[6], uint8_t value, cudaStream_t st) {
@@ -273,10 +287,11 @@ namespace fdtd {
 
 // Interface rows. Every kInterfaceNode node is keyed by its seven cell materials, packed one byte
 // each in the order (i,j,k) (i-1,j,k) (i,j-1,k) (i,j,k-1) (i-1,j-1,k) (i-1,j,k-1) (i,j-1,k-1). The
-// keys are gathered, sorted and made unique on the host, and each unique key gets the coefficient
-// row the general path would build for such a node (e_coef / h_coef: table entries where an edge's
+// distinct keys are collected in a hash set on the device (open addressing, linear probing), only
+// they are sorted on the host, and each of the first kMaxInterfaceRows gets the coefficient row
+// the general path would build for such a node (e_coef / h_coef: table entries where an edge's
 // cells agree, the reference's averages otherwise), so the node's update is the table form with
-// the same bits.
+// the same bits. Nodes whose key has no row take the general path, with the same bits too.
 namespace {
 __device__ __forceinline__ unsigned long long cell_key(const uint8_t* mat, const DeviceGrid& g, long long n) {
     const long long R = g.pitch, P = g.plane;  // interior nodes: every neighbour cell exists
@@ -284,27 +299,73 @@ __device__ __forceinline__ unsigned long long cell_key(const uint8_t* mat, const
            (unsigned long long)mat[n - P] << 24 | (unsigned long long)mat[n - 1 - R] << 32 |
            (unsigned long long)mat[n - 1 - P] << 40 | (unsigned long long)mat[n - R - P] << 48;
 }
+constexpr unsigned long long kEmptyKey = ~0ull;  // keys use 56 bits
+constexpr int kMaxProbes = 64;
+__device__ __forceinline__ unsigned slot_of(unsigned long long key) {
+    return (unsigned)((key * 0x9E3779B97F4A7C15ull) >> (64 - kIfaceTableBits));
+}
+// Slot of `key` in the set, or -1.
+__device__ __forceinline__ int find_slot(const unsigned long long* __restrict__ table, unsigned long long key) {
+    unsigned s = slot_of(key);
+    for (int q = 0; q < kMaxProbes; ++q, s = (s + 1) & (kIfaceTableSize - 1)) {
+        const unsigned long long v = table[s];
+        if (v == key) return (int)s;
+        if (v == kEmptyKey) return -1;
+    }
+    return -1;
+}
 }  // namespace
 
-// Keys of the kInterfaceNode nodes into keys[atomicAdd(count)] (capacity cap; count counts all).
-__global__ void k_iface_keys(const uint8_t* __restrict__ cls, const uint8_t* __restrict__ mat, DeviceGrid g,
-                             unsigned long long* keys, unsigned long long* count, long long cap) {
+// Insert the key of every kInterfaceNode node into the set while it holds fewer than
+// kIfaceTableSize / 2 keys (*filled counts them, a few more may land while it reaches that); a key
+// that finds no room stays out (its nodes take the general path).
+__global__ void k_iface_insert(const uint8_t* __restrict__ cls, const uint8_t* __restrict__ mat, DeviceGrid g,
+                               unsigned long long* table, int* filled) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
     if (i >= g.nx || j >= g.ny) return;
     const long long n = (long long)k * g.plane + (long long)j * g.pitch + i;
     if (cls[n] != kInterfaceNode) return;
-    const unsigned long long q = atomicAdd(count, 1ull);
-    if ((long long)q < cap) keys[q] = cell_key(mat, g, n);
+    const unsigned long long key = cell_key(mat, g, n);
+    unsigned s = slot_of(key);
+    for (int q = 0; q < kMaxProbes; ++q, s = (s + 1) & (kIfaceTableSize - 1)) {
+        const unsigned long long v = *(volatile unsigned long long*)(table + s);
+        if (v == key) return;
+        if (v != kEmptyKey) continue;
+        if (*(volatile int*)filled >= kIfaceTableSize / 2) return;
+        const unsigned long long old = atomicCAS(table + s, kEmptyKey, key);
+        if (old == kEmptyKey) {
+            atomicAdd(filled, 1);
+            return;
+        }
+        if (old == key) return;
+    }
+}
+
+// The keys held in the set, in slot order, to keys[atomicAdd(count)].
+__global__ void k_iface_compact(const unsigned long long* __restrict__ table, unsigned long long* keys, int* count) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= kIfaceTableSize) return;
+    const unsigned long long v = table[s];
+    if (v != kEmptyKey) keys[atomicAdd(count, 1)] = v;
+}
+
+// slot_row[slot of sorted key q] = q for the rows kept.
+__global__ void k_iface_slot_rows(const unsigned long long* __restrict__ table, const unsigned long long* __restrict__ keys,
+                                  int n_keys, int* slot_row) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n_keys) return;
+    const int s = find_slot(table, keys[q]);
+    if (s >= 0) slot_row[s] = q;
 }
 
 // Coefficient rows of every node (StepParams::rec): the material id of fast-path nodes, the
-// interface row of kInterfaceNode nodes whose key is among the n_keys sorted unique keys, and
-// kRecGeneral | class for the rest. kInterfaceNode nodes without a row (more distinct keys than
-// kMaxInterfaceRows) become kGeneral.
+// interface row of kInterfaceNode nodes whose key has one, and kRecGeneral | class for the rest.
+// kInterfaceNode nodes without a row become kGeneral.
 __global__ void k_iface_rows(uint8_t* __restrict__ cls, const uint8_t* __restrict__ mat, DeviceGrid g,
-                             const unsigned long long* __restrict__ keys, int n_keys, uint16_t* __restrict__ rec) {
+                             const unsigned long long* __restrict__ table, const int* __restrict__ slot_row,
+                             uint16_t* __restrict__ rec) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
@@ -315,15 +376,10 @@ __global__ void k_iface_rows(uint8_t* __restrict__ cls, const uint8_t* __restric
     if (c < kUniformGeneral) {
         r = c;
     } else if (c == kInterfaceNode) {
-        const unsigned long long key = cell_key(mat, g, n);
-        int lo = 0, hi = n_keys;  // first key >= key
-        while (lo < hi) {
-            const int mid = (lo + hi) >> 1;
-            if (keys[mid] < key) lo = mid + 1;
-            else hi = mid;
-        }
-        if (lo < n_keys && keys[lo] == key) {
-            r = kFirstInterfaceRow + lo;
+        const int s = find_slot(table, cell_key(mat, g, n));
+        const int row = s >= 0 ? slot_row[s] : -1;
+        if (row >= 0) {
+            r = kFirstInterfaceRow + row;
         } else {
             cls[n] = kGeneral;
             r = kRecGeneral | kGeneral;
@@ -358,17 +414,24 @@ __global__ void k_iface_coefs(const __grid_constant__ StepParams p, const unsign
     coef[kFirstInterfaceRow + q] = c;
 }
 
-cudaError_t launch_iface_keys(const DeviceGrid& g, const uint8_t* cls, const uint8_t* mat, unsigned long long* keys,
-                              unsigned long long* count, long long cap, cudaStream_t st) {
+cudaError_t launch_iface_set(const DeviceGrid& g, const uint8_t* cls, const uint8_t* mat, unsigned long long* table,
+                             int* counters, unsigned long long* keys, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(table, 0xff, sizeof(unsigned long long) * kIfaceTableSize, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(counters, 0, 2 * sizeof(int), st);
+    if (e != cudaSuccess) return e;
     const dim3 block(32, 8, 1), grid((g.nx + 31) / 32, (g.ny + 7) / 8, g.nz);
-    k_iface_keys<<<grid, block, 0, st>>>(cls, mat, g, keys, count, cap);
+    k_iface_insert<<<grid, block, 0, st>>>(cls, mat, g, table, counters);
+    k_iface_compact<<<kIfaceTableSize / 256, 256, 0, st>>>(table, keys, counters + 1);
     return cudaGetLastError();
 }
 
-cudaError_t launch_iface_rows(const DeviceGrid& g, uint8_t* cls, const uint8_t* mat, const unsigned long long* keys,
-                              int n_keys, uint16_t* rec, cudaStream_t st) {
+cudaError_t launch_iface_rows(const DeviceGrid& g, uint8_t* cls, const uint8_t* mat, const unsigned long long* table,
+                              const unsigned long long* keys, int n_keys, int* slot_row, uint16_t* rec, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(slot_row, 0xff, sizeof(int) * kIfaceTableSize, st);
+    if (e != cudaSuccess) return e;
+    if (n_keys > 0) k_iface_slot_rows<<<(n_keys + 127) / 128, 128, 0, st>>>(table, keys, n_keys, slot_row);
     const dim3 block(32, 8, 1), grid((g.nx + 31) / 32, (g.ny + 7) / 8, g.nz);
-    k_iface_rows<<<grid, block, 0, st>>>(cls, mat, g, keys, n_keys, rec);
+    k_iface_rows<<<grid, block, 0, st>>>(cls, mat, g, table, slot_row, rec);
     return cudaGetLastError();
 }
 

@@ -41,27 +41,29 @@ __device__ __forceinline__ int psi_off_z(const DeviceGrid& g, int i, int j, int 
 // (fdtdrav.h:1135, 1153, 1170, reference summation order) and setCoefficients' expressions. Out of
 // line with scalar arguments: it runs only at material interfaces and keeps its divisions out of
 // the hot loop's instruction footprint.
-static __device__ __noinline__ Coef3 e_coef_mixed(const MatProps* props, int m0, int m1, int m2, int m3, float dt,
-                                                  float eps0, float dp, float dm) {
-    const MatProps a = props[m0], b = props[m1], c = props[m2], d = props[m3];
+// axis: the component's axis, whose cell values are averaged.
+static __device__ __noinline__ Coef3 e_coef_mixed(const MatProps* props, int axis, int m0, int m1, int m2, int m3,
+                                                  float dt, float eps0, float dp, float dm) {
+    const MatAxis a = props[m0].a[axis], b = props[m1].a[axis], c = props[m2].a[axis], d = props[m3].a[axis];
     return coef3(avg4(a.eps, b.eps, c.eps, d.eps), avg4(a.sig, b.sig, c.sig, d.sig), dt, eps0, dp, dm);
 }
 // Harmonic means of two cells for an H face (fdtdrav.h:1183-1213).
-static __device__ __noinline__ Coef3 h_coef_mixed(const MatProps* props, int m0, int m1, float dt, float mu0,
+static __device__ __noinline__ Coef3 h_coef_mixed(const MatProps* props, int axis, int m0, int m1, float dt, float mu0,
                                                   float dp, float dm) {
-    const MatProps a = props[m0], b = props[m1];
+    const MatAxis a = props[m0].a[axis], b = props[m1].a[axis];
     return coef3(harm2(a.mu, b.mu), harm2(a.sigm, b.sigm), dt, mu0, dp, dm);
 }
 // A curl coefficient divided by the CPML kappa (setABCPML, fdtdrav.h:1903-1906 and mirrors).
 static __device__ __noinline__ float kappa_div(float c, float kappa) { return __fdiv_rn(c, kappa); }
 
-// eps_r of cell (ci, cj, ck) holding material m: the design array for design cells.
-__device__ __forceinline__ float cell_eps(const StepParams& p, int m, int ci, int cj, int ck) {
+// eps_r of axis `axis` of cell (ci, cj, ck) holding material m: the design array for design
+// cells (isotropic).
+__device__ __forceinline__ float cell_eps(const StepParams& p, int m, int axis, int ci, int cj, int ck) {
     if (m == kDesign && p.deps) {
         const int* d = p.dbox;
         return p.deps[((long long)(ck - d[2]) * (d[4] - d[1]) + (cj - d[1])) * (d[3] - d[0]) + (ci - d[0])];
     }
-    return p.props[m].eps;
+    return p.props[m].a[axis].eps;
 }
 // The averaged eps_r and sigma_e of E edge `comp` at node (i, j, k) over its four cells in the
 // reference's summation order: Ex (i,j,k) (i,j-1,k) (i,j,k-1) (i,j-1,k-1); Ey (i,j,k) (i-1,j,k)
@@ -72,9 +74,9 @@ __device__ __forceinline__ void edge_material(const StepParams& p, int comp, int
     if (comp == 0) { c1j = j - 1; c3j = j - 1; }
     else if (comp == 1) { c1i = i - 1; c3i = i - 1; }
     else { c1i = i - 1; c2k = k; c2j = j - 1; c3i = i - 1; c3j = j - 1; c3k = k; }
-    eps = avg4(cell_eps(p, m0, i, j, k), cell_eps(p, m1, c1i, c1j, c1k), cell_eps(p, m2, c2i, c2j, c2k),
-               cell_eps(p, m3, c3i, c3j, c3k));
-    sig = avg4(p.props[m0].sig, p.props[m1].sig, p.props[m2].sig, p.props[m3].sig);
+    eps = avg4(cell_eps(p, m0, comp, i, j, k), cell_eps(p, m1, comp, c1i, c1j, c1k),
+               cell_eps(p, m2, comp, c2i, c2j, c2k), cell_eps(p, m3, comp, c3i, c3j, c3k));
+    sig = avg4(p.props[m0].a[comp].sig, p.props[m1].a[comp].sig, p.props[m2].a[comp].sig, p.props[m3].a[comp].sig);
 }
 // Coefficients of an E edge with a design cell among its four cells (setCoefficients on the
 // averages, fdtdrav.h:1280-1303). Out of line: design edges are a small region.
@@ -143,7 +145,7 @@ __device__ __forceinline__ Coef3 e_coef(const StepParams& p, int comp, bool uni,
     const DeviceGrid& g = p.g;
     const float dp = comp == 0 ? g.dy : comp == 1 ? g.dz : g.dx;
     const float dm = comp == 0 ? g.dz : comp == 1 ? g.dx : g.dy;
-    return e_coef_mixed(p.props, m0, m1, m2, m3, g.dt, g.eps0, dp, dm);
+    return e_coef_mixed(p.props, comp, m0, m1, m2, m3, g.dt, g.eps0, dp, dm);
 }
 
 // H-face coefficients (fdtdrav.h:1250-1272). `edge`: the low face of the axis (i = 0 for Hx, ...),
@@ -157,7 +159,7 @@ __device__ __forceinline__ Coef3 h_coef(const StepParams& p, int comp, bool edge
     const DeviceGrid& g = p.g;
     const float dp = comp == 0 ? g.dz : comp == 1 ? g.dx : g.dy;
     const float dm = comp == 0 ? g.dy : comp == 1 ? g.dz : g.dx;
-    return h_coef_mixed(p.props, m0, m1, g.dt, g.mu0, dp, dm);
+    return h_coef_mixed(p.props, comp, m0, m1, g.dt, g.mu0, dp, dm);
 }
 
 // Curl coefficient divided by the CPML kappa of its derivative axis. `bg_ok`: the coefficient is

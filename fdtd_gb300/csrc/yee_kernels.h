@@ -41,33 +41,32 @@ cudaError_t launch_plate_e(const StepParams& p, const FieldPtrs& fi, const Field
 cudaError_t launch_shell(bool e_pass, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
                          const PsiSet& pout, const int4* items, int n_items, long long m, cudaStream_t st);
 
-// Fused schedule (yee_fused.cu): per step the shell E pass, the z-marching interior sweep (TMA
-// tiles of buffer A: H with halo, old E, coefficient rows) and the shell H pass; fields A -> B, CPML
-// memory psi_in -> psi_out.
-struct FusedMaps {
+// Fused schedule (yee_fused.cu): per step the per-node E of the shell items, the z-marching
+// sweeps (TMA tiles of buffer A: H with halo, old E, coefficient rows) over interior, wide and
+// narrow items, and the per-node H of the shell items; fields A -> B, CPML memory psi_in -> psi_out.
+// The items come from plan_fused (planner.h).
+struct TileMaps {
     CUtensorMap h[3];
     CUtensorMap e[3];
     CUtensorMap rec;  // coefficient rows (StepParams::rec)
 };
-// Work items of one step (device arrays of int4): interior items {x0, y0, k0, k1} for the sweep
-// (a 32 x 16 column over planes [k0, k1)), general items {x0, y0, k, code} for the shell passes
-// (a block of up to 256 nodes of plane k: shape code & 15, columns (code >> 4) & 511, rows
-// (code >> 13) & 511) (plan_fused).
+struct FusedMaps {
+    TileMaps wide;    // 32 x 16 columns (interior and wide items)
+    TileMaps narrow;  // 16 x 32 columns (narrow items)
+};
+// Work items of one step (device arrays of int4 in the formats of planner.h).
 struct FusedWork {
     const int4* interior;
     int n_interior;
-    const int4* general;
+    const int4* wide;
+    int n_wide;
+    const int4* narrow;
+    int n_narrow;
+    const int4* general;  // shell items
     int n_general;
 };
 cudaError_t fused_configure();
 int fused_smem_bytes();
-int fused_chunk(const DeviceGrid& g);
-int fused_tile_x();
-int fused_tile_y();
-// design_box: the design region's cells (box[6]) or NULL; tiles whose nodes or E halo reach its
-// edge box go to the general items.
-void plan_fused(const DeviceGrid& g, int kc, const int* design_box, std::vector<int4>& interior_items,
-                std::vector<int4>& general_items);
 cudaError_t launch_fused(const FusedMaps& maps, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo,
                          const PsiSet& psi_in, const PsiSet& psi_out, long long m, const FusedWork& w, cudaStream_t st);
 // encode_fn: the driver's cuTensorMapEncodeTiled. Returns 0 on success.
@@ -92,15 +91,22 @@ cudaError_t launch_fill(float* p, long long n, float v, cudaStream_t st);
 cudaError_t launch_class_nodes(const DeviceGrid& g, const int4* nodes, int n, int value, uint8_t* cls, cudaStream_t st);
 cudaError_t launch_node_class(const DeviceGrid& g, const uint8_t* mat, const LumpedEdge* edges, int n_edges,
                               const int* design_box, uint8_t* cls, cudaStream_t st);
+// Largest material index of the grid's cells into *out (device int).
+cudaError_t launch_index_max(const uint8_t* mat, const DeviceGrid& g, int* out, cudaStream_t st);
 cudaError_t launch_paint(uint8_t* mat, const DeviceGrid& g, const int box[6], uint8_t value, cudaStream_t st);
-// Interface rows (setup_kernels.cu): the seven-cell keys of the kInterfaceNode nodes (at most cap
-// of them into keys, *count = all of them), then, from the sorted unique keys, the per-node
-// coefficient rows (StepParams::rec; nodes without a row become kGeneral) and the rows themselves
-// (p: the handle's parameters with the material rows in place).
-cudaError_t launch_iface_keys(const DeviceGrid& g, const uint8_t* cls, const uint8_t* mat, unsigned long long* keys,
-                              unsigned long long* count, long long cap, cudaStream_t st);
-cudaError_t launch_iface_rows(const DeviceGrid& g, uint8_t* cls, const uint8_t* mat, const unsigned long long* keys,
-                              int n_keys, uint16_t* rec, cudaStream_t st);
+// Interface rows (setup_kernels.cu). launch_iface_set collects the distinct seven-cell keys of the
+// kInterfaceNode nodes in a device hash set (table: kIfaceTableSize slots; counters: 2 ints) and
+// lists them, unsorted, in keys (kIfaceTableSize entries; counters[1] = their number).
+// launch_iface_rows, given the n_keys sorted keys that get rows, writes the per-node coefficient
+// rows (StepParams::rec; nodes without a row become kGeneral; slot_row: kIfaceTableSize ints of
+// scratch). launch_iface_coefs computes the rows themselves (p: the handle's parameters with the
+// material rows in place).
+constexpr int kIfaceTableBits = 17;
+constexpr int kIfaceTableSize = 1 << kIfaceTableBits;
+cudaError_t launch_iface_set(const DeviceGrid& g, const uint8_t* cls, const uint8_t* mat, unsigned long long* table,
+                             int* counters, unsigned long long* keys, cudaStream_t st);
+cudaError_t launch_iface_rows(const DeviceGrid& g, uint8_t* cls, const uint8_t* mat, const unsigned long long* table,
+                              const unsigned long long* keys, int n_keys, int* slot_row, uint16_t* rec, cudaStream_t st);
 cudaError_t launch_iface_coefs(const StepParams& p, const unsigned long long* keys, int n_keys, MatCoef* coef,
                                cudaStream_t st);
 

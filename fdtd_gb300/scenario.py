@@ -21,7 +21,7 @@ from __future__ import annotations
 
 import dataclasses
 import math
-from typing import List, Optional, Sequence, Tuple
+from typing import List, Optional, Sequence, Tuple, Union
 
 import numpy as np
 
@@ -62,10 +62,25 @@ def calc_index(coordinate: float, delta: float) -> int:
 
 @dataclasses.dataclass
 class Material:
-    eps_r: float = 1.0
-    sigma_e: float = float(REF_TINY)
-    mu_r: float = 1.0
-    sigma_m: float = float(REF_TINY)
+    """A brick material. Each property is one value (isotropic) or three (x, y, z): setBrick takes
+    the eps_r, sigma_e, mu_r and sigma_m of each axis separately (fdtdrav.h:1524-1531), and each
+    field component averages its own axis' values (setSigmaEpsSigmaMu, fdtdrav.h:1097-1220)."""
+    eps_r: Union[float, Sequence[float]] = 1.0
+    sigma_e: Union[float, Sequence[float]] = float(REF_TINY)
+    mu_r: Union[float, Sequence[float]] = 1.0
+    sigma_m: Union[float, Sequence[float]] = float(REF_TINY)
+
+    def axes(self) -> np.ndarray:
+        """float32 (3, 4): per axis x, y, z the values eps_r, sigma_e, mu_r, sigma_m."""
+        out = np.zeros((3, 4), dtype=np.float32)
+        for q, v in enumerate((self.eps_r, self.sigma_e, self.mu_r, self.sigma_m)):
+            out[:, q] = np.broadcast_to(np.asarray(v, dtype=np.float32), (3,))
+        return out
+
+    @property
+    def anisotropic(self) -> bool:
+        a = self.axes()
+        return not (np.array_equal(a[0], a[1]) and np.array_equal(a[0], a[2]))
 
 
 @dataclasses.dataclass
@@ -142,8 +157,17 @@ class Scenario:
         return idx
 
     def material_table(self) -> np.ndarray:
-        """float32 table (n_materials, 4): eps_r, sigma_e, mu_r, sigma_m."""
-        return np.array([[m.eps_r, m.sigma_e, m.mu_r, m.sigma_m] for m in self.materials], dtype=np.float32)
+        """float32 table (n_materials, 4): eps_r, sigma_e, mu_r, sigma_m (the x values of
+        anisotropic materials)."""
+        return np.array([m.axes()[0] for m in self.materials], dtype=np.float32).reshape(-1, 4)
+
+    def material_table_axes(self) -> np.ndarray:
+        """float32 table (n_materials, 3, 4): per axis x, y, z the values eps_r, sigma_e, mu_r, sigma_m."""
+        return np.array([m.axes() for m in self.materials], dtype=np.float32).reshape(-1, 3, 4)
+
+    @property
+    def anisotropic(self) -> bool:
+        return any(m.anisotropic for m in self.materials)
 
     def signal_per_node(self, s: int) -> np.ndarray:
         """Per-edge source signal, V(t) / (ke - ks) in float (setGauss, fdtdrav.h:1494; fdtdrav.h:3613)."""
@@ -384,14 +408,18 @@ def marching_indices(a: dict) -> dict:
 
 
 def marching_scenario(a: dict, waveform: np.ndarray) -> Tuple[Scenario, Tuple[int, ...], Tuple[int, ...]]:
-    """The scenario marchingLoop builds from ``a`` (isotropic bricks, z plates, z source and
-    resistor), with the source voltage ``waveform``; returns it with the voltage and current boxes."""
+    """The scenario marchingLoop builds from ``a`` (bricks with per-axis materials, z plates, z
+    source and resistor), with the source voltage ``waveform``; returns it with the voltage and
+    current boxes."""
     ix = marching_indices(a)
     mats = [Material()]
     bricks = []
+
+    def axes(name, q):
+        return tuple(float(a[f"brick_{name}_{c}"][q]) for c in "xyz")
     for q, b in enumerate(ix["bricks"]):
-        mats.append(Material(eps_r=float(a["brick_eps_r_x"][q]), sigma_e=float(a["brick_sigma_e_x"][q]),
-                             mu_r=float(a["brick_mu_r_x"][q]), sigma_m=float(a["brick_sigma_m_x"][q])))
+        mats.append(Material(eps_r=axes("eps_r", q), sigma_e=axes("sigma_e", q), mu_r=axes("mu_r", q),
+                             sigma_m=axes("sigma_m", q)))
         bricks.append(Brick(b, q + 1))
     sc = Scenario(name="marching", nx=ix["nx"], ny=ix["ny"], nz=ix["nz"], dx=float(a["dx"]), dy=float(a["dy"]),
                   dz=float(a["dz"]), dt=float(a["dt"]),

@@ -40,6 +40,10 @@ class Material(ctypes.Structure):
     _fields_ = [("eps_r", _f), ("sigma_e", _f), ("mu_r", _f), ("sigma_m", _f)]
 
 
+class MaterialAxes(ctypes.Structure):
+    _fields_ = [("eps_r", _f * 3), ("sigma_e", _f * 3), ("mu_r", _f * 3), ("sigma_m", _f * 3)]
+
+
 class FDTDError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"fdtd error {code}: {msg}")
@@ -55,6 +59,7 @@ SIGNATURES = {
     "fdtd_set_stream": (ctypes.c_int, [_vp, _vp]),
     "fdtd_set_schedule": (ctypes.c_int, [_vp, _i32]),
     "fdtd_set_materials": (ctypes.c_int, [_vp, ctypes.POINTER(Material), _i32]),
+    "fdtd_set_materials_axes": (ctypes.c_int, [_vp, ctypes.POINTER(MaterialAxes), _i32]),
     "fdtd_set_material_index": (ctypes.c_int, [_vp, _pu8]),
     "fdtd_add_brick": (ctypes.c_int, [_vp, _pi32, _i32]),
     "fdtd_add_lumped_source": (ctypes.c_int, [_vp, _i32, _pi32, _f, _pf, _i64, _pi32]),
@@ -182,7 +187,20 @@ class Simulation:
         _check(_lib.fdtd_set_schedule(self._h, schedule))
 
     def set_materials(self, table: np.ndarray) -> None:
-        t = np.asarray(table, dtype=np.float32).reshape(-1, 4)
+        """Material table (n, 4): eps_r, sigma_e, mu_r, sigma_m; or (n, 3, 4) with those values per
+        axis x, y, z (fdtd_set_materials_axes)."""
+        t = np.asarray(table, dtype=np.float32)
+        if t.ndim == 3:
+            rows = []
+            for m in t:
+                r = MaterialAxes()
+                for q, name in enumerate(("eps_r", "sigma_e", "mu_r", "sigma_m")):
+                    getattr(r, name)[:] = [float(v) for v in m[:, q]]
+                rows.append(r)
+            arr = (MaterialAxes * len(rows))(*rows)
+            _check(_lib.fdtd_set_materials_axes(self._h, arr, len(rows)))
+            return
+        t = t.reshape(-1, 4)
         arr = (Material * len(t))(*[Material(*row) for row in t.tolist()])
         _check(_lib.fdtd_set_materials(self._h, arr, len(t)))
 
@@ -358,7 +376,7 @@ class Simulation:
                       probe_capacity: Optional[int] = None) -> "Simulation":
         """Build a simulation from a scenario in the reference's setup order (fdtdrav.h:4104-4310)."""
         sim = cls(sc.nx, sc.ny, sc.nz, sc.dx, sc.dy, sc.dz, sc.dt, sc.pml, sc.eps0, sc.mu0, sc.pi, schedule)
-        sim.set_materials(sc.material_table())
+        sim.set_materials(sc.material_table_axes() if sc.anisotropic else sc.material_table())
         if material_index is not None:
             sim.set_material_index(material_index)
         else:

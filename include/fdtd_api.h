@@ -61,6 +61,14 @@ typedef struct {
     float eps_r, sigma_e, mu_r, sigma_m;
 } fdtd_material;
 
+/* One material with separate values per axis (index 0 x, 1 y, 2 z): setBrick's brick_eps_r_x/y/z,
+ * brick_sigma_e_x/y/z, brick_mu_r_x/y/z and brick_sigma_m_x/y/z (fdtdrav.h:1524-1531). A field
+ * component averages the values of its own axis: Ex the x values of its four cells, Hx the x
+ * values of its two cells, and so on (setSigmaEpsSigmaMu, fdtdrav.h:1097-1220). */
+typedef struct {
+    float eps_r[3], sigma_e[3], mu_r[3], sigma_m[3];
+} fdtd_material_axes;
+
 const char* fdtd_last_error(void);
 const char* fdtd_version(void);
 
@@ -84,8 +92,13 @@ int fdtd_tune_schedule(fdtd_handle* h);
 /* Material table (at most 256 entries). Replaces the per-brick material scalars that setBrick
  * paints into 12 per-cell arrays (fdtdrav.h:1524-1571). */
 int fdtd_set_materials(fdtd_handle* h, const fdtd_material* table, int32_t n);
-/* Per-cell material index, host array of nz*ny*nx bytes. Replaces the painted per-cell
- * material arrays; edge averaging (setSigmaEpsSigmaMu, fdtdrav.h:1097-1220) is done on the fly. */
+/* The same with per-axis (anisotropic) materials, replacing the per-axis scalars of setBrick
+ * (fdtdrav.h:1524-1571). */
+int fdtd_set_materials_axes(fdtd_handle* h, const fdtd_material_axes* table, int32_t n);
+/* Per-cell material index, host array of nz*ny*nx bytes (pinned memory copies fastest). Replaces
+ * the painted per-cell material arrays; edge averaging (setSigmaEpsSigmaMu, fdtdrav.h:1097-1220)
+ * is done on the fly. The indices are checked on the device after the copy: an index outside the
+ * material table gives FDTD_ERR_INVALID and leaves every cell at material 0. */
 int fdtd_set_material_index(fdtd_handle* h, const uint8_t* cells);
 /* Paint cells [is,ie) x [js,je) x [ks,ke) with a material, last call wins (setBrick,
  * fdtdrav.h:1524-1571, called in order at fdtdrav.h:4104-4128). box = {is,js,ks,ie,je,ke}. */
@@ -212,8 +225,8 @@ int fdtd_source_waveform(int32_t type, float amp, float freq, float dt, float t_
  * current (n_t_steps floats each) that receive V(t) and the time-averaged I(t) which the reference
  * computes in calcVoltCurrent and writes to its result files. Geometry in metres is converted to
  * node indices as the reference does (calc_index, offsets of CPML and air buffer, NZ rounded up to
- * a multiple of NUMDEV); the whole domain then runs on the current device. Bricks (isotropic:
- * equal x / y / z values), z plates (pec_*), the z-directed lumped source with its waveform
+ * a multiple of NUMDEV); the whole domain then runs on the current device. Bricks (with their
+ * per-axis values, fdtd_set_materials_axes), z plates (pec_*), the z-directed lumped source with its waveform
  * (source_tp 1 Gaussian, 3 sine, 2 none), the resistor (z edges, as defineResistor) and the port
  * (voltage direction 3, current direction 1 / 2 / 3). c and nc are unused, as in the reference. */
 int fdtd_marching_loop(
@@ -298,8 +311,7 @@ int fdtd_batch_synchronize(fdtd_batch* b);
  * the sweep's work list. Enough for a 64^3 grid with 10-cell CPML on all faces (about 9.8 MiB). */
 #define FDTD_STEP_STATIC_SCRATCH_BYTES (16u << 20)
 
-/* No reference counterpart (the reference allocates all of its arrays in marchingLoop before the
- * loop and has no fused schedule). Advances n steps with the fused sweep like fdtd_step under
+/* No reference counterpart. Advances n steps with the fused sweep like fdtd_step under
  * FDTD_SCHEDULE_FUSED, with bit-identical fields, CPML memory and probe samples. This call
  * allocates no device memory. fdtd_step allocates a second field set and CPML set (plus the
  * sweep's work list) the first time it runs the fused sweep. The ping-pong target here is instead
@@ -315,11 +327,14 @@ int fdtd_batch_synchronize(fdtd_batch* b);
  *  - The first call on each device looks up the array's address (cudaGetSymbolAddress) and sets
  *    the sweep kernels' shared-memory limit; these are not stream operations. A call with n = 0
  *    does only this set-up; make it once per device before a section that must issue nothing
- *    but stream work.
- *  - Nothing in the scratch needs to start at zero or to survive between calls: each call first
- *    copies the handle's CPML memory into it, every scratch element a step reads was written
- *    earlier in the same call, and the result is back in the handle's own buffers when the call's
- *    stream work completes.
+ *    but stream work. The address is kept for the life of the process: after a cudaDeviceReset
+ *    it is stale, so do not use this call across a device reset.
+ *  - Each call uploads the sweep's work list (planned once per handle into pinned host memory)
+ *    into the scratch with one asynchronous host-to-device copy on the handle's stream.
+ *  - Nothing in the scratch needs to start at zero or to survive between calls: with an odd n the
+ *    call first copies the handle's CPML memory into it, every scratch element a step reads was
+ *    written earlier in the same call, and the result is back in the handle's own buffers when
+ *    the call's stream work completes.
  *  - The scratch is one per device and per process. Calls whose stream work overlaps on the device
  *    (other handles, other streams, other threads) race on it and corrupt each other's results;
  *    order them (one stream, or events), as with any shared buffer. */

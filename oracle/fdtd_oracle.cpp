@@ -20,6 +20,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <chrono>
 #include <cstring>
 #include <array>
 #include <vector>
@@ -54,7 +55,7 @@ typedef struct {
     int pml[6];  // x_n, x_p, y_n, y_p, z_n, z_p
     float dx, dy, dz, dt, eps0, mu0, pi;
     const uint8_t* mat;       // (nz, ny, nx)
-    const float* table;       // (n_mat, 4): eps_r, sigma_e, mu_r, sigma_m
+    const float* table;       // (n_mat, 3, 4): per axis x, y, z: eps_r, sigma_e, mu_r, sigma_m
     int n_mat;
     int nsrc; const int* src_box; const float* src_r;  // box is,js,ks,ie,je,ke
     int nres; const int* res_box; const float* res_r;
@@ -160,18 +161,24 @@ int setup(Sim<R>& s, const or_scenario* sc, const float* signal_per_node, int n_
     VEC_LIST(ALLOC)
 #undef ALLOC
     const int NX = s.NX, NY = s.NY, NZ = s.NZ;
-    // per-cell material (setBrick) and edge averages (setSigmaEpsSigmaMu), init 1 / 1.2e-38
-    std::vector<R> ceps(N), csig(N), cmu(N), csm(N);
-    for (size_t n = 0; n < N; ++n) {
-        const float* t = sc->table + 4 * sc->mat[n];
-        ceps[n] = t[0]; csig[n] = t[1]; cmu[n] = t[2]; csm[n] = t[3];
+    // per-cell material of each axis (setBrick, fdtdrav.h:1524-1571) and the edge averages of each
+    // component over its own axis' values (setSigmaEpsSigmaMu, fdtdrav.h:1097-1220), init 1 / 1.2e-38
+    std::vector<R> ceps[3], csig[3], cmu[3], csm[3];
+    for (int a = 0; a < 3; ++a) {
+        ceps[a].resize(N); csig[a].resize(N); cmu[a].resize(N); csm[a].resize(N);
+        for (size_t n = 0; n < N; ++n) {
+            const float* t = sc->table + 12 * sc->mat[n] + 4 * a;
+            ceps[a][n] = t[0]; csig[a][n] = t[1]; cmu[a][n] = t[2]; csm[a][n] = t[3];
+        }
     }
     if (sc->design_eps) {
         const int* d = sc->design_box;
         for (int k = d[2]; k < d[5]; ++k)
             for (int j = d[1]; j < d[4]; ++j)
                 for (int i = d[0]; i < d[3]; ++i)
-                    ceps[s.id(i, j, k)] = (R)sc->design_eps[((size_t)(k - d[2]) * (d[4] - d[1]) + (j - d[1])) * (d[3] - d[0]) + (i - d[0])];
+                    for (int a = 0; a < 3; ++a)
+                        ceps[a][s.id(i, j, k)] =
+                            (R)sc->design_eps[((size_t)(k - d[2]) * (d[4] - d[1]) + (j - d[1])) * (d[3] - d[0]) + (i - d[0])];
     }
     s.eps_x.assign(N, 1); s.eps_y.assign(N, 1); s.eps_z.assign(N, 1);
     s.mu_x.assign(N, 1); s.mu_y.assign(N, 1); s.mu_z.assign(N, 1);
@@ -184,23 +191,26 @@ int setup(Sim<R>& s, const or_scenario* sc, const float* signal_per_node, int n_
             for (int i = 0; i < NX; ++i) {
                 size_t n = s.id(i, j, k);
                 if (j > 0 && k > 0) {
+                    const std::vector<R>&e = ceps[0], &g = csig[0];
                     size_t a = n, b = s.id(i, j - 1, k), c = s.id(i, j, k - 1), d = s.id(i, j - 1, k - 1);
-                    s.eps_x[n] = avg4(ceps[a], ceps[b], ceps[c], ceps[d]);
-                    s.sig_x[n] = avg4(csig[a], csig[b], csig[c], csig[d]);
+                    s.eps_x[n] = avg4(e[a], e[b], e[c], e[d]);
+                    s.sig_x[n] = avg4(g[a], g[b], g[c], g[d]);
                 }
                 if (i > 0 && k > 0) {
+                    const std::vector<R>&e = ceps[1], &g = csig[1];
                     size_t a = n, b = s.id(i - 1, j, k), c = s.id(i, j, k - 1), d = s.id(i - 1, j, k - 1);
-                    s.eps_y[n] = avg4(ceps[a], ceps[b], ceps[c], ceps[d]);
-                    s.sig_y[n] = avg4(csig[a], csig[b], csig[c], csig[d]);
+                    s.eps_y[n] = avg4(e[a], e[b], e[c], e[d]);
+                    s.sig_y[n] = avg4(g[a], g[b], g[c], g[d]);
                 }
                 if (i > 0 && j > 0) {
+                    const std::vector<R>&e = ceps[2], &g = csig[2];
                     size_t a = n, b = s.id(i - 1, j, k), c = s.id(i, j - 1, k), d = s.id(i - 1, j - 1, k);
-                    s.eps_z[n] = avg4(ceps[a], ceps[b], ceps[c], ceps[d]);
-                    s.sig_z[n] = avg4(csig[a], csig[b], csig[c], csig[d]);
+                    s.eps_z[n] = avg4(e[a], e[b], e[c], e[d]);
+                    s.sig_z[n] = avg4(g[a], g[b], g[c], g[d]);
                 }
-                if (i > 0) { size_t b = s.id(i - 1, j, k); s.mu_x[n] = harm(cmu[n], cmu[b]); s.sm_x[n] = harm(csm[n], csm[b]); }
-                if (j > 0) { size_t b = s.id(i, j - 1, k); s.mu_y[n] = harm(cmu[n], cmu[b]); s.sm_y[n] = harm(csm[n], csm[b]); }
-                if (k > 0) { size_t b = s.id(i, j, k - 1); s.mu_z[n] = harm(cmu[n], cmu[b]); s.sm_z[n] = harm(csm[n], csm[b]); }
+                if (i > 0) { size_t b = s.id(i - 1, j, k); s.mu_x[n] = harm(cmu[0][n], cmu[0][b]); s.sm_x[n] = harm(csm[0][n], csm[0][b]); }
+                if (j > 0) { size_t b = s.id(i, j - 1, k); s.mu_y[n] = harm(cmu[1][n], cmu[1][b]); s.sm_y[n] = harm(csm[1][n], csm[1][b]); }
+                if (k > 0) { size_t b = s.id(i, j, k - 1); s.mu_z[n] = harm(cmu[2][n], cmu[2][b]); s.sm_z[n] = harm(csm[2][n], csm[2][b]); }
             }
     // definePlateX / Y / Z (fdtdrav.h:1574-1679, applied between the averages and setCoefficients,
     // fdtdrav.h:4162-4182): each plate sets sigma_e of the edges its kernel's conditions select
@@ -452,6 +462,9 @@ std::vector<R>* psi_arr(Sim<R>& s, int q) {
     return a[q];
 }
 
+// Wall time of the time loop of the last run() (setup and copies excluded), for the CPU baseline.
+double g_last_step_seconds = 0.0;
+
 template <class R>
 int run(const or_scenario* sc, int steps, const float* signal_per_node, int n_sig,
         const float* init_fields, R* probes_out, R* fields_out, int nthreads, int onestep_m,
@@ -477,11 +490,13 @@ int run(const or_scenario* sc, int steps, const float* signal_per_node, int n_si
         if (psi_out) for (int q = 0; q < 12; ++q) std::memcpy(psi_out + (size_t)q * s.N, psi_arr(s, q)->data(), s.N * sizeof(R));
         return 0;
     }
+    const auto t0 = std::chrono::steady_clock::now();
     for (int m = 0; m < steps; ++m) {
         calc_e<R>(s, m, row.data());
         calc_h<R>(s, row.data());
         if (probes_out) for (size_t p = 0; p < np; ++p) probes_out[(size_t)m * np + p] = row[p];
     }
+    g_last_step_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (fields_out)
         for (int c = 0; c < 6; ++c) std::memcpy(fields_out + (size_t)c * s.N, field(s, c)->data(), s.N * sizeof(R));
     return 0;
@@ -699,6 +714,9 @@ int or_fom_grad_f32(const or_scenario* sc, int steps, const float* sig, int n_si
                     double* J, double* grad) {
     return fom_and_grad<float>(sc, steps, sig, n_sig, pi, pj, pk, J, grad);
 }
+
+// Seconds the time loop of the last or_run_f32 / or_run_f64 took (setup excluded).
+double or_last_step_seconds(void) { return g_last_step_seconds; }
 
 // Full run: probes_out (steps, nprobe), fields_out (6, nz, ny, nx). signal_per_node (nsrc, n_sig).
 int or_run_f32(const or_scenario* sc, int steps, const float* sig, int n_sig, const float* init_fields,

@@ -67,6 +67,8 @@ def lib():
         L.or_onestep_f32.argtypes = [ctypes.POINTER(_Scenario), _i, _pf, _i, _pf, _pf, _pf, _pf]
         L.or_coef_f32.argtypes = [ctypes.POINTER(_Scenario), ctypes.c_char_p, _pf]
         L.or_port_vi.argtypes = [_pf, _i, _i, _i, _pi, _pi, _i, _f, _f, _f, _i, _pf, _pf]
+        L.or_last_step_seconds.restype = ctypes.c_double
+        L.or_last_step_seconds.argtypes = []
         for fn in (L.or_fom_grad_f64, L.or_fom_grad_f32):
             fn.argtypes = [ctypes.POINTER(_Scenario), _i, _pf, _i, _i, _i, _i, _pd, _pd]
         _lib = L
@@ -91,7 +93,7 @@ class _Prepared:
         s.dx, s.dy, s.dz, s.dt = sc.dx, sc.dy, sc.dz, sc.dt
         s.eps0, s.mu0, s.pi = sc.eps0, sc.mu0, sc.pi
         mat = np.ascontiguousarray(sc.material_index())
-        tab = np.ascontiguousarray(sc.material_table())
+        tab = np.ascontiguousarray(sc.material_table_axes())
         sb = np.array([x.box for x in sc.sources], dtype=np.int32).reshape(-1, 6)
         sr = np.array([x.resistance for x in sc.sources], dtype=np.float32)
         rb = np.array([x.box for x in sc.resistors], dtype=np.int32).reshape(-1, 6)
@@ -153,6 +155,11 @@ def run(sc, steps: Optional[int] = None, precision: str = "f32", init_fields: Op
     if rc != 0:
         raise RuntimeError("oracle: " + L.or_error().decode())
     return pout[:, :p.n_probes], fout
+
+
+def last_step_seconds() -> float:
+    """Wall time of the time loop of the last ``run`` (setup and copies excluded)."""
+    return float(lib().or_last_step_seconds())
 
 
 # Order of the 12 psi arrays in onestep's init_psi / psi output.

@@ -150,7 +150,8 @@ typedef struct {
     int nxx, nyy, nz;
     int pml[6];  // x_n, x_p, y_n, y_p, z_n, z_p
     float dx, dy, dz, dt, eps0, pi, mu0;
-    int nbricks; const int* brick_box; const float* brick_mat;  // box is,js,ks,ie,je,ke; eps_r, sigma_e, mu_r, sigma_m
+    // box is,js,ks,ie,je,ke; material (nbricks, 3, 4): per axis x, y, z eps_r, sigma_e, mu_r, sigma_m
+    int nbricks; const int* brick_box; const float* brick_mat;
     int nsources; const int* src_box; const float* src_r;       // box is,js,ks,ie,je,ke
     int nres; const int* res_box; const float* res_r;
     int nplates; const int* plate; const float* plate_sig;  // (n, 7): axis, box; (n, 2): sigma_e pair
@@ -256,17 +257,20 @@ int rh_setup(const rh_scenario* s) {
     // setBrick per box (fdtdrav.h:1524, called at 4104-4128)
     for (int b = 0; b < s->nbricks; ++b) {
         const int* bx = s->brick_box + 6 * b;
-        const float* bm = s->brick_mat + 4 * b;
+        const float* bm = s->brick_mat + 12 * b;
         int is = bx[0], js = bx[1], ks = bx[2], ie = bx[3], je = bx[4], ke = bx[5];
-        float se = bm[1], ep = bm[0], sm = bm[3], mu = bm[2];
+        // setBrick's value order: sigma_e, eps_r, sigma_m, mu_r, each x, y, z
+        static float v[12];
+        for (int a = 0; a < 3; ++a) {
+            v[a] = bm[4 * a + 1]; v[3 + a] = bm[4 * a]; v[6 + a] = bm[4 * a + 3]; v[9 + a] = bm[4 * a + 2];
+        }
         static float* P[12];
         const char* order[] = {"mat_eps_x", "mat_eps_y", "mat_eps_z", "mat_sigma_e_x", "mat_sigma_e_y", "mat_sigma_e_z",
                                "mat_mu_x", "mat_mu_y", "mat_mu_z", "mat_sigma_m_x", "mat_sigma_m_y", "mat_sigma_m_z"};
         std::vector<void*> a = {&NX, &NY, &NZ, &NZ_N, &off};
         for (int q = 0; q < 12; ++q) { P[q] = A(order[q]); a.push_back(&P[q]); }
         a.push_back(&is); a.push_back(&js); a.push_back(&ks); a.push_back(&ie); a.push_back(&je); a.push_back(&ke);
-        a.push_back(&se); a.push_back(&se); a.push_back(&se); a.push_back(&ep); a.push_back(&ep); a.push_back(&ep);
-        a.push_back(&sm); a.push_back(&sm); a.push_back(&sm); a.push_back(&mu); a.push_back(&mu); a.push_back(&mu);
+        for (int q = 0; q < 12; ++q) a.push_back(&v[q]);
         if (!launch(K_SETBRICK, grid3d(), block3d(), a)) { free_all(); return -1; }
     }
     // setSigmaEpsSigmaMu (fdtdrav.h:1097, called at 4133-4150)

@@ -73,9 +73,9 @@ class RefHarness:
             s.pml[q] = sc.pml[q]
         s.dx, s.dy, s.dz, s.dt = sc.dx, sc.dy, sc.dz, sc.dt
         s.eps0, s.pi, s.mu0 = sc.eps0, sc.pi, sc.mu0
-        tab = sc.material_table()
+        tab = sc.material_table_axes()
         bb = np.array([b.box for b in sc.bricks], dtype=np.int32).reshape(-1, 6)
-        bm = np.array([tab[b.material] for b in sc.bricks], dtype=np.float32).reshape(-1, 4)
+        bm = np.array([tab[b.material] for b in sc.bricks], dtype=np.float32).reshape(-1, 12)
         sb = np.array([x.box for x in sc.sources], dtype=np.int32).reshape(-1, 6)
         sr = np.array([x.resistance for x in sc.sources], dtype=np.float32)
         rb = np.array([x.box for x in sc.resistors], dtype=np.int32).reshape(-1, 6)

@@ -69,6 +69,24 @@ def two_sources():
     return sc
 
 
+def aniso_scenario():
+    """32x30x26 grid with per-axis (anisotropic) bricks as setBrick takes them (separate x / y / z
+    eps_r, sigma_e, mu_r and sigma_m), overlapping so that edges average different axes' values,
+    one reaching into the CPML; one source, one resistor, 300 steps."""
+    sc = S.scaled_boxes(32, 30, 26, 300, seed=13, pml=5, n_boxes=0, n_sources=1, n_probes=8, name="aniso")
+    sc.pml = (5, 6, 4, 5, 6, 4)
+    sc.materials += [
+        S.Material(eps_r=(2.0, 5.0, 9.0), sigma_e=(0.01, 0.0, 0.03)),
+        S.Material(eps_r=(4.0, 4.0, 1.5), sigma_e=0.02, mu_r=(1.0, 2.5, 1.5), sigma_m=(1e3, 4e3, 2e4)),
+        S.Material(eps_r=(7.0, 3.0, 3.0), sigma_e=(0.0, 0.05, 0.0)),
+    ]
+    sc.bricks = [S.Brick((7, 6, 6, 20, 18, 14), 1), S.Brick((14, 12, 9, 26, 24, 19), 2),
+                 S.Brick((0, 3, 3, 11, 12, 10), 3)]
+    s = sc.sources[0].box
+    sc.resistors = [S.Resistor((s[0] + 2, s[1] + 1, s[2], s[0] + 2, s[1] + 1, s[5]), 60.0)]
+    return sc
+
+
 def onestep_scenario():
     """24x20x18 random boxes with a magnetic box, 4-cell CPML, one source: single-step checks."""
     sc = S.scaled_boxes(24, 20, 18, 16, seed=5, pml=4, n_boxes=6, n_sources=1, n_probes=2,
@@ -117,11 +135,12 @@ def plates_scenario():
     return sc
 
 
-def marching_params(n_t_steps=500, current_direction=2, numdev=1, source_tp=1, resistor_opt=0):
+def marching_params(n_t_steps=500, current_direction=2, numdev=1, source_tp=1, resistor_opt=0, aniso=False):
     """marchingLoop's parameters for a reduced version of the reference driver's microstrip case
     (substrate brick on a ground plate, a feed strip and a wider patch plate, a Gaussian source at
     the feed, voltage and current sampled on the feed line): its cell sizes and constants,
-    a 40 x 60 x 6-cell structure, 6-cell CPML, 4-cell air buffers."""
+    a 40 x 60 x 6-cell structure, 6-cell CPML, 4-cell air buffers. aniso: the substrate takes
+    different eps_r, sigma_e, mu_r and sigma_m per axis."""
     import numpy as np
     f = np.float32
     eps_0 = f(8.854187817e-12)
@@ -159,6 +178,10 @@ def marching_params(n_t_steps=500, current_direction=2, numdev=1, source_tp=1, r
              current_direction=current_direction)
     if current_direction == 3:  # a z loop needs ks < ke: around the feed's vertical edges
         a.update(sampled_current_min_z=f(0), sampled_current_max_z=f(3) * dz)
+    if aniso:
+        a.update(brick_eps_r_x=[2.2], brick_eps_r_y=[3.4], brick_eps_r_z=[6.1], brick_sigma_e_x=[4e-4],
+                 brick_sigma_e_y=[1e-3], brick_sigma_e_z=[0.0], brick_mu_r_x=[1.0], brick_mu_r_y=[1.7],
+                 brick_mu_r_z=[1.2], brick_sigma_m_x=[1.2e-38], brick_sigma_m_y=[5e2], brick_sigma_m_z=[1e3])
     return a
 
 
@@ -171,4 +194,4 @@ PORT_CURRENT_BOX = (13, 12, 8, 16, 15, 11)
 def fixture_scenarios():
     """(scenario, keep full fields?) for every run fixture."""
     return [(vacuum64(), False), (small_vacuum(), True), (boxes_scenario(), True), (two_sources(), True),
-            (plates_scenario(), True)]
+            (plates_scenario(), True), (aniso_scenario(), True)]

@@ -7,7 +7,8 @@ Writes one compressed .npz per scenario: the probe series of every step and, for
 the six final fields; plus ``onestep.npz`` (one calc_e and one calc_h applied to a seeded random
 state) and ``coefs.npz`` (the reference's per-edge coefficients and 1-D CPML profiles for the
 random-box scenario); ``port.npz`` (the reference's own port sampling and time-series kernels,
-voltMgpu / currMgpu / correcI, on the port scenario, plus c_zinS11 on seeded spectra). The
+voltMgpu / currMgpu / correcI, on the port scenario, plus c_zinS11 on seeded spectra);
+``aniso.npz`` (per-axis bricks: the run and the reference's per-edge coefficient arrays). The
 scenarios are defined in golden_scenarios.py so the tests rebuild them
 bit-for-bit without running this script.
 """
@@ -195,7 +196,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
     ap.add_argument("--analysis", default=None, help="also write large analysis-only dumps here")
-    ap.add_argument("--only", default=None, choices=["port", "plates", "marching"], help="write one fixture only")
+    ap.add_argument("--only", default=None, choices=["port", "plates", "marching", "aniso"], help="write one fixture only")
     args = ap.parse_args()
     os.makedirs(args.out, exist_ok=True)
     if args.only == "port":
@@ -205,6 +206,13 @@ def main():
     if args.only == "marching":
         np.savez_compressed(os.path.join(args.out, "marching.npz"), **marching_fixture())
         print("marching fixture written to", args.out)
+        return
+    if args.only == "aniso":
+        sc = gs.aniso_scenario()
+        out = run_scenario(sc, True)
+        out.update({"coef_" + k: v for k, v in coef_dump(sc).items() if not k.startswith("cpml_")})
+        np.savez_compressed(os.path.join(args.out, "aniso.npz"), **out)
+        print("aniso fixture written to", args.out)
         return
     if args.only == "plates":
         np.savez_compressed(os.path.join(args.out, "plates.npz"), **run_scenario(gs.plates_scenario(), True))

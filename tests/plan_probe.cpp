@@ -1,0 +1,23 @@
+// C entry point over the fused schedule's work planner (fdtd_gb300/csrc/planner.cpp) for the CPU
+// tests: compiled with the planner into a small host-only library by tests/test_planner.py.
+#include <cstring>
+#include <vector>
+
+#include "planner.h"
+
+extern "C" int plan_probe(const int* grid9, const int* design_box, int* counts4, int* items, long long cap) {
+    const fdtd::PlanGrid g{grid9[0], grid9[1], grid9[2], grid9[3], grid9[4], grid9[5], grid9[6], grid9[7], grid9[8]};
+    fdtd::FusedPlan plan;
+    const int kc = fdtd::plan_chunk(g);
+    fdtd::plan_fused(g, kc, design_box, plan);
+    const std::vector<fdtd::PlanItem>* lists[4] = {&plan.interior, &plan.wide, &plan.narrow, &plan.shell};
+    long long n = 0;
+    for (int q = 0; q < 4; ++q) {
+        counts4[q] = (int)lists[q]->size();
+        for (const fdtd::PlanItem& it : *lists[q]) {
+            if (items && n < cap) std::memcpy(items + 4 * n, &it, sizeof(it));
+            ++n;
+        }
+    }
+    return kc;
+}

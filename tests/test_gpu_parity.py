@@ -34,7 +34,7 @@ def scenarios():
 
 
 @pytest.mark.parametrize("schedule", SCHEDULES)
-@pytest.mark.parametrize("name", ["small_vacuum", "small_boxes", "vacuum64", "plates"])
+@pytest.mark.parametrize("name", ["small_vacuum", "small_boxes", "vacuum64", "plates", "aniso"])
 def test_matches_reference_kernels_bitwise(gpu_lib, name, schedule):
     """Single-source scenarios: probe series and final fields equal the reference's bit for bit."""
     sc, full = scenarios()[name]

@@ -78,7 +78,7 @@ def test_full_runs(name):
             assert rel_l2_group(fields, ref, c) < REL_L2_TOL, n
 
 
-@pytest.mark.parametrize("name", ["small_vacuum", "small_boxes", "plates"])
+@pytest.mark.parametrize("name", ["small_vacuum", "small_boxes", "plates", "aniso"])
 def test_full_runs_bitwise_with_reference_profiles(name):
     """With the reference's own 1-D CPML b / a profiles (CUDA expf), single-source runs are
     bit-exact: probes of every step and the final fields. The CPML stretching kappa is still the
@@ -127,3 +127,17 @@ def test_onestep_random_psi_bitwise():
         assert bitwise_equal(out[c], fix[key]), key
     for q, n in enumerate(oracle.PSI_NAMES):
         assert bitwise_equal(psi[q], fix[n + "_after"]), n
+
+
+def test_aniso_coefficients_bitwise():
+    """Per-axis bricks: every per-edge array of setSigmaEpsSigmaMu / setCoefficients / setABCPML /
+    defineSourceZ equals the reference's (each component averages its own axis' values)."""
+    if not os.path.exists(os.path.join(GOLDEN, "aniso.npz")):
+        pytest.skip("fixture not generated")
+    sc = gs.aniso_scenario()
+    fix = golden("aniso")
+    names = [n[5:] for n in fix.files if n.startswith("coef_")]
+    assert "eps_r_y" in names and "mu_r_z" in names
+    for name in names:
+        o = oracle.coef(sc, COEF_MAP.get(name, name))
+        assert bitwise_equal(o, fix["coef_" + name]), name
