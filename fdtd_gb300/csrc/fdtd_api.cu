@@ -171,7 +171,7 @@ struct fdtd_handle {
     // on first use; each call uploads it into the scratch with one asynchronous copy
     int4* static_items = nullptr;
     size_t static_n_items = 0;
-    int static_counts[4] = {};     // items per list (interior, wide, narrow, shell)
+    int static_counts[4] = {};     // items per list (interior, then the three shell lists)
     bool static_planned = false;
 
     std::vector<size_t> alloc_sizes;  // bytes of each entry of allocs
@@ -306,11 +306,13 @@ PlanGrid plan_grid(const DeviceGrid& g) {
     return PlanGrid{g.nx, g.ny, g.nz, g.pxn, g.pxp, g.pyn, g.pyp, g.pzn, g.pzp};
 }
 
-// The lists of a plan one after the other (interior, wide, narrow, shell) and their counts.
-std::vector<PlanItem> flatten(const FusedPlan& plan, int counts[4]) {
+// The lists of a plan one after the other (interior, then the shell lists) and their counts.
+constexpr int kWorkLists = 1 + kPlanShellLists;
+static_assert(kWorkLists == 4, "fdtd_handle::static_counts holds one count per work list");
+std::vector<PlanItem> flatten(const FusedPlan& plan, int counts[kWorkLists]) {
     std::vector<PlanItem> all;
-    const std::vector<PlanItem>* lists[4] = {&plan.interior, &plan.wide, &plan.narrow, &plan.shell};
-    for (int q = 0; q < 4; ++q) {
+    const std::vector<PlanItem>* lists[kWorkLists] = {&plan.interior, &plan.shell[0], &plan.shell[1], &plan.shell[2]};
+    for (int q = 0; q < kWorkLists; ++q) {
         counts[q] = (int)lists[q]->size();
         all.insert(all.end(), lists[q]->begin(), lists[q]->end());
     }
@@ -318,9 +320,20 @@ std::vector<PlanItem> flatten(const FusedPlan& plan, int counts[4]) {
 }
 
 // The work lists over a device copy of the flattened plan.
-FusedWork work_of(const int4* d, const int counts[4]) {
-    return FusedWork{d, counts[0], d + counts[0], counts[1], d + counts[0] + counts[1], counts[2],
-                     d + counts[0] + counts[1] + counts[2], counts[3]};
+FusedWork work_of(const int4* d, const int counts[kWorkLists]) {
+    static_assert(kShellLists == kPlanShellLists && kShellZ == kPlanShellZ && kShellYZ == kPlanShellYZ &&
+                      kShellAny == kPlanShellAny,
+                  "planner and shell kernels agree on the shell lists");
+    FusedWork w{};
+    w.interior = d;
+    w.n_interior = counts[0];
+    const int4* at = d + counts[0];
+    for (int q = 0; q < kShellLists; ++q) {
+        w.shell.items[q] = at;
+        w.shell.n[q] = counts[1 + q];
+        at += counts[1 + q];
+    }
+    return w;
 }
 
 // Work items of the fused schedule (planner.cpp). The design region, if any, stays with the shell;
@@ -328,7 +341,7 @@ FusedWork work_of(const int4* d, const int counts[4]) {
 int plan_work(fdtd_handle* h) {
     FusedPlan plan;
     plan_fused(plan_grid(h->g), h->kc, h->has_design ? h->dbox : nullptr, plan);
-    int counts[4];
+    int counts[kWorkLists];
     const std::vector<PlanItem> all = flatten(plan, counts);
     h->release((void*)h->work.interior);
     h->work = FusedWork{};

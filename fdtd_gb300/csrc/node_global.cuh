@@ -16,8 +16,9 @@ namespace fdtd {
 // eps_r of design cells. kPlate (k_plate_e only): plate-covered edges take the plate's sigma_e;
 // the other kernels leave plate nodes (class kPlateNode) alone, CPML memory included.
 // Idx: the integer type of node offsets; uint32_t when the field arrays hold fewer than 2^31
-// elements, which saves the 64-bit address arithmetic of every load and store.
-template <bool kDesign = false, bool kCoherent = false, bool kPlate = false, typename Idx = long long>
+// elements, which saves the 64-bit address arithmetic of every load and store. kSlabs: the CPML
+// slabs (bit 0 x, 1 y, 2 z) the caller's nodes may lie in; the other slab tests compile out.
+template <bool kDesign = false, bool kCoherent = false, bool kPlate = false, typename Idx = long long, int kSlabs = 7>
 __device__ __forceinline__ void e_node_global(const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo,
                                               const PsiSet& pin, const PsiSet& pout, int i, int j, int k, long long m) {
     const DeviceGrid& g = p.g;
@@ -57,10 +58,10 @@ __device__ __forceinline__ void e_node_global(const StepParams& p, const FieldPt
         // plate nodes are k_plate_e's, CPML memory included: the other kernels store nothing of them
         const PsiIO io{pin.f, pout.f, kPlate || c != kPlateNode};
         if (!kDesign && !kPlate && c == kUniformGeneral + p.bg.mat) {  // CPML / boundary background node
-            e_update<false, kCoherent, false, true>(p, nb, i, j, k, m, false, io, out, pre);
+            e_update<false, kCoherent, false, true, kSlabs>(p, nb, i, j, k, m, false, io, out, pre);
         } else {
             const bool plane_lumped = p.lumped_k[k] < p.lumped_k[k + 1];
-            e_update<kDesign, kCoherent, kPlate>(p, nb, i, j, k, m, plane_lumped, io, out, pre);
+            e_update<kDesign, kCoherent, kPlate, false, kSlabs>(p, nb, i, j, k, m, plane_lumped, io, out, pre);
         }
     }
     // k_design_e writes the design region's E, k_plate_e the plate nodes' E
@@ -73,7 +74,7 @@ __device__ __forceinline__ void e_node_global(const StepParams& p, const FieldPt
 }
 
 // H reads the old H from `fi` and the new E from `fe`.
-template <bool kCoherent = false, typename Idx = long long>
+template <bool kCoherent = false, typename Idx = long long, int kSlabs = 7>
 __device__ __forceinline__ void h_node_global(const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fe,
                                               const FieldPtrs& fo, const PsiSet& pin, const PsiSet& pout, int i, int j,
                                               int k, long long m) {
@@ -108,8 +109,8 @@ __device__ __forceinline__ void h_node_global(const StepParams& p, const FieldPt
             nb.mk = k > 0 ? mat[n - P] : 0;
         }
         const PsiIO io{pin.f, pout.f, true};
-        if (c == kUniformGeneral + p.bg.mat) h_update<kCoherent, true>(p, nb, i, j, k, io, out, pre);  // background node
-        else h_update<kCoherent>(p, nb, i, j, k, io, out, pre);
+        if (c == kUniformGeneral + p.bg.mat) h_update<kCoherent, true, kSlabs>(p, nb, i, j, k, io, out, pre);  // background node
+        else h_update<kCoherent, false, kSlabs>(p, nb, i, j, k, io, out, pre);
     }
     fo.hx[n] = out[0]; fo.hy[n] = out[1]; fo.hz[n] = out[2];
     if (p.probe_k[k] < p.probe_k[k + 1]) {

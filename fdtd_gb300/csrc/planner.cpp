@@ -12,8 +12,6 @@ namespace {
 constexpr int kShapes = 9;
 constexpr int kShapeW[kShapes] = {32, 16, 64, 128, 256, 8, 4, 2, 1};
 
-int round_up(int v, int a) { return (v + a - 1) / a * a; }
-
 // Shell items of the rectangle [x0, x0+w) x [y0, y0+h) of planes k .. k+nk-1: the block shape
 // with the fewest items.
 void shell_rect(std::vector<PlanItem>& out, int x0, int y0, int w, int h, int k, int nk) {
@@ -35,39 +33,23 @@ void shell_rect(std::vector<PlanItem>& out, int x0, int y0, int w, int h, int k,
         }
 }
 
-// Shell items of a column [x0, x0+w) x [y0, y0+h) over planes [k0, k1).
-void shell_column(std::vector<PlanItem>& out, int x0, int y0, int w, int h, int k0, int k1) {
-    for (int k = k0; k < k1; k += kShellPlanes) shell_rect(out, x0, y0, w, h, k, std::min(kShellPlanes, k1 - k));
-}
-
-// The E positions a sweep item computes, nodes [x0, x0+tx] x [y0, y0+ty] x [k0, k1], reach the
-// design region's edge box.
-bool touches(const int* d, int x0, int y0, int k0, int tx, int ty, int k1) {
-    return d && x0 <= d[3] && d[0] <= x0 + tx && y0 <= d[4] && d[1] <= y0 + ty && k0 <= d[5] && d[2] <= k1;
-}
-
-// General sweep items over [xa, xb) x [ya, yb) x [za, zb): tiles of tx x ty from (xa, ya), chunks
-// of kc planes; items whose E positions reach the design edge box go to the shell instead.
-void sweep_rect(std::vector<PlanItem>& out, std::vector<PlanItem>& shell, int xa, int xb, int ya, int yb, int za,
-                int zb, int tx, int ty, int kc, const int* design) {
-    if (xa >= xb || ya >= yb || za >= zb) return;
-    for (int y = ya; y < yb; y += ty)
-        for (int x = xa; x < xb; x += tx) {
-            const int w = std::min(tx, xb - x), h = std::min(ty, yb - y);
-            for (int k = za; k < zb; k += kc) {
-                const int k1 = std::min(k + kc, zb);
-                if (touches(design, x, y, k, tx, ty, k1)) {
-                    shell_column(shell, x, y, w, h, k, k1);
-                    continue;
-                }
-                out.push_back(PlanItem{x | w << 16, y | h << 16, k, k1});
-            }
-        }
+// Tile starts along an axis: from lo (rounded up to `align`) while the tile's far E positions
+// (start + size) stay <= hi, plus, when `overlap`, one tile ending on hi (it overlaps its
+// neighbour, which writes the same values there).
+std::vector<int> starts(int lo, int hi, int size, int align, bool overlap) {
+    std::vector<int> v;
+    const int a0 = (lo + align - 1) / align * align;
+    for (int q = a0; q + size <= hi; q += size) v.push_back(q);
+    if (overlap && !v.empty() && v.back() + size < hi) {
+        const int last = (hi - size) / align * align;
+        if (last > v.back()) v.push_back(last);
+    }
+    return v;
 }
 
 }  // namespace
 
-// Planes per sweep item: whole columns unless that leaves too few CTAs to fill the GPU, and at
+// Planes per interior item: whole columns unless that leaves too few CTAs to fill the GPU, and at
 // most kMaxItemPlanes - 2 (an item also streams the plane below and recomputes the one above).
 // Chunks are halved until the grid has at least kMinItems of them; 8192 measured best at 512^3 and
 // 1024 x 1024 x 896 against 2048, 4096 and 16384 (shorter chunks keep the CTAs in flight on fewer
@@ -80,60 +62,72 @@ int plan_chunk(const PlanGrid& g) {
     return std::max(1, std::min(kc, kMaxItemPlanes - 2));
 }
 
-// Interior tiles start at the first interior node rounded up to a multiple of 16 in x and y (the
-// TMA boxes of every sweep then start on 16-byte boundaries, every warp's row of stores on a
-// 32-byte sector, and the bands beside the interior are whole narrow / wide tiles when the CPML
-// is at most 16 cells thick) and step by the tile size while the tile's far E positions stay
-// interior. The rest of the grid goes to the general sweep: the z caps of the interior columns
-// (planes outside the interior z range), the y bands over the interior's x range (wide tiles),
-// and the x bands over the whole y range (narrow tiles). Without interior tiles the whole grid is
-// one general sweep of wide tiles. Tiles that reach a design region's edge box go to the shell.
+// Interior tiles (32 x 16 columns whose E positions x0..x0+TX, y0..y0+TY all lie in the x / y
+// interior) get their interior planes as interior items (chunks of at most kc planes; the E
+// positions of an item's top plane are recomputed, so a chunk keeps its top plane in the interior
+// range). Tiles start at the first interior node (x0 rounded up to a multiple of 8: every TMA box
+// then starts on a 16-byte boundary and every warp's row of stores on a 32-byte sector; origins
+// off the sector grid left sectors half written by two CTAs, which measured up to 30 % slower) and
+// step by the tile size; one more tile per axis ends on the last interior node. With a design
+// region, tiles that reach its edge box stay out of the sweep and no overlapping tiles are added.
+// Everything else is the shell: per run of planes a few rectangles, cut into items of 256 nodes
+// in the block shape that wastes the fewest threads, in the list of the slabs they may touch:
+// planes outside the interior z range split into the part over the interior's x / y range (z
+// slabs only), the y bands beside it (y and z) and the x bands (any); inside the interior z range
+// the y bands over the interior's x range (y and z), the x bands (any) and left-out design tiles
+// (no slab: the z list). Grids without interior tiles are one rectangle per plane (any).
 void plan_fused(const PlanGrid& g, int kc, const int* design_box, FusedPlan& out) {
     out.interior.clear();
-    out.wide.clear();
-    out.narrow.clear();
-    out.shell.clear();
+    for (auto& s : out.shell) s.clear();
     const int xlo = std::max(g.pxn, 1), xhi = std::min(g.nx - 1 - g.pxp, g.nx - 2);  // interior nodes, inclusive
     const int ylo = std::max(g.pyn, 1), yhi = std::min(g.ny - 1 - g.pyp, g.ny - 2);
     const int zlo = std::max(g.pzn, 1), zhi = std::min(g.nz - 1 - g.pzp, g.nz - 2);
+    const bool overlap = design_box == nullptr;
     std::vector<int> xs, ys;
     if (zhi > zlo) {
-        for (int x = round_up(xlo, 16); x + kTileX <= xhi; x += kTileX) xs.push_back(x);
-        for (int y = round_up(ylo, 16); y + kTileY <= yhi; y += kTileY) ys.push_back(y);
+        xs = starts(xlo, xhi, kTileX, 8, overlap);
+        ys = starts(ylo, yhi, kTileY, 1, overlap);
     }
     const int* d = design_box;
-    // general items stream half as many planes as interior ones: they are fewer, and the shorter
-    // marches spread them over more CTAs
-    const int kg = std::min(kc, std::max(8, kc / 2));
-    if (xs.empty() || ys.empty()) {
-        sweep_rect(out.wide, out.shell, 0, g.nx, 0, g.ny, 0, g.nz, kTileX, kTileY, kg, d);
-    } else {
-        const int X0 = xs.front(), X1 = xs.back() + kTileX, Y0 = ys.front(), Y1 = ys.back() + kTileY;
-        for (int y0 : ys)
-            for (int x0 : xs) {
-                if (touches(d, x0, y0, zlo, kTileX, kTileY, zhi)) {
-                    shell_column(out.shell, x0, y0, kTileX, kTileY, zlo, zhi);
-                    continue;
-                }
-                for (int k = zlo; k < zhi; k += kc) out.interior.push_back(PlanItem{x0, y0, k, std::min(k + kc, zhi)});
+    std::vector<PlanItem> left_out;  // tiles inside the swept rectangle that reach the design edge box
+    for (int y0 : ys)
+        for (int x0 : xs) {
+            if (d && x0 <= d[3] && d[0] <= x0 + kTileX && y0 <= d[4] && d[1] <= y0 + kTileY) {
+                left_out.push_back(PlanItem{x0, y0, 0, 0});
+                continue;
             }
-        // z caps of the interior rectangle
-        sweep_rect(out.wide, out.shell, X0, X1, Y0, Y1, 0, zlo, kTileX, kTileY, kg, d);
-        sweep_rect(out.wide, out.shell, X0, X1, Y0, Y1, zhi, g.nz, kTileX, kTileY, kg, d);
-        // y bands over the interior's x range, x bands over the whole y range
-        sweep_rect(out.wide, out.shell, X0, X1, 0, Y0, 0, g.nz, kTileX, kTileY, kg, d);
-        sweep_rect(out.wide, out.shell, X0, X1, Y1, g.ny, 0, g.nz, kTileX, kTileY, kg, d);
-        sweep_rect(out.narrow, out.shell, 0, X0, 0, g.ny, 0, g.nz, kNarrowX, kNarrowY, kg, d);
-        sweep_rect(out.narrow, out.shell, X1, g.nx, 0, g.ny, 0, g.nz, kNarrowX, kNarrowY, kg, d);
+            for (int k = zlo; k < zhi; k += kc) out.interior.push_back(PlanItem{x0, y0, k, std::min(k + kc, zhi)});
+        }
+    const bool swept = !xs.empty() && !ys.empty();
+    const int X0 = swept ? xs.front() : 0, X1 = swept ? xs.back() + kTileX : 0;
+    const int Y0 = swept ? ys.front() : 0, Y1 = swept ? ys.back() + kTileY : 0;
+    std::vector<PlanItem>& sz = out.shell[kPlanShellZ];
+    std::vector<PlanItem>& syz = out.shell[kPlanShellYZ];
+    std::vector<PlanItem>& sany = out.shell[kPlanShellAny];
+    // runs of up to kShellPlanes planes with the same rectangles share items
+    for (int k = 0; k < g.nz;) {
+        const bool caps = swept && (k < zlo || k >= zhi);
+        const int end = !swept ? g.nz : k < zlo ? zlo : k < zhi ? zhi : g.nz;
+        const int nk = std::min(kShellPlanes, end - k);
+        if (!swept) {
+            shell_rect(sany, 0, 0, g.nx, g.ny, k, nk);
+        } else {
+            if (caps) shell_rect(sz, X0, Y0, X1 - X0, Y1 - Y0, k, nk);
+            shell_rect(syz, X0, 0, X1 - X0, Y0, k, nk);
+            shell_rect(syz, X0, Y1, X1 - X0, g.ny - Y1, k, nk);
+            shell_rect(sany, 0, 0, X0, g.ny, k, nk);
+            shell_rect(sany, X1, 0, g.nx - X1, g.ny, k, nk);
+            if (!caps)
+                for (const PlanItem& t : left_out) shell_rect(sz, t.x, t.y, kTileX, kTileY, k, nk);
+        }
+        k += nk;
     }
     // plane-major order: CTAs run in item order, so the CTAs in flight then work on neighbouring
     // planes of many tiles instead of many planes of a few tiles, which keeps the pages they touch
     // few on large grids
     auto by_plane = [](const PlanItem& a, const PlanItem& b) { return a.z < b.z; };
     std::stable_sort(out.interior.begin(), out.interior.end(), by_plane);
-    std::stable_sort(out.wide.begin(), out.wide.end(), by_plane);
-    std::stable_sort(out.narrow.begin(), out.narrow.end(), by_plane);
-    std::stable_sort(out.shell.begin(), out.shell.end(), by_plane);
+    for (auto& s : out.shell) std::stable_sort(s.begin(), s.end(), by_plane);
 }
 
 }  // namespace fdtd

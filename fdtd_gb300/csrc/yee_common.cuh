@@ -274,6 +274,19 @@ __device__ __forceinline__ float psi_step(const float* in, float* out, int q, bo
     return psi_add(f, cpsi, s);
 }
 
+// Component masks of calc_e (fdtdrav.h:665, 696, 720) and calc_h (fdtdrav.h:328, 357, 382).
+__device__ __forceinline__ void e_masks(const DeviceGrid& g, int i, int j, int k, bool& ex_m, bool& ey_m, bool& ez_m) {
+    const bool in_x = i > 0 && i < g.nx - 1, in_y = j > 0 && j < g.ny - 1, in_z = k > 0 && k < g.nz - 1;
+    ex_m = i < g.nx - 1 && in_y && in_z;
+    ey_m = in_x && j < g.ny - 1 && in_z;
+    ez_m = in_x && in_y && k < g.nz - 1;
+}
+__device__ __forceinline__ void h_masks(const DeviceGrid& g, int i, int j, int k, bool& hx_m, bool& hy_m, bool& hz_m) {
+    hx_m = j < g.ny - 1 && k < g.nz - 1;
+    hy_m = i < g.nx - 1 && k < g.nz - 1;
+    hz_m = i < g.nx - 1 && j < g.ny - 1;
+}
+
 // One E node (calc_e fdtdrav.h:577-915): main updates with their masks and the lumped override,
 // then the CPML corrections in the reference's order (x, y, z). pre[] receives the values between
 // the main update and the CPML corrections (the sampleField values, fdtdrav.h:740).
@@ -282,17 +295,16 @@ __device__ __forceinline__ float psi_step(const float* in, float* out, int q, bo
 // node class kPlateNode, instantiates it). kBg: a node whose seven cells all hold the background
 // material and that carries no lumped edge (node class kUniformGeneral + background): the same
 // arithmetic with the uniformity, background and lumped tests decided at compile time.
-template <bool kDesignAware = false, bool kCoherent = false, bool kPlate = false, bool kBg = false>
+// kSlabs: the CPML slabs (bit 0 x, 1 y, 2 z) the node may lie in; the other slab tests compile out.
+template <bool kDesignAware = false, bool kCoherent = false, bool kPlate = false, bool kBg = false, int kSlabs = 7>
 __device__ __forceinline__ void e_update(const StepParams& p, const ENbr& n, int i, int j, int k, long long m,
                                          bool plane_lumped, const PsiIO& ps, float out[3], float pre[3]) {
     const DeviceGrid& g = p.g;
-    const bool in_x = i > 0 && i < g.nx - 1, in_y = j > 0 && j < g.ny - 1, in_z = k > 0 && k < g.nz - 1;
-    const bool ex_m = i < g.nx - 1 && in_y && in_z;  // fdtdrav.h:665
-    const bool ey_m = in_x && j < g.ny - 1 && in_z;  // fdtdrav.h:696
-    const bool ez_m = in_x && in_y && k < g.nz - 1;  // fdtdrav.h:720
-    const bool xs = in_slab(i, g.nx, g.pxn, g.pxp);
-    const bool ys = in_slab(j, g.ny, g.pyn, g.pyp);
-    const bool zs = in_slab(k, g.nz, g.pzn, g.pzp);
+    bool ex_m, ey_m, ez_m;  // fdtdrav.h:665, 696, 720
+    e_masks(g, i, j, k, ex_m, ey_m, ez_m);
+    const bool xs = (kSlabs & 1) && in_slab(i, g.nx, g.pxn, g.pxp);
+    const bool ys = (kSlabs & 2) && in_slab(j, g.ny, g.pyn, g.pyp);
+    const bool zs = (kSlabs & 4) && in_slab(k, g.nz, g.pzn, g.pzp);
     const int bg = p.bg.mat;
     const int m0 = kBg ? bg : n.m0;
     const bool ux = kBg || (n.m0 == n.mj && n.m0 == n.mk && n.m0 == n.mjk);
@@ -369,16 +381,16 @@ __device__ __forceinline__ void e_update(const StepParams& p, const ENbr& n, int
 }
 
 // One H node (calc_h fdtdrav.h:249-573).
-template <bool kCoherent = false, bool kBg = false>
+// kSlabs as for e_update.
+template <bool kCoherent = false, bool kBg = false, int kSlabs = 7>
 __device__ __forceinline__ void h_update(const StepParams& p, const HNbr& n, int i, int j, int k,
                                          const PsiIO& ps, float out[3], float pre[3]) {
     const DeviceGrid& g = p.g;
-    const bool hx_m = j < g.ny - 1 && k < g.nz - 1;  // fdtdrav.h:328
-    const bool hy_m = i < g.nx - 1 && k < g.nz - 1;  // fdtdrav.h:357
-    const bool hz_m = i < g.nx - 1 && j < g.ny - 1;  // fdtdrav.h:382
-    const bool xs = in_slab(i, g.nx, g.pxn, g.pxp);
-    const bool ys = in_slab(j, g.ny, g.pyn, g.pyp);
-    const bool zs = in_slab(k, g.nz, g.pzn, g.pzp);
+    bool hx_m, hy_m, hz_m;  // fdtdrav.h:328, 357, 382
+    h_masks(g, i, j, k, hx_m, hy_m, hz_m);
+    const bool xs = (kSlabs & 1) && in_slab(i, g.nx, g.pxn, g.pxp);
+    const bool ys = (kSlabs & 2) && in_slab(j, g.ny, g.pyn, g.pyp);
+    const bool zs = (kSlabs & 4) && in_slab(k, g.nz, g.pzn, g.pzp);
     const int bg = p.bg.mat;
     const int m0 = kBg ? bg : n.m0;
     const bool ux = kBg || n.m0 == n.mi, uy = kBg || n.m0 == n.mj, uz = kBg || n.m0 == n.mk;

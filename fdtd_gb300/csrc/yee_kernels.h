@@ -36,34 +36,34 @@ cudaError_t launch_design_e(const StepParams& p, const FieldPtrs& fi, const Fiel
 cudaError_t launch_plate_e(const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
                            const PsiSet& pout, long long m, cudaStream_t st);
 
-// Shell passes of the fused schedule (yee_two_pass.cu): E (e_pass) or H of the nodes of `items`,
-// reading fi / pin (buffer A) and writing fo / pout (buffer B).
-cudaError_t launch_shell(bool e_pass, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
-                         const PsiSet& pout, const int4* items, int n_items, long long m, cudaStream_t st);
+// Shell items of the fused schedule (planner.h), one list per set of CPML slabs their nodes may
+// lie in: kShellZ (z slabs only: planes outside the interior z range within the interior's x / y
+// range, and tiles around a design region), kShellYZ (the y bands beside the interior), kShellAny
+// (the x bands, corners included, and whole grids without interior tiles).
+enum { kShellZ = 0, kShellYZ = 1, kShellAny = 2, kShellLists = 3 };
+struct ShellWork {
+    const int4* items[kShellLists];
+    int n[kShellLists];
+};
 
-// Fused schedule (yee_fused.cu): per step the per-node E of the shell items, the z-marching
-// sweeps (TMA tiles of buffer A: H with halo, old E, coefficient rows) over interior, wide and
-// narrow items, and the per-node H of the shell items; fields A -> B, CPML memory psi_in -> psi_out.
-// The items come from plan_fused (planner.h).
-struct TileMaps {
+// Shell passes of the fused schedule (yee_two_pass.cu): E (e_pass) or H of the nodes of the shell
+// items, reading fi / pin (buffer A) and writing fo / pout (buffer B).
+cudaError_t launch_shell(bool e_pass, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
+                         const PsiSet& pout, const ShellWork& w, long long m, cudaStream_t st);
+
+// Fused schedule (yee_fused.cu): per step the shell E pass, the z-marching interior sweep (TMA
+// tiles of buffer A: H with halo, old E, coefficient rows) and the shell H pass; fields A -> B, CPML
+// memory psi_in -> psi_out. The items come from plan_fused (planner.h).
+struct FusedMaps {
     CUtensorMap h[3];
     CUtensorMap e[3];
     CUtensorMap rec;  // coefficient rows (StepParams::rec)
-};
-struct FusedMaps {
-    TileMaps wide;    // 32 x 16 columns (interior and wide items)
-    TileMaps narrow;  // 16 x 32 columns (narrow items)
 };
 // Work items of one step (device arrays of int4 in the formats of planner.h).
 struct FusedWork {
     const int4* interior;
     int n_interior;
-    const int4* wide;
-    int n_wide;
-    const int4* narrow;
-    int n_narrow;
-    const int4* general;  // shell items
-    int n_general;
+    ShellWork shell;
 };
 cudaError_t fused_configure();
 int fused_smem_bytes();

@@ -51,7 +51,9 @@ __device__ __forceinline__ bool shell_node(const int4& it, const DeviceGrid& g, 
     return tx < ((it.w >> 4) & 511) && ty < ((it.w >> 13) & 511) && i < g.nx && j < g.ny;
 }
 
-template <typename Idx>
+// kSlabs: the CPML slabs (bit 0 x, 1 y, 2 z) the items' nodes may lie in (one instantiation per
+// shell list, yee_kernels.h); the other slab tests compile out.
+template <typename Idx, int kSlabs>
 __global__ void __launch_bounds__(256, FDTD_SHELL_MIN_BLOCKS) k_shell_e(const __grid_constant__ StepParams p, FieldPtrs fi, FieldPtrs fo,
                                                  const __grid_constant__ PsiSet pin, const __grid_constant__ PsiSet pout,
                                                  const int4* __restrict__ items, long long m) {
@@ -59,10 +61,10 @@ __global__ void __launch_bounds__(256, FDTD_SHELL_MIN_BLOCKS) k_shell_e(const __
     const int4 it = items[blockIdx.x];
     if (!shell_node(it, p.g, i, j)) return;
     for (int k = it.z, k1 = it.z + ((it.w >> 22) & 15); k <= k1; ++k)
-        e_node_global<false, false, false, Idx>(p, fi, fo, pin, pout, i, j, k, m);
+        e_node_global<false, false, false, Idx, kSlabs>(p, fi, fo, pin, pout, i, j, k, m);
 }
 
-template <typename Idx>
+template <typename Idx, int kSlabs>
 __global__ void __launch_bounds__(256, FDTD_SHELL_MIN_BLOCKS) k_shell_h(const __grid_constant__ StepParams p, FieldPtrs fi, FieldPtrs fo,
                                                  const __grid_constant__ PsiSet pin, const __grid_constant__ PsiSet pout,
                                                  const int4* __restrict__ items, long long m) {
@@ -70,20 +72,30 @@ __global__ void __launch_bounds__(256, FDTD_SHELL_MIN_BLOCKS) k_shell_h(const __
     const int4 it = items[blockIdx.x];
     if (!shell_node(it, p.g, i, j)) return;
     for (int k = it.z, k1 = it.z + ((it.w >> 22) & 15); k <= k1; ++k)
-        h_node_global<false, Idx>(p, fi, fo, fo, pin, pout, i, j, k, m);
+        h_node_global<false, Idx, kSlabs>(p, fi, fo, fo, pin, pout, i, j, k, m);
+}
+
+template <typename Idx, int kSlabs>
+void shell_list(bool e_pass, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
+                const PsiSet& pout, const int4* items, int n, long long m, cudaStream_t st) {
+    if (n <= 0) return;
+    const dim3 b(32, 8, 1);
+    if (e_pass) k_shell_e<Idx, kSlabs><<<n, b, 0, st>>>(p, fi, fo, pin, pout, items, m);
+    else k_shell_h<Idx, kSlabs><<<n, b, 0, st>>>(p, fi, fo, pin, pout, items, m);
+}
+
+template <typename Idx>
+void shell_lists(bool e_pass, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
+                 const PsiSet& pout, const ShellWork& w, long long m, cudaStream_t st) {
+    shell_list<Idx, 4>(e_pass, p, fi, fo, pin, pout, w.items[kShellZ], w.n[kShellZ], m, st);
+    shell_list<Idx, 6>(e_pass, p, fi, fo, pin, pout, w.items[kShellYZ], w.n[kShellYZ], m, st);
+    shell_list<Idx, 7>(e_pass, p, fi, fo, pin, pout, w.items[kShellAny], w.n[kShellAny], m, st);
 }
 
 cudaError_t launch_shell(bool e_pass, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
-                         const PsiSet& pout, const int4* items, int n_items, long long m, cudaStream_t st) {
-    if (n_items <= 0) return cudaSuccess;
-    const dim3 b(32, 8, 1);
-    if (p.g.plane * (long long)(p.g.nz + 1) < (1LL << 31)) {
-        if (e_pass) k_shell_e<uint32_t><<<n_items, b, 0, st>>>(p, fi, fo, pin, pout, items, m);
-        else k_shell_h<uint32_t><<<n_items, b, 0, st>>>(p, fi, fo, pin, pout, items, m);
-    } else {
-        if (e_pass) k_shell_e<long long><<<n_items, b, 0, st>>>(p, fi, fo, pin, pout, items, m);
-        else k_shell_h<long long><<<n_items, b, 0, st>>>(p, fi, fo, pin, pout, items, m);
-    }
+                         const PsiSet& pout, const ShellWork& w, long long m, cudaStream_t st) {
+    if (p.g.plane * (long long)(p.g.nz + 1) < (1LL << 31)) shell_lists<uint32_t>(e_pass, p, fi, fo, pin, pout, w, m, st);
+    else shell_lists<long long>(e_pass, p, fi, fo, pin, pout, w, m, st);
     return cudaGetLastError();
 }
 

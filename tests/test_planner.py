@@ -1,7 +1,8 @@
 """CPU tests of the fused schedule's work planner (fdtd_gb300/csrc/planner.cpp), compiled here with
-g++ into a host-only library: the items of every list together store each node exactly once, sweep
-items keep the TMA alignment and the plane limit, interior items hold only interior nodes (E halo
-included), and no sweep item reaches a design region's edge box."""
+g++ into a host-only library: the items of every list together store each node exactly once
+(overlapping interior tiles write the same values), interior items keep the TMA alignment and the
+plane limit and hold only interior nodes (E halo included) away from a design region's edge box,
+and no shell list holds nodes of a CPML slab its kernel leaves out."""
 import ctypes
 import os
 import subprocess
@@ -15,8 +16,11 @@ BUILD = os.path.join(ROOT, "tests", "_build")
 LIB = os.path.join(BUILD, "libplan_probe.so")
 SRCS = [os.path.join(CSRC, "planner.cpp"), os.path.join(ROOT, "tests", "plan_probe.cpp")]
 
-TILE_X, TILE_Y, NARROW_X, NARROW_Y, MAX_ITEM_PLANES, SHELL_PLANES = 32, 16, 16, 32, 512, 4
+TILE_X, TILE_Y, MAX_ITEM_PLANES, SHELL_PLANES = 32, 16, 512, 4
 SHAPE_W = [32, 16, 64, 128, 256, 8, 4, 2, 1]
+# shell lists and the CPML slabs (bit 0 x, 1 y, 2 z) their kernels test for
+SHELL_LISTS = (("shell_z", 4), ("shell_yz", 6), ("shell_any", 7))
+LISTS = ("interior",) + tuple(n for n, _ in SHELL_LISTS)
 
 
 @pytest.fixture(scope="module")
@@ -33,14 +37,14 @@ def lib():
 def plan(lib, dims, pml, design=None):
     g = (ctypes.c_int * 9)(*dims, *pml)
     d = None if design is None else (ctypes.c_int * 6)(*design)
-    counts = (ctypes.c_int * 4)()
+    counts = (ctypes.c_int * len(LISTS))()
     lib.plan_probe(g, d, counts, None, 0)
     n = sum(counts)
     items = np.zeros((max(n, 1), 4), dtype=np.int32)
     kc = lib.plan_probe(g, d, counts, items.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), n)
-    lists, o = [], 0
-    for q in range(4):
-        lists.append(items[o:o + counts[q]])
+    lists, o = {}, 0
+    for q, name in enumerate(LISTS):
+        lists[name] = items[o:o + counts[q]]
         o += counts[q]
     return kc, lists
 
@@ -49,34 +53,40 @@ def interior_range(n, pn, pp):
     return max(pn, 1), min(n - 1 - pp, n - 2)
 
 
+def in_slab(q, n, pn, pp):
+    return q < pn or q >= n - pp
+
+
 def check(lib, dims, pml, design=None):
     nx, ny, nz = dims
-    kc, (interior, wide, narrow, shell) = plan(lib, dims, pml, design)
-    cover = np.zeros((nz, ny, nx), dtype=np.int32)
+    kc, L = plan(lib, dims, pml, design)
     xlo, xhi = interior_range(nx, pml[0], pml[1])
     ylo, yhi = interior_range(ny, pml[2], pml[3])
     zlo, zhi = interior_range(nz, pml[4], pml[5])
-    for x0, y0, k0, k1 in interior:
+    owned = np.zeros((nz, ny, nx), dtype=np.int32)
+    for x0, y0, k0, k1 in L["interior"]:
         assert x0 % 8 == 0 and 0 < k1 - k0 <= MAX_ITEM_PLANES - 2
         assert xlo <= x0 and x0 + TILE_X <= xhi and ylo <= y0 and y0 + TILE_Y <= yhi and zlo <= k0 and k1 <= zhi
-        cover[k0:k1, y0:y0 + TILE_Y, x0:x0 + TILE_X] += 1
-    for lst, tx, ty in ((wide, TILE_X, TILE_Y), (narrow, NARROW_X, NARROW_Y)):
-        for xw, yh, k0, k1 in lst:
-            x0, w, y0, h = xw & 0xffff, xw >> 16, yh & 0xffff, yh >> 16
-            assert x0 % 4 == 0 and 0 < w <= tx and 0 < h <= ty and 0 < k1 - k0 <= MAX_ITEM_PLANES - 2
-            assert x0 + w <= nx and y0 + h <= ny and 0 <= k0 and k1 <= nz
-            if design is not None:
-                d = design
-                assert not (x0 <= d[3] and d[0] <= x0 + tx and y0 <= d[4] and d[1] <= y0 + ty and k0 <= d[5]
-                            and d[2] <= k1), "a sweep item reaches the design edge box"
-            cover[k0:k1, y0:y0 + h, x0:x0 + w] += 1
-    for x0, y0, k, code in shell:
-        s, cols, rows, nk = code & 15, (code >> 4) & 511, (code >> 13) & 511, ((code >> 22) & 15) + 1
-        bw = SHAPE_W[s]
-        assert cols <= bw and rows <= 256 // bw and nk <= SHELL_PLANES
-        cover[k:k + nk, y0:y0 + rows, x0:x0 + cols] += 1
+        if design is not None:
+            d = design
+            assert not (x0 <= d[3] and d[0] <= x0 + TILE_X and y0 <= d[4] and d[1] <= y0 + TILE_Y), \
+                "an interior tile reaches the design edge box"
+        owned[k0:k1, y0:y0 + TILE_Y, x0:x0 + TILE_X] = 1  # overlapping tiles store the same values
+    cover = owned
+    for name, slabs in SHELL_LISTS:
+        for x0, y0, k, code in L[name]:
+            s, cols, rows, nk = code & 15, (code >> 4) & 511, (code >> 13) & 511, ((code >> 22) & 15) + 1
+            bw = SHAPE_W[s]
+            assert cols <= bw and rows <= 256 // bw and nk <= SHELL_PLANES
+            assert x0 + cols <= nx and y0 + rows <= ny and k + nk <= nz
+            # the slabs the list's kernel leaves out hold none of its nodes
+            if not slabs & 1:
+                assert not any(in_slab(x, nx, pml[0], pml[1]) for x in range(x0, x0 + cols)), name
+            if not slabs & 2:
+                assert not any(in_slab(y, ny, pml[2], pml[3]) for y in range(y0, y0 + rows)), name
+            cover[k:k + nk, y0:y0 + rows, x0:x0 + cols] += 1
     assert cover.min() == 1 and cover.max() == 1, (int(cover.min()), int(cover.max()))
-    return kc, interior, wide, narrow, shell
+    return kc, L
 
 
 @pytest.mark.parametrize("dims,pml", [
@@ -99,13 +109,10 @@ def test_plan_covers_every_node_once(lib, dims, pml):
     check(lib, dims, pml)
 
 
-def test_bench_grid_uses_whole_band_tiles(lib):
-    """512^3 with 10-cell CPML: the x bands are whole narrow tiles, the y bands whole wide tiles, and
-    no shell items remain."""
-    _, interior, wide, narrow, shell = check(lib, (512, 512, 512), (10,) * 6)
-    assert len(shell) == 0 and len(interior) > 0
-    assert all((it[0] >> 16) == NARROW_X and (it[1] >> 16) == NARROW_Y for it in narrow)
-    assert all((it[0] >> 16) == TILE_X and (it[1] >> 16) == TILE_Y for it in wide)
+def test_bench_grid_lists(lib):
+    """512^3 with 10-cell CPML: most nodes interior, every shell list in use."""
+    _, L = check(lib, (512, 512, 512), (10,) * 6)
+    assert len(L["interior"]) > 0 and all(len(L[n]) > 0 for n, _ in SHELL_LISTS)
 
 
 @pytest.mark.parametrize("dims,pml,design", [
@@ -114,5 +121,5 @@ def test_bench_grid_uses_whole_band_tiles(lib):
     ((96, 80, 64), (8,) * 6, (9, 10, 9, 30, 20, 18)),   # reaching into the CPML corner
 ])
 def test_plan_with_design_region(lib, dims, pml, design):
-    _, _, _, _, shell = check(lib, dims, pml, design)
-    assert len(shell) > 0
+    _, L = check(lib, dims, pml, design)
+    assert sum(len(L[n]) for n, _ in SHELL_LISTS) > 0
