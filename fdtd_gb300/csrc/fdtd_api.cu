@@ -85,6 +85,7 @@ struct fdtd_handle {
     int cur = 0;
     bool have_second = false;
     FusedMaps maps[2];
+    FusedFork fork{};  // second stream and events of the fused step (created with the fused buffers)
     int kc = 0;  // planes per CTA chunk of the fused sweep
     FusedWork work{};
     bool replan = false;  // the design region changed since the fused work was planned
@@ -373,6 +374,13 @@ int ensure_fused(fdtd_handle* h) {
             return fail(FDTD_ERR_CUDA, "tensor map encoding failed");
     }
     CUDA_TRY(fused_configure());
+    if (!h->fork.aux) {  // the sweep's stream: as high a priority as the handle's
+        int prio = 0;
+        CUDA_TRY(cudaStreamGetPriority(h->stream, &prio));
+        CUDA_TRY(cudaStreamCreateWithPriority(&h->fork.aux, cudaStreamNonBlocking, prio));
+        CUDA_TRY(cudaEventCreateWithFlags(&h->fork.fork, cudaEventDisableTiming));
+        CUDA_TRY(cudaEventCreateWithFlags(&h->fork.join, cudaEventDisableTiming));
+    }
     h->kc = plan_chunk(plan_grid(h->g));
     rc = plan_work(h);
     if (rc) return rc;
@@ -492,6 +500,12 @@ int fdtd_destroy(fdtd_handle* h) {
     h->allocs.clear();
     h->alloc_sizes.clear();
     if (h->static_items) cudaFreeHost(h->static_items);
+    if (h->fork.aux) {
+        cudaStreamSynchronize(h->fork.aux);
+        cudaEventDestroy(h->fork.fork);
+        cudaEventDestroy(h->fork.join);
+        cudaStreamDestroy(h->fork.aux);
+    }
     delete h;
     return FDTD_OK;
 }
@@ -673,7 +687,8 @@ int steps_fused(fdtd_handle* h, const StepParams& p, int64_t n) {
         const int a = h->cur, b = 1 - h->cur;
         FieldPtrs fi{h->field[a][0], h->field[a][1], h->field[a][2], h->field[a][3], h->field[a][4], h->field[a][5]};
         FieldPtrs fo{h->field[b][0], h->field[b][1], h->field[b][2], h->field[b][3], h->field[b][4], h->field[b][5]};
-        CUDA_TRY(launch_fused(h->maps[a], p, fi, fo, h->psi[a], h->psi[b], h->step, h->work, h->stream));
+        CUDA_TRY(launch_fused(h->maps[a], p, fi, fo, h->psi[a], h->psi[b], h->step, h->work, h->stream,
+                              h->fork.aux ? &h->fork : nullptr));
         h->cur = b;
         ++h->step;
     }

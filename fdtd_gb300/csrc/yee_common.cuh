@@ -262,13 +262,18 @@ struct PsiIO {
     bool write;
 };
 
-// kCoherent: read the old psi through L2 (ld.global.cg) instead of the read-only path; the batched
-// launch needs it, since it rewrites psi in one step and reads it again in the next within the
-// same kernel. The other kernels read each psi once per launch and keep the read-only path.
-template <bool kHyz = false, bool kCoherent = false>
-__device__ __forceinline__ float psi_step(const float* in, float* out, int q, bool write,
-                                          float b, float a, float d, float f, float cpsi) {
-    const float old = kCoherent ? __ldcg(in + q) : __ldg(in + q);
+
+// The old CPML memory of one slot. kCoherent: through L2 (ld.global.cg) instead of the read-only
+// path; the batched persistent launch needs it, since it rewrites psi in one step and reads it
+// again in the next within the same kernel. The other kernels read each psi once per launch.
+template <bool kCoherent = false>
+__device__ __forceinline__ float psi_load(const float* in, int q) {
+    return kCoherent ? __ldcg(in + q) : __ldg(in + q);
+}
+// One CPML recurrence from the old memory value `old`.
+template <bool kHyz = false>
+__device__ __forceinline__ float psi_apply(float old, float* out, int q, bool write, float b, float a, float d, float f,
+                                           float cpsi) {
     const float s = kHyz ? psi_upd_hyz(b, old, a, d) : psi_upd(b, old, a, d);
     if (write) out[q] = s;
     return psi_add(f, cpsi, s);
@@ -360,20 +365,20 @@ __device__ __forceinline__ void e_update(const StepParams& p, const ENbr& n, int
     if (xs && (ey_m || ez_m)) {
         const int q = psi_off_x(g, i, j, k, side);
         const float bb = __ldg(p.bex + i), aa = __ldg(p.aex + i);
-        if (ey_m) vy = psi_step<false, kCoherent>(ps.in[side].e[0], ps.out[side].e[0], q, ps.write, bb, aa, dHz_i, vy, __fmul_rn(cy.bm, g.dx));
-        if (ez_m) vz = psi_step<false, kCoherent>(ps.in[side].e[1], ps.out[side].e[1], q, ps.write, bb, aa, dHy_i, vz, __fmul_rn(cz.bp, g.dx));
+        if (ey_m) vy = psi_apply(psi_load<kCoherent>(ps.in[side].e[0], q), ps.out[side].e[0], q, ps.write, bb, aa, dHz_i, vy, __fmul_rn(cy.bm, g.dx));
+        if (ez_m) vz = psi_apply(psi_load<kCoherent>(ps.in[side].e[1], q), ps.out[side].e[1], q, ps.write, bb, aa, dHy_i, vz, __fmul_rn(cz.bp, g.dx));
     }
     if (ys && (ex_m || ez_m)) {
         const int q = psi_off_y(g, i, j, k, side);
         const float bb = __ldg(p.bey + j), aa = __ldg(p.aey + j);
-        if (ex_m) vx = psi_step<false, kCoherent>(ps.in[2 + side].e[0], ps.out[2 + side].e[0], q, ps.write, bb, aa, dHz_j, vx, __fmul_rn(cx.bp, g.dy));
-        if (ez_m) vz = psi_step<false, kCoherent>(ps.in[2 + side].e[1], ps.out[2 + side].e[1], q, ps.write, bb, aa, dHx_j, vz, __fmul_rn(cz.bm, g.dy));
+        if (ex_m) vx = psi_apply(psi_load<kCoherent>(ps.in[2 + side].e[0], q), ps.out[2 + side].e[0], q, ps.write, bb, aa, dHz_j, vx, __fmul_rn(cx.bp, g.dy));
+        if (ez_m) vz = psi_apply(psi_load<kCoherent>(ps.in[2 + side].e[1], q), ps.out[2 + side].e[1], q, ps.write, bb, aa, dHx_j, vz, __fmul_rn(cz.bm, g.dy));
     }
     if (zs && (ex_m || ey_m)) {
         const int q = psi_off_z(g, i, j, k, side);
         const float bb = __ldg(p.bez + k), aa = __ldg(p.aez + k);
-        if (ex_m) vx = psi_step<false, kCoherent>(ps.in[4 + side].e[0], ps.out[4 + side].e[0], q, ps.write, bb, aa, dHy_k, vx, __fmul_rn(cx.bm, g.dz));
-        if (ey_m) vy = psi_step<false, kCoherent>(ps.in[4 + side].e[1], ps.out[4 + side].e[1], q, ps.write, bb, aa, dHx_k, vy, __fmul_rn(cy.bp, g.dz));
+        if (ex_m) vx = psi_apply(psi_load<kCoherent>(ps.in[4 + side].e[0], q), ps.out[4 + side].e[0], q, ps.write, bb, aa, dHy_k, vx, __fmul_rn(cx.bm, g.dz));
+        if (ey_m) vy = psi_apply(psi_load<kCoherent>(ps.in[4 + side].e[1], q), ps.out[4 + side].e[1], q, ps.write, bb, aa, dHx_k, vy, __fmul_rn(cy.bp, g.dz));
     }
     out[0] = ex_m ? vx : n.ex;
     out[1] = ey_m ? vy : n.ey;
@@ -421,20 +426,20 @@ __device__ __forceinline__ void h_update(const StepParams& p, const HNbr& n, int
     if (xs && (hy_m || hz_m)) {
         const int q = psi_off_x(g, i, j, k, side);
         const float bb = __ldg(p.bmx + i), aa = __ldg(p.amx + i);
-        if (hy_m) vy = psi_step<false, kCoherent>(ps.in[side].h[0], ps.out[side].h[0], q, ps.write, bb, aa, dEz_i, vy, __fmul_rn(cy.bp, g.dx));
-        if (hz_m) vz = psi_step<false, kCoherent>(ps.in[side].h[1], ps.out[side].h[1], q, ps.write, bb, aa, dEy_i, vz, __fmul_rn(cz.bm, g.dx));
+        if (hy_m) vy = psi_apply(psi_load<kCoherent>(ps.in[side].h[0], q), ps.out[side].h[0], q, ps.write, bb, aa, dEz_i, vy, __fmul_rn(cy.bp, g.dx));
+        if (hz_m) vz = psi_apply(psi_load<kCoherent>(ps.in[side].h[1], q), ps.out[side].h[1], q, ps.write, bb, aa, dEy_i, vz, __fmul_rn(cz.bm, g.dx));
     }
     if (ys && (hx_m || hz_m)) {
         const int q = psi_off_y(g, i, j, k, side);
         const float bb = __ldg(p.bmy + j), aa = __ldg(p.amy + j);
-        if (hx_m) vx = psi_step<false, kCoherent>(ps.in[2 + side].h[0], ps.out[2 + side].h[0], q, ps.write, bb, aa, dEz_j, vx, __fmul_rn(cx.bm, g.dy));
-        if (hz_m) vz = psi_step<false, kCoherent>(ps.in[2 + side].h[1], ps.out[2 + side].h[1], q, ps.write, bb, aa, dEx_j, vz, __fmul_rn(cz.bp, g.dy));
+        if (hx_m) vx = psi_apply(psi_load<kCoherent>(ps.in[2 + side].h[0], q), ps.out[2 + side].h[0], q, ps.write, bb, aa, dEz_j, vx, __fmul_rn(cx.bm, g.dy));
+        if (hz_m) vz = psi_apply(psi_load<kCoherent>(ps.in[2 + side].h[1], q), ps.out[2 + side].h[1], q, ps.write, bb, aa, dEx_j, vz, __fmul_rn(cz.bp, g.dy));
     }
     if (zs && (hx_m || hy_m)) {
         const int q = psi_off_z(g, i, j, k, side);
         const float bb = __ldg(p.bmz + k), aa = __ldg(p.amz + k);
-        if (hx_m) vx = psi_step<false, kCoherent>(ps.in[4 + side].h[0], ps.out[4 + side].h[0], q, ps.write, bb, aa, dEy_k, vx, __fmul_rn(cx.bp, g.dz));
-        if (hy_m) vy = psi_step<true, kCoherent>(ps.in[4 + side].h[1], ps.out[4 + side].h[1], q, ps.write, bb, aa, dEx_k, vy, __fmul_rn(cy.bm, g.dz));
+        if (hx_m) vx = psi_apply(psi_load<kCoherent>(ps.in[4 + side].h[0], q), ps.out[4 + side].h[0], q, ps.write, bb, aa, dEy_k, vx, __fmul_rn(cx.bp, g.dz));
+        if (hy_m) vy = psi_apply<true>(psi_load<kCoherent>(ps.in[4 + side].h[1], q), ps.out[4 + side].h[1], q, ps.write, bb, aa, dEx_k, vy, __fmul_rn(cy.bm, g.dz));
     }
     out[0] = hx_m ? vx : n.hx;
     out[1] = hy_m ? vy : n.hy;

@@ -391,15 +391,31 @@ cudaError_t fused_configure() {
 // One fused step: per-node E of the shell items (CPML slabs, boundary planes, strips beside the
 // interior tiles, tiles around a design region), the design region's and the plates' E, the
 // interior sweep, per-node H of the shell items (which reads the new E of its neighbours, written
-// by the sweep).
+// by the sweep). With a fork the sweep runs beside the shell E pass on the second stream.
 cudaError_t launch_fused(const FusedMaps& maps, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo,
-                         const PsiSet& psi_in, const PsiSet& psi_out, long long m, const FusedWork& w, cudaStream_t st) {
-    cudaError_t e = launch_shell(true, p, fi, fo, psi_in, psi_out, w.shell, m, st);
+                         const PsiSet& psi_in, const PsiSet& psi_out, long long m, const FusedWork& w, cudaStream_t st,
+                         const FusedFork* fork) {
+    cudaError_t e = cudaSuccess;
+    const bool split = fork && w.n_interior > 0;
+    if (split) {
+        e = cudaEventRecord(fork->fork, st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(fork->aux, fork->fork, 0);
+        if (e != cudaSuccess) return e;
+        k_sweep_interior<<<w.n_interior, NTH, TileW::SMEM, fork->aux>>>(maps, p, fo, w.interior, m);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaEventRecord(fork->join, fork->aux);
+        if (e != cudaSuccess) return e;
+    }
+    e = launch_shell(true, p, fi, fo, psi_in, psi_out, w.shell, m, st);
     if (e == cudaSuccess) e = launch_design_e(p, fi, fo, psi_in, psi_out, m, st);
     if (e == cudaSuccess) e = launch_plate_e(p, fi, fo, psi_in, psi_out, m, st);
     if (e != cudaSuccess) return e;
-    if (w.n_interior > 0) k_sweep_interior<<<w.n_interior, NTH, TileW::SMEM, st>>>(maps, p, fo, w.interior, m);
-    e = cudaGetLastError();
+    if (split) {
+        e = cudaStreamWaitEvent(st, fork->join, 0);
+    } else if (w.n_interior > 0) {
+        k_sweep_interior<<<w.n_interior, NTH, TileW::SMEM, st>>>(maps, p, fo, w.interior, m);
+        e = cudaGetLastError();
+    }
     if (e != cudaSuccess) return e;
     return launch_shell(false, p, fi, fo, psi_in, psi_out, w.shell, m, st);
 }

@@ -47,7 +47,8 @@ struct ShellWork {
 };
 
 // Shell passes of the fused schedule (yee_two_pass.cu): E (e_pass) or H of the nodes of the shell
-// items, reading fi / pin (buffer A) and writing fo / pout (buffer B).
+// items, reading fi / pin (buffer A) and writing fo / pout (buffer B). The three lists must lie one
+// after the other in device memory (one launch covers them).
 cudaError_t launch_shell(bool e_pass, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
                          const PsiSet& pout, const ShellWork& w, long long m, cudaStream_t st);
 
@@ -67,8 +68,16 @@ struct FusedWork {
 };
 cudaError_t fused_configure();
 int fused_smem_bytes();
+// fork (optional): a second stream and two events; the interior sweep then runs on `aux`,
+// concurrently with the shell E pass on `st` (they read buffer A and write disjoint nodes of B),
+// and `st` waits for it before the shell H pass.
+struct FusedFork {
+    cudaStream_t aux;
+    cudaEvent_t fork, join;
+};
 cudaError_t launch_fused(const FusedMaps& maps, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo,
-                         const PsiSet& psi_in, const PsiSet& psi_out, long long m, const FusedWork& w, cudaStream_t st);
+                         const PsiSet& psi_in, const PsiSet& psi_out, long long m, const FusedWork& w, cudaStream_t st,
+                         const FusedFork* fork = nullptr);
 // encode_fn: the driver's cuTensorMapEncodeTiled. Returns 0 on success.
 int encode_fused_maps(FusedMaps* out, const DeviceGrid& g, float* const h[3], float* const e[3], const uint16_t* rec,
                       void* encode_fn);

@@ -51,51 +51,66 @@ __device__ __forceinline__ bool shell_node(const int4& it, const DeviceGrid& g, 
     return tx < ((it.w >> 4) & 511) && ty < ((it.w >> 13) & 511) && i < g.nx && j < g.ny;
 }
 
-// kSlabs: the CPML slabs (bit 0 x, 1 y, 2 z) the items' nodes may lie in (one instantiation per
-// shell list, yee_kernels.h); the other slab tests compile out.
+// One launch per pass covers the three shell lists (yee_kernels.h), which lie one after the other
+// in device memory: a block takes the instantiation of its list, kSlabs = the CPML slabs (bit 0 x,
+// 1 y, 2 z) its nodes may lie in, so the other slab tests compile out of that list's code. One
+// launch, not one per list, since small grids are bound by the chain of launches.
 template <typename Idx, int kSlabs>
-__global__ void __launch_bounds__(256, FDTD_SHELL_MIN_BLOCKS) k_shell_e(const __grid_constant__ StepParams p, FieldPtrs fi, FieldPtrs fo,
-                                                 const __grid_constant__ PsiSet pin, const __grid_constant__ PsiSet pout,
-                                                 const int4* __restrict__ items, long long m) {
+__device__ __forceinline__ void shell_e_item(const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo,
+                                             const PsiSet& pin, const PsiSet& pout, const int4& it, long long m) {
     int i, j;
-    const int4 it = items[blockIdx.x];
     if (!shell_node(it, p.g, i, j)) return;
     for (int k = it.z, k1 = it.z + ((it.w >> 22) & 15); k <= k1; ++k)
         e_node_global<false, false, false, Idx, kSlabs>(p, fi, fo, pin, pout, i, j, k, m);
 }
-
 template <typename Idx, int kSlabs>
-__global__ void __launch_bounds__(256, FDTD_SHELL_MIN_BLOCKS) k_shell_h(const __grid_constant__ StepParams p, FieldPtrs fi, FieldPtrs fo,
-                                                 const __grid_constant__ PsiSet pin, const __grid_constant__ PsiSet pout,
-                                                 const int4* __restrict__ items, long long m) {
+__device__ __forceinline__ void shell_h_item(const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo,
+                                             const PsiSet& pin, const PsiSet& pout, const int4& it, long long m) {
     int i, j;
-    const int4 it = items[blockIdx.x];
     if (!shell_node(it, p.g, i, j)) return;
     for (int k = it.z, k1 = it.z + ((it.w >> 22) & 15); k <= k1; ++k)
         h_node_global<false, Idx, kSlabs>(p, fi, fo, fo, pin, pout, i, j, k, m);
 }
 
-template <typename Idx, int kSlabs>
-void shell_list(bool e_pass, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
-                const PsiSet& pout, const int4* items, int n, long long m, cudaStream_t st) {
-    if (n <= 0) return;
-    const dim3 b(32, 8, 1);
-    if (e_pass) k_shell_e<Idx, kSlabs><<<n, b, 0, st>>>(p, fi, fo, pin, pout, items, m);
-    else k_shell_h<Idx, kSlabs><<<n, b, 0, st>>>(p, fi, fo, pin, pout, items, m);
+// n_z, n_yz: the item counts of the first two lists (blocks beyond them take the third).
+template <typename Idx>
+__global__ void __launch_bounds__(256, FDTD_SHELL_MIN_BLOCKS) k_shell_e(const __grid_constant__ StepParams p, FieldPtrs fi, FieldPtrs fo,
+                                                 const __grid_constant__ PsiSet pin, const __grid_constant__ PsiSet pout,
+                                                 const int4* __restrict__ items, int n_z, int n_yz, long long m) {
+    const int b = blockIdx.x;
+    const int4 it = items[b];
+    if (b < n_z) shell_e_item<Idx, 4>(p, fi, fo, pin, pout, it, m);
+    else if (b < n_z + n_yz) shell_e_item<Idx, 6>(p, fi, fo, pin, pout, it, m);
+    else shell_e_item<Idx, 7>(p, fi, fo, pin, pout, it, m);
 }
 
 template <typename Idx>
-void shell_lists(bool e_pass, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
-                 const PsiSet& pout, const ShellWork& w, long long m, cudaStream_t st) {
-    shell_list<Idx, 4>(e_pass, p, fi, fo, pin, pout, w.items[kShellZ], w.n[kShellZ], m, st);
-    shell_list<Idx, 6>(e_pass, p, fi, fo, pin, pout, w.items[kShellYZ], w.n[kShellYZ], m, st);
-    shell_list<Idx, 7>(e_pass, p, fi, fo, pin, pout, w.items[kShellAny], w.n[kShellAny], m, st);
+__global__ void __launch_bounds__(256, FDTD_SHELL_MIN_BLOCKS) k_shell_h(const __grid_constant__ StepParams p, FieldPtrs fi, FieldPtrs fo,
+                                                 const __grid_constant__ PsiSet pin, const __grid_constant__ PsiSet pout,
+                                                 const int4* __restrict__ items, int n_z, int n_yz, long long m) {
+    const int b = blockIdx.x;
+    const int4 it = items[b];
+    if (b < n_z) shell_h_item<Idx, 4>(p, fi, fo, pin, pout, it, m);
+    else if (b < n_z + n_yz) shell_h_item<Idx, 6>(p, fi, fo, pin, pout, it, m);
+    else shell_h_item<Idx, 7>(p, fi, fo, pin, pout, it, m);
 }
 
 cudaError_t launch_shell(bool e_pass, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
                          const PsiSet& pout, const ShellWork& w, long long m, cudaStream_t st) {
-    if (p.g.plane * (long long)(p.g.nz + 1) < (1LL << 31)) shell_lists<uint32_t>(e_pass, p, fi, fo, pin, pout, w, m, st);
-    else shell_lists<long long>(e_pass, p, fi, fo, pin, pout, w, m, st);
+    const int n = w.n[kShellZ] + w.n[kShellYZ] + w.n[kShellAny];
+    if (n <= 0) return cudaSuccess;
+    if (w.items[kShellYZ] != w.items[kShellZ] + w.n[kShellZ] || w.items[kShellAny] != w.items[kShellYZ] + w.n[kShellYZ])
+        return cudaErrorInvalidValue;  // the lists must be contiguous
+    const dim3 b(32, 8, 1);
+    const int nz = w.n[kShellZ], nyz = w.n[kShellYZ];
+    const int4* items = w.items[kShellZ];
+    if (p.g.plane * (long long)(p.g.nz + 1) < (1LL << 31)) {
+        if (e_pass) k_shell_e<uint32_t><<<n, b, 0, st>>>(p, fi, fo, pin, pout, items, nz, nyz, m);
+        else k_shell_h<uint32_t><<<n, b, 0, st>>>(p, fi, fo, pin, pout, items, nz, nyz, m);
+    } else {
+        if (e_pass) k_shell_e<long long><<<n, b, 0, st>>>(p, fi, fo, pin, pout, items, nz, nyz, m);
+        else k_shell_h<long long><<<n, b, 0, st>>>(p, fi, fo, pin, pout, items, nz, nyz, m);
+    }
     return cudaGetLastError();
 }
 
