@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-hbm", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 error record (profiling runs)")
     return ap.parse_args()
 
 
@@ -572,7 +573,7 @@ def main():
     if rank == 0:
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline()
-        if world == 1:
+        if world == 1 and not args.no_fp64:
             out["fp64_error"] = fp64_error()
         if not args.no_adjoint and world == 1:
             out["adjoint"] = bench_adjoint()
