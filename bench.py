@@ -40,7 +40,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", choices=["512", "256", "64", "hbm"], default="512")
-    ap.add_argument("--schedule", type=int, default=0, help="0 auto, 1 two-pass, 2 fused")
+    ap.add_argument("--schedule", type=int, default=0,
+                    help="0 auto, 1 two-pass, 2 fused, 3 fused with the CPML sweep (not chosen by auto)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
@@ -265,6 +266,8 @@ FUSED_DRAM_BYTES_PER_CELL = {"512": 62.46, "256": 72.77}
 
 
 def measured_traffic(schedule, cells, config):
+    if schedule == 3:
+        return None  # not profiled
     if schedule == 2:
         per_cell = FUSED_DRAM_BYTES_PER_CELL.get(config, FUSED_DRAM_BYTES_PER_CELL["512"])
     else:
@@ -292,7 +295,8 @@ def bench_ours(args, rank, world):
     sim.step(args.warmup)
     sim.synchronize()
     active = sim.active_schedule
-    launches_per_step = 3 if active == 2 else 2  # fused: shell E, sweep, shell H; two-pass: E and H
+    # fused: shell E, sweep, shell H (and the CPML sweep); two-pass: E and H
+    launches_per_step = {2: 3, 3: 4}.get(active, 2)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     clocks = ClockSampler(torch.cuda.current_device())
@@ -321,7 +325,7 @@ def bench_ours(args, rank, world):
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (seeded random-box scenario)",
            "config": {"workload": desc, "cells": N, "grid": [sc.nx, sc.ny, sc.nz], "cpml": 10,
-                      "schedule": {0: "auto", 1: "two-pass", 2: "fused"}[args.schedule] +
+                      "schedule": {0: "auto", 1: "two-pass", 2: "fused", 3: "fused-cpml"}[args.schedule] +
                                   (" (fused)" if args.schedule == 0 and active == 2 else
                                    " (two-pass)" if args.schedule == 0 else ""),
                       "l2": "inputs larger than L2 (fields 24 B/cell x 134M cells)", "parallelism": f"replicas{world}"},
@@ -429,7 +433,8 @@ def bench_hbm(warmup=3, steps=20):
     achieved = B * sc.cells / (ms * 1e-3) / 1e9
     return {"workload": desc, "grid": [sc.nx, sc.ny, sc.nz], "cells": sc.cells, "steps": steps, "warmup": warmup,
             "value": round(sc.cells / (ms * 1e-3) / 1e9, 3), "unit": "Gcell-updates/s", "ms_per_step": round(ms, 4),
-            "schedule": {1: "two-pass", 2: "fused"}.get(active, str(active)), "device_gb": round(dev_bytes / 1e9, 2),
+            "schedule": {1: "two-pass", 2: "fused", 3: "fused-cpml"}.get(active, str(active)),
+            "device_gb": round(dev_bytes / 1e9, 2),
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "bytes_per_cell_update": round(B, 3),
                          "peak_source": peak_kind},

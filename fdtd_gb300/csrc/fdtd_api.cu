@@ -85,10 +85,11 @@ struct fdtd_handle {
     int cur = 0;
     bool have_second = false;
     FusedMaps maps[2];
+    CpmlMaps cmaps[2];  // the CPML sweep's maps per input buffer
     FusedFork fork{};  // second stream and events of the fused step (created with the fused buffers)
     int kc = 0;  // planes per CTA chunk of the fused sweep
     FusedWork work{};
-    bool replan = false;  // the design region changed since the fused work was planned
+    bool replan = false;  // the design region or the CPML-sweep choice changed since the fused work was planned
     uint8_t* mat = nullptr;
     uint8_t* cls = nullptr;  // node classes, built by ensure_prepared
     uint16_t* rec = nullptr;          // coefficient row per node, built with the classes
@@ -172,7 +173,7 @@ struct fdtd_handle {
     // on first use; each call uploads it into the scratch with one asynchronous copy
     int4* static_items = nullptr;
     size_t static_n_items = 0;
-    int static_counts[4] = {};     // items per list (interior, then the three shell lists)
+    int static_counts[6] = {};     // items per list (interior, the four shell lists, CPML items)
     bool static_planned = false;
 
     std::vector<size_t> alloc_sizes;  // bytes of each entry of allocs
@@ -307,12 +308,14 @@ PlanGrid plan_grid(const DeviceGrid& g) {
     return PlanGrid{g.nx, g.ny, g.nz, g.pxn, g.pxp, g.pyn, g.pyp, g.pzn, g.pzp};
 }
 
-// The lists of a plan one after the other (interior, then the shell lists) and their counts.
-constexpr int kWorkLists = 1 + kPlanShellLists;
-static_assert(kWorkLists == 4, "fdtd_handle::static_counts holds one count per work list");
+// The lists of a plan one after the other (interior, the shell lists, the CPML items) and their
+// counts.
+constexpr int kWorkLists = 2 + kPlanShellLists;
+static_assert(kWorkLists == 6, "fdtd_handle::static_counts holds one count per work list");
 std::vector<PlanItem> flatten(const FusedPlan& plan, int counts[kWorkLists]) {
     std::vector<PlanItem> all;
-    const std::vector<PlanItem>* lists[kWorkLists] = {&plan.interior, &plan.shell[0], &plan.shell[1], &plan.shell[2]};
+    const std::vector<PlanItem>* lists[kWorkLists] = {&plan.interior, &plan.shell[0], &plan.shell[1], &plan.shell[2],
+                                                      &plan.shell[3], &plan.cpml};
     for (int q = 0; q < kWorkLists; ++q) {
         counts[q] = (int)lists[q]->size();
         all.insert(all.end(), lists[q]->begin(), lists[q]->end());
@@ -323,7 +326,7 @@ std::vector<PlanItem> flatten(const FusedPlan& plan, int counts[kWorkLists]) {
 // The work lists over a device copy of the flattened plan.
 FusedWork work_of(const int4* d, const int counts[kWorkLists]) {
     static_assert(kShellLists == kPlanShellLists && kShellZ == kPlanShellZ && kShellYZ == kPlanShellYZ &&
-                      kShellAny == kPlanShellAny,
+                      kShellX == kPlanShellX && kShellAny == kPlanShellAny,
                   "planner and shell kernels agree on the shell lists");
     FusedWork w{};
     w.interior = d;
@@ -334,14 +337,17 @@ FusedWork work_of(const int4* d, const int counts[kWorkLists]) {
         w.shell.n[q] = counts[1 + q];
         at += counts[1 + q];
     }
+    w.cpml = at;
+    w.n_cpml = counts[1 + kShellLists];
     return w;
 }
 
-// Work items of the fused schedule (planner.cpp). The design region, if any, stays with the shell;
-// planned again when it changes.
+// Work items of the fused schedule (planner.cpp), with CPML items under FDTD_SCHEDULE_FUSED_CPML.
+// The design region, if any, stays with the shell; planned again when it or the schedule changes.
 int plan_work(fdtd_handle* h) {
     FusedPlan plan;
-    plan_fused(plan_grid(h->g), h->kc, h->has_design ? h->dbox : nullptr, plan);
+    plan_fused(plan_grid(h->g), h->kc, h->has_design ? h->dbox : nullptr, plan,
+               h->schedule == FDTD_SCHEDULE_FUSED_CPML);
     int counts[kWorkLists];
     const std::vector<PlanItem> all = flatten(plan, counts);
     h->release((void*)h->work.interior);
@@ -370,7 +376,8 @@ int ensure_fused(fdtd_handle* h) {
     for (int b = 0; b < 2; ++b) {
         float* hh[3] = {h->field[b][3], h->field[b][4], h->field[b][5]};
         float* ee[3] = {h->field[b][0], h->field[b][1], h->field[b][2]};
-        if (encode_fused_maps(&h->maps[b], h->g, hh, ee, h->rec, enc) != 0)
+        if (encode_fused_maps(&h->maps[b], h->g, hh, ee, h->rec, enc) != 0 ||
+            encode_cpml_maps(&h->cmaps[b], h->g, hh, ee, h->rec, h->psi[b], enc) != 0)
             return fail(FDTD_ERR_CUDA, "tensor map encoding failed");
     }
     CUDA_TRY(fused_configure());
@@ -391,7 +398,7 @@ int ensure_fused(fdtd_handle* h) {
 
 // AUTO runs two-pass until a trial on the handle's own grid has chosen (auto_trial).
 bool use_fused(const fdtd_handle* h) {
-    return h->schedule == FDTD_SCHEDULE_FUSED ||
+    return h->schedule == FDTD_SCHEDULE_FUSED || h->schedule == FDTD_SCHEDULE_FUSED_CPML ||
            (h->schedule == FDTD_SCHEDULE_AUTO && h->auto_choice == FDTD_SCHEDULE_FUSED);
 }
 
@@ -518,7 +525,9 @@ int fdtd_set_stream(fdtd_handle* h, void* s) {
 
 int fdtd_set_schedule(fdtd_handle* h, int32_t schedule) {
     if (!h) return fail(FDTD_ERR_INVALID, "handle is NULL");
-    if (schedule < FDTD_SCHEDULE_AUTO || schedule > FDTD_SCHEDULE_FUSED) return fail(FDTD_ERR_INVALID, "unknown schedule");
+    if (schedule < FDTD_SCHEDULE_AUTO || schedule > FDTD_SCHEDULE_FUSED_CPML)
+        return fail(FDTD_ERR_INVALID, "unknown schedule");
+    if ((schedule == FDTD_SCHEDULE_FUSED_CPML) != (h->schedule == FDTD_SCHEDULE_FUSED_CPML)) h->replan = true;
     h->schedule = schedule;
     h->auto_choice = FDTD_SCHEDULE_AUTO;  // AUTO runs its trial again
     return FDTD_OK;
@@ -688,7 +697,7 @@ int steps_fused(fdtd_handle* h, const StepParams& p, int64_t n) {
         FieldPtrs fi{h->field[a][0], h->field[a][1], h->field[a][2], h->field[a][3], h->field[a][4], h->field[a][5]};
         FieldPtrs fo{h->field[b][0], h->field[b][1], h->field[b][2], h->field[b][3], h->field[b][4], h->field[b][5]};
         CUDA_TRY(launch_fused(h->maps[a], p, fi, fo, h->psi[a], h->psi[b], h->step, h->work, h->stream,
-                              h->fork.aux ? &h->fork : nullptr));
+                              h->fork.aux ? &h->fork : nullptr, &h->cmaps[a]));
         h->cur = b;
         ++h->step;
     }
@@ -1127,9 +1136,9 @@ int build_plates(fdtd_handle* h) {
     return FDTD_OK;
 }
 
-// Interface rows (kInterfaceNode nodes): gather the seven-cell keys, sort and unique them here,
-// then write each node's coefficient row and the rows themselves. Runs after the node classes and
-// plates are final.
+// Interface rows (kInterfaceNode and kGeneral nodes): gather the seven-cell keys, sort and unique
+// them here, then write each node's coefficient row and the rows themselves. Runs after the node
+// classes and plates are final.
 int build_interface_rows(fdtd_handle* h) {
     const DeviceGrid& g = h->g;
     if (!h->rec) CUDA_TRY(h->alloc((void**)&h->rec, (size_t)vol(h) * sizeof(uint16_t)));
@@ -1166,6 +1175,7 @@ int build_interface_rows(fdtd_handle* h) {
                              h->stream));
     CUDA_TRY(launch_iface_rows(g, h->cls, h->mat, h->iface_table, h->iface_keys, n_rows, h->iface_slot_row, h->rec,
                                h->stream));
+    CUDA_TRY(launch_rec_general(g, h->d_lumped, h->n_lumped_edges, h->rec, h->stream));
     StepParams p{};  // the rows come from the material rows and properties only
     p.g = g;
     p.props = h->props;
@@ -1326,7 +1336,7 @@ extern "C" int fdtd_step_static_scratch(fdtd_handle* h, int64_t n) {
     if (!h->static_planned) {  // planning, as for the fused schedule; host memory only
         FusedPlan plan;
         const PlanGrid pg = plan_grid(h->g);
-        plan_fused(pg, plan_chunk(pg), h->has_design ? h->dbox : nullptr, plan);
+        plan_fused(pg, plan_chunk(pg), h->has_design ? h->dbox : nullptr, plan);  // no CPML items: shell only
         const std::vector<PlanItem> all = flatten(plan, h->static_counts);
         if (h->static_items) CUDA_TRY(cudaFreeHost(h->static_items));
         h->static_items = nullptr;

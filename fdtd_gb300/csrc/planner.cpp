@@ -74,11 +74,18 @@ int plan_chunk(const PlanGrid& g) {
 // in the block shape that wastes the fewest threads, in the list of the slabs they may touch:
 // planes outside the interior z range split into the part over the interior's x / y range (z
 // slabs only), the y bands beside it (y and z) and the x bands (any); inside the interior z range
-// the y bands over the interior's x range (y and z), the x bands (any) and left-out design tiles
-// (no slab: the z list). Grids without interior tiles are one rectangle per plane (any).
-void plan_fused(const PlanGrid& g, int kc, const int* design_box, FusedPlan& out) {
+// the y bands over the interior's x range (y and z), the x bands (x only over the swept rows, any
+// beside them) and left-out design tiles (no slab: the z list). Grids without interior tiles are
+// one rectangle per plane (any).
+// With CPML items, the planes outside the interior z range over the swept rectangle and the y
+// bands over its x range are CPML items instead of shell rectangles: per interior tile one item
+// below and one above the interior planes, and per band tile (rows from 0, and from the end of
+// the swept rectangle, the last one ending on the grid's last row) the whole column in chunks of
+// kc planes.
+void plan_fused(const PlanGrid& g, int kc, const int* design_box, FusedPlan& out, bool cpml_tiles) {
     out.interior.clear();
     for (auto& s : out.shell) s.clear();
+    out.cpml.clear();
     const int xlo = std::max(g.pxn, 1), xhi = std::min(g.nx - 1 - g.pxp, g.nx - 2);  // interior nodes, inclusive
     const int ylo = std::max(g.pyn, 1), yhi = std::min(g.ny - 1 - g.pyp, g.ny - 2);
     const int zlo = std::max(g.pzn, 1), zhi = std::min(g.nz - 1 - g.pzp, g.nz - 2);
@@ -101,8 +108,24 @@ void plan_fused(const PlanGrid& g, int kc, const int* design_box, FusedPlan& out
     const bool swept = !xs.empty() && !ys.empty();
     const int X0 = swept ? xs.front() : 0, X1 = swept ? xs.back() + kTileX : 0;
     const int Y0 = swept ? ys.front() : 0, Y1 = swept ? ys.back() + kTileY : 0;
+    const bool cpml = cpml_tiles && swept && design_box == nullptr && g.ny >= kTileY &&
+                      std::max(std::max(g.pyn, g.pyp), std::max(g.pzn, g.pzp)) <= kCpmlMaxSlab;
+    if (cpml) {
+        for (int y0 : ys)
+            for (int x0 : xs) {
+                out.cpml.push_back(PlanItem{x0, y0, 0, zlo});
+                out.cpml.push_back(PlanItem{x0, y0, zhi, g.nz});
+            }
+        std::vector<int> bands;  // the low band's last tile ends on row Y0, the high band's first starts on Y1
+        for (int y1 = Y0; y1 > 0; y1 -= kTileY) bands.push_back(y1 - kTileY);
+        for (int y0 = Y1; y0 < g.ny; y0 += kTileY) bands.push_back(y0);
+        for (int y0 : bands)
+            for (int x0 : xs)
+                for (int k = 0; k < g.nz; k += kc) out.cpml.push_back(PlanItem{x0, y0, k, std::min(k + kc, g.nz)});
+    }
     std::vector<PlanItem>& sz = out.shell[kPlanShellZ];
     std::vector<PlanItem>& syz = out.shell[kPlanShellYZ];
+    std::vector<PlanItem>& sx = out.shell[kPlanShellX];
     std::vector<PlanItem>& sany = out.shell[kPlanShellAny];
     // runs of up to kShellPlanes planes with the same rectangles share items
     for (int k = 0; k < g.nz;) {
@@ -112,11 +135,22 @@ void plan_fused(const PlanGrid& g, int kc, const int* design_box, FusedPlan& out
         if (!swept) {
             shell_rect(sany, 0, 0, g.nx, g.ny, k, nk);
         } else {
-            if (caps) shell_rect(sz, X0, Y0, X1 - X0, Y1 - Y0, k, nk);
-            shell_rect(syz, X0, 0, X1 - X0, Y0, k, nk);
-            shell_rect(syz, X0, Y1, X1 - X0, g.ny - Y1, k, nk);
-            shell_rect(sany, 0, 0, X0, g.ny, k, nk);
-            shell_rect(sany, X1, 0, g.nx - X1, g.ny, k, nk);
+            if (caps && !cpml) shell_rect(sz, X0, Y0, X1 - X0, Y1 - Y0, k, nk);
+            if (!cpml) {
+                shell_rect(syz, X0, 0, X1 - X0, Y0, k, nk);
+                shell_rect(syz, X0, Y1, X1 - X0, g.ny - Y1, k, nk);
+            }
+            if (caps) {
+                shell_rect(sany, 0, 0, X0, g.ny, k, nk);
+                shell_rect(sany, X1, 0, g.nx - X1, g.ny, k, nk);
+            } else {  // the swept rows lie outside the y slabs, the planes outside the z slabs
+                for (int x0 : {0, X1}) {
+                    const int w = x0 == 0 ? X0 : g.nx - X1;
+                    shell_rect(sany, x0, 0, w, Y0, k, nk);
+                    shell_rect(sx, x0, Y0, w, Y1 - Y0, k, nk);
+                    shell_rect(sany, x0, Y1, w, g.ny - Y1, k, nk);
+                }
+            }
             if (!caps)
                 for (const PlanItem& t : left_out) shell_rect(sz, t.x, t.y, kTileX, kTileY, k, nk);
         }
@@ -127,6 +161,7 @@ void plan_fused(const PlanGrid& g, int kc, const int* design_box, FusedPlan& out
     // few on large grids
     auto by_plane = [](const PlanItem& a, const PlanItem& b) { return a.z < b.z; };
     std::stable_sort(out.interior.begin(), out.interior.end(), by_plane);
+    std::stable_sort(out.cpml.begin(), out.cpml.end(), by_plane);
     for (auto& s : out.shell) std::stable_sort(s.begin(), s.end(), by_plane);
 }
 

@@ -285,19 +285,25 @@ cudaError_t launch_node_class(const DeviceGrid& g, const uint8_t* mat, const Lum
 
 namespace fdtd {
 
-// Interface rows. Every kInterfaceNode node is keyed by its seven cell materials, packed one byte
-// each in the order (i,j,k) (i-1,j,k) (i,j-1,k) (i,j,k-1) (i-1,j-1,k) (i-1,j,k-1) (i,j-1,k-1). The
+// Interface rows. Every kInterfaceNode and kGeneral node is keyed by its seven cell materials,
+// packed one byte each in the order (i,j,k) (i-1,j,k) (i,j-1,k) (i,j,k-1) (i-1,j-1,k) (i-1,j,k-1)
+// (i,j-1,k-1), cells outside the grid as material 0 (as the general path reads them). The
 // distinct keys are collected in a hash set on the device (open addressing, linear probing), only
 // they are sorted on the host, and each of the first kMaxInterfaceRows gets the coefficient row
 // the general path would build for such a node (e_coef / h_coef: table entries where an edge's
-// cells agree, the reference's averages otherwise), so the node's update is the table form with
-// the same bits. Nodes whose key has no row take the general path, with the same bits too.
+// cells agree, the reference's averages otherwise), so an interior node's update is the table
+// form with the same bits. Interior nodes whose key has no row take the general path, with the
+// same bits too. The rows of nodes in CPML slabs or on boundary planes (classes kGeneral and
+// kUniformGeneral + m) serve the CPML sweep, which divides the curl coefficients by the CPML
+// kappa and applies the boundary rules itself; the per-node kernels keep their general path for
+// those nodes. Lumped edges get no row (launch_rec_general).
 namespace {
-__device__ __forceinline__ unsigned long long cell_key(const uint8_t* mat, const DeviceGrid& g, long long n) {
-    const long long R = g.pitch, P = g.plane;  // interior nodes: every neighbour cell exists
-    return (unsigned long long)mat[n] | (unsigned long long)mat[n - 1] << 8 | (unsigned long long)mat[n - R] << 16 |
-           (unsigned long long)mat[n - P] << 24 | (unsigned long long)mat[n - 1 - R] << 32 |
-           (unsigned long long)mat[n - 1 - P] << 40 | (unsigned long long)mat[n - R - P] << 48;
+__device__ __forceinline__ unsigned long long cell_key(const uint8_t* mat, const DeviceGrid& g, int i, int j, int k) {
+    const long long R = g.pitch, P = g.plane, n = (long long)k * P + (long long)j * R + i;
+    const unsigned long long m0 = mat[n], mi = i > 0 ? mat[n - 1] : 0, mj = j > 0 ? mat[n - R] : 0;
+    const unsigned long long mk = k > 0 ? mat[n - P] : 0, mij = (i > 0 && j > 0) ? mat[n - 1 - R] : 0;
+    const unsigned long long mik = (i > 0 && k > 0) ? mat[n - 1 - P] : 0, mjk = (j > 0 && k > 0) ? mat[n - R - P] : 0;
+    return m0 | mi << 8 | mj << 16 | mk << 24 | mij << 32 | mik << 40 | mjk << 48;
 }
 constexpr unsigned long long kEmptyKey = ~0ull;  // keys use 56 bits
 constexpr int kMaxProbes = 64;
@@ -316,7 +322,7 @@ __device__ __forceinline__ int find_slot(const unsigned long long* __restrict__ 
 }
 }  // namespace
 
-// Insert the key of every kInterfaceNode node into the set while it holds fewer than
+// Insert the key of every kInterfaceNode or kGeneral node into the set while it holds fewer than
 // kIfaceTableSize / 2 keys (*filled counts them, a few more may land while it reaches that); a key
 // that finds no room stays out (its nodes take the general path).
 __global__ void k_iface_insert(const uint8_t* __restrict__ cls, const uint8_t* __restrict__ mat, DeviceGrid g,
@@ -326,8 +332,8 @@ __global__ void k_iface_insert(const uint8_t* __restrict__ cls, const uint8_t* _
     const int k = blockIdx.z;
     if (i >= g.nx || j >= g.ny) return;
     const long long n = (long long)k * g.plane + (long long)j * g.pitch + i;
-    if (cls[n] != kInterfaceNode) return;
-    const unsigned long long key = cell_key(mat, g, n);
+    if (cls[n] != kInterfaceNode && cls[n] != kGeneral) return;
+    const unsigned long long key = cell_key(mat, g, i, j, k);
     unsigned s = slot_of(key);
     for (int q = 0; q < kMaxProbes; ++q, s = (s + 1) & (kIfaceTableSize - 1)) {
         const unsigned long long v = *(volatile unsigned long long*)(table + s);
@@ -360,9 +366,10 @@ __global__ void k_iface_slot_rows(const unsigned long long* __restrict__ table, 
     if (s >= 0) slot_row[s] = q;
 }
 
-// Coefficient rows of every node (StepParams::rec): the material id of fast-path nodes, the
-// interface row of kInterfaceNode nodes whose key has one, and kRecGeneral | class for the rest.
-// kInterfaceNode nodes without a row become kGeneral.
+// Coefficient rows of every node (StepParams::rec): the material id of fast-path nodes and of
+// kUniformGeneral + m nodes (m), the interface row of kInterfaceNode and kGeneral nodes whose key
+// has one, and kRecGeneral | class for the rest. kInterfaceNode nodes without a row become
+// kGeneral.
 __global__ void k_iface_rows(uint8_t* __restrict__ cls, const uint8_t* __restrict__ mat, DeviceGrid g,
                              const unsigned long long* __restrict__ table, const int* __restrict__ slot_row,
                              uint16_t* __restrict__ rec) {
@@ -375,17 +382,32 @@ __global__ void k_iface_rows(uint8_t* __restrict__ cls, const uint8_t* __restric
     int r = kRecGeneral | c;
     if (c < kUniformGeneral) {
         r = c;
-    } else if (c == kInterfaceNode) {
-        const int s = find_slot(table, cell_key(mat, g, n));
+    } else if (c < kInterfaceNode) {
+        r = c - kUniformGeneral;
+    } else if (c == kInterfaceNode || c == kGeneral) {
+        const int s = find_slot(table, cell_key(mat, g, i, j, k));
         const int row = s >= 0 ? slot_row[s] : -1;
         if (row >= 0) {
             r = kFirstInterfaceRow + row;
-        } else {
+        } else if (c == kInterfaceNode) {
             cls[n] = kGeneral;
             r = kRecGeneral | kGeneral;
         }
     }
     rec[n] = (uint16_t)r;
+}
+
+// Lumped edges keep the general path in every schedule (their E update is the lumped override).
+__global__ void k_rec_general(uint16_t* rec, DeviceGrid g, const LumpedEdge* edges, int n_edges) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < n_edges)
+        rec[(long long)edges[q].k * g.plane + (long long)edges[q].j * g.pitch + edges[q].i] = (uint16_t)(kRecGeneral | kGeneral);
+}
+
+cudaError_t launch_rec_general(const DeviceGrid& g, const LumpedEdge* edges, int n_edges, uint16_t* rec, cudaStream_t st) {
+    if (n_edges <= 0) return cudaSuccess;
+    k_rec_general<<<(n_edges + 127) / 128, 128, 0, st>>>(rec, g, edges, n_edges);
+    return cudaGetLastError();
 }
 
 // Coefficient row kFirstInterfaceRow + q of unique key q, from the material rows and properties.
@@ -397,7 +419,8 @@ __global__ void k_iface_coefs(const __grid_constant__ StepParams p, const unsign
     const int m0 = (int)(key & 0xff), mi = (int)((key >> 8) & 0xff), mj = (int)((key >> 16) & 0xff);
     const int mk = (int)((key >> 24) & 0xff), mij = (int)((key >> 32) & 0xff), mik = (int)((key >> 40) & 0xff);
     const int mjk = (int)((key >> 48) & 0xff);
-    // interior node: no design cells (those nodes are kDesignNode), no CPML, no boundary face
+    // position-free coefficients: no design cells (those nodes are kDesignNode); CPML kappa and
+    // boundary faces are the CPML sweep's
     const Coef3 ex = e_coef(p, 0, m0 == mj && m0 == mk && m0 == mjk, m0, mj, mk, mjk, 1, 1, 1);
     const Coef3 ey = e_coef(p, 1, m0 == mi && m0 == mk && m0 == mik, m0, mi, mk, mik, 1, 1, 1);
     const Coef3 ez = e_coef(p, 2, m0 == mi && m0 == mj && m0 == mij, m0, mi, mj, mij, 1, 1, 1);

@@ -382,26 +382,534 @@ k_sweep_interior(const __grid_constant__ FusedMaps maps, const __grid_constant__
     }
 }
 
+
+// ---- CPML sweep ----------------------------------------------------------------------------
+// The z-march of k_sweep_interior over columns whose x range (E halo included) is interior but
+// whose planes or rows may lie in the z or y CPML slabs or on the boundary planes and rows: the
+// planes below and above the interior z range of every interior tile, and the y bands beside the
+// swept rectangle. Per plane step it computes E(k) and H(k-1) as the interior sweep does, with
+// the rules of e_update / h_update that such nodes need, decided per plane (z slab, boundary
+// plane) and per row (y slab, boundary row):
+//   * the coefficients come from the node's coefficient row (the material row of nodes of one
+//     material, the row of its seven-cell key otherwise); a curl coefficient along a CPML axis is
+//     divided by that axis' kappa here (the same correctly rounded division the general path and
+//     the background tables make, so the same bits); the H faces on the low boundary plane / row
+//     take the default entry;
+//   * the CPML memory of the y and z faces streams through a two-slot shared-memory ring filled by
+//     TMA with the plane's tiles (slot k & 1: psi of E(k) and of H(k-1)); the new values go to
+//     buffer B with the fields;
+//   * components the boundary masks keep are copied;
+//   * nodes without a coefficient row (lumped edges, plates, interface keys beyond the table)
+//     take e_update / h_update out of line on their neighbourhood from the ring.
+namespace {
+
+template <class T>
+struct CpmlLayout {
+    static constexpr int PE_BYTES = round128(T::EW * T::EH * 4);  // psi of E: an E-tile box
+    static constexpr int PH_BYTES = round128(T::TX * T::TY * 4);  // psi of H: the own nodes
+    static constexpr unsigned PE_TX = T::EW * T::EH * 4, PH_TX = T::TX * T::TY * 4;  // box bytes
+    static constexpr int AXIS_BYTES = 2 * PE_BYTES + 2 * PH_BYTES;  // E arrays 0, 1, then H arrays 0, 1
+    static constexpr int SLOT_BYTES = 2 * AXIS_BYTES;               // y face, then z face
+    static constexpr int PSI_OFF = NSTAGE * T::STAGE_BYTES;
+    static constexpr int ENEW_OFF = PSI_OFF + 2 * SLOT_BYTES;
+    static constexpr int BAR_OFF = ENEW_OFF + T::ENEW_BYTES;
+    static constexpr int SMEM = BAR_OFF + NSTAGE * 8 + kMaxItemPlanes;
+};
+using CpmlW = CpmlLayout<TileW>;
+
+#ifndef FDTD_CPML_MIN_BLOCKS
+#define FDTD_CPML_MIN_BLOCKS 2
+#endif
+
+// z side of plane q: 0 / 1 inside the low / high z slab, -1 outside (or outside the grid).
+__device__ __forceinline__ int z_side(const DeviceGrid& g, int q) {
+    if (q < 0 || q >= g.nz) return -1;
+    return q < g.pzn ? 0 : q >= g.nz - g.pzp ? 1 : -1;
+}
+
+// Per plane: the E (or H) rules of plane q.
+struct CPlane {
+    int zs;             // z face side, -1 outside the z slabs
+    bool in, lt, low;   // 0 < q < nz - 1; q < nz - 1; q == 0
+    float kap, b, a;    // kappa, b, a of the plane (E or H profiles) when zs >= 0
+    float t0, t1;       // the background's kappa-divided z curl coefficients (E: Ex, Ey; H: Hx, Hy)
+    int kz;             // plane index within its z face
+};
+__device__ __forceinline__ CPlane c_plane(const StepParams& p, int q, bool h) {
+    const DeviceGrid& g = p.g;
+    CPlane r;
+    r.zs = z_side(g, q);
+    r.in = q > 0 && q < g.nz - 1;
+    r.lt = q < g.nz - 1;
+    r.low = q == 0;
+    r.kz = r.zs == 1 ? q - (g.nz - g.pzp) : q;
+    r.kap = r.b = r.a = r.t0 = r.t1 = 0.f;
+    if (r.zs >= 0) {
+        r.kap = __ldg((h ? p.kmz : p.kez) + q);
+        r.b = __ldg((h ? p.bmz : p.bez) + q);
+        r.a = __ldg((h ? p.amz : p.aez) + q);
+        r.t0 = __ldg((h ? p.bg.h[2][0] : p.bg.e[2][0]) + q);
+        r.t1 = __ldg((h ? p.bg.h[2][1] : p.bg.e[2][1]) + q);
+    }
+    return r;
+}
+// Per row j of a tile whose rows meet the y face yside (-1: none): the E and H rules of the row.
+struct CRow {
+    bool ok, ys, in, lt, low;   // row of the grid; in the tile's y slab; 0 < j < ny - 1; j < ny - 1; j == 0
+    float ke, be, ae, km, bm, am;
+    float te0, te1, th0, th1;   // the background's kappa-divided y curl coefficients (Ex, Ez; Hx, Hz)
+    int jy;                     // row within its y face
+};
+__device__ __forceinline__ CRow c_row(const StepParams& p, int j, int yside) {
+    const DeviceGrid& g = p.g;
+    CRow r;
+    r.ok = j >= 0 && j < g.ny;
+    r.ys = yside >= 0 && r.ok && in_slab(j, g.ny, g.pyn, g.pyp) && (j < g.pyn ? 0 : 1) == yside;
+    r.in = j > 0 && j < g.ny - 1;
+    r.lt = j < g.ny - 1;
+    r.low = j == 0;
+    r.jy = j < g.pyn ? j : j - (g.ny - g.pyp);
+    r.ke = r.be = r.ae = r.km = r.bm = r.am = r.te0 = r.te1 = r.th0 = r.th1 = 0.f;
+    if (r.ys) {
+        r.ke = __ldg(p.key + j); r.be = __ldg(p.bey + j); r.ae = __ldg(p.aey + j);
+        r.km = __ldg(p.kmy + j); r.bm = __ldg(p.bmy + j); r.am = __ldg(p.amy + j);
+        r.te0 = __ldg(p.bg.e[1][0] + j); r.te1 = __ldg(p.bg.e[1][1] + j);
+        r.th0 = __ldg(p.bg.h[1][0] + j); r.th1 = __ldg(p.bg.h[1][1] + j);
+    }
+    return r;
+}
+
+// psi tiles of one ring slot for the current plane step: E arrays (E-tile index), H arrays (own
+// index), for the y and the z face.
+struct CPsi {
+    const float *ey0, *ey1, *hy0, *hy1, *ez0, *ez1, *hz0, *hz1;
+};
+__device__ __forceinline__ CPsi c_psi(const unsigned char* slot) {
+    using L = CpmlW;
+    CPsi r;
+    const unsigned char* y = slot;
+    const unsigned char* z = slot + L::AXIS_BYTES;
+    r.ey0 = reinterpret_cast<const float*>(y);
+    r.ey1 = reinterpret_cast<const float*>(y + L::PE_BYTES);
+    r.hy0 = reinterpret_cast<const float*>(y + 2 * L::PE_BYTES);
+    r.hy1 = reinterpret_cast<const float*>(y + 2 * L::PE_BYTES + L::PH_BYTES);
+    r.ez0 = reinterpret_cast<const float*>(z);
+    r.ez1 = reinterpret_cast<const float*>(z + L::PE_BYTES);
+    r.hz0 = reinterpret_cast<const float*>(z + 2 * L::PE_BYTES);
+    r.hz1 = reinterpret_cast<const float*>(z + 2 * L::PE_BYTES + L::PH_BYTES);
+    return r;
+}
+
+// E of a node with a coefficient row (e_update's arithmetic for nodes outside the x slabs).
+// ei: the node's E-tile index; w: store the new psi (own node of a stored plane) at global
+// offsets qy (y face yside) / qz (z face of the plane).
+__device__ __forceinline__ void e_cpml_fast(const StepParams& p, const PsiSet& pout, const EIn& a, const CPlane& zp,
+                                            const CRow& yr, int yside, const CPsi& ps, int ei, bool w, int qy, int qz,
+                                            float3& out, float3& pre) {
+    const DeviceGrid& g = p.g;
+    const MatCoef* mc = p.coef + a.c;
+    const float4 cx = __ldg(&mc->e[0]), cy = __ldg(&mc->e[1]), cz = __ldg(&mc->e[2]);
+    const bool zs = zp.zs >= 0, ys = yr.ys, bg = a.c == p.bg.mat;
+    // curl coefficients along a CPML axis over kappa: tabulated for the background row
+    float xp = cx.y, xm = cx.z, yp = cy.y, zm = cz.z;
+    if (ys) {
+        if (bg) { xp = yr.te0; zm = yr.te1; }
+        else { xp = __fdiv_rn(cx.y, yr.ke); zm = __fdiv_rn(cz.z, yr.ke); }
+    }
+    if (zs) {
+        if (bg) { xm = zp.t0; yp = zp.t1; }
+        else { xm = __fdiv_rn(cx.z, zp.kap); yp = __fdiv_rn(cy.y, zp.kap); }
+    }
+    float vx = upd3(cx.x, a.ex, xp, a.dHz_j, xm, a.dHy_k);
+    float vy = upd3(cy.x, a.ey, yp, a.dHx_k, cy.z, a.dHz_i);
+    float vz = upd3(cz.x, a.ez, cz.y, a.dHy_i, zm, a.dHx_j);
+    const bool exm = yr.in && zp.in, eym = yr.lt && zp.in, ezm = yr.in && zp.lt;
+    pre = make_float3(exm ? vx : a.ex, eym ? vy : a.ey, ezm ? vz : a.ez);
+    if (ys && (exm || ezm)) {  // fdtdrav.h:790-827
+        const PsiFace& o = pout.f[2 + yside];
+        if (exm) {
+            const float s = psi_upd(yr.be, ps.ey0[ei], yr.ae, a.dHz_j);
+            if (w) o.e[0][qy] = s;
+            vx = psi_add(vx, __fmul_rn(cx.y, g.dy), s);
+        }
+        if (ezm) {
+            const float s = psi_upd(yr.be, ps.ey1[ei], yr.ae, a.dHx_j);
+            if (w) o.e[1][qy] = s;
+            vz = psi_add(vz, __fmul_rn(cz.z, g.dy), s);
+        }
+    }
+    if (zs && (exm || eym)) {  // fdtdrav.h:829-911
+        const PsiFace& o = pout.f[4 + zp.zs];
+        if (exm) {
+            const float s = psi_upd(zp.b, ps.ez0[ei], zp.a, a.dHy_k);
+            if (w) o.e[0][qz] = s;
+            vx = psi_add(vx, __fmul_rn(cx.z, g.dz), s);
+        }
+        if (eym) {
+            const float s = psi_upd(zp.b, ps.ez1[ei], zp.a, a.dHx_k);
+            if (w) o.e[1][qz] = s;
+            vy = psi_add(vy, __fmul_rn(cy.y, g.dz), s);
+        }
+    }
+    out = make_float3(exm ? vx : a.ex, eym ? vy : a.ey, ezm ? vz : a.ez);
+}
+
+// H of a node with a coefficient row (h_update's arithmetic for nodes outside the x slabs); c:
+// the row; oi: the node's own-tile index.
+__device__ __forceinline__ void h_cpml_fast(const StepParams& p, const PsiSet& pout, const HIn& a, const CPlane& zp,
+                                            const CRow& yr, int yside, const CPsi& ps, int oi, int qy, int qz,
+                                            float3& out, float3& pre) {
+    const DeviceGrid& g = p.g;
+    const float4 cx = __ldg(&p.coef[a.c].h[0]);
+    const float4 cy = __ldg(&p.coef[yr.low ? kDefaultEntry : a.c].h[1]);  // face on the low boundary row
+    const float4 cz = __ldg(&p.coef[zp.low ? kDefaultEntry : a.c].h[2]);  // face on the low boundary plane
+    const bool zs = zp.zs >= 0, ys = yr.ys, bg = a.c == p.bg.mat;
+    // as for E; the default entries of the boundary row / plane are not the background's
+    float xp = cx.y, xm = cx.z, ym = cy.z, zp_ = cz.y;
+    if (zs) {
+        xp = bg ? zp.t0 : __fdiv_rn(cx.y, zp.kap);
+        ym = bg && !yr.low ? zp.t1 : __fdiv_rn(cy.z, zp.kap);
+    }
+    if (ys) {
+        xm = bg ? yr.th0 : __fdiv_rn(cx.z, yr.km);
+        zp_ = bg && !zp.low ? yr.th1 : __fdiv_rn(cz.y, yr.km);
+    }
+    float vx = upd3_hx(cx.x, a.hx, xp, a.dEy_k, xm, a.dEz_j);
+    float vy = upd3(cy.x, a.hy, cy.y, a.dEz_i, ym, a.dEx_k);
+    float vz = upd3(cz.x, a.hz, zp_, a.dEx_j, cz.z, a.dEy_i);
+    const bool hxm = yr.lt && zp.lt, hym = zp.lt, hzm = yr.lt;
+    pre = make_float3(hxm ? vx : a.hx, hym ? vy : a.hy, hzm ? vz : a.hz);
+    if (ys && (hxm || hzm)) {  // fdtdrav.h:445-486
+        const PsiFace& o = pout.f[2 + yside];
+        if (hxm) {
+            const float s = psi_upd(yr.bm, ps.hy0[oi], yr.am, a.dEz_j);
+            o.h[0][qy] = s;
+            vx = psi_add(vx, __fmul_rn(cx.z, g.dy), s);
+        }
+        if (hzm) {
+            const float s = psi_upd(yr.bm, ps.hy1[oi], yr.am, a.dEx_j);
+            o.h[1][qy] = s;
+            vz = psi_add(vz, __fmul_rn(cz.y, g.dy), s);
+        }
+    }
+    if (zs && (hxm || hym)) {  // fdtdrav.h:489-562
+        const PsiFace& o = pout.f[4 + zp.zs];
+        if (hxm) {
+            const float s = psi_upd(zp.b, ps.hz0[oi], zp.a, a.dEy_k);
+            o.h[0][qz] = s;
+            vx = psi_add(vx, __fmul_rn(cx.y, g.dz), s);
+        }
+        if (hym) {
+            const float s = psi_upd_hyz(zp.b, ps.hz1[oi], zp.a, a.dEx_k);
+            o.h[1][qz] = s;
+            vy = psi_add(vy, __fmul_rn(cy.z, g.dz), s);
+        }
+    }
+    out = make_float3(hxm ? vx : a.hx, hym ? vy : a.hy, hzm ? vz : a.hz);
+}
+
+// E of a node without a coefficient row: e_update on its neighbourhood from the ring (cur / prv
+// stage bases, H-tile index hi), cell materials and CPML memory from global memory (psi of buffer
+// A; the new psi stored when `write`). Plate nodes take their plate coefficients; k_plate_e
+// stores them and their psi, so neither is written here. Returns out (x, y, z) then pre.
+static __device__ __noinline__ void e_cpml_slow(const StepParams* pp, const PsiSet* pin, const PsiSet* pout,
+                                                const unsigned char* curb, const unsigned char* prvb, int hi, float ex,
+                                                float ey, float ez, int i, int j, int k, long long m, int lumped,
+                                                bool write, int cls, float* r6) {
+    const StepParams& p = *pp;
+    const DeviceGrid& g = p.g;
+    const StageView<TileW> cur(curb), prv(prvb);
+    constexpr int HW = TileW::HW;
+    ENbr nb;
+    nb.ex = ex; nb.ey = ey; nb.ez = ez;
+    nb.hx = cur.h(0)[hi]; nb.hy = cur.h(1)[hi]; nb.hz = cur.h(2)[hi];
+    nb.hx_jm = cur.h(0)[hi - HW]; nb.hx_km = prv.h(0)[hi];
+    nb.hy_im = cur.h(1)[hi - 1]; nb.hy_km = prv.h(1)[hi];
+    nb.hz_im = cur.h(2)[hi - 1]; nb.hz_jm = cur.h(2)[hi - HW];
+    const long long R = g.pitch, P = g.plane, n = (long long)k * P + (long long)j * R + i;
+    const uint8_t* mat = p.mat;
+    nb.m0 = mat[n];
+    nb.mi = mat[n - 1];  // i > 0: the column is interior
+    nb.mj = j > 0 ? mat[n - R] : 0;
+    nb.mk = k > 0 ? mat[n - P] : 0;
+    nb.mij = j > 0 ? mat[n - 1 - R] : 0;
+    nb.mik = k > 0 ? mat[n - 1 - P] : 0;
+    nb.mjk = (j > 0 && k > 0) ? mat[n - R - P] : 0;
+    const PsiIO io{pin->f, pout->f, write && cls != kPlateNode};
+    float out[3], pre[3];
+    e_update<false, false, true, false, 6>(p, nb, i, j, k, m, lumped != 0, io, out, pre);
+    r6[0] = out[0]; r6[1] = out[1]; r6[2] = out[2];
+    r6[3] = pre[0]; r6[4] = pre[1]; r6[5] = pre[2];
+}
+
+// H of a node without a coefficient row: h_update on its neighbourhood (old H from the prv stage,
+// new E of planes kh and kh + 1 from the new-E tiles, index ni), CPML memory from global memory.
+static __device__ __noinline__ void h_cpml_slow(const StepParams* pp, const PsiSet* pin, const PsiSet* pout,
+                                                const unsigned char* prvb, int hi, const float* en_prv,
+                                                const float* en_cur, int ni, int i, int j, int kh, float* r6) {
+    const StepParams& p = *pp;
+    const DeviceGrid& g = p.g;
+    const StageView<TileW> prv(prvb);
+    constexpr int NF = TileW::N_FLOATS, NW = TileW::NW;
+    HNbr nb;
+    nb.hx = prv.h(0)[hi]; nb.hy = prv.h(1)[hi]; nb.hz = prv.h(2)[hi];
+    nb.ex = en_prv[ni]; nb.ey = en_prv[NF + ni]; nb.ez = en_prv[2 * NF + ni];
+    nb.ey_kp = en_cur[NF + ni]; nb.ex_kp = en_cur[ni];
+    nb.ez_jp = en_prv[2 * NF + ni + NW]; nb.ex_jp = en_prv[ni + NW];
+    nb.ez_ip = en_prv[2 * NF + ni + 1]; nb.ey_ip = en_prv[NF + ni + 1];
+    const long long R = g.pitch, P = g.plane, n = (long long)kh * P + (long long)j * R + i;
+    const uint8_t* mat = p.mat;
+    nb.m0 = mat[n];
+    nb.mi = mat[n - 1];
+    nb.mj = j > 0 ? mat[n - R] : 0;
+    nb.mk = kh > 0 ? mat[n - P] : 0;
+    const PsiIO io{pin->f, pout->f, true};
+    float out[3], pre[3];
+    h_update<false, false, 6>(p, nb, i, j, kh, io, out, pre);
+    r6[0] = out[0]; r6[1] = out[1]; r6[2] = out[2];
+    r6[3] = pre[0]; r6[4] = pre[1]; r6[5] = pre[2];
+}
+
+}  // namespace
+
+// CPML sweep over `items` (int4 {x0, y0, k0, k1}, planner.h's CPML items: 32 x 16 columns with an
+// interior x range, planes [k0, k1) anywhere in [0, nz)). Rows outside the grid are neither
+// computed nor stored. Plane -1, plane nz and rows outside the grid load as zeros (TMA fill): the
+// coefficient row of plane nz, where E is computed for H below it, reads as 0, so those nodes take
+// the fast path; they are never stored. Every wait is bounded as in k_sweep_interior.
+__global__ void __launch_bounds__(NTH, FDTD_CPML_MIN_BLOCKS)
+k_sweep_cpml(const __grid_constant__ CpmlMaps maps, const __grid_constant__ StepParams p, FieldPtrs fo,
+             const __grid_constant__ PsiSet pin, const __grid_constant__ PsiSet pout, const int4* __restrict__ items,
+             long long m) {
+    using T = TileW;
+    using L = CpmlW;
+    constexpr int TX = T::TX, TY = T::TY, RSTEP = T::RSTEP, HW = T::HW, EW = T::EW, MW = T::MW, NW = T::NW;
+    constexpr int NF = T::N_FLOATS;
+    extern __shared__ __align__(128) unsigned char smem[];
+    float* enew = reinterpret_cast<float*>(smem + L::ENEW_OFF);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + L::BAR_OFF);
+    uint8_t* pflags = reinterpret_cast<uint8_t*>(bars + NSTAGE);  // per plane: bit 0 lumped edges, bit 1 probes
+    const DeviceGrid& g = p.g;
+    const int tid = threadIdx.x;
+    const int tx = tid % TX, ty = tid / TX;
+    const int4 it = items[blockIdx.x];
+    const int x0 = it.x, y0 = it.y, k0 = it.z, k1 = it.w;
+    const int kfirst = k0 - 1, klast = k1;
+    const long long row = m % p.ring_cap;
+    const int i = x0 + tx, j = y0 + ty;
+    const int xoff = x0 & 7;
+    const int hi = (ty + 1) * HW + tx + 4, ei = ty * EW + tx, mi = (ty + 1) * MW + tx + xoff, ni = ty * NW + tx;
+    const int oi = ty * TX + tx;
+    const bool halo = tid < T::NHALO;
+    const int hpx = tid < TX ? tid : TX, hpy = tid < TX ? TY : tid - TX;
+    const int hhi = (hpy + 1) * HW + hpx + 4, hei = hpy * EW + hpx, hmi = (hpy + 1) * MW + hpx + xoff, hni = hpy * NW + hpx;
+    const long long n_own = (long long)j * g.pitch + i;
+    const long long n_row = (long long)RSTEP * g.pitch;
+    // the tile's y face (its rows, E halo row included, meet at most one): side, first row; only a
+    // face with CPML cells has maps (maps.faces)
+    const int yside = (g.pyn > 0 && y0 < g.pyn) ? 0 : (g.pyp > 0 && y0 + TY >= g.ny - g.pyp) ? 1 : -1;
+    const int ybase = yside == 1 ? g.ny - g.pyp : 0;
+    const CRow r0 = c_row(p, j, yside), r1 = c_row(p, j + RSTEP, yside);
+    const CRow rh = c_row(p, y0 + hpy, yside);
+    // CPML memory offsets of the own nodes within a y face plane / a z face plane
+    const int qy0 = r0.jy * g.pitch + i, qy1 = r1.jy * g.pitch + i;
+    const int qz0 = j * g.pitch + i, qz1 = (j + RSTEP) * g.pitch + i;
+
+    if (tid == 0) {
+        for (int s = 0; s < NSTAGE; ++s) mbar_init(&bars[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (int q = tid; q <= klast - kfirst; q += NTH) {  // klast - kfirst < kMaxItemPlanes (planner)
+        const int k = kfirst + q;
+        pflags[q] = (k < 0 || k >= g.nz) ? 0
+                    : (p.lumped_k[k] < p.lumped_k[k + 1] ? 1 : 0) | (p.probe_k[k] < p.probe_k[k + 1] ? 2 : 0);
+    }
+    __syncthreads();
+    auto issue = [&](int k, int s) {
+        unsigned char* st = smem + s * T::STAGE_BYTES;
+        unsigned char* ps = smem + L::PSI_OFF + (k & 1) * L::SLOT_BYTES;
+        const bool ne = k >= k0, nh = k > k0;  // E(k), H(k-1) computed at this step
+        int ze = ne ? z_side(g, k) : -1, zh = nh ? z_side(g, k - 1) : -1;
+        if (ze >= 0 && !((maps.faces >> (2 + ze)) & 1)) ze = -1;
+        if (zh >= 0 && !((maps.faces >> (2 + zh)) & 1)) zh = -1;
+        const bool yok = yside >= 0 && ((maps.faces >> yside) & 1);
+        const bool ye = ne && yok, yh = nh && yok;
+        const unsigned bytes = T::TX_BYTES + (ye ? 2 * L::PE_TX : 0) + (yh ? 2 * L::PH_TX : 0) +
+                               (ze >= 0 ? 2 * L::PE_TX : 0) + (zh >= 0 ? 2 * L::PH_TX : 0);
+        mbar_expect_tx(&bars[s], bytes);
+        for (int c = 0; c < 3; ++c) tma_load_3d(st + c * T::H_BYTES, &maps.base.h[c], &bars[s], x0 - 4, y0 - 1, k);
+        for (int c = 0; c < 3; ++c) tma_load_3d(st + 3 * T::H_BYTES + c * T::E_BYTES, &maps.base.e[c], &bars[s], x0, y0, k);
+        tma_load_3d(st + 3 * T::H_BYTES + 3 * T::E_BYTES, &maps.base.rec, &bars[s], x0 - xoff, y0 - 1, k);
+        for (int a = 0; a < 2; ++a) {
+            if (ye) tma_load_3d(ps + a * L::PE_BYTES, &maps.ye[yside][a], &bars[s], x0, y0 - ybase, k);
+            if (yh) tma_load_3d(ps + 2 * L::PE_BYTES + a * L::PH_BYTES, &maps.yh[yside][a], &bars[s], x0, y0 - ybase, k - 1);
+            if (ze >= 0)
+                tma_load_3d(ps + L::AXIS_BYTES + a * L::PE_BYTES, &maps.ze[ze][a], &bars[s], x0, y0,
+                            ze == 1 ? k - (g.nz - g.pzp) : k);
+            if (zh >= 0)
+                tma_load_3d(ps + L::AXIS_BYTES + 2 * L::PE_BYTES + a * L::PH_BYTES, &maps.zh[zh][a], &bars[s], x0, y0,
+                            zh == 1 ? k - 1 - (g.nz - g.pzp) : k - 1);
+        }
+    };
+    if (tid == 0)
+        for (int q = 0; q < AHEAD && kfirst + q <= klast; ++q) issue(kfirst + q, q);
+
+    int s_cur = 0, s_prv = NSTAGE - 1, s_next = AHEAD % NSTAGE;
+    uint32_t parity = 0;
+    for (int k = kfirst; k <= klast; ++k) {
+        if (tid == 0 && k + AHEAD <= klast) {
+            fence_proxy_async();  // generic reads of the recycled stage and psi slot precede the async writes
+            issue(k + AHEAD, s_next);
+        }
+        const bool ok = mbar_wait(&bars[s_cur], parity);
+        const unsigned char* curb = smem + s_cur * T::STAGE_BYTES;
+        const unsigned char* prvb = smem + s_prv * T::STAGE_BYTES;
+        const StageView<T> cur(curb);
+        const StageView<T> prv(prvb);
+        const CPsi ps = c_psi(smem + L::PSI_OFF + (k & 1) * L::SLOT_BYTES);
+        float* en_cur = enew + (k & 1) * 3 * NF;
+        const float* en_prv = enew + ((k - 1) & 1) * 3 * NF;
+        if (k >= k0) {
+            // ---- E(k): own nodes (stored, with their psi, below plane k1), then the halo nodes ----
+            const int fl = pflags[k - kfirst];
+            const bool st = k < k1;
+            const CPlane zp = c_plane(p, k, false);
+            const int qz = zp.kz * g.ny * g.pitch;
+            const int qy = k * (yside == 1 ? g.pyp : g.pyn) * g.pitch;
+            float3 v[2], w[2];
+            bool plate[2];
+#pragma unroll
+            for (int r = 0; r < 2; ++r) {
+                const CRow& yr = r ? r1 : r0;
+                plate[r] = true;  // rows outside the grid: nothing stored
+                if (!yr.ok) continue;
+                const EIn a = e_load(cur, prv, hi + r * RSTEP * HW, ei + r * RSTEP * EW, mi + r * RSTEP * MW);
+                plate[r] = a.c == (kRecGeneral | kPlateNode);
+                if (a.c < kRecGeneral) {
+                    e_cpml_fast(p, pout, a, zp, yr, yside, ps, ei + r * RSTEP * EW, st, qy + (r ? qy1 : qy0),
+                                qz + (r ? qz1 : qz0), v[r], w[r]);
+                } else {
+                    float r6[6];
+                    e_cpml_slow(&p, &pin, &pout, curb, prvb, hi + r * RSTEP * HW, a.ex, a.ey, a.ez, i, j + r * RSTEP, k,
+                                m, fl & 1, st, a.c & 0xff, r6);
+                    v[r] = make_float3(r6[0], r6[1], r6[2]);
+                    w[r] = make_float3(r6[3], r6[4], r6[5]);
+                }
+                const int nn = ni + r * RSTEP * NW;
+                en_cur[nn] = v[r].x; en_cur[NF + nn] = v[r].y; en_cur[2 * NF + nn] = v[r].z;
+            }
+            if (st) {
+                const long long n = (long long)k * g.plane + n_own;
+#pragma unroll
+                for (int r = 0; r < 2; ++r)
+                    if (!plate[r]) store3(fo.ex, fo.ey, fo.ez, n + r * n_row, v[r]);  // k_plate_e stores plate nodes
+                if (fl & 2) {
+                    if (r0.ok) {
+                        sample(p, row, 0, i, j, k, w[0].x); sample(p, row, 1, i, j, k, w[0].y);
+                        sample(p, row, 2, i, j, k, w[0].z);
+                    }
+                    if (r1.ok) {
+                        sample(p, row, 0, i, j + RSTEP, k, w[1].x); sample(p, row, 1, i, j + RSTEP, k, w[1].y);
+                        sample(p, row, 2, i, j + RSTEP, k, w[1].z);
+                    }
+                }
+            }
+            if (halo && rh.ok) {
+                const EIn a = e_load(cur, prv, hhi, hei, hmi);
+                float3 hv, hw;
+                if (a.c < kRecGeneral) {
+                    e_cpml_fast(p, pout, a, zp, rh, yside, ps, hei, false, 0, 0, hv, hw);
+                } else {
+                    float r6[6];
+                    e_cpml_slow(&p, &pin, &pout, curb, prvb, hhi, a.ex, a.ey, a.ez, x0 + hpx, y0 + hpy, k, m, fl & 1,
+                                false, a.c & 0xff, r6);
+                    hv = make_float3(r6[0], r6[1], r6[2]);
+                }
+                en_cur[hni] = hv.x; en_cur[NF + hni] = hv.y; en_cur[2 * NF + hni] = hv.z;
+            }
+        }
+        if (k > k0) {
+            // ---- H(k-1) of the own nodes from E(k-1), E(k) and the old H(k-1) ----
+            const int kh = k - 1;
+            const CPlane zp = c_plane(p, kh, true);
+            const int qz = zp.kz * g.ny * g.pitch;
+            const int qy = kh * (yside == 1 ? g.pyp : g.pyn) * g.pitch;
+            const long long n = (long long)kh * g.plane + n_own;
+            float3 v[2], w[2];
+#pragma unroll
+            for (int r = 0; r < 2; ++r) {
+                const CRow& yr = r ? r1 : r0;
+                if (!yr.ok) continue;
+                const int nn = ni + r * RSTEP * NW;
+                const HIn a = h_load(prv, en_prv, en_cur, hi + r * RSTEP * HW, mi + r * RSTEP * MW, nn);
+                if (a.c < kRecGeneral) {
+                    h_cpml_fast(p, pout, a, zp, yr, yside, ps, oi + r * RSTEP * TX, qy + (r ? qy1 : qy0),
+                                qz + (r ? qz1 : qz0), v[r], w[r]);
+                } else {
+                    float r6[6];
+                    h_cpml_slow(&p, &pin, &pout, prvb, hi + r * RSTEP * HW, en_prv, en_cur, nn, i, j + r * RSTEP, kh, r6);
+                    v[r] = make_float3(r6[0], r6[1], r6[2]);
+                    w[r] = make_float3(r6[3], r6[4], r6[5]);
+                }
+                store3(fo.hx, fo.hy, fo.hz, n + r * n_row, v[r]);
+            }
+            if (pflags[kh - kfirst] & 2) {
+                if (r0.ok) {
+                    sample(p, row, 3, i, j, kh, w[0].x); sample(p, row, 4, i, j, kh, w[0].y);
+                    sample(p, row, 5, i, j, kh, w[0].z);
+                }
+                if (r1.ok) {
+                    sample(p, row, 3, i, j + RSTEP, kh, w[1].x); sample(p, row, 4, i, j + RSTEP, kh, w[1].y);
+                    sample(p, row, 5, i, j + RSTEP, kh, w[1].z);
+                }
+            }
+        }
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) {
+                atomic_flag(p.status, 1);
+                int s = s_cur;
+                uint32_t par = parity;
+                for (int q = k + 1; q <= min(klast, k + AHEAD); ++q) {
+                    if (++s == NSTAGE) { s = 0; par ^= 1u; }
+                    mbar_wait(&bars[s], par);
+                }
+            }
+            __syncthreads();
+            return;
+        }
+        s_prv = s_cur;
+        if (++s_cur == NSTAGE) { s_cur = 0; parity ^= 1u; }
+        if (++s_next == NSTAGE) s_next = 0;
+    }
+}
+
 int fused_smem_bytes() { return TileW::SMEM; }
+int cpml_smem_bytes() { return CpmlW::SMEM; }
 
 cudaError_t fused_configure() {
-    return cudaFuncSetAttribute(k_sweep_interior, cudaFuncAttributeMaxDynamicSharedMemorySize, TileW::SMEM);
+    cudaError_t e = cudaFuncSetAttribute(k_sweep_interior, cudaFuncAttributeMaxDynamicSharedMemorySize, TileW::SMEM);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sweep_cpml, cudaFuncAttributeMaxDynamicSharedMemorySize, CpmlW::SMEM);
+    return e;
 }
 
 // One fused step: per-node E of the shell items (CPML slabs, boundary planes, strips beside the
 // interior tiles, tiles around a design region), the design region's and the plates' E, the
-// interior sweep, per-node H of the shell items (which reads the new E of its neighbours, written
-// by the sweep). With a fork the sweep runs beside the shell E pass on the second stream.
+// interior sweep and the CPML sweep, per-node H of the shell items (which reads the new E of its
+// neighbours, written by the sweeps). With a fork the sweeps run beside the shell E pass on the
+// second stream.
 cudaError_t launch_fused(const FusedMaps& maps, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo,
                          const PsiSet& psi_in, const PsiSet& psi_out, long long m, const FusedWork& w, cudaStream_t st,
-                         const FusedFork* fork) {
+                         const FusedFork* fork, const CpmlMaps* cmaps) {
     cudaError_t e = cudaSuccess;
+    if (w.n_cpml > 0 && !cmaps) return cudaErrorInvalidValue;
     const bool split = fork && w.n_interior > 0;
     if (split) {
         e = cudaEventRecord(fork->fork, st);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(fork->aux, fork->fork, 0);
         if (e != cudaSuccess) return e;
         k_sweep_interior<<<w.n_interior, NTH, TileW::SMEM, fork->aux>>>(maps, p, fo, w.interior, m);
+        if (w.n_cpml > 0)
+            k_sweep_cpml<<<w.n_cpml, NTH, CpmlW::SMEM, fork->aux>>>(*cmaps, p, fo, psi_in, psi_out, w.cpml, m);
         e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaEventRecord(fork->join, fork->aux);
         if (e != cudaSuccess) return e;
@@ -414,6 +922,7 @@ cudaError_t launch_fused(const FusedMaps& maps, const StepParams& p, const Field
         e = cudaStreamWaitEvent(st, fork->join, 0);
     } else if (w.n_interior > 0) {
         k_sweep_interior<<<w.n_interior, NTH, TileW::SMEM, st>>>(maps, p, fo, w.interior, m);
+        if (w.n_cpml > 0) k_sweep_cpml<<<w.n_cpml, NTH, CpmlW::SMEM, st>>>(*cmaps, p, fo, psi_in, psi_out, w.cpml, m);
         e = cudaGetLastError();
     }
     if (e != cudaSuccess) return e;
@@ -455,6 +964,44 @@ int encode_tile_maps(FusedMaps* out, const DeviceGrid& g, float* const h[3], flo
 int encode_fused_maps(FusedMaps* out, const DeviceGrid& g, float* const h[3], float* const e[3], const uint16_t* rec,
                       void* encode_fn) {
     return encode_tile_maps<TileW>(out, g, h, e, rec, reinterpret_cast<EncodeFn>(encode_fn));
+}
+
+// CPML memory maps of the y faces ((nz, P, pitch) arrays) and z faces ((P, ny, pitch)): E arrays in
+// E-tile boxes, H arrays in own-node boxes. Coordinates outside an array load as zeros.
+int encode_cpml_maps(CpmlMaps* out, const DeviceGrid& g, float* const h[3], float* const e[3], const uint16_t* rec,
+                     const PsiSet& psi, void* encode_fn) {
+    using T = TileW;
+    const EncodeFn encode = reinterpret_cast<EncodeFn>(encode_fn);
+    *out = CpmlMaps{};
+    if (encode_tile_maps<T>(&out->base, g, h, e, rec, encode) != 0) return -1;
+    const cuuint32_t ebox[3] = {T::EW, T::EH, 1}, hbox[3] = {T::TX, T::TY, 1}, es[3] = {1, 1, 1};
+    auto map = [&](CUtensorMap* m, float* base, const cuuint64_t* dims, const cuuint64_t* str, const cuuint32_t* box) {
+        return encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, str, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                      CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+                       CUDA_SUCCESS
+                   ? 0
+                   : -1;
+    };
+    for (int s = 0; s < 2; ++s) {
+        const int py = s ? g.pyp : g.pyn, pz = s ? g.pzp : g.pzn;
+        if (py > 0) {
+            out->faces |= 1 << s;
+            const cuuint64_t dims[3] = {(cuuint64_t)g.pitch, (cuuint64_t)py, (cuuint64_t)g.nz};
+            const cuuint64_t str[2] = {(cuuint64_t)g.pitch * 4, (cuuint64_t)py * g.pitch * 4};
+            const PsiFace& f = psi.f[2 + s];
+            for (int a = 0; a < 2; ++a)
+                if (map(&out->ye[s][a], f.e[a], dims, str, ebox) || map(&out->yh[s][a], f.h[a], dims, str, hbox)) return -1;
+        }
+        if (pz > 0) {
+            out->faces |= 4 << s;
+            const cuuint64_t dims[3] = {(cuuint64_t)g.pitch, (cuuint64_t)g.ny, (cuuint64_t)pz};
+            const cuuint64_t str[2] = {(cuuint64_t)g.pitch * 4, (cuuint64_t)g.ny * g.pitch * 4};
+            const PsiFace& f = psi.f[4 + s];
+            for (int a = 0; a < 2; ++a)
+                if (map(&out->ze[s][a], f.e[a], dims, str, ebox) || map(&out->zh[s][a], f.h[a], dims, str, hbox)) return -1;
+        }
+    }
+    return 0;
 }
 
 }  // namespace fdtd

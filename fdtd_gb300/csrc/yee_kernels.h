@@ -38,17 +38,18 @@ cudaError_t launch_plate_e(const StepParams& p, const FieldPtrs& fi, const Field
 
 // Shell items of the fused schedule (planner.h), one list per set of CPML slabs their nodes may
 // lie in: kShellZ (z slabs only: planes outside the interior z range within the interior's x / y
-// range, and tiles around a design region), kShellYZ (the y bands beside the interior), kShellAny
-// (the x bands, corners included, and whole grids without interior tiles).
-enum { kShellZ = 0, kShellYZ = 1, kShellAny = 2, kShellLists = 3 };
+// range, and tiles around a design region), kShellYZ (the y bands beside the interior), kShellX
+// (the x bands beside the swept rows, inside the interior z range), kShellAny (the rest of the x
+// bands, corners included, and whole grids without interior tiles).
+enum { kShellZ = 0, kShellYZ = 1, kShellX = 2, kShellAny = 3, kShellLists = 4 };
 struct ShellWork {
     const int4* items[kShellLists];
     int n[kShellLists];
 };
 
 // Shell passes of the fused schedule (yee_two_pass.cu): E (e_pass) or H of the nodes of the shell
-// items, reading fi / pin (buffer A) and writing fo / pout (buffer B). The three lists must lie one
-// after the other in device memory (one launch covers them).
+// items, reading fi / pin (buffer A) and writing fo / pout (buffer B). The lists must lie one after
+// the other in device memory (one launch covers them).
 cudaError_t launch_shell(bool e_pass, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
                          const PsiSet& pout, const ShellWork& w, long long m, cudaStream_t st);
 
@@ -60,14 +61,28 @@ struct FusedMaps {
     CUtensorMap e[3];
     CUtensorMap rec;  // coefficient rows (StepParams::rec)
 };
+// Tensor maps of the CPML sweep: the sweep's own, plus the CPML memory of buffer A's y and z faces
+// per side (0: n face, 1: p face) and array (the two E, the two H arrays of the face): E arrays in
+// E-tile boxes (the halo nodes' E needs its old psi too), H arrays in boxes of the tile's own nodes.
+// Faces without CPML cells have no maps: bit s of `faces` is set for y side s, bit 2 + s for z
+// side s, and the sweep loads through no other map.
+struct CpmlMaps {
+    FusedMaps base;
+    CUtensorMap ye[2][2], yh[2][2];
+    CUtensorMap ze[2][2], zh[2][2];
+    int faces;
+};
 // Work items of one step (device arrays of int4 in the formats of planner.h).
 struct FusedWork {
     const int4* interior;
     int n_interior;
     ShellWork shell;
+    const int4* cpml;  // CPML items (CPML sweep), run after the interior sweep on its stream
+    int n_cpml;
 };
 cudaError_t fused_configure();
 int fused_smem_bytes();
+int cpml_smem_bytes();
 // fork (optional): a second stream and two events; the interior sweep then runs on `aux`,
 // concurrently with the shell E pass on `st` (they read buffer A and write disjoint nodes of B),
 // and `st` waits for it before the shell H pass.
@@ -75,12 +90,16 @@ struct FusedFork {
     cudaStream_t aux;
     cudaEvent_t fork, join;
 };
+// cmaps: the CPML sweep's maps (buffer A), needed when w.n_cpml > 0.
 cudaError_t launch_fused(const FusedMaps& maps, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo,
                          const PsiSet& psi_in, const PsiSet& psi_out, long long m, const FusedWork& w, cudaStream_t st,
-                         const FusedFork* fork = nullptr);
+                         const FusedFork* fork = nullptr, const CpmlMaps* cmaps = nullptr);
 // encode_fn: the driver's cuTensorMapEncodeTiled. Returns 0 on success.
 int encode_fused_maps(FusedMaps* out, const DeviceGrid& g, float* const h[3], float* const e[3], const uint16_t* rec,
                       void* encode_fn);
+// The CPML sweep's maps of a buffer (fields h, e, CPML memory psi) into out.
+int encode_cpml_maps(CpmlMaps* out, const DeviceGrid& g, float* const h[3], float* const e[3], const uint16_t* rec,
+                     const PsiSet& psi, void* encode_fn);
 
 // Setup kernels (setup_kernels.cu).
 cudaError_t launch_cpml_profiles(const DeviceGrid& g, float pi, float* const prof[18], cudaStream_t st);
@@ -118,5 +137,7 @@ cudaError_t launch_iface_rows(const DeviceGrid& g, uint8_t* cls, const uint8_t* 
                               const unsigned long long* keys, int n_keys, int* slot_row, uint16_t* rec, cudaStream_t st);
 cudaError_t launch_iface_coefs(const StepParams& p, const unsigned long long* keys, int n_keys, MatCoef* coef,
                                cudaStream_t st);
+// The lumped edges' nodes back to kRecGeneral | kGeneral in rec (after launch_iface_rows).
+cudaError_t launch_rec_general(const DeviceGrid& g, const LumpedEdge* edges, int n_edges, uint16_t* rec, cudaStream_t st);
 
 }  // namespace fdtd

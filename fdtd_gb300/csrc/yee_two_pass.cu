@@ -51,7 +51,7 @@ __device__ __forceinline__ bool shell_node(const int4& it, const DeviceGrid& g, 
     return tx < ((it.w >> 4) & 511) && ty < ((it.w >> 13) & 511) && i < g.nx && j < g.ny;
 }
 
-// One launch per pass covers the three shell lists (yee_kernels.h), which lie one after the other
+// One launch per pass covers the four shell lists (yee_kernels.h), which lie one after the other
 // in device memory: a block takes the instantiation of its list, kSlabs = the CPML slabs (bit 0 x,
 // 1 y, 2 z) its nodes may lie in, so the other slab tests compile out of that list's code. One
 // launch, not one per list, since small grids are bound by the chain of launches.
@@ -72,44 +72,48 @@ __device__ __forceinline__ void shell_h_item(const StepParams& p, const FieldPtr
         h_node_global<false, Idx, kSlabs>(p, fi, fo, fo, pin, pout, i, j, k, m);
 }
 
-// n_z, n_yz: the item counts of the first two lists (blocks beyond them take the third).
+// e1, e2, e3: the ends of the first three lists in the launch (blocks from e3 on take the fourth).
 template <typename Idx>
 __global__ void __launch_bounds__(256, FDTD_SHELL_MIN_BLOCKS) k_shell_e(const __grid_constant__ StepParams p, FieldPtrs fi, FieldPtrs fo,
                                                  const __grid_constant__ PsiSet pin, const __grid_constant__ PsiSet pout,
-                                                 const int4* __restrict__ items, int n_z, int n_yz, long long m) {
+                                                 const int4* __restrict__ items, int e1, int e2, int e3, long long m) {
     const int b = blockIdx.x;
     const int4 it = items[b];
-    if (b < n_z) shell_e_item<Idx, 4>(p, fi, fo, pin, pout, it, m);
-    else if (b < n_z + n_yz) shell_e_item<Idx, 6>(p, fi, fo, pin, pout, it, m);
+    if (b < e1) shell_e_item<Idx, 4>(p, fi, fo, pin, pout, it, m);
+    else if (b < e2) shell_e_item<Idx, 6>(p, fi, fo, pin, pout, it, m);
+    else if (b < e3) shell_e_item<Idx, 1>(p, fi, fo, pin, pout, it, m);
     else shell_e_item<Idx, 7>(p, fi, fo, pin, pout, it, m);
 }
 
 template <typename Idx>
 __global__ void __launch_bounds__(256, FDTD_SHELL_MIN_BLOCKS) k_shell_h(const __grid_constant__ StepParams p, FieldPtrs fi, FieldPtrs fo,
                                                  const __grid_constant__ PsiSet pin, const __grid_constant__ PsiSet pout,
-                                                 const int4* __restrict__ items, int n_z, int n_yz, long long m) {
+                                                 const int4* __restrict__ items, int e1, int e2, int e3, long long m) {
     const int b = blockIdx.x;
     const int4 it = items[b];
-    if (b < n_z) shell_h_item<Idx, 4>(p, fi, fo, pin, pout, it, m);
-    else if (b < n_z + n_yz) shell_h_item<Idx, 6>(p, fi, fo, pin, pout, it, m);
+    if (b < e1) shell_h_item<Idx, 4>(p, fi, fo, pin, pout, it, m);
+    else if (b < e2) shell_h_item<Idx, 6>(p, fi, fo, pin, pout, it, m);
+    else if (b < e3) shell_h_item<Idx, 1>(p, fi, fo, pin, pout, it, m);
     else shell_h_item<Idx, 7>(p, fi, fo, pin, pout, it, m);
 }
 
 cudaError_t launch_shell(bool e_pass, const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo, const PsiSet& pin,
                          const PsiSet& pout, const ShellWork& w, long long m, cudaStream_t st) {
-    const int n = w.n[kShellZ] + w.n[kShellYZ] + w.n[kShellAny];
+    int n = 0;
+    for (int q = 0; q < kShellLists; ++q) {
+        if (q > 0 && w.items[q] != w.items[q - 1] + w.n[q - 1]) return cudaErrorInvalidValue;  // the lists must be contiguous
+        n += w.n[q];
+    }
     if (n <= 0) return cudaSuccess;
-    if (w.items[kShellYZ] != w.items[kShellZ] + w.n[kShellZ] || w.items[kShellAny] != w.items[kShellYZ] + w.n[kShellYZ])
-        return cudaErrorInvalidValue;  // the lists must be contiguous
     const dim3 b(32, 8, 1);
-    const int nz = w.n[kShellZ], nyz = w.n[kShellYZ];
+    const int e1 = w.n[kShellZ], e2 = e1 + w.n[kShellYZ], e3 = e2 + w.n[kShellX];
     const int4* items = w.items[kShellZ];
     if (p.g.plane * (long long)(p.g.nz + 1) < (1LL << 31)) {
-        if (e_pass) k_shell_e<uint32_t><<<n, b, 0, st>>>(p, fi, fo, pin, pout, items, nz, nyz, m);
-        else k_shell_h<uint32_t><<<n, b, 0, st>>>(p, fi, fo, pin, pout, items, nz, nyz, m);
+        if (e_pass) k_shell_e<uint32_t><<<n, b, 0, st>>>(p, fi, fo, pin, pout, items, e1, e2, e3, m);
+        else k_shell_h<uint32_t><<<n, b, 0, st>>>(p, fi, fo, pin, pout, items, e1, e2, e3, m);
     } else {
-        if (e_pass) k_shell_e<long long><<<n, b, 0, st>>>(p, fi, fo, pin, pout, items, nz, nyz, m);
-        else k_shell_h<long long><<<n, b, 0, st>>>(p, fi, fo, pin, pout, items, nz, nyz, m);
+        if (e_pass) k_shell_e<long long><<<n, b, 0, st>>>(p, fi, fo, pin, pout, items, e1, e2, e3, m);
+        else k_shell_h<long long><<<n, b, 0, st>>>(p, fi, fo, pin, pout, items, e1, e2, e3, m);
     }
     return cudaGetLastError();
 }

@@ -19,7 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libfdtd_gb300.so")
 
 FDTD_OK = 0
-SCHEDULE_AUTO, SCHEDULE_TWO_PASS, SCHEDULE_FUSED = 0, 1, 2
+SCHEDULE_AUTO, SCHEDULE_TWO_PASS, SCHEDULE_FUSED, SCHEDULE_FUSED_CPML = 0, 1, 2, 3
 
 _i32 = ctypes.c_int32
 _i64 = ctypes.c_int64

@@ -40,7 +40,11 @@ enum {
                                  of >= 8 steps times 4 steps of each schedule and keeps the faster
                                  (that call synchronises the handle's stream) */
     FDTD_SCHEDULE_TWO_PASS = 1, /* E pass then H pass per step, in place (the reference's order) */
-    FDTD_SCHEDULE_FUSED = 2   /* one z-marching sweep per step over ping-pong field buffers   */
+    FDTD_SCHEDULE_FUSED = 2,  /* one z-marching sweep per step over ping-pong field buffers   */
+    FDTD_SCHEDULE_FUSED_CPML = 3 /* FUSED with the z-march also over the z and y CPML slabs and
+                                    the boundary planes beside the interior tiles (slabs of at most
+                                    15 cells, no design region); same bits, slower on the measured
+                                    grids, so AUTO does not choose it */
 };
 
 typedef struct fdtd_handle fdtd_handle;

@@ -1,8 +1,9 @@
 """CPU tests of the fused schedule's work planner (fdtd_gb300/csrc/planner.cpp), compiled here with
 g++ into a host-only library: the items of every list together store each node exactly once
-(overlapping interior tiles write the same values), interior items keep the TMA alignment and the
-plane limit and hold only interior nodes (E halo included) away from a design region's edge box,
-and no shell list holds nodes of a CPML slab its kernel leaves out."""
+(overlapping tiles write the same values), interior items keep the TMA alignment and the plane
+limit and hold only interior nodes (E halo included) away from a design region's edge box, CPML
+items lie inside the grid with an interior x range (E halo included), and no shell list holds
+nodes of a CPML slab its kernel leaves out."""
 import ctypes
 import os
 import subprocess
@@ -19,8 +20,9 @@ SRCS = [os.path.join(CSRC, "planner.cpp"), os.path.join(ROOT, "tests", "plan_pro
 TILE_X, TILE_Y, MAX_ITEM_PLANES, SHELL_PLANES = 32, 16, 512, 4
 SHAPE_W = [32, 16, 64, 128, 256, 8, 4, 2, 1]
 # shell lists and the CPML slabs (bit 0 x, 1 y, 2 z) their kernels test for
-SHELL_LISTS = (("shell_z", 4), ("shell_yz", 6), ("shell_any", 7))
-LISTS = ("interior",) + tuple(n for n, _ in SHELL_LISTS)
+SHELL_LISTS = (("shell_z", 4), ("shell_yz", 6), ("shell_x", 1), ("shell_any", 7))
+LISTS = ("interior",) + tuple(n for n, _ in SHELL_LISTS) + ("cpml",)
+CPML_MAX_SLAB = TILE_Y - 1
 
 
 @pytest.fixture(scope="module")
@@ -34,14 +36,14 @@ def lib():
     return L
 
 
-def plan(lib, dims, pml, design=None):
+def plan(lib, dims, pml, design=None, cpml=False):
     g = (ctypes.c_int * 9)(*dims, *pml)
     d = None if design is None else (ctypes.c_int * 6)(*design)
     counts = (ctypes.c_int * len(LISTS))()
-    lib.plan_probe(g, d, counts, None, 0)
+    lib.plan_probe(g, d, int(cpml), counts, None, 0)
     n = sum(counts)
     items = np.zeros((max(n, 1), 4), dtype=np.int32)
-    kc = lib.plan_probe(g, d, counts, items.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), n)
+    kc = lib.plan_probe(g, d, int(cpml), counts, items.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), n)
     lists, o = {}, 0
     for q, name in enumerate(LISTS):
         lists[name] = items[o:o + counts[q]]
@@ -57,9 +59,9 @@ def in_slab(q, n, pn, pp):
     return q < pn or q >= n - pp
 
 
-def check(lib, dims, pml, design=None):
+def check(lib, dims, pml, design=None, cpml=False):
     nx, ny, nz = dims
-    kc, L = plan(lib, dims, pml, design)
+    kc, L = plan(lib, dims, pml, design, cpml)
     xlo, xhi = interior_range(nx, pml[0], pml[1])
     ylo, yhi = interior_range(ny, pml[2], pml[3])
     zlo, zhi = interior_range(nz, pml[4], pml[5])
@@ -72,7 +74,17 @@ def check(lib, dims, pml, design=None):
             assert not (x0 <= d[3] and d[0] <= x0 + TILE_X and y0 <= d[4] and d[1] <= y0 + TILE_Y), \
                 "an interior tile reaches the design edge box"
         owned[k0:k1, y0:y0 + TILE_Y, x0:x0 + TILE_X] = 1  # overlapping tiles store the same values
-    cover = owned
+    swept_plane = owned[min(zlo, nz - 1)].copy()  # nodes of the interior tiles in one interior plane
+    cp = np.zeros_like(owned)  # overlapping CPML tiles store the same values
+    for x0, y0, k0, k1 in L["cpml"]:
+        assert x0 % 8 == 0 and 0 <= k0 < k1 <= nz and k1 - k0 <= MAX_ITEM_PLANES - 2
+        assert xlo <= x0 and x0 + TILE_X <= xhi and -TILE_Y < y0 < ny
+        ya, yb = max(y0, 0), min(y0 + TILE_Y, ny)
+        if k0 >= zlo and k1 <= zhi:  # a band tile: its rows in the grid lie outside the swept rows
+            swept = swept_plane[:, x0:x0 + TILE_X].any(axis=1)
+            assert not swept[ya:yb].any(), "a band tile recomputes swept rows"
+        cp[k0:k1, ya:yb, x0:x0 + TILE_X] = 1
+    cover = owned + cp
     for name, slabs in SHELL_LISTS:
         for x0, y0, k, code in L[name]:
             s, cols, rows, nk = code & 15, (code >> 4) & 511, (code >> 13) & 511, ((code >> 22) & 15) + 1
@@ -84,6 +96,8 @@ def check(lib, dims, pml, design=None):
                 assert not any(in_slab(x, nx, pml[0], pml[1]) for x in range(x0, x0 + cols)), name
             if not slabs & 2:
                 assert not any(in_slab(y, ny, pml[2], pml[3]) for y in range(y0, y0 + rows)), name
+            if not slabs & 4:
+                assert not any(in_slab(z, nz, pml[4], pml[5]) for z in range(k, k + nk)), name
             cover[k:k + nk, y0:y0 + rows, x0:x0 + cols] += 1
     assert cover.min() == 1 and cover.max() == 1, (int(cover.min()), int(cover.max()))
     return kc, L
@@ -123,3 +137,32 @@ def test_bench_grid_lists(lib):
 def test_plan_with_design_region(lib, dims, pml, design):
     _, L = check(lib, dims, pml, design)
     assert sum(len(L[n]) for n, _ in SHELL_LISTS) > 0
+
+
+@pytest.mark.parametrize("dims,pml", [
+    ((512, 512, 512), (10,) * 6),
+    ((256, 256, 256), (10,) * 6),
+    ((128, 128, 128), (10,) * 6),
+    ((80, 56, 40), (6,) * 6),
+    ((96, 61, 47), (8,) * 6),
+    ((33, 45, 70), (8,) * 6),
+    ((70, 45, 80), (0,) * 6),
+    ((61, 50, 30), (1,) * 6),
+    ((100, 17, 16), (3,) * 6),
+    ((1024, 1024, 64), (10,) * 6),
+    ((300, 200, 100), (0, 16, 12, 5, 15, 1)),
+    ((96, 90, 64), (8, 8, 15, 15, 15, 15)),
+])
+def test_plan_with_cpml_items(lib, dims, pml):
+    """With CPML items every node is still stored once; where the grid has interior tiles and
+    slabs of at most 15 cells, the z and y shell lists are empty."""
+    _, L = check(lib, dims, pml, cpml=True)
+    if len(L["interior"]) and max(pml[2:]) <= CPML_MAX_SLAB:
+        assert len(L["cpml"]) > 0 and len(L["shell_z"]) == 0 and len(L["shell_yz"]) == 0
+    if max(pml[2:]) > CPML_MAX_SLAB:
+        assert len(L["cpml"]) == 0
+
+
+def test_no_cpml_items_with_design(lib):
+    _, L = check(lib, (128, 128, 128), (10,) * 6, (48, 48, 56, 80, 80, 72), cpml=True)
+    assert len(L["cpml"]) == 0 and len(L["shell_z"]) > 0
