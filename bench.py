@@ -260,9 +260,10 @@ TWO_PASS_DRAM_BYTES_PER_CELL = 78.15
 
 
 # DRAM bytes per cell update of one fused step (k_shell_e + k_sweep_interior + k_shell_h),
-# dram__bytes_read.sum + dram__bytes_write.sum from ncu captures: 62.46 B on the 512^3 bench
-# workload itself, 72.77 B at 256^3, where the shell share is larger.
-FUSED_DRAM_BYTES_PER_CELL = {"512": 62.46, "256": 72.77}
+# dram__bytes_read.sum + dram__bytes_write.sum from ncu captures of these kernels (the launch-list
+# commands in profiles/yee_step_boxes512_launch_list.md): 63.46 B on the 512^3 bench workload
+# itself, 72.77 B at 256^3, where the shell share is larger. Refreshed whenever the kernels change.
+FUSED_DRAM_BYTES_PER_CELL = {"512": 63.46, "256": 72.77}
 
 
 def measured_traffic(schedule, cells, config):
@@ -328,7 +329,8 @@ def bench_ours(args, rank, world):
                       "schedule": {0: "auto", 1: "two-pass", 2: "fused", 3: "fused-cpml"}[args.schedule] +
                                   (" (fused)" if args.schedule == 0 and active == 2 else
                                    " (two-pass)" if args.schedule == 0 else ""),
-                      "l2": "inputs larger than L2 (fields 24 B/cell x 134M cells)", "parallelism": f"replicas{world}"},
+                      "l2": f"inputs larger than L2 (fields 24 B/cell x {N / 1e6:.0f}M cells)",
+                      "parallelism": f"replicas{world}"},
            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                         "frac": round(achieved / peak, 4), "traffic": measured_traffic(active, N, args.config),
                         "bytes_per_cell_update": round(B, 3), "peak_source": peak_kind,

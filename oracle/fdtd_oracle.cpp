@@ -700,6 +700,63 @@ int fom_and_grad(const or_scenario* sc, int steps, const float* sig, int n_sig, 
     return 0;
 }
 
+// fom_and_grad for long runs: the forward keeps, per step, only the fields of the design region's
+// nodes and of the node layer below it (all accumulate_grad reads) instead of the whole history,
+// and the reverse sweep writes them back into full-volume scratch arrays before each gradient
+// step. Same arithmetic, same result; memory (steps x 6 x box nodes) instead of (steps x 6 x N).
+template <class R>
+int fom_and_grad_box(const or_scenario* sc, int steps, const float* sig, int n_sig, int pi, int pj, int pk,
+                     double* J_out, double* grad_out) {
+    Sim<R> s;
+    if (setup<R>(s, sc, sig, n_sig)) return -1;
+    const size_t n_p = s.id(pi, pj, pk);
+    const int* d = sc->design_box;
+    const int i0 = std::max(d[0] - 1, 0), i1 = std::min(d[3], s.NX - 1);
+    const int j0 = std::max(d[1] - 1, 0), j1 = std::min(d[4], s.NY - 1);
+    const int k0 = std::max(d[2] - 1, 0), k1 = std::min(d[5], s.NZ - 1);
+    const size_t bx = (size_t)(i1 - i0 + 1), by = (size_t)(j1 - j0 + 1), bz = (size_t)(k1 - k0 + 1);
+    const size_t nb = bx * by * bz;
+    auto box_copy = [&](R* box, std::vector<R>& full, bool to_box) {
+        size_t q = 0;
+        for (int k = k0; k <= k1; ++k)
+            for (int j = j0; j <= j1; ++j)
+                for (int i = i0; i <= i1; ++i, ++q) {
+                    const size_t n = s.id(i, j, k);
+                    if (to_box) box[q] = full[n];
+                    else full[n] = box[q];
+                }
+    };
+    std::vector<R> row(std::max<size_t>(s.probes.size(), 1));
+    std::vector<R> hist(grad_out ? (size_t)steps * 6 * nb : 0);
+    std::vector<R> ezp(steps);
+    for (int m = 0; m < steps; ++m) {
+        if (grad_out)
+            for (int c = 0; c < 6; ++c) box_copy(&hist[((size_t)m * 6 + c) * nb], *field(s, c), true);
+        calc_e<R>(s, m, row.data());
+        ezp[m] = s.Ez[n_p];
+        calc_h<R>(s, row.data());
+    }
+    const double dt = (double)s.dt;
+    double J = 0;
+    for (int m = 0; m < steps; ++m) J += dt * (double)ezp[m] * (double)ezp[m];
+    *J_out = J;
+    if (!grad_out) return 0;
+    std::fill(grad_out, grad_out + (size_t)(d[3] - d[0]) * (d[4] - d[1]) * (d[5] - d[2]), 0.0);
+    std::vector<R> scratch[6];
+    for (auto& v : scratch) v.assign(s.N, (R)0);
+    const std::vector<R>* Em[3] = {&scratch[0], &scratch[1], &scratch[2]};
+    const std::vector<R>* Hm[3] = {&scratch[3], &scratch[4], &scratch[5]};
+    Adj<R> a(s.N);
+    for (int m = steps - 1; m >= 0; --m) {
+        a.ez[n_p] += (R)(2.0 * dt) * ezp[m];
+        reverse_h<R>(s, a);
+        for (int c = 0; c < 6; ++c) box_copy(&hist[((size_t)m * 6 + c) * nb], scratch[c], false);
+        accumulate_grad<R>(s, a, Em, Hm, d, grad_out);
+        reverse_e<R>(s, a);
+    }
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -713,6 +770,11 @@ int or_fom_grad_f64(const or_scenario* sc, int steps, const float* sig, int n_si
 int or_fom_grad_f32(const or_scenario* sc, int steps, const float* sig, int n_sig, int pi, int pj, int pk,
                     double* J, double* grad) {
     return fom_and_grad<float>(sc, steps, sig, n_sig, pi, pj, pk, J, grad);
+}
+// or_fom_grad_f64 keeping only the design region's field history (long runs, large grids).
+int or_fom_grad_box_f64(const or_scenario* sc, int steps, const float* sig, int n_sig, int pi, int pj, int pk,
+                        double* J, double* grad) {
+    return fom_and_grad_box<double>(sc, steps, sig, n_sig, pi, pj, pk, J, grad);
 }
 
 // Seconds the time loop of the last or_run_f32 / or_run_f64 took (setup excluded).

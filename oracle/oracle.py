@@ -69,7 +69,7 @@ def lib():
         L.or_port_vi.argtypes = [_pf, _i, _i, _i, _pi, _pi, _i, _f, _f, _f, _i, _pf, _pf]
         L.or_last_step_seconds.restype = ctypes.c_double
         L.or_last_step_seconds.argtypes = []
-        for fn in (L.or_fom_grad_f64, L.or_fom_grad_f32):
+        for fn in (L.or_fom_grad_f64, L.or_fom_grad_f32, L.or_fom_grad_box_f64):
             fn.argtypes = [ctypes.POINTER(_Scenario), _i, _pf, _i, _i, _i, _i, _pd, _pd]
         _lib = L
     return _lib
@@ -200,16 +200,20 @@ def coef(sc, name: str, profile_override: Optional[dict] = None) -> np.ndarray:
 
 
 def fom_grad(sc, probe, design_box, design_eps, steps: Optional[int] = None, precision: str = "f64",
-             grad: bool = True):
+             grad: bool = True, box_history: bool = False):
     """Figure of merit J = sum_m dt * Ez(probe)^2 over ``steps`` and, if ``grad``, the discrete-adjoint
     gradient dJ/deps_r of the design cells (array shaped like ``design_eps``). The design region
-    ``design_box`` = (i0, j0, k0, i1, j1, k1) overrides the cells' eps_r with ``design_eps``."""
+    ``design_box`` = (i0, j0, k0, i1, j1, k1) overrides the cells' eps_r with ``design_eps``.
+    box_history (FP64 only): keep only the design region's field history (long runs, large grids;
+    same result)."""
     steps = sc.steps if steps is None else steps
     p = _Prepared(sc, design=(design_box, design_eps))
     g = np.zeros(np.shape(design_eps), dtype=np.float64) if grad else None
     J = ctypes.c_double(0.0)
     L = lib()
-    fn = L.or_fom_grad_f64 if precision == "f64" else L.or_fom_grad_f32
+    if box_history and precision != "f64":
+        raise ValueError("box_history is an FP64 form")
+    fn = L.or_fom_grad_box_f64 if box_history else L.or_fom_grad_f64 if precision == "f64" else L.or_fom_grad_f32
     rc = fn(ctypes.byref(p.s), steps, p.sig.ctypes.data_as(_pf), p.n_sig, int(probe[0]), int(probe[1]), int(probe[2]),
             ctypes.byref(J), None if g is None else g.ctypes.data_as(_pd))
     if rc != 0:

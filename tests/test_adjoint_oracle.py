@@ -47,3 +47,13 @@ def test_fp32_adjoint_close_to_fp64():
     _, g64 = oracle.fom_grad(sc, probe, box, eps, precision="f64")
     _, g32 = oracle.fom_grad(sc, probe, box, eps, precision="f32")
     assert np.linalg.norm(g32 - g64) / np.linalg.norm(g64) < 1e-4
+
+
+def test_box_history_form_equals_full_history():
+    """The long-run form (only the design region's field history kept) gives the same J and
+    gradient bits as the full-history form."""
+    d = S.design_problem(24, 60, (6, 6, 4), pml=4, seed=2)
+    e = d.eps.astype(np.float64)
+    J1, g1 = oracle.fom_grad(d.scenario, d.probe, d.box, e)
+    J2, g2 = oracle.fom_grad(d.scenario, d.probe, d.box, e, box_history=True)
+    assert J1 == J2 and np.array_equal(g1, g2)

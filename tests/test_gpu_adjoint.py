@@ -156,3 +156,25 @@ def test_design_problem_sixteen_voxels(gpu_lib):
               oracle.fom_grad(sc, d.probe, d.box, e2, grad=False)) / (2 * h)
         worst = max(worst, abs(g[v] - fd) / abs(fd))
     assert worst <= GRAD_TOL, worst
+
+
+def test_full_size_workload_against_fp64_reference(gpu_lib):
+    """The 128^3 / 4000-step workload itself (32 x 32 x 16 design region, checkpoints every 64
+    steps): the GPU gradient against the FP64 oracle's adjoint gradient over the whole design region
+    and against central differences of the FP64 oracle forward at 16 seeded voxels, both recorded
+    in tests/golden/adjoint_c4.npz by tests/golden/make_adjoint_c4.py."""
+    from conftest import GOLDEN
+    import os
+    path = os.path.join(GOLDEN, "adjoint_c4.npz")
+    if not os.path.exists(path):
+        pytest.skip("reference gradient not generated")
+    ref = np.load(path)
+    d = S.design_problem(128, int(ref["steps"]))
+    assert tuple(ref["box"]) == tuple(d.box) and tuple(ref["probe"]) == tuple(d.probe)
+    J, g = gpu_grad(d.scenario, d.box, d.eps, d.probe, 64)
+    assert abs(J - float(ref["J"])) <= GRAD_TOL * float(ref["J"])
+    g64 = ref["grad"]
+    assert rel(g, g64) <= GRAD_TOL, rel(g, g64)
+    for v, fd in zip(ref["voxels"], ref["fd"]):
+        v = tuple(int(x) for x in v)
+        assert abs(g[v] - fd) <= GRAD_TOL * abs(fd), (v, g[v], fd)
