@@ -364,10 +364,13 @@ int plan_work(fdtd_handle* h) {
 int ensure_fused(fdtd_handle* h) {
     if (h->have_second && h->replan) return plan_work(h);
     if (h->have_second) return FDTD_OK;
+    // no copy of the state: a fused step writes every node of its target buffer (the planner's
+    // items cover each node once; plate and design nodes by their own kernels); the row padding,
+    // which no kernel writes, gets buffer 0's initial value so that saved states agree
     const long long V = vol(h);
     for (int c = 0; c < 6; ++c) {
         CUDA_TRY(h->alloc((void**)&h->field[1][c], (size_t)V * sizeof(float)));
-        CUDA_TRY(cudaMemcpyAsync(h->field[1][c], h->field[0][c], (size_t)V * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
+        CUDA_TRY(launch_fill(h->field[1][c], V, kTiny, h->stream));
     }
     int rc = alloc_psi_set(h, 1);
     if (rc) return rc;
@@ -718,10 +721,39 @@ int steps_two_pass(fdtd_handle* h, const StepParams& p, int64_t n) {
 // 2 * kAutoTrialSteps steps times kAutoTrialSteps fused steps and then as many two-pass steps (real
 // steps: both schedules give the same bits) and keeps the faster schedule for the handle. Which one
 // wins depends on the grid: on GB300 random-box cubes with 10-cell CPML, two-pass below about
-// 224^3 and fused above. Smaller grids take two-pass without a trial. The fused buffers are freed
-// when two-pass wins or cannot be allocated.
+// 224^3 and fused above. Smaller grids take two-pass without a trial. Grids of at least
+// kAutoDirectCells cells whose interior tiles hold at least kAutoDirectInterior of the nodes
+// (512^3 with 10-cell CPML: 0.86) take fused without a trial: there fused won by 16-30 % on every
+// grid measured, and the trial's two-pass steps and synchronisation cost more than a step. The
+// fused buffers are freed when two-pass wins or cannot be allocated.
 constexpr int64_t kAutoTrialSteps = 4;
 constexpr long long kAutoTrialCells = 8LL << 20;
+constexpr long long kAutoDirectCells = 64LL << 20;
+constexpr double kAutoDirectInterior = 0.8;
+
+// Share of the grid's nodes that the interior sweep's tiles hold (overlapping tiles counted once
+// per tile, a slight overestimate).
+double interior_share(const fdtd_handle* h) {
+    FusedPlan plan;
+    const PlanGrid pg = plan_grid(h->g);
+    plan_fused(pg, plan_chunk(pg), h->has_design ? h->dbox : nullptr, plan);
+    long long n = 0;
+    for (const PlanItem& it : plan.interior) n += (long long)(it.w - it.z) * kTileX * kTileY;
+    return (double)n / ((double)h->g.nx * h->g.ny * h->g.nz);
+}
+
+// AUTO's choice without a trial where it is clear (see above); false: run the trial.
+bool auto_direct(fdtd_handle* h) {
+    if ((long long)h->g.nx * h->g.ny * h->g.nz < kAutoDirectCells || interior_share(h) < kAutoDirectInterior) return false;
+    if (ensure_fused(h) != FDTD_OK) {  // no room for the second buffers
+        cudaGetLastError();
+        if (h->cur == 0) release_fused(h);
+        h->auto_choice = FDTD_SCHEDULE_TWO_PASS;
+        return true;
+    }
+    h->auto_choice = FDTD_SCHEDULE_FUSED;
+    return true;
+}
 
 int auto_trial(fdtd_handle* h, const StepParams& p) {
     if (ensure_fused(h) != FDTD_OK) {  // no room for the second buffers
@@ -764,7 +796,7 @@ int fdtd_step(fdtd_handle* h, int64_t n) {
     if (rc) return rc;
     StepParams p = make_params(h);
     if (h->schedule == FDTD_SCHEDULE_AUTO && h->auto_choice == FDTD_SCHEDULE_AUTO && n >= 2 * kAutoTrialSteps &&
-        (long long)h->g.nx * h->g.ny * h->g.nz >= kAutoTrialCells) {
+        (long long)h->g.nx * h->g.ny * h->g.nz >= kAutoTrialCells && !auto_direct(h)) {
         if ((rc = auto_trial(h, p))) return rc;
         n -= 2 * kAutoTrialSteps;
     }
@@ -940,6 +972,7 @@ int fdtd_tune_schedule(fdtd_handle* h) {
         h->auto_choice = FDTD_SCHEDULE_TWO_PASS;
         return FDTD_OK;
     }
+    if (auto_direct(h)) return FDTD_OK;
     // the trial's steps are undone: state and probe ring saved before, restored after
     const size_t ring = sizeof(float) * (size_t)h->ring_cap * std::max<size_t>(h->probes.size(), 1);
     void* saved = nullptr;

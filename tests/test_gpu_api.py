@@ -193,3 +193,26 @@ def test_auto_schedule_trial(gpu_lib):
         assert a.active_schedule == solver.SCHEDULE_TWO_PASS
         assert a.device_bytes() == b.device_bytes()
         assert bitwise_equal(a.fields(), b.fields())
+
+
+def test_auto_schedule_direct_on_large_grids(gpu_lib):
+    """AUTO on a grid of at least 64 Mi cells whose interior tiles hold most nodes: fused without a
+    trial (the first call's steps are all fused steps), the same bits as two-pass."""
+    import torch
+    from fdtd_gb300 import solver
+    sc = S.random_boxes(408, 408, 408, 10, seed=4, n_boxes=24, edge=(16, 128), pml=10, n_sources=2, n_probes=6)
+    mat = sc.material_index()
+    out = []
+    for schedule in (solver.SCHEDULE_AUTO, solver.SCHEDULE_TWO_PASS):
+        with solver.Simulation.from_scenario(sc, schedule, material_index=mat, probe_capacity=10) as sim:
+            sim.step(10)
+            sim.synchronize()
+            if schedule == solver.SCHEDULE_AUTO:
+                assert sim.active_schedule == solver.SCHEDULE_FUSED
+            buf = torch.empty(sim.state_bytes(), dtype=torch.uint8, device="cuda")
+            torch.cuda.synchronize()
+            sim.save_state(buf.data_ptr())
+            torch.cuda.synchronize()
+            out.append((buf.cpu(), sim.read_probes(0, 10)))
+    assert torch.equal(out[0][0], out[1][0])
+    assert bitwise_equal(out[0][1], out[1][1])
