@@ -61,7 +61,7 @@ struct PlateDef {
 // (currMgpu, the groups and cell sizes per direction in port_groups).
 struct PortDef {
     int vbox[6], ibox[6];
-    int current_axis;
+    int current_axis, voltage_axis;
     int first;  // probe id of the first voltage edge
     int n_v;
     int n[4];   // probes of s1..s4
@@ -2087,15 +2087,18 @@ void port_groups(int axis, const int* c, std::vector<Probe> g[4]) {
 extern "C" int fdtd_add_port(fdtd_handle* h, int32_t voltage_axis, const int32_t vbox[6], int32_t current_axis,
                              const int32_t ibox[6], int32_t* id_out) {
     if (!h || !vbox || !ibox) return fail(FDTD_ERR_INVALID, "NULL argument");
-    if (voltage_axis != 2) return fail(FDTD_ERR_INVALID, "only z-directed port voltages (axis 2) are supported");
+    if (voltage_axis < 0 || voltage_axis > 2) return fail(FDTD_ERR_INVALID, "voltage axis must be 0, 1 or 2");
     if (current_axis < 0 || current_axis > 2) return fail(FDTD_ERR_INVALID, "current axis must be 0, 1 or 2");
     if (h->step > 0) return fail(FDTD_ERR_STATE, "ports must be added before the first step");
     const DeviceGrid& g = h->g;
     const int* v = vbox;
     const int* c = ibox;
-    if (v[0] < 0 || v[3] >= g.nx || v[0] > v[3] || v[1] < 0 || v[4] >= g.ny || v[1] > v[4] || v[2] < 0 || v[5] > g.nz ||
-        v[2] >= v[5])
-        return fail(FDTD_ERR_INVALID, "voltage box outside the grid or empty (k range is half-open)");
+    // the summed ranges: half-open along the voltage axis, closed across it
+    const int va = voltage_axis;
+    const int vi1 = va == 0 ? v[3] - 1 : v[3], vj1 = va == 1 ? v[4] - 1 : v[4], vk1 = va == 2 ? v[5] - 1 : v[5];
+    if (v[0] < 0 || v[1] < 0 || v[2] < 0 || vi1 >= g.nx || vj1 >= g.ny || vk1 >= g.nz || v[0] > vi1 || v[1] > vj1 ||
+        v[2] > vk1)
+        return fail(FDTD_ERR_INVALID, "voltage box outside the grid or empty (half-open along the voltage axis)");
     if (c[0] > c[3] || c[1] > c[4] || c[2] > c[5] || (current_axis == 2 && c[5] < 1))
         return fail(FDTD_ERR_INVALID, "current box empty or reversed");
     std::vector<Probe> grp[4];
@@ -2108,10 +2111,11 @@ extern "C" int fdtd_add_port(fdtd_handle* h, int32_t voltage_axis, const int32_t
     std::copy(v, v + 6, P.vbox);
     std::copy(c, c + 6, P.ibox);
     P.current_axis = current_axis;
+    P.voltage_axis = voltage_axis;
     P.first = (int)h->probes.size();
-    for (int k = v[2]; k < v[5]; ++k)
-        for (int j = v[1]; j <= v[4]; ++j)
-            for (int i = v[0]; i <= v[3]; ++i) h->probes.push_back(Probe{FDTD_EZ, i, j, k});
+    for (int k = v[2]; k <= vk1; ++k)
+        for (int j = v[1]; j <= vj1; ++j)
+            for (int i = v[0]; i <= vi1; ++i) h->probes.push_back(Probe{FDTD_EZ, i, j, k});
     P.n_v = (int)h->probes.size() - P.first;
     for (int q = 0; q < 4; ++q) {
         h->probes.insert(h->probes.end(), grp[q].begin(), grp[q].end());
@@ -2135,9 +2139,12 @@ extern "C" int fdtd_read_port(fdtd_handle* h, int32_t id, int64_t first, int64_t
     const PortDef& P = h->ports[id];
     const float dx = h->g.dx, dy = h->g.dy, dz = h->g.dz;
     const float a1 = P.current_axis == 1 ? dz : dy, a2 = P.current_axis == 0 ? dz : dx;
-    // voltMgpu case 3: csuf = -dz / ((ie - is + 1) (je - js + 1)) with float box bounds
-    const float is = (float)P.vbox[0], js = (float)P.vbox[1], ie = (float)P.vbox[3], je = (float)P.vbox[4];
-    const float csuf = (-dz) / ((ie - is + 1) * (je - js + 1));
+    // voltMgpu cases 1 / 2 / 3 (fdtdrav.h:2214-2290), with float box bounds
+    const float is = (float)P.vbox[0], js = (float)P.vbox[1], ks = (float)P.vbox[2];
+    const float ie = (float)P.vbox[3], je = (float)P.vbox[4], ke = (float)P.vbox[5];
+    const float csuf = P.voltage_axis == 0   ? (-dx) / ((je - js + 1) * (ke - ks + 1))
+                       : P.voltage_axis == 1 ? (-dy) / ((ke - ks + 1) * (ie - is + 1))
+                                             : (-dz) / ((ie - is + 1) * (je - js + 1));
     for (int64_t t = 0; t < n; ++t) {
         const float* r = rows.data() + (size_t)t * np + P.first;
         float volt = 0.f;

@@ -235,7 +235,8 @@ class Simulation:
 
     def add_port(self, voltage_box: Sequence[int], current_box: Sequence[int], current_axis: int = 2,
                  voltage_axis: int = 2) -> int:
-        """A port (z-directed voltage edges, current loop around ``current_axis``); returns its id."""
+        """A port (voltage along ``voltage_axis`` from the Ez samples of the box, current loop around
+        ``current_axis``); returns its id."""
         pid = _i32(-1)
         _check(_lib.fdtd_add_port(self._h, voltage_axis, _box(voltage_box), current_axis, _box(current_box),
                                   ctypes.byref(pid)))

@@ -179,11 +179,14 @@ int fdtd_get_cpml_profile(fdtd_handle* h, int32_t axis, int32_t kind, float* hos
 /* Bytes of device memory the handle holds. */
 int64_t fdtd_device_bytes(const fdtd_handle* h);
 
-/* Port voltage and current. Registers the point probes of a port: the Ez edges of the voltage
- * box i in [is,ie], j in [js,je], k in [ks,ke) (voltage_axis 2; the reference's other voltage
- * directions sum the same sampled Ez array, fdtdrav.h:2214-2262, and are not provided), and the
- * current loop of currMgpu around the current box for current_axis 0 / 1 / 2 (x / y / z,
- * fdtdrav.h:2318-2480, cases 1 / 2 / 3):
+/* Port voltage and current. Registers the point probes of a port: the Ez samples of the voltage
+ * box that voltMgpu sums for voltage_axis 0 / 1 / 2 (x / y / z, its direction 1 / 2 / 3; the
+ * reference samples Ez for every direction, sampleField in calc_e fdtdrav.h:740, and only the
+ * ranges and the scale change, fdtdrav.h:2214-2290):
+ *   x: i in [is,ie), j in [js,je], k in [ks,ke];  y: i in [is,ie], j in [js,je), k in [ks,ke];
+ *   z: i in [is,ie], j in [js,je], k in [ks,ke)
+ * (k outer, then j, then i), and the current loop of currMgpu around the current box for
+ * current_axis 0 / 1 / 2 (x / y / z, fdtdrav.h:2318-2480, cases 1 / 2 / 3):
  *   x: Hy(ie-1, j, ks-1), Hz(ie-1, je, k), Hy(ie-1, j, ke), Hz(ie-1, js-1, k)
  *   y: Hz(is-1, je-1, k), Hx(i, je-1, ke), Hz(ie, je-1, k), Hx(i, je-1, ks-1)
  *   z: Hy(ie, j, ke-1), Hx(i, js-1, ke-1), Hy(is-1, j, ke-1), Hx(i, je, ke-1)
@@ -192,7 +195,8 @@ int64_t fdtd_device_bytes(const fdtd_handle* h);
  * ports before the first step; their probes also appear as columns of fdtd_read_probes. */
 int fdtd_add_port(fdtd_handle* h, int32_t voltage_axis, const int32_t voltage_box[6], int32_t current_axis,
                   const int32_t current_box[6], int32_t* id_out);
-/* V(t) = -dz / (n_i n_j) * sum of the voltage edges' Ez and I(t) = a1 s1 + a2 s2 - a1 s3 - a2 s4
+/* V(t) = csuf * sum of the voltage samples, csuf = -dx / ((je-js+1)(ke-ks+1)) (x),
+ * -dy / ((ke-ks+1)(ie-is+1)) (y), -dz / ((ie-is+1)(je-js+1)) (z), and I(t) = a1 s1 + a2 s2 - a1 s3 - a2 s4
  * over the four probe groups above in order (a1, a2 = dy, dz for x; dz, dx for y; dy, dx for z)
  * for steps [first_step, first_step+n_steps), summed in the reference's order (host memory;
  * voltMgpu / currMgpu, fdtdrav.h:2185-2488). With time_average

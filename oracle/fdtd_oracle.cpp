@@ -798,10 +798,12 @@ int or_onestep_f32(const or_scenario* sc, int m, const float* sig, int n_sig, co
 }
 
 // Port voltage and current from sampled series (steps rows of `stride` floats, the port's columns
-// from col0): the voltage box's Ez edges (k in [ks,ke) outer, then j, then i), then four groups of
-// H samples s1..s4 of the current loop for current direction `axis` (0 x, 1 y, 2 z; the groups
-// of fdtd_gb300's port_groups, in summation order). Restates voltMgpu case 3
-// (fdtdrav.h:2268-2290): a float sum in that order times csuf = -dz / ((ie-is+1)(je-js+1));
+// from col0): the voltage box's Ez samples (k outer, then j, then i; the range along the voltage
+// direction `vaxis` half-open, the others closed), then four groups of H samples s1..s4 of the
+// current loop for current direction `axis` (0 x, 1 y, 2 z; the groups of fdtd_gb300's
+// port_groups, in summation order). Restates voltMgpu cases 1-3 (fdtdrav.h:2214-2290): a float
+// sum in that order times csuf = -dx / ((je-js+1)(ke-ks+1)), -dy / ((ke-ks+1)(ie-is+1)) or
+// -dz / ((ie-is+1)(je-js+1));
 // currMgpu cases 1-3 (fdtdrav.h:2318-2480): four float sums and a1*s1 + a2*s2 - a1*s3 - a2*s4
 // (a1, a2 = dy, dz / dz, dx / dy, dx), contracted as the reference's compiled expressions are
 // (x loop: a1*s1 fused with a2*s2 as the addend; y, z loops: a2*s2 fused with a1*s1 as the
@@ -809,8 +811,10 @@ int or_onestep_f32(const or_scenario* sc, int m, const float* sig, int n_sig, co
 // outputs); and, with time_average, correcI
 // (fdtdrav.h:2490-2508) in the order its in-place threads produced their results.
 int or_port_vi(const float* series, int steps, int stride, int col0, const int* vbox, const int* cbox, int axis,
-               float dx, float dy, float dz, int time_average, float* V, float* I) {
-    const int nv = (vbox[3] - vbox[0] + 1) * (vbox[4] - vbox[1] + 1) * (vbox[5] - vbox[2]);
+               int vaxis, float dx, float dy, float dz, int time_average, float* V, float* I) {
+    // voltMgpu (fdtdrav.h:2214-2290): the Ez samples of the box, half-open along the voltage axis
+    const int nv = (vbox[3] - vbox[0] + (vaxis == 0 ? 0 : 1)) * (vbox[4] - vbox[1] + (vaxis == 1 ? 0 : 1)) *
+                   (vbox[5] - vbox[2] + (vaxis == 2 ? 0 : 1));
     const int ni = cbox[3] - cbox[0] + 1, nj = cbox[4] - cbox[1] + 1, nk = cbox[5] - cbox[2] + 1;
     int n[4];
     float a1, a2;
@@ -821,8 +825,11 @@ int or_port_vi(const float* series, int steps, int stride, int col0, const int* 
         g_err = "port columns outside the series";
         return -1;
     }
-    const float is = (float)vbox[0], js = (float)vbox[1], ie = (float)vbox[3], je = (float)vbox[4];
-    const float csuf = (-dz) / ((ie - is + 1) * (je - js + 1));
+    const float is = (float)vbox[0], js = (float)vbox[1], ks = (float)vbox[2];
+    const float ie = (float)vbox[3], je = (float)vbox[4], ke = (float)vbox[5];
+    const float csuf = vaxis == 0   ? (-dx) / ((je - js + 1) * (ke - ks + 1))
+                       : vaxis == 1 ? (-dy) / ((ke - ks + 1) * (ie - is + 1))
+                                    : (-dz) / ((ie - is + 1) * (je - js + 1));
     for (int t = 0; t < steps; ++t) {
         const float* r = series + (size_t)t * stride + col0;
         float v = 0.f;

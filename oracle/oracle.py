@@ -66,7 +66,7 @@ def lib():
         L.or_run_f64.argtypes = [ctypes.POINTER(_Scenario), _i, _pf, _i, _pf, _pd, _pd, _i]
         L.or_onestep_f32.argtypes = [ctypes.POINTER(_Scenario), _i, _pf, _i, _pf, _pf, _pf, _pf]
         L.or_coef_f32.argtypes = [ctypes.POINTER(_Scenario), ctypes.c_char_p, _pf]
-        L.or_port_vi.argtypes = [_pf, _i, _i, _i, _pi, _pi, _i, _f, _f, _f, _i, _pf, _pf]
+        L.or_port_vi.argtypes = [_pf, _i, _i, _i, _pi, _pi, _i, _i, _f, _f, _f, _i, _pf, _pf]
         L.or_last_step_seconds.restype = ctypes.c_double
         L.or_last_step_seconds.argtypes = []
         for fn in (L.or_fom_grad_f64, L.or_fom_grad_f32, L.or_fom_grad_box_f64):
@@ -221,17 +221,20 @@ def fom_grad(sc, probe, design_box, design_eps, steps: Optional[int] = None, pre
     return (J.value, g) if grad else J.value
 
 
-def port_probes(voltage_box: Sequence[int], current_box: Sequence[int], current_axis: int = 2) -> list:
+def port_probes(voltage_box: Sequence[int], current_box: Sequence[int], current_axis: int = 2,
+                voltage_axis: int = 2) -> list:
     """Point probes (component, i, j, k) a port samples, in the order or_port_vi reads them: Ez of the
-    voltage box (k in [ks, ke) outer, j, i), then the four H groups of currMgpu's loop for
+    voltage box (k outer, j, i; half-open along ``voltage_axis``, closed across it, as voltMgpu's
+    directions sum them, fdtdrav.h:2214-2290), then the four H groups of currMgpu's loop for
     ``current_axis`` (fdtdrav.h:2318-2480; i, j, k over the current box's ranges):
     x: Hy(ie-1, j, ks-1), Hz(ie-1, je, k), Hy(ie-1, j, ke), Hz(ie-1, js-1, k);
     y: Hz(is-1, je-1, k), Hx(i, je-1, ke), Hz(ie, je-1, k), Hx(i, je-1, ks-1);
     z: Hy(ie, j, ke-1), Hx(i, js-1, ke-1), Hy(is-1, j, ke-1), Hx(i, je, ke-1)."""
     from fdtd_gb300 import scenario as S
     v, c = [int(x) for x in voltage_box], [int(x) for x in current_box]
-    out = [S.Probe(S.EZ, i, j, k) for k in range(v[2], v[5]) for j in range(v[1], v[4] + 1)
-           for i in range(v[0], v[3] + 1)]
+    end = [v[3] + (voltage_axis != 0), v[4] + (voltage_axis != 1), v[5] + (voltage_axis != 2)]
+    out = [S.Probe(S.EZ, i, j, k) for k in range(v[2], end[2]) for j in range(v[1], end[1])
+           for i in range(v[0], end[0])]
     I, J, K = range(c[0], c[3] + 1), range(c[1], c[4] + 1), range(c[2], c[5] + 1)
     if current_axis == 0:
         out += [S.Probe(S.HY, c[3] - 1, j, c[2] - 1) for j in J] + [S.Probe(S.HZ, c[3] - 1, c[4], k) for k in K]
@@ -247,9 +250,9 @@ def port_probes(voltage_box: Sequence[int], current_box: Sequence[int], current_
 
 
 def port_vi(series: np.ndarray, voltage_box: Sequence[int], current_box: Sequence[int], sc, col0: int = 0,
-            time_average: bool = True, current_axis: int = 2):
+            time_average: bool = True, current_axis: int = 2, voltage_axis: int = 2):
     """(V(t), I(t)) float32 of a port from probe series (steps, n) whose columns from ``col0`` are
-    ``port_probes(voltage_box, current_box, current_axis)``."""
+    ``port_probes(voltage_box, current_box, current_axis, voltage_axis)``."""
     a = np.ascontiguousarray(series, dtype=np.float32)
     steps, stride = a.shape
     vb = np.ascontiguousarray(voltage_box, dtype=np.int32)
@@ -258,7 +261,7 @@ def port_vi(series: np.ndarray, voltage_box: Sequence[int], current_box: Sequenc
     I = np.zeros(steps, dtype=np.float32)
     L = lib()
     if L.or_port_vi(a.ctypes.data_as(_pf), steps, stride, col0, vb.ctypes.data_as(_pi), cb.ctypes.data_as(_pi),
-                    current_axis, sc.dx, sc.dy, sc.dz, int(time_average), V.ctypes.data_as(_pf),
+                    current_axis, voltage_axis, sc.dx, sc.dy, sc.dz, int(time_average), V.ctypes.data_as(_pf),
                     I.ctypes.data_as(_pf)) != 0:
         raise RuntimeError("oracle: " + L.or_error().decode())
     return V, I

@@ -583,17 +583,25 @@ int rh_set_port(const int* vbox, const int* cbox, int n_steps) {
 }
 
 // The reference's port reductions on its own samples, launched as calcVoltCurrent does
-// (fdtdrav.h:3129-3186, NUMDEV = 1, 1-D blocks of 512): voltMgpu (direction 3) and currMgpu
-// (current_direction 1, 2 or 3), then correcI in place. Returns V(t), I(t) before correcI and
-// I(t) after it.
+// (fdtdrav.h:3129-3186, NUMDEV = 1, 1-D blocks of 512): voltMgpu (voltage_direction 1, 2 or 3)
+// and currMgpu (current_direction 1, 2 or 3), then correcI in place. Returns V(t), I(t) before
+// correcI and I(t) after it.
+int rh_port_reduce_dir(int n_steps, int voltage_direction, int current_direction, float* volt, float* curr_raw,
+                       float* curr_avg);
 int rh_port_reduce(int n_steps, int current_direction, float* volt, float* curr_raw, float* curr_avg) {
+    return rh_port_reduce_dir(n_steps, 3, current_direction, volt, curr_raw, curr_avg);
+}
+int rh_port_reduce_dir(int n_steps, int voltage_direction, int current_direction, float* volt, float* curr_raw,
+                       float* curr_avg) {
     if (g_port_steps <= 0 || n_steps != g_port_steps) { g_err = "rh_set_port first, same n_steps"; return -1; }
     float *dv = nullptr, *di = nullptr;
     if (!ck(cudaMalloc(&dv, n_steps * sizeof(float)), "cudaMalloc V") ||
         !ck(cudaMalloc(&di, n_steps * sizeof(float)), "cudaMalloc I")) { cudaFree(dv); return -1; }
     int block = 512, grid = n_steps / block + ((n_steps % block) == 0 ? 0 : 1);
-    int off = 0, dir = 3, cdir = current_direction, n = n_steps;
-    if (cdir < 1 || cdir > 3) { g_err = "current direction must be 1, 2 or 3"; cudaFree(dv); cudaFree(di); return -1; }
+    int off = 0, dir = voltage_direction, cdir = current_direction, n = n_steps;
+    if (cdir < 1 || cdir > 3 || dir < 1 || dir > 3) {
+        g_err = "directions must be 1, 2 or 3"; cudaFree(dv); cudaFree(di); return -1;
+    }
     static int vb[6], cb[6], vn[4], cn[4];
     for (int q = 0; q < 6; ++q) { vb[q] = g_vbox[q]; cb[q] = g_cbox[q]; }
     vn[0] = g_vn[0]; vn[1] = g_vn[1]; vn[2] = g_d.NZ; vn[3] = g_d.NZ_N;

@@ -55,6 +55,7 @@ class RefHarness:
         L.rh_run.argtypes = [_i, _i, _i, _pf, ctypes.c_longlong, _i, _pi, _pi, _pi, _pi, _pf, _pf]
         L.rh_set_port.argtypes = [_pi, _pi, _i]
         L.rh_port_reduce.argtypes = [_i, _i, _pf, _pf, _pf]
+        L.rh_port_reduce_dir.argtypes = [_i, _i, _i, _pf, _pf, _pf]
         L.rh_zin.argtypes = [_i, _pf, _pf, _f, _f, _pf, _pf]
         L.rh_waveform.argtypes = [_i, _f, _i, _f, _f, _f, _f, _f, _i, _pf, _pf]
         self._check(L.rh_load(cubin.encode()))
@@ -138,11 +139,12 @@ class RefHarness:
         c = np.ascontiguousarray(current_box, dtype=np.int32)
         self._check(self.lib.rh_set_port(v.ctypes.data_as(_pi), c.ctypes.data_as(_pi), steps))
 
-    def port_reduce(self, steps: int, current_direction: int = 3) -> tuple:
+    def port_reduce(self, steps: int, current_direction: int = 3, voltage_direction: int = 3) -> tuple:
         """The reference's voltMgpu / currMgpu / correcI on its samples: (V, I before correcI,
-        I after correcI), float32 arrays of ``steps``; current_direction 1 / 2 / 3 = x / y / z."""
+        I after correcI), float32 arrays of ``steps``; directions 1 / 2 / 3 = x / y / z."""
         out = [np.zeros(steps, dtype=np.float32) for _ in range(3)]
-        self._check(self.lib.rh_port_reduce(steps, current_direction, *(o.ctypes.data_as(_pf) for o in out)))
+        self._check(self.lib.rh_port_reduce_dir(steps, voltage_direction, current_direction,
+                                                *(o.ctypes.data_as(_pf) for o in out)))
         return tuple(out)
 
     def zin(self, n_t_steps: int, V: np.ndarray, I: np.ndarray, z0: complex) -> tuple:

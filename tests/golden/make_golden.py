@@ -8,7 +8,8 @@ the six final fields; plus ``onestep.npz`` (one calc_e and one calc_h applied to
 state) and ``coefs.npz`` (the reference's per-edge coefficients and 1-D CPML profiles for the
 random-box scenario); ``port.npz`` (the reference's own port sampling and time-series kernels,
 voltMgpu / currMgpu / correcI, on the port scenario, plus c_zinS11 on seeded spectra);
-``aniso.npz`` (per-axis bricks: the run and the reference's per-edge coefficient arrays). The
+``aniso.npz`` (per-axis bricks: the run and the reference's per-edge coefficient arrays);
+``port_xy.npz`` (voltMgpu's x and y directions on the port run's samples). The
 scenarios are defined in golden_scenarios.py so the tests rebuild them
 bit-for-bit without running this script.
 """
@@ -136,6 +137,20 @@ def onestep_psi(sc, seed=77):
         h.close()
 
 
+def port_xy_fixture():
+    """voltMgpu's three voltage directions (1 / 2 / 3 = x / y / z) on the reference's own Ez samples
+    of the port run: the same sampled array, other ranges and scale (fdtdrav.h:2214-2290)."""
+    sc = gs.port_scenario()
+    h = refharness.RefHarness()
+    try:
+        h.setup(sc)
+        h.set_port(gs.PORT_BOX, gs.PORT_BOX, sc.steps)
+        h.run(sc.steps, src_slot=0, signal=sc.signal_per_node(0))
+        return {f"voltage_d{d}": h.port_reduce(sc.steps, 3, d)[0] for d in (1, 2, 3)}
+    finally:
+        h.close()
+
+
 def port_fixture():
     """Port V(t) / I(t) of the reference's own sampling (calc_e / calc_h sample boxes) and
     reductions; and c_zinS11 applied to seeded random spectra (n = 700, 351 bins)."""
@@ -196,12 +211,16 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
     ap.add_argument("--analysis", default=None, help="also write large analysis-only dumps here")
-    ap.add_argument("--only", default=None, choices=["port", "plates", "marching", "aniso"], help="write one fixture only")
+    ap.add_argument("--only", default=None, choices=["port", "plates", "marching", "aniso", "port_xy"],
+                    help="write one fixture only")
     args = ap.parse_args()
     os.makedirs(args.out, exist_ok=True)
     if args.only == "port":
         np.savez_compressed(os.path.join(args.out, "port.npz"), **port_fixture())
         print("port fixture written to", args.out)
+    if args.only == "port_xy":
+        np.savez_compressed(os.path.join(args.out, "port_xy.npz"), **port_xy_fixture())
+        print("port_xy fixture written to", args.out)
         return
     if args.only == "marching":
         np.savez_compressed(os.path.join(args.out, "marching.npz"), **marching_fixture())

@@ -77,6 +77,31 @@ def test_current_loops_bitwise_vs_reference(gpu_lib, schedule):
             assert bitwise_equal(Iavg, fix[f"current_avg_d{a + 1}"]), a
 
 
+@pytest.mark.parametrize("schedule", [1, 2])
+def test_voltage_directions_bitwise_vs_reference(gpu_lib, schedule):
+    """x, y and z port voltages (voltMgpu directions 1, 2, 3) on one run, against the reference's
+    own reduction of its samples and against the oracle."""
+    import os
+    from conftest import GOLDEN
+    from fdtd_gb300 import solver
+    if not os.path.exists(os.path.join(GOLDEN, "port_xy.npz")):
+        pytest.skip("port_xy fixture not generated")
+    sc = gs.port_scenario()
+    fix = golden("port_xy")
+    with solver.Simulation.from_scenario(sc, schedule, probe_capacity=sc.steps) as sim:
+        ids = [sim.add_port(gs.PORT_BOX, gs.PORT_BOX, voltage_axis=a) for a in (0, 1, 2)]
+        sim.step(sc.steps)
+        sim.synchronize()
+        series = sim.read_probes(0, sc.steps)
+        col = len(sc.probes)
+        for a, pid in enumerate(ids):
+            V, _ = sim.read_port(pid)
+            assert bitwise_equal(V, fix[f"voltage_d{a + 1}"]), a
+            Vo, _ = oracle.port_vi(series, gs.PORT_BOX, gs.PORT_BOX, sc, col0=col, voltage_axis=a)
+            assert bitwise_equal(Vo, V), a
+            col += len(oracle.port_probes(gs.PORT_BOX, gs.PORT_BOX, voltage_axis=a))
+
+
 def test_port_columns_in_probe_series(gpu_lib):
     from fdtd_gb300 import solver
     sc = gs.port_scenario()
@@ -134,9 +159,10 @@ def test_port_validation(gpu_lib):
             with pytest.raises(solver.FDTDError) as e:
                 sim.add_port(vbox, cbox)
             assert e.value.code == FDTD_ERR_INVALID
-        with pytest.raises(solver.FDTDError) as e:
-            sim.add_port(gs.PORT_BOX, gs.PORT_BOX, voltage_axis=0)
-        assert e.value.code == FDTD_ERR_INVALID
+        for vbox, axis in [(gs.PORT_BOX, 3), ((14, 13, 9, 14, 14, 12), 0), ((14, 13, 9, 15, 13, 12), 1)]:
+            with pytest.raises(solver.FDTDError) as e:  # unknown axis; empty x range; empty y range
+                sim.add_port(vbox, gs.PORT_BOX, voltage_axis=axis)
+            assert e.value.code == FDTD_ERR_INVALID
         pid = sim.add_port(gs.PORT_BOX, gs.PORT_BOX)
         sim.step(4)
         with pytest.raises(solver.FDTDError) as e:

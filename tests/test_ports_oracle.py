@@ -38,6 +38,20 @@ def reference_average(raw: np.ndarray) -> np.ndarray:
     return out
 
 
+@pytest.mark.skipif(not os.path.exists(os.path.join(GOLDEN, "port_xy.npz")), reason="port_xy fixture not generated")
+@pytest.mark.parametrize("axis", [0, 1, 2])
+def test_voltage_directions_bitwise(axis):
+    """voltMgpu's x, y and z directions: the same Ez samples summed over the ranges each direction
+    takes, times its scale."""
+    sc = gs.port_scenario()
+    fix = golden("port")
+    prof = {k: fix[v] for k, v in PROFILE_KEYS.items()}
+    probes = list(sc.probes) + oracle.port_probes(gs.PORT_BOX, gs.PORT_BOX, voltage_axis=axis)
+    series, _ = oracle.run(sc, profile_override=prof, probes=probes)
+    V, _ = oracle.port_vi(series, gs.PORT_BOX, gs.PORT_BOX, sc, col0=len(sc.probes), voltage_axis=axis)
+    assert bitwise_equal(V, golden("port_xy")[f"voltage_d{axis + 1}"])
+
+
 def oracle_port(time_average=True):
     sc = gs.port_scenario()
     fix = golden("port")
