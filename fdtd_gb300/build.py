@@ -19,8 +19,9 @@ LIB = os.path.join(HERE, "libfdtd_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code: no floating-point contraction, so that it gives the same bits on x86-64 and aarch64
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-              "--expt-relaxed-constexpr", "-I" + INCLUDE, "-I" + CSRC]
+              "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr", "-I" + INCLUDE, "-I" + CSRC]
 
 
 def nvcc() -> str:

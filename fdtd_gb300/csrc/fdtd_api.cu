@@ -665,6 +665,65 @@ int fdtd_add_plate(fdtd_handle* h, int32_t normal_axis, const int32_t box[6], fl
     return FDTD_OK;
 }
 
+// The sector test of tricheck (fdtdrav.h:56-128) as the reference's kernel evaluates it: point q
+// against the sides p0-p1 and p1-p2 of the triangle p0 p1 p2 (q on the same side of each as the
+// third vertex, or on it) and the disk of radius r around p1. Coordinates are node index times the
+// cell size in float; a coordinate difference a*d - b*d is one float multiply-add of the first
+// product, fma(a, d, -(b*d)), as the reference's compiled kernel forms it (which decides nodes that
+// lie exactly on a side); the side tests multiply those differences in double, the distance is a
+// float sum of squares, again with the first product fused, then a double square root.
+struct SectorPt {
+    int i, j;
+};
+static float sub_f(int a, int b, float d) { return std::fma((float)a, d, -((float)b * d)); }
+static double cross_d(double ax, double ay, double bx, double by) { return std::fma(ax, by, -(ay * bx)); }
+static bool in_sector(SectorPt q, const int32_t* t, float dx, float dy, float r) {
+    const double ax = sub_f(t[2], t[0], dx), ay = sub_f(t[3], t[1], dy);  // p1 - p0
+    const double bx = sub_f(t[4], t[2], dx), by = sub_f(t[5], t[3], dy);  // p2 - p1
+    const double cx = sub_f(t[4], t[0], dx), cy = sub_f(t[5], t[1], dy);  // p2 - p0
+    const double dx0 = sub_f(t[0], t[2], dx), dy0 = sub_f(t[1], t[3], dy);  // p0 - p1
+    if (cross_d(ax, ay, cx, cy) * cross_d(ax, ay, sub_f(q.i, t[0], dx), sub_f(q.j, t[1], dy)) < 0) return false;
+    if (cross_d(bx, by, dx0, dy0) * cross_d(bx, by, sub_f(q.i, t[2], dx), sub_f(q.j, t[3], dy)) < 0) return false;
+    const float u = sub_f(t[2], q.i, dx), v = sub_f(t[3], q.j, dy);
+    return !(std::sqrt((double)std::fma(u, u, v * v)) > (double)r);
+}
+
+int fdtd_add_sector(fdtd_handle* h, const int32_t tri[6], int32_t pz0, float radius, int32_t max_x, int32_t max_y,
+                    float sigma_x, float sigma_y) {
+    if (!h || !tri) return fail(FDTD_ERR_INVALID, "NULL argument");
+    if (h->step > 0) return fail(FDTD_ERR_STATE, "sectors must be added before the first step");
+    if (h->has_design) return fail(FDTD_ERR_STATE, "sectors cannot be combined with a design region");
+    const DeviceGrid& g = h->g;
+    if (pz0 < 0 || pz0 >= g.nz) return fail(FDTD_ERR_INVALID, "sector plane outside the grid");
+    if (max_x < 0 || max_y < 0) return fail(FDTD_ERR_INVALID, "sector bounds must be >= 0");
+    if (!(sigma_x >= 0.f) || !(sigma_y >= 0.f)) return fail(FDTD_ERR_INVALID, "sector conductivities must be >= 0");
+    auto in = [&](int i, int j) { return in_sector(SectorPt{i, j}, tri, g.dx, g.dy, radius); };
+    // Ex edges as one-row z plates (their Ey range is empty), Ey edges as one-column x plates (their
+    // Ez range is empty); the set is the same as the reference's, runs split where the test fails
+    const int ex_i = std::min(max_x, g.nx), ex_j = std::min(max_y, g.ny - 1);  // Ex: i < max_x, j <= max_y
+    const int ey_i = std::min(max_x, g.nx - 1), ey_j = std::min(max_y, g.ny);  // Ey: i <= max_x, j < max_y
+    std::vector<PlateDef> add;
+    for (int j = 0; j <= ex_j; ++j)
+        for (int i = 0; i < ex_i;) {
+            if (!in(i, j)) { ++i; continue; }
+            int e = i;
+            while (e + 1 < ex_i && in(e + 1, j)) ++e;
+            add.push_back(PlateDef{2, {i, j, pz0, e + 1, j, pz0}, {sigma_x, 0.f}});
+            i = e + 1;
+        }
+    for (int i = 0; i <= ey_i; ++i)
+        for (int j = 0; j < ey_j;) {
+            if (!in(i, j)) { ++j; continue; }
+            int e = j;
+            while (e + 1 < ey_j && in(i, e + 1)) ++e;
+            add.push_back(PlateDef{0, {i, j, pz0, i, e + 1, pz0}, {sigma_y, 0.f}});
+            j = e + 1;
+        }
+    h->plates.insert(h->plates.end(), add.begin(), add.end());
+    h->dirty_lumped = true;
+    return FDTD_OK;
+}
+
 int fdtd_add_probe(fdtd_handle* h, int32_t comp, int32_t i, int32_t j, int32_t k, int32_t* id_out) {
     if (!h) return fail(FDTD_ERR_INVALID, "handle is NULL");
     if (comp < 0 || comp > 5) return fail(FDTD_ERR_INVALID, "component must be 0..5");

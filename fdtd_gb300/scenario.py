@@ -110,6 +110,64 @@ class Plate:
     sigma_2: float                            # sigma_e of the second
 
 
+def sector_edges(tri: Sequence[int], pz0: int, radius: float, max_x: int, max_y: int, dx: float, dy: float,
+                 nx: int, ny: int):
+    """Boolean (ny, nx) masks of the Ex and Ey edges in plane pz0 that a sector plate covers
+    (fdtd_add_sector; defineSec / tricheck, fdtdrav.h:1681-1744, 56-128): node (i, j) on the side
+    of the third vertex of the sides p0-p1 and p1-p2 (or on them) and within ``radius`` of the apex
+    p1; Ex for i < max_x, j <= max_y, Ey for i <= max_x, j < max_y. Evaluated as fdtd_add_sector
+    does: a coordinate difference a*d - b*d is the float multiply-add fma(a, d, -(b*d)), the side
+    tests multiply differences in double, the distance is the float fma(u, u, v*v) under a double
+    square root. The float multiply-adds are formed exactly in extended precision (64-bit or wider
+    mantissa) and rounded once."""
+    f32, ld = np.float32, np.longdouble
+    if np.finfo(ld).nmant < 63:
+        raise RuntimeError("sector_edges needs an extended-precision long double")
+    dxf, dyf = f32(dx), f32(dy)
+
+    def sub(a, b, d):  # fma(a, d, -(b * d)) in float: a, b integer arrays or scalars
+        a = np.asarray(a, dtype=np.int64).astype(f32)
+        b = np.asarray(b, dtype=np.int64).astype(f32)
+        return (a.astype(ld) * ld(d) - (b * d).astype(ld)).astype(f32)
+
+    def cross(ax, ay, bx, by):  # fma(ax, by, -(ay * bx)) in double; the products of float values are exact
+        return (np.asarray(ax, np.float64) * np.asarray(by, np.float64)
+                - np.asarray(ay, np.float64) * np.asarray(bx, np.float64))
+
+    t = [int(v) for v in tri]
+    i = np.arange(nx)[None, :]
+    j = np.arange(ny)[:, None]
+    ax, ay = sub(t[2], t[0], dxf), sub(t[3], t[1], dyf)
+    bx, by = sub(t[4], t[2], dxf), sub(t[5], t[3], dyf)
+    cx, cy = sub(t[4], t[0], dxf), sub(t[5], t[1], dyf)
+    ex0, ey0 = sub(t[0], t[2], dxf), sub(t[1], t[3], dyf)
+    s1 = cross(ax, ay, cx, cy) * cross(ax, ay, sub(i, t[0], dxf), sub(j, t[1], dyf))
+    s2 = cross(bx, by, ex0, ey0) * cross(bx, by, sub(i, t[2], dxf), sub(j, t[3], dyf))
+    u, v = sub(t[2], i, dxf), sub(t[3], j, dyf)
+    d2 = (u.astype(ld) * u.astype(ld) + (v * v).astype(ld)).astype(f32)
+    inside = (s1 >= 0) & (s2 >= 0) & ~(np.sqrt(d2.astype(np.float64)) > float(f32(radius)))
+    i, j = np.arange(nx)[None, :], np.arange(ny)[:, None]
+    return inside & (i < max_x) & (j <= max_y), inside & (i <= max_x) & (j < max_y)
+
+
+def sector_plates(tri: Sequence[int], pz0: int, radius: float, max_x: int, max_y: int, sigma_x: float,
+                  sigma_y: float, dx: float, dy: float, nx: int, ny: int) -> List["Plate"]:
+    """The sector plate as plates with the same edges (as fdtd_add_sector builds it): per row, runs
+    of covered Ex edges as one-row z plates; per column, runs of covered Ey edges as one-column x
+    plates."""
+    ex, ey = sector_edges(tri, pz0, radius, max_x, max_y, dx, dy, nx, ny)
+    out = []
+    for j in range(ny):
+        row = np.flatnonzero(ex[j])
+        for run in np.split(row, np.flatnonzero(np.diff(row) > 1) + 1) if row.size else []:
+            out.append(Plate(2, (int(run[0]), j, pz0, int(run[-1]) + 1, j, pz0), sigma_x, 0.0))
+    for i in range(nx):
+        col = np.flatnonzero(ey[:, i])
+        for run in np.split(col, np.flatnonzero(np.diff(col) > 1) + 1) if col.size else []:
+            out.append(Plate(0, (i, int(run[0]), pz0, i, int(run[-1]) + 1, pz0), sigma_y, 0.0))
+    return out
+
+
 @dataclasses.dataclass
 class Probe:
     component: int

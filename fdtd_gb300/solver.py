@@ -88,6 +88,7 @@ SIGNATURES = {
     "fdtd_adjoint_forward": (ctypes.c_int, [_vp, _i64, _i32, _i32, _i32, _i32, ctypes.POINTER(ctypes.c_double)]),
     "fdtd_adjoint_backward": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
     "fdtd_add_plate": (ctypes.c_int, [_vp, _i32, _pi32, ctypes.c_float, ctypes.c_float]),
+    "fdtd_add_sector": (ctypes.c_int, [_vp, _pi32, _i32, ctypes.c_float, _i32, _i32, ctypes.c_float, ctypes.c_float]),
     "fdtd_add_port": (ctypes.c_int, [_vp, _i32, _pi32, _i32, _pi32, _pi32]),
     "fdtd_read_port": (ctypes.c_int, [_vp, _i32, _i64, _i64, _i32, _pf, _pf]),
     "fdtd_port_spectrum": (ctypes.c_int, [_vp, _i32, _i64, _i64, ctypes.c_float, ctypes.c_float, _pf, _pf, _pf, _pf]),
@@ -232,6 +233,13 @@ class Simulation:
     def add_plate(self, normal_axis: int, box: Sequence[int], sigma_1: float, sigma_2: float) -> None:
         """Zero-thickness plate normal to ``normal_axis`` (fdtd_add_plate)."""
         _check(_lib.fdtd_add_plate(self._h, normal_axis, _box(box), sigma_1, sigma_2))
+
+    def add_sector(self, tri: Sequence[int], pz0: int, radius: float, max_x: int, max_y: int, sigma_x: float,
+                   sigma_y: float) -> None:
+        """Zero-thickness sector plate in plane pz0 (fdtd_add_sector); tri = (px0, py0, px1, py1,
+        px2, py2), apex (px1, py1)."""
+        t = (ctypes.c_int32 * 6)(*[int(v) for v in tri])
+        _check(_lib.fdtd_add_sector(self._h, t, pz0, radius, max_x, max_y, sigma_x, sigma_y))
 
     def add_port(self, voltage_box: Sequence[int], current_box: Sequence[int], current_axis: int = 2,
                  voltage_axis: int = 2) -> int:

@@ -130,6 +130,16 @@ int fdtd_add_resistor(fdtd_handle* h, int32_t axis, const int32_t box[6], float 
  * applied at fdtdrav.h:4162-4182). A plate may not cover the Ez edge of a lumped element, and
  * handles with plates take no design region and join no batch. */
 int fdtd_add_plate(fdtd_handle* h, int32_t normal_axis, const int32_t box[6], float sigma_1, float sigma_2);
+/* Zero-thickness sector plate in plane k = pz0: the Ex edges of nodes (i, j), i in [0, max_x),
+ * j in [0, max_y], and the Ey edges of nodes i in [0, max_x], j in [0, max_y), whose position
+ * (i dx, j dy) lies in the sector with apex (px1, py1), sides towards (px0, py0) and (px2, py2)
+ * (node indices; tri = {px0, py0, px1, py1, px2, py2}) and radius `radius` (metres) take sigma_x /
+ * sigma_y, like a plate (later plates and sectors override earlier ones). The test is the
+ * reference's kernel's, with its roundings (nodes exactly on a side included or not as it does):
+ * the point lies on the side of the third vertex of both sides and within the radius of the apex.
+ * Replaces defineSec / tricheck (fdtdrav.h:1681-1744, 56-128). */
+int fdtd_add_sector(fdtd_handle* h, const int32_t tri[6], int32_t pz0, float radius, int32_t max_x, int32_t max_y,
+                    float sigma_x, float sigma_y);
 
 /* Point probe of one field component at node (i,j,k): records, every step, the value right after
  * the component's main update and before its CPML correction, as sampleField does

@@ -34,14 +34,14 @@ cudaLibrary_t g_lib = nullptr;
 
 struct Kern { const char* name; cudaKernel_t k; };
 enum { K_SETZERO, K_SETBRICK, K_SETSIGMA, K_SETCOEF, K_SETABCPML, K_SRCZ, K_RES, K_CALCE, K_CALCH,
-       K_VOLT, K_CURR, K_CORREC, K_PLATEX, K_PLATEY, K_PLATEZ, K_GAUSS, K_SINE, K_ZIN, K_GATHER, K_COUNT };
+       K_VOLT, K_CURR, K_CORREC, K_PLATEX, K_PLATEY, K_PLATEZ, K_GAUSS, K_SINE, K_SEC, K_ZIN, K_GATHER, K_COUNT };
 Kern g_k[K_COUNT] = {
     {"_Z7setZero", nullptr}, {"_Z8setBrick", nullptr}, {"_Z18setSigmaEpsSigmaMu", nullptr},
     {"_Z15setCoefficients", nullptr}, {"_Z9setABCPML", nullptr}, {"_Z13defineSourceZ", nullptr},
     {"_Z14defineResistor", nullptr}, {"_Z6calc_e", nullptr}, {"_Z6calc_h", nullptr},
     {"_Z8voltMgpu", nullptr}, {"_Z8currMgpu", nullptr}, {"_Z7correcI", nullptr},
     {"_Z12definePlateX", nullptr}, {"_Z12definePlateY", nullptr}, {"_Z12definePlateZ", nullptr},
-    {"_Z8setGauss", nullptr}, {"_Z7setSine", nullptr},
+    {"_Z8setGauss", nullptr}, {"_Z7setSine", nullptr}, {"_Z9defineSec", nullptr},
     {"_Z8c_zinS11P6float2S0_iS0_S0_S0_S0_S_f", nullptr}, {"harness_gather", nullptr}};
 
 // Itanium-ABI names of the reference kernels: the parameter lists of fdtdrav.h reduce to runs of
@@ -181,6 +181,7 @@ int rh_load(const char* cubin_path) {
         "5i2p2f6i",                    // definePlateZ
         "2p1f1i3f1i",                  // setGauss
         "2p1i4f1i",                    // setSine
+        "14i3f2p3f",                   // defineSec
         nullptr, nullptr};             // c_zinS11 (float2 parameters, full name above), gather
     for (int k = 0; k < K_COUNT; ++k) {
         std::string nm = (k < K_COUNT && specs[k]) ? mangled(g_k[k].name, specs[k]) : std::string(g_k[k].name);
@@ -634,6 +635,23 @@ int rh_port_reduce_dir(int n_steps, int voltage_direction, int current_direction
     }
     cudaFree(dv); cudaFree(di);
     return ok ? 0 : -1;
+}
+
+// The reference's defineSec (fdtdrav.h:1681-1744) on the set-up handle's averaged sigma_e_x /
+// sigma_e_y arrays, launched as marchingLoop's sector loop would (fdtdrav.h:4175, grid3d, block3d,
+// NUMDEV = 1); tri = {px0, py0, px1, py1, px2, py2}. Read the arrays back with rh_get.
+int rh_sector(const int* tri, int pz0, float raio, int max_x, int max_y, float sx, float sy) {
+    if (!g_ready) { g_err = "not set up"; return -1; }
+    int NX = g_d.NX, NY = g_d.NY, NZ = g_d.NZ, NZ_N = g_d.NZ_N, off = 0, mx = max_x, my = max_y;
+    int t[6] = {tri[0], tri[1], tri[2], tri[3], tri[4], tri[5]};
+    int z = pz0;
+    float r = raio, a = sx, b = sy, dx = g_d.dx, dy = g_d.dy, dz = g_d.dz;
+    static float* P[2];
+    P[0] = A("sigma_e_x");
+    P[1] = A("sigma_e_y");
+    std::vector<void*> args = {&NX, &NY, &NZ, &NZ_N, &off, &mx, &my, &t[0], &t[1], &t[2], &t[3], &t[4], &t[5], &z,
+                               &r, &a, &b, &P[0], &P[1], &dx, &dy, &dz};
+    return launch(K_SEC, grid3d(), block3d(), args) && ck(cudaDeviceSynchronize(), "defineSec sync") ? 0 : -1;
 }
 
 // The reference's c_zinS11 (fdtdrav.h:2510-2548) on given spectra of n_t_steps/2 + 1 bins

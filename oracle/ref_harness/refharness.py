@@ -56,6 +56,7 @@ class RefHarness:
         L.rh_set_port.argtypes = [_pi, _pi, _i]
         L.rh_port_reduce.argtypes = [_i, _i, _pf, _pf, _pf]
         L.rh_port_reduce_dir.argtypes = [_i, _i, _i, _pf, _pf, _pf]
+        L.rh_sector.argtypes = [_pi, _i, _f, _i, _i, _f, _f]
         L.rh_zin.argtypes = [_i, _pf, _pf, _f, _f, _pf, _pf]
         L.rh_waveform.argtypes = [_i, _f, _i, _f, _f, _f, _f, _f, _i, _pf, _pf]
         self._check(L.rh_load(cubin.encode()))
@@ -146,6 +147,11 @@ class RefHarness:
         self._check(self.lib.rh_port_reduce_dir(steps, voltage_direction, current_direction,
                                                 *(o.ctypes.data_as(_pf) for o in out)))
         return tuple(out)
+
+    def sector(self, tri, pz0: int, radius: float, max_x: int, max_y: int, sigma_x: float, sigma_y: float) -> None:
+        """The reference's defineSec on the set-up grid's sigma_e_x / sigma_e_y (read them with get)."""
+        t = np.ascontiguousarray(tri, dtype=np.int32)
+        self._check(self.lib.rh_sector(t.ctypes.data_as(_pi), pz0, radius, max_x, max_y, sigma_x, sigma_y))
 
     def zin(self, n_t_steps: int, V: np.ndarray, I: np.ndarray, z0: complex) -> tuple:
         """The reference's c_zinS11 on spectra V, I (complex64, n_t_steps // 2 + 1 bins)."""

@@ -44,3 +44,24 @@ def test_marching_scenario_structure():
     assert len(sc.resistors) == 1 and sc.sources[0].resistance == 50.0
     assert sc.pml == (6, 6, 6, 6, 6, 6)
     assert vbox[2] < vbox[5]
+
+
+def test_sector_plates_cover_the_sector_edges():
+    """sector_plates decomposes the sector's Ex and Ey edges into plates that cover exactly them."""
+    from fdtd_gb300 import scenario as S
+    nx, ny, dx, dy = 40, 34, 1e-3, 1e-3
+    tri, pz0, r, mx, my = (6, 26, 18, 12, 30, 26), 9, 0.0105, 34, 30
+    ex, ey = S.sector_edges(tri, pz0, r, mx, my, dx, dy, nx, ny)
+    cx, cy = np.zeros(ex.shape, np.int32), np.zeros(ey.shape, np.int32)
+    for p in S.sector_plates(tri, pz0, r, mx, my, 1.0, 2.0, dx, dy, nx, ny):
+        b = p.box
+        assert b[2] == b[5] == pz0
+        if p.axis == 2:  # Ex-only row run
+            assert b[1] == b[4]
+            cx[b[1], b[0]:b[3]] += 1
+        else:            # Ey-only column run
+            assert p.axis == 0 and b[0] == b[3]
+            cy[b[1]:b[4], b[0]] += 1
+    assert np.array_equal(cx, ex.astype(cx.dtype)) and np.array_equal(cy, ey.astype(cy.dtype))
+    # the apex lies in the sector, a point beyond the radius does not
+    assert ex[12, 18] and not ex[12, 33]
