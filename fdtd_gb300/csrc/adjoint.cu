@@ -227,7 +227,7 @@ __device__ __forceinline__ void adj_e_general(const StepParams& p, const AdjStat
         if (xs) { const int q = psi_off_x(g, i, j, k, side); t1 = PsiTerm{psa.f[side].e[1] + q, p.bex[i], p.aex[i], __fmul_rn(cz.bp, g.dx)}; }
         if (ys) { const int q = psi_off_y(g, i, j, k, side); t2 = PsiTerm{psa.f[2 + side].e[1] + q, p.bey[j], p.aey[j], __fmul_rn(cz.bm, g.dy)}; }
         const bool plane_lumped = !kBg && p.lumped_k[k] < p.lumped_k[k + 1];  // background nodes carry none
-        const LumpedEdge* L = plane_lumped ? find_lumped(p, i, j, k) : nullptr;
+        const LumpedEdge* L = plane_lumped ? find_lumped(p, i, j, k, 2) : nullptr;  // design handles have no Ex edges
         float aa, c1, c2;
         if (L) { aa = L->ceze; c1 = L->cezhy; c2 = L->cezhx; }
         else {

@@ -45,8 +45,26 @@ int fail(int code, const std::string& msg) {
 struct LumpedDef {
     int box[6];
     float resistance;
-    int source;  // waveform index or -1
+    int source;    // waveform index or -1
+    int axis = 2;  // 2: Ez edges (defineSourceZ / defineResistor); 0: Ex edges (defineSourceX)
 };
+
+// The edges of a lumped element: Ez edges i in [is,ie], j in [js,je], k in [ks,ke); Ex edges of
+// defineSourceX i in [is,ie), j in [js,ie] (its j bound is the box's ie, fdtdrav.h:1351), k in
+// [ks,ke]. f(i, j, k) for each, k outer.
+template <class F>
+void lumped_edges(const LumpedDef& L, F f) {
+    const int* b = L.box;
+    if (L.axis == 0) {
+        for (int k = b[2]; k <= b[5]; ++k)
+            for (int j = b[1]; j <= b[3]; ++j)
+                for (int i = b[0]; i < b[3]; ++i) f(i, j, k);
+    } else {
+        for (int k = b[2]; k < b[5]; ++k)
+            for (int j = b[1]; j <= b[4]; ++j)
+                for (int i = b[0]; i <= b[3]; ++i) f(i, j, k);
+    }
+}
 
 // A zero-thickness plate (definePlateX / Y / Z): normal axis, box, sigma_e of its two tangential
 // components in axis order.
@@ -599,17 +617,37 @@ int fdtd_add_brick(fdtd_handle* h, const int32_t box[6], int32_t material) {
 
 static int check_lumped_box(fdtd_handle* h, int32_t axis, const int32_t box[6], float r) {
     if (!box) return fail(FDTD_ERR_INVALID, "box is NULL");
-    if (axis != 2) return fail(FDTD_ERR_INVALID, "only z-directed lumped elements (axis 2) are supported");
+    if (axis != 0 && axis != 2) return fail(FDTD_ERR_INVALID, "lumped elements are x- (axis 0) or z-directed (axis 2)");
     const DeviceGrid& g = h->g;
     const int is = box[0], js = box[1], ks = box[2], ie = box[3], je = box[4], ke = box[5];
-    // Ez is updated for 0 < i < nx-1, 0 < j < ny-1, k < nz-1 (fdtdrav.h:720)
-    if (is < 1 || ie > g.nx - 2 || is > ie || js < 1 || je > g.ny - 2 || js > je || ks < 0 || ke > g.nz - 1 || ks >= ke)
-        return fail(FDTD_ERR_INVALID, "lumped box outside the updated Ez edges or empty (k range is half-open)");
+    if (axis == 2) {
+        // Ez is updated for 0 < i < nx-1, 0 < j < ny-1, k < nz-1 (fdtdrav.h:720)
+        if (is < 1 || ie > g.nx - 2 || is > ie || js < 1 || je > g.ny - 2 || js > je || ks < 0 || ke > g.nz - 1 ||
+            ks >= ke)
+            return fail(FDTD_ERR_INVALID, "lumped box outside the updated Ez edges or empty (k range is half-open)");
+    } else {
+        // defineSourceX's Ex edges i in [is,ie), j in [js,ie], k in [ks,ke]; Ex is updated for
+        // i < nx-1, 0 < j < ny-1, 0 < k < nz-1 (fdtdrav.h:665); je enters only its resistance
+        if (is < 0 || ie > g.nx - 1 || is >= ie || js < 1 || ie > g.ny - 2 || js > ie || je < js || ks < 1 ||
+            ke > g.nz - 2 || ks > ke)
+            return fail(FDTD_ERR_INVALID, "x-directed box outside the updated Ex edges or empty "
+                                          "(i in [is,ie), j in [js,ie], k in [ks,ke])");
+        if (h->has_design) return fail(FDTD_ERR_STATE, "x-directed lumped elements cannot be combined with a design region");
+    }
     if (!(r > 0.f) || !std::isfinite(r)) return fail(FDTD_ERR_INVALID, "resistance must be positive");
+    LumpedDef probe;
+    std::copy(box, box + 6, probe.box);
+    probe.axis = axis;
+    std::vector<long long> mine;
+    lumped_edges(probe, [&](int i, int j, int k) { mine.push_back(((long long)k * g.ny + j) * g.nx + i); });
+    std::sort(mine.begin(), mine.end());
     for (const LumpedDef& L : h->lumped) {
-        const int* o = L.box;
-        if (is <= o[3] && o[0] <= ie && js <= o[4] && o[1] <= je && ks < o[5] && o[2] < ke)
-            return fail(FDTD_ERR_INVALID, "lumped elements may not share edges");
+        if (L.axis != axis) continue;  // Ex and Ez edges never coincide
+        bool shared = false;
+        lumped_edges(L, [&](int i, int j, int k) {
+            shared = shared || std::binary_search(mine.begin(), mine.end(), ((long long)k * g.ny + j) * g.nx + i);
+        });
+        if (shared) return fail(FDTD_ERR_INVALID, "lumped elements may not share edges");
     }
     return FDTD_OK;
 }
@@ -623,6 +661,14 @@ int fdtd_add_lumped_source(fdtd_handle* h, int32_t axis, const int32_t box[6], f
     LumpedDef L;
     std::memcpy(L.box, box, sizeof(L.box));
     L.resistance = resistance;
+    if (axis == 0) {  // defineSourceX: coefficients only; the reference never injects it (fdtdrav.h:681)
+        L.source = -1;
+        L.axis = 0;
+        h->lumped.push_back(L);
+        h->dirty_lumped = true;
+        if (id_out) *id_out = -1;
+        return FDTD_OK;
+    }
     L.source = (int)h->waves.size();
     // per-edge signal = V / (ke - ks) (setGauss fdtdrav.h:1494 with v_mag_factor fdtdrav.h:3613)
     const float nseg = (float)(box[5] - box[2]);
@@ -637,6 +683,7 @@ int fdtd_add_lumped_source(fdtd_handle* h, int32_t axis, const int32_t box[6], f
 
 int fdtd_add_resistor(fdtd_handle* h, int32_t axis, const int32_t box[6], float resistance) {
     if (!h) return fail(FDTD_ERR_INVALID, "handle is NULL");
+    if (axis != 2) return fail(FDTD_ERR_INVALID, "resistors are z-directed (defineResistor sets Ez edges only)");
     int rc = check_lumped_box(h, axis, box, resistance);
     if (rc) return rc;
     LumpedDef L;
@@ -1085,12 +1132,10 @@ int build_lumped(fdtd_handle* h) {
     std::vector<int> owner;
     for (size_t q = 0; q < h->lumped.size(); ++q) {
         const LumpedDef& L = h->lumped[q];
-        for (int k = L.box[2]; k < L.box[5]; ++k)
-            for (int j = L.box[1]; j <= L.box[4]; ++j)
-                for (int i = L.box[0]; i <= L.box[3]; ++i) {
-                    edges.push_back(LumpedEdge{i, j, k, L.source, 0.f, 0.f, 0.f, 0.f});
-                    owner.push_back((int)q);
-                }
+        lumped_edges(L, [&](int i, int j, int k) {
+            edges.push_back(LumpedEdge{i, j, k, L.axis, L.source, 0.f, 0.f, 0.f, 0.f});
+            owner.push_back((int)q);
+        });
     }
     std::vector<int> order(edges.size());
     for (size_t q = 0; q < order.size(); ++q) order[q] = (int)q;
@@ -1191,21 +1236,20 @@ int build_plates(fdtd_handle* h) {
             }
     std::sort(nodes.begin(), nodes.end());
     nodes.erase(std::unique(nodes.begin(), nodes.end()), nodes.end());
-    // lumped Ez edges take their own coefficients from the cells' materials: no plate may cover one
-    std::vector<long long> lumped_ez;
+    // lumped edges take their own coefficients from the cells' materials: no plate may cover one
+    std::vector<long long> lumped_e[3];
     for (const LumpedDef& L : h->lumped)
-        for (int k = L.box[2]; k < L.box[5]; ++k)
-            for (int j = L.box[1]; j <= L.box[4]; ++j)
-                for (int i = L.box[0]; i <= L.box[3]; ++i) lumped_ez.push_back(((long long)k * g.ny + j) * g.nx + i);
-    std::sort(lumped_ez.begin(), lumped_ez.end());
+        lumped_edges(L, [&](int i, int j, int k) { lumped_e[L.axis].push_back(((long long)k * g.ny + j) * g.nx + i); });
+    for (auto& v : lumped_e) std::sort(v.begin(), v.end());
     for (const PlateDef& P : h->plates)
         for (const PlateRange& r : plate_ranges(g, P)) {
-            if (r.comp != 2) continue;
+            const std::vector<long long>& le = lumped_e[r.comp];
+            if (le.empty()) continue;
             for (int k = r.lo[2]; k <= r.hi[2]; ++k)
                 for (int j = r.lo[1]; j <= r.hi[1]; ++j)
                     for (int i = r.lo[0]; i <= r.hi[0]; ++i)
-                        if (std::binary_search(lumped_ez.begin(), lumped_ez.end(), ((long long)k * g.ny + j) * g.nx + i))
-                            return fail(FDTD_ERR_INVALID, "a plate covers the Ez edge of a lumped element");
+                        if (std::binary_search(le.begin(), le.end(), ((long long)k * g.ny + j) * g.nx + i))
+                            return fail(FDTD_ERR_INVALID, "a plate covers the edge of a lumped element");
         }
     std::vector<PlateEdges> flat;
     std::vector<int> koff(g.nz + 1, 0);
@@ -1530,6 +1574,9 @@ extern "C" int fdtd_set_design_region(fdtd_handle* h, const int32_t box[6], cons
     if ((int)h->materials.size() > kDesign)
         return fail(FDTD_ERR_INVALID, "material index 255 is reserved for the design region: at most 255 materials");
     if (!h->plates.empty()) return fail(FDTD_ERR_STATE, "a design region cannot be combined with plates");
+    for (const LumpedDef& L : h->lumped)
+        if (L.axis != 2)
+            return fail(FDTD_ERR_STATE, "a design region cannot be combined with x-directed lumped elements");
     for (const LumpedDef& L : h->lumped) {  // the cells of a lumped Ez edge (i,j): i-1..i, j-1..j
         const int* b = L.box;
         if (b[0] - 1 < box[3] && box[0] <= b[3] && b[1] - 1 < box[4] && box[1] <= b[4] && b[2] < box[5] && box[2] < b[5])

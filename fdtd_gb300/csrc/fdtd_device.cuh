@@ -66,9 +66,12 @@ struct PsiFace {
 };
 
 // A lumped element edge (source or resistor) with its coefficient override.
+// An Ez edge (comp 2) holds Ceze, Cezhy, Cezhx, Cezj of defineSourceZ / defineResistor; an Ex edge
+// (comp 0, defineSourceX) holds Cexe, Cexhz, Cexhy in the same slots and never injects.
 struct LumpedEdge {
     int i, j, k;
-    int source;         // index of the driving waveform, -1 for a resistor
+    int comp;           // 0: Ex, 2: Ez
+    int source;         // index of the driving waveform, -1 for a resistor or an Ex edge
     float ceze, cezhy, cezhx, cezj;
 };
 

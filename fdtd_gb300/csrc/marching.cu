@@ -82,8 +82,12 @@ extern "C" int fdtd_marching_loop(
     (void)resistor_direction;    // defineResistor always acts on z edges (fdtdrav.h:1429-1483)
     if (!voltage || !current || n_t_steps < 2 || NUMDEV < 1)
         return report_error(FDTD_ERR_INVALID, "NULL output, fewer than 2 steps or NUMDEV < 1");
-    if (source_direction != 3 || voltage_direction != 3 || current_direction < 1 || current_direction > 3)
-        return report_error(FDTD_ERR_INVALID, "z-directed source and voltage only (direction 3); current direction 1, 2 or 3");
+    // source_direction 1 / 2 would leave defineSourceZ out while calc_e still injects on the z box
+    // through the never-set Cezj (setZero's 1.2e-38): not reproduced; x-directed elements are
+    // available on their own (fdtd_add_lumped_source, axis 0)
+    if (source_direction != 3 || voltage_direction < 1 || voltage_direction > 3 || current_direction < 1 ||
+        current_direction > 3)
+        return report_error(FDTD_ERR_INVALID, "z-directed source only (direction 3); voltage and current direction 1, 2 or 3");
     // domain size (fdtdrav.h:3485-3503); NZ is rounded up to a multiple of NUMDEV as the reference
     // does, then the whole domain runs on one GPU
     const int NXX = X + air_buff_x_n + air_buff_x_p + pml_x_n + pml_x_p;
@@ -149,7 +153,7 @@ extern "C" int fdtd_marching_loop(
         sampled_voltage_max_y, sampled_voltage_max_z, vb);
     box(sampled_current_min_x, sampled_current_min_y, sampled_current_min_z, sampled_current_max_x,
         sampled_current_max_y, sampled_current_max_z, cb);
-    if ((rc = fdtd_add_port(h, 2, vb, current_direction - 1, cb, &port))) return rc;
+    if ((rc = fdtd_add_port(h, voltage_direction - 1, vb, current_direction - 1, cb, &port))) return rc;
     if ((rc = fdtd_set_probe_capacity(h, n_t_steps))) return rc;
     // the time loop (fdtdrav.h:4320-4355) and calcVoltCurrent (fdtdrav.h:3129-3186)
     if ((rc = fdtd_step(h, n_t_steps))) return rc;

@@ -99,7 +99,9 @@ cudaError_t launch_material_tables(const DeviceGrid& g, const MatProps* props, i
 }
 
 // Lumped-edge coefficient overrides (defineSourceZ fdtdrav.h:1368-1426 for sources,
-// defineResistor fdtdrav.h:1429-1483 for resistors), from the edge-averaged eps_z / sigma_z.
+// defineResistor fdtdrav.h:1429-1483 for resistors), from the edge-averaged eps_z / sigma_z; for
+// Ex edges defineSourceX's (fdtdrav.h:1311-1365) from eps_x / sigma_x, with its per-component
+// resistance (1 + je - js)(1 + ke - ks) / (ie - is) * rs and factor dt dx / (r dz dy).
 // boxes: per owner {is,js,ks,ie,je,ke}; owner[e] = index of the element an edge belongs to.
 __global__ void k_lumped_coefs(DeviceGrid g, const uint8_t* mat, const MatProps* props, LumpedEdge* edges,
                                const int* boxes, const float* resist, const int* owner, int n_edges) {
@@ -111,12 +113,30 @@ __global__ void k_lumped_coefs(DeviceGrid g, const uint8_t* mat, const MatProps*
     float rs = resist[owner[e]];
     float _is = (float)b[0], _js = (float)b[1], _ks = (float)b[2];
     float _ie = (float)b[3], _je = (float)b[4], _ke = (float)b[5];
+    const long long n = (long long)L.k * g.plane + (long long)L.j * g.pitch + L.i;
+    if (L.comp == 0) {
+        float r_comp = (1 + _je - _js) * (1 + _ke - _ks) / (_ie - _is);
+        r_comp = r_comp * rs;
+        float rfactor = (dt * dx) / (r_comp * dz * dy);
+        // eps_x / sigma_x of the edge: average of cells (i,j,k), (i,j-1,k), (i,j,k-1), (i,j-1,k-1)
+        const MatAxis a = props[mat[n]].a[0], bb = props[mat[n - g.pitch]].a[0], c = props[mat[n - g.plane]].a[0],
+                      d = props[mat[n - g.pitch - g.plane]].a[0];
+        float eps_x = avg4(a.eps, bb.eps, c.eps, d.eps);
+        float sig_x = avg4(a.sig, bb.sig, c.sig, d.sig);
+        float den = __fadd_rn(__fmaf_rn(2.0f * eps_x, eps_0, __fmul_rn(dt, sig_x)), rfactor);
+        float num = __fsub_rn(__fmaf_rn(2.0f * eps_x, eps_0, -__fmul_rn(dt, sig_x)), rfactor);
+        L.ceze = __fdiv_rn(num, den);
+        L.cezhy = __fdiv_rn(__fdiv_rn(2.0f * dt, dy), den);
+        L.cezhx = __fdiv_rn(__fdiv_rn(-2.0f * dt, dz), den);
+        L.cezj = 0.0f;  // the reference computes Cexj but never injects (calc_e, fdtdrav.h:681-685)
+        edges[e] = L;
+        return;
+    }
     float r_comp = (1 + _ie - _is) * (1 + _je - _js) / (_ke - _ks);
     r_comp = r_comp * rs;
     float rfactor = (dt * dz) / (r_comp * dx * dy);
     float rfactor_aux = (r_comp * dx * dy);
     // eps_z / sigma_z of the edge: average of cells (i,j), (i-1,j), (i,j-1), (i-1,j-1) in plane k
-    const long long n = (long long)L.k * g.plane + (long long)L.j * g.pitch + L.i;
     const MatAxis a = props[mat[n]].a[2], bb = props[mat[n - 1]].a[2], c = props[mat[n - g.pitch]].a[2],
                   d = props[mat[n - 1 - g.pitch]].a[2];
     float eps_z = avg4(a.eps, bb.eps, c.eps, d.eps);

@@ -196,12 +196,13 @@ __device__ __forceinline__ void h_update_interior(const StepParams& p, int m0, f
     out[2] = upd3(c.x, hz, c.y, dEx_j, c.z, dEy_i);
 }
 
-// Lumped-edge override for node (i,j) among the edges bucketed in plane k.
-__device__ __forceinline__ const LumpedEdge* find_lumped(const StepParams& p, int i, int j, int k) {
+// Lumped-edge override of component comp (0 Ex, 2 Ez) for node (i,j) among the edges bucketed
+// in plane k.
+__device__ __forceinline__ const LumpedEdge* find_lumped(const StepParams& p, int i, int j, int k, int comp) {
     const int b = p.lumped_k[k], e = p.lumped_k[k + 1];
     for (int q = b; q < e; ++q) {
         const LumpedEdge& L = p.lumped[q];
-        if (L.i == i && L.j == j) return &L;
+        if (L.i == i && L.j == j && L.comp == comp) return &L;
     }
     return nullptr;
 }
@@ -335,15 +336,17 @@ __device__ __forceinline__ void e_update(const StepParams& p, const ENbr& n, int
     const float dHx_k = __fsub_rn(n.hx, n.hx_km), dHz_i = __fsub_rn(n.hz, n.hz_im);
     const float dHy_i = __fsub_rn(n.hy, n.hy_im), dHx_j = __fsub_rn(n.hx, n.hx_jm);
     const BgCurl& B = p.bg;
-    // Ex (fdtdrav.h:665-676)
-    float vx = upd3(cx.a, n.ex, ys ? kdiv(cx.bp, ux && on_bg && !(pm & 1), B.e[1][0], p.key, j) : cx.bp, dHz_j,
-                    zs ? kdiv(cx.bm, ux && on_bg && !(pm & 1), B.e[2][0], p.kez, k) : cx.bm, dHy_k);
+    // Ex (fdtdrav.h:665-676), with defineSourceX's coefficients on its edges (fdtdrav.h:1311-1365)
+    const LumpedEdge* Lx = (!kBg && plane_lumped) ? find_lumped(p, i, j, k, 0) : nullptr;
+    float vx = Lx ? upd3(Lx->ceze, n.ex, Lx->cezhy, dHz_j, Lx->cezhx, dHy_k)
+                  : upd3(cx.a, n.ex, ys ? kdiv(cx.bp, ux && on_bg && !(pm & 1), B.e[1][0], p.key, j) : cx.bp, dHz_j,
+                         zs ? kdiv(cx.bm, ux && on_bg && !(pm & 1), B.e[2][0], p.kez, k) : cx.bm, dHy_k);
     // Ey (fdtdrav.h:696-707)
     float vy = upd3(cy.a, n.ey, zs ? kdiv(cy.bp, uy && on_bg && !(pm & 2), B.e[2][1], p.kez, k) : cy.bp, dHx_k,
                     xs ? kdiv(cy.bm, uy && on_bg && !(pm & 2), B.e[0][0], p.kex, i) : cy.bm, dHz_i);
     // Ez with lumped elements (fdtdrav.h:720-741)
     float vz;
-    const LumpedEdge* L = (!kBg && plane_lumped) ? find_lumped(p, i, j, k) : nullptr;
+    const LumpedEdge* L = (!kBg && plane_lumped) ? find_lumped(p, i, j, k, 2) : nullptr;
     if (L) {
         if (L->source >= 0) {
             const float s = m < p.wave_len[L->source] ? p.waves[L->source][m] : 0.f;

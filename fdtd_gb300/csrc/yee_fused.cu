@@ -145,9 +145,10 @@ static __device__ __noinline__ float3 e_slow(const StepParams* pp, int i, int j,
         if (hit & 4) cz = pc[2];
     }
     float3 r;
-    r.x = upd3(cx.a, ex, cx.bp, dHz_j, cx.bm, dHy_k);
+    const LumpedEdge* Lx = plane_lumped ? find_lumped(p, i, j, k, 0) : nullptr;  // defineSourceX edge
+    r.x = Lx ? upd3(Lx->ceze, ex, Lx->cezhy, dHz_j, Lx->cezhx, dHy_k) : upd3(cx.a, ex, cx.bp, dHz_j, cx.bm, dHy_k);
     r.y = upd3(cy.a, ey, cy.bp, dHx_k, cy.bm, dHz_i);
-    const LumpedEdge* L = plane_lumped ? find_lumped(p, i, j, k) : nullptr;
+    const LumpedEdge* L = plane_lumped ? find_lumped(p, i, j, k, 2) : nullptr;
     if (L) {
         if (L->source >= 0) {
             const float s = m < p.wave_len[L->source] ? p.waves[L->source][m] : 0.f;

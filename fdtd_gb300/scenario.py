@@ -194,6 +194,9 @@ class Scenario:
     resistors: List[Resistor] = dataclasses.field(default_factory=list)
     probes: List[Probe] = dataclasses.field(default_factory=list)
     plates: List[Plate] = dataclasses.field(default_factory=list)
+    # x-directed lumped elements of defineSourceX (fdtdrav.h:1311-1365): Ex edges i in [is,ie),
+    # j in [js,ie], k in [ks,ke] with its load coefficients; never injected (waveform unused)
+    x_sources: List[LumpedSource] = dataclasses.field(default_factory=list)
     eps0: float = float(REF_EPS0)
     mu0: float = float(REF_MU0)
     pi: float = float(REF_PI)

@@ -393,6 +393,8 @@ class Simulation:
                 sim.add_brick(b.box, b.material)
         for s in sc.sources:
             sim.add_source(s.box, s.resistance, s.waveform)
+        for s in getattr(sc, "x_sources", []):
+            sim.add_source(s.box, s.resistance, np.zeros(0, np.float32), axis=0)
         for r in sc.resistors:
             sim.add_resistor(r.box, r.resistance)
         for q in sc.plates:

@@ -70,6 +70,8 @@ typedef struct {
     // zero-thickness plates, applied in order: (nplate, 7) ints axis, is, js, ks, ie, je, ke and
     // (nplate, 2) floats sigma_e of the two tangential components in axis order
     int nplate; const int* plate; const float* plate_sig;
+    // x-directed elements of defineSourceX: boxes is,js,ks,ie,je,ke and resistances
+    int nsrcx; const int* srcx_box; const float* srcx_r;
 } or_scenario;
 
 const char* or_error(void) { return g_err.c_str(); }
@@ -334,6 +336,27 @@ int setup(Sim<R>& s, const or_scenario* sc, const float* signal_per_node, int n_
         s.signal.push_back(sig);
     }
     for (int q = 0; q < sc->nres; ++q) lumped(sc->res_box + 6 * q, sc->res_r[q], false);
+    // defineSourceX (fdtdrav.h:1311-1365): Ex edges i in [is,ie), j in [js,ie] (its j bound),
+    // k in [ks,ke]; Cexj is never used (calc_e leaves the x injection out, fdtdrav.h:681)
+    for (int q = 0; q < sc->nsrcx; ++q) {
+        const int* bx = sc->srcx_box + 6 * q;
+        R is = bx[0], js = bx[1], ks = bx[2], ie = bx[3], je = bx[4], ke = bx[5];
+        R r_comp = (((R)1 + je) - js) * (((R)1 + ke) - ks) / (ie - is);
+        r_comp = r_comp * (R)sc->srcx_r[q];
+        R rfactor = (dt * dx) / ((r_comp * dz) * dy);
+        for (int k = bx[2]; k <= bx[5]; ++k)
+            for (int j = bx[1]; j <= bx[3]; ++j)
+                for (int i = bx[0]; i < bx[3]; ++i) {
+                    size_t n = s.id(i, j, k);
+                    R two_e = (R)2 * s.eps_x[n];
+                    R dts = dt * s.sig_x[n];
+                    R den = FMA<R>(two_e, s.eps0, dts) + rfactor;
+                    R num = FMA<R>(two_e, s.eps0, -dts) - rfactor;
+                    s.Cexe[n] = num / den;
+                    s.Cexhz[n] = (((R)2 * dt) / dy) / den;
+                    s.Cexhy[n] = (((R)-2 * dt) / dz) / den;
+                }
+    }
     for (int p = 0; p < sc->nprobe; ++p) {
         std::array<int, 4> pr;
         for (int t = 0; t < 4; ++t) pr[t] = sc->probe[4 * p + t];

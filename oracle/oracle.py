@@ -41,7 +41,8 @@ class _Scenario(ctypes.Structure):
                 ("nprobe", _i), ("probe", _pi),
                 ("profile_override", ctypes.POINTER(_pf)),
                 ("design_box", _i * 6), ("design_eps", ctypes.POINTER(ctypes.c_double)),
-                ("nplate", _i), ("plate", _pi), ("plate_sig", _pf)]
+                ("nplate", _i), ("plate", _pi), ("plate_sig", _pf),
+                ("nsrcx", _i), ("srcx_box", _pi), ("srcx_r", _pf)]
 
 
 def build(force: bool = False) -> str:
@@ -103,7 +104,11 @@ class _Prepared:
         plates = getattr(sc, "plates", [])
         pl = np.array([[q.axis, *q.box] for q in plates], dtype=np.int32).reshape(-1, 7)
         ps = np.array([[q.sigma_1, q.sigma_2] for q in plates], dtype=np.float32).reshape(-1, 2)
-        self.keep += [mat, tab, sb, sr, rb, rr, pr, pl, ps]
+        xs = getattr(sc, "x_sources", [])
+        xb = np.array([x.box for x in xs], dtype=np.int32).reshape(-1, 6)
+        xr = np.array([x.resistance for x in xs], dtype=np.float32)
+        self.keep += [mat, tab, sb, sr, rb, rr, pr, pl, ps, xb, xr]
+        s.nsrcx, s.srcx_box, s.srcx_r = len(xs), xb.ctypes.data_as(_pi), xr.ctypes.data_as(_pf)
         s.nplate, s.plate, s.plate_sig = len(plates), pl.ctypes.data_as(_pi), ps.ctypes.data_as(_pf)
         s.mat, s.table, s.n_mat = mat.ctypes.data_as(_pu8), tab.ctypes.data_as(_pf), tab.shape[0]
         s.nsrc, s.src_box, s.src_r = len(sc.sources), sb.ctypes.data_as(_pi), sr.ctypes.data_as(_pf)

@@ -34,14 +34,15 @@ cudaLibrary_t g_lib = nullptr;
 
 struct Kern { const char* name; cudaKernel_t k; };
 enum { K_SETZERO, K_SETBRICK, K_SETSIGMA, K_SETCOEF, K_SETABCPML, K_SRCZ, K_RES, K_CALCE, K_CALCH,
-       K_VOLT, K_CURR, K_CORREC, K_PLATEX, K_PLATEY, K_PLATEZ, K_GAUSS, K_SINE, K_SEC, K_ZIN, K_GATHER, K_COUNT };
+       K_VOLT, K_CURR, K_CORREC, K_PLATEX, K_PLATEY, K_PLATEZ, K_GAUSS, K_SINE, K_SEC, K_SRCX, K_ZIN, K_GATHER,
+       K_COUNT };
 Kern g_k[K_COUNT] = {
     {"_Z7setZero", nullptr}, {"_Z8setBrick", nullptr}, {"_Z18setSigmaEpsSigmaMu", nullptr},
     {"_Z15setCoefficients", nullptr}, {"_Z9setABCPML", nullptr}, {"_Z13defineSourceZ", nullptr},
     {"_Z14defineResistor", nullptr}, {"_Z6calc_e", nullptr}, {"_Z6calc_h", nullptr},
     {"_Z8voltMgpu", nullptr}, {"_Z8currMgpu", nullptr}, {"_Z7correcI", nullptr},
     {"_Z12definePlateX", nullptr}, {"_Z12definePlateY", nullptr}, {"_Z12definePlateZ", nullptr},
-    {"_Z8setGauss", nullptr}, {"_Z7setSine", nullptr}, {"_Z9defineSec", nullptr},
+    {"_Z8setGauss", nullptr}, {"_Z7setSine", nullptr}, {"_Z9defineSec", nullptr}, {"_Z13defineSourceX", nullptr},
     {"_Z8c_zinS11P6float2S0_iS0_S0_S0_S0_S_f", nullptr}, {"harness_gather", nullptr}};
 
 // Itanium-ABI names of the reference kernels: the parameter lists of fdtdrav.h reduce to runs of
@@ -155,6 +156,7 @@ typedef struct {
     int nsources; const int* src_box; const float* src_r;       // box is,js,ks,ie,je,ke
     int nres; const int* res_box; const float* res_r;
     int nplates; const int* plate; const float* plate_sig;  // (n, 7): axis, box; (n, 2): sigma_e pair
+    int nsrcx; const int* srcx_box; const float* srcx_r;     // defineSourceX boxes and resistances
 } rh_scenario;
 
 const char* rh_error(void) { return g_err.c_str(); }
@@ -182,6 +184,7 @@ int rh_load(const char* cubin_path) {
         "2p1f1i3f1i",                  // setGauss
         "2p1i4f1i",                    // setSine
         "14i3f2p3f",                   // defineSec
+        "13i6p6f",                     // defineSourceX
         nullptr, nullptr};             // c_zinS11 (float2 parameters, full name above), gather
     for (int k = 0; k < K_COUNT; ++k) {
         std::string nm = (k < K_COUNT && specs[k]) ? mangled(g_k[k].name, specs[k]) : std::string(g_k[k].name);
@@ -349,6 +352,19 @@ int rh_setup(const rh_scenario* s) {
         a.push_back(&rs); a.push_back(&g_d.dx); a.push_back(&g_d.dy); a.push_back(&g_d.dz); a.push_back(&g_d.dt);
         a.push_back(&g_d.eps0);
         if (!launch(K_SRCZ, grid3d(), block3d(), a)) { free_all(); return -1; }
+    }
+    // defineSourceX per x-directed element (fdtdrav.h:1311, called at 4278 for source_direction 1)
+    for (int q = 0; q < s->nsrcx; ++q) {
+        const int* bx = s->srcx_box + 6 * q;
+        int is = bx[0], js = bx[1], ks = bx[2], ie = bx[3], je = bx[4], ke = bx[5];
+        float rs = s->srcx_r[q];
+        static float* P[6];
+        const char* order[] = {"Cexe", "Cexhz", "Cexhy", "Cexj", "eps_r_x", "sigma_e_x"};
+        std::vector<void*> a = {&NX, &NXX, &NY, &NYY, &NZ, &NZ_N, &off, &is, &js, &ks, &ie, &je, &ke};
+        for (int r = 0; r < 6; ++r) { P[r] = A(order[r]); a.push_back(&P[r]); }
+        a.push_back(&rs); a.push_back(&g_d.dx); a.push_back(&g_d.dy); a.push_back(&g_d.dz); a.push_back(&g_d.dt);
+        a.push_back(&g_d.eps0);
+        if (!launch(K_SRCX, grid3d(), block3d(), a)) { free_all(); return -1; }
     }
     // defineResistor per resistor (fdtdrav.h:1429, called at 4295-4309)
     for (int q = 0; q < s->nres; ++q) {

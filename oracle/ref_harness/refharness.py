@@ -30,7 +30,8 @@ class _Scenario(ctypes.Structure):
                 ("nbricks", _i), ("brick_box", _pi), ("brick_mat", _pf),
                 ("nsources", _i), ("src_box", _pi), ("src_r", _pf),
                 ("nres", _i), ("res_box", _pi), ("res_r", _pf),
-                ("nplates", _i), ("plate", _pi), ("plate_sig", _pf)]
+                ("nplates", _i), ("plate", _pi), ("plate_sig", _pf),
+                ("nsrcx", _i), ("srcx_box", _pi), ("srcx_r", _pf)]
 
 
 def available() -> bool:
@@ -85,8 +86,12 @@ class RefHarness:
         plates = getattr(sc, "plates", [])
         pl = np.array([[q.axis, *q.box] for q in plates], dtype=np.int32).reshape(-1, 7)
         ps = np.array([[q.sigma_1, q.sigma_2] for q in plates], dtype=np.float32).reshape(-1, 2)
-        self._keep = [np.ascontiguousarray(a) for a in (bb, bm, sb, sr, rb, rr, pl, ps)]
-        bb, bm, sb, sr, rb, rr, pl, ps = self._keep
+        xs = getattr(sc, "x_sources", [])
+        xb = np.array([x.box for x in xs], dtype=np.int32).reshape(-1, 6)
+        xr = np.array([x.resistance for x in xs], dtype=np.float32)
+        self._keep = [np.ascontiguousarray(a) for a in (bb, bm, sb, sr, rb, rr, pl, ps, xb, xr)]
+        bb, bm, sb, sr, rb, rr, pl, ps, xb, xr = self._keep
+        s.nsrcx, s.srcx_box, s.srcx_r = len(xs), xb.ctypes.data_as(_pi), xr.ctypes.data_as(_pf)
         s.nplates, s.plate, s.plate_sig = len(plates), pl.ctypes.data_as(_pi), ps.ctypes.data_as(_pf)
         s.nbricks, s.brick_box, s.brick_mat = len(sc.bricks), bb.ctypes.data_as(_pi), bm.ctypes.data_as(_pf)
         s.nsources, s.src_box, s.src_r = len(sc.sources), sb.ctypes.data_as(_pi), sr.ctypes.data_as(_pf)

@@ -40,7 +40,7 @@ def reference_run(a):
         h.setup(sc)
         h.set_port(vbox, cbox, n)
         h.run(n, src_slot=0, signal=per)
-        v, _, i_avg = h.port_reduce(n, a["current_direction"])
+        v, _, i_avg = h.port_reduce(n, a["current_direction"], a["voltage_direction"])
         return sig, v, i_avg
     finally:
         h.close()
@@ -61,12 +61,19 @@ def test_marching_loop_vs_fixture(gpu_lib):
     assert src[5] - src[2] == 3
 
 
-@pytest.mark.parametrize("kw", [dict(current_direction=3), dict(current_direction=2, source_tp=3),
-                                dict(current_direction=2, numdev=4, resistor_opt=1),
-                                dict(current_direction=2, aniso=True)])
-def test_marching_loop_vs_reference_live(gpu_lib, kw):
+@pytest.mark.parametrize("kw,extra", [(dict(current_direction=3), {}), (dict(current_direction=2, source_tp=3), {}),
+                                      (dict(current_direction=2, numdev=4, resistor_opt=1), {}),
+                                      (dict(current_direction=2, aniso=True), {}),
+                                      (dict(current_direction=1), dict(voltage_direction=1)),
+                                      (dict(current_direction=2), dict(voltage_direction=2))])
+def test_marching_loop_vs_reference_live(gpu_lib, kw, extra):
+    """Also the x and y voltage directions (voltMgpu 1 and 2); for y the voltage box gets two
+    rows."""
     from fdtd_gb300 import solver
     a = gs.marching_params(n_t_steps=300, **kw)
+    a.update(extra)
+    if a["voltage_direction"] == 2:
+        a["sampled_voltage_max_y"] = np.float32(a["sampled_voltage_max_y"] + 2 * a["dy"])
     sig, v_ref, i_ref = reference_run(a)
     w = solver.source_waveform(a["source_tp"], a["source_amp"], a["source_freq"], a["dt"], a["t_0"], a["tau"], a["pi"],
                                a["n_t_steps"])
@@ -78,7 +85,7 @@ def test_marching_loop_vs_reference_live(gpu_lib, kw):
 
 def test_marching_loop_validation(gpu_lib):
     from fdtd_gb300 import solver
-    for change in [dict(source_direction=1), dict(voltage_direction=2), dict(current_direction=4),
+    for change in [dict(source_direction=1), dict(voltage_direction=4), dict(current_direction=4),
                    dict(brick_sigma_m_y=[0.0]), dict(NUMDEV=0)]:
         a = gs.marching_params(n_t_steps=20)
         a.update(change)
