@@ -185,6 +185,10 @@ struct fdtd_handle {
         double* acc = nullptr;         // per-edge gradient accumulators
         double* grad = nullptr;        // per-cell gradient
         std::vector<void*> bufs;       // everything above, for release
+        float* pinned_samples = nullptr;  // host copies (pinned: asynchronous copies)
+        double* pinned_grad = nullptr;
+        cudaStream_t rev = nullptr;    // the reverse sweep's stream (K > 0) and its events
+        cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // recompute[2], reverse[2], start / end
     } adj;
 
     // work list of fdtd_step_static_scratch (interior items first) in pinned host memory, planned
@@ -528,6 +532,14 @@ int fdtd_destroy(fdtd_handle* h) {
     h->allocs.clear();
     h->alloc_sizes.clear();
     if (h->static_items) cudaFreeHost(h->static_items);
+    if (h->adj.pinned_samples) cudaFreeHost(h->adj.pinned_samples);
+    if (h->adj.pinned_grad) cudaFreeHost(h->adj.pinned_grad);
+    if (h->adj.rev) {
+        cudaStreamSynchronize(h->adj.rev);
+        for (cudaEvent_t e : h->adj.ev)
+            if (e) cudaEventDestroy(e);
+        cudaStreamDestroy(h->adj.rev);
+    }
     if (h->fork.aux) {
         cudaStreamSynchronize(h->fork.aux);
         cudaEventDestroy(h->fork.fork);
@@ -1621,7 +1633,16 @@ int adj_prepare(fdtd_handle* h, long long n, int K) {
     auto& A = h->adj;
     for (void* p : A.bufs) h->release(p);
     A.bufs.clear();
+    if (A.pinned_samples) cudaFreeHost(A.pinned_samples);
+    if (A.pinned_grad) cudaFreeHost(A.pinned_grad);
+    A.pinned_samples = nullptr;
+    A.pinned_grad = nullptr;
+    const cudaStream_t rev = A.rev;  // kept across runs
+    cudaEvent_t ev[5];
+    std::copy(A.ev, A.ev + 5, ev);
     A = fdtd_handle::Adjoint{};
+    A.rev = rev;
+    std::copy(ev, ev + 5, A.ev);
     const size_t V = (size_t)vol(h) * sizeof(float);
     int rc;
     for (int c = 0; c < 6; ++c) {
@@ -1648,6 +1669,8 @@ int adj_prepare(fdtd_handle* h, long long n, int K) {
         (rc = adj_alloc(h, (void**)&A.acc, sizeof(double) * 3 * (size_t)ne)) ||
         (rc = adj_alloc(h, (void**)&A.grad, sizeof(double) * nd)))
         return rc;
+    CUDA_TRY(cudaMallocHost((void**)&A.pinned_samples, sizeof(float) * (size_t)std::max<long long>(n, 1)));
+    CUDA_TRY(cudaMallocHost((void**)&A.pinned_grad, sizeof(double) * std::max<size_t>(nd, 1)));
     A.n = n;
     A.K = K;
     return FDTD_OK;
@@ -1668,9 +1691,12 @@ int adj_forward_step(fdtd_handle* h, float* sample, float* snap) {
 
 }  // namespace
 
-extern "C" int fdtd_adjoint_forward(fdtd_handle* h, int64_t n, int32_t checkpoint_every, int32_t pi, int32_t pj, int32_t pk,
-                                    double* J) {
-    if (!h || !J) return fail(FDTD_ERR_INVALID, "NULL argument");
+namespace {
+
+// The forward of an adjoint run, enqueued on the handle's stream without waiting: validation,
+// buffers, checkpoints, the steps with their FoM samples and design snapshots, the samples' copy
+// to pinned host memory. adj_forward_finish waits for it.
+int adj_check(const fdtd_handle* h, int64_t n, int32_t checkpoint_every, int32_t pi, int32_t pj, int32_t pk) {
     if (!h->has_design) return fail(FDTD_ERR_STATE, "no design region (fdtd_set_design_region)");
     if (n < 1 || checkpoint_every < 0) return fail(FDTD_ERR_INVALID, "steps >= 1 and checkpoint interval >= 0 required");
     const DeviceGrid& g = h->g;
@@ -1678,7 +1704,14 @@ extern "C" int fdtd_adjoint_forward(fdtd_handle* h, int64_t n, int32_t checkpoin
         return fail(FDTD_ERR_INVALID, "FoM probe must be an updated Ez edge");
     if (in_slab_host(pi, g.nx, g.pxn, g.pxp) || in_slab_host(pj, g.ny, g.pyn, g.pyp) || in_slab_host(pk, g.nz, g.pzn, g.pzp))
         return fail(FDTD_ERR_INVALID, "FoM probe inside the CPML");
-    int rc = ensure_prepared(h);
+    return FDTD_OK;
+}
+
+int adj_forward_enqueue(fdtd_handle* h, int64_t n, int32_t checkpoint_every, int32_t pi, int32_t pj, int32_t pk) {
+    int rc = adj_check(h, n, checkpoint_every, pi, pj, pk);
+    if (rc) return rc;
+    const DeviceGrid& g = h->g;
+    rc = ensure_prepared(h);
     if (rc) return rc;
     const int K = checkpoint_every;
     rc = adj_prepare(h, n, K);
@@ -1696,18 +1729,26 @@ extern "C" int fdtd_adjoint_forward(fdtd_handle* h, int64_t n, int32_t checkpoin
         if ((rc = adj_forward_step(h, A.samples + s, K == 0 ? adj_slot(h, s + 1) : nullptr))) return rc;
     }
     if ((rc = state_copy(h, adj_ckpt(h, A.ckpt_slots - 1), true))) return rc;  // final state
-    A.host_samples.resize((size_t)n);
-    CUDA_TRY(cudaMemcpyAsync(A.host_samples.data(), A.samples, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaMemcpyAsync(A.pinned_samples, A.samples, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost, h->stream));
+    return FDTD_OK;
+}
+
+int adj_forward_finish(fdtd_handle* h, double* J) {
+    auto& A = h->adj;
     CUDA_TRY(cudaStreamSynchronize(h->stream));
+    A.host_samples.assign(A.pinned_samples, A.pinned_samples + A.n);
     double sum = 0.0;
-    for (float v : A.host_samples) sum += (double)g.dt * (double)v * (double)v;
+    for (float v : A.host_samples) sum += (double)h->g.dt * (double)v * (double)v;
     *J = sum;
     A.ready = true;
     return FDTD_OK;
 }
 
-extern "C" int fdtd_adjoint_backward(fdtd_handle* h, double* grad) {
-    if (!h || !grad) return fail(FDTD_ERR_INVALID, "NULL argument");
+// The reverse sweep, enqueued without waiting (the reversal's own stream and events live in the
+// handle): cleared adjoint state, the reverse steps (with segment recomputes for K > 0), the
+// gradient into pinned host memory, the forward's final state restored. adj_backward_finish
+// waits for it.
+int adj_backward_enqueue(fdtd_handle* h) {
     auto& A = h->adj;
     if (!A.ready) return fail(FDTD_ERR_STATE, "no fdtd_adjoint_forward since the last change");
     const size_t V = (size_t)vol(h) * sizeof(float);
@@ -1728,39 +1769,29 @@ extern "C" int fdtd_adjoint_backward(fdtd_handle* h, double* grad) {
     CUDA_TRY(cudaMemsetAsync(A.acc, 0, sizeof(double) * 3 * (size_t)ne, h->stream));
     const StepParams p = make_params(h);
     const float two_dt = 2.0f * h->g.dt;
-    auto reverse = [&](long long m, const float* e_old, const float* e_new) -> int {
-        const AdjStep st{A.probe, two_dt * A.host_samples[(size_t)m], A.acc, e_old, e_new};
-        CUDA_TRY(launch_adj_step(p, A.st, A.psa, st, h->stream));
-        return FDTD_OK;
-    };
     int rc;
     if (A.K == 0) {
-        for (long long m = A.n - 1; m >= 0; --m)
-            if ((rc = reverse(m, adj_slot(h, m), adj_slot(h, m + 1)))) return rc;
+        for (long long m = A.n - 1; m >= 0; --m) {
+            const AdjStep st{A.probe, two_dt * A.host_samples[(size_t)m], A.acc, adj_slot(h, m), adj_slot(h, m + 1)};
+            CUDA_TRY(launch_adj_step(p, A.st, A.psa, st, h->stream));
+        }
     } else {
         // Segments are recomputed on the handle's stream (forward fields) and reversed on a second
         // stream (adjoint state), one segment apart: the recompute of segment sg - 1 runs while
         // segment sg is reversed. Snapshot buffers alternate by segment parity; events order a
         // reversal after its recompute and a recompute after the reversal that last read its
         // buffer.
+        if (!A.rev) {
+            CUDA_TRY(cudaStreamCreateWithFlags(&A.rev, cudaStreamNonBlocking));
+            for (cudaEvent_t& e : A.ev) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        }
         const long long nseg = (A.n + A.K - 1) / A.K;
         const long long half = (long long)A.K + 1;
         auto slot = [&](long long sg, long long t) { return adj_slot(h, (sg & 1) * half + t); };
-        struct Sync {
-            cudaStream_t rev = nullptr;
-            cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // rec[2], rev[2], start
-            ~Sync() {
-                for (cudaEvent_t e : ev)
-                    if (e) cudaEventDestroy(e);
-                if (rev) cudaStreamDestroy(rev);
-            }
-        } S;
-        CUDA_TRY(cudaStreamCreateWithFlags(&S.rev, cudaStreamNonBlocking));
-        for (cudaEvent_t& e : S.ev) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-        cudaEvent_t* ev_rec = S.ev;
-        cudaEvent_t* ev_rev = S.ev + 2;
-        CUDA_TRY(cudaEventRecord(S.ev[4], h->stream));  // the adjoint state is cleared
-        CUDA_TRY(cudaStreamWaitEvent(S.rev, S.ev[4], 0));
+        cudaEvent_t* ev_rec = A.ev;
+        cudaEvent_t* ev_rev = A.ev + 2;
+        CUDA_TRY(cudaEventRecord(A.ev[4], h->stream));  // the adjoint state is cleared
+        CUDA_TRY(cudaStreamWaitEvent(A.rev, A.ev[4], 0));
         auto recompute = [&](long long sg) -> int {
             int r = state_copy(h, adj_ckpt(h, sg), false);
             if (r) return r;
@@ -1776,32 +1807,78 @@ extern "C" int fdtd_adjoint_backward(fdtd_handle* h, double* grad) {
         };
         if ((rc = recompute(nseg - 1))) return rc;
         for (long long sg = nseg - 1; sg >= 0; --sg) {
-            CUDA_TRY(cudaStreamWaitEvent(S.rev, ev_rec[sg & 1], 0));
+            CUDA_TRY(cudaStreamWaitEvent(A.rev, ev_rec[sg & 1], 0));
             const long long len = std::min<long long>(A.K, A.n - sg * A.K);
             for (long long t = len - 1; t >= 0; --t) {
                 const AdjStep st{A.probe, two_dt * A.host_samples[(size_t)(sg * A.K + t)], A.acc, slot(sg, t), slot(sg, t + 1)};
-                CUDA_TRY(launch_adj_step(p, A.st, A.psa, st, S.rev));
+                CUDA_TRY(launch_adj_step(p, A.st, A.psa, st, A.rev));
             }
-            CUDA_TRY(cudaEventRecord(ev_rev[sg & 1], S.rev));
+            CUDA_TRY(cudaEventRecord(ev_rev[sg & 1], A.rev));
             if (sg > 0) {
                 // segment sg - 1 reuses the buffers segment sg + 1 was reversed from
                 if (sg + 1 < nseg) CUDA_TRY(cudaStreamWaitEvent(h->stream, ev_rev[(sg + 1) & 1], 0));
                 if ((rc = recompute(sg - 1))) return rc;
             }
         }
-        CUDA_TRY(cudaEventRecord(S.ev[4], S.rev));
-        CUDA_TRY(cudaStreamWaitEvent(h->stream, S.ev[4], 0));
-        CUDA_TRY(cudaStreamSynchronize(S.rev));
+        CUDA_TRY(cudaEventRecord(A.ev[4], A.rev));
+        CUDA_TRY(cudaStreamWaitEvent(h->stream, A.ev[4], 0));
     }
     CUDA_TRY(launch_grad_finalize(A.acc, h->dbox, A.grad, h->stream));
     const size_t nd = (size_t)(h->dbox[3] - h->dbox[0]) * (h->dbox[4] - h->dbox[1]) * (h->dbox[5] - h->dbox[2]);
-    CUDA_TRY(cudaMemcpyAsync(grad, A.grad, sizeof(double) * nd, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaMemcpyAsync(A.pinned_grad, A.grad, sizeof(double) * nd, cudaMemcpyDeviceToHost, h->stream));
     // leave the handle where the forward left it
     if (A.K > 0) {
         if ((rc = state_copy(h, adj_ckpt(h, A.ckpt_slots - 1), false))) return rc;
         h->step = A.start + A.n;
     }
+    return FDTD_OK;
+}
+
+int adj_backward_finish(fdtd_handle* h, double* grad) {
     CUDA_TRY(cudaStreamSynchronize(h->stream));
+    const size_t nd = (size_t)(h->dbox[3] - h->dbox[0]) * (h->dbox[4] - h->dbox[1]) * (h->dbox[5] - h->dbox[2]);
+    std::memcpy(grad, h->adj.pinned_grad, sizeof(double) * nd);
+    return FDTD_OK;
+}
+
+}  // namespace
+
+extern "C" int fdtd_adjoint_forward(fdtd_handle* h, int64_t n, int32_t checkpoint_every, int32_t pi, int32_t pj, int32_t pk,
+                                    double* J) {
+    if (!h || !J) return fail(FDTD_ERR_INVALID, "NULL argument");
+    int rc = adj_forward_enqueue(h, n, checkpoint_every, pi, pj, pk);
+    return rc ? rc : adj_forward_finish(h, J);
+}
+
+extern "C" int fdtd_adjoint_backward(fdtd_handle* h, double* grad) {
+    if (!h || !grad) return fail(FDTD_ERR_INVALID, "NULL argument");
+    int rc = adj_backward_enqueue(h);
+    return rc ? rc : adj_backward_finish(h, grad);
+}
+
+// Forward and backward of many handles: every handle's work is enqueued before any is waited for,
+// so handles on different streams run concurrently; the results equal per-handle calls.
+extern "C" int fdtd_batch_adjoint(fdtd_handle* const* handles, int32_t n, int64_t steps, int32_t checkpoint_every,
+                                  const int32_t* probes, double* J, double* const* grads) {
+    if (!handles || !probes || !J || !grads || n < 1) return fail(FDTD_ERR_INVALID, "NULL argument or no handles");
+    for (int q = 0; q < n; ++q) {
+        if (!handles[q] || !grads[q]) return fail(FDTD_ERR_INVALID, "NULL handle or gradient");
+        for (int r = 0; r < q; ++r)
+            if (handles[r] == handles[q]) return fail(FDTD_ERR_INVALID, "a handle appears twice");
+    }
+    int rc;
+    for (int q = 0; q < n; ++q)  // nothing is enqueued unless every handle's arguments hold
+        if ((rc = adj_check(handles[q], steps, checkpoint_every, probes[3 * q], probes[3 * q + 1], probes[3 * q + 2])))
+            return rc;
+    for (int q = 0; q < n; ++q)
+        if ((rc = adj_forward_enqueue(handles[q], steps, checkpoint_every, probes[3 * q], probes[3 * q + 1], probes[3 * q + 2])))
+            return rc;
+    for (int q = 0; q < n; ++q)
+        if ((rc = adj_forward_finish(handles[q], J + q))) return rc;
+    for (int q = 0; q < n; ++q)
+        if ((rc = adj_backward_enqueue(handles[q]))) return rc;
+    for (int q = 0; q < n; ++q)
+        if ((rc = adj_backward_finish(handles[q], grads[q]))) return rc;
     return FDTD_OK;
 }
 

@@ -87,6 +87,8 @@ SIGNATURES = {
     "fdtd_set_design_region": (ctypes.c_int, [_vp, _pi32, ctypes.POINTER(Material), _pf]),
     "fdtd_adjoint_forward": (ctypes.c_int, [_vp, _i64, _i32, _i32, _i32, _i32, ctypes.POINTER(ctypes.c_double)]),
     "fdtd_adjoint_backward": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
+    "fdtd_batch_adjoint": (ctypes.c_int, [ctypes.POINTER(_vp), _i32, _i64, _i32, _pi32, ctypes.POINTER(ctypes.c_double),
+                                          ctypes.POINTER(ctypes.POINTER(ctypes.c_double))]),
     "fdtd_add_plate": (ctypes.c_int, [_vp, _i32, _pi32, ctypes.c_float, ctypes.c_float]),
     "fdtd_add_sector": (ctypes.c_int, [_vp, _pi32, _i32, ctypes.c_float, _i32, _i32, ctypes.c_float, ctypes.c_float]),
     "fdtd_add_port": (ctypes.c_int, [_vp, _i32, _pi32, _i32, _pi32, _pi32]),
@@ -499,6 +501,24 @@ class Batch:
 
     def synchronize(self) -> None:
         _check(_lib.fdtd_batch_synchronize(self._b))
+
+
+def batch_adjoint(sims: Sequence[Simulation], steps: int, probes: Sequence[Sequence[int]], checkpoint_every: int = 64):
+    """adjoint_forward then adjoint_backward of every simulation (each with its design region),
+    all enqueued before any is waited for (fdtd_batch_adjoint). Returns (J list, gradient list);
+    they equal the per-simulation calls bit for bit. Give the simulations separate streams
+    (set_stream) to run them concurrently."""
+    sims = list(sims)
+    if len(probes) != len(sims):
+        raise ValueError("one probe per simulation")
+    n = len(sims)
+    handles = (_vp * n)(*[s.handle for s in sims])
+    pr = (_i32 * (3 * n))(*[int(v) for p in probes for v in p])
+    J = (ctypes.c_double * n)()
+    grads = [np.zeros(getattr(s, "_design_shape", (0,)), dtype=np.float64) for s in sims]
+    gp = (ctypes.POINTER(ctypes.c_double) * n)(*[g.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for g in grads])
+    _check(_lib.fdtd_batch_adjoint(handles, n, steps, checkpoint_every, pr, J, gp))
+    return list(J), grads
 
 
 def run_scenario(sc: "S.Scenario", steps: Optional[int] = None, schedule: int = SCHEDULE_AUTO,

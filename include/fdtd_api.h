@@ -291,6 +291,14 @@ int fdtd_adjoint_forward(fdtd_handle* h, int64_t n, int32_t checkpoint_every, in
  * the host array `grad` (shaped like eps_r). The handle ends in the state the forward left. */
 int fdtd_adjoint_backward(fdtd_handle* h, double* grad);
 
+/* fdtd_adjoint_forward and fdtd_adjoint_backward of n distinct handles (each with its own design
+ * region), every handle's work enqueued on its own stream before any is waited for, so that
+ * handles run concurrently. probes holds n (i, j, k) triples, J n sums, grads n host arrays shaped
+ * like each handle's eps_r. J and the gradients equal those of the per-handle calls bit for bit;
+ * each handle ends in the state its forward left. */
+int fdtd_batch_adjoint(fdtd_handle* const* handles, int32_t n, int64_t steps, int32_t checkpoint_every,
+                       const int32_t* probes, double* J, double* const* grads);
+
 /* ---- Batched launch (no reference counterpart: the reference runs one domain per process). A
  * batch advances many independent handles of any sizes together, its launches captured in CUDA
  * graphs, in one of three forms. Chains (cluster -1, the default): each instance runs its own

@@ -178,3 +178,48 @@ def test_full_size_workload_against_fp64_reference(gpu_lib):
     for v, fd in zip(ref["voxels"], ref["fd"]):
         v = tuple(int(x) for x in v)
         assert abs(g[v] - fd) <= GRAD_TOL * abs(fd), (v, g[v], fd)
+
+
+@pytest.mark.parametrize("K", [0, 16])
+def test_batch_adjoint_equals_per_instance(gpu_lib, K):
+    """fdtd_batch_adjoint over three designs (different eps_r, probes and design boxes; each
+    simulation on its own stream) gives the J and gradients of per-instance forward + backward,
+    bit for bit, and leaves every simulation at the forward's final step."""
+    import torch
+    from fdtd_gb300 import solver
+    cases = []
+    for seed, shift in ((1, 0), (2, 1), (5, -1)):
+        sc, box, eps, probe = design_case(seed, steps=120)
+        box = (box[0] + shift, box[1], box[2], box[3] + shift, box[4], box[5])
+        probe = (probe[0], probe[1] + shift, probe[2])
+        cases.append((sc, box, eps, probe))
+    want = [gpu_grad(sc, box, eps, probe, K) for sc, box, eps, probe in cases]
+    streams = [torch.cuda.Stream() for _ in cases]
+    sims = []
+    try:
+        for (sc, box, eps, probe), st in zip(cases, streams):
+            sim = solver.Simulation.from_scenario(sc, probe_capacity=sc.steps)
+            sims.append(sim)
+            sim.set_stream(st.cuda_stream)
+            sim.set_design_region(box, eps)
+        J, grads = solver.batch_adjoint(sims, 120, [c[3] for c in cases], K)
+        for sim in sims:
+            assert sim.current_step == 120
+    finally:
+        for sim in sims:
+            sim.close()
+    for (Jw, gw), Jb, gb in zip(want, J, grads):
+        assert Jb == Jw
+        assert np.array_equal(gb, gw)
+
+
+def test_batch_adjoint_validation(gpu_lib):
+    from fdtd_gb300 import solver
+    sc, box, eps, probe = design_case(steps=20)
+    with solver.Simulation.from_scenario(sc, probe_capacity=20) as a, \
+            solver.Simulation.from_scenario(sc, probe_capacity=20) as b:
+        a.set_design_region(box, eps)
+        with pytest.raises(solver.FDTDError):
+            solver.batch_adjoint([a, b], 20, [probe, probe])  # b has no design region
+        with pytest.raises(solver.FDTDError):
+            solver.batch_adjoint([a, a], 20, [probe, probe])  # a handle twice
