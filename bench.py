@@ -527,6 +527,47 @@ def bench_batched(steps=2000):
             "speedup": round(bat / seq, 2)}
 
 
+def bench_batched_adjoint(n_instances=64, steps=1000, K=64):
+    """Forward + adjoint of independent design problems (cubes with per-instance sizes U{44..96},
+    8-cell CPML, a centred 16x16x8 design region, eps_r ~ U[1,12], one source and one Ez probe
+    each; checkpoints every K steps): the instances one after another through
+    fdtd_adjoint_forward / fdtd_adjoint_backward, then all together through fdtd_batch_adjoint,
+    each simulation on its own stream. Handle creation, setup and the adjoint buffers' allocation
+    (one untimed batched run) are outside both timings."""
+    import torch
+    from fdtd_gb300 import scenario as S, solver
+    rng = np.random.default_rng(21)
+    probs = [S.design_problem(int(rng.integers(44, 97)), steps, (16, 16, 8), pml=8, seed=q) for q in range(n_instances)]
+    streams = [torch.cuda.Stream() for _ in probs]
+    sims = []
+    for d, st in zip(probs, streams):
+        sim = solver.Simulation.from_scenario(d.scenario, probe_capacity=1)
+        sim.set_stream(st.cuda_stream)
+        sim.set_design_region(d.box, d.eps)
+        sim.prepare()
+        sims.append(sim)
+    try:
+        # warm-up: every handle allocates its adjoint buffers once (later runs of the same length reuse them)
+        solver.batch_adjoint(sims, steps, [d.probe for d in probs], K)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for sim, d in zip(sims, probs):
+            sim.adjoint_forward(steps, d.probe, K)
+            sim.adjoint_backward()
+        t_seq = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        solver.batch_adjoint(sims, steps, [d.probe for d in probs], K)
+        t_bat = time.perf_counter() - t0
+    finally:
+        for sim in sims:
+            sim.close()
+    cells = sum(d.scenario.cells for d in probs)
+    return {"workload": f"{n_instances} design instances, cube sizes U{{44..96}}, 8-cell CPML, 16x16x8 design region "
+                        "eps_r~U[1,12], 1 source + 1 Ez probe each, forward + adjoint",
+            "instances": n_instances, "cells": cells, "steps": steps, "checkpoint_every": K,
+            "sequential_s": round(t_seq, 3), "batched_s": round(t_bat, 3), "speedup": round(t_seq / t_bat, 2)}
+
+
 def bench_reference(args, rank, world):
     """The reference's own kernels (calc_e + calc_h from fdtdrav.h, built into oracle/_ref) on the
     same workload, single slab on this GPU."""
@@ -586,6 +627,7 @@ def main():
             out["adjoint"] = bench_adjoint()
         if not args.no_batched and world == 1:
             out["batched"] = bench_batched()
+            out["batched_adjoint"] = bench_batched_adjoint()
         if not args.no_hbm and world == 1 and args.config != "hbm":
             out["hbm"] = bench_hbm()
         print(json.dumps(out))

@@ -189,6 +189,7 @@ struct fdtd_handle {
         double* pinned_grad = nullptr;
         cudaStream_t rev = nullptr;    // the reverse sweep's stream (K > 0) and its events
         cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // recompute[2], reverse[2], start / end
+        long long key[8] = {};         // steps, interval and design box the buffers were sized for
     } adj;
 
     // work list of fdtd_step_static_scratch (interior items first) in pinned host memory, planned
@@ -1631,6 +1632,13 @@ long long edge_box_volume(const int* d) { return (long long)(d[3] - d[0] + 1) * 
 // Buffers of an adjoint run of n steps with checkpoint interval K.
 int adj_prepare(fdtd_handle* h, long long n, int K) {
     auto& A = h->adj;
+    // a run of the same length, interval and design box reuses the buffers: freeing device or
+    // pinned memory synchronises the whole device, which would serialise batched runs
+    const long long key[8] = {n, K, h->dbox[0], h->dbox[1], h->dbox[2], h->dbox[3], h->dbox[4], h->dbox[5]};
+    if (!A.bufs.empty() && A.pinned_samples && std::equal(key, key + 8, A.key)) {
+        A.ready = false;
+        return FDTD_OK;
+    }
     for (void* p : A.bufs) h->release(p);
     A.bufs.clear();
     if (A.pinned_samples) cudaFreeHost(A.pinned_samples);
@@ -1673,6 +1681,7 @@ int adj_prepare(fdtd_handle* h, long long n, int K) {
     CUDA_TRY(cudaMallocHost((void**)&A.pinned_grad, sizeof(double) * std::max<size_t>(nd, 1)));
     A.n = n;
     A.K = K;
+    std::copy(key, key + 8, A.key);
     return FDTD_OK;
 }
 

@@ -223,3 +223,25 @@ def test_batch_adjoint_validation(gpu_lib):
             solver.batch_adjoint([a, b], 20, [probe, probe])  # b has no design region
         with pytest.raises(solver.FDTDError):
             solver.batch_adjoint([a, a], 20, [probe, probe])  # a handle twice
+
+
+@pytest.mark.parametrize("K", [0, 16])
+def test_repeated_adjoint_reuses_buffers(gpu_lib, K):
+    """A second forward + backward of the same length on one handle (its buffers kept from the
+    first) equals a fresh handle's forward + backward started from the same state and step."""
+    from fdtd_gb300 import solver
+    sc, box, eps, probe = design_case(7, steps=80)
+    with solver.Simulation.from_scenario(sc, probe_capacity=160) as a, \
+            solver.Simulation.from_scenario(sc, probe_capacity=160) as b:
+        for s in (a, b):
+            s.set_design_region(box, eps)
+        a.adjoint_forward(80, probe, K)
+        a.adjoint_backward()
+        J1 = a.adjoint_forward(80, probe, K)
+        g1 = a.adjoint_backward()
+        b.step(80)
+        J2 = b.adjoint_forward(80, probe, K)
+        g2 = b.adjoint_backward()
+        assert a.current_step == b.current_step == 160
+        assert J1 == J2 and np.array_equal(g1, g2)
+        assert bitwise_equal(a.fields(), b.fields())
