@@ -325,6 +325,32 @@ cudaError_t launch_after_step(const float* ex, const float* ey, const float* ez,
     return cudaGetLastError();
 }
 
+// The six field components over node box b, to (save) or from a packed buffer of 6 x box volume
+// floats (component-major, x fastest).
+__global__ void k_box_state(FieldPtrs f, DeviceGrid g, NodeBox b, float* buf, bool save) {
+    const int bx = b.x1 - b.x0, by = b.y1 - b.y0;
+    const long long nb = (long long)bx * by * (b.z1 - b.z0);
+    const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (q >= nb) return;
+    const int i = b.x0 + (int)(q % bx), j = b.y0 + (int)((q / bx) % by), k = b.z0 + (int)(q / ((long long)bx * by));
+    const long long n = (long long)k * g.plane + (long long)j * g.pitch + i;
+    float* c[6] = {f.ex, f.ey, f.ez, f.hx, f.hy, f.hz};
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+        if (save) buf[r * nb + q] = c[r][n];
+        else c[r][n] = buf[r * nb + q];
+    }
+}
+
+cudaError_t launch_box_state(const FieldPtrs& f, const DeviceGrid& g, const NodeBox& b, float* buf, bool save,
+                             cudaStream_t s) {
+    if (b.x0 < 0 || b.y0 < 0 || b.z0 < 0 || b.x1 > g.nx || b.y1 > g.ny || b.z1 > g.nz) return cudaErrorInvalidValue;
+    const long long nb = (long long)(b.x1 - b.x0) * (b.y1 - b.y0) * (b.z1 - b.z0);
+    if (nb <= 0) return cudaSuccess;
+    k_box_state<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(f, g, b, buf, save);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_grad_finalize(const double* acc, const int dbox[6], double* grad, cudaStream_t s) {
     const int dx = dbox[3] - dbox[0], dy = dbox[4] - dbox[1], dz = dbox[5] - dbox[2];
     const long long n = (long long)dx * dy * dz;

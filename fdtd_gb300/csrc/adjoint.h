@@ -31,6 +31,10 @@ cudaError_t launch_adj_step(const StepParams& p, const AdjState& a, const PsiSet
 // components over the design edge box into snap (3 x box volume).
 cudaError_t launch_after_step(const float* ex, const float* ey, const float* ez, const DeviceGrid& g, long long probe,
                               float* sample, const int dbox[6], float* snap, cudaStream_t s);
+// The six field components over node box b (inside the grid) saved to / restored from buf
+// (6 x box volume floats).
+cudaError_t launch_box_state(const FieldPtrs& f, const DeviceGrid& g, const NodeBox& b, float* buf, bool save,
+                             cudaStream_t s);
 // grad (design cells, FP64) from the edge accumulators.
 cudaError_t launch_grad_finalize(const double* acc, const int dbox[6], double* grad, cudaStream_t s);
 

@@ -184,6 +184,11 @@ struct fdtd_handle {
         long long ckpt_slots = 0;
         double* acc = nullptr;         // per-edge gradient accumulators
         double* grad = nullptr;        // per-cell gradient
+        int* no_probe_k = nullptr;     // per-plane probe offsets, all zero: the recompute samples nothing
+        int S = 0;                     // box checkpoints every S steps inside a segment (0: none)
+        long long sub_per_seg = 0;     // box checkpoints per segment
+        NodeBox sub_box{};             // the design edge box grown by S nodes
+        float* sub = nullptr;          // the fields over sub_box at those steps
         std::vector<void*> bufs;       // everything above, for release
         float* pinned_samples = nullptr;  // host copies (pinned: asynchronous copies)
         double* pinned_grad = nullptr;
@@ -1629,6 +1634,23 @@ int adj_alloc(fdtd_handle* h, void** p, size_t n) {
 
 long long edge_box_volume(const int* d) { return (long long)(d[3] - d[0] + 1) * (d[4] - d[1] + 1) * (d[5] - d[2] + 1); }
 
+// Interval S of the box checkpoints inside a segment of K steps (0: none). The segment recompute
+// needs only the design region's E, so it sweeps the cone of nodes that E depends on (see
+// adj_recompute_step); a copy of the fields over the design edge box grown by S nodes, saved by
+// the forward every S steps, restarts that cone with a reach below S. S is the largest value up
+// to kAdjSubMax whose box holds interior nodes only (no CPML memory, no boundary plane), used
+// only when it splits a segment.
+constexpr int kAdjSubMax = 16;
+int adj_sub_interval(const fdtd_handle* h, int K) {
+    const DeviceGrid& g = h->g;
+    const int* d = h->dbox;
+    auto lo = [](int pn) { return std::max(pn, 1); };
+    auto hi = [](int nn, int pp) { return std::min(nn - 1 - pp, nn - 2); };
+    const int gap = std::min({kAdjSubMax, d[0] - lo(g.pxn), hi(g.nx, g.pxp) - d[3], d[1] - lo(g.pyn),
+                              hi(g.ny, g.pyp) - d[4], d[2] - lo(g.pzn), hi(g.nz, g.pzp) - d[5]});
+    return (K > 0 && gap >= 1 && gap < K) ? gap : 0;
+}
+
 // Buffers of an adjoint run of n steps with checkpoint interval K.
 int adj_prepare(fdtd_handle* h, long long n, int K) {
     auto& A = h->adj;
@@ -1675,8 +1697,25 @@ int adj_prepare(fdtd_handle* h, long long n, int K) {
         (rc = adj_alloc(h, (void**)&A.hist, sizeof(float) * 3 * (size_t)ne * (size_t)A.hist_slots)) ||
         (rc = adj_alloc(h, (void**)&A.ckpt, (size_t)fdtd_state_bytes(h) * (size_t)A.ckpt_slots)) ||
         (rc = adj_alloc(h, (void**)&A.acc, sizeof(double) * 3 * (size_t)ne)) ||
-        (rc = adj_alloc(h, (void**)&A.grad, sizeof(double) * nd)))
+        (rc = adj_alloc(h, (void**)&A.grad, sizeof(double) * nd)) ||
+        (rc = adj_alloc(h, (void**)&A.no_probe_k, sizeof(int) * (size_t)(h->g.nz + 1))))
         return rc;
+    CUDA_TRY(cudaMemsetAsync(A.no_probe_k, 0, sizeof(int) * (size_t)(h->g.nz + 1), h->stream));
+    A.S = adj_sub_interval(h, K);
+    if (A.S > 0) {
+        const int S = A.S;
+        const int* d = h->dbox;
+        A.sub_box = NodeBox{d[0] - S, d[1] - S, d[2] - S, d[3] + 1 + S, d[4] + 1 + S, d[5] + 1 + S};
+        A.sub_per_seg = (K - 1) / S;
+        const size_t box = (size_t)(A.sub_box.x1 - A.sub_box.x0) * (A.sub_box.y1 - A.sub_box.y0) *
+                           (A.sub_box.z1 - A.sub_box.z0);
+        const size_t slots = (size_t)((n + K - 1) / K) * (size_t)A.sub_per_seg;
+        if (adj_alloc(h, (void**)&A.sub, sizeof(float) * 6 * box * slots) != FDTD_OK) {
+            cudaGetLastError();  // no room: the recompute sweeps the whole cone from the checkpoint
+            A.S = 0;
+            A.sub_per_seg = 0;
+        }
+    }
     CUDA_TRY(cudaMallocHost((void**)&A.pinned_samples, sizeof(float) * (size_t)std::max<long long>(n, 1)));
     CUDA_TRY(cudaMallocHost((void**)&A.pinned_grad, sizeof(double) * std::max<size_t>(nd, 1)));
     A.n = n;
@@ -1685,6 +1724,16 @@ int adj_prepare(fdtd_handle* h, long long n, int K) {
     return FDTD_OK;
 }
 
+// Box checkpoint q (1 .. sub_per_seg: at step q * S of the segment) of segment sg.
+float* adj_sub(fdtd_handle* h, long long sg, long long q) {
+    const NodeBox& b = h->adj.sub_box;
+    const size_t box = (size_t)(b.x1 - b.x0) * (b.y1 - b.y0) * (b.z1 - b.z0);
+    return h->adj.sub + (size_t)(sg * h->adj.sub_per_seg + q - 1) * 6 * box;
+}
+FieldPtrs cur_fields(fdtd_handle* h) {
+    const int c = h->cur;
+    return FieldPtrs{h->field[c][0], h->field[c][1], h->field[c][2], h->field[c][3], h->field[c][4], h->field[c][5]};
+}
 float* adj_slot(fdtd_handle* h, long long s) { return h->adj.hist + (size_t)s * 3 * (size_t)edge_box_volume(h->dbox); }
 char* adj_ckpt(fdtd_handle* h, long long s) { return h->adj.ckpt + (size_t)s * (size_t)fdtd_state_bytes(h); }
 
@@ -1694,6 +1743,29 @@ int adj_forward_step(fdtd_handle* h, float* sample, float* snap) {
     if (rc) return rc;
     const int c = h->cur;
     CUDA_TRY(launch_after_step(h->field[c][0], h->field[c][1], h->field[c][2], h->g, h->adj.probe, sample, h->dbox, snap,
+                               h->stream));
+    return FDTD_OK;
+}
+
+// One step of a segment recompute (K > 0). The backward needs only the design region's E of each
+// recomputed step, and E at the design edge box D after the segment's step t depends only on the
+// segment's starting state within D grown by (segment length - t) nodes on every side: one step
+// of the Yee update reads a node's neighbours one node away along each axis (E the lower H
+// neighbours, H the upper E neighbours). So step t updates only that box (`reach` = length - t,
+// clipped to the grid): the nodes inside take the same bits as in a whole-grid step, and those
+// outside are stale but never read again within the segment. Probes sample nothing (pr has no
+// probe planes): the ring keeps the forward's samples.
+int adj_recompute_step(fdtd_handle* h, const StepParams& pr, long long reach, float* snap) {
+    const DeviceGrid& g = h->g;
+    const int* d = h->dbox;
+    const int e = (int)std::min<long long>(reach, 1LL << 20);
+    const NodeBox b{std::max(0, d[0] - e), std::max(0, d[1] - e), std::max(0, d[2] - e),
+                    std::min(g.nx, d[3] + 1 + e), std::min(g.ny, d[4] + 1 + e), std::min(g.nz, d[5] + 1 + e)};
+    const int c = h->cur;
+    const FieldPtrs f{h->field[c][0], h->field[c][1], h->field[c][2], h->field[c][3], h->field[c][4], h->field[c][5]};
+    CUDA_TRY(launch_two_pass_box(pr, f, h->psi[c], b, h->step, h->stream));
+    ++h->step;
+    CUDA_TRY(launch_after_step(h->field[c][0], h->field[c][1], h->field[c][2], g, h->adj.probe, nullptr, h->dbox, snap,
                                h->stream));
     return FDTD_OK;
 }
@@ -1734,7 +1806,11 @@ int adj_forward_enqueue(fdtd_handle* h, int64_t n, int32_t checkpoint_every, int
                                    h->stream));
     }
     for (long long s = 0; s < n; ++s) {
-        if (K > 0 && s % K == 0 && (rc = state_copy(h, adj_ckpt(h, s / K), true))) return rc;
+        if (K > 0 && s % K == 0) {
+            if ((rc = state_copy(h, adj_ckpt(h, s / K), true))) return rc;
+        } else if (A.S > 0 && (s % K) % A.S == 0) {
+            CUDA_TRY(launch_box_state(cur_fields(h), g, A.sub_box, adj_sub(h, s / K, (s % K) / A.S), true, h->stream));
+        }
         if ((rc = adj_forward_step(h, A.samples + s, K == 0 ? adj_slot(h, s + 1) : nullptr))) return rc;
     }
     if ((rc = state_copy(h, adj_ckpt(h, A.ckpt_slots - 1), true))) return rc;  // final state
@@ -1794,6 +1870,8 @@ int adj_backward_enqueue(fdtd_handle* h) {
             CUDA_TRY(cudaStreamCreateWithFlags(&A.rev, cudaStreamNonBlocking));
             for (cudaEvent_t& e : A.ev) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         }
+        StepParams pr = p;
+        pr.probe_k = A.no_probe_k;
         const long long nseg = (A.n + A.K - 1) / A.K;
         const long long half = (long long)A.K + 1;
         auto slot = [&](long long sg, long long t) { return adj_slot(h, (sg & 1) * half + t); };
@@ -1809,8 +1887,13 @@ int adj_backward_enqueue(fdtd_handle* h) {
             const int c = h->cur;
             CUDA_TRY(launch_after_step(h->field[c][0], h->field[c][1], h->field[c][2], h->g, A.probe, nullptr, h->dbox,
                                        slot(sg, 0), h->stream));
-            for (long long t = 0; t < len; ++t)
-                if ((r = adj_forward_step(h, nullptr, slot(sg, t + 1)))) return r;
+            for (long long t = 0; t < len; ++t) {
+                if (A.S > 0 && t > 0 && t % A.S == 0)
+                    CUDA_TRY(launch_box_state(cur_fields(h), h->g, A.sub_box, adj_sub(h, sg, t / A.S), false, h->stream));
+                // the cone ends at the next box checkpoint (or the segment's end)
+                const long long te = A.S > 0 ? std::min<long long>(len, (t / A.S + 1) * A.S) : len;
+                if ((r = adj_recompute_step(h, pr, te - 1 - t, slot(sg, t + 1)))) return r;
+            }
             CUDA_TRY(cudaEventRecord(ev_rec[sg & 1], h->stream));
             return FDTD_OK;
         };

@@ -22,6 +22,16 @@ struct PsiSet {
 cudaError_t launch_two_pass(const StepParams& p, const FieldPtrs& f, const PsiSet& ps, long long m,
                             cudaStream_t st);
 
+// A box of nodes [x0, x1) x [y0, y1) x [z0, z1).
+struct NodeBox {
+    int x0, y0, z0, x1, y1, z1;
+};
+
+// One two-pass step m over the nodes of box b only (inside the grid; the design region's E and
+// the plate nodes as in launch_two_pass). Nodes outside b keep their values.
+cudaError_t launch_two_pass_box(const StepParams& p, const FieldPtrs& f, const PsiSet& ps, const NodeBox& b, long long m,
+                                cudaStream_t st);
+
 // One two-pass step whose step index is *base + s (device counter), for graph replay; handles
 // without a design region or plates only.
 cudaError_t launch_two_pass_rel(const StepParams& p, const FieldPtrs& f, const PsiSet& ps, const long long* base, int s,

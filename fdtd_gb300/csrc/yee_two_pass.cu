@@ -195,6 +195,48 @@ cudaError_t launch_two_pass_rel(const StepParams& p, const FieldPtrs& f, const P
     return cudaGetLastError();
 }
 
+// Two-pass kernels over the nodes [b.x0, b.x1) x [b.y0, b.y1) x [b.z0, b.z1) only (the adjoint's
+// segment recompute, whose nodes outside a shrinking box around the design region are never read
+// again). Same per-node code, so the nodes inside give the same bits as a whole-grid step.
+template <typename Idx>
+__global__ void __launch_bounds__(256, FDTD_TWO_PASS_MIN_BLOCKS) k_update_e_box(const __grid_constant__ StepParams p,
+                                                                                 FieldPtrs f,
+                                                                                 const __grid_constant__ PsiSet ps,
+                                                                                 NodeBox b, long long m) {
+    const int i = b.x0 + blockIdx.x * 32 + threadIdx.x;
+    const int j = b.y0 + blockIdx.y * 8 + threadIdx.y;
+    if (i >= b.x1 || j >= b.y1) return;
+    e_node_global<false, false, false, Idx>(p, f, f, ps, ps, i, j, b.z0 + blockIdx.z, m);
+}
+template <typename Idx>
+__global__ void __launch_bounds__(256, FDTD_TWO_PASS_MIN_BLOCKS) k_update_h_box(const __grid_constant__ StepParams p,
+                                                                                 FieldPtrs f,
+                                                                                 const __grid_constant__ PsiSet ps,
+                                                                                 NodeBox b, long long m) {
+    const int i = b.x0 + blockIdx.x * 32 + threadIdx.x;
+    const int j = b.y0 + blockIdx.y * 8 + threadIdx.y;
+    if (i >= b.x1 || j >= b.y1) return;
+    h_node_global<false, Idx>(p, f, f, f, ps, ps, i, j, b.z0 + blockIdx.z, m);
+}
+
+cudaError_t launch_two_pass_box(const StepParams& p, const FieldPtrs& f, const PsiSet& ps, const NodeBox& b, long long m,
+                                cudaStream_t st) {
+    const DeviceGrid& g = p.g;
+    if (b.x0 < 0 || b.y0 < 0 || b.z0 < 0 || b.x1 > g.nx || b.y1 > g.ny || b.z1 > g.nz) return cudaErrorInvalidValue;
+    if (b.x1 <= b.x0 || b.y1 <= b.y0 || b.z1 <= b.z0) return cudaSuccess;
+    const dim3 block(32, 8, 1);
+    const dim3 grid((b.x1 - b.x0 + 31) / 32, (b.y1 - b.y0 + 7) / 8, b.z1 - b.z0);
+    const bool idx32 = g.plane * (long long)(g.nz + 1) < (1LL << 31);
+    if (idx32) k_update_e_box<uint32_t><<<grid, block, 0, st>>>(p, f, ps, b, m);
+    else k_update_e_box<long long><<<grid, block, 0, st>>>(p, f, ps, b, m);
+    cudaError_t e = launch_design_e(p, f, f, ps, ps, m, st);
+    if (e == cudaSuccess) e = launch_plate_e(p, f, f, ps, ps, m, st);
+    if (e != cudaSuccess) return e;
+    if (idx32) k_update_h_box<uint32_t><<<grid, block, 0, st>>>(p, f, ps, b, m);
+    else k_update_h_box<long long><<<grid, block, 0, st>>>(p, f, ps, b, m);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_two_pass(const StepParams& p, const FieldPtrs& f, const PsiSet& ps, long long m,
                             cudaStream_t st) {
     dim3 block(32, 8, 1);

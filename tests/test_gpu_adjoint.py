@@ -245,3 +245,47 @@ def test_repeated_adjoint_reuses_buffers(gpu_lib, K):
         assert a.current_step == b.current_step == 160
         assert J1 == J2 and np.array_equal(g1, g2)
         assert bitwise_equal(a.fields(), b.fields())
+
+
+def test_backward_keeps_probe_ring(gpu_lib):
+    """A probe ring shorter than the run: after forward + backward (K = 16, segments recomputed)
+    the ring holds the forward's last samples, as after plain steps; the recompute samples nothing."""
+    from fdtd_gb300 import solver
+    sc, box, eps, probe = design_case(4, steps=96)
+    with solver.Simulation.from_scenario(sc, probe_capacity=24) as a, \
+            solver.Simulation.from_scenario(sc, probe_capacity=24) as b:
+        for s in (a, b):
+            s.set_design_region(box, eps)
+        a.adjoint_forward(96, probe, 16)
+        a.adjoint_backward()
+        b.step(96)
+        b.synchronize()
+        assert bitwise_equal(a.read_probes(72, 24), b.read_probes(72, 24))
+        assert bitwise_equal(a.fields(), b.fields())
+
+
+def test_checkpointed_equals_resident_fused(gpu_lib):
+    """Under the fused schedule the forward ping-pongs between two field buffers, and the segment
+    recompute (two-pass, in place, over the shrinking box around the design region) starts from
+    checkpoints of either buffer: the gradient equals the resident history's bit for bit."""
+    from fdtd_gb300 import solver
+    steps = 50
+    sc = S.vacuum_cube(80, steps, pml=6, name="adjoint_fused")
+    sc.nx, sc.ny, sc.nz = 80, 56, 40
+    sc.sources = [S.LumpedSource((20, 28, 19, 20, 28, 20), 50.0, S.gaussian_derivative(steps, sc.dt, 30e9, 1e-3))]
+    sc.probes = [S.Probe(2, 52, 28, 19), S.Probe(3, 34, 40, 20)]
+    sc.materials.append(S.Material(eps_r=4.0, sigma_e=0.01))
+    sc.bricks.append(S.Brick((44, 10, 8, 60, 40, 30), 1))
+    box = (30, 22, 15, 38, 30, 23)
+    eps = np.random.default_rng(8).uniform(1, 12, size=(8, 8, 8)).astype(np.float32)
+    probe = (52, 28, 19)
+    out = []
+    for K in (0, 9, 20):  # K = 20: box checkpoints every 9 steps inside each segment
+        with solver.Simulation.from_scenario(sc, 2, probe_capacity=steps) as sim:
+            sim.set_design_region(box, eps)
+            J = sim.adjoint_forward(steps, probe, K)
+            g = sim.adjoint_backward()
+            out.append((J, g, sim.fields()))
+    for J, g, f in out[1:]:
+        assert J == out[0][0] and np.array_equal(g, out[0][1])
+        assert bitwise_equal(f, out[0][2])
