@@ -105,6 +105,11 @@ struct fdtd_handle {
     FusedMaps maps[2];
     CpmlMaps cmaps[2];  // the CPML sweep's maps per input buffer
     FusedFork fork{};  // second stream and events of the fused step (created with the fused buffers)
+    struct PlanCache {  // the last fused plan and what it was made for (chunk, schedule, design box)
+        bool valid = false;
+        int key[9] = {};
+        FusedPlan plan;
+    } plan_cache;
     int kc = 0;  // planes per CTA chunk of the fused sweep
     FusedWork work{};
     bool replan = false;  // the design region or the CPML-sweep choice changed since the fused work was planned
@@ -372,10 +377,27 @@ FusedWork work_of(const int4* d, const int counts[kWorkLists]) {
 
 // Work items of the fused schedule (planner.cpp), with CPML items under FDTD_SCHEDULE_FUSED_CPML.
 // The design region, if any, stays with the shell; planned again when it or the schedule changes.
+// The fused plan for the handle's current design box and schedule, from the cache when it holds
+// that plan (planning a 512^3 grid takes most of a millisecond on the host).
+void plan_current(fdtd_handle* h, FusedPlan& plan) {
+    const PlanGrid pg = plan_grid(h->g);
+    const int kc = h->kc > 0 ? h->kc : plan_chunk(pg);
+    const bool cpml = h->schedule == FDTD_SCHEDULE_FUSED_CPML;
+    int key[9] = {kc, cpml, h->has_design, 0, 0, 0, 0, 0, 0};
+    if (h->has_design) std::copy(h->dbox, h->dbox + 6, key + 3);
+    auto& C = h->plan_cache;
+    if (!(C.valid && std::equal(key, key + 9, C.key))) {
+        C.plan = FusedPlan{};
+        plan_fused(pg, kc, h->has_design ? h->dbox : nullptr, C.plan, cpml);
+        std::copy(key, key + 9, C.key);
+        C.valid = true;
+    }
+    plan = C.plan;
+}
+
 int plan_work(fdtd_handle* h) {
     FusedPlan plan;
-    plan_fused(plan_grid(h->g), h->kc, h->has_design ? h->dbox : nullptr, plan,
-               h->schedule == FDTD_SCHEDULE_FUSED_CPML);
+    plan_current(h, plan);
     int counts[kWorkLists];
     const std::vector<PlanItem> all = flatten(plan, counts);
     h->release((void*)h->work.interior);
@@ -392,13 +414,14 @@ int plan_work(fdtd_handle* h) {
 int ensure_fused(fdtd_handle* h) {
     if (h->have_second && h->replan) return plan_work(h);
     if (h->have_second) return FDTD_OK;
-    // no copy of the state: a fused step writes every node of its target buffer (the planner's
-    // items cover each node once; plate and design nodes by their own kernels); the row padding,
-    // which no kernel writes, gets buffer 0's initial value so that saved states agree
+    // no copy of the state and no fill: a fused step writes every node of its target buffer (the
+    // planner's items cover each node once; plate and design nodes by their own kernels); only
+    // the row padding, which no kernel writes, gets buffer 0's initial value so that saved
+    // states agree
     const long long V = vol(h);
     for (int c = 0; c < 6; ++c) {
         CUDA_TRY(h->alloc((void**)&h->field[1][c], (size_t)V * sizeof(float)));
-        CUDA_TRY(launch_fill(h->field[1][c], V, kTiny, h->stream));
+        CUDA_TRY(launch_fill_padding(h->field[1][c], h->g, kTiny, h->stream));
     }
     int rc = alloc_psi_set(h, 1);
     if (rc) return rc;
@@ -857,10 +880,9 @@ constexpr double kAutoDirectInterior = 0.8;
 
 // Share of the grid's nodes that the interior sweep's tiles hold (overlapping tiles counted once
 // per tile, a slight overestimate).
-double interior_share(const fdtd_handle* h) {
+double interior_share(fdtd_handle* h) {
     FusedPlan plan;
-    const PlanGrid pg = plan_grid(h->g);
-    plan_fused(pg, plan_chunk(pg), h->has_design ? h->dbox : nullptr, plan);
+    plan_current(h, plan);
     long long n = 0;
     for (const PlanItem& it : plan.interior) n += (long long)(it.w - it.z) * kTileX * kTileY;
     return (double)n / ((double)h->g.nx * h->g.ny * h->g.nz);

@@ -200,6 +200,23 @@ cudaError_t launch_fill(float* p, long long n, float v, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// The row padding of a field array (columns nx .. pitch-1 of every row) set to v.
+__global__ void k_fill_padding(float* p, DeviceGrid g, float v) {
+    const int w = g.pitch - g.nx;
+    const long long n = (long long)w * g.ny * g.nz;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
+        p[(q / w) * g.pitch + g.nx + q % w] = v;
+}
+
+cudaError_t launch_fill_padding(float* p, const DeviceGrid& g, float v, cudaStream_t st) {
+    const long long n = (long long)(g.pitch - g.nx) * g.ny * g.nz;
+    if (n <= 0) return cudaSuccess;
+    long long blocks = (n + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    k_fill_padding<<<(int)blocks, 256, 0, st>>>(p, g, v);
+    return cudaGetLastError();
+}
+
 // setBrick (fdtdrav.h:1524-1571) on the material index: cells [is,ie) x [js,je) x [ks,ke).
 __global__ void k_paint(uint8_t* mat, DeviceGrid g, int is, int js, int ks, int ie, int je, int ke, uint8_t v) {
     const int i = is + blockIdx.x * blockDim.x + threadIdx.x;

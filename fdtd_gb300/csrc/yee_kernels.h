@@ -123,6 +123,8 @@ cudaError_t launch_lumped_coefs(const DeviceGrid& g, const uint8_t* mat, const M
 cudaError_t launch_bg_curl(const DeviceGrid& g, const MatCoef* coef, int bg, const float* const* kappa_dev,
                            float* const* out_dev, cudaStream_t st);
 cudaError_t launch_fill(float* p, long long n, float v, cudaStream_t st);
+// Columns nx .. pitch-1 of every row of a field array set to v.
+cudaError_t launch_fill_padding(float* p, const DeviceGrid& g, float v, cudaStream_t st);
 // Node classes (StepParams::cls) from the material index and the lumped edges.
 // design_box: the design region's cells or NULL (its edge box gets class kDesignNode).
 // Set the node class of the listed nodes ({i, j, k, -}) to `value`.

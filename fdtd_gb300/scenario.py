@@ -72,13 +72,19 @@ class Material:
 
     def axes(self) -> np.ndarray:
         """float32 (3, 4): per axis x, y, z the values eps_r, sigma_e, mu_r, sigma_m."""
+        vals = (self.eps_r, self.sigma_e, self.mu_r, self.sigma_m)
+        if not any(isinstance(v, (list, tuple, np.ndarray)) for v in vals):  # isotropic: one row, thrice
+            return np.array([vals] * 3, dtype=np.float32)
         out = np.zeros((3, 4), dtype=np.float32)
-        for q, v in enumerate((self.eps_r, self.sigma_e, self.mu_r, self.sigma_m)):
+        for q, v in enumerate(vals):
             out[:, q] = np.broadcast_to(np.asarray(v, dtype=np.float32), (3,))
         return out
 
     @property
     def anisotropic(self) -> bool:
+        vals = (self.eps_r, self.sigma_e, self.mu_r, self.sigma_m)
+        if not any(isinstance(v, (list, tuple, np.ndarray)) for v in vals):
+            return False
         a = self.axes()
         return not (np.array_equal(a[0], a[1]) and np.array_equal(a[0], a[2]))
 
@@ -220,7 +226,8 @@ class Scenario:
     def material_table(self) -> np.ndarray:
         """float32 table (n_materials, 4): eps_r, sigma_e, mu_r, sigma_m (the x values of
         anisotropic materials)."""
-        return np.array([m.axes()[0] for m in self.materials], dtype=np.float32).reshape(-1, 4)
+        return np.array([(m.eps_r, m.sigma_e, m.mu_r, m.sigma_m) if not m.anisotropic else tuple(m.axes()[0])
+                         for m in self.materials], dtype=np.float32).reshape(-1, 4)
 
     def material_table_axes(self) -> np.ndarray:
         """float32 table (n_materials, 3, 4): per axis x, y, z the values eps_r, sigma_e, mu_r, sigma_m."""

@@ -194,17 +194,13 @@ class Simulation:
         axis x, y, z (fdtd_set_materials_axes)."""
         t = np.asarray(table, dtype=np.float32)
         if t.ndim == 3:
-            rows = []
-            for m in t:
-                r = MaterialAxes()
-                for q, name in enumerate(("eps_r", "sigma_e", "mu_r", "sigma_m")):
-                    getattr(r, name)[:] = [float(v) for v in m[:, q]]
-                rows.append(r)
-            arr = (MaterialAxes * len(rows))(*rows)
+            # MaterialAxes holds eps_r[3], sigma_e[3], mu_r[3], sigma_m[3]: the (n, 3, 4) table transposed
+            rows = np.ascontiguousarray(t.transpose(0, 2, 1))
+            arr = (MaterialAxes * len(rows)).from_buffer_copy(rows.tobytes())
             _check(_lib.fdtd_set_materials_axes(self._h, arr, len(rows)))
             return
-        t = t.reshape(-1, 4)
-        arr = (Material * len(t))(*[Material(*row) for row in t.tolist()])
+        t = np.ascontiguousarray(t.reshape(-1, 4))  # rows laid out as Material (four floats)
+        arr = (Material * len(t)).from_buffer_copy(t.tobytes())
         _check(_lib.fdtd_set_materials(self._h, arr, len(t)))
 
     def set_material_index(self, cells: np.ndarray) -> None:
