@@ -264,6 +264,14 @@ struct PsiIO {
 };
 
 
+// Old CPML memory of one node loaded ahead (the per-node kernels issue these loads with the field
+// loads, since the addresses depend only on the node's position): for E (H) the two arrays of the
+// x face, then the y face, then the z face, in e_update's (h_update's) order; entries of slabs the
+// node is not in are unused.
+struct PsiOld {
+    float v[6];
+};
+
 // The old CPML memory of one slot. kCoherent: through L2 (ld.global.cg) instead of the read-only
 // path; the batched persistent launch needs it, since it rewrites psi in one step and reads it
 // again in the next within the same kernel. The other kernels read each psi once per launch.
@@ -271,6 +279,31 @@ template <bool kCoherent = false>
 __device__ __forceinline__ float psi_load(const float* in, int q) {
     return kCoherent ? __ldcg(in + q) : __ldg(in + q);
 }
+// The old CPML memory of node (i, j, k) for e_update (kE) or h_update, for each slab of kSlabs the
+// node lies in (entries of the others are left unset).
+template <bool kE, bool kCoherent, int kSlabs>
+__device__ __forceinline__ void psi_preload(const DeviceGrid& g, const PsiFace* in, int i, int j, int k, PsiOld& o) {
+    int side;
+    if ((kSlabs & 1) && in_slab(i, g.nx, g.pxn, g.pxp)) {
+        const int q = psi_off_x(g, i, j, k, side);
+        const PsiFace& f = in[side];
+        o.v[0] = psi_load<kCoherent>(kE ? f.e[0] : f.h[0], q);
+        o.v[1] = psi_load<kCoherent>(kE ? f.e[1] : f.h[1], q);
+    }
+    if ((kSlabs & 2) && in_slab(j, g.ny, g.pyn, g.pyp)) {
+        const int q = psi_off_y(g, i, j, k, side);
+        const PsiFace& f = in[2 + side];
+        o.v[2] = psi_load<kCoherent>(kE ? f.e[0] : f.h[0], q);
+        o.v[3] = psi_load<kCoherent>(kE ? f.e[1] : f.h[1], q);
+    }
+    if ((kSlabs & 4) && in_slab(k, g.nz, g.pzn, g.pzp)) {
+        const int q = psi_off_z(g, i, j, k, side);
+        const PsiFace& f = in[4 + side];
+        o.v[4] = psi_load<kCoherent>(kE ? f.e[0] : f.h[0], q);
+        o.v[5] = psi_load<kCoherent>(kE ? f.e[1] : f.h[1], q);
+    }
+}
+
 // One CPML recurrence from the old memory value `old`.
 template <bool kHyz = false>
 __device__ __forceinline__ float psi_apply(float old, float* out, int q, bool write, float b, float a, float d, float f,
@@ -304,7 +337,8 @@ __device__ __forceinline__ void h_masks(const DeviceGrid& g, int i, int j, int k
 // kSlabs: the CPML slabs (bit 0 x, 1 y, 2 z) the node may lie in; the other slab tests compile out.
 template <bool kDesignAware = false, bool kCoherent = false, bool kPlate = false, bool kBg = false, int kSlabs = 7>
 __device__ __forceinline__ void e_update(const StepParams& p, const ENbr& n, int i, int j, int k, long long m,
-                                         bool plane_lumped, const PsiIO& ps, float out[3], float pre[3]) {
+                                         bool plane_lumped, const PsiIO& ps, float out[3], float pre[3],
+                                         const PsiOld* old = nullptr) {
     const DeviceGrid& g = p.g;
     bool ex_m, ey_m, ez_m;  // fdtdrav.h:665, 696, 720
     e_masks(g, i, j, k, ex_m, ey_m, ez_m);
@@ -368,20 +402,20 @@ __device__ __forceinline__ void e_update(const StepParams& p, const ENbr& n, int
     if (xs && (ey_m || ez_m)) {
         const int q = psi_off_x(g, i, j, k, side);
         const float bb = __ldg(p.bex + i), aa = __ldg(p.aex + i);
-        if (ey_m) vy = psi_apply(psi_load<kCoherent>(ps.in[side].e[0], q), ps.out[side].e[0], q, ps.write, bb, aa, dHz_i, vy, __fmul_rn(cy.bm, g.dx));
-        if (ez_m) vz = psi_apply(psi_load<kCoherent>(ps.in[side].e[1], q), ps.out[side].e[1], q, ps.write, bb, aa, dHy_i, vz, __fmul_rn(cz.bp, g.dx));
+        if (ey_m) vy = psi_apply(old ? old->v[0] : psi_load<kCoherent>(ps.in[side].e[0], q), ps.out[side].e[0], q, ps.write, bb, aa, dHz_i, vy, __fmul_rn(cy.bm, g.dx));
+        if (ez_m) vz = psi_apply(old ? old->v[1] : psi_load<kCoherent>(ps.in[side].e[1], q), ps.out[side].e[1], q, ps.write, bb, aa, dHy_i, vz, __fmul_rn(cz.bp, g.dx));
     }
     if (ys && (ex_m || ez_m)) {
         const int q = psi_off_y(g, i, j, k, side);
         const float bb = __ldg(p.bey + j), aa = __ldg(p.aey + j);
-        if (ex_m) vx = psi_apply(psi_load<kCoherent>(ps.in[2 + side].e[0], q), ps.out[2 + side].e[0], q, ps.write, bb, aa, dHz_j, vx, __fmul_rn(cx.bp, g.dy));
-        if (ez_m) vz = psi_apply(psi_load<kCoherent>(ps.in[2 + side].e[1], q), ps.out[2 + side].e[1], q, ps.write, bb, aa, dHx_j, vz, __fmul_rn(cz.bm, g.dy));
+        if (ex_m) vx = psi_apply(old ? old->v[2] : psi_load<kCoherent>(ps.in[2 + side].e[0], q), ps.out[2 + side].e[0], q, ps.write, bb, aa, dHz_j, vx, __fmul_rn(cx.bp, g.dy));
+        if (ez_m) vz = psi_apply(old ? old->v[3] : psi_load<kCoherent>(ps.in[2 + side].e[1], q), ps.out[2 + side].e[1], q, ps.write, bb, aa, dHx_j, vz, __fmul_rn(cz.bm, g.dy));
     }
     if (zs && (ex_m || ey_m)) {
         const int q = psi_off_z(g, i, j, k, side);
         const float bb = __ldg(p.bez + k), aa = __ldg(p.aez + k);
-        if (ex_m) vx = psi_apply(psi_load<kCoherent>(ps.in[4 + side].e[0], q), ps.out[4 + side].e[0], q, ps.write, bb, aa, dHy_k, vx, __fmul_rn(cx.bm, g.dz));
-        if (ey_m) vy = psi_apply(psi_load<kCoherent>(ps.in[4 + side].e[1], q), ps.out[4 + side].e[1], q, ps.write, bb, aa, dHx_k, vy, __fmul_rn(cy.bp, g.dz));
+        if (ex_m) vx = psi_apply(old ? old->v[4] : psi_load<kCoherent>(ps.in[4 + side].e[0], q), ps.out[4 + side].e[0], q, ps.write, bb, aa, dHy_k, vx, __fmul_rn(cx.bm, g.dz));
+        if (ey_m) vy = psi_apply(old ? old->v[5] : psi_load<kCoherent>(ps.in[4 + side].e[1], q), ps.out[4 + side].e[1], q, ps.write, bb, aa, dHx_k, vy, __fmul_rn(cy.bp, g.dz));
     }
     out[0] = ex_m ? vx : n.ex;
     out[1] = ey_m ? vy : n.ey;
@@ -392,7 +426,7 @@ __device__ __forceinline__ void e_update(const StepParams& p, const ENbr& n, int
 // kSlabs as for e_update.
 template <bool kCoherent = false, bool kBg = false, int kSlabs = 7>
 __device__ __forceinline__ void h_update(const StepParams& p, const HNbr& n, int i, int j, int k,
-                                         const PsiIO& ps, float out[3], float pre[3]) {
+                                         const PsiIO& ps, float out[3], float pre[3], const PsiOld* old = nullptr) {
     const DeviceGrid& g = p.g;
     bool hx_m, hy_m, hz_m;  // fdtdrav.h:328, 357, 382
     h_masks(g, i, j, k, hx_m, hy_m, hz_m);
@@ -429,20 +463,20 @@ __device__ __forceinline__ void h_update(const StepParams& p, const HNbr& n, int
     if (xs && (hy_m || hz_m)) {
         const int q = psi_off_x(g, i, j, k, side);
         const float bb = __ldg(p.bmx + i), aa = __ldg(p.amx + i);
-        if (hy_m) vy = psi_apply(psi_load<kCoherent>(ps.in[side].h[0], q), ps.out[side].h[0], q, ps.write, bb, aa, dEz_i, vy, __fmul_rn(cy.bp, g.dx));
-        if (hz_m) vz = psi_apply(psi_load<kCoherent>(ps.in[side].h[1], q), ps.out[side].h[1], q, ps.write, bb, aa, dEy_i, vz, __fmul_rn(cz.bm, g.dx));
+        if (hy_m) vy = psi_apply(old ? old->v[0] : psi_load<kCoherent>(ps.in[side].h[0], q), ps.out[side].h[0], q, ps.write, bb, aa, dEz_i, vy, __fmul_rn(cy.bp, g.dx));
+        if (hz_m) vz = psi_apply(old ? old->v[1] : psi_load<kCoherent>(ps.in[side].h[1], q), ps.out[side].h[1], q, ps.write, bb, aa, dEy_i, vz, __fmul_rn(cz.bm, g.dx));
     }
     if (ys && (hx_m || hz_m)) {
         const int q = psi_off_y(g, i, j, k, side);
         const float bb = __ldg(p.bmy + j), aa = __ldg(p.amy + j);
-        if (hx_m) vx = psi_apply(psi_load<kCoherent>(ps.in[2 + side].h[0], q), ps.out[2 + side].h[0], q, ps.write, bb, aa, dEz_j, vx, __fmul_rn(cx.bm, g.dy));
-        if (hz_m) vz = psi_apply(psi_load<kCoherent>(ps.in[2 + side].h[1], q), ps.out[2 + side].h[1], q, ps.write, bb, aa, dEx_j, vz, __fmul_rn(cz.bp, g.dy));
+        if (hx_m) vx = psi_apply(old ? old->v[2] : psi_load<kCoherent>(ps.in[2 + side].h[0], q), ps.out[2 + side].h[0], q, ps.write, bb, aa, dEz_j, vx, __fmul_rn(cx.bm, g.dy));
+        if (hz_m) vz = psi_apply(old ? old->v[3] : psi_load<kCoherent>(ps.in[2 + side].h[1], q), ps.out[2 + side].h[1], q, ps.write, bb, aa, dEx_j, vz, __fmul_rn(cz.bp, g.dy));
     }
     if (zs && (hx_m || hy_m)) {
         const int q = psi_off_z(g, i, j, k, side);
         const float bb = __ldg(p.bmz + k), aa = __ldg(p.amz + k);
-        if (hx_m) vx = psi_apply(psi_load<kCoherent>(ps.in[4 + side].h[0], q), ps.out[4 + side].h[0], q, ps.write, bb, aa, dEy_k, vx, __fmul_rn(cx.bp, g.dz));
-        if (hy_m) vy = psi_apply<true>(psi_load<kCoherent>(ps.in[4 + side].h[1], q), ps.out[4 + side].h[1], q, ps.write, bb, aa, dEx_k, vy, __fmul_rn(cy.bm, g.dz));
+        if (hx_m) vx = psi_apply(old ? old->v[4] : psi_load<kCoherent>(ps.in[4 + side].h[0], q), ps.out[4 + side].h[0], q, ps.write, bb, aa, dEy_k, vx, __fmul_rn(cx.bp, g.dz));
+        if (hy_m) vy = psi_apply<true>(old ? old->v[5] : psi_load<kCoherent>(ps.in[4 + side].h[1], q), ps.out[4 + side].h[1], q, ps.write, bb, aa, dEx_k, vy, __fmul_rn(cy.bm, g.dz));
     }
     out[0] = hx_m ? vx : n.hx;
     out[1] = hy_m ? vy : n.hy;

@@ -16,6 +16,15 @@ namespace fdtd {
 #ifndef FDTD_SHELL_MIN_BLOCKS
 #define FDTD_SHELL_MIN_BLOCKS 6
 #endif
+// The shell E pass loads a CPML node's old psi together with its fields (e_node_global's kEarly):
+// measured at 512^3, the fused step 2.2 % faster (256^3: 3.3 %). The shell H pass gains nothing
+// from it, and the two-pass kernels, whose spills it raises, lose 7-9 % at 64^3 and 128^3.
+#ifndef FDTD_SHELL_EARLY_E
+#define FDTD_SHELL_EARLY_E 1
+#endif
+#ifndef FDTD_SHELL_EARLY_H
+#define FDTD_SHELL_EARLY_H 0
+#endif
 template <typename Idx>
 __global__ void __launch_bounds__(256, FDTD_TWO_PASS_MIN_BLOCKS) k_update_e(const __grid_constant__ StepParams p, FieldPtrs f,
                                                   const __grid_constant__ PsiSet ps, long long m) {
@@ -61,7 +70,7 @@ __device__ __forceinline__ void shell_e_item(const StepParams& p, const FieldPtr
     int i, j;
     if (!shell_node(it, p.g, i, j)) return;
     for (int k = it.z, k1 = it.z + ((it.w >> 22) & 15); k <= k1; ++k)
-        e_node_global<false, false, false, Idx, kSlabs>(p, fi, fo, pin, pout, i, j, k, m);
+        e_node_global<false, false, false, Idx, kSlabs, FDTD_SHELL_EARLY_E != 0>(p, fi, fo, pin, pout, i, j, k, m);
 }
 template <typename Idx, int kSlabs>
 __device__ __forceinline__ void shell_h_item(const StepParams& p, const FieldPtrs& fi, const FieldPtrs& fo,
@@ -69,7 +78,7 @@ __device__ __forceinline__ void shell_h_item(const StepParams& p, const FieldPtr
     int i, j;
     if (!shell_node(it, p.g, i, j)) return;
     for (int k = it.z, k1 = it.z + ((it.w >> 22) & 15); k <= k1; ++k)
-        h_node_global<false, Idx, kSlabs>(p, fi, fo, fo, pin, pout, i, j, k, m);
+        h_node_global<false, Idx, kSlabs, FDTD_SHELL_EARLY_H != 0>(p, fi, fo, fo, pin, pout, i, j, k, m);
 }
 
 // e1, e2, e3: the ends of the first three lists in the launch (blocks from e3 on take the fourth).
