@@ -261,9 +261,9 @@ TWO_PASS_DRAM_BYTES_PER_CELL = 78.15
 
 # DRAM bytes per cell update of one fused step (k_shell_e + k_sweep_interior + k_shell_h),
 # dram__bytes_read.sum + dram__bytes_write.sum from ncu captures of these kernels (the launch-list
-# commands in profiles/yee_step_boxes512_launch_list.md): 63.46 B on the 512^3 bench workload
+# commands in profiles/yee_step_boxes512_launch_list.md): 63.59 B on the 512^3 bench workload
 # itself, 72.77 B at 256^3, where the shell share is larger. Refreshed whenever the kernels change.
-FUSED_DRAM_BYTES_PER_CELL = {"512": 63.46, "256": 72.77}
+FUSED_DRAM_BYTES_PER_CELL = {"512": 63.59, "256": 72.77}
 
 
 def measured_traffic(schedule, cells, config):
