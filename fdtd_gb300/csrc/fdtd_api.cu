@@ -104,6 +104,7 @@ struct fdtd_handle {
     bool have_second = false;
     FusedMaps maps[2];
     CpmlMaps cmaps[2];  // the CPML sweep's maps per input buffer
+    char* psi_base[2] = {nullptr, nullptr};  // the allocation holding each CPML memory set
     FusedFork fork{};  // second stream and events of the fused step (created with the fused buffers)
     struct PlanCache {  // the last fused plan and what it was made for (chunk, schedule, design box)
         bool valid = false;
@@ -306,16 +307,30 @@ int validate_grid(const fdtd_grid* g) {
 int ensure_prepared(fdtd_handle* h);
 
 // One set of CPML memory slabs (4 arrays per face), initialised to 1.2e-38.
+// CPML memory set s: the 24 arrays (4 per face) in one allocation, each array on a 256-byte
+// boundary, filled with the initial value by one launch (separate allocations of this size cost
+// tens of microseconds each).
 int alloc_psi_set(fdtd_handle* h, int s) {
+    size_t off[6], bytes[6], total = 0;
     for (int f = 0; f < 6; ++f) {
-        const long long n = h->psi_elems[f];
-        float* arr[4] = {nullptr, nullptr, nullptr, nullptr};
-        for (int q = 0; q < 4 && n > 0; ++q) {
-            if (h->alloc((void**)&arr[q], sizeof(float) * n) != cudaSuccess) return fail(FDTD_ERR_OOM, "CPML memory allocation failed");
-            if (launch_fill(arr[q], n, kTiny, nullptr) != cudaSuccess) return fail(FDTD_ERR_CUDA, "fill failed");
-        }
-        h->psi[s].f[f].e[0] = arr[0]; h->psi[s].f[f].e[1] = arr[1];
-        h->psi[s].f[f].h[0] = arr[2]; h->psi[s].f[f].h[1] = arr[3];
+        bytes[f] = ((size_t)h->psi_elems[f] * sizeof(float) + 255) / 256 * 256;
+        off[f] = total;
+        total += 4 * bytes[f];
+    }
+    h->psi[s] = PsiSet{};
+    h->psi_base[s] = nullptr;
+    if (total == 0) return FDTD_OK;
+    char* base = nullptr;
+    if (h->alloc((void**)&base, total) != cudaSuccess) return fail(FDTD_ERR_OOM, "CPML memory allocation failed");
+    h->psi_base[s] = base;
+    if (launch_fill((float*)base, (long long)(total / sizeof(float)), kTiny, nullptr) != cudaSuccess)
+        return fail(FDTD_ERR_CUDA, "fill failed");
+    for (int f = 0; f < 6; ++f) {
+        if (h->psi_elems[f] <= 0) continue;
+        float* a[4];
+        for (int q = 0; q < 4; ++q) a[q] = (float*)(base + off[f] + (size_t)q * bytes[f]);
+        h->psi[s].f[f].e[0] = a[0]; h->psi[s].f[f].e[1] = a[1];
+        h->psi[s].f[f].h[0] = a[2]; h->psi[s].f[f].h[1] = a[3];
     }
     return FDTD_OK;
 }
@@ -462,12 +477,9 @@ void release_fused(fdtd_handle* h) {
         h->release(h->field[1][c]);
         h->field[1][c] = nullptr;
     }
-    for (int f = 0; f < 6; ++f) {
-        float* a[4];
-        psi_arrays(h, 1, f, a);
-        for (float* x : a) h->release(x);
-        h->psi[1].f[f] = PsiFace{};
-    }
+    h->release(h->psi_base[1]);
+    h->psi_base[1] = nullptr;
+    h->psi[1] = PsiSet{};
     h->release((void*)h->work.interior);
     h->work = FusedWork{};
     h->have_second = false;
