@@ -9,6 +9,9 @@
 
 namespace fdtd {
 
+// Planes per CTA of the grid-sized setup kernels (one node per thread and plane).
+constexpr int kSetupPlanes = 8;
+
 // One axis of setABCPML (fdtdrav.h:1774-1891 for x_n, 1912-1941 for x_p, and the y / z mirrors).
 // prof = {b_e, a_e, b_m, a_m, kappa_e, kappa_m}, each n entries. Nodes outside both slabs keep
 // b = a = 1.2e-38 (setZero) and kappa = 1.
@@ -230,8 +233,10 @@ __global__ void k_paint(uint8_t* mat, DeviceGrid g, int is, int js, int ks, int 
 __global__ void k_index_max(const uint8_t* __restrict__ mat, DeviceGrid g, int* out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z;
-    int v = (i < g.nx && j < g.ny) ? mat[(long long)k * g.plane + (long long)j * g.pitch + i] : 0;
+    int v = 0;
+    if (i < g.nx && j < g.ny)
+        for (int k = blockIdx.z * kSetupPlanes, k1 = min(g.nz, k + kSetupPlanes); k < k1; ++k)
+            v = max(v, (int)mat[(long long)k * g.plane + (long long)j * g.pitch + i]);
     for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
     if ((threadIdx.x & 31) == 0 && v > 0) atomicMax(out, v);
 }
@@ -239,7 +244,7 @@ __global__ void k_index_max(const uint8_t* __restrict__ mat, DeviceGrid g, int* 
 cudaError_t launch_index_max(const uint8_t* mat, const DeviceGrid& g, int* out, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(out, 0, sizeof(int), st);
     if (e != cudaSuccess) return e;
-    const dim3 block(32, 8, 1), grid((g.nx + 31) / 32, (g.ny + 7) / 8, g.nz);
+    const dim3 block(32, 8, 1), grid((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + kSetupPlanes - 1) / kSetupPlanes);
     k_index_max<<<grid, block, 0, st>>>(mat, g, out);
     return cudaGetLastError();
 }
@@ -265,12 +270,8 @@ namespace fdtd {
 // The seven cells are those the three E edge averages read, (i,j,k) (i-1,j,k) (i,j-1,k) (i,j,k-1)
 // (i-1,j-1,k) (i-1,j,k-1) (i,j-1,k-1); the four cells of the H faces are among them.
 // Nodes of the design region's edge box [dlo, dhi] get kDesignNode.
-__global__ void k_node_class(const uint8_t* __restrict__ mat, uint8_t* __restrict__ cls, DeviceGrid g, int4 dlo,
-                             int4 dhi) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z;
-    if (i >= g.nx || j >= g.ny) return;
+__device__ __forceinline__ void node_class(const uint8_t* __restrict__ mat, uint8_t* __restrict__ cls,
+                                           const DeviceGrid& g, int4 dlo, int4 dhi, int i, int j, int k) {
     const long long n = (long long)k * g.plane + (long long)j * g.pitch + i;
     uint8_t c = kGeneral;
     // the seven cells as the general path reads them (cells outside the grid count as material 0)
@@ -289,6 +290,17 @@ __global__ void k_node_class(const uint8_t* __restrict__ mat, uint8_t* __restric
         c = (uint8_t)(kUniformGeneral + m0);  // general path without the cell-material loads
     if (i >= dlo.x && i <= dhi.x && j >= dlo.y && j <= dhi.y && k >= dlo.z && k <= dhi.z) c = kDesignNode;
     cls[n] = c;
+}
+
+// One CTA per 32 x 8 block of kSetupPlanes planes (one node per thread and plane): a CTA per
+// block of one plane made the grid-sized setup kernels bound by launching CTAs.
+__global__ void k_node_class(const uint8_t* __restrict__ mat, uint8_t* __restrict__ cls, DeviceGrid g, int4 dlo,
+                             int4 dhi) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.nx || j >= g.ny) return;
+    for (int k = blockIdx.z * kSetupPlanes, k1 = min(g.nz, k + kSetupPlanes); k < k1; ++k)
+        node_class(mat, cls, g, dlo, dhi, i, j, k);
 }
 
 __global__ void k_class_lumped(uint8_t* cls, DeviceGrid g, const LumpedEdge* edges, int n_edges) {
@@ -312,7 +324,7 @@ cudaError_t launch_node_class(const DeviceGrid& g, const uint8_t* mat, const Lum
     const int4 dlo = design_box ? make_int4(design_box[0], design_box[1], design_box[2], 0) : make_int4(1, 1, 1, 0);
     const int4 dhi = design_box ? make_int4(design_box[3], design_box[4], design_box[5], 0) : make_int4(0, 0, 0, 0);
     dim3 block(32, 8, 1);
-    dim3 grid((g.nx + 31) / 32, (g.ny + 7) / 8, g.nz);
+    dim3 grid((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + kSetupPlanes - 1) / kSetupPlanes);
     k_node_class<<<grid, block, 0, st>>>(mat, cls, g, dlo, dhi);
     if (n_edges > 0) k_class_lumped<<<(n_edges + 127) / 128, 128, 0, st>>>(cls, g, edges, n_edges);
     return cudaGetLastError();
@@ -362,15 +374,7 @@ __device__ __forceinline__ int find_slot(const unsigned long long* __restrict__ 
 // Insert the key of every kInterfaceNode or kGeneral node into the set while it holds fewer than
 // kIfaceTableSize / 2 keys (*filled counts them, a few more may land while it reaches that); a key
 // that finds no room stays out (its nodes take the general path).
-__global__ void k_iface_insert(const uint8_t* __restrict__ cls, const uint8_t* __restrict__ mat, DeviceGrid g,
-                               unsigned long long* table, int* filled) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z;
-    if (i >= g.nx || j >= g.ny) return;
-    const long long n = (long long)k * g.plane + (long long)j * g.pitch + i;
-    if (cls[n] != kInterfaceNode && cls[n] != kGeneral) return;
-    const unsigned long long key = cell_key(mat, g, i, j, k);
+__device__ __forceinline__ void iface_insert(unsigned long long* table, int* filled, unsigned long long key) {
     unsigned s = slot_of(key);
     for (int q = 0; q < kMaxProbes; ++q, s = (s + 1) & (kIfaceTableSize - 1)) {
         const unsigned long long v = *(volatile unsigned long long*)(table + s);
@@ -383,6 +387,16 @@ __global__ void k_iface_insert(const uint8_t* __restrict__ cls, const uint8_t* _
             return;
         }
         if (old == key) return;
+    }
+}
+__global__ void k_iface_insert(const uint8_t* __restrict__ cls, const uint8_t* __restrict__ mat, DeviceGrid g,
+                               unsigned long long* table, int* filled) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.nx || j >= g.ny) return;
+    for (int k = blockIdx.z * kSetupPlanes, k1 = min(g.nz, k + kSetupPlanes); k < k1; ++k) {
+        const long long n = (long long)k * g.plane + (long long)j * g.pitch + i;
+        if (cls[n] == kInterfaceNode || cls[n] == kGeneral) iface_insert(table, filled, cell_key(mat, g, i, j, k));
     }
 }
 
@@ -407,13 +421,21 @@ __global__ void k_iface_slot_rows(const unsigned long long* __restrict__ table, 
 // kUniformGeneral + m nodes (m), the interface row of kInterfaceNode and kGeneral nodes whose key
 // has one, and kRecGeneral | class for the rest. kInterfaceNode nodes without a row become
 // kGeneral.
+__device__ __forceinline__ void iface_row(uint8_t* __restrict__ cls, const uint8_t* __restrict__ mat, const DeviceGrid& g,
+                                          const unsigned long long* __restrict__ table, const int* __restrict__ slot_row,
+                                          uint16_t* __restrict__ rec, int i, int j, int k);
 __global__ void k_iface_rows(uint8_t* __restrict__ cls, const uint8_t* __restrict__ mat, DeviceGrid g,
                              const unsigned long long* __restrict__ table, const int* __restrict__ slot_row,
                              uint16_t* __restrict__ rec) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z;
     if (i >= g.nx || j >= g.ny) return;
+    for (int k = blockIdx.z * kSetupPlanes, k1 = min(g.nz, k + kSetupPlanes); k < k1; ++k)
+        iface_row(cls, mat, g, table, slot_row, rec, i, j, k);
+}
+__device__ __forceinline__ void iface_row(uint8_t* __restrict__ cls, const uint8_t* __restrict__ mat, const DeviceGrid& g,
+                                          const unsigned long long* __restrict__ table, const int* __restrict__ slot_row,
+                                          uint16_t* __restrict__ rec, int i, int j, int k) {
     const long long n = (long long)k * g.plane + (long long)j * g.pitch + i;
     int c = cls[n];
     int r = kRecGeneral | c;
@@ -479,7 +501,7 @@ cudaError_t launch_iface_set(const DeviceGrid& g, const uint8_t* cls, const uint
     cudaError_t e = cudaMemsetAsync(table, 0xff, sizeof(unsigned long long) * kIfaceTableSize, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(counters, 0, 2 * sizeof(int), st);
     if (e != cudaSuccess) return e;
-    const dim3 block(32, 8, 1), grid((g.nx + 31) / 32, (g.ny + 7) / 8, g.nz);
+    const dim3 block(32, 8, 1), grid((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + kSetupPlanes - 1) / kSetupPlanes);
     k_iface_insert<<<grid, block, 0, st>>>(cls, mat, g, table, counters);
     k_iface_compact<<<kIfaceTableSize / 256, 256, 0, st>>>(table, keys, counters + 1);
     return cudaGetLastError();
@@ -490,7 +512,7 @@ cudaError_t launch_iface_rows(const DeviceGrid& g, uint8_t* cls, const uint8_t* 
     cudaError_t e = cudaMemsetAsync(slot_row, 0xff, sizeof(int) * kIfaceTableSize, st);
     if (e != cudaSuccess) return e;
     if (n_keys > 0) k_iface_slot_rows<<<(n_keys + 127) / 128, 128, 0, st>>>(table, keys, n_keys, slot_row);
-    const dim3 block(32, 8, 1), grid((g.nx + 31) / 32, (g.ny + 7) / 8, g.nz);
+    const dim3 block(32, 8, 1), grid((g.nx + 31) / 32, (g.ny + 7) / 8, (g.nz + kSetupPlanes - 1) / kSetupPlanes);
     k_iface_rows<<<grid, block, 0, st>>>(cls, mat, g, table, slot_row, rec);
     return cudaGetLastError();
 }
