@@ -250,6 +250,7 @@ bool in_slab_host(int q, int n, int pn, int pp) { return q < pn || q >= n - pp; 
 
 StepParams make_params(fdtd_handle* h) {
     StepParams p{};
+    p.fom_node = p.fom_read = -1;
     p.g = h->g;
     p.mat = h->mat;
     p.cls = h->cls;
@@ -1797,10 +1798,10 @@ int adj_recompute_step(fdtd_handle* h, const StepParams& pr, long long reach, fl
                     std::min(g.nx, d[3] + 1 + e), std::min(g.ny, d[4] + 1 + e), std::min(g.nz, d[5] + 1 + e)};
     const int c = h->cur;
     const FieldPtrs f{h->field[c][0], h->field[c][1], h->field[c][2], h->field[c][3], h->field[c][4], h->field[c][5]};
-    CUDA_TRY(launch_two_pass_box(pr, f, h->psi[c], b, h->step, h->stream));
+    StepParams q = pr;
+    q.design_snap = snap;  // k_design_e writes the design region's E of the step
+    CUDA_TRY(launch_two_pass_box(q, f, h->psi[c], b, h->step, h->stream));
     ++h->step;
-    CUDA_TRY(launch_after_step(h->field[c][0], h->field[c][1], h->field[c][2], g, h->adj.probe, nullptr, h->dbox, snap,
-                               h->stream));
     return FDTD_OK;
 }
 
@@ -1839,13 +1840,30 @@ int adj_forward_enqueue(fdtd_handle* h, int64_t n, int32_t checkpoint_every, int
         CUDA_TRY(launch_after_step(h->field[c][0], h->field[c][1], h->field[c][2], g, A.probe, nullptr, h->dbox, adj_slot(h, 0),
                                    h->stream));
     }
+    // two-pass steps take their records in k_design_e (no launch of their own): the E of the
+    // design edge box is final there, and so is every other E
+    const bool two_pass = !use_fused(h);
+    StepParams pa = make_params(h);
+    if (two_pass) {
+        const int* d = h->dbox;
+        const bool in_box = pi >= d[0] && pi <= d[3] && pj >= d[1] && pj <= d[4] && pk >= d[2] && pk <= d[5];
+        pa.fom_node = in_box ? A.probe : -1;
+        pa.fom_read = in_box ? -1 : A.probe;
+    }
     for (long long s = 0; s < n; ++s) {
         if (K > 0 && s % K == 0) {
             if ((rc = state_copy(h, adj_ckpt(h, s / K), true))) return rc;
         } else if (A.S > 0 && (s % K) % A.S == 0) {
             CUDA_TRY(launch_box_state(cur_fields(h), g, A.sub_box, adj_sub(h, s / K, (s % K) / A.S), true, h->stream));
         }
-        if ((rc = adj_forward_step(h, A.samples + s, K == 0 ? adj_slot(h, s + 1) : nullptr))) return rc;
+        if (two_pass) {
+            pa.fom_sample = A.samples + s;
+            pa.design_snap = K == 0 ? adj_slot(h, s + 1) : nullptr;
+            CUDA_TRY(launch_two_pass(pa, cur_fields(h), h->psi[h->cur], h->step, h->stream));
+            ++h->step;
+        } else if ((rc = adj_forward_step(h, A.samples + s, K == 0 ? adj_slot(h, s + 1) : nullptr))) {
+            return rc;
+        }
     }
     if ((rc = state_copy(h, adj_ckpt(h, A.ckpt_slots - 1), true))) return rc;  // final state
     CUDA_TRY(cudaMemcpyAsync(A.pinned_samples, A.samples, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost, h->stream));

@@ -152,6 +152,13 @@ struct StepParams {
     const int* plate_k;
     const int4* plate_nodes;     // nodes of class kPlateNode {i, j, k, 0} (updated by k_plate_e)
     int n_plate_nodes;
+    // records of an adjoint run that k_design_e takes in two-pass steps (NULL otherwise): the new
+    // E of the design edge box into design_snap (three arrays of the box volume, x fastest), and
+    // the FoM sample Ez into *fom_sample, from the design node fom_node when the probe is one
+    // (else -1) or read at node fom_read by the kernel's first thread (else -1)
+    float* design_snap;
+    float* fom_sample;
+    long long fom_node, fom_read;
 };
 
 // ------------------------------------------------------------------------------------------

@@ -74,6 +74,13 @@ __device__ __forceinline__ void e_node_global(const StepParams& p, const FieldPt
     // k_design_e writes the design region's E, k_plate_e the plate nodes' E
     if (!kDesign && !kPlate && (c == kDesignNode || c == kPlateNode)) return;
     fo.ex[n] = out[0]; fo.ey[n] = out[1]; fo.ez[n] = out[2];
+    if (kDesign && p.design_snap) {  // adjoint records (k_design_e covers the design edge box)
+        const int* d = p.dbox;
+        const long long bx = d[3] - d[0] + 1, by = d[4] - d[1] + 1, ne = bx * by * (d[5] - d[2] + 1);
+        const long long q = ((long long)(k - d[2]) * by + (j - d[1])) * bx + (i - d[0]);
+        p.design_snap[q] = out[0]; p.design_snap[ne + q] = out[1]; p.design_snap[2 * ne + q] = out[2];
+    }
+    if (kDesign && p.fom_sample && (long long)n == p.fom_node) *p.fom_sample = out[2];
     if (p.probe_k[k] < p.probe_k[k + 1]) {
         const long long row = m % p.ring_cap;
         for (int q = 0; q < 3; ++q) sample(p, row, q, i, j, k, pre[q]);

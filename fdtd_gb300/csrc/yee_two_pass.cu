@@ -134,6 +134,10 @@ __global__ void __launch_bounds__(256) k_design_e(const __grid_constant__ StepPa
                                                   const __grid_constant__ PsiSet pin,
                                                   const __grid_constant__ PsiSet pout, long long m) {
     const int* d = p.dbox;
+    // an FoM probe outside the design region: its E is final once the other E kernels are done
+    if (p.fom_sample && p.fom_read >= 0 && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 &&
+        threadIdx.y == 0)
+        *p.fom_sample = fi.ez[p.fom_read];
     const int i = d[0] + blockIdx.x * 32 + threadIdx.x;
     const int j = d[1] + blockIdx.y * 8 + threadIdx.y;
     const int k = d[2] + blockIdx.z;

@@ -289,3 +289,23 @@ def test_checkpointed_equals_resident_fused(gpu_lib):
     for J, g, f in out[1:]:
         assert J == out[0][0] and np.array_equal(g, out[0][1])
         assert bitwise_equal(f, out[0][2])
+
+
+@pytest.mark.parametrize("probe", [(12, 10, 9), (18, 11, 9)])
+def test_fom_records_same_in_both_schedules(gpu_lib, probe):
+    """The two-pass steps take the FoM sample and the design-region snapshots inside the design
+    kernel (from the design node itself when the probe is one, first probe: inside the design
+    edge box); the fused steps take them with a kernel of their own. J and the gradient agree bit
+    for bit, and J matches the FP64 oracle."""
+    from fdtd_gb300 import solver
+    sc, box, eps, _ = design_case(6, steps=90)
+    out = []
+    for schedule, K in ((1, 0), (1, 16), (2, 0), (2, 16)):
+        with solver.Simulation.from_scenario(sc, schedule, probe_capacity=sc.steps) as sim:
+            sim.set_design_region(box, eps)
+            J = sim.adjoint_forward(sc.steps, probe, K)
+            out.append((J, sim.adjoint_backward()))
+    for J, g in out[1:]:
+        assert J == out[0][0] and np.array_equal(g, out[0][1])
+    J64 = oracle.fom_grad(sc, probe, box, eps.astype(np.float64), precision="f64", grad=False)
+    assert abs(out[0][0] - J64) <= 1e-4 * abs(J64)
