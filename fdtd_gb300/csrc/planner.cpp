@@ -49,17 +49,21 @@ std::vector<int> starts(int lo, int hi, int size, int align, bool overlap) {
 
 }  // namespace
 
-// Planes per interior item: whole columns unless that leaves too few CTAs to fill the GPU, and at
-// most kMaxItemPlanes - 2 (an item also streams the plane below and recomputes the one above).
-// Chunks are halved until the grid has at least kMinItems of them; 8192 measured best at 512^3 and
-// 1024 x 1024 x 896 against 2048, 4096 and 16384 (shorter chunks keep the CTAs in flight on fewer
-// planes; each chunk re-reads two planes).
+// Planes per interior item: chunks are halved until the grid has at least kMinItems of them, and
+// no chunk is longer than kMaxChunk planes (an item also streams the plane below and recomputes
+// the one above). 8192 items measured best at 512^3 against 2048, 4096 and 16384 (32 planes
+// there). The cap matters on larger grids: at 1024 x 1024 x 896 the item count alone gives
+// 224-plane chunks, and capping them at 32 planes took the fused step from 13.31 to 9.95 ms
+// (70.6 -> 94.4 Gcell-updates/s; 16, 24, 40 and 56 planes: 10.27, 10.05, 9.92, 10.14 ms). Short
+// chunks keep the CTAs in flight on neighbouring planes, so the halo rows one CTA loads are still
+// in L2 when its neighbours load them.
 int plan_chunk(const PlanGrid& g) {
     constexpr long long kMinItems = 8192;
+    constexpr int kMaxChunk = 32;
     const long long tiles = (long long)((g.nx + kTileX - 1) / kTileX) * ((g.ny + kTileY - 1) / kTileY);
     int kc = g.nz;
     while (kc > 16 && tiles * ((g.nz + kc - 1) / kc) < kMinItems) kc = (kc + 1) / 2;
-    return std::max(1, std::min(kc, kMaxItemPlanes - 2));
+    return std::max(1, std::min(kc, kMaxChunk));
 }
 
 // Interior tiles (32 x 16 columns whose E positions x0..x0+TX, y0..y0+TY all lie in the x / y
