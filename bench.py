@@ -270,7 +270,9 @@ def measured_traffic(schedule, cells, config):
     if schedule == 3:
         return None  # not profiled
     if schedule == 2:
-        per_cell = FUSED_DRAM_BYTES_PER_CELL.get(config, FUSED_DRAM_BYTES_PER_CELL["512"])
+        per_cell = FUSED_DRAM_BYTES_PER_CELL.get(config)
+        if per_cell is None:
+            return None  # no capture of this workload's DRAM bytes
     else:
         per_cell = TWO_PASS_DRAM_BYTES_PER_CELL
     return round(per_cell * cells)
