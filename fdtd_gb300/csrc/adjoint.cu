@@ -31,7 +31,13 @@ namespace {
 struct PsiTerm {
     float* mem;  // adjoint psi entry, NULL when the node is outside the slab
     float b, a, cpsi;
+    float old;   // its value before this step
 };
+// The term of adjoint psi entry `mem`, its old value read here: where the term is built, not
+// where it is applied (3-4 % off the reverse step at 128^3).
+__device__ __forceinline__ PsiTerm psi_term(float* mem, float b, float a, float cpsi) {
+    return PsiTerm{mem, b, a, cpsi, *mem};
+}
 
 // Transpose of one component update v' = a v + c1 d1 + c2 d2 (+ psi terms t1 on d1, t2 on d2):
 // returns the new lambda of the component and the contributions g1, g2 to the fields of d1, d2.
@@ -40,12 +46,12 @@ __device__ __forceinline__ float adj_comp(float L, float a, float c1, float c2, 
     g1 = c1 * L;
     g2 = c2 * L;
     if (t1.mem) {
-        const float mm = __fmaf_rn(t1.cpsi, L, *t1.mem);
+        const float mm = __fmaf_rn(t1.cpsi, L, t1.old);
         *t1.mem = t1.b * mm;
         g1 = __fmaf_rn(t1.a, mm, g1);
     }
     if (t2.mem) {
-        const float mm = __fmaf_rn(t2.cpsi, L, *t2.mem);
+        const float mm = __fmaf_rn(t2.cpsi, L, t2.old);
         *t2.mem = t2.b * mm;
         g2 = __fmaf_rn(t2.a, mm, g2);
     }
@@ -93,25 +99,25 @@ __device__ __forceinline__ void adj_h_general(const StepParams& p, const AdjStat
     int side;
     float g0 = 0.f, g1 = 0.f, g2 = 0.f, g3 = 0.f, g4 = 0.f, g5 = 0.f;
     if (hx_m) {  // Hx: c1 on dEy_k (z CPML), c2 on dEz_j (y CPML)
-        PsiTerm t1{nullptr, 0, 0, 0}, t2{nullptr, 0, 0, 0};
-        if (zs) { const int q = psi_off_z(g, i, j, k, side); t1 = PsiTerm{psa.f[4 + side].h[0] + q, p.bmz[k], p.amz[k], __fmul_rn(cx.bp, g.dz)}; }
-        if (ys) { const int q = psi_off_y(g, i, j, k, side); t2 = PsiTerm{psa.f[2 + side].h[0] + q, p.bmy[j], p.amy[j], __fmul_rn(cx.bm, g.dy)}; }
+        PsiTerm t1{nullptr, 0, 0, 0, 0}, t2{nullptr, 0, 0, 0, 0};
+        if (zs) { const int q = psi_off_z(g, i, j, k, side); t1 = psi_term(psa.f[4 + side].h[0] + q, p.bmz[k], p.amz[k], __fmul_rn(cx.bp, g.dz)); }
+        if (ys) { const int q = psi_off_y(g, i, j, k, side); t2 = psi_term(psa.f[2 + side].h[0] + q, p.bmy[j], p.amy[j], __fmul_rn(cx.bm, g.dy)); }
         const float c1 = zs ? kdiv(cx.bp, bx, B.h[2][0], p.kmz, k) : cx.bp;
         const float c2 = ys ? kdiv(cx.bm, bx, B.h[1][0], p.kmy, j) : cx.bm;
         lx = adj_comp(lx, cx.a, c1, c2, t1, t2, g0, g1);
     }
     if (hy_m) {  // Hy: c1 on dEz_i (x CPML), c2 on dEx_k (z CPML)
-        PsiTerm t1{nullptr, 0, 0, 0}, t2{nullptr, 0, 0, 0};
-        if (xs) { const int q = psi_off_x(g, i, j, k, side); t1 = PsiTerm{psa.f[side].h[0] + q, p.bmx[i], p.amx[i], __fmul_rn(cy.bp, g.dx)}; }
-        if (zs) { const int q = psi_off_z(g, i, j, k, side); t2 = PsiTerm{psa.f[4 + side].h[1] + q, p.bmz[k], p.amz[k], __fmul_rn(cy.bm, g.dz)}; }
+        PsiTerm t1{nullptr, 0, 0, 0, 0}, t2{nullptr, 0, 0, 0, 0};
+        if (xs) { const int q = psi_off_x(g, i, j, k, side); t1 = psi_term(psa.f[side].h[0] + q, p.bmx[i], p.amx[i], __fmul_rn(cy.bp, g.dx)); }
+        if (zs) { const int q = psi_off_z(g, i, j, k, side); t2 = psi_term(psa.f[4 + side].h[1] + q, p.bmz[k], p.amz[k], __fmul_rn(cy.bm, g.dz)); }
         const float c1 = xs ? kdiv(cy.bp, by, B.h[0][0], p.kmx, i) : cy.bp;
         const float c2 = zs ? kdiv(cy.bm, by, B.h[2][1], p.kmz, k) : cy.bm;
         ly = adj_comp(ly, cy.a, c1, c2, t1, t2, g2, g3);
     }
     if (hz_m) {  // Hz: c1 on dEx_j (y CPML), c2 on dEy_i (x CPML)
-        PsiTerm t1{nullptr, 0, 0, 0}, t2{nullptr, 0, 0, 0};
-        if (ys) { const int q = psi_off_y(g, i, j, k, side); t1 = PsiTerm{psa.f[2 + side].h[1] + q, p.bmy[j], p.amy[j], __fmul_rn(cz.bp, g.dy)}; }
-        if (xs) { const int q = psi_off_x(g, i, j, k, side); t2 = PsiTerm{psa.f[side].h[1] + q, p.bmx[i], p.amx[i], __fmul_rn(cz.bm, g.dx)}; }
+        PsiTerm t1{nullptr, 0, 0, 0, 0}, t2{nullptr, 0, 0, 0, 0};
+        if (ys) { const int q = psi_off_y(g, i, j, k, side); t1 = psi_term(psa.f[2 + side].h[1] + q, p.bmy[j], p.amy[j], __fmul_rn(cz.bp, g.dy)); }
+        if (xs) { const int q = psi_off_x(g, i, j, k, side); t2 = psi_term(psa.f[side].h[1] + q, p.bmx[i], p.amx[i], __fmul_rn(cz.bm, g.dx)); }
         const float c1 = ys ? kdiv(cz.bp, bz, B.h[1][1], p.kmy, j) : cz.bp;
         const float c2 = xs ? kdiv(cz.bm, bz, B.h[0][1], p.kmx, i) : cz.bm;
         lz = adj_comp(lz, cz.a, c1, c2, t1, t2, g4, g5);
@@ -207,25 +213,25 @@ __device__ __forceinline__ void adj_e_general(const StepParams& p, const AdjStat
     int side;
     float g0 = 0.f, g1 = 0.f, g2 = 0.f, g3 = 0.f, g4 = 0.f, g5 = 0.f;
     if (ex_m) {  // Ex: c1 on dHz_j (y CPML), c2 on dHy_k (z CPML)
-        PsiTerm t1{nullptr, 0, 0, 0}, t2{nullptr, 0, 0, 0};
-        if (ys) { const int q = psi_off_y(g, i, j, k, side); t1 = PsiTerm{psa.f[2 + side].e[0] + q, p.bey[j], p.aey[j], __fmul_rn(cx.bp, g.dy)}; }
-        if (zs) { const int q = psi_off_z(g, i, j, k, side); t2 = PsiTerm{psa.f[4 + side].e[0] + q, p.bez[k], p.aez[k], __fmul_rn(cx.bm, g.dz)}; }
+        PsiTerm t1{nullptr, 0, 0, 0, 0}, t2{nullptr, 0, 0, 0, 0};
+        if (ys) { const int q = psi_off_y(g, i, j, k, side); t1 = psi_term(psa.f[2 + side].e[0] + q, p.bey[j], p.aey[j], __fmul_rn(cx.bp, g.dy)); }
+        if (zs) { const int q = psi_off_z(g, i, j, k, side); t2 = psi_term(psa.f[4 + side].e[0] + q, p.bez[k], p.aez[k], __fmul_rn(cx.bm, g.dz)); }
         const float c1 = ys ? kdiv(cx.bp, ux && on_bg, B.e[1][0], p.key, j) : cx.bp;
         const float c2 = zs ? kdiv(cx.bm, ux && on_bg, B.e[2][0], p.kez, k) : cx.bm;
         lx = adj_comp(lx, cx.a, c1, c2, t1, t2, g0, g1);
     }
     if (ey_m) {  // Ey: c1 on dHx_k (z CPML), c2 on dHz_i (x CPML)
-        PsiTerm t1{nullptr, 0, 0, 0}, t2{nullptr, 0, 0, 0};
-        if (zs) { const int q = psi_off_z(g, i, j, k, side); t1 = PsiTerm{psa.f[4 + side].e[1] + q, p.bez[k], p.aez[k], __fmul_rn(cy.bp, g.dz)}; }
-        if (xs) { const int q = psi_off_x(g, i, j, k, side); t2 = PsiTerm{psa.f[side].e[0] + q, p.bex[i], p.aex[i], __fmul_rn(cy.bm, g.dx)}; }
+        PsiTerm t1{nullptr, 0, 0, 0, 0}, t2{nullptr, 0, 0, 0, 0};
+        if (zs) { const int q = psi_off_z(g, i, j, k, side); t1 = psi_term(psa.f[4 + side].e[1] + q, p.bez[k], p.aez[k], __fmul_rn(cy.bp, g.dz)); }
+        if (xs) { const int q = psi_off_x(g, i, j, k, side); t2 = psi_term(psa.f[side].e[0] + q, p.bex[i], p.aex[i], __fmul_rn(cy.bm, g.dx)); }
         const float c1 = zs ? kdiv(cy.bp, uy && on_bg, B.e[2][1], p.kez, k) : cy.bp;
         const float c2 = xs ? kdiv(cy.bm, uy && on_bg, B.e[0][0], p.kex, i) : cy.bm;
         ly = adj_comp(ly, cy.a, c1, c2, t1, t2, g2, g3);
     }
     if (ez_m) {  // Ez: c1 on dHy_i (x CPML), c2 on dHx_j (y CPML); lumped edges override a, c1, c2
-        PsiTerm t1{nullptr, 0, 0, 0}, t2{nullptr, 0, 0, 0};
-        if (xs) { const int q = psi_off_x(g, i, j, k, side); t1 = PsiTerm{psa.f[side].e[1] + q, p.bex[i], p.aex[i], __fmul_rn(cz.bp, g.dx)}; }
-        if (ys) { const int q = psi_off_y(g, i, j, k, side); t2 = PsiTerm{psa.f[2 + side].e[1] + q, p.bey[j], p.aey[j], __fmul_rn(cz.bm, g.dy)}; }
+        PsiTerm t1{nullptr, 0, 0, 0, 0}, t2{nullptr, 0, 0, 0, 0};
+        if (xs) { const int q = psi_off_x(g, i, j, k, side); t1 = psi_term(psa.f[side].e[1] + q, p.bex[i], p.aex[i], __fmul_rn(cz.bp, g.dx)); }
+        if (ys) { const int q = psi_off_y(g, i, j, k, side); t2 = psi_term(psa.f[2 + side].e[1] + q, p.bey[j], p.aey[j], __fmul_rn(cz.bm, g.dy)); }
         const bool plane_lumped = !kBg && p.lumped_k[k] < p.lumped_k[k + 1];  // background nodes carry none
         const LumpedEdge* L = plane_lumped ? find_lumped(p, i, j, k, 2) : nullptr;  // design handles have no Ex edges
         float aa, c1, c2;
