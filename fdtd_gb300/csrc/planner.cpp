@@ -101,14 +101,16 @@ void plan_fused(const PlanGrid& g, int kc, const int* design_box, FusedPlan& out
     }
     const int* d = design_box;
     std::vector<PlanItem> left_out;  // tiles inside the swept rectangle that reach the design edge box
+    std::vector<PlanItem> swept_tiles;
     for (int y0 : ys)
         for (int x0 : xs) {
-            if (d && x0 <= d[3] && d[0] <= x0 + kTileX && y0 <= d[4] && d[1] <= y0 + kTileY) {
-                left_out.push_back(PlanItem{x0, y0, 0, 0});
-                continue;
-            }
-            for (int k = zlo; k < zhi; k += kc) out.interior.push_back(PlanItem{x0, y0, k, std::min(k + kc, zhi)});
+            if (d && x0 <= d[3] && d[0] <= x0 + kTileX && y0 <= d[4] && d[1] <= y0 + kTileY) left_out.push_back(PlanItem{x0, y0, 0, 0});
+            else swept_tiles.push_back(PlanItem{x0, y0, 0, 0});
         }
+    // plane-major order (see the end): chunks outer, tiles in row order inner
+    out.interior.reserve(swept_tiles.size() * (size_t)std::max(1, (zhi - zlo + kc - 1) / kc));
+    for (int k = zlo; k < zhi; k += kc)
+        for (const PlanItem& t : swept_tiles) out.interior.push_back(PlanItem{t.x, t.y, k, std::min(k + kc, zhi)});
     const bool swept = !xs.empty() && !ys.empty();
     const int X0 = swept ? xs.front() : 0, X1 = swept ? xs.back() + kTileX : 0;
     const int Y0 = swept ? ys.front() : 0, Y1 = swept ? ys.back() + kTileY : 0;
@@ -163,10 +165,15 @@ void plan_fused(const PlanGrid& g, int kc, const int* design_box, FusedPlan& out
     // plane-major order: CTAs run in item order, so the CTAs in flight then work on neighbouring
     // planes of many tiles instead of many planes of a few tiles, which keeps the pages they touch
     // few on large grids
+    // (the interior and shell lists are generated in that order; a stable sort by plane, done only
+    // where a list is out of order, keeps the order of items of one plane)
     auto by_plane = [](const PlanItem& a, const PlanItem& b) { return a.z < b.z; };
-    std::stable_sort(out.interior.begin(), out.interior.end(), by_plane);
-    std::stable_sort(out.cpml.begin(), out.cpml.end(), by_plane);
-    for (auto& s : out.shell) std::stable_sort(s.begin(), s.end(), by_plane);
+    auto order = [&](std::vector<PlanItem>& v) {
+        if (!std::is_sorted(v.begin(), v.end(), by_plane)) std::stable_sort(v.begin(), v.end(), by_plane);
+    };
+    order(out.interior);
+    order(out.cpml);
+    for (auto& s : out.shell) order(s);
 }
 
 }  // namespace fdtd
