@@ -144,6 +144,8 @@ struct fdtd_handle {
     // prepared device tables
     bool prepared = false;
     bool dirty_lumped = true, dirty_probes = true, dirty_materials = true;
+    bool dirty_cpml = false;  // the CPML grading changed after the profiles were built
+    float cpml_r0 = 0.f;      // 0: the reference's sigma_opt grading; else the reflection coefficient
     LumpedEdge* d_lumped = nullptr;
     int* d_lumped_k = nullptr;
     std::vector<PlateDef> plates;
@@ -1155,6 +1157,16 @@ int fdtd_tune_schedule(fdtd_handle* h) {
     return FDTD_OK;
 }
 
+int fdtd_set_cpml_grading(fdtd_handle* h, float r0) {
+    if (!h) return fail(FDTD_ERR_INVALID, "handle is NULL");
+    if (!(r0 == 0.f || (r0 > 0.f && r0 < 1.f))) return fail(FDTD_ERR_INVALID, "r0 must be 0 (reference grading) or in (0, 1)");
+    if (r0 != h->cpml_r0) {
+        h->cpml_r0 = r0;
+        h->dirty_cpml = true;
+    }
+    return FDTD_OK;
+}
+
 int fdtd_get_cpml_profile(fdtd_handle* h, int32_t axis, int32_t kind, float* out) {
     if (!h || !out) return fail(FDTD_ERR_INVALID, "NULL argument");
     if (axis < 0 || axis > 2 || kind < 0 || kind > 5) return fail(FDTD_ERR_INVALID, "axis 0..2, kind 0..5");
@@ -1401,8 +1413,8 @@ int build_probes(fdtd_handle* h) {
 }
 
 int ensure_prepared(fdtd_handle* h) {
-    if (!h->dirty_materials && !h->dirty_lumped && !h->dirty_probes && h->prepared) return FDTD_OK;
-    if (h->dirty_materials || !h->prepared) {
+    if (!h->dirty_materials && !h->dirty_lumped && !h->dirty_probes && !h->dirty_cpml && h->prepared) return FDTD_OK;
+    if (h->dirty_materials || h->dirty_cpml || !h->prepared) {
         std::vector<MatProps> props(kMaxMaterials);
         for (int q = 0; q < kMaxMaterials; ++q) {
             fdtd_material_axes m =
@@ -1413,7 +1425,8 @@ int ensure_prepared(fdtd_handle* h) {
         CUDA_TRY(cudaMemcpy(h->props, props.data(), sizeof(MatProps) * kMaxMaterials, cudaMemcpyHostToDevice));
         const int n_tab = h->has_design ? kMaxMaterials : (int)h->materials.size();
         CUDA_TRY(launch_material_tables(h->g, h->props, n_tab, h->coef, h->stream));
-        if (!h->prepared) CUDA_TRY(launch_cpml_profiles(h->g, h->grid.pi, h->prof, h->stream));
+        if (!h->prepared || h->dirty_cpml) CUDA_TRY(launch_cpml_profiles(h->g, h->grid.pi, h->cpml_r0, h->prof, h->stream));
+        h->dirty_cpml = false;
         CUDA_TRY(launch_bg_curl(h->g, h->coef, 0, h->d_kappa_ptrs, h->d_bg_ptrs, h->stream));
         h->dirty_materials = false;
         h->dirty_lumped = true;

@@ -15,8 +15,11 @@ constexpr int kSetupPlanes = 8;
 // One axis of setABCPML (fdtdrav.h:1774-1891 for x_n, 1912-1941 for x_p, and the y / z mirrors).
 // prof = {b_e, a_e, b_m, a_m, kappa_e, kappa_m}, each n entries. Nodes outside both slabs keep
 // b = a = 1.2e-38 (setZero) and kappa = 1.
+// r0 > 0 (not the reference's): sigma_max from the reflection coefficient r0 of a slab of P cells
+// with grading order m, sigma_max = -(m + 1) ln(r0) / (2 eta0 P delta), eta0 = sqrt(mu0 / eps0)
+// (Gedney's polynomial grading); kappa, alpha and the recurrences as the reference's.
 __global__ void k_cpml_axis(float* be, float* ae, float* bm, float* am, float* ke, float* km, int n,
-                            int pn_i, int pp_i, float delta, float dt, float eps_0, float mu_0, float pi) {
+                            int pn_i, int pp_i, float delta, float dt, float eps_0, float mu_0, float pi, float r0) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
     // parameters of fdtdrav.h:1774-1812, as float locals
@@ -34,10 +37,12 @@ __global__ void k_cpml_axis(float* be, float* ae, float* bm, float* am, float* k
         roe = (pn - q - 0.75) / pn;
         rom = (pn - q - 0.25) / pn;
         in = true;
+        if (r0 > 0.f) sigma_max = -(npml + 1) * logf(r0) / (2.0f * sqrtf(mu_0 / eps_0) * pn * delta);
     } else if (q >= n - pp_i) {
         roe = (q - (n - pp - 1) - 0.75) / pp;
         rom = (q - (n - pp - 1) - 0.25) / pp;
         in = true;
+        if (r0 > 0.f) sigma_max = -(npml + 1) * logf(r0) / (2.0f * sqrtf(mu_0 / eps_0) * pp * delta);
     }
     if (!in) {
         be[q] = kTiny; ae[q] = kTiny; bm[q] = kTiny; am[q] = kTiny; ke[q] = 1.0f; km[q] = 1.0f;
@@ -58,7 +63,7 @@ __global__ void k_cpml_axis(float* be, float* ae, float* bm, float* am, float* k
     be[q] = b_e; ae[q] = a_e; bm[q] = b_m; am[q] = a_m; ke[q] = kappa_e; km[q] = kappa_m;
 }
 
-cudaError_t launch_cpml_profiles(const DeviceGrid& g, float pi, float* const prof[18], cudaStream_t st) {
+cudaError_t launch_cpml_profiles(const DeviceGrid& g, float pi, float r0, float* const prof[18], cudaStream_t st) {
     const int ns[3] = {g.nx, g.ny, g.nz};
     const int pn[3] = {g.pxn, g.pyn, g.pzn};
     const int pp[3] = {g.pxp, g.pyp, g.pzp};
@@ -66,7 +71,7 @@ cudaError_t launch_cpml_profiles(const DeviceGrid& g, float pi, float* const pro
     for (int a = 0; a < 3; ++a) {
         float* const* P = prof + 6 * a;
         k_cpml_axis<<<(ns[a] + 127) / 128, 128, 0, st>>>(P[0], P[1], P[2], P[3], P[4], P[5], ns[a], pn[a], pp[a],
-                                                         d[a], g.dt, g.eps0, g.mu0, pi);
+                                                         d[a], g.dt, g.eps0, g.mu0, pi, r0);
     }
     return cudaGetLastError();
 }

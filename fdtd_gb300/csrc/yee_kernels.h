@@ -112,7 +112,8 @@ int encode_cpml_maps(CpmlMaps* out, const DeviceGrid& g, float* const h[3], floa
                      const PsiSet& psi, void* encode_fn);
 
 // Setup kernels (setup_kernels.cu).
-cudaError_t launch_cpml_profiles(const DeviceGrid& g, float pi, float* const prof[18], cudaStream_t st);
+// r0 = 0: the reference's grading (sigma_opt); r0 > 0: sigma_max from that reflection coefficient.
+cudaError_t launch_cpml_profiles(const DeviceGrid& g, float pi, float r0, float* const prof[18], cudaStream_t st);
 cudaError_t launch_material_tables(const DeviceGrid& g, const MatProps* props, int n, MatCoef* coef,
                                    cudaStream_t st);
 cudaError_t launch_lumped_coefs(const DeviceGrid& g, const uint8_t* mat, const MatProps* props,

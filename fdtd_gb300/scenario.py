@@ -207,6 +207,9 @@ class Scenario:
     mu0: float = float(REF_MU0)
     pi: float = float(REF_PI)
     seed: Optional[int] = None
+    # CPML grading: 0 = the reference's sigma_opt; 0 < r0 < 1 = sigma_max from that reflection
+    # coefficient (fdtd_set_cpml_grading)
+    cpml_r0: float = 0.0
 
     @property
     def cells(self) -> int:

@@ -82,6 +82,7 @@ SIGNATURES = {
     "fdtd_save_state": (ctypes.c_int, [_vp, _vp]),
     "fdtd_load_state": (ctypes.c_int, [_vp, _vp]),
     "fdtd_get_cpml_profile": (ctypes.c_int, [_vp, _i32, _i32, _pf]),
+    "fdtd_set_cpml_grading": (ctypes.c_int, [_vp, ctypes.c_float]),
     "fdtd_device_bytes": (_i64, [_vp]),
     "fdtd_step_static_scratch": (ctypes.c_int, [_vp, _i64]),
     "fdtd_set_design_region": (ctypes.c_int, [_vp, _pi32, ctypes.POINTER(Material), _pf]),
@@ -334,6 +335,11 @@ class Simulation:
     def load_state(self, dev_ptr: int) -> None:
         _check(_lib.fdtd_load_state(self._h, _vp(dev_ptr)))
 
+    def set_cpml_grading(self, r0: float = 0.0) -> None:
+        """0: the reference's sigma_opt grading (default); 0 < r0 < 1: sigma_max per slab from the
+        reflection coefficient r0 (fdtd_set_cpml_grading)."""
+        _check(_lib.fdtd_set_cpml_grading(self._h, float(r0)))
+
     def cpml_profile(self, axis: int, kind: int) -> np.ndarray:
         """1-D CPML profile: kind 0 b_e, 1 a_e, 2 b_m, 3 a_m, 4 kappa_e, 5 kappa_m."""
         n = (self.shape[2], self.shape[1], self.shape[0])[axis]
@@ -383,6 +389,8 @@ class Simulation:
                       probe_capacity: Optional[int] = None) -> "Simulation":
         """Build a simulation from a scenario in the reference's setup order (fdtdrav.h:4104-4310)."""
         sim = cls(sc.nx, sc.ny, sc.nz, sc.dx, sc.dy, sc.dz, sc.dt, sc.pml, sc.eps0, sc.mu0, sc.pi, schedule)
+        if getattr(sc, "cpml_r0", 0.0):
+            sim.set_cpml_grading(sc.cpml_r0)
         sim.set_materials(sc.material_table_axes() if sc.anisotropic else sc.material_table())
         if material_index is not None:
             sim.set_material_index(material_index)

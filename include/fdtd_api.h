@@ -180,6 +180,15 @@ int64_t fdtd_state_bytes(const fdtd_handle* h);
 int fdtd_save_state(fdtd_handle* h, void* dev_buf);
 int fdtd_load_state(fdtd_handle* h, const void* dev_buf);
 
+/* CPML grading (replaces setABCPML's sigma_max, fdtdrav.h:1794-1812). r0 = 0, the default: the
+ * reference's sigma_opt = (m + 1) / (150 pi delta) times 1.5, the same for every slab thickness (the
+ * reference has no reflection-coefficient parameter). 0 < r0 < 1: sigma_max of each slab from its
+ * reflection coefficient at normal incidence, -(m + 1) ln(r0) / (2 eta0 P delta) with
+ * eta0 = sqrt(mu0 / eps0), P the slab's cells and delta the axis' cell size (Gedney's polynomial
+ * grading). The grading order m = 3, kappa_max = 5 and the linear alpha profile stay the
+ * reference's. Takes effect at the next preparation or step; the CPML memory is kept. */
+int fdtd_set_cpml_grading(fdtd_handle* h, float r0);
+
 /* One 1-D CPML profile of an axis (0 = x, 1 = y, 2 = z) into host memory (n_axis floats):
  * kind 0 = b_e, 1 = a_e, 2 = b_m, 3 = a_m, 4 = kappa_e, 5 = kappa_m. These are the d_cpml_b/a
  * arrays and the kappa values that setABCPML computes (fdtdrav.h:1863-1906); nodes outside the
