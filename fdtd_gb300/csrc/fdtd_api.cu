@@ -1853,6 +1853,11 @@ int adj_forward_enqueue(fdtd_handle* h, int64_t n, int32_t checkpoint_every, int
         CUDA_TRY(launch_after_step(h->field[c][0], h->field[c][1], h->field[c][2], g, A.probe, nullptr, h->dbox, adj_slot(h, 0),
                                    h->stream));
     }
+    // one step per fdtd_step call never runs AUTO's trial: apply its direct choice (large grids
+    // with mostly interior tiles take fused) before stepping
+    if (h->schedule == FDTD_SCHEDULE_AUTO && h->auto_choice == FDTD_SCHEDULE_AUTO &&
+        (long long)g.nx * g.ny * g.nz >= kAutoTrialCells)
+        auto_direct(h);
     // two-pass steps take their records in k_design_e (no launch of their own): the E of the
     // design edge box is final there, and so is every other E
     const bool two_pass = !use_fused(h);

@@ -309,3 +309,27 @@ def test_fom_records_same_in_both_schedules(gpu_lib, probe):
         assert J == out[0][0] and np.array_equal(g, out[0][1])
     J64 = oracle.fom_grad(sc, probe, box, eps.astype(np.float64), precision="f64", grad=False)
     assert abs(out[0][0] - J64) <= 1e-4 * abs(J64)
+
+
+def test_auto_adjoint_on_a_large_grid_takes_fused(gpu_lib):
+    """On a grid where AUTO's direct rule chooses the fused schedule (64 Mi cells, mostly interior
+    tiles), the adjoint forward applies that choice; J and the gradient equal the two-pass
+    schedule's bit for bit."""
+    from fdtd_gb300 import solver
+    steps = 24
+    sc = S.vacuum_cube(64, steps, pml=10, name="adjoint_large")
+    sc.nx, sc.ny, sc.nz = 512, 512, 256
+    sc.sources = [S.LumpedSource((246, 256, 128, 246, 256, 129), 50.0, S.gaussian_derivative(steps, sc.dt, 30e9, 1e-3))]
+    sc.probes = []
+    box, probe = (250, 248, 124, 266, 264, 132), (268, 256, 128)
+    eps = np.random.default_rng(2).uniform(1, 12, size=(8, 16, 16)).astype(np.float32)
+    out = []
+    for schedule in (0, 1):
+        with solver.Simulation.from_scenario(sc, schedule, probe_capacity=steps) as sim:
+            sim.set_design_region(box, eps)
+            J = sim.adjoint_forward(steps, probe, 4)
+            g = sim.adjoint_backward()
+            out.append((J, g, sim.active_schedule))
+    assert out[0][2] == 2 and out[1][2] == 1
+    assert out[0][0] == out[1][0] and np.array_equal(out[0][1], out[1][1])
+    assert np.abs(out[0][1]).max() > 0
