@@ -393,11 +393,23 @@ FusedWork work_of(const int4* d, const int counts[kWorkLists]) {
     return w;
 }
 
-// Work items of the fused schedule (planner.cpp), with CPML items under FDTD_SCHEDULE_FUSED_CPML.
-// The design region, if any, stays with the shell; planned again when it or the schedule changes.
+// The AUTO trial: on grids of at least kAutoTrialCells cells, the first fdtd_step call of at least
+// 2 * kAutoTrialSteps steps times kAutoTrialSteps fused steps and then as many two-pass steps (real
+// steps: both schedules give the same bits) and keeps the faster schedule for the handle. Which one
+// wins depends on the grid: on GB300 random-box cubes with 10-cell CPML, two-pass below about
+// 224^3 and fused above. Smaller grids take two-pass without a trial. Grids of at least
+// kAutoDirectCells cells whose interior tiles hold at least kAutoDirectInterior of the nodes
+// (512^3 with 10-cell CPML: 0.86) take fused without a trial: there fused won by 16-30 % on every
+// grid measured, and the trial's two-pass steps and synchronisation cost more than a step. The
+// fused buffers are freed when two-pass wins or cannot be allocated.
+constexpr int64_t kAutoTrialSteps = 4;
+constexpr long long kAutoTrialCells = 8LL << 20;
+constexpr long long kAutoDirectCells = 64LL << 20;
+constexpr double kAutoDirectInterior = 0.8;
+
 // The fused plan for the handle's current design box and schedule, from the cache when it holds
-// that plan (planning a 512^3 grid takes most of a millisecond on the host).
-void plan_current(fdtd_handle* h, FusedPlan& plan) {
+// that plan (planning a 512^3 grid takes a few hundred microseconds on the host).
+const FusedPlan& plan_current(fdtd_handle* h) {
     const PlanGrid pg = plan_grid(h->g);
     const int kc = h->kc > 0 ? h->kc : plan_chunk(pg);
     const bool cpml = h->schedule == FDTD_SCHEDULE_FUSED_CPML;
@@ -410,12 +422,13 @@ void plan_current(fdtd_handle* h, FusedPlan& plan) {
         std::copy(key, key + 9, C.key);
         C.valid = true;
     }
-    plan = C.plan;
+    return C.plan;
 }
 
+// Work items of the fused schedule (planner.cpp), with CPML items under FDTD_SCHEDULE_FUSED_CPML.
+// The design region, if any, stays with the shell; planned again when it or the schedule changes.
 int plan_work(fdtd_handle* h) {
-    FusedPlan plan;
-    plan_current(h, plan);
+    const FusedPlan& plan = plan_current(h);
     int counts[kWorkLists];
     const std::vector<PlanItem> all = flatten(plan, counts);
     h->release((void*)h->work.interior);
@@ -562,6 +575,9 @@ int fdtd_create(const fdtd_grid* grid, fdtd_handle** out) {
     if (cudaMemset(h->mat, 0, (size_t)V) != cudaSuccess || cudaMemset(h->status, 0, sizeof(int)) != cudaSuccess)
         return cleanup(fail(FDTD_ERR_CUDA, "memset failed"));
     h->materials.push_back(axes_of(fdtd_material{1.0f, kTiny, 1.0f, kTiny}));
+    // grids large enough for AUTO to weigh the fused schedule: plan its work on the host while the
+    // fills run (the plan is cached for the first step)
+    if ((long long)g.nx * g.ny * g.nz >= kAutoTrialCells) plan_current(h);
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return cleanup(fail(FDTD_ERR_CUDA, std::string("init: ") + cudaGetErrorString(e)));
     *out = h;
@@ -879,25 +895,10 @@ int steps_two_pass(fdtd_handle* h, const StepParams& p, int64_t n) {
     return FDTD_OK;
 }
 
-// The AUTO trial: on grids of at least kAutoTrialCells cells, the first fdtd_step call of at least
-// 2 * kAutoTrialSteps steps times kAutoTrialSteps fused steps and then as many two-pass steps (real
-// steps: both schedules give the same bits) and keeps the faster schedule for the handle. Which one
-// wins depends on the grid: on GB300 random-box cubes with 10-cell CPML, two-pass below about
-// 224^3 and fused above. Smaller grids take two-pass without a trial. Grids of at least
-// kAutoDirectCells cells whose interior tiles hold at least kAutoDirectInterior of the nodes
-// (512^3 with 10-cell CPML: 0.86) take fused without a trial: there fused won by 16-30 % on every
-// grid measured, and the trial's two-pass steps and synchronisation cost more than a step. The
-// fused buffers are freed when two-pass wins or cannot be allocated.
-constexpr int64_t kAutoTrialSteps = 4;
-constexpr long long kAutoTrialCells = 8LL << 20;
-constexpr long long kAutoDirectCells = 64LL << 20;
-constexpr double kAutoDirectInterior = 0.8;
-
 // Share of the grid's nodes that the interior sweep's tiles hold (overlapping tiles counted once
 // per tile, a slight overestimate).
 double interior_share(fdtd_handle* h) {
-    FusedPlan plan;
-    plan_current(h, plan);
+    const FusedPlan& plan = plan_current(h);
     long long n = 0;
     for (const PlanItem& it : plan.interior) n += (long long)(it.w - it.z) * kTileX * kTileY;
     return (double)n / ((double)h->g.nx * h->g.ny * h->g.nz);
