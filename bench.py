@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-steps", type=int, default=4000,
+                    help="steps of the adjoint workload (4000 is the workload; fewer for profiling)")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-hbm", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 error record (profiling runs)")
@@ -445,14 +447,14 @@ def bench_hbm(warmup=3, steps=20):
             "clocks": clk}
 
 
-def bench_adjoint():
+def bench_adjoint(steps=4000):
     """Adjoint cost on the 128^3 design problem (32x32x16 centred design region, eps_r ~ U[1,12],
     10-cell CPML, one source, one Ez probe, 4000 steps): plain forward, forward with checkpoints
     every 64 steps + backward with segment recompute, and the resident-history variant (K = 0).
     Wall-clock around the synchronous C calls; every run starts from a fresh handle."""
     import torch
     from fdtd_gb300 import scenario as S, solver
-    d = S.design_problem()
+    d = S.design_problem(steps=steps)
     sc = d.scenario
 
     def fresh():
@@ -626,7 +628,7 @@ def main():
         if world == 1 and not args.no_fp64:
             out["fp64_error"] = fp64_error()
         if not args.no_adjoint and world == 1:
-            out["adjoint"] = bench_adjoint()
+            out["adjoint"] = bench_adjoint(args.adjoint_steps)
         if not args.no_batched and world == 1:
             out["batched"] = bench_batched()
             out["batched_adjoint"] = bench_batched_adjoint()
