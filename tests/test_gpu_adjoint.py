@@ -333,3 +333,15 @@ def test_auto_adjoint_on_a_large_grid_takes_fused(gpu_lib):
     assert out[0][2] == 2 and out[1][2] == 1
     assert out[0][0] == out[1][0] and np.array_equal(out[0][1], out[1][1])
     assert np.abs(out[0][1]).max() > 0
+
+
+@pytest.mark.parametrize("K", [1, 2, 3, 64, 200])
+def test_checkpoint_interval_edge_cases(gpu_lib, K):
+    """Checkpoint intervals of one step (segments of one step: the recompute updates only the
+    design edge box), two and three steps (at or below the box-checkpoint interval), and longer
+    than the run (a single partial segment with box checkpoints): the gradient equals the resident
+    history's bit for bit."""
+    sc, box, eps, probe = design_case(9, steps=50)
+    J0, g0 = gpu_grad(sc, box, eps, probe, 0)
+    J1, g1 = gpu_grad(sc, box, eps, probe, K)
+    assert J0 == J1 and np.array_equal(g0, g1)
