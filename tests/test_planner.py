@@ -129,6 +129,25 @@ def test_bench_grid_lists(lib):
     assert len(L["interior"]) > 0 and all(len(L[n]) > 0 for n, _ in SHELL_LISTS)
 
 
+@pytest.mark.parametrize("dims,kc_want", [((512, 512, 512), 32), ((1024, 1024, 896), 32), ((256, 256, 256), 16),
+                                          ((1024, 1024, 128), 32)])
+def test_interior_chunks_capped_and_plane_major(lib, dims, kc_want):
+    """Interior items are at most 32 planes long (the cap that keeps the CTAs in flight on
+    neighbouring planes; the 1024 x 1024 x 896 grid alone would give 224-plane chunks) and every
+    list runs in plane-major order, tiles in row order within a plane."""
+    kc, L = plan(lib, dims, (10,) * 6)
+    assert kc == kc_want
+    it = L["interior"]
+    assert (it[:, 3] - it[:, 2] <= kc).all() and (it[:, 3] > it[:, 2]).all()
+    for name in LISTS:
+        z = L[name][:, 2]
+        assert (np.diff(z) >= 0).all(), name
+    # within one plane of the interior list: y outer, x inner
+    first = it[it[:, 2] == it[0, 2]]
+    order = np.lexsort((first[:, 0], first[:, 1]))
+    assert (order == np.arange(len(first))).all()
+
+
 @pytest.mark.parametrize("dims,pml,design", [
     ((128, 128, 128), (10,) * 6, (48, 48, 56, 80, 80, 72)),
     ((40, 40, 40), (6,) * 6, (16, 16, 17, 24, 24, 23)),
