@@ -530,9 +530,12 @@ int fdtd_create(const fdtd_grid* grid, fdtd_handle** out) {
     g.dx = grid->dx; g.dy = grid->dy; g.dz = grid->dz; g.dt = grid->dt; g.eps0 = grid->eps0; g.mu0 = grid->mu0;
     auto cleanup = [&](int code) { fdtd_destroy(h); return code; };
     const long long V = vol(h);
+    // each field's fill (setZero's 1.2e-38) is launched as soon as it is allocated, so the device
+    // fills while the host makes the remaining allocations
     for (int c = 0; c < 6; ++c) {
         cudaError_t e = h->alloc((void**)&h->field[0][c], (size_t)V * sizeof(float));
         if (e != cudaSuccess) return cleanup(fail(FDTD_ERR_OOM, "field allocation failed: " + std::string(cudaGetErrorString(e))));
+        if (launch_fill(h->field[0][c], V, kTiny, nullptr) != cudaSuccess) return cleanup(fail(FDTD_ERR_CUDA, "fill failed"));
     }
     if (h->alloc((void**)&h->mat, (size_t)V) != cudaSuccess) return cleanup(fail(FDTD_ERR_OOM, "material index allocation failed"));
     if (h->alloc((void**)&h->props, sizeof(MatProps) * kMaxMaterials) != cudaSuccess ||
@@ -569,9 +572,7 @@ int fdtd_create(const fdtd_grid* grid, fdtd_handle** out) {
     }
     rc = alloc_psi_set(h, 0);
     if (rc) return cleanup(rc);
-    // initial state of setZero: fields and psi 1.2e-38, material 0 everywhere
-    for (int c = 0; c < 6; ++c)
-        if (launch_fill(h->field[0][c], V, kTiny, nullptr) != cudaSuccess) return cleanup(fail(FDTD_ERR_CUDA, "fill failed"));
+    // initial state of setZero: fields (filled above) and psi 1.2e-38, material 0 everywhere
     if (cudaMemset(h->mat, 0, (size_t)V) != cudaSuccess || cudaMemset(h->status, 0, sizeof(int)) != cudaSuccess)
         return cleanup(fail(FDTD_ERR_CUDA, "memset failed"));
     h->materials.push_back(axes_of(fdtd_material{1.0f, kTiny, 1.0f, kTiny}));
