@@ -572,6 +572,17 @@ int fdtd_create(const fdtd_grid* grid, fdtd_handle** out) {
     }
     rc = alloc_psi_set(h, 0);
     if (rc) return cleanup(rc);
+    // node classes, coefficient rows and the interface-key set, which every preparation builds:
+    // allocated here, while the fills run
+    if (h->alloc((void**)&h->cls, (size_t)V) != cudaSuccess ||
+        h->alloc((void**)&h->rec, (size_t)V * sizeof(uint16_t)) != cudaSuccess ||
+        h->alloc((void**)&h->iface_table, sizeof(unsigned long long) * kIfaceTableSize) != cudaSuccess ||
+        h->alloc((void**)&h->iface_keys, sizeof(unsigned long long) * kIfaceTableSize) != cudaSuccess ||
+        h->alloc((void**)&h->iface_slot_row, sizeof(int) * kIfaceTableSize) != cudaSuccess ||
+        h->alloc((void**)&h->iface_counters, sizeof(int) * 2) != cudaSuccess)
+        return cleanup(fail(FDTD_ERR_OOM, "node class allocation failed"));
+    if (cudaMemsetAsync(h->cls, kGeneral, (size_t)V, nullptr) != cudaSuccess)
+        return cleanup(fail(FDTD_ERR_CUDA, "memset failed"));
     // initial state of setZero: fields (filled above) and psi 1.2e-38, material 0 everywhere
     if (cudaMemset(h->mat, 0, (size_t)V) != cudaSuccess || cudaMemset(h->status, 0, sizeof(int)) != cudaSuccess)
         return cleanup(fail(FDTD_ERR_CUDA, "memset failed"));
