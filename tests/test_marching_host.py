@@ -65,3 +65,23 @@ def test_sector_plates_cover_the_sector_edges():
     assert np.array_equal(cx, ex.astype(cx.dtype)) and np.array_equal(cy, ey.astype(cy.dtype))
     # the apex lies in the sector, a point beyond the radius does not
     assert ex[12, 18] and not ex[12, 33]
+
+
+def test_material_tables_for_isotropic_and_per_axis_materials():
+    """The scenario's material tables (the isotropic shortcut and the per-axis path) equal the
+    values written out per axis in float32, for scalars, numpy scalars and per-axis sequences."""
+    mats = [S.Material(), S.Material(eps_r=2.5, sigma_e=0.01), S.Material(eps_r=np.float64(3.3), mu_r=np.float32(1.7)),
+            S.Material(eps_r=(2.0, 3.0, 4.0), sigma_e=0.02), S.Material(eps_r=[5.0, 5.0, 5.0], sigma_m=(1e3, 2e3, 3e3))]
+    sc = S.Scenario("m", 8, 8, 8, 1e-3, 1e-3, 1e-3, 1e-12, (2,) * 6, 1, mats)
+
+    def axes(m):
+        out = np.zeros((3, 4), dtype=np.float32)
+        for q, v in enumerate((m.eps_r, m.sigma_e, m.mu_r, m.sigma_m)):
+            out[:, q] = np.broadcast_to(np.asarray(v, dtype=np.float32), (3,))
+        return out
+
+    want = np.stack([axes(m) for m in mats])
+    assert np.array_equal(sc.material_table_axes().view(np.uint32), want.view(np.uint32))
+    assert np.array_equal(sc.material_table().view(np.uint32), want[:, 0, :].view(np.uint32))
+    assert [m.anisotropic for m in mats] == [False, False, False, True, True]
+    assert sc.anisotropic
